@@ -1,0 +1,378 @@
+#!/usr/bin/env python3
+"""Benchmark of the batched HEALPix spherical-harmonic transform on GB300.
+
+Workload (one GPU): map2alm (t2alm) of a batch of 500 temperature maps at
+nside 1024 / lmax 2047, maps resident in HBM (50 GB, far above the 129 MB L2, so
+no flush is needed between steps).  One step = one t2alm of the whole batch =
+500 map.SHT.  Inputs: Gaussian alm with C_l ~ l^-2 (seed 2, a00 = 0) synthesised
+to maps on the device by alm2t.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+--impl reference times the reference algorithm's CPU restatement (the oracle:
+NumPy/OpenBLAS DGEMMs, scipy.fft, the C recursion) on this host's cores on a
+sample of the batch, scaled to the batch the way the reference computes it
+(recursion once per m for the batch, FFT and DGEMM per map).  The reference's own
+Fortran/MKL build cannot be compiled here (no Fortran compiler, no MKL).
+
+Under torchrun (N > 1) every rank runs its own 500-map batch on its own GPU
+(replicas; no collective on the data path), value = all maps / max time.
+"""
+from __future__ import annotations
+
+import os
+
+os.environ.setdefault("OMP_WAIT_POLICY", "PASSIVE")
+
+import argparse
+import json
+import math
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+if str(ROOT) not in sys.path:
+    sys.path.insert(0, str(ROOT))
+
+import numpy as np
+
+METRIC = "maps·SHT/s at nside 1024 (FP64 vs split-prec @ stated error); p50/p99 latency"
+UNIT = "maps·SHT/s"
+
+
+def flop_per_map(nside, lmax):
+    """Algorithmic FLOP of one spin-0 transform direction: one real x complex
+    FMA (4 flop) per (north ring, l, m) after north/south folding."""
+    return 4.0 * nside * (lmax + 1) * (lmax + 2)
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--nside", type=int, default=1024)
+    ap.add_argument("--lmax", type=int, default=None)
+    ap.add_argument("--nmaps", type=int, default=500)
+    ap.add_argument("--cpu-maps", type=int, default=32,
+                    help="maps in the CPU baseline sample")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--e2e-maps", type=int, default=None)
+    a = ap.parse_args()
+    if a.lmax is None:
+        a.lmax = 2 * a.nside - 1
+    if a.warmup < 3 and a.impl == "ours":
+        print("warning: fewer than 3 warm-up steps", file=sys.stderr)
+    return a
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+# ---------------------------------------------------------------- clocks
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        fd, self.path = tempfile.mkstemp(prefix="clocks_", suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, power = [], [], []
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        with open(self.path) as f:
+            for line in f:
+                parts = [p.strip() for p in line.split(",")]
+                if len(parts) < 9:
+                    continue
+                try:
+                    sm.append(float(parts[1]))
+                    smax.append(float(parts[2]))
+                    power.append(float(parts[3]))
+                except ValueError:
+                    continue
+                for nm, v in zip(names, parts[5:9]):
+                    if v.lower().startswith("active"):
+                        reasons.add(nm)
+        os.unlink(self.path)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax),
+                "power_w_max": max(power), "samples": len(sm), "reasons": sorted(reasons)}
+
+
+# ---------------------------------------------------------------- inputs
+def device_alm(nside, lmax, nmaps, seed, device):
+    """Gaussian square-real alm (L, L, nmaps) on the device, C_l = l^-2 (l >= 1),
+    a00 = 0: N(0, C_l) at m = 0 and N(0, C_l/2) per component at m > 0."""
+    import torch
+    L = lmax + 1
+    l = torch.arange(L, dtype=torch.float64, device=device)
+    cl = torch.where(l > 0, 1.0 / torch.clamp(l, min=1.0) ** 2, torch.zeros_like(l))
+    c = torch.arange(L, device=device).view(L, 1)          # column
+    r = torch.arange(L, device=device).view(1, L)          # row
+    # Re of m = c at row l = r (r >= c); Im of m = L - c at l = r + m (r < c)
+    m_im = L - c
+    l_of = torch.where(r >= c, r, r + m_im)
+    half = torch.where((r >= c) & (c == 0), torch.ones_like(r, dtype=torch.float64),
+                       torch.full_like(r, 0.5, dtype=torch.float64))
+    sd = torch.sqrt(cl[l_of.clamp(max=lmax)] * half)
+    g = torch.Generator(device=device)
+    g.manual_seed(seed)
+    alm = torch.randn((L, L, nmaps), dtype=torch.float64, device=device, generator=g)
+    alm *= sd.unsqueeze(-1)
+    return alm
+
+
+# ---------------------------------------------------------------- CPU baseline
+def cpu_baseline(nside, lmax, nmaps, sample_maps, maps_np, ring_tab, want_alm=False):
+    """Times the oracle (reference algorithm restated on the CPU) on `sample_maps`
+    maps; returns maps.SHT/s scaled to an `nmaps` batch plus the phase times."""
+    from oracle import OracleSHT
+    threads = os.cpu_count() or 1
+    o = OracleSHT(nside, lmax, ring_tab=ring_tab, fft_workers=threads)
+    alm, tm = o.t2alm_timed(maps_np)
+    k = maps_np.shape[1]
+    t_batch = tm["plm"] + (nmaps / k) * (tm["fft"] + tm["gemm"])
+    out = {"value": nmaps / t_batch, "unit": UNIT, "cores": threads, "kind": "port",
+           "sample": (f"{k} of {nmaps} maps, all m; recursion timed once per batch (the "
+                      f"reference computes it once per m for the whole batch), FFT + "
+                      f"gather + DGEMM scaled by {nmaps}/{k}"),
+           "phase_s": {kk: round(v, 3) for kk, v in tm.items()}}
+    return (out, alm) if want_alm else out
+
+
+def reference_arm(args, rank, world):
+    if rank != 0:
+        return
+    from oracle import alm_square_to_healpy  # noqa: F401  (import check)
+    golden = np.load(ROOT / "tests" / "golden" / "ring_skip.npz")
+    ring_tab = golden[f"ns_{args.nside}"][:args.lmax + 1]
+    rng = np.random.default_rng(2)
+    npix = 12 * args.nside ** 2
+    k = args.cpu_maps
+    # band-limited-ish maps are not needed for timing: N(0,1) pixels, seed 2
+    maps = np.asfortranarray(rng.standard_normal((npix, k)))
+    vals = []
+    for it in range(args.warmup + args.steps):
+        r = cpu_baseline(args.nside, args.lmax, args.nmaps, k, maps, ring_tab)
+        if it >= args.warmup:
+            vals.append(r)
+    v = statistics.median([r["value"] for r in vals])
+    last = vals[-1]
+    line = {
+        "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1000.0 * args.nmaps / v, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": workload_config(args),
+        "cpu_baseline": {"value": v, "unit": UNIT, "cores": last["cores"], "kind": "port",
+                         "sample": last["sample"]},
+        "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": ("reference CPU build (Fortran/OpenMP + MKL) cannot be compiled here; this is "
+                 "the oracle restatement of its algorithm"),
+    }
+    print(json.dumps(line), flush=True)
+
+
+def workload_config(args):
+    return {"workload": (f"t2alm (map2alm) of {args.nmaps} T maps per GPU, nside {args.nside}, "
+                         f"lmax {args.lmax}, plain FP64 method"),
+            "nside": args.nside, "lmax": args.lmax, "nmaps_per_gpu": args.nmaps,
+            "method": "fp64", "niter": 0,
+            "inputs": "Gaussian alm, C_l ~ l^-2 (seed 2), synthesised to maps on the device",
+            "l2": "inputs larger than L2 (maps resident in HBM), no flush",
+            "parallelism": f"replicas x{args.gpus}"}
+
+
+# ---------------------------------------------------------------- our arm
+def ours(args, rank, world, local):
+    import ctypes as C
+    import torch
+    import torch.distributed as dist
+    from fastsht_gb300 import SHT, _lib
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    lib = _lib.load(build_if_missing=True)
+    if world > 1:
+        dist.init_process_group("nccl", device_id=dev)
+
+    nside, lmax, nmaps = args.nside, args.lmax, args.nmaps
+    npix = 12 * nside * nside
+    peak64 = C.c_double()
+    _lib.call("fsht_measure_fp64_peak", C.byref(peak64))
+    peaks = {}
+    pk = ROOT / "MEASURED_PEAKS.json"
+    if pk.exists():
+        peaks = json.loads(pk.read_text())
+
+    sht = SHT(nside, lmax, nmaps, device=local)
+    alm_true = device_alm(nside, lmax, nmaps, 2 + rank, dev)
+    maps = sht.alm2t(alm_true.permute(2, 1, 0))        # (npix, nmaps) Fortran view
+    del alm_true
+    torch.cuda.synchronize()
+
+    def step():
+        return sht.t2alm(maps)
+
+    for _ in range(args.warmup):
+        out = step()
+    torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+    lib.fsht_profile_enable(sht._plan, 1)
+    _lib.call("fsht_profile_read", sht._plan, 0, None, None)     # clear
+    clocks = ClockSampler(local)
+    clocks.start()
+    torch.cuda.synchronize()
+    s = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(s)
+    for _ in range(args.steps):
+        out = step()
+    e1.record(s)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    ms = e0.elapsed_time(e1)
+    counts = (C.c_int * _lib.KCAT_COUNT)()
+    kms = (C.c_double * _lib.KCAT_COUNT)()
+    _lib.call("fsht_profile_read", sht._plan, _lib.KCAT_COUNT, counts, kms)
+    lib.fsht_profile_enable(sht._plan, 0)
+    if world > 1:
+        t = torch.tensor([ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+        dist.barrier()
+    ms_per_step = ms / args.steps
+    value = world * nmaps * args.steps / (ms / 1000.0)
+
+    per_kernel = {}
+    for i, name in enumerate(_lib.KCAT_NAMES):
+        if counts[i]:
+            per_kernel[name] = {"launches": counts[i], "ms_total": round(kms[i], 3),
+                                "share": round(kms[i] / ms, 4) if ms else None}
+    launches = int(sum(counts[i] for i in range(_lib.KCAT_COUNT)))
+    fl = flop_per_map(nside, lmax) * nmaps * args.steps
+    ana_ms = kms[2]
+    achieved = fl / (ana_ms / 1000.0) / 1e12 if ana_ms > 0 else None
+    traffic = None
+    tf = ROOT / "profiles" / "traffic.json"
+    kchunk = sht.plan_info()["maps_per_chunk"]
+    if tf.exists():
+        tr = json.loads(tf.read_text()).get("legendre_analysis_fp64")
+        if tr and tr.get("bytes_per_map"):
+            traffic = tr["bytes_per_map"] * kchunk
+    roof = {"bound": "fp64", "kernel": "k_analysis_fp64<0> (legendre_analysis)",
+            "achieved": achieved, "peak": peak64.value, "unit": "TFLOP/s",
+            "frac": (achieved / peak64.value) if achieved else None,
+            "peak_source": ("DFMA loop measured by bench.py on this GPU (fsht_measure_fp64_peak); "
+                            "MEASURED_PEAKS.json holds HBM and BF16 figures only"),
+            "algorithmic_flop_per_launch": flop_per_map(nside, lmax) * kchunk,
+            "traffic": traffic}
+    fft_ms = kms[0]
+    fft_bytes = 16.0 * npix * nmaps * args.steps
+    roof_fft = {"bound": "hbm", "kernel": "k_ring_fft_fwd", "achieved":
+                fft_bytes / (fft_ms / 1000.0) / 1e9 if fft_ms > 0 else None,
+                "peak": peaks.get("hbm_gbs", 6800.0), "unit": "GB/s",
+                "peak_source": "MEASURED_PEAKS.json hbm_gbs" if "hbm_gbs" in peaks else "fallback"}
+    if roof_fft["achieved"]:
+        roof_fft["frac"] = roof_fft["achieved"] / roof_fft["peak"]
+
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "config": workload_config(args), "clocks": clk,
+            "gpu_launches": launches, "per_kernel": per_kernel, "roofline": roof,
+            "roofline_fft": roof_fft, "fp64_peak_tflops": peak64.value}
+
+    # -------- e2e through the public API with host (pinned) buffers
+    if not args.no_e2e:
+        ke = args.e2e_maps or nmaps
+        line["e2e"] = e2e(sht if ke == nmaps else SHT(nside, lmax, ke, device=local),
+                          maps, ke, args, world)
+    # -------- CPU baseline and parity sample (rank 0, N = 1)
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        k = min(args.cpu_maps, nmaps)
+        maps_np = np.asfortranarray(maps[:, :k].cpu().numpy())
+        cb, alm_ref = cpu_baseline(nside, lmax, nmaps, k, maps_np, sht.ring_skip(),
+                                   want_alm=True)
+        line["cpu_baseline"] = cb
+        got = out[:k].cpu().numpy()
+        d = np.abs(got - alm_ref).reshape(k, -1).max(axis=1)
+        sc = np.abs(alm_ref).reshape(k, -1).max(axis=1)
+        line["parity"] = {"max_rel_alm_err_vs_oracle": float((d / sc).max()),
+                          "maps_checked": k, "tolerance": 1e-11}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+
+
+def e2e(sht, maps_dev, ke, args, world):
+    """Same metric through SHT.t2alm with host buffers: every step copies the maps
+    host->device and the alm device->host (pinned buffers, reused)."""
+    import torch
+    npix = sht.npix
+    L = sht.lmax + 1
+    host = torch.empty((ke, npix), dtype=torch.float64, pin_memory=True)
+    host.copy_(maps_dev.T[:ke])
+    maps_np = host.numpy().T                     # (npix, ke) Fortran order
+    out_t = torch.empty((L, L, ke), dtype=torch.float64, pin_memory=True)
+    out_np = out_t.numpy().T                     # (ke, L, L) Fortran order
+    sht.t2alm(maps_np, alms_in=out_np)           # warm-up
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        sht.t2alm(maps_np, alms_in=out_np)
+    torch.cuda.synchronize()
+    dt = time.perf_counter() - t0
+    return {"value": world * ke * args.steps / dt, "unit": UNIT,
+            "h2d_bytes_per_step": ke * npix * 8, "d2h_bytes_per_step": ke * L * L * 8,
+            "maps_per_step": ke}
+
+
+def main():
+    args = parse()
+    rank, world, local = dist_env()
+    if args.impl == "reference":
+        reference_arm(args, rank, world)
+        return
+    ours(args, rank, world, local)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,48 @@
+// Measurement helper: FP64 FMA throughput of the current device, the roofline
+// denominator for the plain-FP64 kernels (the measured peaks cover HBM and
+// BF16 only).
+#include "common.cuh"
+
+namespace {
+__global__ void k_dfma_loop(double* out, int iters, double a, double b) {
+  double x0 = threadIdx.x, x1 = x0 + 1, x2 = x0 + 2, x3 = x0 + 3;
+  double x4 = x0 + 4, x5 = x0 + 5, x6 = x0 + 6, x7 = x0 + 7;
+  for (int i = 0; i < iters; ++i) {
+    x0 = fma(x0, a, b); x1 = fma(x1, a, b); x2 = fma(x2, a, b); x3 = fma(x3, a, b);
+    x4 = fma(x4, a, b); x5 = fma(x5, a, b); x6 = fma(x6, a, b); x7 = fma(x7, a, b);
+  }
+  out[blockIdx.x * blockDim.x + threadIdx.x] = x0 + x1 + x2 + x3 + x4 + x5 + x6 + x7;
+}
+}  // namespace
+
+extern "C" int fsht_measure_fp64_peak(double* tflops) {
+  if (!tflops) {
+    fsht_set_error("null output");
+    return FSHT_EINVAL;
+  }
+  int dev = 0, nsm = 0;
+  FSHT_CUDA_TRY(cudaGetDevice(&dev));
+  FSHT_CUDA_TRY(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+  const int blocks = nsm * 8, threads = 256, iters = 8000;
+  double* out = nullptr;
+  FSHT_CUDA_TRY(cudaMalloc(&out, sizeof(double) * blocks * threads));
+  cudaEvent_t e0, e1;
+  FSHT_CUDA_TRY(cudaEventCreate(&e0));
+  FSHT_CUDA_TRY(cudaEventCreate(&e1));
+  float best = 1e30f;
+  for (int rep = 0; rep < 3; ++rep) {
+    FSHT_CUDA_TRY(cudaEventRecord(e0, 0));
+    k_dfma_loop<<<blocks, threads>>>(out, iters, 0.999, 1e-3);
+    FSHT_LAUNCH_CHECK();
+    FSHT_CUDA_TRY(cudaEventRecord(e1, 0));
+    FSHT_CUDA_TRY(cudaEventSynchronize(e1));
+    float ms = 0.f;
+    FSHT_CUDA_TRY(cudaEventElapsedTime(&ms, e0, e1));
+    if (ms < best) best = ms;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(out);
+  *tflops = 2.0 * 8 * (double)iters * blocks * threads / (best * 1e-3) / 1e12;
+  return FSHT_OK;
+}

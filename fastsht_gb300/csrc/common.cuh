@@ -1,0 +1,119 @@
+// Shared device/host helpers for the fastsht_gb300 CUDA library (sm_103a).
+#pragma once
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <cstddef>
+
+#define FSHT_HD __host__ __device__ __forceinline__
+
+// ---------------------------------------------------------------- complex FP64
+FSHT_HD double2 cadd(double2 a, double2 b) { return make_double2(a.x + b.x, a.y + b.y); }
+FSHT_HD double2 csub(double2 a, double2 b) { return make_double2(a.x - b.x, a.y - b.y); }
+FSHT_HD double2 cmul(double2 a, double2 b) {
+  return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+FSHT_HD double2 cconj(double2 a) { return make_double2(a.x, -a.y); }
+FSHT_HD double2 cscale(double2 a, double s) { return make_double2(a.x * s, a.y * s); }
+
+// ---------------------------------------------------------------- ring geometry
+// Ring i of 4*nside-1: start pixel and length (reference get_ring_info,
+// src/sht_data_init.f90:644-686).
+FSHT_HD long long ring_start(int ns, int i) {
+  long long n = ns;
+  if (i < ns) return 2LL * i * (i + 1);
+  if (i < 3 * ns - 1) return 2 * n + 4 * n * i - 2 * n * n;
+  long long r = 4 * n - i;
+  return 12 * n * n - 2 * (r - 1) * r;
+}
+FSHT_HD int ring_len(int ns, int i) {
+  if (i < ns) return 4 * (i + 1);
+  if (i < 3 * ns - 1) return 4 * ns;
+  return 4 * (4 * ns - 1 - i);
+}
+// The first pixel of north ring i sits at phi0 = pi * s / n with s in {0, 1}:
+// cap rings phi0 = pi/(4(i+1)) = pi/n; belt rings phi0 = pi/(4 nside) when
+// (i+1-nside) is even, else 0 (HEALPix pix2ang, used by SHT.py:47-50).
+FSHT_HD int ring_phase_flag(int ns, int i) {
+  if (i < ns) return 1;
+  return ((i + 1 - ns) % 2 == 0) ? 1 : 0;
+}
+
+// ---------------------------------------------------------------- plan
+struct FshtRingFFT {
+  int n;          // ring length
+  int P;          // FFT size used (n when pow2, else the Bluestein size)
+  int logP;
+  int bluestein;  // 1 when n is not a power of two
+  long long chirp_off;  // offset (double2) of w_j = exp(-i pi j^2/n), j < n
+  long long bhat_off;   // offset (double2) of FFT_P(conj chirp, wrapped)
+};
+
+struct fsht_plan {
+  int nside, lmax, nring, nnorth;  // nnorth = 2*nside (north rings incl. equator)
+  long long npix;
+  int nmaps_max, kchunk;           // maps per workspace pass
+  int pol, precision;
+  cudaStream_t stream;
+  double pa;                       // 4 pi / npix (sht_data_init.f90:18)
+  // device tables
+  double* d_cth;                   // cos(theta_i), i < 2 nside
+  double* d_sth;                   // sin(theta_i)
+  double* d_pref;                  // sqrt(diag_fac(m) / (4 pi)), m <= lmax
+  int* d_ring_i0;                  // first kept ring for order m (m <= lmax)
+  int* h_ring_i0;
+  FshtRingFFT* d_rfft;             // per north ring
+  double2* d_chirp;                // Bluestein chirps
+  double2* d_bhat;                 // Bluestein filter spectra
+  double2* d_tw;                   // exp(-2 pi i j / Pmax), j < Pmax/2
+  int Pmax, logPmax;
+  // workspace: phase matrices [m][i][k] x 2 complex, one per buffer
+  double2* d_work;
+  size_t work_bytes;
+  int nbuf;
+  size_t fft_smem;                 // dynamic smem of the ring FFT kernels
+  struct FshtProfile* prof;        // non-null while per-kernel timing is on
+};
+
+// ---------------------------------------------------------------- status codes
+#include "../../include/fastsht.h"
+
+void fsht_set_error(const char* fmt, ...);
+
+#define FSHT_CUDA_TRY(expr)                                                   \
+  do {                                                                        \
+    cudaError_t _e = (expr);                                                  \
+    if (_e != cudaSuccess) {                                                  \
+      fsht_set_error("%s:%d: %s: %s", __FILE__, __LINE__, #expr,              \
+                     cudaGetErrorString(_e));                                 \
+      return FSHT_ECUDA;                                                      \
+    }                                                                         \
+  } while (0)
+
+#define FSHT_LAUNCH_CHECK()                                                   \
+  do {                                                                        \
+    cudaError_t _e = cudaGetLastError();                                      \
+    if (_e != cudaSuccess) {                                                  \
+      fsht_set_error("%s:%d: kernel launch: %s", __FILE__, __LINE__,          \
+                     cudaGetErrorString(_e));                                 \
+      return FSHT_ECUDA;                                                      \
+    }                                                                         \
+  } while (0)
+
+// ---------------------------------------------------------------- internal API
+int fsht_fft_tables_init(fsht_plan* p);
+int fsht_launch_ring_fft_fwd(fsht_plan* p, const double* maps, long long map_stride,
+                             int kc, double2* W, cudaStream_t s);
+int fsht_launch_ring_fft_inv(fsht_plan* p, const double2* W, double* maps,
+                             long long map_stride, int kc, cudaStream_t s);
+int fsht_launch_fourier_residual(fsht_plan* p, const double2* X, double2* GR, int kc,
+                                 int prefix, cudaStream_t s);
+int fsht_launch_ring_skip(fsht_plan* p, cudaStream_t s);
+// Legendre contraction, FP64.  alm layout: [col][l][k] with ld = nmaps total,
+// k offset k0.  which: bit0 = E (or T), bit1 = B.
+int fsht_launch_analysis_fp64(fsht_plan* p, int spin, const double2* WQ,
+                              const double2* WU, double* almE, double* almB,
+                              int nmaps_total, int k0, int kc, int accumulate,
+                              int which, cudaStream_t s);
+int fsht_launch_synthesis_fp64(fsht_plan* p, int spin, const double* almE,
+                               const double* almB, double2* WQ, double2* WU,
+                               int nmaps_total, int k0, int kc, cudaStream_t s);

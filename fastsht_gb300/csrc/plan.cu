@@ -1,0 +1,557 @@
+// Plan management and the C ABI of fastsht_gb300 (include/fastsht.h).
+//
+// A plan replaces the reference's global Fortran module state
+// (src/sht_data_module.f90, allocated by sht_data_alloc / sht_set_data,
+// src/sht_data_init.f90:2-311): ring geometry, recursion seeds, ring-skip table,
+// FFT tables and the phase-matrix workspace all live in one object bound to a
+// CUDA stream, so independent plans can run concurrently.
+#include "common.cuh"
+
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+namespace {
+thread_local std::string g_last_error;
+constexpr size_t kDefaultWorkspace = 16ull << 30;
+}  // namespace
+
+// Per-kernel event timing (enabled by fsht_profile_enable).
+struct FshtProfile {
+  std::vector<cudaEvent_t> pending[FSHT_KCAT_COUNT];   // begin/end pairs
+  int launches[FSHT_KCAT_COUNT] = {0};
+  double ms[FSHT_KCAT_COUNT] = {0.0};
+  std::vector<cudaEvent_t> pool;
+  cudaEvent_t get() {
+    if (!pool.empty()) {
+      cudaEvent_t e = pool.back();
+      pool.pop_back();
+      return e;
+    }
+    cudaEvent_t e = nullptr;
+    cudaEventCreate(&e);
+    return e;
+  }
+};
+
+namespace {
+struct ProfScope {
+  fsht_plan* p;
+  int cat;
+  ProfScope(fsht_plan* pp, int c) : p(pp), cat(c) {
+    if (p->prof) {
+      cudaEvent_t e = p->prof->get();
+      cudaEventRecord(e, p->stream);
+      p->prof->pending[cat].push_back(e);
+    }
+  }
+  ~ProfScope() {
+    if (p->prof) {
+      cudaEvent_t e = p->prof->get();
+      cudaEventRecord(e, p->stream);
+      p->prof->pending[cat].push_back(e);
+    }
+  }
+};
+}  // namespace
+#define FSHT_PROF(cat) ProfScope _prof_scope_##__LINE__(p, cat)
+
+void fsht_set_error(const char* fmt, ...) {
+  char buf[1024];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  g_last_error = buf;
+}
+
+namespace {
+
+void free_plan_memory(fsht_plan* p) {
+  if (!p) return;
+  cudaFree(p->d_cth);
+  cudaFree(p->d_sth);
+  cudaFree(p->d_pref);
+  cudaFree(p->d_ring_i0);
+  cudaFree(p->d_rfft);
+  cudaFree(p->d_chirp);
+  cudaFree(p->d_bhat);
+  cudaFree(p->d_tw);
+  cudaFree(p->d_work);
+  delete[] p->h_ring_i0;
+  if (p->prof) {
+    for (auto& v : p->prof->pending)
+      for (auto e : v) cudaEventDestroy(e);
+    for (auto e : p->prof->pool) cudaEventDestroy(e);
+    delete p->prof;
+    p->prof = nullptr;
+  }
+}
+
+// theta of the first pixel of north ring i (HEALPix pix2loc, as used through
+// healpy.pix2ang at the ring start pixels, SHT.py:47-50).
+double ring_theta(int ns, int i) {
+  const double npix = 12.0 * ns * ns;
+  const double fact2 = 4.0 / npix;
+  const double fact1 = (double)(2 * ns) * fact2;
+  const int ir = i + 1;
+  if (ir < ns) {
+    const double tmp = (double)ir * (double)ir * fact2;
+    const double z = 1.0 - tmp;
+    if (z > 0.99) return std::atan2(std::sqrt(tmp * (2.0 - tmp)), z);
+    return std::acos(z);
+  }
+  const double z = (double)(2 * ns - ir) * fact1;
+  return std::acos(z);
+}
+
+int check_plan(const fsht_plan* p) {
+  if (!p) {
+    fsht_set_error("null plan");
+    return FSHT_EINVAL;
+  }
+  return FSHT_OK;
+}
+
+size_t per_map_buffer_bytes(const fsht_plan* p) {
+  return (size_t)(p->lmax + 1) * p->nnorth * 2 * sizeof(double2);
+}
+
+double2* work_buf(fsht_plan* p, int b, int kc) {
+  return p->d_work + (size_t)b * kc * (size_t)(p->lmax + 1) * p->nnorth * 2;
+}
+
+int check_call(fsht_plan* p, int nmaps, const void* a, const void* b) {
+  int rc = check_plan(p);
+  if (rc) return rc;
+  if (nmaps < 1 || nmaps > p->nmaps_max) {
+    fsht_set_error("nmaps = %d outside [1, %d] of this plan", nmaps, p->nmaps_max);
+    return FSHT_EINVAL;
+  }
+  if (!a || !b) {
+    fsht_set_error("null array pointer");
+    return FSHT_EINVAL;
+  }
+  return FSHT_OK;
+}
+
+int need_bufs(fsht_plan* p, int nb) {
+  if (nb > p->nbuf) {
+    fsht_set_error("this call needs %d workspace buffers but the plan holds %d "
+                   "(create it with FSHT_FLAG_POL / FSHT_FLAG_ITER)", nb, p->nbuf);
+    return FSHT_EINVAL;
+  }
+  return FSHT_OK;
+}
+
+#define FSHT_TRY(expr)       \
+  do {                       \
+    int _rc = (expr);        \
+    if (_rc) return _rc;     \
+  } while (0)
+
+}  // namespace
+
+extern "C" {
+
+int fsht_last_error(char* buf, size_t len) {
+  if (buf && len) {
+    size_t n = g_last_error.size() < len - 1 ? g_last_error.size() : len - 1;
+    memcpy(buf, g_last_error.data(), n);
+    buf[n] = 0;
+  }
+  return (int)g_last_error.size();
+}
+
+int fsht_plan_create(int nside, int lmax, int nmaps_max, int flags, int precision,
+                     size_t workspace_limit_bytes, void* stream, fsht_plan** out) {
+  if (!out) {
+    fsht_set_error("null output pointer");
+    return FSHT_EINVAL;
+  }
+  *out = nullptr;
+  if (nside < 1 || nside > 1024 || (nside & (nside - 1))) {
+    fsht_set_error("nside = %d: must be a power of two in [1, 1024]", nside);
+    return nside > 1024 && !(nside & (nside - 1)) ? FSHT_EUNSUPPORTED : FSHT_EINVAL;
+  }
+  if (lmax < 0 || lmax > 4 * nside) {
+    fsht_set_error("lmax = %d outside [0, 4*nside = %d]", lmax, 4 * nside);
+    return FSHT_EINVAL;
+  }
+  if (nmaps_max < 1) {
+    fsht_set_error("nmaps_max = %d must be >= 1", nmaps_max);
+    return FSHT_EINVAL;
+  }
+  if (precision != FSHT_PREC_FP64) {
+    fsht_set_error("precision %d not available in this plan kind", precision);
+    return FSHT_EUNSUPPORTED;
+  }
+  fsht_plan* p = new (std::nothrow) fsht_plan();
+  if (!p) {
+    fsht_set_error("host allocation failed");
+    return FSHT_ENOMEM;
+  }
+  memset(p, 0, sizeof(*p));
+  p->nside = nside;
+  p->lmax = lmax;
+  p->nring = 4 * nside - 1;
+  p->nnorth = 2 * nside;
+  p->npix = 12LL * nside * nside;
+  p->nmaps_max = nmaps_max;
+  p->pol = (flags & FSHT_FLAG_POL) ? 1 : 0;
+  p->precision = precision;
+  p->stream = (cudaStream_t)stream;
+  p->pa = 4.0 * M_PI / (double)p->npix;
+  p->nbuf = ((flags & FSHT_FLAG_POL) ? 2 : 1) * ((flags & FSHT_FLAG_ITER) ? 2 : 1);
+  p->h_ring_i0 = new (std::nothrow) int[lmax + 1];
+  int rc = FSHT_OK;
+  auto fail = [&](int code) {
+    free_plan_memory(p);
+    delete p;
+    return code;
+  };
+  if (!p->h_ring_i0) {
+    fsht_set_error("host allocation failed");
+    return fail(FSHT_ENOMEM);
+  }
+  // ---- ring tables
+  const int nn = p->nnorth;
+  std::vector<double> cth(nn), sth(nn), pref(lmax + 1);
+  for (int i = 0; i < nn; ++i) {
+    const double th = ring_theta(nside, i);
+    cth[i] = std::cos(th);
+    sth[i] = std::sin(th);
+  }
+  // diag_fac(m) = prod_{k<=m} (2k+1)/(2k)  (set_out_of_loop_constants,
+  // src/sht_data_init.f90:414-418); seed prefactor sqrt(diag_fac/4/pi)
+  // (get_plm_recursive.f90:46)
+  double df = 1.0;
+  for (int m = 0; m <= lmax; ++m) {
+    if (m > 0) df = df * (2 * m + 1) / 2 / m;
+    pref[m] = std::sqrt(df / 4 / M_PI);
+  }
+  auto dalloc = [&](void** ptr, size_t bytes) -> int {
+    cudaError_t e = cudaMalloc(ptr, bytes);
+    if (e != cudaSuccess) {
+      fsht_set_error("cudaMalloc(%zu): %s", bytes, cudaGetErrorString(e));
+      return e == cudaErrorMemoryAllocation ? FSHT_ENOMEM : FSHT_ECUDA;
+    }
+    return FSHT_OK;
+  };
+  if ((rc = dalloc((void**)&p->d_cth, sizeof(double) * nn))) return fail(rc);
+  if ((rc = dalloc((void**)&p->d_sth, sizeof(double) * nn))) return fail(rc);
+  if ((rc = dalloc((void**)&p->d_pref, sizeof(double) * (lmax + 1)))) return fail(rc);
+  if ((rc = dalloc((void**)&p->d_ring_i0, sizeof(int) * (lmax + 1)))) return fail(rc);
+  cudaError_t ce;
+  if ((ce = cudaMemcpyAsync(p->d_cth, cth.data(), sizeof(double) * nn, cudaMemcpyHostToDevice,
+                            p->stream)) != cudaSuccess ||
+      (ce = cudaMemcpyAsync(p->d_sth, sth.data(), sizeof(double) * nn, cudaMemcpyHostToDevice,
+                            p->stream)) != cudaSuccess ||
+      (ce = cudaMemcpyAsync(p->d_pref, pref.data(), sizeof(double) * (lmax + 1),
+                            cudaMemcpyHostToDevice, p->stream)) != cudaSuccess) {
+    fsht_set_error("table upload: %s", cudaGetErrorString(ce));
+    return fail(FSHT_ECUDA);
+  }
+  if ((rc = fsht_launch_ring_skip(p, p->stream))) return fail(rc);
+  if ((rc = fsht_fft_tables_init(p))) return fail(rc);
+  // ---- workspace: nbuf phase matrices of kchunk maps
+  const size_t limit = workspace_limit_bytes ? workspace_limit_bytes : kDefaultWorkspace;
+  const size_t per_map = per_map_buffer_bytes(p) * p->nbuf;
+  size_t kc = limit / per_map;
+  if (kc < 1) {
+    fsht_set_error("workspace limit %zu bytes is below one map's %zu bytes", limit, per_map);
+    return fail(FSHT_EINVAL);
+  }
+  if (kc > (size_t)nmaps_max) kc = nmaps_max;
+  p->kchunk = (int)kc;
+  p->work_bytes = per_map * kc;
+  if ((rc = dalloc((void**)&p->d_work, p->work_bytes))) return fail(rc);
+  if ((ce = cudaStreamSynchronize(p->stream)) != cudaSuccess) {
+    fsht_set_error("plan setup: %s", cudaGetErrorString(ce));
+    return fail(FSHT_ECUDA);
+  }
+  *out = p;
+  return FSHT_OK;
+}
+
+int fsht_plan_destroy(fsht_plan* p) {
+  if (!p) return FSHT_OK;
+  cudaStreamSynchronize(p->stream);
+  free_plan_memory(p);
+  delete p;
+  return FSHT_OK;
+}
+
+int fsht_plan_set_stream(fsht_plan* p, void* stream) {
+  FSHT_TRY(check_plan(p));
+  p->stream = (cudaStream_t)stream;
+  return FSHT_OK;
+}
+
+int fsht_plan_info(const fsht_plan* p, size_t* device_bytes, int* maps_per_chunk) {
+  FSHT_TRY(check_plan(p));
+  if (device_bytes) {
+    size_t b = p->work_bytes;
+    b += sizeof(double) * (2 * p->nnorth + p->lmax + 1) + sizeof(int) * (p->lmax + 1);
+    *device_bytes = b;
+  }
+  if (maps_per_chunk) *maps_per_chunk = p->kchunk;
+  return FSHT_OK;
+}
+
+int fsht_plan_ring_skip(const fsht_plan* p, int* out) {
+  FSHT_TRY(check_plan(p));
+  if (!out) {
+    fsht_set_error("null output");
+    return FSHT_EINVAL;
+  }
+  memcpy(out, p->h_ring_i0, sizeof(int) * (p->lmax + 1));
+  return FSHT_OK;
+}
+
+int fsht_profile_enable(fsht_plan* p, int on) {
+  FSHT_TRY(check_plan(p));
+  if (on && !p->prof) p->prof = new (std::nothrow) FshtProfile();
+  if (on && !p->prof) {
+    fsht_set_error("host allocation failed");
+    return FSHT_ENOMEM;
+  }
+  if (!on && p->prof) {
+    cudaStreamSynchronize(p->stream);
+    for (auto& v : p->prof->pending)
+      for (auto e : v) cudaEventDestroy(e);
+    for (auto e : p->prof->pool) cudaEventDestroy(e);
+    delete p->prof;
+    p->prof = nullptr;
+  }
+  return FSHT_OK;
+}
+
+int fsht_profile_read(fsht_plan* p, int ncat, int* launches, double* total_ms) {
+  FSHT_TRY(check_plan(p));
+  if (!p->prof) {
+    fsht_set_error("profiling is not enabled on this plan");
+    return FSHT_EINVAL;
+  }
+  FSHT_CUDA_TRY(cudaStreamSynchronize(p->stream));
+  FshtProfile& pr = *p->prof;
+  for (int c = 0; c < FSHT_KCAT_COUNT; ++c) {
+    auto& v = pr.pending[c];
+    for (size_t j = 0; j + 1 < v.size(); j += 2) {
+      float ms = 0.f;
+      FSHT_CUDA_TRY(cudaEventElapsedTime(&ms, v[j], v[j + 1]));
+      pr.ms[c] += ms;
+      pr.launches[c] += 1;
+    }
+    for (auto e : v) pr.pool.push_back(e);
+    v.clear();
+    if (c < ncat) {
+      if (launches) launches[c] = pr.launches[c];
+      if (total_ms) total_ms[c] = pr.ms[c];
+    }
+    pr.launches[c] = 0;
+    pr.ms[c] = 0.0;
+  }
+  return FSHT_OK;
+}
+
+int fsht_run_stage(fsht_plan* p, int stage, const void* in, void* out, int nmaps) {
+  FSHT_TRY(check_call(p, nmaps, in, out));
+  if (nmaps > p->kchunk) {
+    fsht_set_error("run_stage: nmaps %d above maps_per_chunk %d", nmaps, p->kchunk);
+    return FSHT_EINVAL;
+  }
+  switch (stage) {
+    case FSHT_STAGE_FFT_FWD:
+      return fsht_launch_ring_fft_fwd(p, (const double*)in, p->npix, nmaps, (double2*)out,
+                                      p->stream);
+    case FSHT_STAGE_ANALYSIS:
+      return fsht_launch_analysis_fp64(p, 0, (const double2*)in, nullptr, (double*)out, nullptr,
+                                       nmaps, 0, nmaps, 0, 1, p->stream);
+    case FSHT_STAGE_SYNTHESIS:
+      return fsht_launch_synthesis_fp64(p, 0, (const double*)in, nullptr, (double2*)out, nullptr,
+                                        nmaps, 0, nmaps, p->stream);
+    case FSHT_STAGE_FFT_INV:
+      return fsht_launch_ring_fft_inv(p, (const double2*)in, (double*)out, p->npix, nmaps,
+                                      p->stream);
+    default:
+      fsht_set_error("unknown stage %d", stage);
+      return FSHT_EINVAL;
+  }
+}
+
+int fsht_plan_sync(fsht_plan* p) {
+  FSHT_TRY(check_plan(p));
+  FSHT_CUDA_TRY(cudaStreamSynchronize(p->stream));
+  return FSHT_OK;
+}
+
+// ----------------------------------------------------------------- temperature
+int fsht_t2alm(fsht_plan* p, const double* maps, double* alm, int nmaps, int niter, int method) {
+  FSHT_TRY(check_call(p, nmaps, maps, alm));
+  if (niter < 0 || method < 0 || method > 1) {
+    fsht_set_error("niter = %d, method = %d: need niter >= 0 and method 0 (old) or 1 (new)",
+                   niter, method);
+    return FSHT_EINVAL;
+  }
+  FSHT_TRY(need_bufs(p, niter > 0 ? 2 : 1));
+  for (int c0 = 0; c0 < nmaps; c0 += p->kchunk) {
+    const int kc = nmaps - c0 < p->kchunk ? nmaps - c0 : p->kchunk;
+    double2* W0 = work_buf(p, 0, kc);
+    double2* W1 = work_buf(p, 1, kc);
+    {
+      FSHT_PROF(FSHT_KCAT_FFT_FWD);
+      FSHT_TRY(fsht_launch_ring_fft_fwd(p, maps + (size_t)c0 * p->npix, p->npix, kc, W0, p->stream));
+    }
+    {
+      FSHT_PROF(FSHT_KCAT_ANALYSIS);
+      FSHT_TRY(fsht_launch_analysis_fp64(p, 0, W0, nullptr, alm, nullptr, nmaps, c0, kc, 0, 1,
+                                         p->stream));
+    }
+    for (int it = 0; it < niter; ++it) {
+      {
+        FSHT_PROF(FSHT_KCAT_SYNTHESIS);
+        FSHT_TRY(fsht_launch_synthesis_fp64(p, 0, alm, nullptr, W1, nullptr, nmaps, c0, kc,
+                                            p->stream));
+      }
+      {
+        FSHT_PROF(FSHT_KCAT_RESIDUAL);
+        FSHT_TRY(fsht_launch_fourier_residual(p, W0, W1, kc, method, p->stream));
+      }
+      {
+        FSHT_PROF(FSHT_KCAT_ANALYSIS);
+        FSHT_TRY(fsht_launch_analysis_fp64(p, 0, W1, nullptr, alm, nullptr, nmaps, c0, kc, 1, 1,
+                                           p->stream));
+      }
+    }
+  }
+  return FSHT_OK;
+}
+
+int fsht_alm2t(fsht_plan* p, const double* alm, double* maps, int nmaps) {
+  FSHT_TRY(check_call(p, nmaps, maps, alm));
+  for (int c0 = 0; c0 < nmaps; c0 += p->kchunk) {
+    const int kc = nmaps - c0 < p->kchunk ? nmaps - c0 : p->kchunk;
+    double2* W0 = work_buf(p, 0, kc);
+    {
+      FSHT_PROF(FSHT_KCAT_SYNTHESIS);
+      FSHT_TRY(fsht_launch_synthesis_fp64(p, 0, alm, nullptr, W0, nullptr, nmaps, c0, kc,
+                                          p->stream));
+    }
+    {
+      FSHT_PROF(FSHT_KCAT_FFT_INV);
+      FSHT_TRY(fsht_launch_ring_fft_inv(p, W0, maps + (size_t)c0 * p->npix, p->npix, kc, p->stream));
+    }
+  }
+  return FSHT_OK;
+}
+
+// ----------------------------------------------------------------- spin 2
+static int qu_analysis(fsht_plan* p, const double* Q, const double* U, double* almE,
+                       double* almB, int nmaps, int niter, int method, int which) {
+  FSHT_TRY(need_bufs(p, niter > 0 ? 4 : 2));
+  for (int c0 = 0; c0 < nmaps; c0 += p->kchunk) {
+    const int kc = nmaps - c0 < p->kchunk ? nmaps - c0 : p->kchunk;
+    double2* WQ = work_buf(p, 0, kc);
+    double2* WU = work_buf(p, 1, kc);
+    {
+      FSHT_PROF(FSHT_KCAT_FFT_FWD);
+      FSHT_TRY(fsht_launch_ring_fft_fwd(p, Q + (size_t)c0 * p->npix, p->npix, kc, WQ, p->stream));
+    }
+    {
+      FSHT_PROF(FSHT_KCAT_FFT_FWD);
+      FSHT_TRY(fsht_launch_ring_fft_fwd(p, U + (size_t)c0 * p->npix, p->npix, kc, WU, p->stream));
+    }
+    {
+      FSHT_PROF(FSHT_KCAT_ANALYSIS);
+      FSHT_TRY(fsht_launch_analysis_fp64(p, 2, WQ, WU, almE, almB, nmaps, c0, kc, 0, which,
+                                         p->stream));
+    }
+    if (niter > 0) {
+      double2* RQ = work_buf(p, 2, kc);
+      double2* RU = work_buf(p, 3, kc);
+      for (int it = 0; it < niter; ++it) {
+        {
+          FSHT_PROF(FSHT_KCAT_SYNTHESIS);
+          FSHT_TRY(fsht_launch_synthesis_fp64(p, 2, almE, almB, RQ, RU, nmaps, c0, kc, p->stream));
+        }
+        {
+          FSHT_PROF(FSHT_KCAT_RESIDUAL);
+          FSHT_TRY(fsht_launch_fourier_residual(p, WQ, RQ, kc, method, p->stream));
+        }
+        {
+          FSHT_PROF(FSHT_KCAT_RESIDUAL);
+          FSHT_TRY(fsht_launch_fourier_residual(p, WU, RU, kc, method, p->stream));
+        }
+        {
+          FSHT_PROF(FSHT_KCAT_ANALYSIS);
+          FSHT_TRY(fsht_launch_analysis_fp64(p, 2, RQ, RU, almE, almB, nmaps, c0, kc, 1, which,
+                                             p->stream));
+        }
+      }
+    }
+  }
+  return FSHT_OK;
+}
+
+int fsht_qu2eb(fsht_plan* p, const double* Q, const double* U, double* almE, double* almB,
+               int nmaps, int niter) {
+  FSHT_TRY(check_call(p, nmaps, Q, U));
+  if (!almE || !almB || niter < 0) {
+    fsht_set_error("null alm pointer or niter < 0");
+    return FSHT_EINVAL;
+  }
+  return qu_analysis(p, Q, U, almE, almB, nmaps, niter, 0, 3);
+}
+
+int fsht_qu2e(fsht_plan* p, const double* Q, const double* U, double* almE, int nmaps) {
+  FSHT_TRY(check_call(p, nmaps, Q, U));
+  if (!almE) {
+    fsht_set_error("null alm pointer");
+    return FSHT_EINVAL;
+  }
+  return qu_analysis(p, Q, U, almE, nullptr, nmaps, 0, 0, 1);
+}
+
+int fsht_qu2b(fsht_plan* p, const double* Q, const double* U, double* almB, int nmaps) {
+  FSHT_TRY(check_call(p, nmaps, Q, U));
+  if (!almB) {
+    fsht_set_error("null alm pointer");
+    return FSHT_EINVAL;
+  }
+  return qu_analysis(p, Q, U, nullptr, almB, nmaps, 0, 0, 2);
+}
+
+int fsht_eb2qu(fsht_plan* p, const double* almE, const double* almB, double* Q, double* U,
+               int nmaps) {
+  FSHT_TRY(check_call(p, nmaps, almE, almB));
+  if (!Q || !U) {
+    fsht_set_error("null map pointer");
+    return FSHT_EINVAL;
+  }
+  FSHT_TRY(need_bufs(p, 2));
+  for (int c0 = 0; c0 < nmaps; c0 += p->kchunk) {
+    const int kc = nmaps - c0 < p->kchunk ? nmaps - c0 : p->kchunk;
+    double2* WQ = work_buf(p, 0, kc);
+    double2* WU = work_buf(p, 1, kc);
+    {
+      FSHT_PROF(FSHT_KCAT_SYNTHESIS);
+      FSHT_TRY(fsht_launch_synthesis_fp64(p, 2, almE, almB, WQ, WU, nmaps, c0, kc, p->stream));
+    }
+    {
+      FSHT_PROF(FSHT_KCAT_FFT_INV);
+      FSHT_TRY(fsht_launch_ring_fft_inv(p, WQ, Q + (size_t)c0 * p->npix, p->npix, kc, p->stream));
+    }
+    {
+      FSHT_PROF(FSHT_KCAT_FFT_INV);
+      FSHT_TRY(fsht_launch_ring_fft_inv(p, WU, U + (size_t)c0 * p->npix, p->npix, kc, p->stream));
+    }
+  }
+  return FSHT_OK;
+}
+
+}  // extern "C"

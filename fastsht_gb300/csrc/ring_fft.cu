@@ -1,0 +1,597 @@
+// Batched FP64 ring FFTs for HEALPix maps, with the phi0 phase shift, the
+// m-aliasing and the north/south folding done in the same pass.
+//
+// Replaces the reference's map2fft / fft2map (src/compute_fft.f90:15-280, MKL DFTI
+// on the host + per-ring PCIe copies) and the per-m gathers fft2mat_fast /
+// mat2fft_fast / mat2fft_fast_iter (src/fft_mapping.f90:19-190).
+//
+// Phase-matrix layout written/read by these kernels ("W"), one per field:
+//   W[((m * nnorth + i) * kc + k) * 2 + {0,1}]  (double2)
+// for order m <= lmax, north ring i < 2*nside, map k < kc.
+//   analysis:  {S, D} = {F_m(i) + F_m(i'), F_m(i) - F_m(i')},  i' = nring-1-i,
+//              F_m(i) = sum_j x_{i,j} exp(-i m (phi0_i + 2 pi j / n_i))
+//   synthesis: {G_m(i), G_m(i')} with map_{i,j} = Re sum_m c_m G_m(i) e^{i m (phi0 + 2 pi j/n)},
+//              c_0 = 1, c_{m>0} = 2.
+// The equator ring (i = 2 nside - 1) is its own mirror: S = D = F_m, and only
+// G_m(i) is used.
+#include "common.cuh"
+#include <cmath>
+#include <vector>
+#include <climits>
+
+namespace {
+
+// In-place radix-2 DIT FFT of P = 2^logP points held in shared memory.
+// tw[j] = exp(-2 pi i j / 2^logPmax), j < 2^(logPmax-1).  inverse: exp(+...),
+// unnormalised.  All threads of the block must call it; it synchronises the block
+// on entry and on exit.
+__device__ void smem_fft(double2* buf, int P, int logP, const double2* __restrict__ tw,
+                         int logPmax, bool inverse) {
+  const int tid = threadIdx.x, nt = blockDim.x;
+  __syncthreads();   // the caller's writes to buf must land before the permutation
+  if (logP > 0) {
+    for (int i = tid; i < P; i += nt) {
+      int j = (int)(__brev((unsigned)i) >> (32 - logP));
+      if (j > i) {
+        double2 t = buf[i];
+        buf[i] = buf[j];
+        buf[j] = t;
+      }
+    }
+  }
+  __syncthreads();
+  for (int s = 1; s <= logP; ++s) {
+    const int half = 1 << (s - 1);
+    const int shift = logPmax - s;
+    for (int idx = tid; idx < (P >> 1); idx += nt) {
+      const int j = idx & (half - 1);
+      const int a = ((idx >> (s - 1)) << s) + j;
+      const int b = a + half;
+      double2 w = __ldg(&tw[j << shift]);
+      if (inverse) w.y = -w.y;
+      const double2 u = buf[a];
+      const double2 t = cmul(w, buf[b]);
+      buf[a] = cadd(u, t);
+      buf[b] = csub(u, t);
+    }
+    __syncthreads();
+  }
+}
+
+// DFT of n points (in buf[0..n)) -> Z (in buf[0..n)); forward (e^{-2 pi i jk/n}).
+// For non power-of-two n uses Bluestein with the ring's precomputed chirp and
+// filter spectrum (filter already divided by P).
+__device__ void ring_dft(double2* buf, const FshtRingFFT& rf, const double2* __restrict__ tw,
+                         int logPmax, const double2* __restrict__ chirp,
+                         const double2* __restrict__ bhat) {
+  const int tid = threadIdx.x, nt = blockDim.x;
+  if (!rf.bluestein) {
+    smem_fft(buf, rf.P, rf.logP, tw, logPmax, false);
+    return;
+  }
+  const int n = rf.n, P = rf.P;
+  for (int j = tid; j < P; j += nt) {
+    if (j < n) buf[j] = cmul(buf[j], __ldg(&chirp[j]));
+    else buf[j] = make_double2(0.0, 0.0);
+  }
+  smem_fft(buf, P, rf.logP, tw, logPmax, false);
+  for (int j = tid; j < P; j += nt) buf[j] = cmul(buf[j], __ldg(&bhat[j]));
+  smem_fft(buf, P, rf.logP, tw, logPmax, true);
+  for (int j = tid; j < n; j += nt) buf[j] = cmul(buf[j], __ldg(&chirp[j]));
+  __syncthreads();
+}
+
+// ------------------------------------------------------------------ tables
+__global__ void k_twiddles(double2* tw, int Pmax) {
+  int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j < Pmax / 2) {
+    double s, c;
+    sincospi(-2.0 * (double)j / (double)Pmax, &s, &c);
+    tw[j] = make_double2(c, s);
+  }
+}
+
+// chirp w_j = exp(-i pi j^2 / n) and the wrapped filter b (time domain) for one ring;
+// block per Bluestein ring.
+__global__ void k_bluestein_tables(const FshtRingFFT* rfs, const int* rings, double2* chirp,
+                                   double2* bhat, const double2* tw, int logPmax) {
+  extern __shared__ double2 sbuf[];
+  const FshtRingFFT rf = rfs[rings[blockIdx.x]];
+  const int n = rf.n, P = rf.P;
+  double2* w = chirp + rf.chirp_off;
+  for (int j = threadIdx.x; j < n; j += blockDim.x) {
+    long long r = ((long long)j * j) % (2LL * n);
+    double s, c;
+    sincospi(-(double)r / (double)n, &s, &c);
+    w[j] = make_double2(c, s);
+  }
+  __syncthreads();
+  for (int j = threadIdx.x; j < P; j += blockDim.x) {
+    double2 v = make_double2(0.0, 0.0);
+    if (j < n) v = cconj(w[j]);
+    else if (P - j < n) v = cconj(w[P - j]);
+    sbuf[j] = v;
+  }
+  __syncthreads();
+  smem_fft(sbuf, P, rf.logP, tw, logPmax, false);
+  const double invP = 1.0 / (double)P;
+  for (int j = threadIdx.x; j < P; j += blockDim.x) bhat[rf.bhat_off + j] = cscale(sbuf[j], invP);
+}
+
+// ------------------------------------------------------------------ forward
+struct FwdArgs {
+  const double* maps;       // chunk base: map k at maps + k * map_stride
+  long long map_stride;
+  int kc;                   // maps in this chunk
+  int maps_per_block;
+  int nside, lmax, nnorth, nring, ring_base;
+  const FshtRingFFT* rfs;
+  const double2* tw;
+  int logPmax;
+  const double2* chirp;
+  const double2* bhat;
+  const int* ring_i0;
+  double2* W;
+};
+
+__global__ void __launch_bounds__(512) k_ring_fft_fwd(FwdArgs a) {
+  extern __shared__ double2 smem[];
+  const int i = a.ring_base + blockIdx.x;      // north ring index
+  const FshtRingFFT rf = a.rfs[i];
+  const int n = rf.n;
+  double2* buf = smem;                          // rf.P entries
+  double2* ph = smem + rf.P;                    // lmax+1 phase factors exp(-i m phi0)
+  const int tid = threadIdx.x, nt = blockDim.x;
+  const bool equator = (i == a.nnorth - 1);
+  const int ip = a.nring - 1 - i;
+  const long long off_n = ring_start(a.nside, i);
+  const long long off_s = ring_start(a.nside, ip);
+  const int sflag = ring_phase_flag(a.nside, i);
+  // highest m for which ring i is kept (ring_i0 is non-decreasing in m)
+  int mtop = a.lmax;
+  while (mtop >= 0 && a.ring_i0[mtop] > i) --mtop;   // uniform loop, lmax small-ish
+  for (int m = tid; m <= mtop; m += nt) {
+    double s = 0.0, c = 1.0;
+    if (sflag) {
+      long long r = (long long)m % (2LL * n);
+      sincospi(-(double)r / (double)n, &s, &c);
+    }
+    ph[m] = make_double2(c, s);
+  }
+  const int k_begin = blockIdx.y * a.maps_per_block;
+  const int k_end = min(a.kc, k_begin + a.maps_per_block);
+  const double2* chirp = a.chirp + rf.chirp_off;
+  const double2* bhat = a.bhat + rf.bhat_off;
+  for (int k = k_begin; k < k_end; ++k) {
+    const double* xn = a.maps + (long long)k * a.map_stride + off_n;
+    const double* xs = a.maps + (long long)k * a.map_stride + off_s;
+    __syncthreads();
+    for (int j = tid; j < n; j += nt)
+      buf[j] = make_double2(__ldg(&xn[j]), equator ? 0.0 : __ldg(&xs[j]));
+    __syncthreads();
+    ring_dft(buf, rf, a.tw, a.logPmax, chirp, bhat);
+    // Z = FFT(x_N + i x_S): X_N[q] = (Z[q] + conj Z[-q])/2, X_S[q] = (Z[q] - conj Z[-q])/(2i)
+    for (int m = tid; m <= mtop; m += nt) {
+      const int q = m % n;
+      const int qn = (q == 0) ? 0 : n - q;
+      const double2 zq = buf[q];
+      const double2 zn = cconj(buf[qn]);
+      const double2 xN = cscale(cadd(zq, zn), 0.5);
+      const double2 dd = csub(zq, zn);
+      const double2 xS = make_double2(0.5 * dd.y, -0.5 * dd.x);
+      const double2 p = ph[m];
+      const double2 fN = cmul(p, xN);
+      double2* w = a.W + (((long long)m * a.nnorth + i) * a.kc + k) * 2;
+      if (equator) {
+        w[0] = fN;
+        w[1] = fN;
+      } else {
+        const double2 fS = cmul(p, xS);
+        w[0] = cadd(fN, fS);
+        w[1] = csub(fN, fS);
+      }
+    }
+  }
+}
+
+// ------------------------------------------------------------------ inverse
+struct InvArgs {
+  const double2* W;
+  double* maps;
+  long long map_stride;
+  int kc, maps_per_block;
+  int nside, lmax, nnorth, nring, ring_base;
+  const FshtRingFFT* rfs;
+  const double2* tw;
+  int logPmax;
+  const double2* chirp;
+  const double2* bhat;
+  const int* ring_i0;
+};
+
+// Builds, in buf[0..n), the packed spectrum Z[q] = Y_N[q] + i Y_S[q] of the two
+// real rings from G_m (north) and G_m(i') (south), m <= mtop:
+//   Y[q] = sum_{m = q mod n} (c_m/2) G_m e^{i m phi0} + sum_{m = -q mod n} (c_m/2) conj(G_m e^{i m phi0})
+__device__ void build_spectrum(double2* buf, const double2* ph, const double2* __restrict__ W,
+                               long long stride_m, int n, int mtop, bool equator) {
+  for (int q = threadIdx.x; q < n; q += blockDim.x) {
+    double2 yN = make_double2(0.0, 0.0), yS = make_double2(0.0, 0.0);
+    // m = q (mod n)
+    for (int m = q; m <= mtop; m += n) {
+      const double2* w = W + (long long)m * stride_m;
+      const double c = (m == 0) ? 0.5 : 1.0;
+      yN = cadd(yN, cscale(cmul(ph[m], w[0]), c));
+      if (!equator) yS = cadd(yS, cscale(cmul(ph[m], w[1]), c));
+    }
+    // m = -q (mod n)
+    const int q2 = (q == 0) ? 0 : n - q;
+    for (int m = q2; m <= mtop; m += n) {
+      const double2* w = W + (long long)m * stride_m;
+      const double c = (m == 0) ? 0.5 : 1.0;
+      yN = cadd(yN, cscale(cconj(cmul(ph[m], w[0])), c));
+      if (!equator) yS = cadd(yS, cscale(cconj(cmul(ph[m], w[1])), c));
+    }
+    buf[q] = make_double2(yN.x - yS.y, yN.y + yS.x);   // Y_N + i Y_S
+  }
+}
+
+__global__ void __launch_bounds__(512) k_ring_fft_inv(InvArgs a) {
+  extern __shared__ double2 smem[];
+  const int i = a.ring_base + blockIdx.x;
+  const FshtRingFFT rf = a.rfs[i];
+  const int n = rf.n;
+  double2* buf = smem;
+  double2* ph = smem + rf.P;
+  const int tid = threadIdx.x, nt = blockDim.x;
+  const bool equator = (i == a.nnorth - 1);
+  const int ip = a.nring - 1 - i;
+  const long long off_n = ring_start(a.nside, i);
+  const long long off_s = ring_start(a.nside, ip);
+  const int sflag = ring_phase_flag(a.nside, i);
+  int mtop = a.lmax;
+  while (mtop >= 0 && a.ring_i0[mtop] > i) --mtop;
+  for (int m = tid; m <= mtop; m += nt) {
+    double s = 0.0, c = 1.0;
+    if (sflag) {
+      long long r = (long long)m % (2LL * n);
+      sincospi((double)r / (double)n, &s, &c);
+    }
+    ph[m] = make_double2(c, s);
+  }
+  const int k_begin = blockIdx.y * a.maps_per_block;
+  const int k_end = min(a.kc, k_begin + a.maps_per_block);
+  const double2* chirp = a.chirp + rf.chirp_off;
+  const double2* bhat = a.bhat + rf.bhat_off;
+  const long long stride_m = (long long)a.nnorth * a.kc * 2;
+  for (int k = k_begin; k < k_end; ++k) {
+    __syncthreads();
+    build_spectrum(buf, ph, a.W + ((long long)i * a.kc + k) * 2, stride_m, n, mtop, equator);
+    __syncthreads();
+    // inverse DFT = conj(DFT(conj Z))
+    for (int j = tid; j < n; j += nt) buf[j] = cconj(buf[j]);
+    __syncthreads();
+    ring_dft(buf, rf, a.tw, a.logPmax, chirp, bhat);
+    double* xn = a.maps + (long long)k * a.map_stride + off_n;
+    double* xs = a.maps + (long long)k * a.map_stride + off_s;
+    for (int j = tid; j < n; j += nt) {
+      const double2 z = buf[j];   // conj applied: x_N = Re, x_S = -Im of the DFT output
+      xn[j] = z.x;
+      if (!equator) xs[j] = -z.y;
+    }
+  }
+}
+
+// ------------------------------------------------------------------ residual
+// Fourier-space residual of the Jacobi iterations (reference mat2fft_fast_iter,
+// src/fft_mapping.f90:142-190, read back by fft2mat_fast): for every kept m,
+//   F^R_m(i) = F^X_m(i) - n_i e^{-i m phi0} Y_i[m mod n_i],
+// where Y_i is the Hermitian spectrum synthesised from G (every m' = +-q mod n_i
+// lands in bin q).  X holds {S, D}; GR holds {G_N, G_S} on entry and {S_R, D_R}
+// on exit.  prefix = 0 ("old" method, t2alm_iter_old): Y sums all m'.  prefix = 1
+// ("new" method, t2alm_iter, sht_main.f90:171-264): the reference forms each
+// order's residual right after its own synthesis, so Y only holds m' <= m.
+// Thread per half-spectrum bin p in [0, n/2]: it owns every m that lands in p or
+// n - p, walks them in ascending order and needs no shared spectrum.
+struct ResArgs {
+  const double2* X;
+  double2* GR;
+  int kc, maps_per_block;
+  int nside, lmax, nnorth, ring_base, prefix;
+  const FshtRingFFT* rfs;
+  const int* ring_i0;
+};
+
+__global__ void __launch_bounds__(512) k_fourier_residual(ResArgs a) {
+  extern __shared__ double2 smem[];
+  const int i = a.ring_base + blockIdx.x;
+  const int n = a.rfs[i].n;
+  double2* phf = smem;   // lmax+1: exp(+i m phi0)
+  const int tid = threadIdx.x, nt = blockDim.x;
+  const bool equator = (i == a.nnorth - 1);
+  const int sflag = ring_phase_flag(a.nside, i);
+  int mtop = a.lmax;
+  while (mtop >= 0 && a.ring_i0[mtop] > i) --mtop;
+  for (int m = tid; m <= mtop; m += nt) {
+    double s = 0.0, c = 1.0;
+    if (sflag) {
+      long long r = (long long)m % (2LL * n);
+      sincospi((double)r / (double)n, &s, &c);
+    }
+    phf[m] = make_double2(c, s);
+  }
+  __syncthreads();
+  const long long stride_m = (long long)a.nnorth * a.kc * 2;
+  const int k_begin = blockIdx.y * a.maps_per_block;
+  const int k_end = min(a.kc, k_begin + a.maps_per_block);
+  const int half = n / 2;
+  const double dn = (double)n;
+  for (int k = k_begin; k < k_end; ++k) {
+    const long long base = ((long long)i * a.kc + k) * 2;
+    for (int p = tid; p <= half; p += nt) {
+      const int pn = (n - p) % n;     // the mirrored bin (p itself for p = 0, n/2)
+      // ascending merge of {p + t n} and {pn + t n}; when p == pn one list
+      int ma = p, mb = (pn == p) ? INT_MAX : pn;
+      double2 yN = make_double2(0.0, 0.0), yS = make_double2(0.0, 0.0);
+      // pass 0 (old method only): totals; pass 1: emit residuals (accumulating
+      // the prefix first when prefix = 1)
+      for (int pass = a.prefix ? 1 : 0; pass < 2; ++pass) {
+        int ua = ma, ub = mb;
+        while (true) {
+          const int m = min(ua, ub);
+          if (m > mtop) break;
+          const bool inA = (m == ua);
+          if (inA) ua += n; else ub += n;
+          const double2* g = a.GR + base + (long long)m * stride_m;
+          const double c = (m == 0) ? 0.5 : 1.0;
+          const double2 hN = cscale(cmul(phf[m], g[0]), c);
+          const double2 hS = equator ? make_double2(0.0, 0.0) : cscale(cmul(phf[m], g[1]), c);
+          const int q = m % n;
+          // this m adds to bin p: h if q == p, conj(h) if q == n - p (both when p == pn)
+          if (pass == 0 || a.prefix) {
+            if (q == p) { yN = cadd(yN, hN); yS = cadd(yS, hS); }
+            if (q == pn) { yN = cadd(yN, cconj(hN)); yS = cadd(yS, cconj(hS)); }
+          }
+          if (pass == 1) {
+            // Y[q] = Y[p] when q == p, conj(Y[p]) otherwise
+            const double2 vN = (q == p) ? yN : cconj(yN);
+            const double2 vS = (q == p) ? yS : cconj(yS);
+            const double2 e = cconj(phf[m]);
+            const double2 rN = cscale(cmul(e, vN), dn);
+            const double2* x = a.X + base + (long long)m * stride_m;
+            double2* o = a.GR + base + (long long)m * stride_m;
+            const double2 x0 = x[0], x1 = x[1];
+            if (equator) {
+              o[0] = csub(x0, rN);
+              o[1] = csub(x1, rN);
+            } else {
+              const double2 rS = cscale(cmul(e, vS), dn);
+              o[0] = csub(x0, cadd(rN, rS));
+              o[1] = csub(x1, csub(rN, rS));
+            }
+          }
+        }
+      }
+    }
+  }
+}
+
+// ------------------------------------------------------------------ ring skip
+// kept(i, m): max_{m <= l <= lcap} |lambda_lm(theta_i)| >= 1e-20, evaluated with the
+// exponent-rescaled recursion (values carried as v * 2^(600 e), e <= 0).
+__device__ bool ring_kept(double c, double s, double pref, int m, int lcap) {
+  int ex;
+  double mt = frexp(s, &ex);
+  double rm = 1.0, bm = mt;
+  long long re = 0, be = ex;
+  for (int k = m; k; k >>= 1) {
+    if (k & 1) { rm *= bm; re += be; int t; rm = frexp(rm, &t); re += t; }
+    if (k > 1) { bm *= bm; be *= 2; int t; bm = frexp(bm, &t); be += t; }
+  }
+  rm *= pref;
+  { int t; rm = frexp(rm, &t); re += t; }
+  int e = (re >= -300) ? 0 : (int)floor((double)(re + 300) / 600.0);
+  double cur = ldexp(rm, (int)(re - 600LL * e)), prev = 0.0;
+  if (e == 0 && fabs(cur) >= 1e-20) return true;
+  const double mm = (double)m * (double)m;
+  for (int l = m + 1; l <= lcap; ++l) {
+    const double dl = (double)l;
+    const double al = sqrt((4.0 * dl * dl - 1.0) / (dl * dl - mm));
+    const double bl = sqrt(((dl - 1.0) * (dl - 1.0) - mm) / ((2.0 * dl - 3.0) * (2.0 * dl - 1.0))) * al;
+    const double nx = al * c * cur - bl * prev;
+    prev = cur;
+    cur = nx;
+    if (e < 0 && fabs(cur) > 0x1p300) { cur *= 0x1p-600; prev *= 0x1p-600; ++e; }
+    if (e == 0 && fabs(cur) >= 1e-20) return true;
+  }
+  return false;
+}
+
+// i0(m) = first north ring kept for order m (the rule the reference's
+// SHT_ring_skip_table/<nside>.bin follows).  max_l |lambda_lm| grows toward the
+// equator, so a binary search over rings suffices; thread per m.  The host makes
+// the result non-decreasing in m.
+__global__ void k_ring_first_kept(const double* cth, const double* sth, const double* pref,
+                                  int nnorth, int lcap, int mmax, int* first) {
+  const int m = blockIdx.x * blockDim.x + threadIdx.x;
+  if (m > mmax) return;
+  int lo = 0, hi = nnorth - 1;     // the equator ring is always kept for m <= lcap
+  while (lo < hi) {
+    const int mid = (lo + hi) >> 1;
+    if (ring_kept(cth[mid], sth[mid], pref[m], m, lcap)) hi = mid;
+    else lo = mid + 1;
+  }
+  first[m] = lo;
+}
+
+int maps_per_block_for(int kc, int nrings_launched) {
+  // aim for >= ~8 blocks per SM over 152 SMs
+  long long target = 152LL * 8;
+  int g = (int)((long long)kc * nrings_launched / target);
+  if (g < 1) g = 1;
+  if (g > 16) g = 16;
+  return g;
+}
+
+}  // namespace
+
+// ================================================================== host side
+int fsht_fft_tables_init(fsht_plan* p) {
+  const int ns = p->nside, nn = p->nnorth;
+  std::vector<FshtRingFFT> rfs(nn);
+  long long chirp_total = 0, bhat_total = 0;
+  int Pmax = 2;
+  std::vector<int> blue_rings;
+  for (int i = 0; i < nn; ++i) {
+    FshtRingFFT r{};
+    r.n = ring_len(ns, i);
+    const bool pow2 = (r.n & (r.n - 1)) == 0;
+    r.bluestein = pow2 ? 0 : 1;
+    int P = 1, logP = 0;
+    const int need = pow2 ? r.n : 2 * r.n - 1;
+    while (P < need) { P <<= 1; ++logP; }
+    r.P = P;
+    r.logP = logP;
+    if (r.bluestein) {
+      r.chirp_off = chirp_total;
+      r.bhat_off = bhat_total;
+      chirp_total += r.n;
+      bhat_total += P;
+      blue_rings.push_back(i);
+    }
+    if (P > Pmax) Pmax = P;
+    rfs[i] = r;
+  }
+  int logPmax = 0;
+  while ((1 << logPmax) < Pmax) ++logPmax;
+  // The phase table (lmax+1) and the FFT buffer (Pmax) share the dynamic smem.
+  size_t smem = (size_t)(Pmax + p->lmax + 1) * sizeof(double2);
+  if (smem > 227 * 1024) {
+    fsht_set_error("ring FFT needs %zu bytes of shared memory (nside %d, lmax %d): unsupported",
+                   smem, ns, p->lmax);
+    return FSHT_EUNSUPPORTED;
+  }
+  p->Pmax = Pmax;
+  p->logPmax = logPmax;
+  p->fft_smem = smem;
+  FSHT_CUDA_TRY(cudaMalloc(&p->d_rfft, sizeof(FshtRingFFT) * nn));
+  FSHT_CUDA_TRY(cudaMemcpyAsync(p->d_rfft, rfs.data(), sizeof(FshtRingFFT) * nn,
+                                cudaMemcpyHostToDevice, p->stream));
+  FSHT_CUDA_TRY(cudaMalloc(&p->d_tw, sizeof(double2) * (Pmax / 2)));
+  k_twiddles<<<(Pmax / 2 + 255) / 256, 256, 0, p->stream>>>(p->d_tw, Pmax);
+  FSHT_LAUNCH_CHECK();
+  FSHT_CUDA_TRY(cudaMalloc(&p->d_chirp, sizeof(double2) * (chirp_total > 0 ? chirp_total : 1)));
+  FSHT_CUDA_TRY(cudaMalloc(&p->d_bhat, sizeof(double2) * (bhat_total > 0 ? bhat_total : 1)));
+  if (!blue_rings.empty()) {
+    int* d_rings = nullptr;
+    FSHT_CUDA_TRY(cudaMalloc(&d_rings, sizeof(int) * blue_rings.size()));
+    FSHT_CUDA_TRY(cudaMemcpyAsync(d_rings, blue_rings.data(), sizeof(int) * blue_rings.size(),
+                                  cudaMemcpyHostToDevice, p->stream));
+    const size_t sm = (size_t)Pmax * sizeof(double2);
+    FSHT_CUDA_TRY(cudaFuncSetAttribute(k_bluestein_tables,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    k_bluestein_tables<<<(unsigned)blue_rings.size(), 512, sm, p->stream>>>(
+        p->d_rfft, d_rings, p->d_chirp, p->d_bhat, p->d_tw, logPmax);
+    FSHT_LAUNCH_CHECK();
+    FSHT_CUDA_TRY(cudaStreamSynchronize(p->stream));
+    FSHT_CUDA_TRY(cudaFree(d_rings));
+  }
+  FSHT_CUDA_TRY(cudaFuncSetAttribute(k_ring_fft_fwd, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)p->fft_smem));
+  FSHT_CUDA_TRY(cudaFuncSetAttribute(k_ring_fft_inv, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)p->fft_smem));
+  FSHT_CUDA_TRY(cudaFuncSetAttribute(k_fourier_residual,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p->fft_smem));
+  return FSHT_OK;
+}
+
+int fsht_launch_ring_skip(fsht_plan* p, cudaStream_t s) {
+  const int lcap = (4 * p->nside > p->lmax) ? 4 * p->nside : p->lmax;
+  int* d_first = nullptr;
+  FSHT_CUDA_TRY(cudaMalloc(&d_first, sizeof(int) * (p->lmax + 1)));
+  k_ring_first_kept<<<(p->lmax + 1 + 63) / 64, 64, 0, s>>>(p->d_cth, p->d_sth, p->d_pref,
+                                                             p->nnorth, lcap, p->lmax, d_first);
+  FSHT_LAUNCH_CHECK();
+  FSHT_CUDA_TRY(cudaMemcpyAsync(p->h_ring_i0, d_first, sizeof(int) * (p->lmax + 1),
+                                cudaMemcpyDeviceToHost, s));
+  FSHT_CUDA_TRY(cudaStreamSynchronize(s));
+  FSHT_CUDA_TRY(cudaFree(d_first));
+  int run = 0;
+  for (int m = 0; m <= p->lmax; ++m) {
+    if (p->h_ring_i0[m] > run) run = p->h_ring_i0[m];
+    p->h_ring_i0[m] = run;
+  }
+  FSHT_CUDA_TRY(cudaMemcpyAsync(p->d_ring_i0, p->h_ring_i0, sizeof(int) * (p->lmax + 1),
+                                cudaMemcpyHostToDevice, s));
+  FSHT_CUDA_TRY(cudaStreamSynchronize(s));
+  return FSHT_OK;
+}
+
+int fsht_launch_ring_fft_fwd(fsht_plan* p, const double* maps, long long map_stride, int kc,
+                             double2* W, cudaStream_t s) {
+  FwdArgs a;
+  a.maps = maps;
+  a.map_stride = map_stride;
+  a.kc = kc;
+  a.nside = p->nside;
+  a.lmax = p->lmax;
+  a.nnorth = p->nnorth;
+  a.nring = p->nring;
+  a.ring_base = 0;
+  a.rfs = p->d_rfft;
+  a.tw = p->d_tw;
+  a.logPmax = p->logPmax;
+  a.chirp = p->d_chirp;
+  a.bhat = p->d_bhat;
+  a.ring_i0 = p->d_ring_i0;
+  a.W = W;
+  a.maps_per_block = maps_per_block_for(kc, p->nnorth);
+  dim3 grid(p->nnorth, (kc + a.maps_per_block - 1) / a.maps_per_block);
+  k_ring_fft_fwd<<<grid, 512, p->fft_smem, s>>>(a);
+  FSHT_LAUNCH_CHECK();
+  return FSHT_OK;
+}
+
+int fsht_launch_ring_fft_inv(fsht_plan* p, const double2* W, double* maps, long long map_stride,
+                             int kc, cudaStream_t s) {
+  InvArgs a;
+  a.W = W;
+  a.maps = maps;
+  a.map_stride = map_stride;
+  a.kc = kc;
+  a.nside = p->nside;
+  a.lmax = p->lmax;
+  a.nnorth = p->nnorth;
+  a.nring = p->nring;
+  a.ring_base = 0;
+  a.rfs = p->d_rfft;
+  a.tw = p->d_tw;
+  a.logPmax = p->logPmax;
+  a.chirp = p->d_chirp;
+  a.bhat = p->d_bhat;
+  a.ring_i0 = p->d_ring_i0;
+  a.maps_per_block = maps_per_block_for(kc, p->nnorth);
+  dim3 grid(p->nnorth, (kc + a.maps_per_block - 1) / a.maps_per_block);
+  k_ring_fft_inv<<<grid, 512, p->fft_smem, s>>>(a);
+  FSHT_LAUNCH_CHECK();
+  return FSHT_OK;
+}
+
+int fsht_launch_fourier_residual(fsht_plan* p, const double2* X, double2* GR, int kc,
+                                 int prefix, cudaStream_t s) {
+  ResArgs a;
+  a.X = X;
+  a.GR = GR;
+  a.kc = kc;
+  a.nside = p->nside;
+  a.lmax = p->lmax;
+  a.nnorth = p->nnorth;
+  a.ring_base = 0;
+  a.prefix = prefix;
+  a.rfs = p->d_rfft;
+  a.ring_i0 = p->d_ring_i0;
+  a.maps_per_block = maps_per_block_for(kc, p->nnorth);
+  dim3 grid(p->nnorth, (kc + a.maps_per_block - 1) / a.maps_per_block);
+  k_fourier_residual<<<grid, 512, p->fft_smem, s>>>(a);
+  FSHT_LAUNCH_CHECK();
+  return FSHT_OK;
+}

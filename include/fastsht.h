@@ -1,0 +1,137 @@
+/*
+ * fastsht_gb300 — C ABI of the batched HEALPix spherical-harmonic transform path
+ * for NVIDIA GB300 (sm_103a).
+ *
+ * Every entry point is `extern "C"`, takes plain pointers and sizes, returns an
+ * int status (FSHT_OK = 0, negative on error) and never throws.  The text of the
+ * last error of the calling thread is available from fsht_last_error().
+ *
+ * Array conventions (identical to the reference's Fortran-order NumPy arrays):
+ *   maps : float64, nmaps x npix, each map contiguous (reference: maps(npix, nsim)
+ *          in Fortran order), HEALPix RING ordering, npix = 12 nside^2.
+ *   alm  : float64, (lmax+1) x (lmax+1) x nmaps with the map index fastest
+ *          (reference: alm(nsim, 0:lmax, 0:lmax) in Fortran order), "square-real"
+ *          packing: Re a_lm at [m][l][k] (l >= m), Im a_lm at [lmax+1-m][l-m][k]
+ *          (m >= 1).  Slots not named by this packing do not exist: every one of
+ *          the (lmax+1)^2 slots is either a Re or an Im of some a_lm.
+ * Transform entry points take DEVICE pointers and run asynchronously on the
+ * plan's stream (fsht_plan_set_stream).  The *_host entry points take host
+ * pointers and return after the result is in host memory.
+ */
+#ifndef FASTSHT_GB300_H
+#define FASTSHT_GB300_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct fsht_plan fsht_plan;
+
+enum {
+  FSHT_OK = 0,
+  FSHT_EINVAL = -1,       /* bad argument (sizes, null pointers, nmaps > plan) */
+  FSHT_ENOMEM = -2,       /* device allocation failed                          */
+  FSHT_ECUDA = -3,        /* CUDA runtime error (message in fsht_last_error)   */
+  FSHT_ETIMEOUT = -4,     /* a bounded device-side wait expired                */
+  FSHT_EUNSUPPORTED = -5  /* size or mode outside what this build supports     */
+};
+
+enum { FSHT_PREC_FP64 = 0, FSHT_PREC_SPLIT = 1 };
+
+/* Plan flags: which workspace buffers to hold (reference nbuff, SHT.py:52-59). */
+enum { FSHT_FLAG_POL = 1, FSHT_FLAG_ITER = 2 };
+
+/* Plan creation: replaces the reference's SHT.__init__ -> sht_data_alloc +
+ * sht_set_data (SHT.py:17-62; src/sht_data_init.f90:2-269, 275-311).  Computes
+ * the ring geometry, ring-skip table, FFT tables and workspace on the device.
+ *   nside      power of two, 1..1024
+ *   lmax       0 <= lmax <= 4*nside
+ *   nmaps_max  largest nmaps a transform call on this plan will pass
+ *   flags      FSHT_FLAG_POL for spin-2 (Q/U) transforms, FSHT_FLAG_ITER for
+ *              niter > 0 (each doubles the workspace, like the reference's nbuff)
+ *   precision  FSHT_PREC_FP64 (plain)
+ *   workspace_limit_bytes  upper bound for the plan's phase-matrix workspace
+ *              (0 = default 16 GiB); maps are processed in chunks that fit.
+ *   stream     cudaStream_t (NULL = legacy default stream) */
+int fsht_plan_create(int nside, int lmax, int nmaps_max, int flags, int precision,
+                     size_t workspace_limit_bytes, void* stream, fsht_plan** plan);
+/* Releases a plan (reference: sht_data_free, src/sht_data_init.f90:319-372). */
+int fsht_plan_destroy(fsht_plan* plan);
+int fsht_plan_set_stream(fsht_plan* plan, void* stream);
+/* Device bytes the plan holds (tables + workspace) and maps per chunk. */
+int fsht_plan_info(const fsht_plan* plan, size_t* device_bytes, int* maps_per_chunk);
+/* First kept ring i0(m) for m = 0..lmax (reference SHT_ring_skip_table/<nside>.bin,
+ * read at SHT.py:31-32); out must hold lmax+1 ints (host memory). */
+int fsht_plan_ring_skip(const fsht_plan* plan, int* out);
+
+/* Temperature analysis.  niter = 0: reference t2alm (src/sht_main.f90:38-89).
+ * niter > 0, method 0: t2alm_iter_old (src/sht_main.f90:276-367);
+ * method 1: t2alm_iter (src/sht_main.f90:171-264). */
+int fsht_t2alm(fsht_plan* plan, const double* maps, double* alm, int nmaps,
+               int niter, int method);
+/* Temperature synthesis: reference alm2t (src/sht_main.f90:96-155). */
+int fsht_alm2t(fsht_plan* plan, const double* alm, double* maps, int nmaps);
+/* Spin-2 analysis.  niter = 0: QU2EB (src/sht_main.f90:383-436);
+ * niter > 0: qu2eb_iter_old (src/sht_main.f90:563-673). */
+int fsht_qu2eb(fsht_plan* plan, const double* Q, const double* U, double* almE,
+               double* almB, int nmaps, int niter);
+/* E only: QU2E (src/sht_main.f90:955-1005). */
+int fsht_qu2e(fsht_plan* plan, const double* Q, const double* U, double* almE, int nmaps);
+/* B only: QU2B (src/sht_main.f90:1016-1064). */
+int fsht_qu2b(fsht_plan* plan, const double* Q, const double* U, double* almB, int nmaps);
+/* Spin-2 synthesis: EB2QU (src/sht_main.f90:1079-1147). */
+int fsht_eb2qu(fsht_plan* plan, const double* almE, const double* almB, double* Q,
+               double* U, int nmaps);
+
+/* Square-real alm -> healpy layout (interleaved re,im per (l,m), index
+ * m(2 lmax+1-m)/2 + l, map index slowest: out[k][idx][2]).  Reference:
+ * convert_alm_healpy1 (src/convert_alm.f90:34-56) as used by
+ * SHT.convert_alm_healpy (SHT.py:204-210).  Device pointers, plan's stream. */
+int fsht_convert_alm_healpy(fsht_plan* plan, const double* alm, double* alm_hp, int nmaps);
+/* Inverse: convert_alm_healpy_inv1 (src/convert_alm.f90:87-107). */
+int fsht_convert_alm_healpy_inv(fsht_plan* plan, const double* alm_hp, double* alm, int nmaps);
+
+/* Per-kernel timing with CUDA events on the plan's stream (no host sync per
+ * launch).  Categories: FSHT_KCAT_*.  fsht_profile_read synchronises the stream,
+ * returns per-category launch counts and summed milliseconds, and clears them. */
+enum {
+  FSHT_KCAT_FFT_FWD = 0,
+  FSHT_KCAT_FFT_INV = 1,
+  FSHT_KCAT_ANALYSIS = 2,
+  FSHT_KCAT_SYNTHESIS = 3,
+  FSHT_KCAT_RESIDUAL = 4,
+  FSHT_KCAT_OTHER = 5,
+  FSHT_KCAT_COUNT = 8
+};
+int fsht_profile_enable(fsht_plan* plan, int on);
+int fsht_profile_read(fsht_plan* plan, int ncat, int* launches, double* total_ms);
+
+/* Measures this device's FP64 FMA throughput (TFLOP/s) with a DFMA loop kernel:
+ * the roofline denominator for the FP64 kernels. */
+int fsht_measure_fp64_peak(double* tflops);
+
+/* Runs one stage of the pipeline on device buffers (testing and profiling hook;
+ * no counterpart in the reference, whose stages are internal):
+ *   FSHT_STAGE_FFT_FWD   maps -> phase matrix {S, D}        (in: maps, out: W)
+ *   FSHT_STAGE_ANALYSIS  phase matrix -> alm (spin 0)       (in: W, out: alm)
+ *   FSHT_STAGE_SYNTHESIS alm -> phase matrix {G_N, G_S}     (in: alm, out: W)
+ *   FSHT_STAGE_FFT_INV   phase matrix -> maps               (in: W, out: maps)
+ * W is laid out [m][ring][map][2] complex (double2), ring < 2 nside, m <= lmax,
+ * for nmaps <= the plan's maps_per_chunk. */
+enum { FSHT_STAGE_FFT_FWD = 0, FSHT_STAGE_ANALYSIS = 1, FSHT_STAGE_SYNTHESIS = 2,
+       FSHT_STAGE_FFT_INV = 3 };
+int fsht_run_stage(fsht_plan* plan, int stage, const void* in, void* out, int nmaps);
+
+/* Blocks until the plan's stream is idle; returns FSHT_ECUDA on an async error. */
+int fsht_plan_sync(fsht_plan* plan);
+
+/* Copies the calling thread's last error message into buf (NUL-terminated);
+ * returns its full length. */
+int fsht_last_error(char* buf, size_t len);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* FASTSHT_GB300_H */

@@ -1,0 +1,61 @@
+"""The C-ABI library builds, loads and exports every entry point that
+include/fastsht.h declares; argument validation works without a GPU."""
+import ctypes as C
+import re
+from pathlib import Path
+
+import pytest
+
+from fastsht_gb300 import _lib, build
+
+HEADER = Path(__file__).resolve().parent.parent / "include" / "fastsht.h"
+
+
+def declared_functions():
+    txt = HEADER.read_text()
+    return sorted(set(re.findall(r"^\s*int\s+(fsht_\w+)\s*\(", txt, flags=re.M)))
+
+
+@pytest.fixture(scope="module")
+def lib():
+    build.build()
+    return _lib.load()
+
+
+def test_header_declares_entry_points():
+    names = declared_functions()
+    for want in ("fsht_plan_create", "fsht_plan_destroy", "fsht_t2alm", "fsht_alm2t",
+                 "fsht_qu2eb", "fsht_eb2qu", "fsht_last_error"):
+        assert want in names
+
+
+def test_library_exports_every_declared_symbol(lib):
+    missing = [n for n in declared_functions() if not hasattr(lib, n)]
+    assert not missing, missing
+
+
+def test_python_binding_covers_header(lib):
+    assert set(declared_functions()) <= set(_lib.SIGNATURES)
+
+
+@pytest.mark.parametrize("args,code", [
+    ((3, 8, 1, 0, 0), _lib.FSHT_EINVAL),          # nside not a power of two
+    ((0, 8, 1, 0, 0), _lib.FSHT_EINVAL),
+    ((8, 33, 1, 0, 0), _lib.FSHT_EINVAL),         # lmax > 4 nside
+    ((8, -1, 1, 0, 0), _lib.FSHT_EINVAL),
+    ((8, 16, 0, 0, 0), _lib.FSHT_EINVAL),         # nmaps_max < 1
+    ((2048, 100, 1, 0, 0), _lib.FSHT_EUNSUPPORTED),
+    ((8, 16, 1, 0, 7), _lib.FSHT_EUNSUPPORTED),   # unknown precision
+])
+def test_plan_create_rejects_bad_arguments(lib, args, code):
+    plan = C.c_void_p()
+    rc = lib.fsht_plan_create(*args, 0, None, C.byref(plan))
+    assert rc == code
+    assert plan.value is None
+    assert len(_lib.last_error()) > 0
+
+
+def test_null_plan_is_an_error(lib):
+    rc = lib.fsht_t2alm(None, None, None, 1, 0, 0)
+    assert rc == _lib.FSHT_EINVAL
+    assert "plan" in _lib.last_error()
