@@ -100,6 +100,17 @@ void fsht_set_error(const char* fmt, ...);
   } while (0)
 
 // ---------------------------------------------------------------- internal API
+struct FshtFftLayout {
+  int Pmax, logPmax, nblue;
+  long long chirp_total, bhat_total;
+  size_t smem;
+};
+// Host-side FFT table layout for nside/lmax; fills rfs[2 nside] and blue_rings
+// (indices of Bluestein rings) when non-null.
+int fsht_fft_layout(int nside, int lmax, FshtFftLayout* lay, FshtRingFFT* rfs, int* blue_rings);
+// Fills the twiddle and Bluestein tables at p->d_tw / d_chirp / d_bhat (device
+// ring descriptors at p->d_rfft must already be in place).  Allocates nothing.
+int fsht_fft_tables_fill(fsht_plan* p, const int* d_blue_rings, int nblue, cudaStream_t s);
 int fsht_fft_tables_init(fsht_plan* p);
 int fsht_launch_ring_fft_fwd(fsht_plan* p, const double* maps, long long map_stride,
                              int kc, double2* W, cudaStream_t s);

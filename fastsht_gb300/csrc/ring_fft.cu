@@ -435,15 +435,13 @@ int maps_per_block_for(int kc, int nrings_launched) {
 }  // namespace
 
 // ================================================================== host side
-int fsht_fft_tables_init(fsht_plan* p) {
-  const int ns = p->nside, nn = p->nnorth;
-  std::vector<FshtRingFFT> rfs(nn);
+int fsht_fft_layout(int nside, int lmax, FshtFftLayout* lay, FshtRingFFT* rfs, int* blue_rings) {
+  const int nn = 2 * nside;
   long long chirp_total = 0, bhat_total = 0;
-  int Pmax = 2;
-  std::vector<int> blue_rings;
+  int Pmax = 2, nblue = 0;
   for (int i = 0; i < nn; ++i) {
     FshtRingFFT r{};
-    r.n = ring_len(ns, i);
+    r.n = ring_len(nside, i);
     const bool pow2 = (r.n & (r.n - 1)) == 0;
     r.bluestein = pow2 ? 0 : 1;
     int P = 1, logP = 0;
@@ -456,52 +454,69 @@ int fsht_fft_tables_init(fsht_plan* p) {
       r.bhat_off = bhat_total;
       chirp_total += r.n;
       bhat_total += P;
-      blue_rings.push_back(i);
+      if (blue_rings) blue_rings[nblue] = i;
+      ++nblue;
     }
     if (P > Pmax) Pmax = P;
-    rfs[i] = r;
+    if (rfs) rfs[i] = r;
   }
   int logPmax = 0;
   while ((1 << logPmax) < Pmax) ++logPmax;
+  lay->Pmax = Pmax;
+  lay->logPmax = logPmax;
+  lay->chirp_total = chirp_total;
+  lay->bhat_total = bhat_total;
+  lay->nblue = nblue;
   // The phase table (lmax+1) and the FFT buffer (Pmax) share the dynamic smem.
-  size_t smem = (size_t)(Pmax + p->lmax + 1) * sizeof(double2);
-  if (smem > 227 * 1024) {
+  lay->smem = (size_t)(Pmax + lmax + 1) * sizeof(double2);
+  if (lay->smem > 227 * 1024) {
     fsht_set_error("ring FFT needs %zu bytes of shared memory (nside %d, lmax %d): unsupported",
-                   smem, ns, p->lmax);
+                   lay->smem, nside, lmax);
     return FSHT_EUNSUPPORTED;
   }
-  p->Pmax = Pmax;
-  p->logPmax = logPmax;
-  p->fft_smem = smem;
+  return FSHT_OK;
+}
+
+int fsht_fft_tables_fill(fsht_plan* p, const int* d_blue_rings, int nblue, cudaStream_t s) {
+  k_twiddles<<<(p->Pmax / 2 + 255) / 256, 256, 0, s>>>(p->d_tw, p->Pmax);
+  FSHT_LAUNCH_CHECK();
+  if (nblue > 0) {
+    const size_t sm = (size_t)p->Pmax * sizeof(double2);
+    FSHT_CUDA_TRY(cudaFuncSetAttribute(k_bluestein_tables,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    k_bluestein_tables<<<(unsigned)nblue, 512, sm, s>>>(p->d_rfft, d_blue_rings, p->d_chirp,
+                                                         p->d_bhat, p->d_tw, p->logPmax);
+    FSHT_LAUNCH_CHECK();
+  }
+  return FSHT_OK;
+}
+
+int fsht_fft_tables_init(fsht_plan* p) {
+  const int nn = p->nnorth;
+  std::vector<FshtRingFFT> rfs(nn);
+  std::vector<int> blue_rings(nn);
+  FshtFftLayout lay;
+  int rc = fsht_fft_layout(p->nside, p->lmax, &lay, rfs.data(), blue_rings.data());
+  if (rc) return rc;
+  p->Pmax = lay.Pmax;
+  p->logPmax = lay.logPmax;
+  p->fft_smem = lay.smem;
   FSHT_CUDA_TRY(cudaMalloc(&p->d_rfft, sizeof(FshtRingFFT) * nn));
   FSHT_CUDA_TRY(cudaMemcpyAsync(p->d_rfft, rfs.data(), sizeof(FshtRingFFT) * nn,
                                 cudaMemcpyHostToDevice, p->stream));
-  FSHT_CUDA_TRY(cudaMalloc(&p->d_tw, sizeof(double2) * (Pmax / 2)));
-  k_twiddles<<<(Pmax / 2 + 255) / 256, 256, 0, p->stream>>>(p->d_tw, Pmax);
-  FSHT_LAUNCH_CHECK();
-  FSHT_CUDA_TRY(cudaMalloc(&p->d_chirp, sizeof(double2) * (chirp_total > 0 ? chirp_total : 1)));
-  FSHT_CUDA_TRY(cudaMalloc(&p->d_bhat, sizeof(double2) * (bhat_total > 0 ? bhat_total : 1)));
-  if (!blue_rings.empty()) {
-    int* d_rings = nullptr;
-    FSHT_CUDA_TRY(cudaMalloc(&d_rings, sizeof(int) * blue_rings.size()));
-    FSHT_CUDA_TRY(cudaMemcpyAsync(d_rings, blue_rings.data(), sizeof(int) * blue_rings.size(),
+  FSHT_CUDA_TRY(cudaMalloc(&p->d_tw, sizeof(double2) * (lay.Pmax / 2)));
+  FSHT_CUDA_TRY(cudaMalloc(&p->d_chirp, sizeof(double2) * (lay.chirp_total > 0 ? lay.chirp_total : 1)));
+  FSHT_CUDA_TRY(cudaMalloc(&p->d_bhat, sizeof(double2) * (lay.bhat_total > 0 ? lay.bhat_total : 1)));
+  int* d_rings = nullptr;
+  if (lay.nblue > 0) {
+    FSHT_CUDA_TRY(cudaMalloc(&d_rings, sizeof(int) * lay.nblue));
+    FSHT_CUDA_TRY(cudaMemcpyAsync(d_rings, blue_rings.data(), sizeof(int) * lay.nblue,
                                   cudaMemcpyHostToDevice, p->stream));
-    const size_t sm = (size_t)Pmax * sizeof(double2);
-    FSHT_CUDA_TRY(cudaFuncSetAttribute(k_bluestein_tables,
-                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-    k_bluestein_tables<<<(unsigned)blue_rings.size(), 512, sm, p->stream>>>(
-        p->d_rfft, d_rings, p->d_chirp, p->d_bhat, p->d_tw, logPmax);
-    FSHT_LAUNCH_CHECK();
-    FSHT_CUDA_TRY(cudaStreamSynchronize(p->stream));
-    FSHT_CUDA_TRY(cudaFree(d_rings));
   }
-  FSHT_CUDA_TRY(cudaFuncSetAttribute(k_ring_fft_fwd, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     (int)p->fft_smem));
-  FSHT_CUDA_TRY(cudaFuncSetAttribute(k_ring_fft_inv, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     (int)p->fft_smem));
-  FSHT_CUDA_TRY(cudaFuncSetAttribute(k_fourier_residual,
-                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p->fft_smem));
-  return FSHT_OK;
+  rc = fsht_fft_tables_fill(p, d_rings, lay.nblue, p->stream);
+  FSHT_CUDA_TRY(cudaStreamSynchronize(p->stream));
+  if (d_rings) FSHT_CUDA_TRY(cudaFree(d_rings));
+  return rc;
 }
 
 int fsht_launch_ring_skip(fsht_plan* p, cudaStream_t s) {
@@ -546,6 +561,8 @@ int fsht_launch_ring_fft_fwd(fsht_plan* p, const double* maps, long long map_str
   a.W = W;
   a.maps_per_block = maps_per_block_for(kc, p->nnorth);
   dim3 grid(p->nnorth, (kc + a.maps_per_block - 1) / a.maps_per_block);
+  FSHT_CUDA_TRY(cudaFuncSetAttribute(k_ring_fft_fwd, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)p->fft_smem));
   k_ring_fft_fwd<<<grid, 512, p->fft_smem, s>>>(a);
   FSHT_LAUNCH_CHECK();
   return FSHT_OK;
@@ -571,6 +588,8 @@ int fsht_launch_ring_fft_inv(fsht_plan* p, const double2* W, double* maps, long 
   a.ring_i0 = p->d_ring_i0;
   a.maps_per_block = maps_per_block_for(kc, p->nnorth);
   dim3 grid(p->nnorth, (kc + a.maps_per_block - 1) / a.maps_per_block);
+  FSHT_CUDA_TRY(cudaFuncSetAttribute(k_ring_fft_inv, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)p->fft_smem));
   k_ring_fft_inv<<<grid, 512, p->fft_smem, s>>>(a);
   FSHT_LAUNCH_CHECK();
   return FSHT_OK;
@@ -591,6 +610,8 @@ int fsht_launch_fourier_residual(fsht_plan* p, const double2* X, double2* GR, in
   a.ring_i0 = p->d_ring_i0;
   a.maps_per_block = maps_per_block_for(kc, p->nnorth);
   dim3 grid(p->nnorth, (kc + a.maps_per_block - 1) / a.maps_per_block);
+  FSHT_CUDA_TRY(cudaFuncSetAttribute(k_fourier_residual,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p->fft_smem));
   k_fourier_residual<<<grid, 512, p->fft_smem, s>>>(a);
   FSHT_LAUNCH_CHECK();
   return FSHT_OK;

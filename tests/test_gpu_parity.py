@@ -208,3 +208,14 @@ def test_linearity_at_c3_size():
     a2 = sht.t2alm(2.5 * m)
     assert rel_alm_err(a2, 2.5 * a1) <= 1e-13
     assert rel_alm_err(a1, alm) < 1e-2
+
+
+def test_plans_of_different_sizes_coexist():
+    """A later, smaller plan must not break an earlier plan's kernel launches."""
+    big = SHT(64, 191, 2)
+    maps = maps_normal(64, 2, 9)
+    a1 = big.t2alm(maps)
+    small = SHT(2, 5, 1)
+    small.t2alm(maps_normal(2, 1, 1))
+    assert np.array_equal(big.t2alm(maps), a1)
+    assert big.alm2t(a1).shape == (12 * 64 * 64, 2)
