@@ -73,6 +73,23 @@ int fsht_t2alm(fsht_plan* plan, const double* maps, double* alm, int nmaps,
                int niter, int method);
 /* Temperature synthesis: reference alm2t (src/sht_main.f90:96-155). */
 int fsht_alm2t(fsht_plan* plan, const double* alm, double* maps, int nmaps);
+/* Temperature analysis that allocates no device memory and needs no plan
+ * (niter = 0, plain FP64, same results as fsht_t2alm within 1e-11 relative).
+ * No counterpart in the reference.  It is for callers that cannot call
+ * cudaMalloc where they run the transform: a host application that reserved all
+ * device memory for its own pool and gives plug-ins buffers but no right to
+ * allocate, or a latency-critical loop where an allocation would synchronise the
+ * device.  Scratch comes from one fixed 32 MiB array of device memory inside the
+ * library (every GPU that loads the library holds it until exit), which covers
+ * nside <= 256 at any lmax <= 4 nside; larger sizes return FSHT_EUNSUPPORTED.
+ * maps / alm are device pointers (layouts as above); stream is a cudaStream_t.
+ * The first call on a device looks up the scratch address with that device
+ * current: make it before any stream capture.  Calls share the scratch, so calls
+ * that overlap on the GPU (other streams or threads) race; calls on one stream
+ * are ordered. */
+int fsht_t2alm_noalloc(int nside, int lmax, const double* maps, double* alm, int nmaps,
+                       void* stream);
+
 /* Spin-2 analysis.  niter = 0: QU2EB (src/sht_main.f90:383-436);
  * niter > 0: qu2eb_iter_old (src/sht_main.f90:563-673). */
 int fsht_qu2eb(fsht_plan* plan, const double* Q, const double* U, double* almE,
