@@ -5,7 +5,10 @@ Workload (one GPU): map2alm (t2alm) of a batch of 500 temperature maps at
 nside 1024 / lmax 2047, maps resident in HBM (50 GB, far above the 129 MB L2, so
 no flush is needed between steps).  One step = one t2alm of the whole batch =
 500 map.SHT.  Inputs: Gaussian alm with C_l ~ l^-2 (seed 2, a00 = 0) synthesised
-to maps on the device by alm2t.
+to maps on the device by alm2t.  The headline is the split-precision form
+(--precision split, the default); the plain FP64 path runs on the same maps and
+its throughput, the split form's alm error against it and the round-trip map
+residuals go in "fp64_plain".
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
@@ -65,6 +68,11 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--e2e-maps", type=int, default=None)
+    ap.add_argument("--precision", choices=["split", "fp64"], default="split",
+                    help="split: tcgen05 BF16-digit contraction (the precision form); "
+                         "fp64: the plain method")
+    ap.add_argument("--no-fp64", action="store_true",
+                    help="skip the plain-FP64 comparison run of the split form")
     a = ap.parse_args()
     if a.lmax is None:
         a.lmax = 2 * a.nside - 1
@@ -209,16 +217,72 @@ def reference_arm(args, rank, world):
 
 
 def workload_config(args):
+    method = ("split-precision form (BF16 digit UMMAs on tcgen05, FP64 recursion and FFT)"
+              if getattr(args, "precision", "fp64") == "split" else "plain FP64 method")
     return {"workload": (f"t2alm (map2alm) of {args.nmaps} T maps per GPU, nside {args.nside}, "
-                         f"lmax {args.lmax}, plain FP64 method"),
+                         f"lmax {args.lmax}, {method}"),
             "nside": args.nside, "lmax": args.lmax, "nmaps_per_gpu": args.nmaps,
-            "method": "fp64", "niter": 0,
+            "method": getattr(args, "precision", "fp64"), "niter": 0,
             "inputs": "Gaussian alm, C_l ~ l^-2 (seed 2), synthesised to maps on the device",
             "l2": "inputs larger than L2 (maps resident in HBM), no flush",
             "parallelism": f"replicas x{args.gpus}"}
 
 
 # ---------------------------------------------------------------- our arm
+def timed_steps(lib, sht, maps, steps, warmup, world, dist, dev, local, sample_clocks=True):
+    """W untimed + K timed t2alm steps on the plan's stream; per-kernel CUDA-event
+    times from the library's profiler over the timed region."""
+    import ctypes as C
+    import torch
+    from fastsht_gb300 import _lib
+    out = None
+    for _ in range(warmup):
+        out = sht.t2alm(maps)
+    torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+    lib.fsht_profile_enable(sht._plan, 1)
+    _lib.call("fsht_profile_read", sht._plan, 0, None, None)     # clear
+    clocks = ClockSampler(local) if sample_clocks else None
+    if clocks:
+        clocks.start()
+    torch.cuda.synchronize()
+    s = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(s)
+    for _ in range(steps):
+        out = sht.t2alm(maps)
+    e1.record(s)
+    torch.cuda.synchronize()
+    clk = clocks.stop() if clocks else None
+    ms = e0.elapsed_time(e1)
+    counts = (C.c_int * _lib.KCAT_COUNT)()
+    kms = (C.c_double * _lib.KCAT_COUNT)()
+    _lib.call("fsht_profile_read", sht._plan, _lib.KCAT_COUNT, counts, kms)
+    lib.fsht_profile_enable(sht._plan, 0)
+    if world > 1:
+        t = torch.tensor([ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+        dist.barrier()
+    per_kernel = {}
+    for i, name in enumerate(_lib.KCAT_NAMES):
+        if counts[i]:
+            per_kernel[name] = {"launches": counts[i], "ms_total": round(kms[i], 3),
+                                "share": round(kms[i] / ms, 4) if ms else None}
+    launches = int(sum(counts[i] for i in range(_lib.KCAT_COUNT)))
+    return ms, out, per_kernel, [kms[i] for i in range(_lib.KCAT_COUNT)], launches, clk
+
+
+def rel_err_per_map(a, ref):
+    """max over maps of max_{l,m}|a - ref| / max|ref| (device tensors (nmaps, L, L))."""
+    import torch
+    n = ref.shape[0]
+    d = (a - ref).abs().reshape(n, -1).amax(dim=1)
+    s = ref.abs().reshape(n, -1).amax(dim=1)
+    return float((d / s).max().item())
+
+
 def ours(args, rank, world, local):
     import ctypes as C
     import torch
@@ -240,90 +304,118 @@ def ours(args, rank, world, local):
     if pk.exists():
         peaks = json.loads(pk.read_text())
 
-    sht = SHT(nside, lmax, nmaps, device=local)
+    sht64 = SHT(nside, lmax, nmaps, device=local)
     alm_true = device_alm(nside, lmax, nmaps, 2 + rank, dev)
-    maps = sht.alm2t(alm_true.permute(2, 1, 0))        # (npix, nmaps) Fortran view
+    maps = sht64.alm2t(alm_true.permute(2, 1, 0))        # (npix, nmaps) Fortran view
     del alm_true
     torch.cuda.synchronize()
+    sht = sht64 if args.precision == "fp64" else SHT(nside, lmax, nmaps, device=local,
+                                                      precision="split")
 
-    def step():
-        return sht.t2alm(maps)
-
-    for _ in range(args.warmup):
-        out = step()
-    torch.cuda.synchronize()
-    if world > 1:
-        dist.barrier()
-    lib.fsht_profile_enable(sht._plan, 1)
-    _lib.call("fsht_profile_read", sht._plan, 0, None, None)     # clear
-    clocks = ClockSampler(local)
-    clocks.start()
-    torch.cuda.synchronize()
-    s = torch.cuda.current_stream()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record(s)
-    for _ in range(args.steps):
-        out = step()
-    e1.record(s)
-    torch.cuda.synchronize()
-    clk = clocks.stop()
-    ms = e0.elapsed_time(e1)
-    counts = (C.c_int * _lib.KCAT_COUNT)()
-    kms = (C.c_double * _lib.KCAT_COUNT)()
-    _lib.call("fsht_profile_read", sht._plan, _lib.KCAT_COUNT, counts, kms)
-    lib.fsht_profile_enable(sht._plan, 0)
-    if world > 1:
-        t = torch.tensor([ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-        dist.barrier()
+    ms, out, per_kernel, kms, launches, clk = timed_steps(lib, sht, maps, args.steps,
+                                                          args.warmup, world, dist, dev, local)
     ms_per_step = ms / args.steps
     value = world * nmaps * args.steps / (ms / 1000.0)
-
-    per_kernel = {}
-    for i, name in enumerate(_lib.KCAT_NAMES):
-        if counts[i]:
-            per_kernel[name] = {"launches": counts[i], "ms_total": round(kms[i], 3),
-                                "share": round(kms[i] / ms, 4) if ms else None}
-    launches = int(sum(counts[i] for i in range(_lib.KCAT_COUNT)))
-    fl = flop_per_map(nside, lmax) * nmaps * args.steps
-    ana_ms = kms[2]
-    achieved = fl / (ana_ms / 1000.0) / 1e12 if ana_ms > 0 else None
-    traffic = None
-    tf = ROOT / "profiles" / "traffic.json"
     kchunk = sht.plan_info()["maps_per_chunk"]
-    if tf.exists():
-        tr = json.loads(tf.read_text()).get("legendre_analysis_fp64")
-        if tr and tr.get("bytes_per_map"):
-            traffic = tr["bytes_per_map"] * kchunk
-    roof = {"bound": "fp64", "kernel": "k_analysis_fp64<0> (legendre_analysis)",
-            "achieved": achieved, "peak": peak64.value, "unit": "TFLOP/s",
-            "frac": (achieved / peak64.value) if achieved else None,
-            "peak_source": ("DFMA loop measured by bench.py on this GPU (fsht_measure_fp64_peak); "
-                            "MEASURED_PEAKS.json holds HBM and BF16 figures only"),
-            "algorithmic_flop_per_launch": flop_per_map(nside, lmax) * kchunk,
-            "traffic": traffic}
-    fft_ms = kms[0]
+    fl_step = flop_per_map(nside, lmax) * nmaps
+    # dominant kernel of the step and its roofline
+    names = _lib.KCAT_NAMES
+    top = max(range(len(names)), key=lambda i: kms[i])
+    fft_ms, ana_ms = kms[0], kms[2]
     fft_bytes = 16.0 * npix * nmaps * args.steps
     roof_fft = {"bound": "hbm", "kernel": "k_ring_fft_fwd", "achieved":
                 fft_bytes / (fft_ms / 1000.0) / 1e9 if fft_ms > 0 else None,
                 "peak": peaks.get("hbm_gbs", 6800.0), "unit": "GB/s",
-                "peak_source": "MEASURED_PEAKS.json hbm_gbs" if "hbm_gbs" in peaks else "fallback"}
+                "peak_source": ("MEASURED_PEAKS.json hbm_gbs (measured)" if "hbm_gbs" in peaks
+                                else "fallback 6800 GB/s"),
+                "traffic": None,
+                "note": ("the FP64 ring FFT is FP64-pipe bound on GB300 (83 % of the FP64 pipe "
+                         "in ncu), so its HBM fraction is small")}
     if roof_fft["achieved"]:
         roof_fft["frac"] = roof_fft["achieved"] / roof_fft["peak"]
+    ana_tf = fl_step * args.steps / (ana_ms / 1000.0) / 1e12 if ana_ms > 0 else None
+    traffic = None
+    tf = ROOT / "profiles" / "traffic.json"
+    if tf.exists():
+        tr = json.loads(tf.read_text()).get(
+            "legendre_analysis_split" if args.precision == "split" else "legendre_analysis_fp64")
+        if tr and tr.get("bytes_per_map"):
+            traffic = tr["bytes_per_map"] * kchunk
+    if args.precision == "split":
+        bf = peaks.get("bf16_tflops", 1900.0)
+        roof_ana = {"bound": "tensor", "kernel": "k_analysis_split (tcgen05 BF16 digit UMMAs)",
+                    "achieved": ana_tf, "peak": bf, "unit": "TFLOP/s",
+                    "frac": ana_tf / bf if ana_tf else None,
+                    "peak_source": ("MEASURED_PEAKS.json bf16_tflops (measured)"
+                                    if "bf16_tflops" in peaks else "fallback 1900 TFLOP/s"),
+                    "algorithmic_flop_per_launch": flop_per_map(nside, lmax) * kchunk,
+                    "executed_tensor_flop_per_launch": 10 * flop_per_map(nside, lmax) * kchunk,
+                    "traffic": traffic,
+                    "note": ("achieved counts algorithmic FLOP (4 nside (lmax+1)(lmax+2) per map); "
+                             "the kernel executes 10 BF16 digit products per algorithmic FMA")}
+    else:
+        roof_ana = {"bound": "fp64", "kernel": "k_analysis_fp64<0>", "achieved": ana_tf,
+                    "peak": peak64.value, "unit": "TFLOP/s",
+                    "frac": ana_tf / peak64.value if ana_tf else None,
+                    "peak_source": ("DFMA loop measured by bench.py on this GPU "
+                                    "(fsht_measure_fp64_peak); MEASURED_PEAKS.json holds HBM "
+                                    "and BF16 figures only"),
+                    "algorithmic_flop_per_launch": flop_per_map(nside, lmax) * kchunk,
+                    "traffic": traffic}
+    roof = roof_fft if names[top] == "ring_fft_fwd" else roof_ana
+    roof = dict(roof, dominant_kernel_share=per_kernel.get(names[top], {}).get("share"))
 
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step,
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64" if args.precision == "fp64" else "bf16x4-split of f64 (FP32 accum)",
             "data": "synthetic", "config": workload_config(args), "clocks": clk,
             "gpu_launches": launches, "per_kernel": per_kernel, "roofline": roof,
-            "roofline_fft": roof_fft, "fp64_peak_tflops": peak64.value}
+            "roofline_fft": roof_fft, "roofline_contraction": roof_ana,
+            "fp64_peak_tflops": peak64.value}
 
+    # -------- the plain FP64 path on the same maps (precision reference + speed ratio)
+    if args.precision == "split" and not args.no_fp64:
+        ms64, out64, pk64, kms64, _, _ = timed_steps(lib, sht64, maps, 1, 1, world, dist, dev,
+                                                     local, sample_clocks=False)
+        v64 = world * nmaps / (ms64 / 1000.0)
+        sd = float(maps.std().item())
+
+        def maxabs_minus(rt, ref=None, chunk=50):
+            # max |rt - ref| over (npix, nmaps) Fortran views, a few maps at a time
+            best = 0.0
+            for c0 in range(0, nmaps, chunk):
+                d = rt[:, c0:c0 + chunk] if ref is None else rt[:, c0:c0 + chunk] - ref[:, c0:c0 + chunk]
+                best = max(best, float(d.abs().max().item()))
+            return best
+
+        rt = sht64.alm2t(out)
+        res_split = maxabs_minus(rt, maps) / sd
+        del rt
+        rt = sht64.alm2t(out64)
+        res_64 = maxabs_minus(rt, maps) / sd
+        del rt
+        rt = sht64.alm2t(out - out64)          # linearity: the precision-induced part
+        res_diff = maxabs_minus(rt) / sd
+        del rt
+        line["fp64_plain"] = {
+            "value": v64, "unit": UNIT, "ms_per_step": ms64, "per_kernel": pk64,
+            "split_speedup": value / v64,
+            "max_rel_alm_err_split_vs_fp64": rel_err_per_map(out, out64),
+            "roundtrip_map_residual_split": res_split,
+            "roundtrip_map_residual_fp64": res_64,
+            "roundtrip_split_vs_fp64": res_diff,
+            "metric_note": ("alm error = max over maps of max_lm|a - a_fp64| / max_lm|a_fp64|; "
+                            "map residuals = max|T' - T| / std(T) (the reference's map metric); "
+                            "the round-trip residual of both forms is the niter = 0 quadrature "
+                            "error, the split-vs-fp64 term is the precision-induced part")}
+        del out64
+        torch.cuda.empty_cache()
     # -------- e2e through the public API with host (pinned) buffers
     if not args.no_e2e:
         ke = args.e2e_maps or nmaps
-        line["e2e"] = e2e(sht if ke == nmaps else SHT(nside, lmax, ke, device=local),
-                          maps, ke, args, world)
+        sh = sht if ke == nmaps else SHT(nside, lmax, ke, device=local, precision=args.precision)
+        line["e2e"] = e2e(sh, maps, ke, args, world)
     # -------- CPU baseline and parity sample (rank 0, N = 1)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         k = min(args.cpu_maps, nmaps)
@@ -335,7 +427,8 @@ def ours(args, rank, world, local):
         d = np.abs(got - alm_ref).reshape(k, -1).max(axis=1)
         sc = np.abs(alm_ref).reshape(k, -1).max(axis=1)
         line["parity"] = {"max_rel_alm_err_vs_oracle": float((d / sc).max()),
-                          "maps_checked": k, "tolerance": 1e-11}
+                          "maps_checked": k,
+                          "tolerance": 1e-7 if args.precision == "split" else 1e-11}
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:

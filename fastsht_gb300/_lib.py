@@ -22,7 +22,7 @@ FSHT_PREC_SPLIT = 1
 FSHT_FLAG_POL = 1
 FSHT_FLAG_ITER = 2
 KCAT_NAMES = ["ring_fft_fwd", "ring_fft_inv", "legendre_analysis", "legendre_synthesis",
-              "fourier_residual", "other"]
+              "fourier_residual", "split_slice", "other"]
 KCAT_COUNT = 8
 
 _vp = C.c_void_p

@@ -72,6 +72,11 @@ struct fsht_plan {
   int nbuf;
   size_t fft_smem;                 // dynamic smem of the ring FFT kernels
   struct FshtProfile* prof;        // non-null while per-kernel timing is on
+  int* d_err;                      // device error word (bounded waits that expired)
+  // split-precision form: sliced phase tiles and their column exponents
+  unsigned char* d_ws;
+  int* d_eb;
+  size_t ws_bytes;
 };
 
 // ---------------------------------------------------------------- status codes
@@ -125,6 +130,17 @@ int fsht_launch_analysis_fp64(fsht_plan* p, int spin, const double2* WQ,
                               const double2* WU, double* almE, double* almB,
                               int nmaps_total, int k0, int kc, int accumulate,
                               int which, cudaStream_t s);
+size_t fsht_split_ws_bytes(int lmax, int nnorth, int kc);
+size_t fsht_split_eb_bytes(int lmax, int kc);
+// Split-precision (BF16 digits on tcgen05) spin-0 analysis of one chunk: prepare
+// cuts the {S, D} phase matrix W into digit tiles WS and column exponents EB (and
+// clears alm's chunk columns when K-chunks will add into it); analysis runs the UMMA
+// contraction into alm.
+int fsht_launch_split_prepare(fsht_plan* p, const double2* W, unsigned char* WS, int* EB,
+                              double* alm, int nmaps_total, int k0, int kc, int accumulate,
+                              cudaStream_t s);
+int fsht_launch_analysis_split(fsht_plan* p, const unsigned char* WS, const int* EB, double* alm,
+                               int nmaps_total, int k0, int kc, int accumulate, cudaStream_t s);
 int fsht_launch_synthesis_fp64(fsht_plan* p, int spin, const double* almE,
                                const double* almB, double2* WQ, double2* WU,
                                int nmaps_total, int k0, int kc, cudaStream_t s);

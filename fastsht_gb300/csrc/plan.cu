@@ -18,6 +18,7 @@
 namespace {
 thread_local std::string g_last_error;
 constexpr size_t kDefaultWorkspace = 16ull << 30;
+constexpr size_t kDefaultWorkspaceSplit = 40ull << 30;   // 128-map groups at nside 1024
 }  // namespace
 
 // Per-kernel event timing (enabled by fsht_profile_enable).
@@ -82,6 +83,9 @@ void free_plan_memory(fsht_plan* p) {
   cudaFree(p->d_bhat);
   cudaFree(p->d_tw);
   cudaFree(p->d_work);
+  cudaFree(p->d_err);
+  cudaFree(p->d_ws);
+  cudaFree(p->d_eb);
   delete[] p->h_ring_i0;
   if (p->prof) {
     for (auto& v : p->prof->pending)
@@ -186,8 +190,8 @@ int fsht_plan_create(int nside, int lmax, int nmaps_max, int flags, int precisio
     fsht_set_error("nmaps_max = %d must be >= 1", nmaps_max);
     return FSHT_EINVAL;
   }
-  if (precision != FSHT_PREC_FP64) {
-    fsht_set_error("precision %d not available in this plan kind", precision);
+  if (precision != FSHT_PREC_FP64 && precision != FSHT_PREC_SPLIT) {
+    fsht_set_error("precision %d: use FSHT_PREC_FP64 or FSHT_PREC_SPLIT", precision);
     return FSHT_EUNSUPPORTED;
   }
   fsht_plan* p = new (std::nothrow) fsht_plan();
@@ -258,18 +262,36 @@ int fsht_plan_create(int nside, int lmax, int nmaps_max, int flags, int precisio
   }
   if ((rc = fsht_launch_ring_skip(p, p->stream))) return fail(rc);
   if ((rc = fsht_fft_tables_init(p))) return fail(rc);
-  // ---- workspace: nbuf phase matrices of kchunk maps
-  const size_t limit = workspace_limit_bytes ? workspace_limit_bytes : kDefaultWorkspace;
+  // ---- workspace: nbuf phase matrices of kchunk maps (+ the sliced copy for the
+  // split form, sized in groups of 128 maps)
+  const size_t limit = workspace_limit_bytes
+                           ? workspace_limit_bytes
+                           : (precision == FSHT_PREC_SPLIT ? kDefaultWorkspaceSplit : kDefaultWorkspace);
   const size_t per_map = per_map_buffer_bytes(p) * p->nbuf;
-  size_t kc = limit / per_map;
-  if (kc < 1) {
-    fsht_set_error("workspace limit %zu bytes is below one map's %zu bytes", limit, per_map);
+  auto need = [&](size_t k) -> size_t {
+    size_t b = per_map * k;
+    if (precision == FSHT_PREC_SPLIT) b += fsht_split_ws_bytes(lmax, p->nnorth, (int)k);
+    return b;
+  };
+  size_t kc = (size_t)nmaps_max;
+  while (kc > 1 && need(kc) > limit) kc = (kc > 128 && kc % 128) ? kc - kc % 128 : kc - (kc > 128 ? 128 : 1);
+  if (need(kc) > limit) {
+    fsht_set_error("workspace limit %zu bytes is below one map's %zu bytes", limit, need(1));
     return fail(FSHT_EINVAL);
   }
-  if (kc > (size_t)nmaps_max) kc = nmaps_max;
   p->kchunk = (int)kc;
   p->work_bytes = per_map * kc;
   if ((rc = dalloc((void**)&p->d_work, p->work_bytes))) return fail(rc);
+  if ((rc = dalloc((void**)&p->d_err, sizeof(int)))) return fail(rc);
+  if ((ce = cudaMemsetAsync(p->d_err, 0, sizeof(int), p->stream)) != cudaSuccess) {
+    fsht_set_error("memset: %s", cudaGetErrorString(ce));
+    return fail(FSHT_ECUDA);
+  }
+  if (precision == FSHT_PREC_SPLIT) {
+    p->ws_bytes = fsht_split_ws_bytes(lmax, p->nnorth, p->kchunk);
+    if ((rc = dalloc((void**)&p->d_ws, p->ws_bytes))) return fail(rc);
+    if ((rc = dalloc((void**)&p->d_eb, fsht_split_eb_bytes(lmax, p->kchunk)))) return fail(rc);
+  }
   if ((ce = cudaStreamSynchronize(p->stream)) != cudaSuccess) {
     fsht_set_error("plan setup: %s", cudaGetErrorString(ce));
     return fail(FSHT_ECUDA);
@@ -387,6 +409,14 @@ int fsht_run_stage(fsht_plan* p, int stage, const void* in, void* out, int nmaps
 int fsht_plan_sync(fsht_plan* p) {
   FSHT_TRY(check_plan(p));
   FSHT_CUDA_TRY(cudaStreamSynchronize(p->stream));
+  int err = 0;
+  FSHT_CUDA_TRY(cudaMemcpy(&err, p->d_err, sizeof(int), cudaMemcpyDeviceToHost));
+  if (err) {
+    FSHT_CUDA_TRY(cudaMemset(p->d_err, 0, sizeof(int)));
+    fsht_set_error("a bounded device-side wait expired (error word %d); results are invalid",
+                   err);
+    return FSHT_ETIMEOUT;
+  }
   return FSHT_OK;
 }
 
@@ -399,6 +429,32 @@ int fsht_t2alm(fsht_plan* p, const double* maps, double* alm, int nmaps, int nit
     return FSHT_EINVAL;
   }
   FSHT_TRY(need_bufs(p, niter > 0 ? 2 : 1));
+  if (p->precision == FSHT_PREC_SPLIT) {
+    if (niter > 0) {
+      fsht_set_error("the split-precision form runs niter = 0 analyses");
+      return FSHT_EUNSUPPORTED;
+    }
+    for (int c0 = 0; c0 < nmaps; c0 += p->kchunk) {
+      const int kc = nmaps - c0 < p->kchunk ? nmaps - c0 : p->kchunk;
+      double2* W0 = work_buf(p, 0, kc);
+      {
+        FSHT_PROF(FSHT_KCAT_FFT_FWD);
+        FSHT_TRY(fsht_launch_ring_fft_fwd(p, maps + (size_t)c0 * p->npix, p->npix, kc, W0,
+                                          p->stream));
+      }
+      {
+        FSHT_PROF(FSHT_KCAT_SLICE);
+        FSHT_TRY(fsht_launch_split_prepare(p, W0, p->d_ws, p->d_eb, alm, nmaps, c0, kc, 0,
+                                           p->stream));
+      }
+      {
+        FSHT_PROF(FSHT_KCAT_ANALYSIS);
+        FSHT_TRY(fsht_launch_analysis_split(p, p->d_ws, p->d_eb, alm, nmaps, c0, kc, 0,
+                                            p->stream));
+      }
+    }
+    return FSHT_OK;
+  }
   for (int c0 = 0; c0 < nmaps; c0 += p->kchunk) {
     const int kc = nmaps - c0 < p->kchunk ? nmaps - c0 : p->kchunk;
     double2* W0 = work_buf(p, 0, kc);

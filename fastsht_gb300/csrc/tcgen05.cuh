@@ -1,0 +1,168 @@
+// Thin inline-PTX helpers for Blackwell (sm_103a): mbarriers, bulk async copies,
+// tcgen05 (UMMA) descriptors, MMA, commit and TMEM loads.  Every wait is bounded:
+// on expiry it raises a CTA-wide abort flag and the caller unwinds.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace tc {
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count));
+}
+__device__ __forceinline__ void mbar_fence_init() {
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
+               "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+      "selp.u32 %0, 1, 0, p;\n}"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+// Bounded wait: returns false (and sets *abort) when the phase does not complete
+// within the iteration budget or when another thread already aborted.
+constexpr uint32_t kWaitLimit = 1u << 24;
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity,
+                                          volatile int* abort) {
+  for (uint32_t it = 0; it < kWaitLimit; ++it) {
+    if (mbar_try_wait(bar, parity)) return true;
+    if (*abort) return false;
+    if (it > 64) __nanosleep(32);
+  }
+  *abort = 1;
+  return false;
+}
+
+// 1-D bulk copy global -> shared, completion signalled on an mbarrier (TMA engine).
+// dst, src and bytes must be multiples of 16.
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes,
+                                         uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::
+          "r"(smem_u32(dst)),
+      "l"(src), "r"(bytes), "r"(smem_u32(bar))
+      : "memory");
+}
+
+__device__ __forceinline__ void fence_proxy_async() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+// ------------------------------------------------------------------ UMMA
+// Shared-memory matrix descriptor, no swizzle, K-major core matrices (8 rows x 16 B):
+// lbo = byte stride between core matrices adjacent along K, sbo = along M/N.
+__device__ __forceinline__ uint64_t umma_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+  uint64_t d = 0;
+  d |= (uint64_t)((saddr >> 4) & 0x3FFF);
+  d |= (uint64_t)((lbo >> 4) & 0x3FFF) << 16;
+  d |= (uint64_t)((sbo >> 4) & 0x3FFF) << 32;
+  d |= (uint64_t)1 << 46;   // descriptor version for tcgen05
+  return d;
+}
+// Instruction descriptor, kind::f16: BF16 x BF16 -> F32, both operands K-major.
+__host__ __device__ constexpr uint32_t umma_idesc_bf16(int M, int N) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) |
+         ((uint32_t)(M >> 4) << 24);
+}
+__device__ __forceinline__ void umma_bf16(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc,
+                                          uint32_t idesc, uint32_t accumulate) {
+  asm volatile(
+      "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}" ::"r"(d_tmem),
+      "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+      : "memory");
+}
+// Arrive on bar when every previously issued tcgen05.mma of this thread completes.
+__device__ __forceinline__ void umma_commit(uint64_t* bar) {
+  asm volatile(
+      "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+          smem_u32(bar))
+      : "memory");
+}
+__device__ __forceinline__ void tmem_alloc(uint32_t* dst_smem, uint32_t ncols) {
+  asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                   smem_u32(dst_smem)),
+               "r"(ncols)
+               : "memory");
+  asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+}
+__device__ __forceinline__ void tmem_dealloc(uint32_t taddr, uint32_t ncols) {
+  asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols)
+               : "memory");
+}
+__device__ __forceinline__ void tc_fence_before() {
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ void tc_fence_after() {
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+}
+// 32 lanes x 32 bit, 16 consecutive columns per thread.
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t (&v)[16]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 "
+      "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+      : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]),
+        "=r"(v[7]), "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]),
+        "=r"(v[14]), "=r"(v[15])
+      : "r"(taddr)
+      : "memory");
+}
+__device__ __forceinline__ void tmem_wait_ld() {
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
+
+// ------------------------------------------------------------------ slicing
+// Four balanced base-256 digits of an FP64 value v against a power-of-two scale 2^E
+// (|v| < 2^E):  |v| 2^(6-E) = d0 + d1 2^-8 + d2 2^-16 + d3 2^-24 + r,  |r| <= 2^-25,
+// |d0| <= 64, |d1..3| <= 128, every digit carrying the sign of v.  Each digit is an
+// integer that BF16 holds exactly, so slice products are exact integers.  Integer
+// operations only.
+__device__ __forceinline__ uint16_t bf16_of_int(int d) {
+  if (d == 0) return 0;
+  const uint32_t sign = d < 0 ? 0x8000u : 0u;
+  const uint32_t b = (uint32_t)(d < 0 ? -d : d);   // 1..255
+  const int msb = 31 - __clz(b);
+  const uint32_t mant = (b << (7 - msb)) & 0x7F;
+  return (uint16_t)(sign | ((uint32_t)(127 + msb) << 7) | mant);
+}
+__device__ __forceinline__ void digits4(double v, int E, uint16_t (&s)[4]) {
+  const unsigned long long bits = (unsigned long long)__double_as_longlong(v);
+  const int eb = (int)((bits >> 52) & 0x7FF);
+  long long T = 0;
+  if (eb != 0 && eb != 0x7FF) {
+    const unsigned long long mant = (bits & ((1ull << 52) - 1)) | (1ull << 52);
+    const int sh = E - (eb - 1023) + 22;      // >= 23 when |v| < 2^E
+    if (sh < 23) T = 1ll << 30;               // out of range: saturate (never for valid scales)
+    else if (sh < 64) T = (long long)((mant + (1ull << (sh - 1))) >> sh);
+  }
+  const int neg = (bits >> 63) ? -1 : 1;
+  int d[4];
+#pragma unroll
+  for (int j = 3; j >= 1; --j) {
+    const int dj = (int)((T + 128) & 255) - 128;
+    d[j] = dj;
+    T = (T - dj) >> 8;
+  }
+  d[0] = (int)T;
+#pragma unroll
+  for (int j = 0; j < 4; ++j) s[j] = bf16_of_int(neg * d[j]);
+}
+
+}  // namespace tc

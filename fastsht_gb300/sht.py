@@ -47,11 +47,13 @@ class SHT:
 
     SHT(nside, lmax, nsim, niter=0, pol=False, all_buff=False) as in the
     reference (SHT.py:17).  Extra keywords: ``device`` (CUDA device index),
-    ``workspace_limit`` (bytes of phase-matrix workspace, 0 = 16 GiB).
+    ``workspace_limit`` (bytes of workspace, 0 = library default) and ``precision``:
+    "fp64" (the plain method, all FP64) or "split" (t2alm's Legendre contraction as
+    BF16 slice products on the tensor cores, ~1e-8 max relative alm error).
     """
 
     def __init__(self, nside, lmax, nsim, niter=0, pol=False, all_buff=False, *,
-                 device=None, workspace_limit=0):
+                 device=None, workspace_limit=0, precision="fp64"):
         if not torch.cuda.is_available():
             raise RuntimeError("fastsht_gb300 needs a CUDA device (no CPU fallback)")
         self.nside = int(nside)
@@ -62,6 +64,9 @@ class SHT:
         self.nring = 4 * self.nside - 1
         self.npix = 12 * self.nside ** 2
         self.device = torch.device("cuda", torch.cuda.current_device() if device is None else device)
+        if precision not in ("fp64", "split"):
+            raise ValueError("precision must be 'fp64' or 'split'")
+        self.precision = precision
         # workspace buffers, like the reference's nbuff (SHT.py:52-59)
         flags = 0
         if pol or all_buff:
@@ -76,8 +81,8 @@ class SHT:
         with torch.cuda.device(self.device):
             stream = torch.cuda.current_stream(self.device).cuda_stream
             _lib.call("fsht_plan_create", self.nside, self.lmax, self.nsim, flags,
-                      _lib.FSHT_PREC_FP64, int(workspace_limit), C.c_void_p(stream),
-                      C.byref(plan))
+                      _lib.FSHT_PREC_SPLIT if precision == "split" else _lib.FSHT_PREC_FP64,
+                      int(workspace_limit), C.c_void_p(stream), C.byref(plan))
         self._plan = plan
 
     # ------------------------------------------------------------ lifetime
@@ -210,6 +215,8 @@ class SHT:
             _lib.call("fsht_t2alm", self._plan, C.c_void_p(dmaps.data_ptr()),
                       C.c_void_p(dalm.data_ptr()), self.nsim, self.niter,
                       0 if method == 'old' else 1)
+            if self.precision == "split":
+                _lib.call("fsht_plan_sync", self._plan)   # surfaces expired device waits
             self._dev_alm = dalm
             if not get_alm:
                 return None

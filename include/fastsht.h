@@ -51,9 +51,11 @@ enum { FSHT_FLAG_POL = 1, FSHT_FLAG_ITER = 2 };
  *   nmaps_max  largest nmaps a transform call on this plan will pass
  *   flags      FSHT_FLAG_POL for spin-2 (Q/U) transforms, FSHT_FLAG_ITER for
  *              niter > 0 (each doubles the workspace, like the reference's nbuff)
- *   precision  FSHT_PREC_FP64 (plain)
- *   workspace_limit_bytes  upper bound for the plan's phase-matrix workspace
- *              (0 = default 16 GiB); maps are processed in chunks that fit.
+ *   precision  FSHT_PREC_FP64 (plain, all FP64) or FSHT_PREC_SPLIT (t2alm's Legendre
+ *              contraction as BF16 slice products on the tensor cores, max relative
+ *              alm error ~1e-9..1e-8 against FP64; other transforms stay FP64)
+ *   workspace_limit_bytes  upper bound for the plan's workspace (0 = default 16 GiB,
+ *              40 GiB for FSHT_PREC_SPLIT); maps are processed in chunks that fit.
  *   stream     cudaStream_t (NULL = legacy default stream) */
 int fsht_plan_create(int nside, int lmax, int nmaps_max, int flags, int precision,
                      size_t workspace_limit_bytes, void* stream, fsht_plan** plan);
@@ -119,7 +121,8 @@ enum {
   FSHT_KCAT_ANALYSIS = 2,
   FSHT_KCAT_SYNTHESIS = 3,
   FSHT_KCAT_RESIDUAL = 4,
-  FSHT_KCAT_OTHER = 5,
+  FSHT_KCAT_SLICE = 5,      /* split form: phase matrix -> BF16 digit tiles */
+  FSHT_KCAT_OTHER = 6,
   FSHT_KCAT_COUNT = 8
 };
 int fsht_profile_enable(fsht_plan* plan, int on);
