@@ -73,6 +73,17 @@ def parse():
                          "fp64: the plain method")
     ap.add_argument("--no-fp64", action="store_true",
                     help="skip the plain-FP64 comparison run of the split form")
+    ap.add_argument("--workload", choices=["c3", "batched", "serving"], default="c3",
+                    help="c3: the headline 500-map nside-1024 analysis; batched: a mix of map "
+                         "sets in CUDA-graph launches; serving: a Poisson request stream")
+    ap.add_argument("--sets", type=int, default=64, help="batched: map sets in the mix")
+    ap.add_argument("--max-maps", type=int, default=None,
+                    help="batched/serving: upper end of the uniform nmaps draw")
+    ap.add_argument("--max-nside", type=int, default=1024,
+                    help="batched/serving: upper end of the log-uniform nside draw")
+    ap.add_argument("--requests", type=int, default=2000, help="serving: requests")
+    ap.add_argument("--rate", type=float, default=200.0, help="serving: mean arrivals per s")
+    ap.add_argument("--budget-gb", type=float, default=150.0, help="serving: HBM budget")
     a = ap.parse_args()
     if a.lmax is None:
         a.lmax = 2 * a.nside - 1
@@ -458,11 +469,218 @@ def e2e(sht, maps_dev, ke, args, world):
             "maps_per_step": ke}
 
 
+# ---------------------------------------------------------------- batched form
+def batched_mix(nsets, max_nside, max_maps, seed=3):
+    """The batched mix: nside = 2^U{5..log2 max_nside}, lmax ~ U[2 nside, 3 nside - 1],
+    nmaps ~ U[1, max_maps], even sets T-only and odd sets I/Q/U."""
+    rng = np.random.default_rng(seed)
+    hi = int(round(math.log2(max_nside)))
+    sets = []
+    for s in range(nsets):
+        ns = int(2 ** rng.integers(5, hi + 1))
+        lmax = int(rng.integers(2 * ns, 3 * ns))
+        nm = int(rng.integers(1, max_maps + 1))
+        sets.append((ns, lmax, nm, bool(s % 2)))
+    return sets
+
+
+def bench_batched(args, rank, world, local):
+    """Every set's analysis (t2alm of I; qu2eb of Q/U for I/Q/U sets) as one batch, run as
+    CUDA-graph launches (one per group of sets that fits the HBM budget).  value =
+    map.SHT/s over the whole mix with T jobs in the split-precision form; the same mix
+    all-FP64 is reported beside it."""
+    import torch
+    import torch.distributed as dist
+    from fastsht_gb300 import _lib
+    from fastsht_gb300.batch import Batch
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    _lib.load(build_if_missing=True)
+    if world > 1:
+        dist.init_process_group("nccl", device_id=dev)
+    max_maps = args.max_maps or 16
+    sets = batched_mix(args.sets, args.max_nside, max_maps, seed=3 + rank)
+    mapsht = sum(nm * (3 if pol else 1) for ns, lmax, nm, pol in sets)
+    flops = sum(flop_per_map(ns, lmax) * nm * (5 if pol else 1) for ns, lmax, nm, pol in sets)
+
+    def build(precision):
+        b = Batch(device=local, nslots=4, autotune=True)
+        for ns, lmax, nm, pol in sets:
+            j = b.add("t2alm", ns, lmax, nm, precision=precision)
+            j.inputs[0].normal_()
+            if pol:
+                jp = b.add("qu2eb", ns, lmax, nm)
+                for t in jp.inputs:
+                    t.normal_()
+        t0 = time.perf_counter()
+        b.build()
+        torch.cuda.synchronize()
+        return b, time.perf_counter() - t0
+
+    def run(b, steps, warmup, clocks=None):
+        for _ in range(warmup):
+            b.run()
+        torch.cuda.synchronize()
+        if world > 1:
+            dist.barrier()
+        if clocks:
+            clocks.start()
+        s = torch.cuda.current_stream()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(s)
+        for _ in range(steps):
+            b.run()
+        e1.record(s)
+        torch.cuda.synchronize()
+        clk = clocks.stop() if clocks else None
+        ms = e0.elapsed_time(e1)
+        if world > 1:
+            t = torch.tensor([ms], device=dev)
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            ms = float(t.item())
+        return ms, clk
+
+    b_split, t_build = build("split")
+    info = b_split.info()
+    ms, clk = run(b_split, args.steps, args.warmup, ClockSampler(local))
+    b_split.close()
+    del b_split
+    torch.cuda.empty_cache()
+    b64, _ = build("fp64")
+    ms64, _ = run(b64, max(1, args.steps // 2), 1)
+    b64.close()
+    value = world * mapsht * args.steps / (ms / 1000.0)
+    v64 = world * mapsht * max(1, args.steps // 2) / (ms64 / 1000.0)
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None,
+        "dtype": "T jobs bf16x4-split of f64, Q/U jobs f64", "data": "synthetic",
+        "config": {"workload": (f"batched form: {len(sets)} map sets, nside 2^U{{5..."
+                                f"{int(round(math.log2(args.max_nside)))}}}, lmax ~ U[2 nside, "
+                                f"3 nside - 1], nmaps ~ U[1, {max_maps}], even sets T, odd "
+                                f"sets I/Q/U; analysis (t2alm + qu2eb); seed 3"),
+                   "sets": len(sets), "maps_sht_per_step": mapsht,
+                   "graph": info, "build_s": round(t_build, 3),
+                   "l2": "N(0,1) pixel inputs resident in HBM, no flush (sets up to "
+                         f"{max(ns for ns, *_ in sets)} nside exceed L2 in total)",
+                   "parallelism": f"replicas x{world}"},
+        "clocks": clk,
+        "flop_rate_tflops": world * flops * args.steps / (ms / 1000.0) / 1e12,
+        "fp64_all": {"value": v64, "unit": UNIT, "ms_per_step": ms64 / max(1, args.steps // 2),
+                     "split_speedup": value / v64},
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+
+
+# ---------------------------------------------------------------- serving form
+def bench_serving(args, rank, world, local):
+    """Open-loop Poisson stream into fastsht_gb300.serve.Server: map2alm or alm2map, T or
+    Q/U with equal odds, nside = 2^U{6..log2 max_nside}, lmax = 2 nside, nmaps ~
+    U[1, max_maps], FP64 or split per request (the split form applies to T map2alm; the
+    other kinds run FP64), seed 4.  Inputs are device-resident views of pre-generated
+    pools.  value = map.SHT/s over the run; p50/p99 latency from arrival to result."""
+    import torch
+    from fastsht_gb300 import _lib
+    from fastsht_gb300.serve import Server
+
+    if rank != 0:
+        return
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    _lib.load(build_if_missing=True)
+    max_maps = args.max_maps or 8
+    rng = np.random.default_rng(4)
+    hi = int(round(math.log2(args.max_nside)))
+    kinds = ["t2alm", "alm2t", "qu2eb", "eb2qu"]
+    reqs = []
+    t = 0.0
+    for _ in range(args.requests):
+        t += rng.exponential(1.0 / args.rate)
+        ns = int(2 ** rng.integers(6, hi + 1))
+        reqs.append((t, kinds[int(rng.integers(0, 4))], ns, 2 * ns,
+                     int(rng.integers(1, max_maps + 1)),
+                     "split" if rng.integers(0, 2) else "fp64"))
+    pools = {}
+    for ns in sorted({r[2] for r in reqs}):
+        L = 2 * ns + 1
+        gm = torch.Generator(device=dev)
+        gm.manual_seed(ns)
+        pools[ns] = (torch.randn((2, max_maps, 12 * ns * ns), dtype=torch.float64, device=dev,
+                                 generator=gm),
+                     torch.randn((2, L, L, max_maps), dtype=torch.float64, device=dev,
+                                 generator=gm))
+
+    def inputs(kind, ns, nm):
+        maps, alm = pools[ns]
+        nf = 2 if kind in ("qu2eb", "eb2qu") else 1
+        if kind in ("t2alm", "qu2eb"):
+            return [maps[f, :nm] for f in range(nf)]
+        return [alm[f, :, :, :nm].contiguous() for f in range(nf)]
+
+    budget = args.budget_gb * 1e9
+    srv = Server(hbm_budget=budget, nslots=8, device=local)
+    # warm-up: every (kind, nside, precision) once, so plans and autotuning are in place
+    for kind in kinds:
+        for ns in pools:
+            for prec in ("fp64", "split"):
+                srv.submit(kind, ns, 2 * ns, inputs(kind, ns, 1),
+                           precision=prec if kind == "t2alm" else "fp64")
+    srv.drain()
+    srv.completed.clear()
+    clocks = ClockSampler(local)
+    clocks.start()
+    t0 = time.perf_counter()
+    for (ta, kind, ns, lmax, nm, prec) in reqs:
+        now = time.perf_counter() - t0
+        if ta > now:
+            time.sleep(ta - now)
+        srv.submit(kind, ns, lmax, inputs(kind, ns, nm),
+                   precision=prec if kind == "t2alm" else "fp64", t_arrival=t0 + ta)
+    srv.drain()
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    clk = clocks.stop()
+    st = srv.stats()
+    srv.close()
+    mapsht = sum(nm * (2 if kind in ("qu2eb", "eb2qu") else 1) for _, kind, _, _, nm, _ in reqs)
+    line = {
+        "metric": METRIC, "value": mapsht / wall, "unit": UNIT, "n_gpus": 1,
+        "steps": 1, "warmup": 1, "ms_per_step": wall * 1000.0, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64; T map2alm requests drawn split run bf16x4-split of f64",
+        "data": "synthetic",
+        "config": {"workload": (f"serving form: Poisson stream of {args.requests} requests "
+                                f"(mean {args.rate}/s), map2alm or alm2map x T or Q/U, nside "
+                                f"2^U{{6..{hi}}}, lmax = 2 nside, nmaps ~ U[1, {max_maps}], "
+                                f"FP64 or split per request, seed 4; HBM budget "
+                                f"{args.budget_gb} GB"),
+                   "offered_s": reqs[-1][0], "nslots": 8},
+        "clocks": clk,
+        "latency_ms": {"p50": st.get("p50_ms"), "p99": st.get("p99_ms"),
+                       "mean": st.get("mean_ms")},
+        "requests_per_s": args.requests / wall,
+        "max_inflight": st.get("max_inflight"),
+        "high_water_bytes": st.get("high_water_bytes"),
+    }
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     rank, world, local = dist_env()
     if args.impl == "reference":
         reference_arm(args, rank, world)
+        return
+    if args.workload == "batched":
+        bench_batched(args, rank, world, local)
+        return
+    if args.workload == "serving":
+        bench_serving(args, rank, world, local)
         return
     ours(args, rank, world, local)
 

@@ -21,8 +21,17 @@ FSHT_PREC_FP64 = 0
 FSHT_PREC_SPLIT = 1
 FSHT_FLAG_POL = 1
 FSHT_FLAG_ITER = 2
+FSHT_FLAG_TABLES_ONLY = 4
+FSHT_JOB_T2ALM, FSHT_JOB_ALM2T, FSHT_JOB_QU2EB, FSHT_JOB_EB2QU = 0, 1, 2, 3
+
+
+class FshtJob(C.Structure):
+    _fields_ = [("nside", C.c_int), ("lmax", C.c_int), ("nmaps", C.c_int), ("kind", C.c_int),
+                ("precision", C.c_int), ("in0", C.c_void_p), ("in1", C.c_void_p),
+                ("out0", C.c_void_p), ("out1", C.c_void_p)]
+
 KCAT_NAMES = ["ring_fft_fwd", "ring_fft_inv", "legendre_analysis", "legendre_synthesis",
-              "fourier_residual", "split_slice", "other"]
+              "fourier_residual", "split_slice", "other", "split_lambda"]
 KCAT_COUNT = 8
 
 _vp = C.c_void_p
@@ -51,6 +60,15 @@ SIGNATURES = {
     "fsht_profile_read": [_vp, _i, C.POINTER(_i), C.POINTER(C.c_double)],
     "fsht_measure_fp64_peak": [C.POINTER(C.c_double)],
     "fsht_last_error": [C.c_char_p, _sz],
+    "fsht_batch_create": [C.c_void_p, _i, _i, _sz, _i, _vp, C.POINTER(_vp)],
+    "fsht_batch_run": [_vp],
+    "fsht_batch_sync": [_vp],
+    "fsht_batch_info": [_vp, C.POINTER(_i), C.POINTER(_i)],
+    "fsht_batch_destroy": [_vp],
+    "fsht_plan_autotune": [_vp, _i],
+    "fsht_job_workspace": [_vp, _vp, _i, C.POINTER(_sz)],
+    "fsht_run_job": [_vp, _vp, _vp, _sz, _vp],
+    "fsht_plan_tuning": [_vp, C.POINTER(_i), C.POINTER(_i)],
 }
 
 _lib = None

@@ -48,6 +48,14 @@ struct FshtRingFFT {
   long long bhat_off;   // offset (double2) of FFT_P(conj chirp, wrapped)
 };
 
+// Split-precision form: per (l, m) row of the scaled recursion (legendre_split.cu).
+struct FshtLamRow {
+  double beta;   // mu_l = x mu_{l-1} - beta mu_{l-2}
+  double rs;     // row scale of the GEMM epilogue, Dm_l 2^EA(l)
+  int erow;      // EA(l) - Dx_l: digit exponent of row l before the per-ring offset
+  int pad;
+};
+
 struct fsht_plan {
   int nside, lmax, nring, nnorth;  // nnorth = 2*nside (north rings incl. equator)
   long long npix;
@@ -71,12 +79,20 @@ struct fsht_plan {
   size_t work_bytes;
   int nbuf;
   size_t fft_smem;                 // dynamic smem of the ring FFT kernels
+  int fft_mpb, fft_threads;        // ring-FFT launch shape (0: heuristic), set by the autotuner
   struct FshtProfile* prof;        // non-null while per-kernel timing is on
   int* d_err;                      // device error word (bounded waits that expired)
-  // split-precision form: sliced phase tiles and their column exponents
+  // split-precision form: sliced phase tiles and their column exponents, the scaled
+  // recursion rows, and the lambda-digit staging buffer with its waves of m
   unsigned char* d_ws;
   int* d_eb;
   size_t ws_bytes;
+  FshtLamRow* d_lamtab;            // triangular, (l, m) at m(2 lmax + 3 - m)/2 + l - m
+  long long* d_lam_off;            // per pair-ordered index q: first 16 KB tile unit
+  int* h_waves;                    // per wave: q0, q1, max l-tiles, max K-chunks, max ring blocks
+  int nwaves;
+  unsigned char* d_lbuf;
+  size_t lbuf_bytes;
 };
 
 // ---------------------------------------------------------------- status codes
@@ -132,15 +148,20 @@ int fsht_launch_analysis_fp64(fsht_plan* p, int spin, const double2* WQ,
                               int which, cudaStream_t s);
 size_t fsht_split_ws_bytes(int lmax, int nnorth, int kc);
 size_t fsht_split_eb_bytes(int lmax, int kc);
-// Split-precision (BF16 digits on tcgen05) spin-0 analysis of one chunk: prepare
-// cuts the {S, D} phase matrix W into digit tiles WS and column exponents EB (and
-// clears alm's chunk columns when K-chunks will add into it); analysis runs the UMMA
-// contraction into alm.
+// Split-precision (BF16 digits on tcgen05) spin-0 analysis of one chunk.  Tables (plan
+// creation): recursion rows, per-m tile offsets, waves of m and the staging size.
+// prepare cuts the {S, D} phase matrix W into digit tiles WS and column exponents EB
+// (and clears alm's chunk columns when K-chunks will add into it); then, per wave w,
+// lambda writes the wave's lambda digit tiles into lbuf and gemm contracts them with WS
+// into alm.
+int fsht_split_tables_init(fsht_plan* p);
 int fsht_launch_split_prepare(fsht_plan* p, const double2* W, unsigned char* WS, int* EB,
                               double* alm, int nmaps_total, int k0, int kc, int accumulate,
                               cudaStream_t s);
-int fsht_launch_analysis_split(fsht_plan* p, const unsigned char* WS, const int* EB, double* alm,
-                               int nmaps_total, int k0, int kc, int accumulate, cudaStream_t s);
+int fsht_launch_split_lambda(fsht_plan* p, int w, unsigned char* lbuf, cudaStream_t s);
+int fsht_launch_split_gemm(fsht_plan* p, int w, const unsigned char* WS, const int* EB,
+                           const unsigned char* lbuf, double* alm, int nmaps_total, int k0,
+                           int kc, cudaStream_t s);
 int fsht_launch_synthesis_fp64(fsht_plan* p, int spin, const double* almE,
                                const double* almB, double2* WQ, double2* WU,
                                int nmaps_total, int k0, int kc, cudaStream_t s);

@@ -4,30 +4,31 @@
 // + mat2alm, src/get_plm_recursive.f90:17-98, src/sht_core.f90:30-89):
 //   a_lm = pa sum_i lambda_lm(theta_i) P_m(i),  P = S (l-m even) or D (l-m odd).
 // Both operands are written as four balanced base-256 digits against power-of-two
-// scales (rows of lambda: 2^EA(l) with |lambda_lm| <= sqrt((2l+1)/4pi) < 2^EA(l);
-// columns of P: 2^EB from the column maximum).  Digits are integers (|d0| <= 64,
-// |d1..3| <= 128) that BF16 holds exactly, so every UMMA product is an exact integer.
-// The ten digit products of level a+b <= 3 run as BF16 UMMAs with FP32 accumulation,
-// one TMEM accumulator per level:
+// scales (rows of lambda: 2^EA(l) from the |Y_lm| bound; columns of P: 2^EB from the
+// column maximum).  Digits are integers (|d0| <= 64, |d1..3| <= 128) that BF16 holds
+// exactly, so every UMMA product is an exact integer.  The ten digit products of level
+// a+b <= 3 run as BF16 UMMAs with FP32 accumulation, one TMEM accumulator per level:
 //   level 0 and level 1 sums stay below 2^24 over <= 1024 rings, so they are exact
 //   (rings beyond 1024 go to another CTA: K-chunks, combined with FP64 atomics);
 //   levels 2 and 3 carry weights 2^-16 and 2^-24, so FP32 rounding there is far
 //   below the ~2^-31 representation error.
-// The epilogue combines the four levels and applies the scales in FP64.  The
-// recursion stays FP64 (exponent-rescaled, as in the plain path) and is computed on
-// the fly: no P_lm table is materialised.  Max relative alm error against FP64:
-// ~2e-8 (tests/test_gpu_split.py).
+// The epilogue combines the four levels and applies the scales in FP64.
 //
-// CTA = (m-pair, parity, K-chunk of <= 1024 rings, 64-map group); it walks l in tiles
-// of 128 rows of one parity (256 consecutive l) and keeps each ring's recursion state
-// in shared memory between tiles.  Roles (192 threads): warps 0-3 run the recursion
-// for 128 rings at a time and write lambda digits to shared memory, then read TMEM in
-// the epilogue; warp 4 streams the pre-sliced P tiles with bulk async copies (TMA
-// engine); warp 5 issues the UMMAs.
+// Three kernels per chunk of maps:
+//   k_slice_phase    P -> digit tiles WS and column exponents EB (per 64-map group);
+//   k_lambda_digits  the FP64 exponent-rescaled recursion, once per (m, ring) for all
+//                    map groups, written as lambda digit tiles into a staging buffer that
+//                    holds one wave of m (a few GB at most: no P_lm table is kept);
+//   k_split_gemm     one 128 x 128 output tile per CTA, both operands streamed by bulk
+//                    async copies (TMA engine) into a 6-stage ring, UMMAs into TMEM.
+// Max relative alm error against FP64: ~3e-8 (tests/test_gpu_split.py).
 #include "common.cuh"
 #include "tcgen05.cuh"
 
+#include <algorithm>
 #include <cmath>
+#include <new>
+#include <vector>
 
 namespace {
 
@@ -35,15 +36,11 @@ constexpr int kRows = 128;          // UMMA M: rows of one parity per l-tile
 constexpr int kCols = 128;          // UMMA N: 64 maps x {Re, Im}
 constexpr int kGroupMaps = 64;
 constexpr int kKStep = 16;          // rings per UMMA
-constexpr int kSCRings = 128;       // rings per recursion super-chunk
-constexpr int kSCSteps = kSCRings / kKStep;
+constexpr int kSCRings = 128;       // rings per lambda-digit block
 constexpr int kKChunk = 1024;       // rings per CTA (keeps levels 0 and 1 exact)
 constexpr int kSlices = 4;
-constexpr int kStages = 3;
 constexpr uint32_t kATileBytes = kRows * kKStep * 2;    // 4 KB per (k-step, digit)
 constexpr uint32_t kBTileBytes = kCols * kKStep * 2;    // 4 KB per (k-step, digit)
-constexpr uint32_t kABufBytes = kSCSteps * kSlices * kATileBytes;   // 128 KB
-constexpr uint32_t kBStageBytes = kSlices * kBTileBytes;            // 16 KB
 constexpr int kThreads = 192;
 constexpr int kEmptyExp = -4000;    // column exponent of an all-zero column
 
@@ -139,270 +136,337 @@ __global__ void __launch_bounds__(128) k_slice_phase(SliceArgs a) {
   }
 }
 
-// ------------------------------------------------------------------ analysis
-struct SplitArgs {
-  int lmax, nnorth, ngroups, nks_max, nkc;
+// ------------------------------------------------------------------ lambda digits
+// Scaled recursion.  With D_l = prod_{k=m+1..l} a_k (D_m = 1) and mu_l = lambda_l / D_l:
+//   mu_l = x mu_{l-1} - beta_l mu_{l-2},   beta_l = b_l / (a_l a_{l-1})   (beta_{m+1} = 0),
+// two FP64 operations per step instead of four.  Rows are digitised as
+// lambda_l / Dm_l = mu 2^(Et + Dx_l) against 2^EA(l) with EA(l) from |lambda| / Dm_l <=
+// sqrt((2l+1)/4pi) / Dm_l (D_l = Dm_l 2^Dx_l, Dm_l in [1, 2)); the GEMM epilogue multiplies
+// row l by rs = Dm_l 2^EA(l).  Et is the per-ring exponent carried with the state.
+__device__ __forceinline__ int m_of_q(int q, int lmax) {
+  return (q & 1) ? lmax - (q >> 1) : (q >> 1);
+}
+__host__ __device__ __forceinline__ long long tri_off(int m, int lmax) {
+  return (long long)m * (2LL * lmax + 3 - m) / 2;
+}
+
+// One thread per m, sequential in l: beta_l, rs_l and erow_l = EA(l) - Dx_l.
+__global__ void k_lam_table(int lmax, FshtLamRow* tab) {
+  const int m = blockIdx.x * blockDim.x + threadIdx.x;
+  if (m > lmax) return;
+  FshtLamRow* row = tab + tri_off(m, lmax);
+  double dm = 1.0, a_prev = 0.0;
+  int dx = 0;
+  for (int l = m; l <= lmax; ++l) {
+    double beta = 0.0;
+    if (l > m) {
+      const RecConst c = rec_coeffs(l, m);
+      beta = (l == m + 1) ? 0.0 : c.b / (c.a * a_prev);
+      int t;
+      dm = frexp(dm * c.a, &t);     // [0.5, 1)
+      dm *= 2.0;
+      dx += t - 1;
+      a_prev = c.a;
+    }
+    const double bound = sqrt((2.0 * l + 1.0) / (4.0 * M_PI)) * (1.0 + 0x1p-30) / dm;
+    const int ea = ilogb(bound) + 1;
+    FshtLamRow r;
+    r.beta = beta;
+    r.rs = ldexp(dm, ea);
+    r.erow = ea - dx;
+    r.pad = 0;
+    row[l - m] = r;
+  }
+}
+
+// grid (q in wave, 128-ring block), 128 threads = rings.  Writes the four digit tiles of
+// every (parity, l-tile, k-step) the block covers, in the UMMA K-major core-matrix layout
+// (core matrix 8 rows x 8 rings, 128 B, at (row/8)*256 + (ring/8)*128 within a 4 KB tile).
+struct LamArgs {
+  int lmax, nnorth, q0;
   const double* cth;
   const double* sth;
   const double* pref;
   const int* ring_i0;
+  const FshtLamRow* tab;
+  const long long* lam_off;
+  unsigned char* lbuf;
+};
+
+constexpr int kLamBlock = 32;                 // l per staging block (16 rows per parity)
+constexpr int kStageStride = kSCRings + 2;    // uint64 per staged row (+16 B against conflicts)
+
+__global__ void __launch_bounds__(128) k_lambda_digits(LamArgs a) {
+  __shared__ __align__(16) unsigned long long S[2][kLamBlock / 2][kStageStride];
+  const int q = a.q0 + blockIdx.x;
+  const int m = m_of_q(q, a.lmax);
+  const int i0 = a.ring_i0[m];
+  const int K = a.nnorth - i0;
+  const int rb = blockIdx.y;
+  if (rb * kSCRings >= K) return;
+  const int tid = threadIdx.x;
+  const int r = rb * kSCRings + tid;
+  const bool valid = r < K;
+  const int nks = (K + kKStep - 1) / kKStep;
+  const int ntiles = (a.lmax - m + 1 + 2 * kRows - 1) / (2 * kRows);
+  unsigned char* base = a.lbuf + (size_t)(a.lam_off[q] - a.lam_off[a.q0]) * kSlices * kATileBytes;
+  const FshtLamRow* tab = a.tab + tri_off(m, a.lmax);
+
+  double x = 0.0, s1 = 0.0, s2 = 0.0;
+  int et = 0;
+  if (valid) {
+    int e;
+    x = a.cth[i0 + r];
+    rec_seed(a.sth[i0 + r], a.pref[m], m, s1, e);
+    et = 600 * e;
+  }
+  const int lend = ntiles * 2 * kRows;
+  for (int lb = 0; lb < lend; lb += kLamBlock) {
+#pragma unroll 4
+    for (int jj = 0; jj < kLamBlock; ++jj) {
+      const int j = lb + jj;
+      unsigned long long pk = 0;
+      if (m + j <= a.lmax) {
+        const double beta = tab[j].beta;
+        const int erow = tab[j].erow;
+        if (j > 0) {
+          const double t = beta * s2;
+          const double nx = fma(x, s1, -t);
+          s2 = s1;
+          s1 = nx;
+        }
+        if (valid) {
+          uint16_t d[4];
+          tc::digits4(s1, erow - et, d);
+          pk = (unsigned long long)d[0] | ((unsigned long long)d[1] << 16) |
+               ((unsigned long long)d[2] << 32) | ((unsigned long long)d[3] << 48);
+        }
+      }
+      S[jj & 1][jj >> 1][tid] = pk;
+    }
+    {   // keep the state within 2^-300 .. 2^300; growth per block stays far below 2^300
+      const double am = fmax(fabs(s1), fabs(s2));
+      if (am > 0x1p300) {
+        s1 *= 0x1p-600;
+        s2 *= 0x1p-600;
+        et += 600;
+      } else if (am > 0.0 && am < 0x1p-300) {
+        s1 *= 0x1p600;
+        s2 *= 0x1p600;
+        et -= 600;
+      }
+    }
+    __syncthreads();
+    // write-out: unit u = (r8: 3 bits, khalf, rg, ks: 3 bits, parity); a warp stores 512
+    // contiguous bytes of one digit tile per instruction
+    const int t = lb / (2 * kRows);
+    const int rowt0 = (lb % (2 * kRows)) >> 1;
+    for (int u = tid; u < 2 * (kLamBlock / 2) * (kSCRings / 8); u += 128) {
+      const int r8 = u & 7, khalf = (u >> 3) & 1, rg = (u >> 4) & 1, ks = (u >> 5) & 7,
+                p = u >> 8;
+      const int gks = rb * (kSCRings / kKStep) + ks;
+      if (gks >= nks) continue;
+      const int row = rg * 8 + r8;
+      const unsigned long long* src = &S[p][row][ks * kKStep + khalf * 8];
+      unsigned long long v[8];
+#pragma unroll
+      for (int i = 0; i < 8; i += 2) {
+        const ulonglong2 w = *reinterpret_cast<const ulonglong2*>(src + i);
+        v[i] = w.x;
+        v[i + 1] = w.y;
+      }
+      const int rowt = rowt0 + row;
+      unsigned char* tile =
+          base + ((size_t)(p * ntiles + t) * nks + gks) * kSlices * kATileBytes +
+          (rowt >> 3) * 256 + khalf * 128 + (rowt & 7) * 16;
+#pragma unroll
+      for (int d = 0; d < kSlices; ++d) {
+        uint32_t h[8];
+#pragma unroll
+        for (int i = 0; i < 8; ++i) h[i] = (uint32_t)(v[i] >> (16 * d)) & 0xFFFFu;
+        uint4 o;
+        o.x = h[0] | (h[1] << 16);
+        o.y = h[2] | (h[3] << 16);
+        o.z = h[4] | (h[5] << 16);
+        o.w = h[6] | (h[7] << 16);
+        *reinterpret_cast<uint4*>(tile + (size_t)d * kATileBytes) = o;
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// ------------------------------------------------------------------ split GEMM
+// CTA = (64-map group, parity x l-tile x K-chunk, q): one 128-row x 128-column output tile
+// over <= 64 k-steps of 16 rings.  Warp 4 lane 0 streams lambda and P digit tiles (bulk
+// async copies, kStagesG deep), warp 5 lane 0 issues the ten level-ordered UMMAs per k-step,
+// warps 0-3 run the epilogue.
+constexpr int kStagesG = 6;
+constexpr uint32_t kStageBytesG = 2 * kSlices * kATileBytes;    // 32 KB: A then B
+
+struct GemmArgs {
+  int lmax, nnorth, ngroups, nks_max, nkc_glob, q0, ntmax, nkcmax;
+  const int* ring_i0;
+  const long long* lam_off;
+  const FshtLamRow* tab;
+  const unsigned char* lbuf;
   const unsigned char* WS;
   const int* EB;
   double* alm;
-  int ld, k0, kc;      // alm map extent, chunk offset, maps in the chunk
+  int ld, k0, kc;
   double pa;
-  int accumulate;      // add into alm (iterations); with nkc > 1 alm is pre-zeroed
   int* err;
 };
 
-struct __align__(8) SplitSmemHdr {
-  uint64_t bfull[kStages], bempty[kStages], afull, aempty, tfull, tempty, fin;
+struct __align__(8) GemmSmemHdr {
+  uint64_t full[kStagesG], empty[kStagesG], tfull, fin;
   uint32_t tmem;
   int abort;
 };
 
-__global__ void __launch_bounds__(kThreads, 1) k_analysis_split(SplitArgs a) {
+__global__ void __launch_bounds__(kThreads, 1) k_split_gemm(GemmArgs a) {
   extern __shared__ __align__(1024) unsigned char smem[];
-  unsigned char* sA = smem;                                     // 128 KB
-  unsigned char* sB = smem + kABufBytes;                        // 3 x 16 KB
-  double* st_cur = reinterpret_cast<double*>(sB + kStages * kBStageBytes);
-  double* st_prev = st_cur + kKChunk;
-  int* st_e = reinterpret_cast<int*>(st_prev + kKChunk);
-  __shared__ SplitSmemHdr h;
-  __shared__ RecConst s_rc[2 * kRows];
-  __shared__ int s_ea[kRows];
+  __shared__ GemmSmemHdr h;
   __shared__ double s_cs[kCols];
+  __shared__ double s_rs[kRows];
+
+  const int g = blockIdx.x;
+  const int p = blockIdx.y & 1;
+  const int kci = (blockIdx.y >> 1) % a.nkcmax;
+  const int t = (blockIdx.y >> 1) / a.nkcmax;
+  const int q = a.q0 + blockIdx.z;
+  const int m = m_of_q(q, a.lmax);
+  const int i0 = a.ring_i0[m];
+  const int K = a.nnorth - i0;
+  const int nks = (K + kKStep - 1) / kKStep;
+  const int ntiles = (a.lmax - m + 1 + 2 * kRows - 1) / (2 * kRows);
+  const int ks0 = kci * (kKChunk / kKStep);
+  const int ks1 = min(nks, ks0 + kKChunk / kKStep);
+  if (t >= ntiles || ks0 >= ks1) return;          // uniform: before any barrier or TMEM
+  const int nk = ks1 - ks0;
+  const int lt0 = m + t * 2 * kRows;
 
   const int tid = threadIdx.x;
   const int warp = tid >> 5;
-  const int p = blockIdx.y / a.nkc;
-  const int kci = blockIdx.y % a.nkc;
-  const int g = blockIdx.z;
   volatile int* abort = &h.abort;
-
   if (tid == 0) {
-    for (int s = 0; s < kStages; ++s) {
-      tc::mbar_init(&h.bfull[s], 1);
-      tc::mbar_init(&h.bempty[s], 1);
+    for (int s = 0; s < kStagesG; ++s) {
+      tc::mbar_init(&h.full[s], 1);
+      tc::mbar_init(&h.empty[s], 1);
     }
-    tc::mbar_init(&h.afull, kSCRings);
-    tc::mbar_init(&h.aempty, 1);
     tc::mbar_init(&h.tfull, 1);
-    tc::mbar_init(&h.tempty, 128);
     tc::mbar_init(&h.fin, 1);
     h.abort = 0;
     tc::mbar_fence_init();
+  }
+  if (tid < kCols) {
+    const int eb = a.EB[(((long long)m * 2 + p) * a.ngroups + g) * kCols + tid];
+    s_cs[tid] = (eb == kEmptyExp) ? 0.0 : ldexp(a.pa, eb - 12);
+    const int l = lt0 + p + 2 * tid;
+    s_rs[tid] = (l <= a.lmax) ? a.tab[tri_off(m, a.lmax) + (l - m)].rs : 0.0;
   }
   if (warp == 0) tc::tmem_alloc(&h.tmem, 512);
   tc::tc_fence_before();
   __syncthreads();
   tc::tc_fence_after();
   const uint32_t tmem = h.tmem;
-  const uint32_t idesc = tc::umma_idesc_bf16(kRows, kCols);
 
-  // per-thread counters carrying mbarrier phases across m passes and l-tiles
-  uint32_t q_load = 0, q_mma = 0, sc_cnt = 0, tile_cnt = 0;
-
-  for (int pass = 0; pass < 2; ++pass) {
-    const int m = pass == 0 ? (int)blockIdx.x : a.lmax - (int)blockIdx.x;
-    if (pass == 1 && m == (int)blockIdx.x) break;
-    const int i0 = a.ring_i0[m];
-    const int Ktot = a.nnorth - i0;
-    const int r0 = kci * kKChunk;                 // first ring (relative to i0) of this chunk
-    const int K = min(kKChunk, Ktot - r0);        // rings in this chunk
-    if (K <= 0) continue;
-    const int t0 = r0 / kKStep;                   // first global k-step
-    const int nks = (K + kKStep - 1) / kKStep;
-    const int nsc = (K + kSCRings - 1) / kSCRings;
-    const int ntiles = (a.lmax - m + 1 + 2 * kRows - 1) / (2 * kRows);
-    const unsigned char* wsb =
-        a.WS + (((size_t)(m * 2 + p) * a.ngroups + g) * a.nks_max) * kSlices * kBTileBytes;
-    if (tid < 128) {
-      for (int r = tid; r < K; r += 128) {
-        double v;
-        int e;
-        rec_seed(a.sth[i0 + r0 + r], a.pref[m], m, v, e);
-        st_cur[r] = 0.0;   // lambda_{m-1}
-        st_prev[r] = v;    // the seed, consumed by the l = m step (a = 0, b = -1)
-        st_e[r] = e;
-      }
-      {
-        const int c = tid;
-        const int eb = a.EB[(((long long)m * 2 + p) * a.ngroups + g) * kCols + c];
-        s_cs[c] = (eb == kEmptyExp) ? 0.0 : ldexp(a.pa, eb - 12);
-      }
+  uint32_t n_loaded = 0;
+  if (tid == 128) {
+    const unsigned char* asrc =
+        a.lbuf + (size_t)(a.lam_off[q] - a.lam_off[a.q0]) * kSlices * kATileBytes +
+        ((size_t)(p * ntiles + t) * nks + ks0) * kSlices * kATileBytes;
+    const unsigned char* bsrc =
+        a.WS + ((((size_t)m * 2 + p) * a.ngroups + g) * a.nks_max + ks0) * kSlices * kBTileBytes;
+    for (int i = 0; i < nk; ++i) {
+      const uint32_t st = i % kStagesG;
+      if (!tc::mbar_wait(&h.empty[st], ((i / kStagesG) & 1) ^ 1, abort)) break;
+      unsigned char* dst = smem + st * kStageBytesG;
+      tc::mbar_arrive_expect_tx(&h.full[st], kStageBytesG);
+      tc::bulk_g2s(dst, asrc + (size_t)i * kSlices * kATileBytes, kSlices * kATileBytes,
+                   &h.full[st]);
+      tc::bulk_g2s(dst + kSlices * kATileBytes, bsrc + (size_t)i * kSlices * kBTileBytes,
+                   kSlices * kBTileBytes, &h.full[st]);
+      ++n_loaded;
     }
-    __syncthreads();
-
-    for (int tt = 0; tt < ntiles; ++tt) {
-      const int lt0 = m + tt * 2 * kRows;
-      if (tid < 128) {
-        for (int j = tid; j < 2 * kRows; j += 128) {
-          const int l = lt0 + j;
-          s_rc[j] = (l <= a.lmax) ? rec_coeffs(l, m) : RecConst{0.0, 0.0};
-        }
-        s_ea[tid] = row_exp(lt0 + p + 2 * tid);
-        asm volatile("bar.sync 1, 128;" ::: "memory");
-        // ---------------- producers: lambda digits for 128 rings at a time
-        for (int sc = 0; sc < nsc; ++sc, ++sc_cnt) {
-          if (!tc::mbar_wait(&h.aempty, (sc_cnt & 1) ^ 1, abort)) break;
-          const int r = sc * kSCRings + tid;
-          const int ks = tid / kKStep, kk = tid % kKStep;
-          unsigned char* col = sA + ks * kSlices * kATileBytes + (kk >> 3) * 128 + (kk & 7) * 2;
-          if (r < K) {
-            double cur = st_cur[r], prev = st_prev[r];
-            int e = st_e[r];
-            const double cth = a.cth[i0 + r0 + r];
-            for (int j2 = 0; j2 < 2 * kRows; ++j2) {
-              const int l = lt0 + j2;
-              double lam = 0.0;
-              if (l <= a.lmax) {
-                const double nx = s_rc[j2].a * cth * cur - s_rc[j2].b * prev;
-                prev = cur;
-                cur = nx;
-                if (e < 0 && fabs(cur) > 0x1p300) {
-                  cur *= 0x1p-600;
-                  prev *= 0x1p-600;
-                  ++e;
-                }
-                lam = (e == 0) ? cur : 0.0;
-              }
-              if ((j2 & 1) == p) {
-                const int row = j2 >> 1;
-                uint16_t dg[4];
-                tc::digits4(lam, s_ea[row], dg);
-                unsigned char* dst = col + (row >> 3) * 256 + (row & 7) * 16;
+  } else if (tid == 160) {
+    const uint32_t idesc = tc::umma_idesc_bf16(kRows, kCols);
+    const uint32_t s_u = tc::smem_u32(smem);
+    for (int i = 0; i < nk; ++i) {
+      const uint32_t st = i % kStagesG;
+      if (!tc::mbar_wait(&h.full[st], (i / kStagesG) & 1, abort)) break;
+      tc::tc_fence_after();
+      const uint32_t abase = s_u + st * kStageBytesG;
+      const uint32_t bbase = abase + kSlices * kATileBytes;
 #pragma unroll
-                for (int s = 0; s < kSlices; ++s)
-                  *reinterpret_cast<uint16_t*>(dst + s * kATileBytes) = dg[s];
-              }
-            }
-            st_cur[r] = cur;
-            st_prev[r] = prev;
-            st_e[r] = e;
-          } else {
-            for (int row = 0; row < kRows; ++row) {
-              unsigned char* dst = col + (row >> 3) * 256 + (row & 7) * 16;
+      for (int lev = 0; lev <= 3; ++lev) {
 #pragma unroll
-              for (int s = 0; s < kSlices; ++s)
-                *reinterpret_cast<uint16_t*>(dst + s * kATileBytes) = 0;
-            }
-          }
-          tc::fence_proxy_async();
-          tc::mbar_arrive(&h.afull);
+        for (int aa = 0; aa <= lev; ++aa) {
+          const uint64_t ad = tc::umma_desc(abase + aa * kATileBytes, 128, 256);
+          const uint64_t bd = tc::umma_desc(bbase + (lev - aa) * kBTileBytes, 128, 256);
+          tc::umma_bf16(tmem + lev * kCols, ad, bd, idesc, (i > 0 || aa > 0) ? 1u : 0u);
         }
-      } else if (tid == 128) {
-        // ---------------- P tiles: bulk async copies, kStages-deep ring
-        for (int t = 0; t < nks; ++t, ++q_load) {
-          const uint32_t st = q_load % kStages;
-          if (!tc::mbar_wait(&h.bempty[st], ((q_load / kStages) & 1) ^ 1, abort)) break;
-          tc::mbar_arrive_expect_tx(&h.bfull[st], kBStageBytes);
-          tc::bulk_g2s(sB + st * kBStageBytes, wsb + (size_t)(t0 + t) * kSlices * kBTileBytes,
-                       kBStageBytes, &h.bfull[st]);
-        }
-      } else if (tid == 160) {
-        // ---------------- UMMA issue: level L digit products into accumulator L
-        bool ok = tc::mbar_wait(&h.tempty, (tile_cnt & 1) ^ 1, abort);
-        tc::tc_fence_after();
-        const uint32_t sA_u = tc::smem_u32(sA), sB_u = tc::smem_u32(sB);
-        int t = 0;
-        uint32_t started = 0;   // bit L: accumulator L written in this tile
-        for (int sc = 0; ok && sc < nsc; ++sc) {
-          ok = tc::mbar_wait(&h.afull, (sc_cnt + sc) & 1, abort);
-          if (!ok) break;
-          tc::tc_fence_after();
-          for (int ks = 0; ks < kSCSteps && t < nks; ++ks, ++t, ++q_mma) {
-            const uint32_t st = q_mma % kStages;
-            ok = tc::mbar_wait(&h.bfull[st], (q_mma / kStages) & 1, abort);
-            if (!ok) break;
-            tc::tc_fence_after();
-            const uint32_t abase = sA_u + ks * kSlices * kATileBytes;
-            const uint32_t bbase = sB_u + st * kBStageBytes;
-#pragma unroll
-            for (int lev = 0; lev <= 3; ++lev) {
-#pragma unroll
-              for (int aa = 0; aa <= lev; ++aa) {
-                const int bb = lev - aa;
-                const uint64_t ad = tc::umma_desc(abase + aa * kATileBytes, 128, 256);
-                const uint64_t bd = tc::umma_desc(bbase + bb * kBTileBytes, 128, 256);
-                tc::umma_bf16(tmem + lev * kCols, ad, bd, idesc, (started >> lev) & 1u);
-                started |= 1u << lev;
-              }
-            }
-            tc::umma_commit(&h.bempty[st]);
-          }
-          tc::umma_commit(&h.aempty);
-        }
-        tc::umma_commit(&h.tfull);
       }
-      if (tid >= 128) sc_cnt += nsc;   // the producers advanced it in their loop
-      // ---------------- epilogue (warps 0-3): TMEM -> alm
-      if (tid < 128) {
-        bool ok = tc::mbar_wait(&h.tfull, tile_cnt & 1, abort);
-        ok = __all_sync(0xffffffffu, ok);   // tcgen05.ld below is warp-collective
-        tc::tc_fence_after();
-        const int row = (warp << 5) + (tid & 31);
-        const int l = lt0 + p + 2 * row;
-        const bool rowok = l <= a.lmax;
-        if (ok) {
-          const double rs = ldexp(1.0, s_ea[row]);
-          const long long L1 = a.lmax + 1;
-          const uint32_t lane_base = tmem + ((uint32_t)(warp << 5) << 16);
-          for (int c0 = 0; c0 < kCols; c0 += 16) {
-            uint32_t v0[16], v1[16], v2[16], v3[16];
-            tc::tmem_ld16(lane_base + 0 * kCols + c0, v0);
-            tc::tmem_ld16(lane_base + 1 * kCols + c0, v1);
-            tc::tmem_ld16(lane_base + 2 * kCols + c0, v2);
-            tc::tmem_ld16(lane_base + 3 * kCols + c0, v3);
-            tc::tmem_wait_ld();
-            const int comp = c0 >> 6;
-            const bool store = rowok && !(comp == 1 && m == 0);
-            const long long rowidx =
-                comp == 0 ? ((long long)m * L1 + l) : ((L1 - m) * L1 + (l - m));
-#pragma unroll
-            for (int j = 0; j < 16; ++j) {
-              const int c = c0 + j;
-              const int k = g * kGroupMaps + (c & 63);
-              if (store && k < a.kc) {
-                // levels 0 and 1 are exact integers: their weighted sum is exact in
-                // FP32 as a (hi, lo) pair; levels 2 and 3 only touch lo.
-                const float L0 = __uint_as_float(v0[j]);
-                const float L1f = __uint_as_float(v1[j]) * 0x1p-8f;
-                const float hi = L0 + L1f;
-                const float bv = hi - L0;
-                const float lo = ((L0 - (hi - bv)) + (L1f - bv)) +
-                                 (__uint_as_float(v2[j]) * 0x1p-16f +
-                                  __uint_as_float(v3[j]) * 0x1p-24f);
-                const double v = ((double)hi + (double)lo) * rs * s_cs[c];
-                double* dst = a.alm + rowidx * a.ld + a.k0 + k;
-                if (a.nkc > 1) atomicAdd(dst, v);
-                else if (a.accumulate) *dst += v;
-                else *dst = v;
-              }
-            }
-          }
-        }
-        tc::tc_fence_before();
-        tc::mbar_arrive(&h.tempty);
-      }
-      ++tile_cnt;
-      if (*abort) break;
+      tc::umma_commit(&h.empty[st]);
     }
-    __syncthreads();
-    if (*abort) break;
+    tc::umma_commit(&h.tfull);
   }
-  // drain: the UMMA issuer waits for its last products before TMEM is released, and
-  // the loader for its last copies
+  // ---------------- epilogue (warps 0-3): TMEM -> alm
+  if (tid < 128) {
+    bool ok = tc::mbar_wait(&h.tfull, 0, abort);
+    ok = __all_sync(0xffffffffu, ok);      // tcgen05.ld below is warp-collective
+    tc::tc_fence_after();
+    const int row = (warp << 5) + (tid & 31);
+    const int l = lt0 + p + 2 * row;
+    const bool rowok = l <= a.lmax;
+    if (ok) {
+      const double rs = s_rs[row];
+      const long long L1 = a.lmax + 1;
+      const uint32_t lane_base = tmem + ((uint32_t)(warp << 5) << 16);
+      for (int c0 = 0; c0 < kCols; c0 += 16) {
+        uint32_t v0[16], v1[16], v2[16], v3[16];
+        tc::tmem_ld16(lane_base + 0 * kCols + c0, v0);
+        tc::tmem_ld16(lane_base + 1 * kCols + c0, v1);
+        tc::tmem_ld16(lane_base + 2 * kCols + c0, v2);
+        tc::tmem_ld16(lane_base + 3 * kCols + c0, v3);
+        tc::tmem_wait_ld();
+        const int comp = c0 >> 6;
+        const bool store = rowok && !(comp == 1 && m == 0);
+        const long long rowidx = comp == 0 ? ((long long)m * L1 + l) : ((L1 - m) * L1 + (l - m));
+#pragma unroll
+        for (int j = 0; j < 16; ++j) {
+          const int c = c0 + j;
+          const int k = g * kGroupMaps + (c & 63);
+          if (store && k < a.kc) {
+            // levels 0 and 1 are exact integers: their weighted sum is exact in FP32 as
+            // a (hi, lo) pair; levels 2 and 3 only touch lo.
+            const float L0 = __uint_as_float(v0[j]);
+            const float L1f = __uint_as_float(v1[j]) * 0x1p-8f;
+            const float hi = L0 + L1f;
+            const float bv = hi - L0;
+            const float lo = ((L0 - (hi - bv)) + (L1f - bv)) +
+                             (__uint_as_float(v2[j]) * 0x1p-16f + __uint_as_float(v3[j]) * 0x1p-24f);
+            const double v = ((double)hi + (double)lo) * rs * s_cs[c];
+            double* dst = a.alm + rowidx * a.ld + a.k0 + k;
+            if (a.nkc_glob > 1) atomicAdd(dst, v);
+            else *dst = v;
+          }
+        }
+      }
+    }
+  }
+  // drain: the UMMA issuer waits for its last products before TMEM is released, and the
+  // loader for its last copies
   if (tid == 160) {
     tc::umma_commit(&h.fin);
     for (uint32_t it = 0; it < tc::kWaitLimit; ++it)
       if (tc::mbar_try_wait(&h.fin, 0)) break;
   }
   if (tid == 128) {
-    for (uint32_t d = 0; d < (uint32_t)kStages && d < q_load; ++d) {
-      const uint32_t q = q_load - 1 - d;
+    for (uint32_t d = 0; d < (uint32_t)kStagesG && d < n_loaded; ++d) {
+      const uint32_t i = n_loaded - 1 - d;
       for (uint32_t it = 0; it < tc::kWaitLimit; ++it)
-        if (tc::mbar_try_wait(&h.bfull[q % kStages], (q / kStages) & 1)) break;
+        if (tc::mbar_try_wait(&h.full[i % kStagesG], (i / kStagesG) & 1)) break;
     }
   }
   tc::tc_fence_before();
@@ -449,21 +513,97 @@ int fsht_launch_split_prepare(fsht_plan* p, const double2* W, unsigned char* WS,
   return FSHT_OK;
 }
 
-int fsht_launch_analysis_split(fsht_plan* p, const unsigned char* WS, const int* EB, double* alm,
-                               int nmaps_total, int k0, int kc, int accumulate, cudaStream_t s) {
-  const int ngroups = (kc + kGroupMaps - 1) / kGroupMaps;
-  const int nks_max = (p->nnorth + kKStep - 1) / kKStep;
-  const int nkc = (p->nnorth + kKChunk - 1) / kKChunk;
-  SplitArgs a;
+// ------------------------------------------------------------------ host side
+namespace {
+constexpr size_t kLbufCap = 2ull << 30;     // lambda-digit staging per wave
+}
+
+int fsht_split_tables_init(fsht_plan* p) {
+  const int lmax = p->lmax;
+  const size_t ntab = (size_t)tri_off(lmax + 1, lmax);
+  FSHT_CUDA_TRY(cudaMalloc(&p->d_lamtab, sizeof(FshtLamRow) * (ntab ? ntab : 1)));
+  FSHT_CUDA_TRY(cudaMalloc(&p->d_lam_off, sizeof(long long) * (lmax + 2)));
+  k_lam_table<<<(lmax + 1 + 127) / 128, 128, 0, p->stream>>>(lmax, p->d_lamtab);
+  FSHT_LAUNCH_CHECK();
+  // per q (pair order): 16 KB units of the lambda digit tiles of m(q)
+  std::vector<long long> off(lmax + 2, 0);
+  std::vector<int> ntl(lmax + 1), nkm(lmax + 1);
+  for (int q = 0; q <= lmax; ++q) {
+    const int m = (q & 1) ? lmax - (q >> 1) : (q >> 1);
+    const int K = p->nnorth - p->h_ring_i0[m];
+    ntl[q] = (lmax - m + 1 + 2 * kRows - 1) / (2 * kRows);
+    nkm[q] = K > 0 ? (K + kKStep - 1) / kKStep : 0;
+    off[q + 1] = off[q] + 2LL * ntl[q] * nkm[q];
+  }
+  const size_t unit = (size_t)kSlices * kATileBytes;
+  size_t cap_units = kLbufCap / unit;
+  // waves: consecutive q ranges whose tiles fit the staging buffer
+  std::vector<int> waves;
+  size_t lbuf_units = 0;
+  for (int q0 = 0; q0 <= lmax;) {
+    int q1 = q0 + 1;
+    while (q1 <= lmax && (size_t)(off[q1 + 1] - off[q0]) <= cap_units) ++q1;
+    int ntmax = 0, nkc = 0, nrb = 0;
+    for (int q = q0; q < q1; ++q) {
+      ntmax = std::max(ntmax, ntl[q]);
+      nkc = std::max(nkc, (nkm[q] * kKStep + kKChunk - 1) / kKChunk);
+      nrb = std::max(nrb, (nkm[q] * kKStep + kSCRings - 1) / kSCRings);
+    }
+    waves.insert(waves.end(), {q0, q1, ntmax, nkc, nrb});
+    lbuf_units = std::max(lbuf_units, (size_t)(off[q1] - off[q0]));
+    q0 = q1;
+  }
+  p->nwaves = (int)waves.size() / 5;
+  p->h_waves = new (std::nothrow) int[waves.size()];
+  if (!p->h_waves) {
+    fsht_set_error("host allocation failed");
+    return FSHT_ENOMEM;
+  }
+  std::copy(waves.begin(), waves.end(), p->h_waves);
+  p->lbuf_bytes = std::max<size_t>(lbuf_units * unit, 256);
+  FSHT_CUDA_TRY(cudaMemcpyAsync(p->d_lam_off, off.data(), sizeof(long long) * (lmax + 2),
+                                cudaMemcpyHostToDevice, p->stream));
+  FSHT_CUDA_TRY(cudaStreamSynchronize(p->stream));   // off[] is a stack vector
+  return FSHT_OK;
+}
+
+int fsht_launch_split_lambda(fsht_plan* p, int w, unsigned char* lbuf, cudaStream_t s) {
+  const int* wv = p->h_waves + 5 * w;
+  LamArgs a;
   a.lmax = p->lmax;
   a.nnorth = p->nnorth;
-  a.ngroups = ngroups;
-  a.nks_max = nks_max;
-  a.nkc = nkc;
+  a.q0 = wv[0];
   a.cth = p->d_cth;
   a.sth = p->d_sth;
   a.pref = p->d_pref;
   a.ring_i0 = p->d_ring_i0;
+  a.tab = p->d_lamtab;
+  a.lam_off = p->d_lam_off;
+  a.lbuf = lbuf;
+  if (wv[4] == 0) return FSHT_OK;
+  k_lambda_digits<<<dim3(wv[1] - wv[0], wv[4]), 128, 0, s>>>(a);
+  FSHT_LAUNCH_CHECK();
+  return FSHT_OK;
+}
+
+int fsht_launch_split_gemm(fsht_plan* p, int w, const unsigned char* WS, const int* EB,
+                           const unsigned char* lbuf, double* alm, int nmaps_total, int k0,
+                           int kc, cudaStream_t s) {
+  const int* wv = p->h_waves + 5 * w;
+  if (wv[3] == 0) return FSHT_OK;
+  GemmArgs a;
+  a.lmax = p->lmax;
+  a.nnorth = p->nnorth;
+  a.ngroups = (kc + kGroupMaps - 1) / kGroupMaps;
+  a.nks_max = (p->nnorth + kKStep - 1) / kKStep;
+  a.nkc_glob = (p->nnorth + kKChunk - 1) / kKChunk;
+  a.q0 = wv[0];
+  a.ntmax = wv[2];
+  a.nkcmax = wv[3];
+  a.ring_i0 = p->d_ring_i0;
+  a.lam_off = p->d_lam_off;
+  a.tab = p->d_lamtab;
+  a.lbuf = lbuf;
   a.WS = WS;
   a.EB = EB;
   a.alm = alm;
@@ -471,13 +611,11 @@ int fsht_launch_analysis_split(fsht_plan* p, const unsigned char* WS, const int*
   a.k0 = k0;
   a.kc = kc;
   a.pa = p->pa;
-  a.accumulate = accumulate;
   a.err = p->d_err;
-  const size_t sm = kABufBytes + kStages * kBStageBytes + (size_t)kKChunk * 20 + 1024;
-  FSHT_CUDA_TRY(cudaFuncSetAttribute(k_analysis_split, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     (int)sm));
-  const int npair = (p->lmax + 2) / 2;
-  k_analysis_split<<<dim3(npair, 2 * nkc, ngroups), kThreads, sm, s>>>(a);
+  const size_t sm = (size_t)kStagesG * kStageBytesG;
+  FSHT_CUDA_TRY(
+      cudaFuncSetAttribute(k_split_gemm, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+  k_split_gemm<<<dim3(a.ngroups, 2 * a.ntmax * a.nkcmax, wv[1] - wv[0]), kThreads, sm, s>>>(a);
   FSHT_LAUNCH_CHECK();
   return FSHT_OK;
 }

@@ -86,6 +86,10 @@ void free_plan_memory(fsht_plan* p) {
   cudaFree(p->d_err);
   cudaFree(p->d_ws);
   cudaFree(p->d_eb);
+  cudaFree(p->d_lamtab);
+  cudaFree(p->d_lam_off);
+  cudaFree(p->d_lbuf);
+  delete[] p->h_waves;
   delete[] p->h_ring_i0;
   if (p->prof) {
     for (auto& v : p->prof->pending)
@@ -132,6 +136,10 @@ double2* work_buf(fsht_plan* p, int b, int kc) {
 int check_call(fsht_plan* p, int nmaps, const void* a, const void* b) {
   int rc = check_plan(p);
   if (rc) return rc;
+  if (p->kchunk < 1 || !p->d_work) {
+    fsht_set_error("this plan holds no workspace (created with FSHT_FLAG_TABLES_ONLY)");
+    return FSHT_EINVAL;
+  }
   if (nmaps < 1 || nmaps > p->nmaps_max) {
     fsht_set_error("nmaps = %d outside [1, %d] of this plan", nmaps, p->nmaps_max);
     return FSHT_EINVAL;
@@ -262,6 +270,7 @@ int fsht_plan_create(int nside, int lmax, int nmaps_max, int flags, int precisio
   }
   if ((rc = fsht_launch_ring_skip(p, p->stream))) return fail(rc);
   if ((rc = fsht_fft_tables_init(p))) return fail(rc);
+  if (precision == FSHT_PREC_SPLIT && (rc = fsht_split_tables_init(p))) return fail(rc);
   // ---- workspace: nbuf phase matrices of kchunk maps (+ the sliced copy for the
   // split form, sized in groups of 128 maps)
   const size_t limit = workspace_limit_bytes
@@ -270,27 +279,31 @@ int fsht_plan_create(int nside, int lmax, int nmaps_max, int flags, int precisio
   const size_t per_map = per_map_buffer_bytes(p) * p->nbuf;
   auto need = [&](size_t k) -> size_t {
     size_t b = per_map * k;
-    if (precision == FSHT_PREC_SPLIT) b += fsht_split_ws_bytes(lmax, p->nnorth, (int)k);
+    if (precision == FSHT_PREC_SPLIT)
+      b += fsht_split_ws_bytes(lmax, p->nnorth, (int)k) + fsht_split_eb_bytes(lmax, (int)k) +
+           p->lbuf_bytes;
     return b;
   };
+  const bool tables_only = (flags & FSHT_FLAG_TABLES_ONLY) != 0;
   size_t kc = (size_t)nmaps_max;
   while (kc > 1 && need(kc) > limit) kc = (kc > 128 && kc % 128) ? kc - kc % 128 : kc - (kc > 128 ? 128 : 1);
-  if (need(kc) > limit) {
+  if (!tables_only && need(kc) > limit) {
     fsht_set_error("workspace limit %zu bytes is below one map's %zu bytes", limit, need(1));
     return fail(FSHT_EINVAL);
   }
-  p->kchunk = (int)kc;
-  p->work_bytes = per_map * kc;
-  if ((rc = dalloc((void**)&p->d_work, p->work_bytes))) return fail(rc);
+  p->kchunk = tables_only ? 0 : (int)kc;
+  p->work_bytes = tables_only ? 0 : per_map * kc;
+  if (!tables_only && (rc = dalloc((void**)&p->d_work, p->work_bytes))) return fail(rc);
   if ((rc = dalloc((void**)&p->d_err, sizeof(int)))) return fail(rc);
   if ((ce = cudaMemsetAsync(p->d_err, 0, sizeof(int), p->stream)) != cudaSuccess) {
     fsht_set_error("memset: %s", cudaGetErrorString(ce));
     return fail(FSHT_ECUDA);
   }
-  if (precision == FSHT_PREC_SPLIT) {
+  if (precision == FSHT_PREC_SPLIT && !tables_only) {
     p->ws_bytes = fsht_split_ws_bytes(lmax, p->nnorth, p->kchunk);
     if ((rc = dalloc((void**)&p->d_ws, p->ws_bytes))) return fail(rc);
     if ((rc = dalloc((void**)&p->d_eb, fsht_split_eb_bytes(lmax, p->kchunk)))) return fail(rc);
+    if ((rc = dalloc((void**)&p->d_lbuf, p->lbuf_bytes))) return fail(rc);
   }
   if ((ce = cudaStreamSynchronize(p->stream)) != cudaSuccess) {
     fsht_set_error("plan setup: %s", cudaGetErrorString(ce));
@@ -447,10 +460,16 @@ int fsht_t2alm(fsht_plan* p, const double* maps, double* alm, int nmaps, int nit
         FSHT_TRY(fsht_launch_split_prepare(p, W0, p->d_ws, p->d_eb, alm, nmaps, c0, kc, 0,
                                            p->stream));
       }
-      {
-        FSHT_PROF(FSHT_KCAT_ANALYSIS);
-        FSHT_TRY(fsht_launch_analysis_split(p, p->d_ws, p->d_eb, alm, nmaps, c0, kc, 0,
-                                            p->stream));
+      for (int w = 0; w < p->nwaves; ++w) {
+        {
+          FSHT_PROF(FSHT_KCAT_LAMBDA);
+          FSHT_TRY(fsht_launch_split_lambda(p, w, p->d_lbuf, p->stream));
+        }
+        {
+          FSHT_PROF(FSHT_KCAT_ANALYSIS);
+          FSHT_TRY(fsht_launch_split_gemm(p, w, p->d_ws, p->d_eb, p->d_lbuf, alm, nmaps, c0, kc,
+                                          p->stream));
+        }
       }
     }
     return FSHT_OK;

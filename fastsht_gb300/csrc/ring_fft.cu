@@ -559,11 +559,11 @@ int fsht_launch_ring_fft_fwd(fsht_plan* p, const double* maps, long long map_str
   a.bhat = p->d_bhat;
   a.ring_i0 = p->d_ring_i0;
   a.W = W;
-  a.maps_per_block = maps_per_block_for(kc, p->nnorth);
+  a.maps_per_block = p->fft_mpb > 0 ? p->fft_mpb : maps_per_block_for(kc, p->nnorth);
   dim3 grid(p->nnorth, (kc + a.maps_per_block - 1) / a.maps_per_block);
   FSHT_CUDA_TRY(cudaFuncSetAttribute(k_ring_fft_fwd, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      (int)p->fft_smem));
-  k_ring_fft_fwd<<<grid, 512, p->fft_smem, s>>>(a);
+  k_ring_fft_fwd<<<grid, p->fft_threads > 0 ? p->fft_threads : 512, p->fft_smem, s>>>(a);
   FSHT_LAUNCH_CHECK();
   return FSHT_OK;
 }
@@ -586,11 +586,11 @@ int fsht_launch_ring_fft_inv(fsht_plan* p, const double2* W, double* maps, long 
   a.chirp = p->d_chirp;
   a.bhat = p->d_bhat;
   a.ring_i0 = p->d_ring_i0;
-  a.maps_per_block = maps_per_block_for(kc, p->nnorth);
+  a.maps_per_block = p->fft_mpb > 0 ? p->fft_mpb : maps_per_block_for(kc, p->nnorth);
   dim3 grid(p->nnorth, (kc + a.maps_per_block - 1) / a.maps_per_block);
   FSHT_CUDA_TRY(cudaFuncSetAttribute(k_ring_fft_inv, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      (int)p->fft_smem));
-  k_ring_fft_inv<<<grid, 512, p->fft_smem, s>>>(a);
+  k_ring_fft_inv<<<grid, p->fft_threads > 0 ? p->fft_threads : 512, p->fft_smem, s>>>(a);
   FSHT_LAUNCH_CHECK();
   return FSHT_OK;
 }
@@ -608,11 +608,11 @@ int fsht_launch_fourier_residual(fsht_plan* p, const double2* X, double2* GR, in
   a.prefix = prefix;
   a.rfs = p->d_rfft;
   a.ring_i0 = p->d_ring_i0;
-  a.maps_per_block = maps_per_block_for(kc, p->nnorth);
+  a.maps_per_block = p->fft_mpb > 0 ? p->fft_mpb : maps_per_block_for(kc, p->nnorth);
   dim3 grid(p->nnorth, (kc + a.maps_per_block - 1) / a.maps_per_block);
   FSHT_CUDA_TRY(cudaFuncSetAttribute(k_fourier_residual,
                                      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p->fft_smem));
-  k_fourier_residual<<<grid, 512, p->fft_smem, s>>>(a);
+  k_fourier_residual<<<grid, p->fft_threads > 0 ? p->fft_threads : 512, p->fft_smem, s>>>(a);
   FSHT_LAUNCH_CHECK();
   return FSHT_OK;
 }

@@ -1,0 +1,343 @@
+"""Serving form: a continuous-batching request loop for mixed-size transforms.
+
+Requests (map2alm / alm2map, T or Q/U, any supported nside / lmax / nmaps, FP64 or
+split precision) are admitted while earlier ones are still on the GPU, as soon as
+a stream slot and enough of the HBM budget are free; admitted requests run
+concurrently on their slots' streams.  Inputs and results stay resident on the
+device (CUDA tensors); host arrays are copied in on the request's stream.  A
+request whose footprint exceeds the whole budget is split along maps.  Each
+request records arrival, admission and completion times, from which the server
+reports p50 / p99 latency beside throughput.
+
+No counterpart in the reference (one SHT instance, one blocking call at a time,
+SHT.py:16-227); every transform runs through the C ABI's fsht_run_job on a shared
+table-only plan per (nside, lmax, precision).
+"""
+from __future__ import annotations
+
+import collections
+import ctypes as C
+import threading
+import time
+from concurrent.futures import Future
+from dataclasses import dataclass, field
+
+import numpy as np
+import torch
+
+from . import _lib
+
+_KINDS = {"t2alm": _lib.FSHT_JOB_T2ALM, "alm2t": _lib.FSHT_JOB_ALM2T,
+          "qu2eb": _lib.FSHT_JOB_QU2EB, "eb2qu": _lib.FSHT_JOB_EB2QU}
+
+
+@dataclass
+class Request:
+    kind: str
+    nside: int
+    lmax: int
+    nmaps: int
+    precision: str
+    inputs: list                      # device tensors in the library layout
+    t_arrival: float
+    future: Future = field(default_factory=Future)
+    outputs: list = field(default_factory=list)
+    t_admit: float = 0.0
+    t_done: float = 0.0
+    parts: int = 1                    # sub-requests (split along maps)
+    ready: torch.cuda.Event = None    # inputs written (submitting thread's stream)
+
+    @property
+    def nfields(self):
+        return 2 if self.kind in ("qu2eb", "eb2qu") else 1
+
+    @property
+    def analysis(self):
+        return self.kind in ("t2alm", "qu2eb")
+
+
+@dataclass
+class _Part:
+    req: Request
+    m0: int
+    m1: int
+    inputs: list
+    outputs: list
+    workspace: torch.Tensor = None
+    event: torch.cuda.Event = None
+    slot: int = -1
+    nbytes: int = 0
+
+
+def _maps_shape(nside, nmaps):
+    return (nmaps, 12 * nside * nside)
+
+
+def _alm_shape(lmax, nmaps):
+    return (lmax + 1, lmax + 1, nmaps)
+
+
+class Server:
+    """Continuous-batching SHT server on one GPU.
+
+    hbm_budget: device bytes the server may hold for in-flight requests (inputs,
+    outputs and workspaces); nslots: concurrent CUDA streams.
+    """
+
+    def __init__(self, hbm_budget=150e9, nslots=8, device=None, poll_s=5e-5):
+        self.device = torch.device("cuda", torch.cuda.current_device() if device is None else device)
+        self.budget = int(hbm_budget)
+        self.nslots = nslots
+        self.poll_s = poll_s
+        with torch.cuda.device(self.device):
+            self.streams = [torch.cuda.Stream(self.device) for _ in range(nslots)]
+        self._plans = {}
+        self._pending = collections.deque()
+        self._inflight: list[_Part] = []
+        self._free_slots = list(range(nslots))
+        self._used = 0
+        self.high_water = 0
+        self.max_inflight = 0
+        self.completed: list[Request] = []
+        self._lock = threading.Condition()
+        self._stop = False
+        self._error = None
+        self._thread = threading.Thread(target=self._loop, name="fsht-server", daemon=True)
+        self._thread.start()
+
+    # ------------------------------------------------------------ client side
+    def submit(self, kind, nside, lmax, inputs, precision="fp64", t_arrival=None) -> Future:
+        """inputs: list of CUDA float64 tensors (maps (nmaps, npix) or alm
+        (lmax+1, lmax+1, nmaps), contiguous) or NumPy arrays in the reference's
+        Fortran layout (copied to the device on admission)."""
+        if kind not in _KINDS:
+            raise ValueError(f"kind must be one of {sorted(_KINDS)}")
+        if precision not in ("fp64", "split"):
+            raise ValueError("precision must be 'fp64' or 'split'")
+        nf = 2 if kind in ("qu2eb", "eb2qu") else 1
+        if len(inputs) != nf:
+            raise ValueError(f"{kind} takes {nf} input field(s)")
+        ins = []
+        for x in inputs:
+            if isinstance(x, torch.Tensor):
+                if not (x.is_cuda and x.dtype == torch.float64 and x.is_contiguous()):
+                    raise ValueError("device inputs must be contiguous float64 CUDA tensors")
+                ins.append(x)
+            else:
+                ins.append(np.ascontiguousarray(np.asarray(x, dtype=np.float64).T))
+        nmaps = ins[0].shape[0] if kind in ("t2alm", "qu2eb") else ins[0].shape[-1]
+        req = Request(kind, int(nside), int(lmax), int(nmaps), precision, ins,
+                      time.perf_counter() if t_arrival is None else t_arrival)
+        if any(isinstance(x, torch.Tensor) for x in ins):
+            # device inputs may still be in flight on the caller's stream
+            req.ready = torch.cuda.Event()
+            req.ready.record(torch.cuda.current_stream(self.device))
+        with self._lock:
+            if self._error:
+                raise RuntimeError(f"server failed: {self._error}")
+            self._pending.append(req)
+            self._lock.notify()
+        return req.future
+
+    def drain(self, timeout=None):
+        """Block until every submitted request has completed."""
+        t0 = time.perf_counter()
+        with self._lock:
+            while self._pending or self._inflight:
+                if self._error:
+                    raise RuntimeError(f"server failed: {self._error}")
+                self._lock.wait(0.01)
+                if timeout is not None and time.perf_counter() - t0 > timeout:
+                    raise TimeoutError("drain timed out")
+
+    def close(self):
+        with self._lock:
+            self._stop = True
+            self._lock.notify()
+        self._thread.join()
+        for p in self._plans.values():
+            _lib.load().fsht_plan_destroy(p)
+        self._plans.clear()
+
+    def stats(self):
+        lat = np.array([r.t_done - r.t_arrival for r in self.completed])
+        if lat.size == 0:
+            return {}
+        t0 = min(r.t_arrival for r in self.completed)
+        t1 = max(r.t_done for r in self.completed)
+        mapsht = sum(r.nmaps * r.nfields for r in self.completed)
+        return {"requests": int(lat.size), "p50_ms": float(np.percentile(lat, 50) * 1e3),
+                "p99_ms": float(np.percentile(lat, 99) * 1e3),
+                "mean_ms": float(lat.mean() * 1e3), "wall_s": t1 - t0,
+                "requests_per_s": lat.size / (t1 - t0),
+                "maps_sht_per_s": mapsht / (t1 - t0),
+                "high_water_bytes": self.high_water, "budget_bytes": self.budget,
+                "max_inflight": self.max_inflight}
+
+    # ------------------------------------------------------------ internals
+    def _plan(self, nside, lmax, precision):
+        key = (nside, lmax, precision)
+        p = self._plans.get(key)
+        if p is None:
+            p = C.c_void_p()
+            with torch.cuda.device(self.device):
+                _lib.call("fsht_plan_create", nside, lmax, 1, _lib.FSHT_FLAG_TABLES_ONLY,
+                          _lib.FSHT_PREC_SPLIT if precision == "split" else _lib.FSHT_PREC_FP64,
+                          0, None, C.byref(p))
+            self._plans[key] = p
+        return p
+
+    def _job(self, req, m0, m1, ins, outs):
+        j = _lib.FshtJob()
+        j.nside, j.lmax, j.nmaps = req.nside, req.lmax, m1 - m0
+        j.kind = _KINDS[req.kind]
+        j.precision = _lib.FSHT_PREC_SPLIT if req.precision == "split" else _lib.FSHT_PREC_FP64
+        j.in0 = ins[0].data_ptr()
+        j.in1 = ins[1].data_ptr() if len(ins) > 1 else None
+        j.out0 = outs[0].data_ptr()
+        j.out1 = outs[1].data_ptr() if len(outs) > 1 else None
+        return j
+
+    def _io_bytes(self, req, n):
+        npix = 12 * req.nside ** 2
+        L = req.lmax + 1
+        return 8 * n * (npix + L * L) * req.nfields
+
+    def _workspace_bytes(self, req, n, kc):
+        plan = self._plan(req.nside, req.lmax, req.precision)
+        j = _lib.FshtJob()
+        j.nside, j.lmax, j.nmaps, j.kind = req.nside, req.lmax, n, _KINDS[req.kind]
+        j.precision = _lib.FSHT_PREC_SPLIT if req.precision == "split" else _lib.FSHT_PREC_FP64
+        b = C.c_size_t()
+        _lib.call("fsht_job_workspace", plan, C.byref(j), kc, C.byref(b))
+        return int(b.value)
+
+    def _fit(self, req, avail):
+        """Largest (maps, maps-per-chunk) of req's remaining maps whose footprint fits."""
+        n = req.nmaps - req._next
+        while n >= 1:
+            kc = min(n, 128)
+            while kc >= 1:
+                need = self._io_bytes(req, n) + self._workspace_bytes(req, n, kc)
+                if need <= avail:
+                    return n, kc, need
+                kc //= 2
+            n //= 2
+        return None
+
+    def _admit_one(self, req) -> bool:
+        if not self._free_slots:
+            return False
+        avail = self.budget - self._used
+        fit = self._fit(req, avail)
+        if fit is None:
+            if self._used == 0:
+                raise RuntimeError(f"request (nside {req.nside}, lmax {req.lmax}) does not fit "
+                                   f"the {self.budget}-byte budget even for one map")
+            return False
+        n, kc, need = fit
+        slot = self._free_slots.pop()
+        stream = self.streams[slot]
+        m0, m1 = req._next, req._next + n
+        with torch.cuda.device(self.device), torch.cuda.stream(stream):
+            if req.ready is not None:
+                stream.wait_event(req.ready)
+            ins = []
+            for x in req.inputs:
+                if isinstance(x, torch.Tensor):
+                    part = x[m0:m1] if req.analysis else x[..., m0:m1]
+                    ins.append(part.contiguous())
+                else:
+                    part = x[m0:m1] if req.analysis else x[..., m0:m1]
+                    ins.append(torch.from_numpy(np.ascontiguousarray(part)).to(
+                        self.device, non_blocking=True))
+            if req.analysis:
+                outs = [torch.empty(_alm_shape(req.lmax, n), dtype=torch.float64,
+                                    device=self.device) for _ in range(req.nfields)]
+            else:
+                outs = [torch.empty(_maps_shape(req.nside, n), dtype=torch.float64,
+                                    device=self.device) for _ in range(req.nfields)]
+            ws_bytes = self._workspace_bytes(req, n, kc)
+            ws = torch.empty(max(ws_bytes, 256), dtype=torch.uint8, device=self.device)
+            plan = self._plan(req.nside, req.lmax, req.precision)
+            job = self._job(req, m0, m1, ins, outs)
+            _lib.call("fsht_run_job", plan, C.byref(job), C.c_void_p(ws.data_ptr()),
+                      ws.numel(), C.c_void_p(stream.cuda_stream))
+            ev = torch.cuda.Event()
+            ev.record(stream)
+        if req._next == 0:
+            req.t_admit = time.perf_counter()
+        req._next = m1
+        self._used += need
+        self.high_water = max(self.high_water, self._used)
+        self._inflight.append(_Part(req, m0, m1, ins, outs, ws, ev, slot, need))
+        self.max_inflight = max(self.max_inflight, len(self._inflight))
+        if req._next < req.nmaps:
+            req.parts += 1
+        return True
+
+    def _finish(self, part: _Part):
+        req = part.req
+        self._used -= part.nbytes
+        self._free_slots.append(part.slot)
+        req._parts_out.append(part)
+        done_maps = sum(p.m1 - p.m0 for p in req._parts_out)
+        if done_maps == req.nmaps:
+            req._parts_out.sort(key=lambda p: p.m0)
+            if len(req._parts_out) == 1:
+                req.outputs = req._parts_out[0].outputs
+            else:
+                with torch.cuda.device(self.device):
+                    dim = -1 if req.analysis else 0
+                    req.outputs = [torch.cat([p.outputs[f] for p in req._parts_out], dim=dim)
+                                   for f in range(req.nfields)]
+                    torch.cuda.current_stream(self.device).synchronize()
+            req.t_done = time.perf_counter()
+            self.completed.append(req)
+            req.future.set_result(req.outputs)
+
+    def _loop(self):
+        try:
+            while True:
+                with self._lock:
+                    if self._stop and not self._pending and not self._inflight:
+                        return
+                    # completions
+                    still = []
+                    for part in self._inflight:
+                        if part.event.query():
+                            self._finish(part)
+                        else:
+                            still.append(part)
+                    self._inflight = still
+                    # admissions: arrival order, but a request that does not fit yet does
+                    # not block smaller ones behind it
+                    for req in list(self._pending):
+                        if not self._free_slots:
+                            break
+                        if not hasattr(req, "_next"):
+                            req._next = 0
+                            req._parts_out = []
+                        while self._free_slots and req._next < req.nmaps:
+                            if not self._admit_one(req):
+                                break
+                        if req._next >= req.nmaps:
+                            self._pending.remove(req)
+                    self._lock.notify_all()
+                    idle = not self._pending and not self._inflight
+                    if idle:
+                        self._lock.wait(0.01)
+                if not idle:
+                    time.sleep(self.poll_s)
+        except Exception as e:   # surface to clients instead of dying silently
+            with self._lock:
+                self._error = repr(e)
+                for req in list(self._pending):
+                    if not req.future.done():
+                        req.future.set_exception(e)
+                for part in self._inflight:
+                    if not part.req.future.done():
+                        part.req.future.set_exception(e)
+                self._pending.clear()
+                self._inflight.clear()
+                self._lock.notify_all()

@@ -40,8 +40,10 @@ enum {
 
 enum { FSHT_PREC_FP64 = 0, FSHT_PREC_SPLIT = 1 };
 
-/* Plan flags: which workspace buffers to hold (reference nbuff, SHT.py:52-59). */
-enum { FSHT_FLAG_POL = 1, FSHT_FLAG_ITER = 2 };
+/* Plan flags: which workspace buffers to hold (reference nbuff, SHT.py:52-59).
+ * FSHT_FLAG_TABLES_ONLY: geometry and FFT tables without a workspace (for plans
+ * that only lend their tables to a batch; transforms on them return FSHT_EINVAL). */
+enum { FSHT_FLAG_POL = 1, FSHT_FLAG_ITER = 2, FSHT_FLAG_TABLES_ONLY = 4 };
 
 /* Plan creation: replaces the reference's SHT.__init__ -> sht_data_alloc +
  * sht_set_data (SHT.py:17-62; src/sht_data_init.f90:2-269, 275-311).  Computes
@@ -123,6 +125,7 @@ enum {
   FSHT_KCAT_RESIDUAL = 4,
   FSHT_KCAT_SLICE = 5,      /* split form: phase matrix -> BF16 digit tiles */
   FSHT_KCAT_OTHER = 6,
+  FSHT_KCAT_LAMBDA = 7,     /* split form: FP64 recursion -> BF16 lambda digit tiles */
   FSHT_KCAT_COUNT = 8
 };
 int fsht_profile_enable(fsht_plan* plan, int on);
@@ -143,6 +146,58 @@ int fsht_measure_fp64_peak(double* tflops);
 enum { FSHT_STAGE_FFT_FWD = 0, FSHT_STAGE_ANALYSIS = 1, FSHT_STAGE_SYNTHESIS = 2,
        FSHT_STAGE_FFT_INV = 3 };
 int fsht_run_stage(fsht_plan* plan, int stage, const void* in, void* out, int nmaps);
+
+/* ---------------------------------------------------------------------------
+ * Batched form: many map sets with different nside / lmax / nmaps / spin /
+ * precision run as one CUDA-graph launch.  No counterpart in the reference, which
+ * runs one SHT instance (module-global state) and one transform per Python call
+ * (SHT.py:16-227).  Buffers are device pointers fixed at creation: rerunning the
+ * batch reuses them (write new inputs in place, then fsht_batch_run again).
+ *   kind  T2ALM: in0 maps -> out0 alm      ALM2T: in0 alm -> out0 maps
+ *         QU2EB: in0 Q, in1 U -> out0 E, out1 B
+ *         EB2QU: in0 E, in1 B -> out0 Q, out1 U
+ * Layouts as for the single-plan entry points, per job. */
+enum { FSHT_JOB_T2ALM = 0, FSHT_JOB_ALM2T = 1, FSHT_JOB_QU2EB = 2, FSHT_JOB_EB2QU = 3 };
+typedef struct fsht_job {
+  int nside, lmax, nmaps, kind, precision;
+  const double* in0;
+  const double* in1;
+  double* out0;
+  double* out1;
+} fsht_job;
+typedef struct fsht_batch fsht_batch;
+/* One table-only plan per distinct (nside, lmax, precision); workspace_budget_bytes
+ * (0 = 64 GiB) is cut into nslots stream slots (0 = 4) that run jobs concurrently,
+ * longest first.  autotune != 0 picks each plan's ring-FFT launch shape by timing
+ * (fsht_plan_autotune).  The first fsht_batch_run captures the whole batch into a
+ * CUDA graph on `stream` (NULL: a stream the batch creates; graphs cannot be captured
+ * on the legacy default stream); every run (including the first) is one graph launch.
+ * fsht_batch_sync waits for it. */
+int fsht_batch_create(const fsht_job* jobs, int njobs, int nslots, size_t workspace_budget_bytes,
+                      int autotune, void* stream, fsht_batch** batch);
+int fsht_batch_run(fsht_batch* batch);
+/* Number of distinct plans and of nodes in the captured graph (0 before the first run). */
+int fsht_batch_info(const fsht_batch* batch, int* nplans, int* nnodes);
+int fsht_batch_sync(fsht_batch* batch);
+int fsht_batch_destroy(fsht_batch* batch);
+
+/* One job on a caller-provided workspace and stream, using the tables of a plan
+ * with the same nside / lmax / precision (typically FSHT_FLAG_TABLES_ONLY).  Jobs
+ * sharing one plan may run concurrently on different streams with different
+ * workspaces: this is the execution primitive of the serving loop
+ * (fastsht_gb300.serve).  fsht_job_workspace gives the bytes needed for a given
+ * number of maps per chunk (>= 1); a larger workspace lets more maps share a pass. */
+int fsht_job_workspace(const fsht_plan* tables, const fsht_job* job, int maps_per_chunk,
+                       size_t* bytes);
+int fsht_run_job(const fsht_plan* tables, const fsht_job* job, void* workspace,
+                 size_t workspace_bytes, void* stream);
+
+/* Autotuner: times the ring-FFT launch shapes (maps per CTA 1..16, 256 or 512
+ * threads) on sample_maps maps and keeps the fastest in the plan; results are
+ * cached per (nside, lmax bucket of 256, sample_maps) for the process.  No
+ * counterpart in the reference. */
+int fsht_plan_autotune(fsht_plan* plan, int sample_maps);
+int fsht_plan_tuning(const fsht_plan* plan, int* maps_per_block, int* threads);
 
 /* Blocks until the plan's stream is idle; returns FSHT_ECUDA on an async error. */
 int fsht_plan_sync(fsht_plan* plan);

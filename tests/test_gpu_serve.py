@@ -1,0 +1,102 @@
+"""Serving form: continuous batching with HBM-budget admission.  Each result is
+the same alone and in a mix; requests overlap on the device; a request larger
+than the budget is split along maps and still exact; the budget is respected."""
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _cuda():
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from fastsht_gb300 import build
+    build.build()
+
+
+def _inputs(kind, ns, lmax, nmaps, gen):
+    nf = 2 if kind in ("qu2eb", "eb2qu") else 1
+    if kind in ("t2alm", "qu2eb"):
+        return [torch.randn((nmaps, 12 * ns * ns), dtype=torch.float64, device="cuda",
+                            generator=gen) for _ in range(nf)]
+    L = lmax + 1
+    return [torch.randn((L, L, nmaps), dtype=torch.float64, device="cuda", generator=gen)
+            for _ in range(nf)]
+
+
+def _direct(kind, ns, lmax, ins, precision):
+    from fastsht_gb300 import SHT
+    nmaps = ins[0].shape[0] if kind in ("t2alm", "qu2eb") else ins[0].shape[-1]
+    sht = SHT(ns, lmax, nmaps, pol=kind in ("qu2eb", "eb2qu"), precision=precision)
+    if kind == "t2alm":
+        out = [sht.t2alm(ins[0].T)]
+    elif kind == "alm2t":
+        out = [sht.alm2t(ins[0].permute(2, 1, 0))]
+    elif kind == "qu2eb":
+        out = list(sht.qu2eb(ins[0].T, ins[1].T))
+    else:
+        out = list(sht.eb2qu(ins[0].permute(2, 1, 0), ins[1].permute(2, 1, 0)))
+    # back to the library layouts
+    if kind in ("t2alm", "qu2eb"):
+        return [o.permute(2, 1, 0).contiguous() for o in out]
+    return [o.T.contiguous() for o in out]
+
+
+def _close(a, b, tol=1e-12):
+    return (a - b).abs().max().item() <= tol * max(b.abs().max().item(), 1e-300)
+
+
+def test_result_is_the_same_alone_and_in_a_mix():
+    from fastsht_gb300.serve import Server
+    gen = torch.Generator(device="cuda").manual_seed(4)
+    probe = ("t2alm", 32, 80, 5, "split")
+    pins = _inputs(*probe[:4], gen)
+    torch.cuda.synchronize()
+    srv = Server(hbm_budget=4e9, nslots=4)
+    alone = srv.submit(probe[0], probe[1], probe[2], pins, precision=probe[4]).result(timeout=120)
+    rng = np.random.default_rng(4)
+    reqs = []
+    for i in range(14):
+        kind = ["t2alm", "alm2t", "qu2eb", "eb2qu"][i % 4]
+        ns = int(2 ** rng.integers(3, 7))
+        lmax = 2 * ns
+        nmaps = int(rng.integers(1, 9))
+        prec = "split" if (kind == "t2alm" and i % 3 == 0) else "fp64"
+        ins = _inputs(kind, ns, lmax, nmaps, gen)
+        reqs.append((kind, ns, lmax, ins, prec))
+    torch.cuda.synchronize()
+    futs = []
+    for i, (kind, ns, lmax, ins, prec) in enumerate(reqs):
+        futs.append(srv.submit(kind, ns, lmax, ins, precision=prec))
+        if i == 6:
+            mixed = srv.submit(probe[0], probe[1], probe[2], pins, precision=probe[4])
+    srv.drain(timeout=300)
+    st = srv.stats()
+    assert st["max_inflight"] >= 2            # requests overlapped on the device
+    for a, b in zip(mixed.result(), alone):
+        assert torch.equal(a, b)
+    for f, (kind, ns, lmax, ins, prec) in zip(futs, reqs):
+        for got, want in zip(f.result(), _direct(kind, ns, lmax, ins, prec)):
+            assert _close(got, want)
+    assert st["p99_ms"] >= st["p50_ms"] > 0
+    srv.close()
+
+
+def test_request_larger_than_budget_is_split_and_exact():
+    from fastsht_gb300.serve import Server
+    gen = torch.Generator(device="cuda").manual_seed(5)
+    ns, lmax, nmaps = 32, 64, 24
+    ins = _inputs("t2alm", ns, lmax, nmaps, gen)
+    torch.cuda.synchronize()
+    budget = 2_500_000           # a few maps' worth
+    srv = Server(hbm_budget=budget, nslots=3)
+    out = srv.submit("t2alm", ns, lmax, ins).result(timeout=120)
+    srv.drain()
+    st = srv.stats()
+    assert st["high_water_bytes"] <= budget
+    assert srv.completed[0].parts > 1
+    assert _close(out[0], _direct("t2alm", ns, lmax, ins, "fp64")[0])
+    srv.close()
