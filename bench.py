@@ -44,6 +44,8 @@ if str(ROOT) not in sys.path:
 
 import numpy as np
 
+from fastsht_gb300.replicas import max_over_ranks
+
 METRIC = "maps·SHT/s at nside 1024 (FP64 vs split-prec @ stated error); p50/p99 latency"
 UNIT = "maps·SHT/s"
 
@@ -272,9 +274,7 @@ def timed_steps(lib, sht, maps, steps, warmup, world, dist, dev, local, sample_c
     _lib.call("fsht_profile_read", sht._plan, _lib.KCAT_COUNT, counts, kms)
     lib.fsht_profile_enable(sht._plan, 0)
     if world > 1:
-        t = torch.tensor([ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+        ms = max_over_ranks(ms, dist, dev)
         dist.barrier()
     per_kernel = {}
     for i, name in enumerate(_lib.KCAT_NAMES):
@@ -536,9 +536,7 @@ def bench_batched(args, rank, world, local):
         clk = clocks.stop() if clocks else None
         ms = e0.elapsed_time(e1)
         if world > 1:
-            t = torch.tensor([ms], device=dev)
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            ms = float(t.item())
+            ms = max_over_ranks(ms, dist, dev)
         return ms, clk
 
     b_split, t_build = build("split")
