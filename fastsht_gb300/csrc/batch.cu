@@ -56,7 +56,7 @@ JobLayout job_layout(const fsht_plan* p, const fsht_job& j, int kc) {
   L.eb_off = L.ws_off;
   L.lb_off = L.ws_off;
   L.total = L.ws_off;
-  if (p->precision == FSHT_PREC_SPLIT && j.kind == FSHT_JOB_T2ALM) {
+  if (p->precision == FSHT_PREC_SPLIT && (j.kind == FSHT_JOB_T2ALM || j.kind == FSHT_JOB_ALM2T)) {
     L.eb_off = align_up(L.ws_off + fsht_split_ws_bytes(p->lmax, p->nnorth, kc));
     L.lb_off = align_up(L.eb_off + fsht_split_eb_bytes(p->lmax, kc));
     L.total = align_up(L.lb_off + p->lbuf_bytes);

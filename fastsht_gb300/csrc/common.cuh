@@ -41,19 +41,48 @@ FSHT_HD int ring_phase_flag(int ns, int i) {
 // ---------------------------------------------------------------- plan
 struct FshtRingFFT {
   int n;          // ring length
-  int P;          // FFT size used (n when pow2, else the Bluestein size)
-  int logP;
+  int P;          // transform size: n (power of two) or the Bluestein size 2^logT or 3*2^logT
+  int logT;       // log2 of the power-of-two factor of P
+  int r3;         // 1 when P = 3 * 2^logT
   int bluestein;  // 1 when n is not a power of two
   long long chirp_off;  // offset (double2) of w_j = exp(-i pi j^2/n), j < n
-  long long bhat_off;   // offset (double2) of FFT_P(conj chirp, wrapped)
+  long long bhat_off;   // offset (double2) of the filter spectrum (transform order), P entries
 };
+
+// Transform size of a ring of n points: n itself when n is a power of two, else the
+// smallest 2^k or 3*2^k >= 2n - 1 (Bluestein's linear convolution of length 2n - 1).
+FSHT_HD void fsht_ring_fft_size(FshtRingFFT& r) {
+  const int n = r.n;
+  r.r3 = 0;
+  if ((n & (n - 1)) == 0) {
+    r.bluestein = 0;
+    r.P = n;
+    int l = 0;
+    while ((1 << l) < n) ++l;
+    r.logT = l;
+    return;
+  }
+  r.bluestein = 1;
+  const int need = 2 * n - 1;
+  int l2 = 0, l3 = 0;
+  while ((1 << l2) < need) ++l2;
+  while (3 * (1 << l3) < need) ++l3;
+  if (3 * (1 << l3) < (1 << l2)) {
+    r.P = 3 << l3;
+    r.logT = l3;
+    r.r3 = 1;
+  } else {
+    r.P = 1 << l2;
+    r.logT = l2;
+  }
+}
 
 // Split-precision form: per (l, m) row of the scaled recursion (legendre_split.cu).
 struct FshtLamRow {
   double beta;   // mu_l = x mu_{l-1} - beta mu_{l-2}
-  double rs;     // row scale of the GEMM epilogue, Dm_l 2^EA(l)
-  int erow;      // EA(l) - Dx_l: digit exponent of row l before the per-ring offset
-  int pad;
+  double dm;     // D_l = prod_{k=m+1..l} a_k = dm 2^dx, dm in [1, 2)
+  int erow;      // EA(l) - dx: digit exponent of row l before the per-ring offset
+  int dx;
 };
 
 struct fsht_plan {
@@ -72,8 +101,9 @@ struct fsht_plan {
   FshtRingFFT* d_rfft;             // per north ring
   double2* d_chirp;                // Bluestein chirps
   double2* d_bhat;                 // Bluestein filter spectra
-  double2* d_tw;                   // exp(-2 pi i j / Pmax), j < Pmax/2
-  int Pmax, logPmax;
+  double2* d_tw;                   // [exp(-2 pi i t / Tmax), t < Tmax][exp(-2 pi i t / P3max), t < P3max]
+  int Pmax;                        // largest transform size (shared-memory sizing)
+  int Tmax, logTmax, P3max;        // twiddle tables: largest power-of-two factor, largest 3*2^k size
   // workspace: phase matrices [m][i][k] x 2 complex, one per buffer
   double2* d_work;
   size_t work_bytes;
@@ -89,7 +119,8 @@ struct fsht_plan {
   size_t ws_bytes;
   FshtLamRow* d_lamtab;            // triangular, (l, m) at m(2 lmax + 3 - m)/2 + l - m
   long long* d_lam_off;            // per pair-ordered index q: first 16 KB tile unit
-  int* h_waves;                    // per wave: q0, q1, max l-tiles, max K-chunks, max ring blocks
+  long long* d_lam_offT;           // the same for the synthesis (ring-row) tile layout
+  int* h_waves;                    // per wave: see kWaveInts in legendre_split.cu
   int nwaves;
   unsigned char* d_lbuf;
   size_t lbuf_bytes;
@@ -122,7 +153,7 @@ void fsht_set_error(const char* fmt, ...);
 
 // ---------------------------------------------------------------- internal API
 struct FshtFftLayout {
-  int Pmax, logPmax, nblue;
+  int Pmax, Tmax, logTmax, P3max, nblue;
   long long chirp_total, bhat_total;
   size_t smem;
 };
@@ -161,7 +192,15 @@ int fsht_launch_split_prepare(fsht_plan* p, const double2* W, unsigned char* WS,
 int fsht_launch_split_lambda(fsht_plan* p, int w, unsigned char* lbuf, cudaStream_t s);
 int fsht_launch_split_gemm(fsht_plan* p, int w, const unsigned char* WS, const int* EB,
                            const unsigned char* lbuf, double* alm, int nmaps_total, int k0,
-                           int kc, cudaStream_t s);
+                           int kc, int accumulate, cudaStream_t s);
+// Split-precision synthesis of one chunk into W = {G_N, G_S}: prepare cuts alm into digit
+// tiles WS / exponents EB (and clears W when l-chunks will add into it); per wave, lambdaT
+// writes ring-row lambda tiles and synth contracts them with WS.
+int fsht_launch_split_synth_prepare(fsht_plan* p, const double* alm, unsigned char* WS, int* EB,
+                                    double2* W, int nmaps_total, int k0, int kc, cudaStream_t s);
+int fsht_launch_split_lambdaT(fsht_plan* p, int w, unsigned char* lbuf, cudaStream_t s);
+int fsht_launch_split_synth(fsht_plan* p, int w, const unsigned char* WS, const int* EB,
+                            const unsigned char* lbuf, double2* W, int kc, cudaStream_t s);
 int fsht_launch_synthesis_fp64(fsht_plan* p, int spin, const double* almE,
                                const double* almB, double2* WQ, double2* WU,
                                int nmaps_total, int k0, int kc, cudaStream_t s);

@@ -142,7 +142,7 @@ __global__ void __launch_bounds__(128) k_slice_phase(SliceArgs a) {
 // two FP64 operations per step instead of four.  Rows are digitised as
 // lambda_l / Dm_l = mu 2^(Et + Dx_l) against 2^EA(l) with EA(l) from |lambda| / Dm_l <=
 // sqrt((2l+1)/4pi) / Dm_l (D_l = Dm_l 2^Dx_l, Dm_l in [1, 2)); the GEMM epilogue multiplies
-// row l by rs = Dm_l 2^EA(l).  Et is the per-ring exponent carried with the state.
+// row l by Dm_l 2^EA(l).  Et is the per-ring exponent carried with the state.
 __device__ __forceinline__ int m_of_q(int q, int lmax) {
   return (q & 1) ? lmax - (q >> 1) : (q >> 1);
 }
@@ -150,7 +150,7 @@ __host__ __device__ __forceinline__ long long tri_off(int m, int lmax) {
   return (long long)m * (2LL * lmax + 3 - m) / 2;
 }
 
-// One thread per m, sequential in l: beta_l, rs_l and erow_l = EA(l) - Dx_l.
+// One thread per m, sequential in l: beta_l, Dm_l, Dx_l and erow_l = EA(l) - Dx_l.
 __global__ void k_lam_table(int lmax, FshtLamRow* tab) {
   const int m = blockIdx.x * blockDim.x + threadIdx.x;
   if (m > lmax) return;
@@ -172,9 +172,9 @@ __global__ void k_lam_table(int lmax, FshtLamRow* tab) {
     const int ea = ilogb(bound) + 1;
     FshtLamRow r;
     r.beta = beta;
-    r.rs = ldexp(dm, ea);
+    r.dm = dm;
     r.erow = ea - dx;
-    r.pad = 0;
+    r.dx = dx;
     row[l - m] = r;
   }
 }
@@ -305,7 +305,7 @@ constexpr int kStagesG = 6;
 constexpr uint32_t kStageBytesG = 2 * kSlices * kATileBytes;    // 32 KB: A then B
 
 struct GemmArgs {
-  int lmax, nnorth, ngroups, nks_max, nkc_glob, q0, ntmax, nkcmax;
+  int lmax, nnorth, ngroups, nks_max, nkc_glob, q0, ntmax, nkcmax, accumulate;
   const int* ring_i0;
   const long long* lam_off;
   const FshtLamRow* tab;
@@ -363,7 +363,12 @@ __global__ void __launch_bounds__(kThreads, 1) k_split_gemm(GemmArgs a) {
     const int eb = a.EB[(((long long)m * 2 + p) * a.ngroups + g) * kCols + tid];
     s_cs[tid] = (eb == kEmptyExp) ? 0.0 : ldexp(a.pa, eb - 12);
     const int l = lt0 + p + 2 * tid;
-    s_rs[tid] = (l <= a.lmax) ? a.tab[tri_off(m, a.lmax) + (l - m)].rs : 0.0;
+    if (l <= a.lmax) {
+      const FshtLamRow rw = a.tab[tri_off(m, a.lmax) + (l - m)];
+      s_rs[tid] = ldexp(rw.dm, rw.erow + rw.dx);
+    } else {
+      s_rs[tid] = 0.0;
+    }
   }
   if (warp == 0) tc::tmem_alloc(&h.tmem, 512);
   tc::tc_fence_before();
@@ -449,6 +454,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_split_gemm(GemmArgs a) {
             const double v = ((double)hi + (double)lo) * rs * s_cs[c];
             double* dst = a.alm + rowidx * a.ld + a.k0 + k;
             if (a.nkc_glob > 1) atomicAdd(dst, v);
+            else if (a.accumulate) *dst += v;
             else *dst = v;
           }
         }
@@ -475,12 +481,355 @@ __global__ void __launch_bounds__(kThreads, 1) k_split_gemm(GemmArgs a) {
   if (tid == 0 && h.abort) atomicOr(a.err, 1);
 }
 
+
+// ------------------------------------------------------------------ synthesis
+// G_m(i) = sum_l a_lm lambda_lm(theta_i) as even-l and odd-l parts E, O (G_N = E + O,
+// G_S = E - O).  GEMM per (m, parity): D[ring][col] = sum_l lambda[l][ring] a[l][col] with
+// K = l.  A scale must not depend on the summation index, so lambda is digitised against
+// one global 2^EAG (EAG from sqrt((2 lmax + 1)/4pi)) as lambda = mu Dm 2^(Et + Dx): one more
+// FP64 multiply per step than the analysis tiles.  Tiles: 128 rings x 16 l of one parity,
+// K-major (core matrix 8 rings x 8 l at (ring/8)*256 + (l/8)*128).
+
+// grid (q in wave, 128-ring block), 128 threads = rings; every thread stores its own
+// 16-byte core-matrix rows (8 l of one parity), no staging.
+struct LamTArgs {
+  int lmax, nnorth, q0, eag;
+  const double* cth;
+  const double* sth;
+  const double* pref;
+  const int* ring_i0;
+  const FshtLamRow* tab;
+  const long long* lam_offT;
+  unsigned char* lbuf;
+};
+
+__global__ void __launch_bounds__(128) k_lambda_digits_T(LamTArgs a) {
+  const int q = a.q0 + blockIdx.x;
+  const int m = m_of_q(q, a.lmax);
+  const int i0 = a.ring_i0[m];
+  const int K = a.nnorth - i0;
+  const int rb = blockIdx.y;
+  if (rb * kSCRings >= K) return;
+  const int tid = threadIdx.x;
+  const int r = rb * kSCRings + tid;
+  const bool valid = r < K;
+  const int nrb = (K + kSCRings - 1) / kSCRings;
+  const int nkl = ((a.lmax - m) / 2 + 1 + kKStep - 1) / kKStep;
+  unsigned char* base =
+      a.lbuf + (size_t)(a.lam_offT[q] - a.lam_offT[a.q0]) * kSlices * kATileBytes +
+      (tid >> 3) * 256 + (tid & 7) * 16;
+  const FshtLamRow* tab = a.tab + tri_off(m, a.lmax);
+  double x = 0.0, s1 = 0.0, s2 = 0.0;
+  int et = 0;
+  if (valid) {
+    int e;
+    x = a.cth[i0 + r];
+    rec_seed(a.sth[i0 + r], a.pref[m], m, s1, e);
+    et = 600 * e;
+  }
+  for (int kl = 0; kl < nkl; ++kl) {
+#pragma unroll
+    for (int half = 0; half < 2; ++half) {
+      uint32_t pk[2][kSlices][4];
+#pragma unroll
+      for (int pp = 0; pp < 2; ++pp)
+#pragma unroll
+        for (int d = 0; d < kSlices; ++d)
+#pragma unroll
+          for (int w = 0; w < 4; ++w) pk[pp][d][w] = 0;
+#pragma unroll
+      for (int jj = 0; jj < 16; ++jj) {
+        const int j = kl * 32 + half * 16 + jj;
+        uint16_t d[4] = {0, 0, 0, 0};
+        if (m + j <= a.lmax) {
+          const FshtLamRow rw = tab[j];
+          if (j > 0) {
+            const double t = rw.beta * s2;
+            const double nx = fma(x, s1, -t);
+            s2 = s1;
+            s1 = nx;
+          }
+          if (valid) tc::digits4(s1 * rw.dm, a.eag - et - rw.dx, d);
+        }
+        const int par = jj & 1, slot = jj >> 1;
+#pragma unroll
+        for (int dd = 0; dd < kSlices; ++dd)
+          pk[par][dd][slot >> 1] |= (uint32_t)d[dd] << (16 * (slot & 1));
+      }
+#pragma unroll
+      for (int par = 0; par < 2; ++par)
+#pragma unroll
+        for (int dd = 0; dd < kSlices; ++dd) {
+          uint4 o;
+          o.x = pk[par][dd][0];
+          o.y = pk[par][dd][1];
+          o.z = pk[par][dd][2];
+          o.w = pk[par][dd][3];
+          *reinterpret_cast<uint4*>(
+              base + (((size_t)(par * nrb + rb) * nkl + kl) * kSlices + dd) * kATileBytes +
+              half * 128) = o;
+        }
+    }
+    const double am = fmax(fabs(s1), fabs(s2));
+    if (am > 0x1p300) {
+      s1 *= 0x1p-600;
+      s2 *= 0x1p-600;
+      et += 600;
+    } else if (am > 0.0 && am < 0x1p-300) {
+      s1 *= 0x1p600;
+      s2 *= 0x1p600;
+      et -= 600;
+    }
+  }
+}
+
+// alm -> digit tiles: grid (m, parity, group), 128 threads = columns (map = c & 63,
+// Re/Im = c >> 6).  Tile (m, p, g, l-step): 128 columns x 16 l, K-major.
+struct SliceAArgs {
+  const double* alm;
+  int ld, k0, kc, lmax, ngroups, nkl_max;
+  unsigned char* WS;
+  int* EB;
+};
+
+__global__ void __launch_bounds__(128) k_slice_alm(SliceAArgs a) {
+  const int m = blockIdx.x, p = blockIdx.y, g = blockIdx.z;
+  const int c = threadIdx.x;
+  const int k = g * kGroupMaps + (c & 63);
+  const int comp = c >> 6;
+  const bool valid = k < a.kc && !(comp == 1 && m == 0);
+  const long long L1 = a.lmax + 1;
+  const int cnt0 = (a.lmax - m) / 2 + 1;
+  const int cnt = (p == 0) ? cnt0 : (a.lmax > m ? (a.lmax - m - 1) / 2 + 1 : 0);
+  auto val = [&](int idx) -> double {
+    if (!valid || idx >= cnt) return 0.0;
+    const int l = m + p + 2 * idx;
+    const long long row = comp == 0 ? (long long)m * L1 + l : (L1 - m) * L1 + (l - m);
+    return a.alm[row * a.ld + a.k0 + k];
+  };
+  double mx = 0.0;
+  for (int idx = 0; idx < cnt; ++idx) mx = fmax(mx, fabs(val(idx)));
+  const int E = (mx > 0.0) ? ilogb(mx) + 1 : kEmptyExp;
+  a.EB[(((long long)m * 2 + p) * a.ngroups + g) * kCols + c] = E;
+  const int nkl = (cnt0 + kKStep - 1) / kKStep;
+  unsigned char* base = a.WS +
+                        (((size_t)(m * 2 + p) * a.ngroups + g) * a.nkl_max) * kSlices * kBTileBytes +
+                        (c >> 3) * 256 + (c & 7) * 16;
+  for (int kl = 0; kl < nkl; ++kl) {
+    for (int half = 0; half < 2; ++half) {
+      uint16_t sl[kSlices][8];
+      for (int j = 0; j < 8; ++j) {
+        uint16_t q4[4] = {0, 0, 0, 0};
+        if (E != kEmptyExp) tc::digits4(val(kl * kKStep + half * 8 + j), E, q4);
+        for (int d = 0; d < kSlices; ++d) sl[d][j] = q4[d];
+      }
+      for (int d = 0; d < kSlices; ++d) {
+        uint4 pk;
+        pk.x = sl[d][0] | ((uint32_t)sl[d][1] << 16);
+        pk.y = sl[d][2] | ((uint32_t)sl[d][3] << 16);
+        pk.z = sl[d][4] | ((uint32_t)sl[d][5] << 16);
+        pk.w = sl[d][6] | ((uint32_t)sl[d][7] << 16);
+        *reinterpret_cast<uint4*>(base + ((size_t)kl * kSlices + d) * kBTileBytes + half * 128) = pk;
+      }
+    }
+  }
+}
+
+// CTA = (64-map group, 128-ring block x l-chunk, q): both parities in turn through the same
+// TMEM accumulators (E first, written as G_N = G_S = E; then O, added to G_N and subtracted
+// from G_S by the same threads).  Roles as in k_split_gemm.
+struct SynthArgs {
+  int lmax, nnorth, ngroups, nkl_max, nkcl_glob, q0, nkclmax, eag;
+  const int* ring_i0;
+  const long long* lam_offT;
+  const unsigned char* lbuf;
+  const unsigned char* WS;
+  const int* EB;
+  double* W;           // double2 {G_N, G_S} as doubles
+  int kc;
+  int* err;
+};
+
+struct __align__(8) SynthSmemHdr {
+  uint64_t full[kStagesG], empty[kStagesG], tfull, tempty, fin;
+  uint32_t tmem;
+  int abort;
+};
+
+__global__ void __launch_bounds__(kThreads, 1) k_split_synth(SynthArgs a) {
+  extern __shared__ __align__(1024) unsigned char smem[];
+  __shared__ SynthSmemHdr h;
+  __shared__ double s_cs[2][kCols];
+
+  const int g = blockIdx.x;
+  const int rb = blockIdx.y / a.nkclmax;
+  const int kcl = blockIdx.y % a.nkclmax;
+  const int q = a.q0 + blockIdx.z;
+  const int m = m_of_q(q, a.lmax);
+  const int i0 = a.ring_i0[m];
+  const int K = a.nnorth - i0;
+  const int nrb = (K + kSCRings - 1) / kSCRings;
+  const int nkl = ((a.lmax - m) / 2 + 1 + kKStep - 1) / kKStep;
+  const int kl0 = kcl * (kKChunk / kKStep);
+  const int kl1 = min(nkl, kl0 + kKChunk / kKStep);
+  if (rb >= nrb || kl0 >= kl1) return;            // uniform: before any barrier or TMEM
+  const int nk = kl1 - kl0;
+
+  const int tid = threadIdx.x;
+  const int warp = tid >> 5;
+  volatile int* abort = &h.abort;
+  if (tid == 0) {
+    for (int s = 0; s < kStagesG; ++s) {
+      tc::mbar_init(&h.full[s], 1);
+      tc::mbar_init(&h.empty[s], 1);
+    }
+    tc::mbar_init(&h.tfull, 1);
+    tc::mbar_init(&h.tempty, 128);
+    tc::mbar_init(&h.fin, 1);
+    h.abort = 0;
+    tc::mbar_fence_init();
+  }
+  if (tid < kCols) {
+    for (int pp = 0; pp < 2; ++pp) {
+      const int eb = a.EB[(((long long)m * 2 + pp) * a.ngroups + g) * kCols + tid];
+      s_cs[pp][tid] = (eb == kEmptyExp) ? 0.0 : ldexp(1.0, a.eag + eb - 12);
+    }
+  }
+  if (warp == 0) tc::tmem_alloc(&h.tmem, 512);
+  tc::tc_fence_before();
+  __syncthreads();
+  tc::tc_fence_after();
+  const uint32_t tmem = h.tmem;
+
+  uint32_t n_loaded = 0;
+  if (tid == 128) {
+    const unsigned char* abase =
+        a.lbuf + (size_t)(a.lam_offT[q] - a.lam_offT[a.q0]) * kSlices * kATileBytes;
+    for (int i = 0; i < 2 * nk; ++i) {
+      const int par = i / nk, kk = kl0 + i % nk;
+      const uint32_t st = i % kStagesG;
+      if (!tc::mbar_wait(&h.empty[st], ((i / kStagesG) & 1) ^ 1, abort)) break;
+      unsigned char* dst = smem + st * kStageBytesG;
+      const unsigned char* asrc =
+          abase + ((size_t)(par * nrb + rb) * nkl + kk) * kSlices * kATileBytes;
+      const unsigned char* bsrc =
+          a.WS + ((((size_t)m * 2 + par) * a.ngroups + g) * a.nkl_max + kk) * kSlices * kBTileBytes;
+      tc::mbar_arrive_expect_tx(&h.full[st], kStageBytesG);
+      tc::bulk_g2s(dst, asrc, kSlices * kATileBytes, &h.full[st]);
+      tc::bulk_g2s(dst + kSlices * kATileBytes, bsrc, kSlices * kBTileBytes, &h.full[st]);
+      ++n_loaded;
+    }
+  } else if (tid == 160) {
+    const uint32_t idesc = tc::umma_idesc_bf16(kRows, kCols);
+    const uint32_t s_u = tc::smem_u32(smem);
+    for (int i = 0; i < 2 * nk; ++i) {
+      if (i == nk) {
+        // E is complete: hand TMEM to the epilogue, take it back for O
+        tc::umma_commit(&h.tfull);
+        if (!tc::mbar_wait(&h.tempty, 0, abort)) break;
+        tc::tc_fence_after();
+      }
+      const uint32_t st = i % kStagesG;
+      if (!tc::mbar_wait(&h.full[st], (i / kStagesG) & 1, abort)) break;
+      tc::tc_fence_after();
+      const uint32_t abase = s_u + st * kStageBytesG;
+      const uint32_t bbase = abase + kSlices * kATileBytes;
+      const bool first = (i % nk) == 0;
+#pragma unroll
+      for (int lev = 0; lev <= 3; ++lev) {
+#pragma unroll
+        for (int aa = 0; aa <= lev; ++aa) {
+          const uint64_t ad = tc::umma_desc(abase + aa * kATileBytes, 128, 256);
+          const uint64_t bd = tc::umma_desc(bbase + (lev - aa) * kBTileBytes, 128, 256);
+          tc::umma_bf16(tmem + lev * kCols, ad, bd, idesc, (!first || aa > 0) ? 1u : 0u);
+        }
+      }
+      tc::umma_commit(&h.empty[st]);
+    }
+    tc::umma_commit(&h.tfull);
+  }
+  if (tid < 128) {
+    const int row = (warp << 5) + (tid & 31);
+    const int rr = rb * kSCRings + row;
+    const bool rowok = rr < K;
+    const int i = i0 + rr;
+    for (int par = 0; par < 2; ++par) {
+      bool ok = tc::mbar_wait(&h.tfull, par, abort);
+      ok = __all_sync(0xffffffffu, ok);
+      tc::tc_fence_after();
+      if (!ok) break;
+      const uint32_t lane_base = tmem + ((uint32_t)(warp << 5) << 16);
+      for (int c0 = 0; c0 < kCols; c0 += 16) {
+        uint32_t v0[16], v1[16], v2[16], v3[16];
+        tc::tmem_ld16(lane_base + 0 * kCols + c0, v0);
+        tc::tmem_ld16(lane_base + 1 * kCols + c0, v1);
+        tc::tmem_ld16(lane_base + 2 * kCols + c0, v2);
+        tc::tmem_ld16(lane_base + 3 * kCols + c0, v3);
+        tc::tmem_wait_ld();
+        const int comp = c0 >> 6;
+#pragma unroll
+        for (int j = 0; j < 16; ++j) {
+          const int c = c0 + j;
+          const int k = g * kGroupMaps + (c & 63);
+          if (rowok && k < a.kc) {
+            const float L0 = __uint_as_float(v0[j]);
+            const float L1f = __uint_as_float(v1[j]) * 0x1p-8f;
+            const float hi = L0 + L1f;
+            const float bv = hi - L0;
+            const float lo = ((L0 - (hi - bv)) + (L1f - bv)) +
+                             (__uint_as_float(v2[j]) * 0x1p-16f + __uint_as_float(v3[j]) * 0x1p-24f);
+            const double v = ((double)hi + (double)lo) * s_cs[par][c];
+            double* gn = a.W + ((((long long)m * a.nnorth + i) * a.kc + k) * 2) * 2 + comp;
+            double* gs = gn + 2;
+            if (a.nkcl_glob > 1) {
+              atomicAdd(gn, v);
+              atomicAdd(gs, par ? -v : v);
+            } else if (par == 0) {
+              *gn = v;
+              *gs = v;
+            } else {
+              *gn += v;
+              *gs -= v;
+            }
+          }
+        }
+      }
+      tc::tc_fence_before();
+      if (par == 0) tc::mbar_arrive(&h.tempty);
+    }
+  }
+  if (tid == 160) {
+    tc::umma_commit(&h.fin);
+    for (uint32_t it = 0; it < tc::kWaitLimit; ++it)
+      if (tc::mbar_try_wait(&h.fin, 0)) break;
+  }
+  if (tid == 128) {
+    for (uint32_t d = 0; d < (uint32_t)kStagesG && d < n_loaded; ++d) {
+      const uint32_t i = n_loaded - 1 - d;
+      for (uint32_t it = 0; it < tc::kWaitLimit; ++it)
+        if (tc::mbar_try_wait(&h.full[i % kStagesG], (i / kStagesG) & 1)) break;
+    }
+  }
+  tc::tc_fence_before();
+  __syncthreads();
+  if (warp == 0) tc::tmem_dealloc(tmem, 512);
+  if (tid == 0 && h.abort) atomicOr(a.err, 1);
+}
+
+}  // namespace
+
+namespace {
+// k-steps per (m, parity, group) row of WS: rings (analysis) or l of one parity (synthesis)
+int ws_ksteps(int lmax, int nnorth) {
+  const int nks = (nnorth + kKStep - 1) / kKStep;
+  const int nkl = (lmax / 2 + 1 + kKStep - 1) / kKStep;
+  return nks > nkl ? nks : nkl;
+}
 }  // namespace
 
 size_t fsht_split_ws_bytes(int lmax, int nnorth, int kc) {
   const int ngroups = (kc + kGroupMaps - 1) / kGroupMaps;
-  const int nks_max = (nnorth + kKStep - 1) / kKStep;
-  return (size_t)(lmax + 1) * 2 * ngroups * nks_max * kSlices * kBTileBytes;
+  return (size_t)(lmax + 1) * 2 * ngroups * ws_ksteps(lmax, nnorth) * kSlices * kBTileBytes;
 }
 size_t fsht_split_eb_bytes(int lmax, int kc) {
   const int ngroups = (kc + kGroupMaps - 1) / kGroupMaps;
@@ -491,14 +840,13 @@ int fsht_launch_split_prepare(fsht_plan* p, const double2* W, unsigned char* WS,
                               double* alm, int nmaps_total, int k0, int kc, int accumulate,
                               cudaStream_t s) {
   const int ngroups = (kc + kGroupMaps - 1) / kGroupMaps;
-  const int nks_max = (p->nnorth + kKStep - 1) / kKStep;
   const int nkc = (p->nnorth + kKChunk - 1) / kKChunk;
   SliceArgs sa;
   sa.W = W;
   sa.kc = kc;
   sa.nnorth = p->nnorth;
   sa.ngroups = ngroups;
-  sa.nks_max = nks_max;
+  sa.nks_max = ws_ksteps(p->lmax, p->nnorth);
   sa.ring_i0 = p->d_ring_i0;
   sa.WS = WS;
   sa.EB = EB;
@@ -516,6 +864,14 @@ int fsht_launch_split_prepare(fsht_plan* p, const double2* W, unsigned char* WS,
 // ------------------------------------------------------------------ host side
 namespace {
 constexpr size_t kLbufCap = 2ull << 30;     // lambda-digit staging per wave
+// per wave: q0, q1, max l-tiles, max ring K-chunks (analysis), max 128-ring blocks,
+// max l-steps, max l K-chunks (synthesis)
+constexpr int kWaveInts = 7;
+
+int eag_of(int lmax) {
+  const double b = std::sqrt((2.0 * lmax + 1.0) / (4.0 * M_PI)) * (1.0 + 0x1p-30);
+  return std::ilogb(b) + 1;
+}
 }
 
 int fsht_split_tables_init(fsht_plan* p) {
@@ -523,37 +879,47 @@ int fsht_split_tables_init(fsht_plan* p) {
   const size_t ntab = (size_t)tri_off(lmax + 1, lmax);
   FSHT_CUDA_TRY(cudaMalloc(&p->d_lamtab, sizeof(FshtLamRow) * (ntab ? ntab : 1)));
   FSHT_CUDA_TRY(cudaMalloc(&p->d_lam_off, sizeof(long long) * (lmax + 2)));
+  FSHT_CUDA_TRY(cudaMalloc(&p->d_lam_offT, sizeof(long long) * (lmax + 2)));
   k_lam_table<<<(lmax + 1 + 127) / 128, 128, 0, p->stream>>>(lmax, p->d_lamtab);
   FSHT_LAUNCH_CHECK();
-  // per q (pair order): 16 KB units of the lambda digit tiles of m(q)
-  std::vector<long long> off(lmax + 2, 0);
-  std::vector<int> ntl(lmax + 1), nkm(lmax + 1);
+  // per q (pair order): 16 KB units of m(q)'s analysis tiles (l-rows) and synthesis tiles
+  // (ring rows)
+  std::vector<long long> off(lmax + 2, 0), offT(lmax + 2, 0);
+  std::vector<int> ntl(lmax + 1), nkm(lmax + 1), nrb(lmax + 1), nkl(lmax + 1);
   for (int q = 0; q <= lmax; ++q) {
     const int m = (q & 1) ? lmax - (q >> 1) : (q >> 1);
     const int K = p->nnorth - p->h_ring_i0[m];
     ntl[q] = (lmax - m + 1 + 2 * kRows - 1) / (2 * kRows);
     nkm[q] = K > 0 ? (K + kKStep - 1) / kKStep : 0;
+    nrb[q] = K > 0 ? (K + kSCRings - 1) / kSCRings : 0;
+    nkl[q] = ((lmax - m) / 2 + 1 + kKStep - 1) / kKStep;
     off[q + 1] = off[q] + 2LL * ntl[q] * nkm[q];
+    offT[q + 1] = offT[q] + 2LL * nrb[q] * nkl[q];
   }
   const size_t unit = (size_t)kSlices * kATileBytes;
-  size_t cap_units = kLbufCap / unit;
-  // waves: consecutive q ranges whose tiles fit the staging buffer
+  const size_t cap_units = kLbufCap / unit;
+  auto span = [&](int q0, int q1) -> size_t {
+    return (size_t)std::max(off[q1] - off[q0], offT[q1] - offT[q0]);
+  };
+  // waves: consecutive q ranges whose tiles (either layout) fit the staging buffer
   std::vector<int> waves;
   size_t lbuf_units = 0;
   for (int q0 = 0; q0 <= lmax;) {
     int q1 = q0 + 1;
-    while (q1 <= lmax && (size_t)(off[q1 + 1] - off[q0]) <= cap_units) ++q1;
-    int ntmax = 0, nkc = 0, nrb = 0;
+    while (q1 <= lmax && span(q0, q1 + 1) <= cap_units) ++q1;
+    int wv[kWaveInts] = {q0, q1, 0, 0, 0, 0, 0};
     for (int q = q0; q < q1; ++q) {
-      ntmax = std::max(ntmax, ntl[q]);
-      nkc = std::max(nkc, (nkm[q] * kKStep + kKChunk - 1) / kKChunk);
-      nrb = std::max(nrb, (nkm[q] * kKStep + kSCRings - 1) / kSCRings);
+      wv[2] = std::max(wv[2], ntl[q]);
+      wv[3] = std::max(wv[3], (nkm[q] * kKStep + kKChunk - 1) / kKChunk);
+      wv[4] = std::max(wv[4], nrb[q]);
+      wv[5] = std::max(wv[5], nkl[q]);
+      wv[6] = std::max(wv[6], (nkl[q] * kKStep + kKChunk - 1) / kKChunk);
     }
-    waves.insert(waves.end(), {q0, q1, ntmax, nkc, nrb});
-    lbuf_units = std::max(lbuf_units, (size_t)(off[q1] - off[q0]));
+    waves.insert(waves.end(), wv, wv + kWaveInts);
+    lbuf_units = std::max(lbuf_units, span(q0, q1));
     q0 = q1;
   }
-  p->nwaves = (int)waves.size() / 5;
+  p->nwaves = (int)waves.size() / kWaveInts;
   p->h_waves = new (std::nothrow) int[waves.size()];
   if (!p->h_waves) {
     fsht_set_error("host allocation failed");
@@ -563,12 +929,14 @@ int fsht_split_tables_init(fsht_plan* p) {
   p->lbuf_bytes = std::max<size_t>(lbuf_units * unit, 256);
   FSHT_CUDA_TRY(cudaMemcpyAsync(p->d_lam_off, off.data(), sizeof(long long) * (lmax + 2),
                                 cudaMemcpyHostToDevice, p->stream));
-  FSHT_CUDA_TRY(cudaStreamSynchronize(p->stream));   // off[] is a stack vector
+  FSHT_CUDA_TRY(cudaMemcpyAsync(p->d_lam_offT, offT.data(), sizeof(long long) * (lmax + 2),
+                                cudaMemcpyHostToDevice, p->stream));
+  FSHT_CUDA_TRY(cudaStreamSynchronize(p->stream));   // the offsets are stack vectors
   return FSHT_OK;
 }
 
 int fsht_launch_split_lambda(fsht_plan* p, int w, unsigned char* lbuf, cudaStream_t s) {
-  const int* wv = p->h_waves + 5 * w;
+  const int* wv = p->h_waves + kWaveInts * w;
   LamArgs a;
   a.lmax = p->lmax;
   a.nnorth = p->nnorth;
@@ -588,15 +956,16 @@ int fsht_launch_split_lambda(fsht_plan* p, int w, unsigned char* lbuf, cudaStrea
 
 int fsht_launch_split_gemm(fsht_plan* p, int w, const unsigned char* WS, const int* EB,
                            const unsigned char* lbuf, double* alm, int nmaps_total, int k0,
-                           int kc, cudaStream_t s) {
-  const int* wv = p->h_waves + 5 * w;
+                           int kc, int accumulate, cudaStream_t s) {
+  const int* wv = p->h_waves + kWaveInts * w;
   if (wv[3] == 0) return FSHT_OK;
   GemmArgs a;
   a.lmax = p->lmax;
   a.nnorth = p->nnorth;
   a.ngroups = (kc + kGroupMaps - 1) / kGroupMaps;
-  a.nks_max = (p->nnorth + kKStep - 1) / kKStep;
+  a.nks_max = ws_ksteps(p->lmax, p->nnorth);
   a.nkc_glob = (p->nnorth + kKChunk - 1) / kKChunk;
+  a.accumulate = accumulate;
   a.q0 = wv[0];
   a.ntmax = wv[2];
   a.nkcmax = wv[3];
@@ -616,6 +985,78 @@ int fsht_launch_split_gemm(fsht_plan* p, int w, const unsigned char* WS, const i
   FSHT_CUDA_TRY(
       cudaFuncSetAttribute(k_split_gemm, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
   k_split_gemm<<<dim3(a.ngroups, 2 * a.ntmax * a.nkcmax, wv[1] - wv[0]), kThreads, sm, s>>>(a);
+  FSHT_LAUNCH_CHECK();
+  return FSHT_OK;
+}
+
+int fsht_launch_split_synth_prepare(fsht_plan* p, const double* alm, unsigned char* WS, int* EB,
+                                    double2* W, int nmaps_total, int k0, int kc, cudaStream_t s) {
+  SliceAArgs a;
+  a.alm = alm;
+  a.ld = nmaps_total;
+  a.k0 = k0;
+  a.kc = kc;
+  a.lmax = p->lmax;
+  a.ngroups = (kc + kGroupMaps - 1) / kGroupMaps;
+  a.nkl_max = ws_ksteps(p->lmax, p->nnorth);
+  a.WS = WS;
+  a.EB = EB;
+  k_slice_alm<<<dim3(p->lmax + 1, 2, a.ngroups), 128, 0, s>>>(a);
+  FSHT_LAUNCH_CHECK();
+  const int nkl0 = (p->lmax / 2 + 1 + kKStep - 1) / kKStep;
+  if (nkl0 * kKStep > kKChunk) {
+    // l-chunks add into W: clear it first
+    FSHT_CUDA_TRY(cudaMemsetAsync(W, 0, sizeof(double2) * 2 * (size_t)(p->lmax + 1) * p->nnorth * kc,
+                                  s));
+  }
+  return FSHT_OK;
+}
+
+int fsht_launch_split_lambdaT(fsht_plan* p, int w, unsigned char* lbuf, cudaStream_t s) {
+  const int* wv = p->h_waves + kWaveInts * w;
+  if (wv[4] == 0) return FSHT_OK;
+  LamTArgs a;
+  a.lmax = p->lmax;
+  a.nnorth = p->nnorth;
+  a.q0 = wv[0];
+  a.eag = eag_of(p->lmax);
+  a.cth = p->d_cth;
+  a.sth = p->d_sth;
+  a.pref = p->d_pref;
+  a.ring_i0 = p->d_ring_i0;
+  a.tab = p->d_lamtab;
+  a.lam_offT = p->d_lam_offT;
+  a.lbuf = lbuf;
+  k_lambda_digits_T<<<dim3(wv[1] - wv[0], wv[4]), 128, 0, s>>>(a);
+  FSHT_LAUNCH_CHECK();
+  return FSHT_OK;
+}
+
+int fsht_launch_split_synth(fsht_plan* p, int w, const unsigned char* WS, const int* EB,
+                            const unsigned char* lbuf, double2* W, int kc, cudaStream_t s) {
+  const int* wv = p->h_waves + kWaveInts * w;
+  if (wv[4] == 0 || wv[6] == 0) return FSHT_OK;
+  SynthArgs a;
+  a.lmax = p->lmax;
+  a.nnorth = p->nnorth;
+  a.ngroups = (kc + kGroupMaps - 1) / kGroupMaps;
+  a.nkl_max = ws_ksteps(p->lmax, p->nnorth);
+  a.nkcl_glob = ((p->lmax / 2 + 1 + kKStep - 1) / kKStep * kKStep + kKChunk - 1) / kKChunk;
+  a.q0 = wv[0];
+  a.nkclmax = wv[6];
+  a.eag = eag_of(p->lmax);
+  a.ring_i0 = p->d_ring_i0;
+  a.lam_offT = p->d_lam_offT;
+  a.lbuf = lbuf;
+  a.WS = WS;
+  a.EB = EB;
+  a.W = reinterpret_cast<double*>(W);
+  a.kc = kc;
+  a.err = p->d_err;
+  const size_t sm = (size_t)kStagesG * kStageBytesG;
+  FSHT_CUDA_TRY(
+      cudaFuncSetAttribute(k_split_synth, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+  k_split_synth<<<dim3(a.ngroups, wv[4] * wv[6], wv[1] - wv[0]), kThreads, sm, s>>>(a);
   FSHT_LAUNCH_CHECK();
   return FSHT_OK;
 }

@@ -50,7 +50,7 @@ ScratchLayout layout_for(int nside, int lmax, const FshtFftLayout& f) {
   L.ring_i0 = o; o = align256(o + sizeof(int) * (lmax + 1));
   L.rfs = o;     o = align256(o + sizeof(FshtRingFFT) * nn);
   L.blue = o;    o = align256(o + sizeof(int) * nn);
-  L.tw = o;      o = align256(o + sizeof(double2) * (f.Pmax / 2));
+  L.tw = o;      o = align256(o + sizeof(double2) * (f.Tmax + f.P3max));
   L.chirp = o;   o = align256(o + sizeof(double2) * (size_t)(f.chirp_total > 0 ? f.chirp_total : 1));
   L.bhat = o;    o = align256(o + sizeof(double2) * (size_t)(f.bhat_total > 0 ? f.bhat_total : 1));
   L.work = o;
@@ -93,20 +93,14 @@ __global__ void k_noalloc_tables(int nside, int lmax, double* cth, double* sth, 
     for (int i = 0; i < nn; ++i) {
       FshtRingFFT r;
       r.n = ring_len(nside, i);
-      const bool pow2 = (r.n & (r.n - 1)) == 0;
-      r.bluestein = pow2 ? 0 : 1;
-      int P = 1, logP = 0;
-      const int need = pow2 ? r.n : 2 * r.n - 1;
-      while (P < need) { P <<= 1; ++logP; }
-      r.P = P;
-      r.logP = logP;
+      fsht_ring_fft_size(r);
       r.chirp_off = 0;
       r.bhat_off = 0;
       if (r.bluestein) {
         r.chirp_off = chirp_total;
         r.bhat_off = bhat_total;
         chirp_total += r.n;
-        bhat_total += P;
+        bhat_total += r.P;
         blue[nblue++] = i;
       }
       rfs[i] = r;
@@ -190,7 +184,9 @@ extern "C" int fsht_t2alm_noalloc(int nside, int lmax, const double* maps, doubl
   p.d_bhat = reinterpret_cast<double2*>(base + L.bhat);
   p.d_work = reinterpret_cast<double2*>(base + L.work);
   p.Pmax = f.Pmax;
-  p.logPmax = f.logPmax;
+  p.Tmax = f.Tmax;
+  p.logTmax = f.logTmax;
+  p.P3max = f.P3max;
   p.fft_smem = f.smem;
   p.nbuf = 1;
   int* blue = reinterpret_cast<int*>(base + L.blue);

@@ -433,6 +433,50 @@ int fsht_plan_sync(fsht_plan* p) {
   return FSHT_OK;
 }
 
+// ----------------------------------------------------------------- split form
+// One chunk's split-precision analysis of the {S, D} matrix W into alm (added when
+// accumulate), and synthesis of alm into W = {G_N, G_S}.
+static int split_analysis(fsht_plan* p, const double2* W, double* alm, int nmaps, int c0, int kc,
+                          int accumulate) {
+  {
+    FSHT_PROF(FSHT_KCAT_SLICE);
+    FSHT_TRY(fsht_launch_split_prepare(p, W, p->d_ws, p->d_eb, alm, nmaps, c0, kc, accumulate,
+                                       p->stream));
+  }
+  for (int w = 0; w < p->nwaves; ++w) {
+    {
+      FSHT_PROF(FSHT_KCAT_LAMBDA);
+      FSHT_TRY(fsht_launch_split_lambda(p, w, p->d_lbuf, p->stream));
+    }
+    {
+      FSHT_PROF(FSHT_KCAT_ANALYSIS);
+      FSHT_TRY(fsht_launch_split_gemm(p, w, p->d_ws, p->d_eb, p->d_lbuf, alm, nmaps, c0, kc,
+                                      accumulate, p->stream));
+    }
+  }
+  return FSHT_OK;
+}
+
+static int split_synthesis(fsht_plan* p, const double* alm, double2* W, int nmaps, int c0,
+                           int kc) {
+  {
+    FSHT_PROF(FSHT_KCAT_SLICE);
+    FSHT_TRY(fsht_launch_split_synth_prepare(p, alm, p->d_ws, p->d_eb, W, nmaps, c0, kc,
+                                             p->stream));
+  }
+  for (int w = 0; w < p->nwaves; ++w) {
+    {
+      FSHT_PROF(FSHT_KCAT_LAMBDA);
+      FSHT_TRY(fsht_launch_split_lambdaT(p, w, p->d_lbuf, p->stream));
+    }
+    {
+      FSHT_PROF(FSHT_KCAT_SYNTHESIS);
+      FSHT_TRY(fsht_launch_split_synth(p, w, p->d_ws, p->d_eb, p->d_lbuf, W, kc, p->stream));
+    }
+  }
+  return FSHT_OK;
+}
+
 // ----------------------------------------------------------------- temperature
 int fsht_t2alm(fsht_plan* p, const double* maps, double* alm, int nmaps, int niter, int method) {
   FSHT_TRY(check_call(p, nmaps, maps, alm));
@@ -443,10 +487,6 @@ int fsht_t2alm(fsht_plan* p, const double* maps, double* alm, int nmaps, int nit
   }
   FSHT_TRY(need_bufs(p, niter > 0 ? 2 : 1));
   if (p->precision == FSHT_PREC_SPLIT) {
-    if (niter > 0) {
-      fsht_set_error("the split-precision form runs niter = 0 analyses");
-      return FSHT_EUNSUPPORTED;
-    }
     for (int c0 = 0; c0 < nmaps; c0 += p->kchunk) {
       const int kc = nmaps - c0 < p->kchunk ? nmaps - c0 : p->kchunk;
       double2* W0 = work_buf(p, 0, kc);
@@ -455,21 +495,17 @@ int fsht_t2alm(fsht_plan* p, const double* maps, double* alm, int nmaps, int nit
         FSHT_TRY(fsht_launch_ring_fft_fwd(p, maps + (size_t)c0 * p->npix, p->npix, kc, W0,
                                           p->stream));
       }
-      {
-        FSHT_PROF(FSHT_KCAT_SLICE);
-        FSHT_TRY(fsht_launch_split_prepare(p, W0, p->d_ws, p->d_eb, alm, nmaps, c0, kc, 0,
-                                           p->stream));
-      }
-      for (int w = 0; w < p->nwaves; ++w) {
+      FSHT_TRY(split_analysis(p, W0, alm, nmaps, c0, kc, 0));
+      // Jacobi refinement: FP64 Fourier-space residual of a split synthesis, analysed
+      // in split precision and added
+      for (int it = 0; it < niter; ++it) {
+        double2* W1 = work_buf(p, 1, kc);
+        FSHT_TRY(split_synthesis(p, alm, W1, nmaps, c0, kc));
         {
-          FSHT_PROF(FSHT_KCAT_LAMBDA);
-          FSHT_TRY(fsht_launch_split_lambda(p, w, p->d_lbuf, p->stream));
+          FSHT_PROF(FSHT_KCAT_RESIDUAL);
+          FSHT_TRY(fsht_launch_fourier_residual(p, W0, W1, kc, method, p->stream));
         }
-        {
-          FSHT_PROF(FSHT_KCAT_ANALYSIS);
-          FSHT_TRY(fsht_launch_split_gemm(p, w, p->d_ws, p->d_eb, p->d_lbuf, alm, nmaps, c0, kc,
-                                          p->stream));
-        }
+        FSHT_TRY(split_analysis(p, W1, alm, nmaps, c0, kc, 1));
       }
     }
     return FSHT_OK;
@@ -512,7 +548,9 @@ int fsht_alm2t(fsht_plan* p, const double* alm, double* maps, int nmaps) {
   for (int c0 = 0; c0 < nmaps; c0 += p->kchunk) {
     const int kc = nmaps - c0 < p->kchunk ? nmaps - c0 : p->kchunk;
     double2* W0 = work_buf(p, 0, kc);
-    {
+    if (p->precision == FSHT_PREC_SPLIT) {
+      FSHT_TRY(split_synthesis(p, alm, W0, nmaps, c0, kc));
+    } else {
       FSHT_PROF(FSHT_KCAT_SYNTHESIS);
       FSHT_TRY(fsht_launch_synthesis_fp64(p, 0, alm, nullptr, W0, nullptr, nmaps, c0, kc,
                                           p->stream));

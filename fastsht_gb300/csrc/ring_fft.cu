@@ -21,52 +21,152 @@
 
 namespace {
 
-// In-place radix-2 DIT FFT of P = 2^logP points held in shared memory.
-// tw[j] = exp(-2 pi i j / 2^logPmax), j < 2^(logPmax-1).  inverse: exp(+...),
-// unnormalised.  All threads of the block must call it; it synchronises the block
-// on entry and on exit.
-__device__ void smem_fft(double2* buf, int P, int logP, const double2* __restrict__ tw,
-                         int logPmax, bool inverse) {
+// Twiddle tables: tw2[t] = exp(-2 pi i t / Tmax), t < Tmax (full circle, Tmax the largest
+// power-of-two factor of any transform size), tw3[t] = exp(-2 pi i t / P3max) for the
+// 3*2^k sizes.
+struct FftTw {
+  const double2* tw2;
+  const double2* tw3;
+  int logTmax, P3max;
+};
+
+constexpr double kSqrt3Half = 0.86602540378443864676;
+
+// In-place decimation-in-frequency FFT of rf.P points in shared memory, natural order in,
+// transform order out: an optional radix-3 pass (P = 3 T) splits the data into three
+// blocks of T = 2^logT, then radix-4 passes (radix-2^2 butterflies: three twiddles, none
+// in the last pass) and a radix-2 pass when logT is odd.  A power-of-two transform
+// leaves bin q at bit-reverse(q).  All threads of the block call it; it synchronises on
+// entry and after every pass.
+__device__ void fft_dif(double2* buf, const FshtRingFFT& rf, const FftTw& tw) {
   const int tid = threadIdx.x, nt = blockDim.x;
-  __syncthreads();   // the caller's writes to buf must land before the permutation
-  if (logP > 0) {
-    for (int i = tid; i < P; i += nt) {
-      int j = (int)(__brev((unsigned)i) >> (32 - logP));
-      if (j > i) {
-        double2 t = buf[i];
-        buf[i] = buf[j];
-        buf[j] = t;
+  const int logT = rf.logT, T = 1 << logT;
+  const int nblk = rf.r3 ? 3 : 1;
+  __syncthreads();   // the caller's writes to buf must land first
+  if (rf.r3) {
+    const int sc = tw.P3max / rf.P;
+    for (int j = tid; j < T; j += nt) {
+      const double2 a = buf[j], b = buf[j + T], c = buf[j + 2 * T];
+      const double2 sm = cadd(b, c), df = csub(b, c);
+      const double2 t = make_double2(fma(-0.5, sm.x, a.x), fma(-0.5, sm.y, a.y));
+      // w3 = exp(-2 pi i / 3): a + w3 b + w3^2 c = t - i (sqrt3/2) df, the other t + i ...
+      const double2 y1 = make_double2(fma(kSqrt3Half, df.y, t.x), fma(-kSqrt3Half, df.x, t.y));
+      const double2 y2 = make_double2(fma(-kSqrt3Half, df.y, t.x), fma(kSqrt3Half, df.x, t.y));
+      buf[j] = cadd(a, sm);
+      buf[j + T] = cmul(y1, __ldg(&tw.tw3[j * sc]));
+      buf[j + 2 * T] = cmul(y2, __ldg(&tw.tw3[2 * j * sc]));
+    }
+    __syncthreads();
+  }
+  int logspan = logT;
+  for (; logspan >= 2; logspan -= 2) {
+    const int lh = logspan - 2, h = 1 << lh;
+    const int per_blk = 1 << (logT - 2);
+    const int sh = tw.logTmax - logspan;
+    for (int idx = tid; idx < nblk * per_blk; idx += nt) {
+      const int blk = idx >> (logT - 2);
+      const int r = idx & (per_blk - 1);
+      const int j = r & (h - 1);
+      const int i0 = (blk << logT) + ((r >> lh) << logspan) + j;
+      const double2 a = buf[i0], b = buf[i0 + h], c = buf[i0 + 2 * h], d = buf[i0 + 3 * h];
+      const double2 apc = cadd(a, c), amc = csub(a, c), bpd = cadd(b, d), bmd = csub(b, d);
+      const double2 y1 = csub(apc, bpd);
+      const double2 y2 = make_double2(amc.x + bmd.y, amc.y - bmd.x);   // (a-c) - i(b-d)
+      const double2 y3 = make_double2(amc.x - bmd.y, amc.y + bmd.x);   // (a-c) + i(b-d)
+      buf[i0] = cadd(apc, bpd);
+      if (h == 1) {
+        buf[i0 + h] = y1;
+        buf[i0 + 2 * h] = y2;
+        buf[i0 + 3 * h] = y3;
+      } else {
+        buf[i0 + h] = cmul(y1, __ldg(&tw.tw2[(2 * j) << sh]));
+        buf[i0 + 2 * h] = cmul(y2, __ldg(&tw.tw2[j << sh]));
+        buf[i0 + 3 * h] = cmul(y3, __ldg(&tw.tw2[(3 * j) << sh]));
       }
     }
+    __syncthreads();
   }
-  __syncthreads();
-  for (int s = 1; s <= logP; ++s) {
-    const int half = 1 << (s - 1);
-    const int shift = logPmax - s;
-    for (int idx = tid; idx < (P >> 1); idx += nt) {
-      const int j = idx & (half - 1);
-      const int a = ((idx >> (s - 1)) << s) + j;
-      const int b = a + half;
-      double2 w = __ldg(&tw[j << shift]);
-      if (inverse) w.y = -w.y;
-      const double2 u = buf[a];
-      const double2 t = cmul(w, buf[b]);
-      buf[a] = cadd(u, t);
-      buf[b] = csub(u, t);
+  if (logspan == 1) {
+    for (int idx = tid; idx < nblk << (logT - 1); idx += nt) {
+      const double2 a = buf[2 * idx], b = buf[2 * idx + 1];
+      buf[2 * idx] = cadd(a, b);
+      buf[2 * idx + 1] = csub(a, b);
     }
     __syncthreads();
   }
 }
 
-// DFT of n points (in buf[0..n)) -> Z (in buf[0..n)); forward (e^{-2 pi i jk/n}).
-// For non power-of-two n uses Bluestein with the ring's precomputed chirp and
-// filter spectrum (filter already divided by P).
-__device__ void ring_dft(double2* buf, const FshtRingFFT& rf, const double2* __restrict__ tw,
-                         int logPmax, const double2* __restrict__ chirp,
-                         const double2* __restrict__ bhat) {
+// The inverse of fft_dif without normalisation (P times the inverse DFT): transform order
+// in, natural order out; the passes of fft_dif in reverse with conjugate twiddles.
+__device__ void fft_dit_inv(double2* buf, const FshtRingFFT& rf, const FftTw& tw) {
+  const int tid = threadIdx.x, nt = blockDim.x;
+  const int logT = rf.logT, T = 1 << logT;
+  const int nblk = rf.r3 ? 3 : 1;
+  __syncthreads();
+  int logspan = 2;
+  if (logT & 1) {
+    for (int idx = tid; idx < nblk << (logT - 1); idx += nt) {
+      const double2 a = buf[2 * idx], b = buf[2 * idx + 1];
+      buf[2 * idx] = cadd(a, b);
+      buf[2 * idx + 1] = csub(a, b);
+    }
+    __syncthreads();
+    logspan = 3;
+  }
+  for (; logspan <= logT; logspan += 2) {
+    const int lh = logspan - 2, h = 1 << lh;
+    const int per_blk = 1 << (logT - 2);
+    const int sh = tw.logTmax - logspan;
+    for (int idx = tid; idx < nblk * per_blk; idx += nt) {
+      const int blk = idx >> (logT - 2);
+      const int r = idx & (per_blk - 1);
+      const int j = r & (h - 1);
+      const int i0 = (blk << logT) + ((r >> lh) << logspan) + j;
+      const double2 y0 = buf[i0];
+      double2 z1 = buf[i0 + h], z2 = buf[i0 + 2 * h], z3 = buf[i0 + 3 * h];
+      if (h > 1) {
+        z1 = cmul(z1, cconj(__ldg(&tw.tw2[(2 * j) << sh])));
+        z2 = cmul(z2, cconj(__ldg(&tw.tw2[j << sh])));
+        z3 = cmul(z3, cconj(__ldg(&tw.tw2[(3 * j) << sh])));
+      }
+      const double2 sp = cadd(y0, z1), dm = csub(y0, z1), e = cadd(z2, z3), f = csub(z2, z3);
+      buf[i0] = cadd(sp, e);
+      buf[i0 + 2 * h] = csub(sp, e);
+      buf[i0 + h] = make_double2(dm.x - f.y, dm.y + f.x);       // d + i f
+      buf[i0 + 3 * h] = make_double2(dm.x + f.y, dm.y - f.x);   // d - i f
+    }
+    __syncthreads();
+  }
+  if (rf.r3) {
+    const int sc = tw.P3max / rf.P;
+    for (int j = tid; j < T; j += nt) {
+      const double2 a = buf[j];
+      const double2 b = cmul(buf[j + T], cconj(__ldg(&tw.tw3[j * sc])));
+      const double2 c = cmul(buf[j + 2 * T], cconj(__ldg(&tw.tw3[2 * j * sc])));
+      const double2 sm = cadd(b, c), df = csub(b, c);
+      const double2 t = make_double2(fma(-0.5, sm.x, a.x), fma(-0.5, sm.y, a.y));
+      buf[j] = cadd(a, sm);
+      buf[j + T] = make_double2(fma(-kSqrt3Half, df.y, t.x), fma(kSqrt3Half, df.x, t.y));
+      buf[j + 2 * T] = make_double2(fma(kSqrt3Half, df.y, t.x), fma(-kSqrt3Half, df.x, t.y));
+    }
+    __syncthreads();
+  }
+}
+
+// Where bin q of ring_dft's output sits in buf.
+__device__ __forceinline__ int dft_bin(const FshtRingFFT& rf, int q) {
+  return rf.bluestein ? q : (int)(__brev((unsigned)q) >> (32 - rf.logT));
+}
+
+// DFT of n points (in buf[0..n)), forward (e^{-2 pi i jk/n}); bin q lands at
+// buf[dft_bin(rf, q)].  A power-of-two ring is one fft_dif; any other length uses
+// Bluestein with the ring's chirp and filter spectrum (transform order, divided by P):
+// chirp, fft_dif, filter, fft_dit_inv, chirp, natural order out.
+__device__ void ring_dft(double2* buf, const FshtRingFFT& rf, const FftTw& tw,
+                         const double2* __restrict__ chirp, const double2* __restrict__ bhat) {
   const int tid = threadIdx.x, nt = blockDim.x;
   if (!rf.bluestein) {
-    smem_fft(buf, rf.P, rf.logP, tw, logPmax, false);
+    fft_dif(buf, rf, tw);
     return;
   }
   const int n = rf.n, P = rf.P;
@@ -74,27 +174,31 @@ __device__ void ring_dft(double2* buf, const FshtRingFFT& rf, const double2* __r
     if (j < n) buf[j] = cmul(buf[j], __ldg(&chirp[j]));
     else buf[j] = make_double2(0.0, 0.0);
   }
-  smem_fft(buf, P, rf.logP, tw, logPmax, false);
+  fft_dif(buf, rf, tw);
   for (int j = tid; j < P; j += nt) buf[j] = cmul(buf[j], __ldg(&bhat[j]));
-  smem_fft(buf, P, rf.logP, tw, logPmax, true);
+  fft_dit_inv(buf, rf, tw);
   for (int j = tid; j < n; j += nt) buf[j] = cmul(buf[j], __ldg(&chirp[j]));
   __syncthreads();
 }
 
 // ------------------------------------------------------------------ tables
-__global__ void k_twiddles(double2* tw, int Pmax) {
-  int j = blockIdx.x * blockDim.x + threadIdx.x;
-  if (j < Pmax / 2) {
-    double s, c;
-    sincospi(-2.0 * (double)j / (double)Pmax, &s, &c);
+__global__ void k_twiddles(double2* tw, int Tmax, int P3max) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  double s, c;
+  if (j < Tmax) {
+    sincospi(-2.0 * (double)j / (double)Tmax, &s, &c);
+    tw[j] = make_double2(c, s);
+  } else if (j < Tmax + P3max) {
+    const int t = j - Tmax;
+    sincospi(-2.0 * (double)t / (double)P3max, &s, &c);
     tw[j] = make_double2(c, s);
   }
 }
 
-// chirp w_j = exp(-i pi j^2 / n) and the wrapped filter b (time domain) for one ring;
-// block per Bluestein ring.
+// chirp w_j = exp(-i pi j^2 / n) and the filter spectrum (fft_dif of the wrapped conj
+// chirp, over P) for one ring; block per Bluestein ring.
 __global__ void k_bluestein_tables(const FshtRingFFT* rfs, const int* rings, double2* chirp,
-                                   double2* bhat, const double2* tw, int logPmax) {
+                                   double2* bhat, FftTw tw) {
   extern __shared__ double2 sbuf[];
   const FshtRingFFT rf = rfs[rings[blockIdx.x]];
   const int n = rf.n, P = rf.P;
@@ -112,8 +216,7 @@ __global__ void k_bluestein_tables(const FshtRingFFT* rfs, const int* rings, dou
     else if (P - j < n) v = cconj(w[P - j]);
     sbuf[j] = v;
   }
-  __syncthreads();
-  smem_fft(sbuf, P, rf.logP, tw, logPmax, false);
+  fft_dif(sbuf, rf, tw);
   const double invP = 1.0 / (double)P;
   for (int j = threadIdx.x; j < P; j += blockDim.x) bhat[rf.bhat_off + j] = cscale(sbuf[j], invP);
 }
@@ -126,8 +229,7 @@ struct FwdArgs {
   int maps_per_block;
   int nside, lmax, nnorth, nring, ring_base;
   const FshtRingFFT* rfs;
-  const double2* tw;
-  int logPmax;
+  FftTw tw;
   const double2* chirp;
   const double2* bhat;
   const int* ring_i0;
@@ -169,13 +271,13 @@ __global__ void __launch_bounds__(512) k_ring_fft_fwd(FwdArgs a) {
     for (int j = tid; j < n; j += nt)
       buf[j] = make_double2(__ldg(&xn[j]), equator ? 0.0 : __ldg(&xs[j]));
     __syncthreads();
-    ring_dft(buf, rf, a.tw, a.logPmax, chirp, bhat);
+    ring_dft(buf, rf, a.tw, chirp, bhat);
     // Z = FFT(x_N + i x_S): X_N[q] = (Z[q] + conj Z[-q])/2, X_S[q] = (Z[q] - conj Z[-q])/(2i)
     for (int m = tid; m <= mtop; m += nt) {
       const int q = m % n;
       const int qn = (q == 0) ? 0 : n - q;
-      const double2 zq = buf[q];
-      const double2 zn = cconj(buf[qn]);
+      const double2 zq = buf[dft_bin(rf, q)];
+      const double2 zn = cconj(buf[dft_bin(rf, qn)]);
       const double2 xN = cscale(cadd(zq, zn), 0.5);
       const double2 dd = csub(zq, zn);
       const double2 xS = make_double2(0.5 * dd.y, -0.5 * dd.x);
@@ -202,8 +304,7 @@ struct InvArgs {
   int kc, maps_per_block;
   int nside, lmax, nnorth, nring, ring_base;
   const FshtRingFFT* rfs;
-  const double2* tw;
-  int logPmax;
+  FftTw tw;
   const double2* chirp;
   const double2* bhat;
   const int* ring_i0;
@@ -270,11 +371,11 @@ __global__ void __launch_bounds__(512) k_ring_fft_inv(InvArgs a) {
     // inverse DFT = conj(DFT(conj Z))
     for (int j = tid; j < n; j += nt) buf[j] = cconj(buf[j]);
     __syncthreads();
-    ring_dft(buf, rf, a.tw, a.logPmax, chirp, bhat);
+    ring_dft(buf, rf, a.tw, chirp, bhat);
     double* xn = a.maps + (long long)k * a.map_stride + off_n;
     double* xs = a.maps + (long long)k * a.map_stride + off_s;
     for (int j = tid; j < n; j += nt) {
-      const double2 z = buf[j];   // conj applied: x_N = Re, x_S = -Im of the DFT output
+      const double2 z = buf[dft_bin(rf, j)];   // conj applied: x_N = Re, x_S = -Im of the DFT
       xn[j] = z.x;
       if (!equator) xs[j] = -z.y;
     }
@@ -438,32 +539,28 @@ int maps_per_block_for(int kc, int nrings_launched) {
 int fsht_fft_layout(int nside, int lmax, FshtFftLayout* lay, FshtRingFFT* rfs, int* blue_rings) {
   const int nn = 2 * nside;
   long long chirp_total = 0, bhat_total = 0;
-  int Pmax = 2, nblue = 0;
+  int Pmax = 4, logTmax = 2, P3max = 0, nblue = 0;
   for (int i = 0; i < nn; ++i) {
     FshtRingFFT r{};
     r.n = ring_len(nside, i);
-    const bool pow2 = (r.n & (r.n - 1)) == 0;
-    r.bluestein = pow2 ? 0 : 1;
-    int P = 1, logP = 0;
-    const int need = pow2 ? r.n : 2 * r.n - 1;
-    while (P < need) { P <<= 1; ++logP; }
-    r.P = P;
-    r.logP = logP;
+    fsht_ring_fft_size(r);
     if (r.bluestein) {
       r.chirp_off = chirp_total;
       r.bhat_off = bhat_total;
       chirp_total += r.n;
-      bhat_total += P;
+      bhat_total += r.P;
       if (blue_rings) blue_rings[nblue] = i;
       ++nblue;
     }
-    if (P > Pmax) Pmax = P;
+    if (r.P > Pmax) Pmax = r.P;
+    if (r.logT > logTmax) logTmax = r.logT;
+    if (r.r3 && r.P > P3max) P3max = r.P;
     if (rfs) rfs[i] = r;
   }
-  int logPmax = 0;
-  while ((1 << logPmax) < Pmax) ++logPmax;
   lay->Pmax = Pmax;
-  lay->logPmax = logPmax;
+  lay->Tmax = 1 << logTmax;
+  lay->logTmax = logTmax;
+  lay->P3max = P3max;
   lay->chirp_total = chirp_total;
   lay->bhat_total = bhat_total;
   lay->nblue = nblue;
@@ -477,15 +574,27 @@ int fsht_fft_layout(int nside, int lmax, FshtFftLayout* lay, FshtRingFFT* rfs, i
   return FSHT_OK;
 }
 
+namespace {
+FftTw plan_tw(const fsht_plan* p) {
+  FftTw t;
+  t.tw2 = p->d_tw;
+  t.tw3 = p->d_tw + p->Tmax;
+  t.logTmax = p->logTmax;
+  t.P3max = p->P3max;
+  return t;
+}
+}  // namespace
+
 int fsht_fft_tables_fill(fsht_plan* p, const int* d_blue_rings, int nblue, cudaStream_t s) {
-  k_twiddles<<<(p->Pmax / 2 + 255) / 256, 256, 0, s>>>(p->d_tw, p->Pmax);
+  const int ntw = p->Tmax + p->P3max;
+  k_twiddles<<<(ntw + 255) / 256, 256, 0, s>>>(p->d_tw, p->Tmax, p->P3max);
   FSHT_LAUNCH_CHECK();
   if (nblue > 0) {
     const size_t sm = (size_t)p->Pmax * sizeof(double2);
     FSHT_CUDA_TRY(cudaFuncSetAttribute(k_bluestein_tables,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
     k_bluestein_tables<<<(unsigned)nblue, 512, sm, s>>>(p->d_rfft, d_blue_rings, p->d_chirp,
-                                                         p->d_bhat, p->d_tw, p->logPmax);
+                                                         p->d_bhat, plan_tw(p));
     FSHT_LAUNCH_CHECK();
   }
   return FSHT_OK;
@@ -499,12 +608,14 @@ int fsht_fft_tables_init(fsht_plan* p) {
   int rc = fsht_fft_layout(p->nside, p->lmax, &lay, rfs.data(), blue_rings.data());
   if (rc) return rc;
   p->Pmax = lay.Pmax;
-  p->logPmax = lay.logPmax;
+  p->Tmax = lay.Tmax;
+  p->logTmax = lay.logTmax;
+  p->P3max = lay.P3max;
   p->fft_smem = lay.smem;
   FSHT_CUDA_TRY(cudaMalloc(&p->d_rfft, sizeof(FshtRingFFT) * nn));
   FSHT_CUDA_TRY(cudaMemcpyAsync(p->d_rfft, rfs.data(), sizeof(FshtRingFFT) * nn,
                                 cudaMemcpyHostToDevice, p->stream));
-  FSHT_CUDA_TRY(cudaMalloc(&p->d_tw, sizeof(double2) * (lay.Pmax / 2)));
+  FSHT_CUDA_TRY(cudaMalloc(&p->d_tw, sizeof(double2) * (lay.Tmax + lay.P3max)));
   FSHT_CUDA_TRY(cudaMalloc(&p->d_chirp, sizeof(double2) * (lay.chirp_total > 0 ? lay.chirp_total : 1)));
   FSHT_CUDA_TRY(cudaMalloc(&p->d_bhat, sizeof(double2) * (lay.bhat_total > 0 ? lay.bhat_total : 1)));
   int* d_rings = nullptr;
@@ -553,8 +664,7 @@ int fsht_launch_ring_fft_fwd(fsht_plan* p, const double* maps, long long map_str
   a.nring = p->nring;
   a.ring_base = 0;
   a.rfs = p->d_rfft;
-  a.tw = p->d_tw;
-  a.logPmax = p->logPmax;
+  a.tw = plan_tw(p);
   a.chirp = p->d_chirp;
   a.bhat = p->d_bhat;
   a.ring_i0 = p->d_ring_i0;
@@ -581,8 +691,7 @@ int fsht_launch_ring_fft_inv(fsht_plan* p, const double2* W, double* maps, long 
   a.nring = p->nring;
   a.ring_base = 0;
   a.rfs = p->d_rfft;
-  a.tw = p->d_tw;
-  a.logPmax = p->logPmax;
+  a.tw = plan_tw(p);
   a.chirp = p->d_chirp;
   a.bhat = p->d_bhat;
   a.ring_i0 = p->d_ring_i0;

@@ -48,8 +48,9 @@ class SHT:
     SHT(nside, lmax, nsim, niter=0, pol=False, all_buff=False) as in the
     reference (SHT.py:17).  Extra keywords: ``device`` (CUDA device index),
     ``workspace_limit`` (bytes of workspace, 0 = library default) and ``precision``:
-    "fp64" (the plain method, all FP64) or "split" (t2alm's Legendre contraction as
-    BF16 slice products on the tensor cores, ~1e-8 max relative alm error).
+    "fp64" (the plain method, all FP64) or "split" (the temperature Legendre
+    contractions of t2alm and alm2t as BF16 digit products on the tensor cores, ~3e-8 max
+    relative alm error; niter > 0 refines with the FP64 Fourier-space residual).
     """
 
     def __init__(self, nside, lmax, nsim, niter=0, pol=False, all_buff=False, *,
@@ -230,6 +231,8 @@ class SHT:
             dmaps = self._new_dev_maps()
             _lib.call("fsht_alm2t", self._plan, C.c_void_p(dalm.data_ptr()),
                       C.c_void_p(dmaps.data_ptr()), self.nsim)
+            if self.precision == "split":
+                _lib.call("fsht_plan_sync", self._plan)   # surfaces expired device waits
             return self._maps_out(dmaps, maps_in, as_torch)
 
     def qu2eb(self, Q, U, almEs_in=None, almBs_in=None, method='old'):

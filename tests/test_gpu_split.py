@@ -65,3 +65,64 @@ def test_split_matches_fp64_path_at_nside_1024():
     a64 = SHT(ns, lmax, nsim).t2alm(maps)
     a16 = SHT(ns, lmax, nsim, precision="split").t2alm(maps)
     assert rel_alm_err(a16, a64) <= SPLIT_TOL
+
+
+def rel_map_err(a, b):
+    """max over maps of max_pix |a - b| / max_pix |b| ((npix, nsim) arrays)."""
+    d = np.abs(np.asarray(a) - np.asarray(b)).max(axis=0)
+    return float((d / np.abs(np.asarray(b)).max(axis=0)).max())
+
+
+def _alm(lmax, nsim, seed):
+    rng = np.random.default_rng(seed)
+    l = np.arange(lmax + 1, dtype=float)
+    cl = 1.0 / np.maximum(l, 1.0) ** 2
+    cl[0] = 0
+    return gaussian_alm(cl, lmax, nsim, rng)
+
+
+@pytest.mark.parametrize("ns,lmax,nsim", [(4, 11, 2), (16, 47, 5), (64, 191, 70), (128, 300, 3)])
+def test_split_alm2t_matches_oracle(ns, lmax, nsim):
+    """Split synthesis (lambda against one global scale, alm digits per column) against
+    the FP64 oracle's alm2map."""
+    alm = _alm(lmax, nsim, ns + 7)
+    sht = SHT(ns, lmax, nsim, precision="split")
+    got = sht.alm2t(alm)
+    want = OracleSHT(ns, lmax, ring_tab=sht.ring_skip()).alm2t(alm)
+    assert rel_map_err(got, want) <= SPLIT_TOL
+
+
+def test_split_alm2t_l_chunks_at_lmax_2100():
+    """lmax 2100: more than 1024 l of one parity, so l-chunks add into the phase matrix."""
+    ns, lmax, nsim = 512, 2100, 2
+    alm = _alm(lmax, nsim, 11)
+    m64 = SHT(ns, lmax, nsim).alm2t(alm)
+    m16 = SHT(ns, lmax, nsim, precision="split").alm2t(alm)
+    assert rel_map_err(m16, m64) <= SPLIT_TOL
+
+
+@pytest.mark.parametrize("method", ["old", "new"])
+@pytest.mark.parametrize("niter", [1, 2])
+def test_split_refinement_matches_fp64_iterations(niter, method):
+    """niter Jacobi refinement steps in the split form (split synthesis and analysis, FP64
+    Fourier-space residual) against the plain path with the same niter and method."""
+    ns, lmax, nsim = 64, 191, 6
+    maps = bandlimited_maps(ns, lmax, nsim, 5)
+    a64 = SHT(ns, lmax, nsim, niter=niter).t2alm(maps, method=method)
+    a16 = SHT(ns, lmax, nsim, niter=niter, precision="split").t2alm(maps, method=method)
+    assert rel_alm_err(a16, a64) <= SPLIT_TOL
+    # the refinement does its job: the round trip improves over niter = 0
+    a0 = SHT(ns, lmax, nsim, precision="split").t2alm(maps)
+    back = SHT(ns, lmax, nsim)
+    r0 = np.abs(back.alm2t(a0) - maps).max()
+    r1 = np.abs(back.alm2t(a16) - maps).max()
+    assert r1 < 0.5 * r0
+
+
+def test_split_refinement_at_nside_1024():
+    """One refinement step at the precision-form config size (4 maps)."""
+    ns, lmax, nsim = 1024, 2047, 4
+    maps = bandlimited_maps(ns, lmax, nsim, 2)
+    a64 = SHT(ns, lmax, nsim, niter=1).t2alm(maps)
+    a16 = SHT(ns, lmax, nsim, niter=1, precision="split").t2alm(maps)
+    assert rel_alm_err(a16, a64) <= SPLIT_TOL
