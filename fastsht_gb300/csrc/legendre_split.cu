@@ -41,6 +41,10 @@ constexpr int kKChunk = 1024;       // rings per CTA (keeps levels 0 and 1 exact
 constexpr int kSlices = 4;
 constexpr uint32_t kATileBytes = kRows * kKStep * 2;    // 4 KB per (k-step, digit)
 constexpr uint32_t kBTileBytes = kCols * kKStep * 2;    // 4 KB per (k-step, digit)
+// Synthesis B tiles carry three more digit planes, d1..d3 times 2^-8 (exact in BF16), so
+// the level-4 products fold into the level-3 accumulator.
+constexpr int kSynthPlanes = 7;
+constexpr uint32_t kSynthBBytes = kSynthPlanes * kBTileBytes;   // 28 KB per l-step
 constexpr int kThreads = 192;
 constexpr int kEmptyExp = -4000;    // column exponent of an all-zero column
 
@@ -89,7 +93,8 @@ __device__ __forceinline__ void rec_seed(double sth, double pref, int m, double&
 // rings, 128 B) at (c/8)*256 + (k/8)*128.  Rings beyond the kept range are zero.
 struct SliceArgs {
   const double2* W;
-  int kc, nnorth, ngroups, nks_max;
+  int kc, nnorth, ngroups;
+  size_t row_bytes;      // WS bytes per (m, parity, group)
   const int* ring_i0;
   unsigned char* WS;
   int* EB;
@@ -114,7 +119,7 @@ __global__ void __launch_bounds__(128) k_slice_phase(SliceArgs a) {
   a.EB[(((long long)m * 2 + p) * a.ngroups + g) * kCols + c] = E;
   const int nks = (K + kKStep - 1) / kKStep;
   unsigned char* base =
-      a.WS + (((size_t)(m * 2 + p) * a.ngroups + g) * a.nks_max) * kSlices * kBTileBytes;
+      a.WS + ((size_t)(m * 2 + p) * a.ngroups + g) * a.row_bytes;
   for (int t = 0; t < nks; ++t) {
     for (int half = 0; half < 2; ++half) {
       uint16_t s[kSlices][8];
@@ -220,6 +225,15 @@ __global__ void __launch_bounds__(128) k_lambda_digits(LamArgs a) {
     rec_seed(a.sth[i0 + r], a.pref[m], m, s1, e);
     et = 600 * e;
   }
+  // the 32 recursion rows of the current block, staged in shared memory (uniform reads
+  // off the dependency chain)
+  __shared__ double s_beta[kLamBlock];
+  __shared__ int s_erow[kLamBlock];
+  if (tid < kLamBlock && m + tid <= a.lmax) {
+    s_beta[tid] = tab[tid].beta;
+    s_erow[tid] = tab[tid].erow;
+  }
+  __syncthreads();
   const int lend = ntiles * 2 * kRows;
   for (int lb = 0; lb < lend; lb += kLamBlock) {
 #pragma unroll 4
@@ -227,8 +241,8 @@ __global__ void __launch_bounds__(128) k_lambda_digits(LamArgs a) {
       const int j = lb + jj;
       unsigned long long pk = 0;
       if (m + j <= a.lmax) {
-        const double beta = tab[j].beta;
-        const int erow = tab[j].erow;
+        const double beta = s_beta[jj];
+        const int erow = s_erow[jj];
         if (j > 0) {
           const double t = beta * s2;
           const double nx = fma(x, s1, -t);
@@ -292,6 +306,10 @@ __global__ void __launch_bounds__(128) k_lambda_digits(LamArgs a) {
         *reinterpret_cast<uint4*>(tile + (size_t)d * kATileBytes) = o;
       }
     }
+    if (tid < kLamBlock && m + lb + kLamBlock + tid <= a.lmax) {
+      s_beta[tid] = tab[lb + kLamBlock + tid].beta;
+      s_erow[tid] = tab[lb + kLamBlock + tid].erow;
+    }
     __syncthreads();
   }
 }
@@ -305,7 +323,8 @@ constexpr int kStagesG = 6;
 constexpr uint32_t kStageBytesG = 2 * kSlices * kATileBytes;    // 32 KB: A then B
 
 struct GemmArgs {
-  int lmax, nnorth, ngroups, nks_max, nkc_glob, q0, ntmax, nkcmax, accumulate;
+  int lmax, nnorth, ngroups, nkc_glob, q0, ntmax, nkcmax, accumulate;
+  size_t row_bytes;
   const int* ring_i0;
   const long long* lam_off;
   const FshtLamRow* tab;
@@ -382,7 +401,8 @@ __global__ void __launch_bounds__(kThreads, 1) k_split_gemm(GemmArgs a) {
         a.lbuf + (size_t)(a.lam_off[q] - a.lam_off[a.q0]) * kSlices * kATileBytes +
         ((size_t)(p * ntiles + t) * nks + ks0) * kSlices * kATileBytes;
     const unsigned char* bsrc =
-        a.WS + ((((size_t)m * 2 + p) * a.ngroups + g) * a.nks_max + ks0) * kSlices * kBTileBytes;
+        a.WS + (((size_t)m * 2 + p) * a.ngroups + g) * a.row_bytes +
+        (size_t)ks0 * kSlices * kBTileBytes;
     for (int i = 0; i < nk; ++i) {
       const uint32_t st = i % kStagesG;
       if (!tc::mbar_wait(&h.empty[st], ((i / kStagesG) & 1) ^ 1, abort)) break;
@@ -527,7 +547,11 @@ __global__ void __launch_bounds__(128) k_lambda_digits_T(LamTArgs a) {
     rec_seed(a.sth[i0 + r], a.pref[m], m, s1, e);
     et = 600 * e;
   }
+  __shared__ FshtLamRow s_tab[32];
   for (int kl = 0; kl < nkl; ++kl) {
+    __syncthreads();                      // the previous block's rows are no longer read
+    if (tid < 32 && m + kl * 32 + tid <= a.lmax) s_tab[tid] = tab[kl * 32 + tid];
+    __syncthreads();
 #pragma unroll
     for (int half = 0; half < 2; ++half) {
       uint32_t pk[2][kSlices][4];
@@ -542,7 +566,7 @@ __global__ void __launch_bounds__(128) k_lambda_digits_T(LamTArgs a) {
         const int j = kl * 32 + half * 16 + jj;
         uint16_t d[4] = {0, 0, 0, 0};
         if (m + j <= a.lmax) {
-          const FshtLamRow rw = tab[j];
+          const FshtLamRow rw = s_tab[half * 16 + jj];
           if (j > 0) {
             const double t = rw.beta * s2;
             const double nx = fma(x, s1, -t);
@@ -587,7 +611,8 @@ __global__ void __launch_bounds__(128) k_lambda_digits_T(LamTArgs a) {
 // Re/Im = c >> 6).  Tile (m, p, g, l-step): 128 columns x 16 l, K-major.
 struct SliceAArgs {
   const double* alm;
-  int ld, k0, kc, lmax, ngroups, nkl_max;
+  int ld, k0, kc, lmax, ngroups;
+  size_t row_bytes;
   unsigned char* WS;
   int* EB;
 };
@@ -613,23 +638,25 @@ __global__ void __launch_bounds__(128) k_slice_alm(SliceAArgs a) {
   a.EB[(((long long)m * 2 + p) * a.ngroups + g) * kCols + c] = E;
   const int nkl = (cnt0 + kKStep - 1) / kKStep;
   unsigned char* base = a.WS +
-                        (((size_t)(m * 2 + p) * a.ngroups + g) * a.nkl_max) * kSlices * kBTileBytes +
+                        ((size_t)(m * 2 + p) * a.ngroups + g) * a.row_bytes +
                         (c >> 3) * 256 + (c & 7) * 16;
   for (int kl = 0; kl < nkl; ++kl) {
     for (int half = 0; half < 2; ++half) {
-      uint16_t sl[kSlices][8];
+      uint16_t sl[kSynthPlanes][8];
       for (int j = 0; j < 8; ++j) {
         uint16_t q4[4] = {0, 0, 0, 0};
         if (E != kEmptyExp) tc::digits4(val(kl * kKStep + half * 8 + j), E, q4);
         for (int d = 0; d < kSlices; ++d) sl[d][j] = q4[d];
+        for (int d = 1; d < kSlices; ++d) sl[kSlices - 1 + d][j] = tc::bf16_scale_2m8(q4[d]);
       }
-      for (int d = 0; d < kSlices; ++d) {
+      for (int d = 0; d < kSynthPlanes; ++d) {
         uint4 pk;
         pk.x = sl[d][0] | ((uint32_t)sl[d][1] << 16);
         pk.y = sl[d][2] | ((uint32_t)sl[d][3] << 16);
         pk.z = sl[d][4] | ((uint32_t)sl[d][5] << 16);
         pk.w = sl[d][6] | ((uint32_t)sl[d][7] << 16);
-        *reinterpret_cast<uint4*>(base + ((size_t)kl * kSlices + d) * kBTileBytes + half * 128) = pk;
+        *reinterpret_cast<uint4*>(base + (size_t)kl * kSynthBBytes + (size_t)d * kBTileBytes +
+                                  half * 128) = pk;
       }
     }
   }
@@ -639,7 +666,8 @@ __global__ void __launch_bounds__(128) k_slice_alm(SliceAArgs a) {
 // TMEM accumulators (E first, written as G_N = G_S = E; then O, added to G_N and subtracted
 // from G_S by the same threads).  Roles as in k_split_gemm.
 struct SynthArgs {
-  int lmax, nnorth, ngroups, nkl_max, nkcl_glob, q0, nkclmax, eag;
+  int lmax, nnorth, ngroups, nkcl_glob, q0, nkclmax, eag;
+  size_t row_bytes;
   const int* ring_i0;
   const long long* lam_offT;
   const unsigned char* lbuf;
@@ -650,8 +678,11 @@ struct SynthArgs {
   int* err;
 };
 
+constexpr int kStagesS = 4;
+constexpr uint32_t kStageBytesS = kSlices * kATileBytes + kSynthBBytes;   // 44 KB
+
 struct __align__(8) SynthSmemHdr {
-  uint64_t full[kStagesG], empty[kStagesG], tfull, tempty, fin;
+  uint64_t full[kStagesS], empty[kStagesS], tfull, tempty, fin;
   uint32_t tmem;
   int abort;
 };
@@ -679,7 +710,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_split_synth(SynthArgs a) {
   const int warp = tid >> 5;
   volatile int* abort = &h.abort;
   if (tid == 0) {
-    for (int s = 0; s < kStagesG; ++s) {
+    for (int s = 0; s < kStagesS; ++s) {
       tc::mbar_init(&h.full[s], 1);
       tc::mbar_init(&h.empty[s], 1);
     }
@@ -707,16 +738,16 @@ __global__ void __launch_bounds__(kThreads, 1) k_split_synth(SynthArgs a) {
         a.lbuf + (size_t)(a.lam_offT[q] - a.lam_offT[a.q0]) * kSlices * kATileBytes;
     for (int i = 0; i < 2 * nk; ++i) {
       const int par = i / nk, kk = kl0 + i % nk;
-      const uint32_t st = i % kStagesG;
-      if (!tc::mbar_wait(&h.empty[st], ((i / kStagesG) & 1) ^ 1, abort)) break;
-      unsigned char* dst = smem + st * kStageBytesG;
+      const uint32_t st = i % kStagesS;
+      if (!tc::mbar_wait(&h.empty[st], ((i / kStagesS) & 1) ^ 1, abort)) break;
+      unsigned char* dst = smem + st * kStageBytesS;
       const unsigned char* asrc =
           abase + ((size_t)(par * nrb + rb) * nkl + kk) * kSlices * kATileBytes;
-      const unsigned char* bsrc =
-          a.WS + ((((size_t)m * 2 + par) * a.ngroups + g) * a.nkl_max + kk) * kSlices * kBTileBytes;
-      tc::mbar_arrive_expect_tx(&h.full[st], kStageBytesG);
+      const unsigned char* bsrc = a.WS + (((size_t)m * 2 + par) * a.ngroups + g) * a.row_bytes +
+                                  (size_t)kk * kSynthBBytes;
+      tc::mbar_arrive_expect_tx(&h.full[st], kStageBytesS);
       tc::bulk_g2s(dst, asrc, kSlices * kATileBytes, &h.full[st]);
-      tc::bulk_g2s(dst + kSlices * kATileBytes, bsrc, kSlices * kBTileBytes, &h.full[st]);
+      tc::bulk_g2s(dst + kSlices * kATileBytes, bsrc, kSynthBBytes, &h.full[st]);
       ++n_loaded;
     }
   } else if (tid == 160) {
@@ -729,10 +760,10 @@ __global__ void __launch_bounds__(kThreads, 1) k_split_synth(SynthArgs a) {
         if (!tc::mbar_wait(&h.tempty, 0, abort)) break;
         tc::tc_fence_after();
       }
-      const uint32_t st = i % kStagesG;
-      if (!tc::mbar_wait(&h.full[st], (i / kStagesG) & 1, abort)) break;
+      const uint32_t st = i % kStagesS;
+      if (!tc::mbar_wait(&h.full[st], (i / kStagesS) & 1, abort)) break;
       tc::tc_fence_after();
-      const uint32_t abase = s_u + st * kStageBytesG;
+      const uint32_t abase = s_u + st * kStageBytesS;
       const uint32_t bbase = abase + kSlices * kATileBytes;
       const bool first = (i % nk) == 0;
 #pragma unroll
@@ -743,6 +774,15 @@ __global__ void __launch_bounds__(kThreads, 1) k_split_synth(SynthArgs a) {
           const uint64_t bd = tc::umma_desc(bbase + (lev - aa) * kBTileBytes, 128, 256);
           tc::umma_bf16(tmem + lev * kCols, ad, bd, idesc, (!first || aa > 0) ? 1u : 0u);
         }
+      }
+      // level 4 (a1 b3, a2 b2, a3 b1) into the level-3 accumulator via the 2^-8 planes:
+      // with lambda against one scale its digits are often small, and dropping level 4
+      // would cost ~2e-7
+#pragma unroll
+      for (int aa = 1; aa <= 3; ++aa) {
+        const uint64_t ad = tc::umma_desc(abase + aa * kATileBytes, 128, 256);
+        const uint64_t bd = tc::umma_desc(bbase + (kSlices - 1 + (4 - aa)) * kBTileBytes, 128, 256);
+        tc::umma_bf16(tmem + 3 * kCols, ad, bd, idesc, 1u);
       }
       tc::umma_commit(&h.empty[st]);
     }
@@ -804,10 +844,10 @@ __global__ void __launch_bounds__(kThreads, 1) k_split_synth(SynthArgs a) {
       if (tc::mbar_try_wait(&h.fin, 0)) break;
   }
   if (tid == 128) {
-    for (uint32_t d = 0; d < (uint32_t)kStagesG && d < n_loaded; ++d) {
+    for (uint32_t d = 0; d < (uint32_t)kStagesS && d < n_loaded; ++d) {
       const uint32_t i = n_loaded - 1 - d;
       for (uint32_t it = 0; it < tc::kWaitLimit; ++it)
-        if (tc::mbar_try_wait(&h.full[i % kStagesG], (i / kStagesG) & 1)) break;
+        if (tc::mbar_try_wait(&h.full[i % kStagesS], (i / kStagesS) & 1)) break;
     }
   }
   tc::tc_fence_before();
@@ -819,17 +859,19 @@ __global__ void __launch_bounds__(kThreads, 1) k_split_synth(SynthArgs a) {
 }  // namespace
 
 namespace {
-// k-steps per (m, parity, group) row of WS: rings (analysis) or l of one parity (synthesis)
-int ws_ksteps(int lmax, int nnorth) {
-  const int nks = (nnorth + kKStep - 1) / kKStep;
-  const int nkl = (lmax / 2 + 1 + kKStep - 1) / kKStep;
-  return nks > nkl ? nks : nkl;
+// WS bytes per (m, parity, group): the analysis P tiles (rings) or the synthesis alm tiles
+// (l of one parity), whichever is larger
+size_t ws_row_bytes(int lmax, int nnorth) {
+  const size_t nks = (size_t)(nnorth + kKStep - 1) / kKStep;
+  const size_t nkl = (size_t)(lmax / 2 + 1 + kKStep - 1) / kKStep;
+  const size_t a = nks * kSlices * kBTileBytes, b = nkl * kSynthBBytes;
+  return a > b ? a : b;
 }
 }  // namespace
 
 size_t fsht_split_ws_bytes(int lmax, int nnorth, int kc) {
   const int ngroups = (kc + kGroupMaps - 1) / kGroupMaps;
-  return (size_t)(lmax + 1) * 2 * ngroups * ws_ksteps(lmax, nnorth) * kSlices * kBTileBytes;
+  return (size_t)(lmax + 1) * 2 * ngroups * ws_row_bytes(lmax, nnorth);
 }
 size_t fsht_split_eb_bytes(int lmax, int kc) {
   const int ngroups = (kc + kGroupMaps - 1) / kGroupMaps;
@@ -846,7 +888,7 @@ int fsht_launch_split_prepare(fsht_plan* p, const double2* W, unsigned char* WS,
   sa.kc = kc;
   sa.nnorth = p->nnorth;
   sa.ngroups = ngroups;
-  sa.nks_max = ws_ksteps(p->lmax, p->nnorth);
+  sa.row_bytes = ws_row_bytes(p->lmax, p->nnorth);
   sa.ring_i0 = p->d_ring_i0;
   sa.WS = WS;
   sa.EB = EB;
@@ -963,7 +1005,7 @@ int fsht_launch_split_gemm(fsht_plan* p, int w, const unsigned char* WS, const i
   a.lmax = p->lmax;
   a.nnorth = p->nnorth;
   a.ngroups = (kc + kGroupMaps - 1) / kGroupMaps;
-  a.nks_max = ws_ksteps(p->lmax, p->nnorth);
+  a.row_bytes = ws_row_bytes(p->lmax, p->nnorth);
   a.nkc_glob = (p->nnorth + kKChunk - 1) / kKChunk;
   a.accumulate = accumulate;
   a.q0 = wv[0];
@@ -998,7 +1040,7 @@ int fsht_launch_split_synth_prepare(fsht_plan* p, const double* alm, unsigned ch
   a.kc = kc;
   a.lmax = p->lmax;
   a.ngroups = (kc + kGroupMaps - 1) / kGroupMaps;
-  a.nkl_max = ws_ksteps(p->lmax, p->nnorth);
+  a.row_bytes = ws_row_bytes(p->lmax, p->nnorth);
   a.WS = WS;
   a.EB = EB;
   k_slice_alm<<<dim3(p->lmax + 1, 2, a.ngroups), 128, 0, s>>>(a);
@@ -1040,7 +1082,7 @@ int fsht_launch_split_synth(fsht_plan* p, int w, const unsigned char* WS, const 
   a.lmax = p->lmax;
   a.nnorth = p->nnorth;
   a.ngroups = (kc + kGroupMaps - 1) / kGroupMaps;
-  a.nkl_max = ws_ksteps(p->lmax, p->nnorth);
+  a.row_bytes = ws_row_bytes(p->lmax, p->nnorth);
   a.nkcl_glob = ((p->lmax / 2 + 1 + kKStep - 1) / kKStep * kKStep + kKChunk - 1) / kKChunk;
   a.q0 = wv[0];
   a.nkclmax = wv[6];
@@ -1053,7 +1095,7 @@ int fsht_launch_split_synth(fsht_plan* p, int w, const unsigned char* WS, const 
   a.W = reinterpret_cast<double*>(W);
   a.kc = kc;
   a.err = p->d_err;
-  const size_t sm = (size_t)kStagesG * kStageBytesG;
+  const size_t sm = (size_t)kStagesS * kStageBytesS;
   FSHT_CUDA_TRY(
       cudaFuncSetAttribute(k_split_synth, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
   k_split_synth<<<dim3(a.ngroups, wv[4] * wv[6], wv[1] - wv[0]), kThreads, sm, s>>>(a);

@@ -394,31 +394,6 @@ int fsht_profile_read(fsht_plan* p, int ncat, int* launches, double* total_ms) {
   return FSHT_OK;
 }
 
-int fsht_run_stage(fsht_plan* p, int stage, const void* in, void* out, int nmaps) {
-  FSHT_TRY(check_call(p, nmaps, in, out));
-  if (nmaps > p->kchunk) {
-    fsht_set_error("run_stage: nmaps %d above maps_per_chunk %d", nmaps, p->kchunk);
-    return FSHT_EINVAL;
-  }
-  switch (stage) {
-    case FSHT_STAGE_FFT_FWD:
-      return fsht_launch_ring_fft_fwd(p, (const double*)in, p->npix, nmaps, (double2*)out,
-                                      p->stream);
-    case FSHT_STAGE_ANALYSIS:
-      return fsht_launch_analysis_fp64(p, 0, (const double2*)in, nullptr, (double*)out, nullptr,
-                                       nmaps, 0, nmaps, 0, 1, p->stream);
-    case FSHT_STAGE_SYNTHESIS:
-      return fsht_launch_synthesis_fp64(p, 0, (const double*)in, nullptr, (double2*)out, nullptr,
-                                        nmaps, 0, nmaps, p->stream);
-    case FSHT_STAGE_FFT_INV:
-      return fsht_launch_ring_fft_inv(p, (const double2*)in, (double*)out, p->npix, nmaps,
-                                      p->stream);
-    default:
-      fsht_set_error("unknown stage %d", stage);
-      return FSHT_EINVAL;
-  }
-}
-
 int fsht_plan_sync(fsht_plan* p) {
   FSHT_TRY(check_plan(p));
   FSHT_CUDA_TRY(cudaStreamSynchronize(p->stream));
@@ -475,6 +450,35 @@ static int split_synthesis(fsht_plan* p, const double* alm, double2* W, int nmap
     }
   }
   return FSHT_OK;
+}
+
+int fsht_run_stage(fsht_plan* p, int stage, const void* in, void* out, int nmaps) {
+  FSHT_TRY(check_call(p, nmaps, in, out));
+  if (nmaps > p->kchunk) {
+    fsht_set_error("run_stage: nmaps %d above maps_per_chunk %d", nmaps, p->kchunk);
+    return FSHT_EINVAL;
+  }
+  switch (stage) {
+    case FSHT_STAGE_FFT_FWD:
+      return fsht_launch_ring_fft_fwd(p, (const double*)in, p->npix, nmaps, (double2*)out,
+                                      p->stream);
+    case FSHT_STAGE_ANALYSIS:
+      if (p->precision == FSHT_PREC_SPLIT)
+        return split_analysis(p, (const double2*)in, (double*)out, nmaps, 0, nmaps, 0);
+      return fsht_launch_analysis_fp64(p, 0, (const double2*)in, nullptr, (double*)out, nullptr,
+                                       nmaps, 0, nmaps, 0, 1, p->stream);
+    case FSHT_STAGE_SYNTHESIS:
+      if (p->precision == FSHT_PREC_SPLIT)
+        return split_synthesis(p, (const double*)in, (double2*)out, nmaps, 0, nmaps);
+      return fsht_launch_synthesis_fp64(p, 0, (const double*)in, nullptr, (double2*)out, nullptr,
+                                        nmaps, 0, nmaps, p->stream);
+    case FSHT_STAGE_FFT_INV:
+      return fsht_launch_ring_fft_inv(p, (const double2*)in, (double*)out, p->npix, nmaps,
+                                      p->stream);
+    default:
+      fsht_set_error("unknown stage %d", stage);
+      return FSHT_EINVAL;
+  }
 }
 
 // ----------------------------------------------------------------- temperature

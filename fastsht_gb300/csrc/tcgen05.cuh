@@ -142,6 +142,11 @@ __device__ __forceinline__ uint16_t bf16_of_int(int d) {
   const uint32_t mant = (b << (7 - msb)) & 0x7F;
   return (uint16_t)(sign | ((uint32_t)(127 + msb) << 7) | mant);
 }
+// The BF16 digit h times 2^-8 (exact: only the exponent moves; digits are >= 1 in
+// magnitude, so the result stays normal).
+__device__ __forceinline__ uint16_t bf16_scale_2m8(uint16_t h) {
+  return (h & 0x7FFF) ? (uint16_t)(h - (8u << 7)) : h;
+}
 __device__ __forceinline__ void digits4(double v, int E, uint16_t (&s)[4]) {
   const unsigned long long bits = (unsigned long long)__double_as_longlong(v);
   const int eb = (int)((bits >> 52) & 0x7FF);

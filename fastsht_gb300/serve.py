@@ -2,12 +2,14 @@
 
 Requests (map2alm / alm2map, T or Q/U, any supported nside / lmax / nmaps, FP64 or
 split precision) are admitted while earlier ones are still on the GPU, as soon as
-a stream slot and enough of the HBM budget are free; admitted requests run
-concurrently on their slots' streams.  Inputs and results stay resident on the
-device (CUDA tensors); host arrays are copied in on the request's stream.  A
-request whose footprint exceeds the whole budget is split along maps.  Each
-request records arrival, admission and completion times, from which the server
-reports p50 / p99 latency beside throughput.
+a stream slot and enough of the HBM budget are free; admitted work runs
+concurrently on the slots' streams.  Waiting requests with the same configuration
+(kind, nside, lmax, precision) are fused into one job along the map axis, so they
+share the per-(l, m, ring) recursion and fill the kernels' 64-map tiles.  A request
+whose footprint exceeds the whole budget is split along maps.  Inputs and results
+stay resident on the device (CUDA tensors); host arrays are copied in on the job's
+stream.  Each request records arrival, admission and completion times, from which
+the server reports p50 / p99 latency beside throughput.
 
 No counterpart in the reference (one SHT instance, one blocking call at a time,
 SHT.py:16-227); every transform runs through the C ABI's fsht_run_job on a shared
@@ -38,14 +40,21 @@ class Request:
     lmax: int
     nmaps: int
     precision: str
-    inputs: list                      # device tensors in the library layout
+    inputs: list                      # device tensors in the library layout (or host arrays)
     t_arrival: float
     future: Future = field(default_factory=Future)
     outputs: list = field(default_factory=list)
     t_admit: float = 0.0
     t_done: float = 0.0
-    parts: int = 1                    # sub-requests (split along maps)
+    parts: int = 0                    # jobs this request ran in (split along maps)
+    fused: int = 1                    # largest number of requests sharing one of its jobs
     ready: torch.cuda.Event = None    # inputs written (submitting thread's stream)
+    next_map: int = 0                 # first map not yet admitted
+    done_parts: list = field(default_factory=list)   # (m0, outputs) per finished piece
+
+    @property
+    def key(self):
+        return (self.kind, self.nside, self.lmax, self.precision)
 
     @property
     def nfields(self):
@@ -58,12 +67,10 @@ class Request:
 
 @dataclass
 class _Part:
-    req: Request
-    m0: int
-    m1: int
-    inputs: list
+    members: list                     # (request, m0, m1, offset of m0 in this job)
+    nmaps: int
     outputs: list
-    workspace: torch.Tensor = None
+    keep: list                        # tensors the job reads (kept alive until it ends)
     event: torch.cuda.Event = None
     slot: int = -1
     nbytes: int = 0
@@ -80,24 +87,28 @@ def _alm_shape(lmax, nmaps):
 class Server:
     """Continuous-batching SHT server on one GPU.
 
-    hbm_budget: device bytes the server may hold for in-flight requests (inputs,
-    outputs and workspaces); nslots: concurrent CUDA streams.
+    hbm_budget: device bytes the server may hold for in-flight jobs (inputs, outputs and
+    workspaces); nslots: concurrent CUDA streams; fuse_maps: most maps one fused job may
+    gather from waiting requests of the same configuration (0 disables fusing).
     """
 
-    def __init__(self, hbm_budget=150e9, nslots=8, device=None, poll_s=5e-5):
+    def __init__(self, hbm_budget=150e9, nslots=8, device=None, poll_s=5e-5, fuse_maps=128):
         self.device = torch.device("cuda", torch.cuda.current_device() if device is None else device)
         self.budget = int(hbm_budget)
         self.nslots = nslots
         self.poll_s = poll_s
+        self.fuse_maps = int(fuse_maps)
         with torch.cuda.device(self.device):
             self.streams = [torch.cuda.Stream(self.device) for _ in range(nslots)]
         self._plans = {}
+        self._ws_cache = {}
         self._pending = collections.deque()
         self._inflight: list[_Part] = []
         self._free_slots = list(range(nslots))
         self._used = 0
         self.high_water = 0
         self.max_inflight = 0
+        self.max_fused = 1
         self.completed: list[Request] = []
         self._lock = threading.Condition()
         self._stop = False
@@ -172,7 +183,7 @@ class Server:
                 "requests_per_s": lat.size / (t1 - t0),
                 "maps_sht_per_s": mapsht / (t1 - t0),
                 "high_water_bytes": self.high_water, "budget_bytes": self.budget,
-                "max_inflight": self.max_inflight}
+                "max_inflight": self.max_inflight, "max_fused": self.max_fused}
 
     # ------------------------------------------------------------ internals
     def _plan(self, nside, lmax, precision):
@@ -187,15 +198,16 @@ class Server:
             self._plans[key] = p
         return p
 
-    def _job(self, req, m0, m1, ins, outs):
+    def _fsht_job(self, req, n, ins=None, outs=None):
         j = _lib.FshtJob()
-        j.nside, j.lmax, j.nmaps = req.nside, req.lmax, m1 - m0
+        j.nside, j.lmax, j.nmaps = req.nside, req.lmax, n
         j.kind = _KINDS[req.kind]
         j.precision = _lib.FSHT_PREC_SPLIT if req.precision == "split" else _lib.FSHT_PREC_FP64
-        j.in0 = ins[0].data_ptr()
-        j.in1 = ins[1].data_ptr() if len(ins) > 1 else None
-        j.out0 = outs[0].data_ptr()
-        j.out1 = outs[1].data_ptr() if len(outs) > 1 else None
+        if ins is not None:
+            j.in0 = ins[0].data_ptr()
+            j.in1 = ins[1].data_ptr() if len(ins) > 1 else None
+            j.out0 = outs[0].data_ptr()
+            j.out1 = outs[1].data_ptr() if len(outs) > 1 else None
         return j
 
     def _io_bytes(self, req, n):
@@ -204,17 +216,19 @@ class Server:
         return 8 * n * (npix + L * L) * req.nfields
 
     def _workspace_bytes(self, req, n, kc):
-        plan = self._plan(req.nside, req.lmax, req.precision)
-        j = _lib.FshtJob()
-        j.nside, j.lmax, j.nmaps, j.kind = req.nside, req.lmax, n, _KINDS[req.kind]
-        j.precision = _lib.FSHT_PREC_SPLIT if req.precision == "split" else _lib.FSHT_PREC_FP64
-        b = C.c_size_t()
-        _lib.call("fsht_job_workspace", plan, C.byref(j), kc, C.byref(b))
-        return int(b.value)
+        key = req.key + (n, kc)
+        b = self._ws_cache.get(key)
+        if b is None:
+            plan = self._plan(req.nside, req.lmax, req.precision)
+            j = self._fsht_job(req, n)
+            out = C.c_size_t()
+            _lib.call("fsht_job_workspace", plan, C.byref(j), kc, C.byref(out))
+            b = self._ws_cache[key] = int(out.value)
+        return b
 
-    def _fit(self, req, avail):
-        """Largest (maps, maps-per-chunk) of req's remaining maps whose footprint fits."""
-        n = req.nmaps - req._next
+    def _fit(self, req, n_max, avail):
+        """Largest (maps <= n_max, maps-per-chunk) of req's configuration whose footprint fits."""
+        n = n_max
         while n >= 1:
             kc = min(n, 128)
             while kc >= 1:
@@ -225,76 +239,121 @@ class Server:
             n //= 2
         return None
 
-    def _admit_one(self, req) -> bool:
+    def _gather(self, head):
+        """head plus waiting, not yet started requests of its configuration (arrival
+        order), up to fuse_maps maps in total."""
+        group = [head]
+        if self.fuse_maps and head.next_map == 0:
+            total = head.nmaps
+            for r in self._pending:
+                if r is head or r.next_map or r.key != head.key:
+                    continue
+                if total + r.nmaps > self.fuse_maps:
+                    break
+                group.append(r)
+                total += r.nmaps
+        return group
+
+    def _admit(self, head) -> bool:
+        """Admit one job led by `head`: the rest of head's maps (as many as fit), or head
+        fused with waiting requests of the same configuration."""
         if not self._free_slots:
             return False
         avail = self.budget - self._used
-        fit = self._fit(req, avail)
+        group = self._gather(head)
+        while True:
+            total = sum(r.nmaps - r.next_map for r in group)
+            fit = self._fit(head, total, avail)
+            if fit is None or fit[0] == total or len(group) == 1:
+                break
+            group.pop()                 # the fused job does not fit whole: fuse fewer
         if fit is None:
             if self._used == 0:
-                raise RuntimeError(f"request (nside {req.nside}, lmax {req.lmax}) does not fit "
+                raise RuntimeError(f"request (nside {head.nside}, lmax {head.lmax}) does not fit "
                                    f"the {self.budget}-byte budget even for one map")
             return False
         n, kc, need = fit
+        members, off = [], 0
+        for r in group:
+            k = min(r.nmaps - r.next_map, n - off)
+            if k <= 0:
+                break
+            members.append((r, r.next_map, r.next_map + k, off))
+            off += k
         slot = self._free_slots.pop()
         stream = self.streams[slot]
-        m0, m1 = req._next, req._next + n
         with torch.cuda.device(self.device), torch.cuda.stream(stream):
-            if req.ready is not None:
-                stream.wait_event(req.ready)
+            for r, *_ in members:
+                if r.ready is not None:
+                    stream.wait_event(r.ready)
             ins = []
-            for x in req.inputs:
-                if isinstance(x, torch.Tensor):
-                    part = x[m0:m1] if req.analysis else x[..., m0:m1]
-                    ins.append(part.contiguous())
+            for f in range(head.nfields):
+                pieces = []
+                for r, m0, m1, _ in members:
+                    x = r.inputs[f]
+                    if isinstance(x, torch.Tensor):
+                        pieces.append(x[m0:m1] if r.analysis else x[..., m0:m1])
+                    else:
+                        part = x[m0:m1] if r.analysis else x[..., m0:m1]
+                        pieces.append(torch.from_numpy(np.ascontiguousarray(part)).to(
+                            self.device, non_blocking=True))
+                if len(pieces) == 1:
+                    ins.append(pieces[0].contiguous())
                 else:
-                    part = x[m0:m1] if req.analysis else x[..., m0:m1]
-                    ins.append(torch.from_numpy(np.ascontiguousarray(part)).to(
-                        self.device, non_blocking=True))
-            if req.analysis:
-                outs = [torch.empty(_alm_shape(req.lmax, n), dtype=torch.float64,
-                                    device=self.device) for _ in range(req.nfields)]
-            else:
-                outs = [torch.empty(_maps_shape(req.nside, n), dtype=torch.float64,
-                                    device=self.device) for _ in range(req.nfields)]
-            ws_bytes = self._workspace_bytes(req, n, kc)
-            ws = torch.empty(max(ws_bytes, 256), dtype=torch.uint8, device=self.device)
-            plan = self._plan(req.nside, req.lmax, req.precision)
-            job = self._job(req, m0, m1, ins, outs)
+                    ins.append(torch.cat(pieces, dim=0 if head.analysis else -1))
+            shape = _alm_shape(head.lmax, n) if head.analysis else _maps_shape(head.nside, n)
+            outs = [torch.empty(shape, dtype=torch.float64, device=self.device)
+                    for _ in range(head.nfields)]
+            ws = torch.empty(max(self._workspace_bytes(head, n, kc), 256), dtype=torch.uint8,
+                             device=self.device)
+            plan = self._plan(head.nside, head.lmax, head.precision)
+            job = self._fsht_job(head, n, ins, outs)
             _lib.call("fsht_run_job", plan, C.byref(job), C.c_void_p(ws.data_ptr()),
                       ws.numel(), C.c_void_p(stream.cuda_stream))
             ev = torch.cuda.Event()
             ev.record(stream)
-        if req._next == 0:
-            req.t_admit = time.perf_counter()
-        req._next = m1
+        now = time.perf_counter()
+        for r, m0, m1, _ in members:
+            if r.next_map == 0:
+                r.t_admit = now
+            r.next_map = m1
+            r.parts += 1
+            r.fused = max(r.fused, len(members))
+            if r.next_map >= r.nmaps:
+                self._pending.remove(r)
+        self.max_fused = max(self.max_fused, len(members))
         self._used += need
         self.high_water = max(self.high_water, self._used)
-        self._inflight.append(_Part(req, m0, m1, ins, outs, ws, ev, slot, need))
+        self._inflight.append(_Part(members, n, outs, ins + [ws], ev, slot, need))
         self.max_inflight = max(self.max_inflight, len(self._inflight))
-        if req._next < req.nmaps:
-            req.parts += 1
         return True
 
     def _finish(self, part: _Part):
-        req = part.req
         self._used -= part.nbytes
         self._free_slots.append(part.slot)
-        req._parts_out.append(part)
-        done_maps = sum(p.m1 - p.m0 for p in req._parts_out)
-        if done_maps == req.nmaps:
-            req._parts_out.sort(key=lambda p: p.m0)
-            if len(req._parts_out) == 1:
-                req.outputs = req._parts_out[0].outputs
+        for r, m0, m1, off in part.members:
+            if len(part.members) == 1 and m0 == 0 and m1 == r.nmaps:
+                piece = part.outputs
+            elif r.analysis:
+                piece = [o[..., off:off + (m1 - m0)] for o in part.outputs]
             else:
-                with torch.cuda.device(self.device):
-                    dim = -1 if req.analysis else 0
-                    req.outputs = [torch.cat([p.outputs[f] for p in req._parts_out], dim=dim)
-                                   for f in range(req.nfields)]
-                    torch.cuda.current_stream(self.device).synchronize()
-            req.t_done = time.perf_counter()
-            self.completed.append(req)
-            req.future.set_result(req.outputs)
+                piece = [o[off:off + (m1 - m0)] for o in part.outputs]
+            r.done_parts.append((m0, piece))
+            if sum(p[0].shape[-1 if r.analysis else 0] for _, p in r.done_parts) < r.nmaps:
+                continue
+            r.done_parts.sort(key=lambda t: t[0])
+            with torch.cuda.device(self.device):
+                if len(r.done_parts) == 1:
+                    r.outputs = [t.contiguous() for t in r.done_parts[0][1]]
+                else:
+                    dim = -1 if r.analysis else 0
+                    r.outputs = [torch.cat([p[f] for _, p in r.done_parts], dim=dim)
+                                 for f in range(r.nfields)]
+                torch.cuda.current_stream(self.device).synchronize()
+            r.done_parts = []
+            r.t_done = time.perf_counter()
+            self.completed.append(r)
+            r.future.set_result(r.outputs)
 
     def _loop(self):
         try:
@@ -302,7 +361,6 @@ class Server:
                 with self._lock:
                     if self._stop and not self._pending and not self._inflight:
                         return
-                    # completions
                     still = []
                     for part in self._inflight:
                         if part.event.query():
@@ -310,19 +368,16 @@ class Server:
                         else:
                             still.append(part)
                     self._inflight = still
-                    # admissions: arrival order, but a request that does not fit yet does
-                    # not block smaller ones behind it
+                    # admissions in arrival order; a request that does not fit yet does not
+                    # block smaller ones behind it
                     for req in list(self._pending):
                         if not self._free_slots:
                             break
-                        if not hasattr(req, "_next"):
-                            req._next = 0
-                            req._parts_out = []
-                        while self._free_slots and req._next < req.nmaps:
-                            if not self._admit_one(req):
+                        if req not in self._pending:      # fused into an earlier job
+                            continue
+                        while self._free_slots and req.next_map < req.nmaps:
+                            if not self._admit(req):
                                 break
-                        if req._next >= req.nmaps:
-                            self._pending.remove(req)
                     self._lock.notify_all()
                     idle = not self._pending and not self._inflight
                     if idle:
@@ -336,8 +391,9 @@ class Server:
                     if not req.future.done():
                         req.future.set_exception(e)
                 for part in self._inflight:
-                    if not part.req.future.done():
-                        part.req.future.set_exception(e)
+                    for r, *_ in part.members:
+                        if not r.future.done():
+                            r.future.set_exception(e)
                 self._pending.clear()
                 self._inflight.clear()
                 self._lock.notify_all()

@@ -100,3 +100,24 @@ def test_request_larger_than_budget_is_split_and_exact():
     assert srv.completed[0].parts > 1
     assert _close(out[0], _direct("t2alm", ns, lmax, ins, "fp64")[0])
     srv.close()
+
+
+def test_waiting_requests_of_one_configuration_are_fused():
+    """Requests of one (kind, nside, lmax, precision) that wait together run as one job
+    along the map axis; each still gets its own maps' results."""
+    from fastsht_gb300.serve import Server
+    gen = torch.Generator(device="cuda").manual_seed(6)
+    ns, lmax = 64, 128
+    blocker = _inputs("t2alm", 256, 512, 16, gen)        # keeps the single slot busy
+    reqs = [_inputs("t2alm", ns, lmax, n, gen) for n in (3, 1, 5, 2)]
+    torch.cuda.synchronize()
+    srv = Server(hbm_budget=8e9, nslots=1)
+    srv.submit("t2alm", 256, 512, blocker)
+    futs = [srv.submit("t2alm", ns, lmax, ins) for ins in reqs]
+    srv.drain(timeout=120)
+    assert srv.stats()["max_fused"] >= 2
+    for f, ins in zip(futs, reqs):
+        got = f.result()[0]
+        want = _direct("t2alm", ns, lmax, ins, "fp64")[0]
+        assert got.shape == want.shape and _close(got, want)
+    srv.close()
