@@ -56,6 +56,54 @@ def flop_per_map(nside, lmax):
     return 4.0 * nside * (lmax + 1) * (lmax + 2)
 
 
+def fft_alg_flop_per_map(nside):
+    """Conventional FFT flop count of one map's ring DFTs: 5 n log2 n per complex length-n
+    transform, one per north/south ring pair (the equator ring alone)."""
+    tot = 0.0
+    for i in range(2 * nside):
+        n = 4 * (i + 1) if i < nside else 4 * nside
+        tot += 5.0 * n * math.log2(n)
+    return tot
+
+
+def fft_dp_ops_per_map(nside):
+    """FP64 instructions one forward ring FFT pass executes per map (the kernels' radix-4 /
+    radix-2 / radix-3 passes, Bluestein chirps and filter; the fold and phase are left out):
+    the FFT is FP64-pipe bound, so this over the DFMA rate is its roofline."""
+    def size(n):
+        if n & (n - 1) == 0:
+            return n, 0
+        need = 2 * n - 1
+        p2 = 1 << (need - 1).bit_length()
+        p3 = 3
+        while p3 < need:
+            p3 *= 2
+        return (p3, 1) if p3 < p2 else (p2, 0)
+
+    def dif(P, r3):
+        T = P // 3 if r3 else P
+        nblk = 3 if r3 else 1
+        ops = 22 * T if r3 else 0
+        L = T.bit_length() - 1
+        first = True
+        while L >= 2:
+            ops += nblk * (T // 4) * (16 if L == 2 else 28)
+            L -= 2
+        if L == 1:
+            ops += nblk * (T // 2) * 4
+        return ops
+
+    total = 0
+    for i in range(2 * nside):                 # ring pairs (N + iS), equator alone
+        n = 4 * (i + 1) if i < nside else 4 * nside
+        P, r3 = size(n)
+        if P == n:
+            total += dif(P, 0)
+        else:
+            total += 2 * dif(P, r3) + 4 * P + 8 * n
+    return total
+
+
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -334,18 +382,40 @@ def ours(args, rank, world, local):
     top = max(range(len(names)), key=lambda i: kms[i])
     fft_ms, ana_ms = kms[0], kms[2]
     fft_bytes = 16.0 * npix * nmaps * args.steps
-    roof_fft = {"bound": "hbm", "kernel": "k_ring_fft_fwd", "achieved":
-                fft_bytes / (fft_ms / 1000.0) / 1e9 if fft_ms > 0 else None,
-                "peak": peaks.get("hbm_gbs", 6800.0), "unit": "GB/s",
-                "peak_source": ("MEASURED_PEAKS.json hbm_gbs (measured)" if "hbm_gbs" in peaks
-                                else "fallback 6800 GB/s"),
-                "traffic": None,
-                "note": ("the FP64 ring FFT is FP64-pipe bound on GB300 (83 % of the FP64 pipe "
-                         "in ncu), so its HBM fraction is small")}
+    # The FP64 ring FFT is bound by the FP64 pipe (GB300: ~1.25 TFLOP/s FP64 against
+    # 6.8 TB/s of HBM, 0.09 flop/B; the FFT does ~3 flop/B), so its roofline is FP64:
+    # algorithmic flops = 5 n log2 n per complex length-n ring DFT (N + iS packed).
+    fft_alg = fft_alg_flop_per_map(nside) * nmaps * args.steps
+    fft_traffic = None
+    tf_fft = ROOT / "profiles" / "traffic.json"
+    if tf_fft.exists():
+        tr = json.loads(tf_fft.read_text()).get("ring_fft_fwd")
+        if tr and tr.get("bytes_per_map"):
+            fft_traffic = tr["bytes_per_map"] * kchunk
+    roof_fft = {"bound": "fp64", "kernel": "k_ring_fft_fwd",
+                "achieved": fft_alg / (fft_ms / 1000.0) / 1e12 if fft_ms > 0 else None,
+                "peak": peak64.value, "unit": "TFLOP/s",
+                "peak_source": ("DFMA loop measured by bench.py on this GPU "
+                                "(fsht_measure_fp64_peak); MEASURED_PEAKS.json holds HBM and "
+                                "BF16 figures only"),
+                "algorithmic_flop_per_map": fft_alg_flop_per_map(nside),
+                "traffic": fft_traffic,
+                "hbm": {"achieved_gbs": fft_bytes / (fft_ms / 1000.0) / 1e9 if fft_ms > 0 else None,
+                        "peak_gbs": peaks.get("hbm_gbs", 6800.0),
+                        "algorithmic_bytes_per_map": 16.0 * npix}}
     if roof_fft["achieved"]:
         roof_fft["frac"] = roof_fft["achieved"] / roof_fft["peak"]
+        roof_fft["hbm"]["frac"] = roof_fft["hbm"]["achieved_gbs"] / roof_fft["hbm"]["peak_gbs"]
+        dp = fft_dp_ops_per_map(nside) * nmaps * args.steps / (fft_ms / 1000.0)
+        roof_fft["fp64_pipe"] = {"dp_instr_per_map": fft_dp_ops_per_map(nside),
+                                 "achieved_g_per_s": dp / 1e9,
+                                 "peak_g_per_s": peak64.value * 1e12 / 2 / 1e9,
+                                 "frac": dp / (peak64.value * 1e12 / 2),
+                                 "note": "FP64 instructions executed (radix passes, Bluestein "
+                                         "chirps and filter; an FMA counts once) over the DFMA "
+                                         "instruction rate measured in this run"}
     ana_tf = fl_step * args.steps / (ana_ms / 1000.0) / 1e12 if ana_ms > 0 else None
-    traffic = None
+    traffic = None          # bytes per chunk of maps (all of its launches)
     tf = ROOT / "profiles" / "traffic.json"
     if tf.exists():
         tr = json.loads(tf.read_text()).get(
@@ -354,16 +424,20 @@ def ours(args, rank, world, local):
             traffic = tr["bytes_per_map"] * kchunk
     if args.precision == "split":
         bf = peaks.get("bf16_tflops", 1900.0)
-        roof_ana = {"bound": "tensor", "kernel": "k_analysis_split (tcgen05 BF16 digit UMMAs)",
+        ex_tf = 10 * ana_tf if ana_tf else None
+        roof_ana = {"bound": "tensor", "kernel": "k_split_gemm (tcgen05 BF16 digit UMMAs)",
                     "achieved": ana_tf, "peak": bf, "unit": "TFLOP/s",
                     "frac": ana_tf / bf if ana_tf else None,
                     "peak_source": ("MEASURED_PEAKS.json bf16_tflops (measured)"
                                     if "bf16_tflops" in peaks else "fallback 1900 TFLOP/s"),
-                    "algorithmic_flop_per_launch": flop_per_map(nside, lmax) * kchunk,
-                    "executed_tensor_flop_per_launch": 10 * flop_per_map(nside, lmax) * kchunk,
+                    "algorithmic_flop_per_chunk": flop_per_map(nside, lmax) * kchunk,
+                    "executed_tensor_tflops": ex_tf,
+                    "executed_frac": ex_tf / bf if ex_tf else None,
                     "traffic": traffic,
                     "note": ("achieved counts algorithmic FLOP (4 nside (lmax+1)(lmax+2) per map); "
-                             "the kernel executes 10 BF16 digit products per algorithmic FMA")}
+                             "the kernel executes 10 BF16 digit products per algorithmic FMA "
+                             "(executed_*); one chunk of maps is several wave launches, traffic "
+                             "is per chunk")}
     else:
         roof_ana = {"bound": "fp64", "kernel": "k_analysis_fp64<0>", "achieved": ana_tf,
                     "peak": peak64.value, "unit": "TFLOP/s",
@@ -421,6 +495,31 @@ def ours(args, rank, world, local):
                             "the round-trip residual of both forms is the niter = 0 quadrature "
                             "error, the split-vs-fp64 term is the precision-induced part")}
         del out64
+        torch.cuda.empty_cache()
+    # -------- one refinement step (niter = 1) in the split form, against the plain path
+    # with the same niter on the first maps of the batch
+    if args.precision == "split" and not args.no_fp64:
+        sr = SHT(nside, lmax, nmaps, niter=1, device=local, precision="split")
+        ms_r, out_r, pk_r, _, _, _ = timed_steps(lib, sr, maps, 1, 1, world, dist, dev, local,
+                                                 sample_clocks=False)
+        sr.close()
+        ks = min(64, nmaps)
+        s64r = SHT(nside, lmax, ks, niter=1, device=local)
+        out64r = s64r.t2alm(maps[:, :ks])
+        vr = world * nmaps / (ms_r / 1000.0)
+        sd = float(maps[:, :ks].std().item())
+        first = out_r.permute(2, 1, 0)[..., :ks].contiguous().permute(2, 1, 0)   # (ks, L, L) F-order
+        res_r = float((s64r.alm2t(first) - maps[:, :ks]).abs().max().item()) / sd
+        del first
+        line["refined"] = {
+            "niter": 1, "value": vr, "unit": UNIT, "ms_per_step": ms_r, "per_kernel": pk_r,
+            "speedup_vs_plain_niter0": vr / line["fp64_plain"]["value"] if "fp64_plain" in line else None,
+            "max_rel_alm_err_vs_fp64_niter1": rel_err_per_map(out_r[:ks], out64r),
+            "roundtrip_map_residual": res_r, "maps_checked": ks,
+            "note": ("one Jacobi refinement step: split synthesis, FP64 Fourier-space residual, "
+                     "split analysis added; the error is against the plain path with niter = 1")}
+        s64r.close()
+        del out_r, out64r
         torch.cuda.empty_cache()
     # -------- e2e through the public API with host (pinned) buffers
     if not args.no_e2e:
@@ -510,7 +609,7 @@ def bench_batched(args, rank, world, local):
             j = b.add("t2alm", ns, lmax, nm, precision=precision)
             j.inputs[0].normal_()
             if pol:
-                jp = b.add("qu2eb", ns, lmax, nm)
+                jp = b.add("qu2eb", ns, lmax, nm, precision=precision)
                 for t in jp.inputs:
                     t.normal_()
         t0 = time.perf_counter()
@@ -554,7 +653,7 @@ def bench_batched(args, rank, world, local):
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None,
-        "dtype": "T jobs bf16x4-split of f64, Q/U jobs f64", "data": "synthetic",
+        "dtype": "bf16x4-split of f64 (FP32 accum)", "data": "synthetic",
         "config": {"workload": (f"batched form: {len(sets)} map sets, nside 2^U{{5..."
                                 f"{int(round(math.log2(args.max_nside)))}}}, lmax ~ U[2 nside, "
                                 f"3 nside - 1], nmaps ~ U[1, {max_maps}], even sets T, odd "
@@ -579,8 +678,8 @@ def bench_batched(args, rank, world, local):
 def bench_serving(args, rank, world, local):
     """Open-loop Poisson stream into fastsht_gb300.serve.Server: map2alm or alm2map, T or
     Q/U with equal odds, nside = 2^U{6..log2 max_nside}, lmax = 2 nside, nmaps ~
-    U[1, max_maps], FP64 or split per request (the split form applies to T map2alm; the
-    other kinds run FP64), seed 4.  Inputs are device-resident views of pre-generated
+    U[1, max_maps], FP64 or split per request (the split form covers map2alm T and Q/U and
+    alm2map T; alm2map Q/U runs FP64), seed 4.  Inputs are device-resident views of pre-generated
     pools.  value = map.SHT/s over the run; p50/p99 latency from arrival to result."""
     import torch
     from fastsht_gb300 import _lib
@@ -627,7 +726,7 @@ def bench_serving(args, rank, world, local):
         for ns in pools:
             for prec in ("fp64", "split"):
                 srv.submit(kind, ns, 2 * ns, inputs(kind, ns, 1),
-                           precision=prec if kind == "t2alm" else "fp64")
+                           precision=prec if kind != "eb2qu" else "fp64")
     srv.drain()
     srv.completed.clear()
     clocks = ClockSampler(local)
@@ -638,7 +737,7 @@ def bench_serving(args, rank, world, local):
         if ta > now:
             time.sleep(ta - now)
         srv.submit(kind, ns, lmax, inputs(kind, ns, nm),
-                   precision=prec if kind == "t2alm" else "fp64", t_arrival=t0 + ta)
+                   precision=prec if kind != "eb2qu" else "fp64", t_arrival=t0 + ta)
     srv.drain()
     torch.cuda.synchronize()
     wall = time.perf_counter() - t0
@@ -650,7 +749,7 @@ def bench_serving(args, rank, world, local):
         "metric": METRIC, "value": mapsht / wall, "unit": UNIT, "n_gpus": 1,
         "steps": 1, "warmup": 1, "ms_per_step": wall * 1000.0, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None,
-        "dtype": "f64; T map2alm requests drawn split run bf16x4-split of f64",
+        "dtype": "f64 and bf16x4-split of f64 (per request)",
         "data": "synthetic",
         "config": {"workload": (f"serving form: Poisson stream of {args.requests} requests "
                                 f"(mean {args.rate}/s), map2alm or alm2map x T or Q/U, nside "

@@ -56,9 +56,10 @@ JobLayout job_layout(const fsht_plan* p, const fsht_job& j, int kc) {
   L.eb_off = L.ws_off;
   L.lb_off = L.ws_off;
   L.total = L.ws_off;
-  if (p->precision == FSHT_PREC_SPLIT && (j.kind == FSHT_JOB_T2ALM || j.kind == FSHT_JOB_ALM2T)) {
-    L.eb_off = align_up(L.ws_off + fsht_split_ws_bytes(p->lmax, p->nnorth, kc));
-    L.lb_off = align_up(L.eb_off + fsht_split_eb_bytes(p->lmax, kc));
+  if (p->precision == FSHT_PREC_SPLIT && j.kind != FSHT_JOB_EB2QU) {
+    const size_t f = j.kind == FSHT_JOB_QU2EB ? 2 : 1;   // spin 2: tiles of Q and U
+    L.eb_off = align_up(L.ws_off + f * fsht_split_ws_bytes(p->lmax, p->nnorth, kc));
+    L.lb_off = align_up(L.eb_off + f * fsht_split_eb_bytes(p->lmax, kc));
     L.total = align_up(L.lb_off + p->lbuf_bytes);
   }
   return L;
@@ -260,9 +261,9 @@ extern "C" int fsht_batch_create(const fsht_job* jobs, int njobs, int nslots,
     auto it = key_plan.find(key);
     if (it == key_plan.end()) {
       fsht_plan* p = nullptr;
-      // tables only; the slots hold the workspaces
-      int rc = fsht_plan_create(j.nside, j.lmax, 1, FSHT_FLAG_TABLES_ONLY, j.precision, 0,
-                                b->stream, &p);
+      // tables only (spin-2 tables too in the split form); the slots hold the workspaces
+      const int flags = FSHT_FLAG_TABLES_ONLY | (j.precision == FSHT_PREC_SPLIT ? FSHT_FLAG_POL : 0);
+      int rc = fsht_plan_create(j.nside, j.lmax, 1, flags, j.precision, 0, b->stream, &p);
       if (rc) return fail(rc);
       b->plans.push_back(p);
       it = key_plan.emplace(key, (int)b->plans.size() - 1).first;

@@ -85,6 +85,11 @@ struct FshtLamRow {
   int dx;
 };
 
+// Spin-2 split form: per (l, m) factors of lambda1 / lambda2 (legendre_split_pol.cu).
+struct FshtPolRow {
+  double c1, c2, c3, c4;
+};
+
 struct fsht_plan {
   int nside, lmax, nring, nnorth;  // nnorth = 2*nside (north rings incl. equator)
   long long npix;
@@ -124,6 +129,7 @@ struct fsht_plan {
   int nwaves;
   unsigned char* d_lbuf;
   size_t lbuf_bytes;
+  FshtPolRow* d_poltab;            // spin-2 plans only, same triangular index as d_lamtab
 };
 
 // ---------------------------------------------------------------- status codes
@@ -199,6 +205,15 @@ int fsht_launch_split_gemm(fsht_plan* p, int w, const unsigned char* WS, const i
 int fsht_launch_split_synth_prepare(fsht_plan* p, const double* alm, unsigned char* WS, int* EB,
                                     double2* W, int nmaps_total, int k0, int kc, cudaStream_t s);
 int fsht_launch_split_lambdaT(fsht_plan* p, int w, unsigned char* lbuf, cudaStream_t s);
+// Split-precision spin-2 analysis: lambda1/lambda2 digit tiles per wave, then the E/B
+// contraction (which: bit0 E, bit1 B) against the Q and U digit tiles of k_slice_phase.
+int fsht_split_pol_tables_init(fsht_plan* p);
+int fsht_launch_split_lambda_pol(fsht_plan* p, int w, unsigned char* lbuf, cudaStream_t s);
+int fsht_launch_split_gemm_pol(fsht_plan* p, int w, const unsigned char* WSQ, const int* EBQ,
+                               const unsigned char* WSU, const int* EBU,
+                               const unsigned char* lbuf, double* almE, double* almB,
+                               int nmaps_total, int k0, int kc, int accumulate, int which,
+                               cudaStream_t s);
 int fsht_launch_split_synth(fsht_plan* p, int w, const unsigned char* WS, const int* EB,
                             const unsigned char* lbuf, double2* W, int kc, cudaStream_t s);
 int fsht_launch_synthesis_fp64(fsht_plan* p, int spin, const double* almE,

@@ -22,8 +22,7 @@
 //   k_split_gemm     one 128 x 128 output tile per CTA, both operands streamed by bulk
 //                    async copies (TMA engine) into a 6-stage ring, UMMAs into TMEM.
 // Max relative alm error against FP64: ~3e-8 (tests/test_gpu_split.py).
-#include "common.cuh"
-#include "tcgen05.cuh"
+#include "split_common.cuh"
 
 #include <algorithm>
 #include <cmath>
@@ -31,61 +30,6 @@
 #include <vector>
 
 namespace {
-
-constexpr int kRows = 128;          // UMMA M: rows of one parity per l-tile
-constexpr int kCols = 128;          // UMMA N: 64 maps x {Re, Im}
-constexpr int kGroupMaps = 64;
-constexpr int kKStep = 16;          // rings per UMMA
-constexpr int kSCRings = 128;       // rings per lambda-digit block
-constexpr int kKChunk = 1024;       // rings per CTA (keeps levels 0 and 1 exact)
-constexpr int kSlices = 4;
-constexpr uint32_t kATileBytes = kRows * kKStep * 2;    // 4 KB per (k-step, digit)
-constexpr uint32_t kBTileBytes = kCols * kKStep * 2;    // 4 KB per (k-step, digit)
-// Synthesis B tiles carry three more digit planes, d1..d3 times 2^-8 (exact in BF16), so
-// the level-4 products fold into the level-3 accumulator.
-constexpr int kSynthPlanes = 7;
-constexpr uint32_t kSynthBBytes = kSynthPlanes * kBTileBytes;   // 28 KB per l-step
-constexpr int kThreads = 192;
-constexpr int kEmptyExp = -4000;    // column exponent of an all-zero column
-
-struct RecConst {
-  double a, b;
-};
-
-__device__ __forceinline__ RecConst rec_coeffs(int l, int m) {
-  RecConst c;
-  if (l == m) {          // state convention: lambda_m = -b prev = the seed
-    c.a = 0.0;
-    c.b = -1.0;
-    return c;
-  }
-  const long long L = l, M = m;
-  c.a = sqrt((double)((2 * L - 1) * (2 * L + 1)) / (double)(L * L - M * M));
-  c.b = sqrt((double)((L - 1) * (L - 1) - M * M) / (double)((2 * L - 3) * (2 * L - 1))) * c.a;
-  return c;
-}
-
-// Row scale: |lambda_lm(theta)| <= sqrt((2l+1)/(4 pi)) < 2^EA (the |Y_lm| bound).
-__device__ __forceinline__ int row_exp(int l) {
-  const double b = sqrt((2.0 * l + 1.0) / (4.0 * M_PI)) * (1.0 + 0x1p-30);
-  return ilogb(b) + 1;
-}
-
-__device__ __forceinline__ void rec_seed(double sth, double pref, int m, double& v, int& e) {
-  int ex;
-  double mt = frexp(sth, &ex);
-  double rm = 1.0, bm = mt;
-  long long re = 0, be = ex;
-  for (int k = m; k; k >>= 1) {
-    if (k & 1) { rm *= bm; re += be; int t; rm = frexp(rm, &t); re += t; }
-    if (k > 1) { bm *= bm; be *= 2; int t; bm = frexp(bm, &t); be += t; }
-  }
-  rm *= pref;
-  { int t; rm = frexp(rm, &t); re += t; }
-  if (m & 1) rm = -rm;
-  e = (re >= -300) ? 0 : (int)floor((double)(re + 300) / 600.0);
-  v = ldexp(rm, (int)(re - 600LL * e));
-}
 
 // ------------------------------------------------------------------ P digits
 // grid (m, parity, group), 128 threads = columns (map = c & 63, Re/Im = c >> 6).
@@ -148,13 +92,6 @@ __global__ void __launch_bounds__(128) k_slice_phase(SliceArgs a) {
 // lambda_l / Dm_l = mu 2^(Et + Dx_l) against 2^EA(l) with EA(l) from |lambda| / Dm_l <=
 // sqrt((2l+1)/4pi) / Dm_l (D_l = Dm_l 2^Dx_l, Dm_l in [1, 2)); the GEMM epilogue multiplies
 // row l by Dm_l 2^EA(l).  Et is the per-ring exponent carried with the state.
-__device__ __forceinline__ int m_of_q(int q, int lmax) {
-  return (q & 1) ? lmax - (q >> 1) : (q >> 1);
-}
-__host__ __device__ __forceinline__ long long tri_off(int m, int lmax) {
-  return (long long)m * (2LL * lmax + 3 - m) / 2;
-}
-
 // One thread per m, sequential in l: beta_l, Dm_l, Dx_l and erow_l = EA(l) - Dx_l.
 __global__ void k_lam_table(int lmax, FshtLamRow* tab) {
   const int m = blockIdx.x * blockDim.x + threadIdx.x;
@@ -463,15 +400,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_split_gemm(GemmArgs a) {
           const int c = c0 + j;
           const int k = g * kGroupMaps + (c & 63);
           if (store && k < a.kc) {
-            // levels 0 and 1 are exact integers: their weighted sum is exact in FP32 as
-            // a (hi, lo) pair; levels 2 and 3 only touch lo.
-            const float L0 = __uint_as_float(v0[j]);
-            const float L1f = __uint_as_float(v1[j]) * 0x1p-8f;
-            const float hi = L0 + L1f;
-            const float bv = hi - L0;
-            const float lo = ((L0 - (hi - bv)) + (L1f - bv)) +
-                             (__uint_as_float(v2[j]) * 0x1p-16f + __uint_as_float(v3[j]) * 0x1p-24f);
-            const double v = ((double)hi + (double)lo) * rs * s_cs[c];
+            const double v = combine_levels(v0[j], v1[j], v2[j], v3[j]) * rs * s_cs[c];
             double* dst = a.alm + rowidx * a.ld + a.k0 + k;
             if (a.nkc_glob > 1) atomicAdd(dst, v);
             else if (a.accumulate) *dst += v;
@@ -812,13 +741,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_split_synth(SynthArgs a) {
           const int c = c0 + j;
           const int k = g * kGroupMaps + (c & 63);
           if (rowok && k < a.kc) {
-            const float L0 = __uint_as_float(v0[j]);
-            const float L1f = __uint_as_float(v1[j]) * 0x1p-8f;
-            const float hi = L0 + L1f;
-            const float bv = hi - L0;
-            const float lo = ((L0 - (hi - bv)) + (L1f - bv)) +
-                             (__uint_as_float(v2[j]) * 0x1p-16f + __uint_as_float(v3[j]) * 0x1p-24f);
-            const double v = ((double)hi + (double)lo) * s_cs[par][c];
+            const double v = combine_levels(v0[j], v1[j], v2[j], v3[j]) * s_cs[par][c];
             double* gn = a.W + ((((long long)m * a.nnorth + i) * a.kc + k) * 2) * 2 + comp;
             double* gs = gn + 2;
             if (a.nkcl_glob > 1) {
@@ -858,16 +781,6 @@ __global__ void __launch_bounds__(kThreads, 1) k_split_synth(SynthArgs a) {
 
 }  // namespace
 
-namespace {
-// WS bytes per (m, parity, group): the analysis P tiles (rings) or the synthesis alm tiles
-// (l of one parity), whichever is larger
-size_t ws_row_bytes(int lmax, int nnorth) {
-  const size_t nks = (size_t)(nnorth + kKStep - 1) / kKStep;
-  const size_t nkl = (size_t)(lmax / 2 + 1 + kKStep - 1) / kKStep;
-  const size_t a = nks * kSlices * kBTileBytes, b = nkl * kSynthBBytes;
-  return a > b ? a : b;
-}
-}  // namespace
 
 size_t fsht_split_ws_bytes(int lmax, int nnorth, int kc) {
   const int ngroups = (kc + kGroupMaps - 1) / kGroupMaps;
@@ -894,7 +807,7 @@ int fsht_launch_split_prepare(fsht_plan* p, const double2* W, unsigned char* WS,
   sa.EB = EB;
   k_slice_phase<<<dim3(p->lmax + 1, 2, ngroups), 128, 0, s>>>(sa);
   FSHT_LAUNCH_CHECK();
-  if (nkc > 1 && !accumulate) {
+  if (nkc > 1 && !accumulate && alm) {
     // K-chunks add into alm: clear this chunk's columns first
     const size_t L1 = (size_t)p->lmax + 1;
     FSHT_CUDA_TRY(cudaMemset2DAsync(alm + k0, sizeof(double) * nmaps_total, 0,
@@ -906,9 +819,6 @@ int fsht_launch_split_prepare(fsht_plan* p, const double2* W, unsigned char* WS,
 // ------------------------------------------------------------------ host side
 namespace {
 constexpr size_t kLbufCap = 2ull << 30;     // lambda-digit staging per wave
-// per wave: q0, q1, max l-tiles, max ring K-chunks (analysis), max 128-ring blocks,
-// max l-steps, max l K-chunks (synthesis)
-constexpr int kWaveInts = 7;
 
 int eag_of(int lmax) {
   const double b = std::sqrt((2.0 * lmax + 1.0) / (4.0 * M_PI)) * (1.0 + 0x1p-30);
@@ -940,8 +850,10 @@ int fsht_split_tables_init(fsht_plan* p) {
   }
   const size_t unit = (size_t)kSlices * kATileBytes;
   const size_t cap_units = kLbufCap / unit;
+  // spin-2 plans stage lambda1 and lambda2: twice the analysis tiles
+  const long long fa = p->pol ? 2 : 1;
   auto span = [&](int q0, int q1) -> size_t {
-    return (size_t)std::max(off[q1] - off[q0], offT[q1] - offT[q0]);
+    return (size_t)std::max(fa * (off[q1] - off[q0]), offT[q1] - offT[q0]);
   };
   // waves: consecutive q ranges whose tiles (either layout) fit the staging buffer
   std::vector<int> waves;

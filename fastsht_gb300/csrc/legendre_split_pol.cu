@@ -1,0 +1,484 @@
+// Split-precision spin-2 analysis (Q/U -> E/B) on the tcgen05 tensor cores.
+//
+// The precision form of the reference's QU2EB contraction (get_plm_recursive.f90:101-125 for
+// lambda1/lambda2, sht_core.f90:30-89 with the spin-2 GEMM types, sht_main.f90:383-436):
+//   E = -pa [ sum_i lambda1 Q_p(i) + i sum_i lambda2 U_{1-p}(i) ]
+//   B = -pa [ sum_i lambda1 U_p(i) - i sum_i lambda2 Q_{1-p}(i) ]
+// with p = (l - m) mod 2 selecting S (p = 0) or D (p = 1) of each field (lambda1 has the
+// north/south parity of lambda, lambda2 the opposite one).  Digits, levels and scales are
+// those of the spin-0 form (legendre_split.cu); |lambda1|, |lambda2| <= 0.62 sqrt((2l+1)/4pi)
+// (checked against the oracle), so they share the spin-0 row scales.
+//
+//   k_pol_table          per (l, m): c1..c4 of the scaled lambda1/lambda2 formulas;
+//   k_lambda_digits_pol  the FP64 recursion (mu form) once per (m, ring), lambda1 and
+//                        lambda2 digit tiles into the wave's staging buffer;
+//   k_split_gemm_pol     CTA = (64-map group, field, parity, l-tile, ring K-chunk): the
+//                        lambda1 product then the lambda2 product through the same TMEM
+//                        accumulators, each with its own column scales; the epilogue routes
+//                        (Re, Im) of the second product by the factor +-i.
+#include "split_common.cuh"
+
+#include <algorithm>
+#include <vector>
+
+namespace {
+
+__device__ __forceinline__ double pol_normal_l(int l) {
+  if (l < 2) return 0.0;
+  return 1.0 / sqrt((double)(l + 2) * (double)(l + 1) * (double)l * (double)(l - 1));
+}
+
+// lambda1 / D_l = mu_{l-1} c1 cos/s^2 - mu_l (c2 / s^2 + c3)
+// lambda2 / D_l = (mu_{l-1} c1 - mu_l c4 cos) m / s^2
+// c1 = lam_fact nl / a_l, c2 = 2 (l - m^2) nl, c3 = l (l - 1) nl, c4 = 2 (l - 1) nl.  At l = m
+// (mu_{m-1} = 0) these reduce to the reference's diagonal formulas.
+__global__ void k_pol_table(int lmax, FshtPolRow* tab) {
+  const int m = blockIdx.x * blockDim.x + threadIdx.x;
+  if (m > lmax) return;
+  FshtPolRow* row = tab + tri_off(m, lmax);
+  const int m1 = m > 1 ? m : 1;
+  for (int l = m; l <= lmax; ++l) {
+    const double nl = pol_normal_l(l);
+    double c1 = 0.0;
+    if (l > m && l > m1) {
+      const double lf =
+          2.0 * sqrt((double)(2 * l + 1) / (double)(2 * l - 1) * (double)((long long)l * l - (long long)m * m));
+      c1 = lf * nl / rec_coeffs(l, m).a;
+    }
+    FshtPolRow r;
+    r.c1 = c1;
+    r.c2 = 2.0 * ((double)l - (double)m * (double)m) * nl;
+    r.c3 = (double)l * ((double)l - 1.0) * nl;
+    r.c4 = 2.0 * ((double)l - 1.0) * nl;
+    row[l - m] = r;
+  }
+}
+
+// grid (q in wave, 128-ring block), 128 threads = rings.  Tiles of m: (parity, l-tile,
+// part (lambda1, lambda2), k-step) x 4 digits, at twice the spin-0 offset of q.
+struct LamPArgs {
+  int lmax, nnorth, q0;
+  const double* cth;
+  const double* sth;
+  const double* pref;
+  const int* ring_i0;
+  const FshtLamRow* tab;
+  const FshtPolRow* ptab;
+  const long long* lam_off;
+  unsigned char* lbuf;
+};
+
+constexpr int kPolBlock = 32;                 // l per staging block
+constexpr int kPolStride = kSCRings + 2;      // uint64 per staged row (+16 B)
+constexpr size_t kPolStageBytes = (size_t)2 * 2 * (kPolBlock / 2) * kPolStride * 8;
+
+__global__ void __launch_bounds__(128) k_lambda_digits_pol(LamPArgs a) {
+  extern __shared__ __align__(16) unsigned long long S[];     // [part][parity][row][ring]
+  __shared__ double s_beta[kPolBlock];
+  __shared__ int s_erow[kPolBlock];
+  __shared__ FshtPolRow s_pc[kPolBlock];
+  const int q = a.q0 + blockIdx.x;
+  const int m = m_of_q(q, a.lmax);
+  const int i0 = a.ring_i0[m];
+  const int K = a.nnorth - i0;
+  const int rb = blockIdx.y;
+  if (rb * kSCRings >= K) return;
+  const int tid = threadIdx.x;
+  const int r = rb * kSCRings + tid;
+  const bool valid = r < K;
+  const int nks = (K + kKStep - 1) / kKStep;
+  const int ntiles = (a.lmax - m + 1 + 2 * kRows - 1) / (2 * kRows);
+  unsigned char* base =
+      a.lbuf + (size_t)(2 * (a.lam_off[q] - a.lam_off[a.q0])) * kSlices * kATileBytes;
+  const FshtLamRow* tab = a.tab + tri_off(m, a.lmax);
+  const FshtPolRow* ptab = a.ptab + tri_off(m, a.lmax);
+  auto stage = [&](int j0) {
+    if (tid < kPolBlock && m + j0 + tid <= a.lmax) {
+      s_beta[tid] = tab[j0 + tid].beta;
+      s_erow[tid] = tab[j0 + tid].erow;
+      s_pc[tid] = ptab[j0 + tid];
+    }
+  };
+
+  double x = 0.0, inv_s2 = 0.0, b_w = 0.0, c_w = 0.0, s1 = 0.0, s2 = 0.0;
+  int et = 0;
+  if (valid) {
+    int e;
+    const double sth = a.sth[i0 + r];
+    x = a.cth[i0 + r];
+    inv_s2 = 1.0 / (sth * sth);
+    b_w = x * inv_s2;
+    c_w = (double)m * inv_s2;
+    rec_seed(sth, a.pref[m], m, s1, e);
+    et = 600 * e;
+  }
+  stage(0);
+  __syncthreads();
+  const int lend = ntiles * 2 * kRows;
+  auto Sidx = [&](int part, int par, int row, int col) -> unsigned long long& {
+    return S[((part * 2 + par) * (kPolBlock / 2) + row) * kPolStride + col];
+  };
+  for (int lb = 0; lb < lend; lb += kPolBlock) {
+#pragma unroll 2
+    for (int jj = 0; jj < kPolBlock; ++jj) {
+      const int j = lb + jj;
+      unsigned long long pk1 = 0, pk2 = 0;
+      if (m + j <= a.lmax) {
+        if (j > 0) {
+          const double t = s_beta[jj] * s2;
+          const double nx = fma(x, s1, -t);
+          s2 = s1;
+          s1 = nx;
+        }
+        if (valid) {
+          const FshtPolRow c = s_pc[jj];
+          const double u = s2 * c.c1;
+          const double l1 = fma(u, b_w, -s1 * fma(c.c2, inv_s2, c.c3));
+          const double l2 = fma(-s1, c.c4 * x, u) * c_w;
+          uint16_t d[4];
+          tc::digits4(l1, s_erow[jj] - et, d);
+          pk1 = (unsigned long long)d[0] | ((unsigned long long)d[1] << 16) |
+                ((unsigned long long)d[2] << 32) | ((unsigned long long)d[3] << 48);
+          tc::digits4(l2, s_erow[jj] - et, d);
+          pk2 = (unsigned long long)d[0] | ((unsigned long long)d[1] << 16) |
+                ((unsigned long long)d[2] << 32) | ((unsigned long long)d[3] << 48);
+        }
+      }
+      Sidx(0, jj & 1, jj >> 1, tid) = pk1;
+      Sidx(1, jj & 1, jj >> 1, tid) = pk2;
+    }
+    {
+      const double am = fmax(fabs(s1), fabs(s2));
+      if (am > 0x1p300) {
+        s1 *= 0x1p-600;
+        s2 *= 0x1p-600;
+        et += 600;
+      } else if (am > 0.0 && am < 0x1p-300) {
+        s1 *= 0x1p600;
+        s2 *= 0x1p600;
+        et -= 600;
+      }
+    }
+    __syncthreads();
+    const int t = lb / (2 * kRows);
+    const int rowt0 = (lb % (2 * kRows)) >> 1;
+    for (int u = tid; u < 2 * 2 * (kPolBlock / 2) * (kSCRings / 8); u += 128) {
+      const int r8 = u & 7, khalf = (u >> 3) & 1, rg = (u >> 4) & 1, ks = (u >> 5) & 7,
+                par = (u >> 8) & 1, part = u >> 9;
+      const int gks = rb * (kSCRings / kKStep) + ks;
+      if (gks >= nks) continue;
+      const int row = rg * 8 + r8;
+      const unsigned long long* src = &Sidx(part, par, row, ks * kKStep + khalf * 8);
+      unsigned long long v[8];
+#pragma unroll
+      for (int i = 0; i < 8; i += 2) {
+        const ulonglong2 w = *reinterpret_cast<const ulonglong2*>(src + i);
+        v[i] = w.x;
+        v[i + 1] = w.y;
+      }
+      const int rowt = rowt0 + row;
+      unsigned char* tile =
+          base + (((size_t)(par * ntiles + t) * 2 + part) * nks + gks) * kSlices * kATileBytes +
+          (rowt >> 3) * 256 + khalf * 128 + (rowt & 7) * 16;
+#pragma unroll
+      for (int d = 0; d < kSlices; ++d) {
+        uint32_t h[8];
+#pragma unroll
+        for (int i = 0; i < 8; ++i) h[i] = (uint32_t)(v[i] >> (16 * d)) & 0xFFFFu;
+        uint4 o;
+        o.x = h[0] | (h[1] << 16);
+        o.y = h[2] | (h[3] << 16);
+        o.z = h[4] | (h[5] << 16);
+        o.w = h[6] | (h[7] << 16);
+        *reinterpret_cast<uint4*>(tile + (size_t)d * kATileBytes) = o;
+      }
+    }
+    stage(lb + kPolBlock);
+    __syncthreads();
+  }
+}
+
+// CTA = (group, field x parity x l-tile x K-chunk, q): the lambda1 pass then the lambda2
+// pass through the same TMEM accumulators.
+constexpr int kStagesP = 6;
+constexpr uint32_t kStageBytesP = 2 * kSlices * kATileBytes;    // 32 KB: A then B
+
+struct GemmPArgs {
+  int lmax, nnorth, ngroups, nkc_glob, q0, ntmax, nkcmax, accumulate, which;
+  size_t row_bytes;
+  const int* ring_i0;
+  const long long* lam_off;
+  const FshtLamRow* tab;
+  const unsigned char* lbuf;
+  const unsigned char* WSQ;
+  const unsigned char* WSU;
+  const int* EBQ;
+  const int* EBU;
+  double* almE;
+  double* almB;
+  int ld, k0, kc;
+  double pa;
+  int* err;
+};
+
+struct __align__(8) GemmPSmemHdr {
+  uint64_t full[kStagesP], empty[kStagesP], tfull, tempty, fin;
+  uint32_t tmem;
+  int abort;
+};
+
+__global__ void __launch_bounds__(kThreads, 1) k_split_gemm_pol(GemmPArgs a) {
+  extern __shared__ __align__(1024) unsigned char smem[];
+  __shared__ GemmPSmemHdr h;
+  __shared__ double s_cs[2][kCols];
+  __shared__ double s_rs[kRows];
+
+  const int g = blockIdx.x;
+  const int field = blockIdx.y & 1;            // 0: E, 1: B
+  const int p = (blockIdx.y >> 1) & 1;
+  const int rest = blockIdx.y >> 2;
+  const int kci = rest % a.nkcmax;
+  const int t = rest / a.nkcmax;
+  if (!(a.which & (1 << field))) return;
+  const int q = a.q0 + blockIdx.z;
+  const int m = m_of_q(q, a.lmax);
+  const int i0 = a.ring_i0[m];
+  const int K = a.nnorth - i0;
+  const int nks = (K + kKStep - 1) / kKStep;
+  const int ntiles = (a.lmax - m + 1 + 2 * kRows - 1) / (2 * kRows);
+  const int ks0 = kci * (kKChunk / kKStep);
+  const int ks1 = min(nks, ks0 + kKChunk / kKStep);
+  if (t >= ntiles || ks0 >= ks1) return;          // uniform: before any barrier or TMEM
+  const int nk = ks1 - ks0;
+  const int lt0 = m + t * 2 * kRows;
+  // B operands and their column exponents: part 0 multiplies lambda1, part 1 lambda2
+  const unsigned char* ws[2];
+  const int* eb[2];
+  int bpar[2] = {p, 1 - p};
+  ws[0] = field == 0 ? a.WSQ : a.WSU;
+  eb[0] = field == 0 ? a.EBQ : a.EBU;
+  ws[1] = field == 0 ? a.WSU : a.WSQ;
+  eb[1] = field == 0 ? a.EBU : a.EBQ;
+
+  const int tid = threadIdx.x;
+  const int warp = tid >> 5;
+  volatile int* abort = &h.abort;
+  if (tid == 0) {
+    for (int s = 0; s < kStagesP; ++s) {
+      tc::mbar_init(&h.full[s], 1);
+      tc::mbar_init(&h.empty[s], 1);
+    }
+    tc::mbar_init(&h.tfull, 1);
+    tc::mbar_init(&h.tempty, 128);
+    tc::mbar_init(&h.fin, 1);
+    h.abort = 0;
+    tc::mbar_fence_init();
+  }
+  if (tid < kCols) {
+    for (int part = 0; part < 2; ++part) {
+      const int e = eb[part][(((long long)m * 2 + bpar[part]) * a.ngroups + g) * kCols + tid];
+      s_cs[part][tid] = (e == kEmptyExp) ? 0.0 : ldexp(-a.pa, e - 12);
+    }
+    const int l = lt0 + p + 2 * tid;
+    if (l <= a.lmax) {
+      const FshtLamRow rw = a.tab[tri_off(m, a.lmax) + (l - m)];
+      s_rs[tid] = ldexp(rw.dm, rw.erow + rw.dx);
+    } else {
+      s_rs[tid] = 0.0;
+    }
+  }
+  if (warp == 0) tc::tmem_alloc(&h.tmem, 512);
+  tc::tc_fence_before();
+  __syncthreads();
+  tc::tc_fence_after();
+  const uint32_t tmem = h.tmem;
+
+  uint32_t n_loaded = 0;
+  if (tid == 128) {
+    const unsigned char* lam =
+        a.lbuf + (size_t)(2 * (a.lam_off[q] - a.lam_off[a.q0])) * kSlices * kATileBytes;
+    for (int i = 0; i < 2 * nk; ++i) {
+      const int part = i / nk, ks = ks0 + i % nk;
+      const uint32_t st = i % kStagesP;
+      if (!tc::mbar_wait(&h.empty[st], ((i / kStagesP) & 1) ^ 1, abort)) break;
+      unsigned char* dst = smem + st * kStageBytesP;
+      const unsigned char* asrc =
+          lam + (((size_t)(p * ntiles + t) * 2 + part) * nks + ks) * kSlices * kATileBytes;
+      const unsigned char* bsrc =
+          ws[part] + (((size_t)m * 2 + bpar[part]) * a.ngroups + g) * a.row_bytes +
+          (size_t)ks * kSlices * kBTileBytes;
+      tc::mbar_arrive_expect_tx(&h.full[st], kStageBytesP);
+      tc::bulk_g2s(dst, asrc, kSlices * kATileBytes, &h.full[st]);
+      tc::bulk_g2s(dst + kSlices * kATileBytes, bsrc, kSlices * kBTileBytes, &h.full[st]);
+      ++n_loaded;
+    }
+  } else if (tid == 160) {
+    const uint32_t idesc = tc::umma_idesc_bf16(kRows, kCols);
+    const uint32_t s_u = tc::smem_u32(smem);
+    for (int i = 0; i < 2 * nk; ++i) {
+      if (i == nk) {
+        tc::umma_commit(&h.tfull);
+        if (!tc::mbar_wait(&h.tempty, 0, abort)) break;
+        tc::tc_fence_after();
+      }
+      const uint32_t st = i % kStagesP;
+      if (!tc::mbar_wait(&h.full[st], (i / kStagesP) & 1, abort)) break;
+      tc::tc_fence_after();
+      const uint32_t abase = s_u + st * kStageBytesP;
+      const uint32_t bbase = abase + kSlices * kATileBytes;
+      const bool first = (i % nk) == 0;
+#pragma unroll
+      for (int lev = 0; lev <= 3; ++lev) {
+#pragma unroll
+        for (int aa = 0; aa <= lev; ++aa) {
+          const uint64_t ad = tc::umma_desc(abase + aa * kATileBytes, 128, 256);
+          const uint64_t bd = tc::umma_desc(bbase + (lev - aa) * kBTileBytes, 128, 256);
+          tc::umma_bf16(tmem + lev * kCols, ad, bd, idesc, (!first || aa > 0) ? 1u : 0u);
+        }
+      }
+      tc::umma_commit(&h.empty[st]);
+    }
+    tc::umma_commit(&h.tfull);
+  }
+  if (tid < 128) {
+    const int row = (warp << 5) + (tid & 31);
+    const int l = lt0 + p + 2 * row;
+    const bool rowok = l <= a.lmax;
+    const long long L1 = a.lmax + 1;
+    const long long re_row = (long long)m * L1 + l;
+    const long long im_row = (L1 - m) * L1 + (l - m);
+    double* alm = field == 0 ? a.almE : a.almB;
+    const double rs = s_rs[row];
+    for (int part = 0; part < 2; ++part) {
+      bool ok = tc::mbar_wait(&h.tfull, part, abort);
+      ok = __all_sync(0xffffffffu, ok);
+      tc::tc_fence_after();
+      if (!ok) break;
+      const uint32_t lane_base = tmem + ((uint32_t)(warp << 5) << 16);
+      for (int c0 = 0; c0 < kCols; c0 += 16) {
+        uint32_t v0[16], v1[16], v2[16], v3[16];
+        tc::tmem_ld16(lane_base + 0 * kCols + c0, v0);
+        tc::tmem_ld16(lane_base + 1 * kCols + c0, v1);
+        tc::tmem_ld16(lane_base + 2 * kCols + c0, v2);
+        tc::tmem_ld16(lane_base + 3 * kCols + c0, v3);
+        tc::tmem_wait_ld();
+        const int comp = c0 >> 6;
+        // part 0: (Re, Im) -> (Re, Im).  part 1 (factor +i for E, -i for B):
+        //   E: Re <- -Im, Im <- +Re;   B: Re <- +Im, Im <- -Re
+        int tgt = comp;
+        double sgn = 1.0;
+        if (part == 1) {
+          tgt = 1 - comp;
+          sgn = (field == 0) == (comp == 1) ? -1.0 : 1.0;
+        }
+        if (!rowok || (tgt == 1 && m == 0)) continue;
+        const long long rowidx = tgt == 0 ? re_row : im_row;
+#pragma unroll
+        for (int j = 0; j < 16; ++j) {
+          const int c = c0 + j;
+          const int k = g * kGroupMaps + (c & 63);
+          if (k < a.kc) {
+            const double v = sgn * combine_levels(v0[j], v1[j], v2[j], v3[j]) * rs * s_cs[part][c];
+            double* dst = alm + rowidx * a.ld + a.k0 + k;
+            if (a.nkc_glob > 1) atomicAdd(dst, v);
+            else if (part == 0 && !a.accumulate) *dst = v;
+            else *dst += v;
+          }
+        }
+      }
+      tc::tc_fence_before();
+      if (part == 0) tc::mbar_arrive(&h.tempty);
+    }
+  }
+  if (tid == 160) {
+    tc::umma_commit(&h.fin);
+    for (uint32_t it = 0; it < tc::kWaitLimit; ++it)
+      if (tc::mbar_try_wait(&h.fin, 0)) break;
+  }
+  if (tid == 128) {
+    for (uint32_t d = 0; d < (uint32_t)kStagesP && d < n_loaded; ++d) {
+      const uint32_t i = n_loaded - 1 - d;
+      for (uint32_t it = 0; it < tc::kWaitLimit; ++it)
+        if (tc::mbar_try_wait(&h.full[i % kStagesP], (i / kStagesP) & 1)) break;
+    }
+  }
+  tc::tc_fence_before();
+  __syncthreads();
+  if (warp == 0) tc::tmem_dealloc(tmem, 512);
+  if (tid == 0 && h.abort) atomicOr(a.err, 1);
+}
+
+}  // namespace
+
+int fsht_split_pol_tables_init(fsht_plan* p) {
+  const int lmax = p->lmax;
+  const size_t ntab = (size_t)tri_off(lmax + 1, lmax);
+  FSHT_CUDA_TRY(cudaMalloc(&p->d_poltab, sizeof(FshtPolRow) * (ntab ? ntab : 1)));
+  k_pol_table<<<(lmax + 1 + 127) / 128, 128, 0, p->stream>>>(lmax, p->d_poltab);
+  FSHT_LAUNCH_CHECK();
+  return FSHT_OK;
+}
+
+int fsht_launch_split_lambda_pol(fsht_plan* p, int w, unsigned char* lbuf, cudaStream_t s) {
+  const int* wv = p->h_waves + kWaveInts * w;
+  if (wv[4] == 0) return FSHT_OK;
+  LamPArgs a;
+  a.lmax = p->lmax;
+  a.nnorth = p->nnorth;
+  a.q0 = wv[0];
+  a.cth = p->d_cth;
+  a.sth = p->d_sth;
+  a.pref = p->d_pref;
+  a.ring_i0 = p->d_ring_i0;
+  a.tab = p->d_lamtab;
+  a.ptab = p->d_poltab;
+  a.lam_off = p->d_lam_off;
+  a.lbuf = lbuf;
+  FSHT_CUDA_TRY(cudaFuncSetAttribute(k_lambda_digits_pol,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)kPolStageBytes));
+  k_lambda_digits_pol<<<dim3(wv[1] - wv[0], wv[4]), 128, kPolStageBytes, s>>>(a);
+  FSHT_LAUNCH_CHECK();
+  return FSHT_OK;
+}
+
+int fsht_launch_split_gemm_pol(fsht_plan* p, int w, const unsigned char* WSQ, const int* EBQ,
+                               const unsigned char* WSU, const int* EBU,
+                               const unsigned char* lbuf, double* almE, double* almB,
+                               int nmaps_total, int k0, int kc, int accumulate, int which,
+                               cudaStream_t s) {
+  const int* wv = p->h_waves + kWaveInts * w;
+  if (wv[3] == 0) return FSHT_OK;
+  GemmPArgs a;
+  a.lmax = p->lmax;
+  a.nnorth = p->nnorth;
+  a.ngroups = (kc + kGroupMaps - 1) / kGroupMaps;
+  a.nkc_glob = (p->nnorth + kKChunk - 1) / kKChunk;
+  a.q0 = wv[0];
+  a.ntmax = wv[2];
+  a.nkcmax = wv[3];
+  a.accumulate = accumulate;
+  a.which = which;
+  a.row_bytes = ws_row_bytes(p->lmax, p->nnorth);
+  a.ring_i0 = p->d_ring_i0;
+  a.lam_off = p->d_lam_off;
+  a.tab = p->d_lamtab;
+  a.lbuf = lbuf;
+  a.WSQ = WSQ;
+  a.WSU = WSU;
+  a.EBQ = EBQ;
+  a.EBU = EBU;
+  a.almE = almE;
+  a.almB = almB;
+  a.ld = nmaps_total;
+  a.k0 = k0;
+  a.kc = kc;
+  a.pa = p->pa;
+  a.err = p->d_err;
+  const size_t sm = (size_t)kStagesP * kStageBytesP;
+  FSHT_CUDA_TRY(cudaFuncSetAttribute(k_split_gemm_pol,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+  k_split_gemm_pol<<<dim3(a.ngroups, 4 * a.ntmax * a.nkcmax, wv[1] - wv[0]), kThreads, sm, s>>>(a);
+  FSHT_LAUNCH_CHECK();
+  return FSHT_OK;
+}

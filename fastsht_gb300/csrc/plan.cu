@@ -89,6 +89,7 @@ void free_plan_memory(fsht_plan* p) {
   cudaFree(p->d_lamtab);
   cudaFree(p->d_lam_off);
   cudaFree(p->d_lbuf);
+  cudaFree(p->d_poltab);
   delete[] p->h_waves;
   delete[] p->h_ring_i0;
   if (p->prof) {
@@ -271,6 +272,8 @@ int fsht_plan_create(int nside, int lmax, int nmaps_max, int flags, int precisio
   if ((rc = fsht_launch_ring_skip(p, p->stream))) return fail(rc);
   if ((rc = fsht_fft_tables_init(p))) return fail(rc);
   if (precision == FSHT_PREC_SPLIT && (rc = fsht_split_tables_init(p))) return fail(rc);
+  if (precision == FSHT_PREC_SPLIT && p->pol && (rc = fsht_split_pol_tables_init(p)))
+    return fail(rc);
   // ---- workspace: nbuf phase matrices of kchunk maps (+ the sliced copy for the
   // split form, sized in groups of 128 maps)
   const size_t limit = workspace_limit_bytes
@@ -279,8 +282,9 @@ int fsht_plan_create(int nside, int lmax, int nmaps_max, int flags, int precisio
   const size_t per_map = per_map_buffer_bytes(p) * p->nbuf;
   auto need = [&](size_t k) -> size_t {
     size_t b = per_map * k;
-    if (precision == FSHT_PREC_SPLIT)
-      b += fsht_split_ws_bytes(lmax, p->nnorth, (int)k) + fsht_split_eb_bytes(lmax, (int)k) +
+    if (precision == FSHT_PREC_SPLIT)   // spin 2: digit tiles of Q and U
+      b += (p->pol ? 2 : 1) * (fsht_split_ws_bytes(lmax, p->nnorth, (int)k) +
+                               fsht_split_eb_bytes(lmax, (int)k)) +
            p->lbuf_bytes;
     return b;
   };
@@ -300,9 +304,10 @@ int fsht_plan_create(int nside, int lmax, int nmaps_max, int flags, int precisio
     return fail(FSHT_ECUDA);
   }
   if (precision == FSHT_PREC_SPLIT && !tables_only) {
-    p->ws_bytes = fsht_split_ws_bytes(lmax, p->nnorth, p->kchunk);
+    const size_t f = p->pol ? 2 : 1;
+    p->ws_bytes = f * fsht_split_ws_bytes(lmax, p->nnorth, p->kchunk);
     if ((rc = dalloc((void**)&p->d_ws, p->ws_bytes))) return fail(rc);
-    if ((rc = dalloc((void**)&p->d_eb, fsht_split_eb_bytes(lmax, p->kchunk)))) return fail(rc);
+    if ((rc = dalloc((void**)&p->d_eb, f * fsht_split_eb_bytes(lmax, p->kchunk)))) return fail(rc);
     if ((rc = dalloc((void**)&p->d_lbuf, p->lbuf_bytes))) return fail(rc);
   }
   if ((ce = cudaStreamSynchronize(p->stream)) != cudaSuccess) {
@@ -568,6 +573,44 @@ int fsht_alm2t(fsht_plan* p, const double* alm, double* maps, int nmaps) {
 }
 
 // ----------------------------------------------------------------- spin 2
+// One chunk's spin-2 analysis of {S, D}(Q), {S, D}(U) into E/B (which: bit0 E, bit1 B),
+// added when accumulate: the FP64 kernel, or the split form's tiles and waves.
+static int pol_analysis(fsht_plan* p, const double2* WQ, const double2* WU, double* almE,
+                        double* almB, int nmaps, int c0, int kc, int accumulate, int which) {
+  if (p->precision != FSHT_PREC_SPLIT) {
+    FSHT_PROF(FSHT_KCAT_ANALYSIS);
+    return fsht_launch_analysis_fp64(p, 2, WQ, WU, almE, almB, nmaps, c0, kc, accumulate, which,
+                                     p->stream);
+  }
+  if (!p->d_poltab) {
+    fsht_set_error("spin-2 split analysis needs a plan created with FSHT_FLAG_POL");
+    return FSHT_EUNSUPPORTED;
+  }
+  unsigned char* wsq = p->d_ws;
+  unsigned char* wsu = p->d_ws + fsht_split_ws_bytes(p->lmax, p->nnorth, kc);
+  int* ebq = p->d_eb;
+  int* ebu = p->d_eb + fsht_split_eb_bytes(p->lmax, kc) / sizeof(int);
+  {
+    FSHT_PROF(FSHT_KCAT_SLICE);
+    FSHT_TRY(fsht_launch_split_prepare(p, WQ, wsq, ebq, (which & 1) ? almE : nullptr, nmaps, c0,
+                                       kc, accumulate, p->stream));
+    FSHT_TRY(fsht_launch_split_prepare(p, WU, wsu, ebu, (which & 2) ? almB : nullptr, nmaps, c0,
+                                       kc, accumulate, p->stream));
+  }
+  for (int w = 0; w < p->nwaves; ++w) {
+    {
+      FSHT_PROF(FSHT_KCAT_LAMBDA);
+      FSHT_TRY(fsht_launch_split_lambda_pol(p, w, p->d_lbuf, p->stream));
+    }
+    {
+      FSHT_PROF(FSHT_KCAT_ANALYSIS);
+      FSHT_TRY(fsht_launch_split_gemm_pol(p, w, wsq, ebq, wsu, ebu, p->d_lbuf, almE, almB, nmaps,
+                                          c0, kc, accumulate, which, p->stream));
+    }
+  }
+  return FSHT_OK;
+}
+
 static int qu_analysis(fsht_plan* p, const double* Q, const double* U, double* almE,
                        double* almB, int nmaps, int niter, int method, int which) {
   FSHT_TRY(need_bufs(p, niter > 0 ? 4 : 2));
@@ -583,12 +626,9 @@ static int qu_analysis(fsht_plan* p, const double* Q, const double* U, double* a
       FSHT_PROF(FSHT_KCAT_FFT_FWD);
       FSHT_TRY(fsht_launch_ring_fft_fwd(p, U + (size_t)c0 * p->npix, p->npix, kc, WU, p->stream));
     }
-    {
-      FSHT_PROF(FSHT_KCAT_ANALYSIS);
-      FSHT_TRY(fsht_launch_analysis_fp64(p, 2, WQ, WU, almE, almB, nmaps, c0, kc, 0, which,
-                                         p->stream));
-    }
+    FSHT_TRY(pol_analysis(p, WQ, WU, almE, almB, nmaps, c0, kc, 0, which));
     if (niter > 0) {
+      // the split form refines with the FP64 spin-2 synthesis and residual
       double2* RQ = work_buf(p, 2, kc);
       double2* RU = work_buf(p, 3, kc);
       for (int it = 0; it < niter; ++it) {
@@ -604,11 +644,7 @@ static int qu_analysis(fsht_plan* p, const double* Q, const double* U, double* a
           FSHT_PROF(FSHT_KCAT_RESIDUAL);
           FSHT_TRY(fsht_launch_fourier_residual(p, WU, RU, kc, method, p->stream));
         }
-        {
-          FSHT_PROF(FSHT_KCAT_ANALYSIS);
-          FSHT_TRY(fsht_launch_analysis_fp64(p, 2, RQ, RU, almE, almB, nmaps, c0, kc, 1, which,
-                                             p->stream));
-        }
+        FSHT_TRY(pol_analysis(p, RQ, RU, almE, almB, nmaps, c0, kc, 1, which));
       }
     }
   }

@@ -192,8 +192,10 @@ class Server:
         if p is None:
             p = C.c_void_p()
             with torch.cuda.device(self.device):
-                _lib.call("fsht_plan_create", nside, lmax, 1, _lib.FSHT_FLAG_TABLES_ONLY,
-                          _lib.FSHT_PREC_SPLIT if precision == "split" else _lib.FSHT_PREC_FP64,
+                split = precision == "split"
+                flags = _lib.FSHT_FLAG_TABLES_ONLY | (_lib.FSHT_FLAG_POL if split else 0)
+                _lib.call("fsht_plan_create", nside, lmax, 1, flags,
+                          _lib.FSHT_PREC_SPLIT if split else _lib.FSHT_PREC_FP64,
                           0, None, C.byref(p))
             self._plans[key] = p
         return p

@@ -39,7 +39,8 @@ def test_mixed_batch_matches_single_plans():
              ("alm2t", 16, 40, 5, "fp64"), ("eb2qu", 16, 33, 2, "fp64"),
              ("t2alm", 32, 70, 7, "split"), ("t2alm", 32, 95, 1, "fp64"),
              ("qu2eb", 4, 11, 4, "fp64"), ("t2alm", 64, 150, 9, "split"),
-             ("alm2t", 8, 23, 2, "fp64"), ("t2alm", 16, 40, 70, "split")]
+             ("alm2t", 8, 23, 2, "fp64"), ("t2alm", 16, 40, 70, "split"),
+             ("qu2eb", 32, 70, 3, "split"), ("alm2t", 32, 70, 4, "split")]
     b = Batch(nslots=3)
     refs = []
     for i, (kind, ns, lmax, nmaps, prec) in enumerate(specs):
@@ -75,6 +76,7 @@ def test_mixed_batch_matches_single_plans():
                 assert torch.isfinite(got).all()
                 scale = want.abs().max().item()
                 err = (got - want).abs().max().item() / scale
+                # split jobs: identical to the split single-plan path
                 assert err <= 1e-12, (j.kind, j.nside, j.lmax, j.precision, rep, err)
     info = b.info()
     assert info["graph_nodes"] > 0 and info["plans"] == len({(s[1], s[2], s[4]) for s in specs})

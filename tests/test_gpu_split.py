@@ -127,3 +127,46 @@ def test_split_refinement_at_nside_1024():
     a64 = SHT(ns, lmax, nsim, niter=1).t2alm(maps)
     a16 = SHT(ns, lmax, nsim, niter=1, precision="split").t2alm(maps)
     assert rel_alm_err(a16, a64) <= SPLIT_TOL
+
+
+def _pol_maps(ns, lmax, nsim, seed):
+    rng = np.random.default_rng(seed)
+    l = np.arange(lmax + 1, dtype=float)
+    cl = np.where(l >= 2, 1.0 / np.maximum(l * (l + 1), 1.0), 0.0)
+    E = gaussian_alm(cl, lmax, nsim, rng)
+    B = gaussian_alm(0.1 * cl, lmax, nsim, rng)
+    return SHT(ns, lmax, nsim, pol=True).eb2qu(E, B)
+
+
+@pytest.mark.parametrize("ns,lmax,nsim", [(4, 11, 2), (16, 47, 5), (64, 191, 70), (128, 300, 3)])
+def test_split_qu2eb_matches_fp64(ns, lmax, nsim):
+    """Spin-2 split analysis (lambda1/lambda2 digit products, the +-i routing) against the
+    plain path, E and B each within the bar."""
+    Q, U = _pol_maps(ns, lmax, nsim, ns + 3)
+    E64, B64 = SHT(ns, lmax, nsim, pol=True).qu2eb(Q, U)
+    sht = SHT(ns, lmax, nsim, pol=True, precision="split")
+    E16, B16 = sht.qu2eb(Q, U)
+    assert rel_alm_err(E16, E64) <= SPLIT_TOL
+    assert rel_alm_err(B16, B64) <= SPLIT_TOL
+    assert rel_alm_err(sht.qu2e(Q, U), E64) <= SPLIT_TOL
+    assert rel_alm_err(sht.qu2b(Q, U), B64) <= SPLIT_TOL
+
+
+def test_split_qu2eb_ring_chunks_at_nside_1024():
+    """nside 1024: 2048 north rings, so ring K-chunks add into E/B with atomics."""
+    ns, lmax, nsim = 1024, 2047, 2
+    Q, U = _pol_maps(ns, lmax, nsim, 9)
+    E64, B64 = SHT(ns, lmax, nsim, pol=True).qu2eb(Q, U)
+    E16, B16 = SHT(ns, lmax, nsim, pol=True, precision="split").qu2eb(Q, U)
+    assert rel_alm_err(E16, E64) <= SPLIT_TOL
+    assert rel_alm_err(B16, B64) <= SPLIT_TOL
+
+
+def test_split_qu2eb_refinement():
+    """niter = 1 on Q/U: FP64 spin-2 synthesis and residual, split analyses."""
+    ns, lmax, nsim = 32, 80, 4
+    Q, U = _pol_maps(ns, lmax, nsim, 10)
+    E64, B64 = SHT(ns, lmax, nsim, niter=1, pol=True).qu2eb(Q, U)
+    E16, B16 = SHT(ns, lmax, nsim, niter=1, pol=True, precision="split").qu2eb(Q, U)
+    assert rel_alm_err(E16, E64) <= SPLIT_TOL
+    assert rel_alm_err(B16, B64) <= SPLIT_TOL
