@@ -499,7 +499,8 @@ def ours(args, rank, world, local):
     # -------- one refinement step (niter = 1) in the split form, against the plain path
     # with the same niter on the first maps of the batch
     if args.precision == "split" and not args.no_fp64:
-        sr = SHT(nside, lmax, nmaps, niter=1, device=local, precision="split")
+        sr = SHT(nside, lmax, nmaps, niter=1, device=local, precision="split",
+                 workspace_limit=40 << 30)
         ms_r, out_r, pk_r, _, _, _ = timed_steps(lib, sr, maps, 1, 1, world, dist, dev, local,
                                                  sample_clocks=False)
         sr.close()

@@ -58,8 +58,8 @@ JobLayout job_layout(const fsht_plan* p, const fsht_job& j, int kc) {
   L.total = L.ws_off;
   if (p->precision == FSHT_PREC_SPLIT && j.kind != FSHT_JOB_EB2QU) {
     const size_t f = j.kind == FSHT_JOB_QU2EB ? 2 : 1;   // spin 2: tiles of Q and U
-    L.eb_off = align_up(L.ws_off + f * fsht_split_ws_bytes(p->lmax, p->nnorth, kc));
-    L.lb_off = align_up(L.eb_off + f * fsht_split_eb_bytes(p->lmax, kc));
+    L.eb_off = align_up(L.ws_off + f * fsht_split_ws_bytes(p, kc));
+    L.lb_off = align_up(L.eb_off + f * fsht_split_eb_bytes(p, kc));
     L.total = align_up(L.lb_off + p->lbuf_bytes);
   }
   return L;

@@ -41,18 +41,21 @@ FSHT_HD int ring_phase_flag(int ns, int i) {
 // ---------------------------------------------------------------- plan
 struct FshtRingFFT {
   int n;          // ring length
-  int P;          // transform size: n (power of two) or the Bluestein size 2^logT or 3*2^logT
+  int nd;         // DFT length: n (north + i south packed), or n/2 (each ring alone as its
+                  // even/odd samples packed) when the packed transform exceeds shared memory
+  int P;          // transform size: nd (power of two) or the Bluestein size 2^logT or 3*2^logT
   int logT;       // log2 of the power-of-two factor of P
   int r3;         // 1 when P = 3 * 2^logT
-  int bluestein;  // 1 when n is not a power of two
-  long long chirp_off;  // offset (double2) of w_j = exp(-i pi j^2/n), j < n
+  int bluestein;  // 1 when nd is not a power of two
+  long long chirp_off;  // offset (double2) of w_j = exp(-i pi j^2/nd), j < nd
   long long bhat_off;   // offset (double2) of the filter spectrum (transform order), P entries
+  long long rtw_off;    // nd = n/2 only: offset of exp(-2 pi i k / n), k <= nd
 };
 
-// Transform size of a ring of n points: n itself when n is a power of two, else the
-// smallest 2^k or 3*2^k >= 2n - 1 (Bluestein's linear convolution of length 2n - 1).
+// Transform size of a DFT of nd points: nd itself when nd is a power of two, else the
+// smallest 2^k or 3*2^k >= 2 nd - 1 (Bluestein's linear convolution of length 2 nd - 1).
 FSHT_HD void fsht_ring_fft_size(FshtRingFFT& r) {
-  const int n = r.n;
+  const int n = r.nd;
   r.r3 = 0;
   if ((n & (n - 1)) == 0) {
     r.bluestein = 0;
@@ -105,6 +108,7 @@ struct fsht_plan {
   int* h_ring_i0;
   FshtRingFFT* d_rfft;             // per north ring
   double2* d_chirp;                // Bluestein chirps
+  double2* d_rtw;                  // half-length rings: exp(-2 pi i k / n)
   double2* d_bhat;                 // Bluestein filter spectra
   double2* d_tw;                   // [exp(-2 pi i t / Tmax), t < Tmax][exp(-2 pi i t / P3max), t < P3max]
   int Pmax;                        // largest transform size (shared-memory sizing)
@@ -129,6 +133,7 @@ struct fsht_plan {
   int nwaves;
   unsigned char* d_lbuf;
   size_t lbuf_bytes;
+  int wave_qmax;                   // most orders in one wave
   FshtPolRow* d_poltab;            // spin-2 plans only, same triangular index as d_lamtab
 };
 
@@ -159,8 +164,8 @@ void fsht_set_error(const char* fmt, ...);
 
 // ---------------------------------------------------------------- internal API
 struct FshtFftLayout {
-  int Pmax, Tmax, logTmax, P3max, nblue;
-  long long chirp_total, bhat_total;
+  int Pmax, Tmax, logTmax, P3max, nblue, nhalf;
+  long long chirp_total, bhat_total, rtw_total;
   size_t smem;
 };
 // Host-side FFT table layout for nside/lmax; fills rfs[2 nside] and blue_rings
@@ -183,27 +188,29 @@ int fsht_launch_analysis_fp64(fsht_plan* p, int spin, const double2* WQ,
                               const double2* WU, double* almE, double* almB,
                               int nmaps_total, int k0, int kc, int accumulate,
                               int which, cudaStream_t s);
-size_t fsht_split_ws_bytes(int lmax, int nnorth, int kc);
-size_t fsht_split_eb_bytes(int lmax, int kc);
-// Split-precision (BF16 digits on tcgen05) spin-0 analysis of one chunk.  Tables (plan
-// creation): recursion rows, per-m tile offsets, waves of m and the staging size.
-// prepare cuts the {S, D} phase matrix W into digit tiles WS and column exponents EB
-// (and clears alm's chunk columns when K-chunks will add into it); then, per wave w,
-// lambda writes the wave's lambda digit tiles into lbuf and gemm contracts them with WS
-// into alm.
+// Split-precision form.  WS / EB: digit tiles and column exponents of one wave of m.
+size_t fsht_split_ws_bytes(const fsht_plan* p, int kc);
+size_t fsht_split_eb_bytes(const fsht_plan* p, int kc);
+// Spin-0 analysis of one chunk (BF16 digits on tcgen05).  Tables (plan creation): recursion
+// rows, per-m tile offsets, waves of m and the staging size.  Per chunk: clear alm's chunk
+// columns when ring K-chunks will add into it; per wave w: slice cuts the {S, D} matrix W of
+// the wave's orders into digit tiles WS and column exponents EB, lambda writes the wave's
+// lambda digit tiles into lbuf, gemm contracts them into alm.
 int fsht_split_tables_init(fsht_plan* p);
-int fsht_launch_split_prepare(fsht_plan* p, const double2* W, unsigned char* WS, int* EB,
-                              double* alm, int nmaps_total, int k0, int kc, int accumulate,
-                              cudaStream_t s);
+int fsht_split_clear_alm(fsht_plan* p, double* alm, int nmaps_total, int k0, int kc,
+                         cudaStream_t s);
+int fsht_launch_split_slice(fsht_plan* p, int w, const double2* W, unsigned char* WS, int* EB,
+                            int kc, cudaStream_t s);
 int fsht_launch_split_lambda(fsht_plan* p, int w, unsigned char* lbuf, cudaStream_t s);
 int fsht_launch_split_gemm(fsht_plan* p, int w, const unsigned char* WS, const int* EB,
                            const unsigned char* lbuf, double* alm, int nmaps_total, int k0,
                            int kc, int accumulate, cudaStream_t s);
-// Split-precision synthesis of one chunk into W = {G_N, G_S}: prepare cuts alm into digit
-// tiles WS / exponents EB (and clears W when l-chunks will add into it); per wave, lambdaT
-// writes ring-row lambda tiles and synth contracts them with WS.
-int fsht_launch_split_synth_prepare(fsht_plan* p, const double* alm, unsigned char* WS, int* EB,
-                                    double2* W, int nmaps_total, int k0, int kc, cudaStream_t s);
+// Split-precision synthesis of one chunk into W = {G_N, G_S}: clear W when l-chunks will
+// add into it; per wave: slice_alm cuts alm into digit tiles WS / exponents EB, lambdaT
+// writes ring-row lambda tiles, synth contracts them.
+int fsht_split_clear_w(fsht_plan* p, double2* W, int kc, cudaStream_t s);
+int fsht_launch_split_slice_alm(fsht_plan* p, int w, const double* alm, unsigned char* WS,
+                                int* EB, int nmaps_total, int k0, int kc, cudaStream_t s);
 int fsht_launch_split_lambdaT(fsht_plan* p, int w, unsigned char* lbuf, cudaStream_t s);
 // Split-precision spin-2 analysis: lambda1/lambda2 digit tiles per wave, then the E/B
 // contraction (which: bit0 E, bit1 B) against the Q and U digit tiles of k_slice_phase.

@@ -36,50 +36,52 @@ namespace {
 // WS tile (m, p, g, t, digit): 128 columns x 16 rings, core matrices (8 cols x 8
 // rings, 128 B) at (c/8)*256 + (k/8)*128.  Rings beyond the kept range are zero.
 struct SliceArgs {
-  const double2* W;
-  int kc, nnorth, ngroups;
-  size_t row_bytes;      // WS bytes per (m, parity, group)
+  const double* W;       // {S, D} as doubles: [m][ring][map][S|D][Re|Im]
+  int kc, nnorth, ngroups, q0, lmax;
+  size_t row_bytes;      // WS bytes per (wave-local q, parity, group)
   const int* ring_i0;
   unsigned char* WS;
   int* EB;
 };
 
-__global__ void __launch_bounds__(128) k_slice_phase(SliceArgs a) {
-  const int m = blockIdx.x, p = blockIdx.y, g = blockIdx.z;
-  const int c = threadIdx.x;
-  const int k = g * kGroupMaps + (c & 63);
-  const int comp = c >> 6;
+// grid (q in wave, group), 256 threads = (map, parity, Re/Im) with Re/Im fastest, so a warp
+// reads 8 maps' whole 32-byte {S, D} entries of one ring: every W sector is read once per
+// pass (two passes: the column maximum, then the digits).
+__global__ void __launch_bounds__(256) k_slice_phase(SliceArgs a) {
+  const int qi = blockIdx.x, g = blockIdx.y;
+  const int m = m_of_q(a.q0 + qi, a.lmax);
+  const int t = threadIdx.x;
+  const int comp = t & 1, p = (t >> 1) & 1, kl = t >> 2;
+  const int k = g * kGroupMaps + kl;
+  const int c = comp * kGroupMaps + kl;
   const int i0 = a.ring_i0[m];
   const int K = a.nnorth - i0;
   const bool valid = k < a.kc;
-  auto val = [&](int r) -> double {
-    if (!valid || r >= K) return 0.0;
-    const double2 w = a.W[(((long long)m * a.nnorth + i0 + r) * a.kc + k) * 2 + p];
-    return comp ? w.y : w.x;
-  };
+  const double* col = a.W + ((((long long)m * a.nnorth + i0) * a.kc + k) * 2 + p) * 2 + comp;
+  const long long rstride = (long long)a.kc * 4;
+  auto val = [&](int r) -> double { return (valid && r < K) ? col[r * rstride] : 0.0; };
   double mx = 0.0;
   for (int r = 0; r < K; ++r) mx = fmax(mx, fabs(val(r)));
   const int E = (mx > 0.0) ? ilogb(mx) + 1 : kEmptyExp;
-  a.EB[(((long long)m * 2 + p) * a.ngroups + g) * kCols + c] = E;
+  a.EB[(((long long)qi * 2 + p) * a.ngroups + g) * kCols + c] = E;
   const int nks = (K + kKStep - 1) / kKStep;
-  unsigned char* base =
-      a.WS + ((size_t)(m * 2 + p) * a.ngroups + g) * a.row_bytes;
-  for (int t = 0; t < nks; ++t) {
+  unsigned char* base = a.WS + ((size_t)(qi * 2 + p) * a.ngroups + g) * a.row_bytes +
+                        (c >> 3) * 256 + (c & 7) * 16;
+  for (int ts = 0; ts < nks; ++ts) {
     for (int half = 0; half < 2; ++half) {
-      uint16_t s[kSlices][8];
+      uint16_t sl[kSlices][8];
       for (int j = 0; j < 8; ++j) {
-        uint16_t q[4] = {0, 0, 0, 0};
-        if (E != kEmptyExp) tc::digits4(val(t * kKStep + half * 8 + j), E, q);
-        for (int sl = 0; sl < kSlices; ++sl) s[sl][j] = q[sl];
+        uint16_t q4[4] = {0, 0, 0, 0};
+        if (E != kEmptyExp) tc::digits4(val(ts * kKStep + half * 8 + j), E, q4);
+        for (int d = 0; d < kSlices; ++d) sl[d][j] = q4[d];
       }
-      for (int sl = 0; sl < kSlices; ++sl) {
+      for (int d = 0; d < kSlices; ++d) {
         uint4 pk;
-        pk.x = s[sl][0] | ((uint32_t)s[sl][1] << 16);
-        pk.y = s[sl][2] | ((uint32_t)s[sl][3] << 16);
-        pk.z = s[sl][4] | ((uint32_t)s[sl][5] << 16);
-        pk.w = s[sl][6] | ((uint32_t)s[sl][7] << 16);
-        unsigned char* tile = base + ((size_t)t * kSlices + sl) * kBTileBytes;
-        *reinterpret_cast<uint4*>(tile + (c >> 3) * 256 + half * 128 + (c & 7) * 16) = pk;
+        pk.x = sl[d][0] | ((uint32_t)sl[d][1] << 16);
+        pk.y = sl[d][2] | ((uint32_t)sl[d][3] << 16);
+        pk.z = sl[d][4] | ((uint32_t)sl[d][5] << 16);
+        pk.w = sl[d][6] | ((uint32_t)sl[d][7] << 16);
+        *reinterpret_cast<uint4*>(base + ((size_t)ts * kSlices + d) * kBTileBytes + half * 128) = pk;
       }
     }
   }
@@ -316,7 +318,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_split_gemm(GemmArgs a) {
     tc::mbar_fence_init();
   }
   if (tid < kCols) {
-    const int eb = a.EB[(((long long)m * 2 + p) * a.ngroups + g) * kCols + tid];
+    const int eb = a.EB[(((long long)blockIdx.z * 2 + p) * a.ngroups + g) * kCols + tid];
     s_cs[tid] = (eb == kEmptyExp) ? 0.0 : ldexp(a.pa, eb - 12);
     const int l = lt0 + p + 2 * tid;
     if (l <= a.lmax) {
@@ -338,7 +340,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_split_gemm(GemmArgs a) {
         a.lbuf + (size_t)(a.lam_off[q] - a.lam_off[a.q0]) * kSlices * kATileBytes +
         ((size_t)(p * ntiles + t) * nks + ks0) * kSlices * kATileBytes;
     const unsigned char* bsrc =
-        a.WS + (((size_t)m * 2 + p) * a.ngroups + g) * a.row_bytes +
+        a.WS + (((size_t)blockIdx.z * 2 + p) * a.ngroups + g) * a.row_bytes +
         (size_t)ks0 * kSlices * kBTileBytes;
     for (int i = 0; i < nk; ++i) {
       const uint32_t st = i % kStagesG;
@@ -540,14 +542,15 @@ __global__ void __launch_bounds__(128) k_lambda_digits_T(LamTArgs a) {
 // Re/Im = c >> 6).  Tile (m, p, g, l-step): 128 columns x 16 l, K-major.
 struct SliceAArgs {
   const double* alm;
-  int ld, k0, kc, lmax, ngroups;
+  int ld, k0, kc, lmax, ngroups, q0;
   size_t row_bytes;
   unsigned char* WS;
   int* EB;
 };
 
 __global__ void __launch_bounds__(128) k_slice_alm(SliceAArgs a) {
-  const int m = blockIdx.x, p = blockIdx.y, g = blockIdx.z;
+  const int qi = blockIdx.x, p = blockIdx.y, g = blockIdx.z;
+  const int m = m_of_q(a.q0 + qi, a.lmax);
   const int c = threadIdx.x;
   const int k = g * kGroupMaps + (c & 63);
   const int comp = c >> 6;
@@ -564,10 +567,10 @@ __global__ void __launch_bounds__(128) k_slice_alm(SliceAArgs a) {
   double mx = 0.0;
   for (int idx = 0; idx < cnt; ++idx) mx = fmax(mx, fabs(val(idx)));
   const int E = (mx > 0.0) ? ilogb(mx) + 1 : kEmptyExp;
-  a.EB[(((long long)m * 2 + p) * a.ngroups + g) * kCols + c] = E;
+  a.EB[(((long long)qi * 2 + p) * a.ngroups + g) * kCols + c] = E;
   const int nkl = (cnt0 + kKStep - 1) / kKStep;
   unsigned char* base = a.WS +
-                        ((size_t)(m * 2 + p) * a.ngroups + g) * a.row_bytes +
+                        ((size_t)(qi * 2 + p) * a.ngroups + g) * a.row_bytes +
                         (c >> 3) * 256 + (c & 7) * 16;
   for (int kl = 0; kl < nkl; ++kl) {
     for (int half = 0; half < 2; ++half) {
@@ -651,7 +654,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_split_synth(SynthArgs a) {
   }
   if (tid < kCols) {
     for (int pp = 0; pp < 2; ++pp) {
-      const int eb = a.EB[(((long long)m * 2 + pp) * a.ngroups + g) * kCols + tid];
+      const int eb = a.EB[(((long long)blockIdx.z * 2 + pp) * a.ngroups + g) * kCols + tid];
       s_cs[pp][tid] = (eb == kEmptyExp) ? 0.0 : ldexp(1.0, a.eag + eb - 12);
     }
   }
@@ -672,7 +675,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_split_synth(SynthArgs a) {
       unsigned char* dst = smem + st * kStageBytesS;
       const unsigned char* asrc =
           abase + ((size_t)(par * nrb + rb) * nkl + kk) * kSlices * kATileBytes;
-      const unsigned char* bsrc = a.WS + (((size_t)m * 2 + par) * a.ngroups + g) * a.row_bytes +
+      const unsigned char* bsrc = a.WS + (((size_t)blockIdx.z * 2 + par) * a.ngroups + g) * a.row_bytes +
                                   (size_t)kk * kSynthBBytes;
       tc::mbar_arrive_expect_tx(&h.full[st], kStageBytesS);
       tc::bulk_g2s(dst, asrc, kSlices * kATileBytes, &h.full[st]);
@@ -782,37 +785,44 @@ __global__ void __launch_bounds__(kThreads, 1) k_split_synth(SynthArgs a) {
 }  // namespace
 
 
-size_t fsht_split_ws_bytes(int lmax, int nnorth, int kc) {
+// WS and EB hold one wave of m (the wave with the most orders).
+size_t fsht_split_ws_bytes(const fsht_plan* p, int kc) {
   const int ngroups = (kc + kGroupMaps - 1) / kGroupMaps;
-  return (size_t)(lmax + 1) * 2 * ngroups * ws_row_bytes(lmax, nnorth);
+  return (size_t)p->wave_qmax * 2 * ngroups * ws_row_bytes(p->lmax, p->nnorth);
 }
-size_t fsht_split_eb_bytes(int lmax, int kc) {
+size_t fsht_split_eb_bytes(const fsht_plan* p, int kc) {
   const int ngroups = (kc + kGroupMaps - 1) / kGroupMaps;
-  return (size_t)(lmax + 1) * 2 * ngroups * kCols * sizeof(int);
+  return (size_t)p->wave_qmax * 2 * ngroups * kCols * sizeof(int);
 }
 
-int fsht_launch_split_prepare(fsht_plan* p, const double2* W, unsigned char* WS, int* EB,
-                              double* alm, int nmaps_total, int k0, int kc, int accumulate,
-                              cudaStream_t s) {
-  const int ngroups = (kc + kGroupMaps - 1) / kGroupMaps;
+int fsht_split_clear_alm(fsht_plan* p, double* alm, int nmaps_total, int k0, int kc,
+                         cudaStream_t s) {
   const int nkc = (p->nnorth + kKChunk - 1) / kKChunk;
-  SliceArgs sa;
-  sa.W = W;
-  sa.kc = kc;
-  sa.nnorth = p->nnorth;
-  sa.ngroups = ngroups;
-  sa.row_bytes = ws_row_bytes(p->lmax, p->nnorth);
-  sa.ring_i0 = p->d_ring_i0;
-  sa.WS = WS;
-  sa.EB = EB;
-  k_slice_phase<<<dim3(p->lmax + 1, 2, ngroups), 128, 0, s>>>(sa);
-  FSHT_LAUNCH_CHECK();
-  if (nkc > 1 && !accumulate && alm) {
+  if (nkc > 1 && alm) {
     // K-chunks add into alm: clear this chunk's columns first
     const size_t L1 = (size_t)p->lmax + 1;
     FSHT_CUDA_TRY(cudaMemset2DAsync(alm + k0, sizeof(double) * nmaps_total, 0,
                                     sizeof(double) * kc, L1 * L1, s));
   }
+  return FSHT_OK;
+}
+
+int fsht_launch_split_slice(fsht_plan* p, int w, const double2* W, unsigned char* WS, int* EB,
+                            int kc, cudaStream_t s) {
+  const int* wv = p->h_waves + kWaveInts * w;
+  SliceArgs sa;
+  sa.W = reinterpret_cast<const double*>(W);
+  sa.kc = kc;
+  sa.nnorth = p->nnorth;
+  sa.ngroups = (kc + kGroupMaps - 1) / kGroupMaps;
+  sa.q0 = wv[0];
+  sa.lmax = p->lmax;
+  sa.row_bytes = ws_row_bytes(p->lmax, p->nnorth);
+  sa.ring_i0 = p->d_ring_i0;
+  sa.WS = WS;
+  sa.EB = EB;
+  k_slice_phase<<<dim3(wv[1] - wv[0], sa.ngroups), 256, 0, s>>>(sa);
+  FSHT_LAUNCH_CHECK();
   return FSHT_OK;
 }
 
@@ -871,6 +881,7 @@ int fsht_split_tables_init(fsht_plan* p) {
     }
     waves.insert(waves.end(), wv, wv + kWaveInts);
     lbuf_units = std::max(lbuf_units, span(q0, q1));
+    p->wave_qmax = std::max(p->wave_qmax, q1 - q0);
     q0 = q1;
   }
   p->nwaves = (int)waves.size() / kWaveInts;
@@ -943,8 +954,19 @@ int fsht_launch_split_gemm(fsht_plan* p, int w, const unsigned char* WS, const i
   return FSHT_OK;
 }
 
-int fsht_launch_split_synth_prepare(fsht_plan* p, const double* alm, unsigned char* WS, int* EB,
-                                    double2* W, int nmaps_total, int k0, int kc, cudaStream_t s) {
+int fsht_split_clear_w(fsht_plan* p, double2* W, int kc, cudaStream_t s) {
+  const int nkl0 = (p->lmax / 2 + 1 + kKStep - 1) / kKStep;
+  if (nkl0 * kKStep > kKChunk) {
+    // l-chunks add into W: clear it first
+    FSHT_CUDA_TRY(cudaMemsetAsync(W, 0, sizeof(double2) * 2 * (size_t)(p->lmax + 1) * p->nnorth * kc,
+                                  s));
+  }
+  return FSHT_OK;
+}
+
+int fsht_launch_split_slice_alm(fsht_plan* p, int w, const double* alm, unsigned char* WS,
+                                int* EB, int nmaps_total, int k0, int kc, cudaStream_t s) {
+  const int* wv = p->h_waves + kWaveInts * w;
   SliceAArgs a;
   a.alm = alm;
   a.ld = nmaps_total;
@@ -952,17 +974,12 @@ int fsht_launch_split_synth_prepare(fsht_plan* p, const double* alm, unsigned ch
   a.kc = kc;
   a.lmax = p->lmax;
   a.ngroups = (kc + kGroupMaps - 1) / kGroupMaps;
+  a.q0 = wv[0];
   a.row_bytes = ws_row_bytes(p->lmax, p->nnorth);
   a.WS = WS;
   a.EB = EB;
-  k_slice_alm<<<dim3(p->lmax + 1, 2, a.ngroups), 128, 0, s>>>(a);
+  k_slice_alm<<<dim3(wv[1] - wv[0], 2, a.ngroups), 128, 0, s>>>(a);
   FSHT_LAUNCH_CHECK();
-  const int nkl0 = (p->lmax / 2 + 1 + kKStep - 1) / kKStep;
-  if (nkl0 * kKStep > kKChunk) {
-    // l-chunks add into W: clear it first
-    FSHT_CUDA_TRY(cudaMemsetAsync(W, 0, sizeof(double2) * 2 * (size_t)(p->lmax + 1) * p->nnorth * kc,
-                                  s));
-  }
   return FSHT_OK;
 }
 

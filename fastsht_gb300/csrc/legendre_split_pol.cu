@@ -276,7 +276,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_split_gemm_pol(GemmPArgs a) {
   }
   if (tid < kCols) {
     for (int part = 0; part < 2; ++part) {
-      const int e = eb[part][(((long long)m * 2 + bpar[part]) * a.ngroups + g) * kCols + tid];
+      const int e = eb[part][(((long long)blockIdx.z * 2 + bpar[part]) * a.ngroups + g) * kCols + tid];
       s_cs[part][tid] = (e == kEmptyExp) ? 0.0 : ldexp(-a.pa, e - 12);
     }
     const int l = lt0 + p + 2 * tid;
@@ -305,7 +305,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_split_gemm_pol(GemmPArgs a) {
       const unsigned char* asrc =
           lam + (((size_t)(p * ntiles + t) * 2 + part) * nks + ks) * kSlices * kATileBytes;
       const unsigned char* bsrc =
-          ws[part] + (((size_t)m * 2 + bpar[part]) * a.ngroups + g) * a.row_bytes +
+          ws[part] + (((size_t)blockIdx.z * 2 + bpar[part]) * a.ngroups + g) * a.row_bytes +
           (size_t)ks * kSlices * kBTileBytes;
       tc::mbar_arrive_expect_tx(&h.full[st], kStageBytesP);
       tc::bulk_g2s(dst, asrc, kSlices * kATileBytes, &h.full[st]);

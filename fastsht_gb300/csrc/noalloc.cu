@@ -93,6 +93,8 @@ __global__ void k_noalloc_tables(int nside, int lmax, double* cth, double* sth, 
     for (int i = 0; i < nn; ++i) {
       FshtRingFFT r;
       r.n = ring_len(nside, i);
+      r.nd = r.n;
+      r.rtw_off = 0;
       fsht_ring_fft_size(r);
       r.chirp_off = 0;
       r.bhat_off = 0;
@@ -149,6 +151,11 @@ extern "C" int fsht_t2alm_noalloc(int nside, int lmax, const double* maps, doubl
   FshtFftLayout f;
   int rc = fsht_fft_layout(nside, lmax, &f, nullptr, nullptr);
   if (rc) return rc;
+  if (f.nhalf > 0) {
+    fsht_set_error("t2alm_noalloc: nside %d needs half-length ring transforms; use fsht_t2alm",
+                   nside);
+    return FSHT_EUNSUPPORTED;
+  }
   const ScratchLayout L = layout_for(nside, lmax, f);
   const size_t per_map = (size_t)(lmax + 1) * 2 * nside * 2 * sizeof(double2);
   if (L.work + per_map > kNoAllocScratchBytes) {

@@ -18,7 +18,7 @@
 namespace {
 thread_local std::string g_last_error;
 constexpr size_t kDefaultWorkspace = 16ull << 30;
-constexpr size_t kDefaultWorkspaceSplit = 40ull << 30;   // 128-map groups at nside 1024
+constexpr size_t kDefaultWorkspaceSplit = 80ull << 30;   // 500 maps at nside 1024 in one chunk
 }  // namespace
 
 // Per-kernel event timing (enabled by fsht_profile_enable).
@@ -80,6 +80,7 @@ void free_plan_memory(fsht_plan* p) {
   cudaFree(p->d_ring_i0);
   cudaFree(p->d_rfft);
   cudaFree(p->d_chirp);
+  cudaFree(p->d_rtw);
   cudaFree(p->d_bhat);
   cudaFree(p->d_tw);
   cudaFree(p->d_work);
@@ -187,9 +188,9 @@ int fsht_plan_create(int nside, int lmax, int nmaps_max, int flags, int precisio
     return FSHT_EINVAL;
   }
   *out = nullptr;
-  if (nside < 1 || nside > 1024 || (nside & (nside - 1))) {
-    fsht_set_error("nside = %d: must be a power of two in [1, 1024]", nside);
-    return nside > 1024 && !(nside & (nside - 1)) ? FSHT_EUNSUPPORTED : FSHT_EINVAL;
+  if (nside < 1 || nside > 2048 || (nside & (nside - 1))) {
+    fsht_set_error("nside = %d: must be a power of two in [1, 2048]", nside);
+    return nside > 2048 && !(nside & (nside - 1)) ? FSHT_EUNSUPPORTED : FSHT_EINVAL;
   }
   if (lmax < 0 || lmax > 4 * nside) {
     fsht_set_error("lmax = %d outside [0, 4*nside = %d]", lmax, 4 * nside);
@@ -283,8 +284,7 @@ int fsht_plan_create(int nside, int lmax, int nmaps_max, int flags, int precisio
   auto need = [&](size_t k) -> size_t {
     size_t b = per_map * k;
     if (precision == FSHT_PREC_SPLIT)   // spin 2: digit tiles of Q and U
-      b += (p->pol ? 2 : 1) * (fsht_split_ws_bytes(lmax, p->nnorth, (int)k) +
-                               fsht_split_eb_bytes(lmax, (int)k)) +
+      b += (p->pol ? 2 : 1) * (fsht_split_ws_bytes(p, (int)k) + fsht_split_eb_bytes(p, (int)k)) +
            p->lbuf_bytes;
     return b;
   };
@@ -305,9 +305,9 @@ int fsht_plan_create(int nside, int lmax, int nmaps_max, int flags, int precisio
   }
   if (precision == FSHT_PREC_SPLIT && !tables_only) {
     const size_t f = p->pol ? 2 : 1;
-    p->ws_bytes = f * fsht_split_ws_bytes(lmax, p->nnorth, p->kchunk);
+    p->ws_bytes = f * fsht_split_ws_bytes(p, p->kchunk);
     if ((rc = dalloc((void**)&p->d_ws, p->ws_bytes))) return fail(rc);
-    if ((rc = dalloc((void**)&p->d_eb, f * fsht_split_eb_bytes(lmax, p->kchunk)))) return fail(rc);
+    if ((rc = dalloc((void**)&p->d_eb, f * fsht_split_eb_bytes(p, p->kchunk)))) return fail(rc);
     if ((rc = dalloc((void**)&p->d_lbuf, p->lbuf_bytes))) return fail(rc);
   }
   if ((ce = cudaStreamSynchronize(p->stream)) != cudaSuccess) {
@@ -418,12 +418,12 @@ int fsht_plan_sync(fsht_plan* p) {
 // accumulate), and synthesis of alm into W = {G_N, G_S}.
 static int split_analysis(fsht_plan* p, const double2* W, double* alm, int nmaps, int c0, int kc,
                           int accumulate) {
-  {
-    FSHT_PROF(FSHT_KCAT_SLICE);
-    FSHT_TRY(fsht_launch_split_prepare(p, W, p->d_ws, p->d_eb, alm, nmaps, c0, kc, accumulate,
-                                       p->stream));
-  }
+  if (!accumulate) FSHT_TRY(fsht_split_clear_alm(p, alm, nmaps, c0, kc, p->stream));
   for (int w = 0; w < p->nwaves; ++w) {
+    {
+      FSHT_PROF(FSHT_KCAT_SLICE);
+      FSHT_TRY(fsht_launch_split_slice(p, w, W, p->d_ws, p->d_eb, kc, p->stream));
+    }
     {
       FSHT_PROF(FSHT_KCAT_LAMBDA);
       FSHT_TRY(fsht_launch_split_lambda(p, w, p->d_lbuf, p->stream));
@@ -439,12 +439,13 @@ static int split_analysis(fsht_plan* p, const double2* W, double* alm, int nmaps
 
 static int split_synthesis(fsht_plan* p, const double* alm, double2* W, int nmaps, int c0,
                            int kc) {
-  {
-    FSHT_PROF(FSHT_KCAT_SLICE);
-    FSHT_TRY(fsht_launch_split_synth_prepare(p, alm, p->d_ws, p->d_eb, W, nmaps, c0, kc,
-                                             p->stream));
-  }
+  FSHT_TRY(fsht_split_clear_w(p, W, kc, p->stream));
   for (int w = 0; w < p->nwaves; ++w) {
+    {
+      FSHT_PROF(FSHT_KCAT_SLICE);
+      FSHT_TRY(fsht_launch_split_slice_alm(p, w, alm, p->d_ws, p->d_eb, nmaps, c0, kc,
+                                           p->stream));
+    }
     {
       FSHT_PROF(FSHT_KCAT_LAMBDA);
       FSHT_TRY(fsht_launch_split_lambdaT(p, w, p->d_lbuf, p->stream));
@@ -587,17 +588,19 @@ static int pol_analysis(fsht_plan* p, const double2* WQ, const double2* WU, doub
     return FSHT_EUNSUPPORTED;
   }
   unsigned char* wsq = p->d_ws;
-  unsigned char* wsu = p->d_ws + fsht_split_ws_bytes(p->lmax, p->nnorth, kc);
+  unsigned char* wsu = p->d_ws + fsht_split_ws_bytes(p, kc);
   int* ebq = p->d_eb;
-  int* ebu = p->d_eb + fsht_split_eb_bytes(p->lmax, kc) / sizeof(int);
-  {
-    FSHT_PROF(FSHT_KCAT_SLICE);
-    FSHT_TRY(fsht_launch_split_prepare(p, WQ, wsq, ebq, (which & 1) ? almE : nullptr, nmaps, c0,
-                                       kc, accumulate, p->stream));
-    FSHT_TRY(fsht_launch_split_prepare(p, WU, wsu, ebu, (which & 2) ? almB : nullptr, nmaps, c0,
-                                       kc, accumulate, p->stream));
+  int* ebu = p->d_eb + fsht_split_eb_bytes(p, kc) / sizeof(int);
+  if (!accumulate) {
+    if (which & 1) FSHT_TRY(fsht_split_clear_alm(p, almE, nmaps, c0, kc, p->stream));
+    if (which & 2) FSHT_TRY(fsht_split_clear_alm(p, almB, nmaps, c0, kc, p->stream));
   }
   for (int w = 0; w < p->nwaves; ++w) {
+    {
+      FSHT_PROF(FSHT_KCAT_SLICE);
+      FSHT_TRY(fsht_launch_split_slice(p, w, WQ, wsq, ebq, kc, p->stream));
+      FSHT_TRY(fsht_launch_split_slice(p, w, WU, wsu, ebu, kc, p->stream));
+    }
     {
       FSHT_PROF(FSHT_KCAT_LAMBDA);
       FSHT_TRY(fsht_launch_split_lambda_pol(p, w, p->d_lbuf, p->stream));

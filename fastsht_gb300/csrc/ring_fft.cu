@@ -158,7 +158,7 @@ __device__ __forceinline__ int dft_bin(const FshtRingFFT& rf, int q) {
   return rf.bluestein ? q : (int)(__brev((unsigned)q) >> (32 - rf.logT));
 }
 
-// DFT of n points (in buf[0..n)), forward (e^{-2 pi i jk/n}); bin q lands at
+// DFT of rf.nd points (in buf[0..nd)), forward (e^{-2 pi i jk/nd}); bin q lands at
 // buf[dft_bin(rf, q)].  A power-of-two ring is one fft_dif; any other length uses
 // Bluestein with the ring's chirp and filter spectrum (transform order, divided by P):
 // chirp, fft_dif, filter, fft_dit_inv, chirp, natural order out.
@@ -169,7 +169,7 @@ __device__ void ring_dft(double2* buf, const FshtRingFFT& rf, const FftTw& tw,
     fft_dif(buf, rf, tw);
     return;
   }
-  const int n = rf.n, P = rf.P;
+  const int n = rf.nd, P = rf.P;
   for (int j = tid; j < P; j += nt) {
     if (j < n) buf[j] = cmul(buf[j], __ldg(&chirp[j]));
     else buf[j] = make_double2(0.0, 0.0);
@@ -195,13 +195,20 @@ __global__ void k_twiddles(double2* tw, int Tmax, int P3max) {
   }
 }
 
-// chirp w_j = exp(-i pi j^2 / n) and the filter spectrum (fft_dif of the wrapped conj
-// chirp, over P) for one ring; block per Bluestein ring.
+// chirp w_j = exp(-i pi j^2 / nd) and the filter spectrum (fft_dif of the wrapped conj
+// chirp, over P) for one ring, and a half-length ring's twiddles; block per Bluestein ring.
 __global__ void k_bluestein_tables(const FshtRingFFT* rfs, const int* rings, double2* chirp,
-                                   double2* bhat, FftTw tw) {
+                                   double2* bhat, double2* rtw, FftTw tw) {
   extern __shared__ double2 sbuf[];
   const FshtRingFFT rf = rfs[rings[blockIdx.x]];
-  const int n = rf.n, P = rf.P;
+  const int n = rf.nd, P = rf.P;
+  if (rf.nd != rf.n) {     // half-length ring: exp(-2 pi i k / n_ring), k <= nd
+    for (int k = threadIdx.x; k <= n; k += blockDim.x) {
+      double s, c;
+      sincospi(-2.0 * (double)k / (double)rf.n, &s, &c);
+      rtw[rf.rtw_off + k] = make_double2(c, s);
+    }
+  }
   double2* w = chirp + rf.chirp_off;
   for (int j = threadIdx.x; j < n; j += blockDim.x) {
     long long r = ((long long)j * j) % (2LL * n);
@@ -232,6 +239,7 @@ struct FwdArgs {
   FftTw tw;
   const double2* chirp;
   const double2* bhat;
+  const double2* rtw;
   const int* ring_i0;
   double2* W;
 };
@@ -264,6 +272,47 @@ __global__ void __launch_bounds__(512) k_ring_fft_fwd(FwdArgs a) {
   const int k_end = min(a.kc, k_begin + a.maps_per_block);
   const double2* chirp = a.chirp + rf.chirp_off;
   const double2* bhat = a.bhat + rf.bhat_off;
+  if (rf.nd != n) {
+    // Half-length ring (a cap ring whose packed transform exceeds shared memory; never the
+    // equator): each of the two rings as z_j = x_{2j} + i x_{2j+1}, Z = DFT_nd(z); then
+    // X_q = E_q + e^{-2 pi i q/n} O_q with E = (Z_q + conj Z_{nd-q})/2, O = (Z_q - conj
+    // Z_{nd-q})/(2i).  The north ring writes {S, D} = {F_N, F_N}, the south ring adds +-F_S
+    // (the same thread owns each m in both passes).
+    const int nd = rf.nd;
+    const double2* rtw = a.rtw + rf.rtw_off;
+    for (int k = k_begin; k < k_end; ++k) {
+      for (int side = 0; side < 2; ++side) {
+        const double* x = a.maps + (long long)k * a.map_stride + (side ? off_s : off_n);
+        __syncthreads();
+        for (int j = tid; j < nd; j += nt)
+          buf[j] = make_double2(__ldg(&x[2 * j]), __ldg(&x[2 * j + 1]));
+        __syncthreads();
+        ring_dft(buf, rf, a.tw, chirp, bhat);
+        for (int m = tid; m <= mtop; m += nt) {
+          const int q = m % n;
+          const bool cj = q > nd;
+          const int kk = cj ? n - q : q;
+          const double2 za = buf[dft_bin(rf, kk == nd ? 0 : kk)];
+          const double2 zb = cconj(buf[dft_bin(rf, kk == 0 ? 0 : nd - kk)]);
+          const double2 e = cscale(cadd(za, zb), 0.5);
+          const double2 dd = csub(za, zb);
+          const double2 o = make_double2(0.5 * dd.y, -0.5 * dd.x);
+          double2 xq = cadd(e, cmul(__ldg(&rtw[kk]), o));
+          if (cj) xq = cconj(xq);
+          const double2 f = cmul(ph[m], xq);
+          double2* w = a.W + (((long long)m * a.nnorth + i) * a.kc + k) * 2;
+          if (side == 0) {
+            w[0] = f;
+            w[1] = f;
+          } else {
+            w[0] = cadd(w[0], f);
+            w[1] = csub(w[1], f);
+          }
+        }
+      }
+    }
+    return;
+  }
   for (int k = k_begin; k < k_end; ++k) {
     const double* xn = a.maps + (long long)k * a.map_stride + off_n;
     const double* xs = a.maps + (long long)k * a.map_stride + off_s;
@@ -307,6 +356,7 @@ struct InvArgs {
   FftTw tw;
   const double2* chirp;
   const double2* bhat;
+  const double2* rtw;
   const int* ring_i0;
 };
 
@@ -334,6 +384,24 @@ __device__ void build_spectrum(double2* buf, const double2* ph, const double2* _
     }
     buf[q] = make_double2(yN.x - yS.y, yN.y + yS.x);   // Y_N + i Y_S
   }
+}
+
+// Bin q of one ring's Hermitian spectrum (side 0: north from G_N, side 1: south from G_S),
+// the aliased sum build_spectrum forms for both rings at once.
+__device__ __forceinline__ double2 spectrum_bin(const double2* ph, const double2* __restrict__ W,
+                                                long long stride_m, int n, int mtop, int side,
+                                                int q) {
+  double2 y = make_double2(0.0, 0.0);
+  for (int m = q; m <= mtop; m += n) {
+    const double c = (m == 0) ? 0.5 : 1.0;
+    y = cadd(y, cscale(cmul(ph[m], W[(long long)m * stride_m + side]), c));
+  }
+  const int q2 = (q == 0) ? 0 : n - q;
+  for (int m = q2; m <= mtop; m += n) {
+    const double c = (m == 0) ? 0.5 : 1.0;
+    y = cadd(y, cscale(cconj(cmul(ph[m], W[(long long)m * stride_m + side])), c));
+  }
+  return y;
 }
 
 __global__ void __launch_bounds__(512) k_ring_fft_inv(InvArgs a) {
@@ -364,6 +432,34 @@ __global__ void __launch_bounds__(512) k_ring_fft_inv(InvArgs a) {
   const double2* chirp = a.chirp + rf.chirp_off;
   const double2* bhat = a.bhat + rf.bhat_off;
   const long long stride_m = (long long)a.nnorth * a.kc * 2;
+  if (rf.nd != n) {
+    // Half-length ring: x_{2j} + i x_{2j+1} = sum_k Z_k e^{2 pi i jk/nd} with
+    // Z_k = (Y_k + Y_{k+nd}) + i (Y_k - Y_{k+nd}) e^{2 pi i k/n}, one ring at a time.
+    const int nd = rf.nd;
+    const double2* rtw = a.rtw + rf.rtw_off;
+    for (int k = k_begin; k < k_end; ++k) {
+      const double2* Wk = a.W + ((long long)i * a.kc + k) * 2;
+      for (int side = 0; side < 2; ++side) {
+        __syncthreads();
+        for (int kk = tid; kk < nd; kk += nt) {
+          const double2 y0 = spectrum_bin(ph, Wk, stride_m, n, mtop, side, kk);
+          const double2 y1 = spectrum_bin(ph, Wk, stride_m, n, mtop, side, kk + nd);
+          const double2 b = cmul(csub(y0, y1), cconj(__ldg(&rtw[kk])));
+          const double2 sa = cadd(y0, y1);
+          buf[kk] = cconj(make_double2(sa.x - b.y, sa.y + b.x));   // conj(A + i B)
+        }
+        __syncthreads();
+        ring_dft(buf, rf, a.tw, chirp, bhat);
+        double* x = a.maps + (long long)k * a.map_stride + (side ? off_s : off_n);
+        for (int j = tid; j < nd; j += nt) {
+          const double2 z = buf[dft_bin(rf, j)];   // conj(z): x_{2j} = Re, x_{2j+1} = -Im
+          x[2 * j] = z.x;
+          x[2 * j + 1] = -z.y;
+        }
+      }
+    }
+    return;
+  }
   for (int k = k_begin; k < k_end; ++k) {
     __syncthreads();
     build_spectrum(buf, ph, a.W + ((long long)i * a.kc + k) * 2, stride_m, n, mtop, equator);
@@ -538,16 +634,26 @@ int maps_per_block_for(int kc, int nrings_launched) {
 // ================================================================== host side
 int fsht_fft_layout(int nside, int lmax, FshtFftLayout* lay, FshtRingFFT* rfs, int* blue_rings) {
   const int nn = 2 * nside;
-  long long chirp_total = 0, bhat_total = 0;
-  int Pmax = 4, logTmax = 2, P3max = 0, nblue = 0;
+  const size_t smem_cap = 227 * 1024;
+  long long chirp_total = 0, bhat_total = 0, rtw_total = 0;
+  int Pmax = 4, logTmax = 2, P3max = 0, nblue = 0, nhalf = 0;
   for (int i = 0; i < nn; ++i) {
     FshtRingFFT r{};
     r.n = ring_len(nside, i);
+    r.nd = r.n;
     fsht_ring_fft_size(r);
+    if (r.bluestein && (size_t)(r.P + lmax + 1) * sizeof(double2) > smem_cap) {
+      // the packed N + iS transform does not fit: transform each ring at half length
+      r.nd = r.n / 2;
+      fsht_ring_fft_size(r);
+      r.rtw_off = rtw_total;
+      rtw_total += r.nd + 1;
+      ++nhalf;
+    }
     if (r.bluestein) {
       r.chirp_off = chirp_total;
       r.bhat_off = bhat_total;
-      chirp_total += r.n;
+      chirp_total += r.nd;
       bhat_total += r.P;
       if (blue_rings) blue_rings[nblue] = i;
       ++nblue;
@@ -563,10 +669,12 @@ int fsht_fft_layout(int nside, int lmax, FshtFftLayout* lay, FshtRingFFT* rfs, i
   lay->P3max = P3max;
   lay->chirp_total = chirp_total;
   lay->bhat_total = bhat_total;
+  lay->rtw_total = rtw_total;
   lay->nblue = nblue;
+  lay->nhalf = nhalf;
   // The phase table (lmax+1) and the FFT buffer (Pmax) share the dynamic smem.
   lay->smem = (size_t)(Pmax + lmax + 1) * sizeof(double2);
-  if (lay->smem > 227 * 1024) {
+  if (lay->smem > smem_cap) {
     fsht_set_error("ring FFT needs %zu bytes of shared memory (nside %d, lmax %d): unsupported",
                    lay->smem, nside, lmax);
     return FSHT_EUNSUPPORTED;
@@ -594,7 +702,7 @@ int fsht_fft_tables_fill(fsht_plan* p, const int* d_blue_rings, int nblue, cudaS
     FSHT_CUDA_TRY(cudaFuncSetAttribute(k_bluestein_tables,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
     k_bluestein_tables<<<(unsigned)nblue, 512, sm, s>>>(p->d_rfft, d_blue_rings, p->d_chirp,
-                                                         p->d_bhat, plan_tw(p));
+                                                         p->d_bhat, p->d_rtw, plan_tw(p));
     FSHT_LAUNCH_CHECK();
   }
   return FSHT_OK;
@@ -618,6 +726,7 @@ int fsht_fft_tables_init(fsht_plan* p) {
   FSHT_CUDA_TRY(cudaMalloc(&p->d_tw, sizeof(double2) * (lay.Tmax + lay.P3max)));
   FSHT_CUDA_TRY(cudaMalloc(&p->d_chirp, sizeof(double2) * (lay.chirp_total > 0 ? lay.chirp_total : 1)));
   FSHT_CUDA_TRY(cudaMalloc(&p->d_bhat, sizeof(double2) * (lay.bhat_total > 0 ? lay.bhat_total : 1)));
+  FSHT_CUDA_TRY(cudaMalloc(&p->d_rtw, sizeof(double2) * (lay.rtw_total > 0 ? lay.rtw_total : 1)));
   int* d_rings = nullptr;
   if (lay.nblue > 0) {
     FSHT_CUDA_TRY(cudaMalloc(&d_rings, sizeof(int) * lay.nblue));
@@ -665,6 +774,7 @@ int fsht_launch_ring_fft_fwd(fsht_plan* p, const double* maps, long long map_str
   a.ring_base = 0;
   a.rfs = p->d_rfft;
   a.tw = plan_tw(p);
+  a.rtw = p->d_rtw;
   a.chirp = p->d_chirp;
   a.bhat = p->d_bhat;
   a.ring_i0 = p->d_ring_i0;
@@ -692,6 +802,7 @@ int fsht_launch_ring_fft_inv(fsht_plan* p, const double2* W, double* maps, long 
   a.ring_base = 0;
   a.rfs = p->d_rfft;
   a.tw = plan_tw(p);
+  a.rtw = p->d_rtw;
   a.chirp = p->d_chirp;
   a.bhat = p->d_bhat;
   a.ring_i0 = p->d_ring_i0;

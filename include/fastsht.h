@@ -48,7 +48,7 @@ enum { FSHT_FLAG_POL = 1, FSHT_FLAG_ITER = 2, FSHT_FLAG_TABLES_ONLY = 4 };
 /* Plan creation: replaces the reference's SHT.__init__ -> sht_data_alloc +
  * sht_set_data (SHT.py:17-62; src/sht_data_init.f90:2-269, 275-311).  Computes
  * the ring geometry, ring-skip table, FFT tables and workspace on the device.
- *   nside      power of two, 1..1024
+ *   nside      power of two, 1..2048
  *   lmax       0 <= lmax <= 4*nside
  *   nmaps_max  largest nmaps a transform call on this plan will pass
  *   flags      FSHT_FLAG_POL for spin-2 (Q/U) transforms, FSHT_FLAG_ITER for

@@ -44,7 +44,7 @@ def test_python_binding_covers_header(lib):
     ((8, 33, 1, 0, 0), _lib.FSHT_EINVAL),         # lmax > 4 nside
     ((8, -1, 1, 0, 0), _lib.FSHT_EINVAL),
     ((8, 16, 0, 0, 0), _lib.FSHT_EINVAL),         # nmaps_max < 1
-    ((2048, 100, 1, 0, 0), _lib.FSHT_EUNSUPPORTED),
+    ((4096, 100, 1, 0, 0), _lib.FSHT_EUNSUPPORTED),   # above nside 2048
     ((8, 16, 1, 0, 7), _lib.FSHT_EUNSUPPORTED),   # unknown precision
 ])
 def test_plan_create_rejects_bad_arguments(lib, args, code):

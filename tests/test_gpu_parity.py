@@ -219,3 +219,29 @@ def test_plans_of_different_sizes_coexist():
     small.t2alm(maps_normal(2, 1, 1))
     assert np.array_equal(big.t2alm(maps), a1)
     assert big.alm2t(a1).shape == (12 * 64 * 64, 2)
+
+
+def test_nside_2048_half_length_rings_match_oracle():
+    """nside 2048: cap rings longer than 4096 pixels are transformed at half length (each
+    ring's even/odd samples packed), forward and inverse; lmax 64 keeps the oracle quick."""
+    ns, lmax, nsim = 2048, 64, 1
+    sht = SHT(ns, lmax, nsim)
+    o = OracleSHT(ns, lmax, ring_tab=sht.ring_skip())
+    maps = maps_normal(ns, nsim, 2048)
+    assert rel_alm_err(sht.t2alm(maps), o.t2alm(maps)) <= TOL
+    alm = alm_powerlaw(lmax, nsim, 2049)
+    assert rel_map_err(sht.alm2t(alm), o.alm2t(alm)) <= TOL
+
+
+def test_nside_2048_lmax_4096_roundtrip_and_split():
+    """The serving configuration's largest size, nside 2048 / lmax 4096: the split form
+    against the plain path, and a synthesis -> analysis round trip of a band-limited map."""
+    ns, lmax, nsim = 2048, 4096, 1
+    alm = alm_powerlaw(lmax, nsim, 7, lmin=1)
+    sht = SHT(ns, lmax, nsim)
+    maps = sht.alm2t(alm)
+    a64 = sht.t2alm(maps)
+    a16 = SHT(ns, lmax, nsim, precision="split").t2alm(maps)
+    assert rel_alm_err(a16, a64) <= 1e-7
+    # niter = 0 quadrature error only (lmax = 2 nside): bounded, not exact
+    assert rel_alm_err(a64, alm) < 0.5
