@@ -640,8 +640,8 @@ def bench_batched(args, rank, world, local):
         return ms, clk
 
     b_split, t_build = build("split")
-    info = b_split.info()
     ms, clk = run(b_split, args.steps, args.warmup, ClockSampler(local))
+    info = b_split.info()          # the graph is captured on the first run
     b_split.close()
     del b_split
     torch.cuda.empty_cache()

@@ -53,6 +53,10 @@ SIGNATURES = {
     "fsht_qu2b": [_vp, _vp, _vp, _vp, _i],
     "fsht_eb2qu": [_vp, _vp, _vp, _vp, _vp, _i],
     "fsht_convert_alm_healpy": [_vp, _vp, _vp, _i],
+    "fsht_alm2cl": [_vp, _vp, _vp, _i, _i, _i, _vp],
+    "fsht_alm_filter": [_vp, _vp, _i, _i, _vp],
+    "fsht_alm_norm": [_vp, _vp, _vp, _vp, C.c_double, _i, _i, _vp],
+    "fsht_cl2alm": [_vp, _i, _i, _i, _i, C.c_ulonglong, _vp, _vp, _vp, _vp],
     "fsht_convert_alm_healpy_inv": [_vp, _vp, _vp, _i],
     "fsht_plan_sync": [_vp],
     "fsht_run_stage": [_vp, _i, _vp, _vp, _i],

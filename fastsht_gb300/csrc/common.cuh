@@ -152,6 +152,12 @@ void fsht_set_error(const char* fmt, ...);
     }                                                                         \
   } while (0)
 
+#define FSHT_TRY(expr)       \
+  do {                       \
+    int _rc = (expr);        \
+    if (_rc) return _rc;     \
+  } while (0)
+
 #define FSHT_LAUNCH_CHECK()                                                   \
   do {                                                                        \
     cudaError_t _e = cudaGetLastError();                                      \

@@ -162,12 +162,6 @@ int need_bufs(fsht_plan* p, int nb) {
   return FSHT_OK;
 }
 
-#define FSHT_TRY(expr)       \
-  do {                       \
-    int _rc = (expr);        \
-    if (_rc) return _rc;     \
-  } while (0)
-
 }  // namespace
 
 extern "C" {

@@ -114,6 +114,28 @@ int fsht_convert_alm_healpy(fsht_plan* plan, const double* alm, double* alm_hp, 
 /* Inverse: convert_alm_healpy_inv1 (src/convert_alm.f90:87-107). */
 int fsht_convert_alm_healpy_inv(fsht_plan* plan, const double* alm_hp, double* alm, int nmaps);
 
+/* ---------------------------------------------------------------- alm utilities
+ * Square-real alm, device pointers, layout [lmax+1][lmax+1][nmaps] (map fastest), async on
+ * `stream` (a cudaStream_t, NULL = legacy default stream).  No plan needed.
+ *
+ * fsht_alm2cl: cl[l][k] = sum_m fac_m Re(a1_lm conj a2_lm) / (2l+1), fac_0 = 1, fac_m = 2,
+ *   zero for l < lmin; alm2 = NULL or alm1 gives the auto spectrum.  cl: [lmax+1][nmaps].
+ *   Replaces alm2cl_TEB1 / alm2cl_T1 (src/alm2cl_TEB.f90:22-110), one spectrum per call.
+ * fsht_alm_filter: alm(l, m) *= win[l].  Replaces filt_alm1 (src/filt_alm.f90:16-37).
+ * fsht_alm_norm: out = in * fac[l] + shift[l], the m = 0 entries also times m0.  Replaces
+ *   norm_alm1 (src/norm_alm.f90:14-35).
+ * fsht_cl2alm: Gaussian alm with spectra cl ([lmax+1][ncl], ncl = 1: TT, or 6: TT EE BB TE TB
+ *   EB), zero for l < lmin, from a counter-based generator keyed by seed.  Replaces
+ *   cl2alm_TEB1 / cl2alm_T1 (src/cl2alm_TEB.f90:25-171); the reference's MKL MCG31 stream is
+ *   not reproduced (same statistics, different draws).  almE / almB may be NULL when ncl = 1. */
+int fsht_alm2cl(const double* alm1, const double* alm2, double* cl, int lmax, int nmaps,
+                int lmin, void* stream);
+int fsht_alm_filter(double* alm, const double* win, int lmax, int nmaps, void* stream);
+int fsht_alm_norm(const double* alm_in, double* alm_out, const double* fac, const double* shift,
+                  double m0, int lmax, int nmaps, void* stream);
+int fsht_cl2alm(const double* cl, int ncl, int lmin, int lmax, int nmaps, unsigned long long seed,
+                double* almT, double* almE, double* almB, void* stream);
+
 /* Per-kernel timing with CUDA events on the plan's stream (no host sync per
  * launch).  Categories: FSHT_KCAT_*.  fsht_profile_read synchronises the stream,
  * returns per-category launch counts and summed milliseconds, and clears them. */
