@@ -323,4 +323,44 @@ class SHT:
             return self._alm_out(self._dev_alm, alms_in, False)
 
     def fix_eb(self, Q, U, mask):
-        raise NotImplementedError("fix_eb (EB-leakage cleaning) is outside this library's scope")
+        """EB-leakage cleaning on a masked sky (reference SHT.fix_eb, SHT.py:192-202, over
+        fix_eb in src/sht_main.f90:801-941): mask Q/U, iterate (niter) to E/B, synthesise
+        Q/U from E alone, mask again, iterate to the leakage template's B, take the B alm and
+        the template to pixels with the spin-0 synthesis, and on the pixels where mask == 1
+        return the residual of the per-map linear fit (lin_resi_mini, src/sht_core.f90:232-
+        253) of the B map on the template; zero elsewhere.  As in the reference, Q and U
+        are masked in place.  Returns Bmap (npix, nsim), on the device for tensor inputs."""
+        if not self.pol:
+            raise ValueError("fix_eb needs SHT(..., pol=True)")
+        with torch.cuda.device(self.device):
+            self._stream()
+            dQ, as_torch = self._dev_maps(Q, "Q")
+            dU, _ = self._dev_maps(U, "U")
+            m = torch.as_tensor(np.asarray(mask, dtype=np.float64) if not _is_torch(mask) else mask,
+                                dtype=torch.float64, device=self.device).reshape(-1)
+            if m.numel() != self.npix:
+                raise ValueError(f"mask: expected {self.npix} pixels")
+            dQ.mul_(m)                                  # (nsim, npix): masked in place
+            dU.mul_(m)
+            if not as_torch:                            # the reference masks the caller's arrays
+                np.asarray(Q)[...] = dQ.cpu().numpy().T
+                np.asarray(U)[...] = dU.cpu().numpy().T
+            E, B = self.qu2eb(dQ.T, dU.T)
+            q2, u2 = self.eb2qu(E, torch.zeros_like(E))
+            q2.mul_(m[:, None])
+            u2.mul_(m[:, None])
+            _, btpl_alm = self.qu2eb(q2, u2)
+            y_all = self.alm2t(B)                       # (npix, nsim) views
+            x_all = self.alm2t(btpl_alm)
+            vid = torch.nonzero(m == 1).reshape(-1)
+            x, y = x_all[vid], y_all[vid]
+            mx, my = x.mean(dim=0), y.mean(dim=0)
+            a1 = ((y - my) * (x - mx)).sum(dim=0) / ((x - mx) ** 2).sum(dim=0)
+            a0 = my - mx * a1
+            out = torch.zeros((self.nsim, self.npix), dtype=torch.float64, device=self.device).T
+            out[vid] = y - a0 - a1 * x
+            if as_torch:
+                return out
+            res = _pinned_empty_fortran((self.npix, self.nsim))
+            torch.from_numpy(res.T).copy_(out.T)
+            return res

@@ -24,7 +24,7 @@ import scipy.fft
 __all__ = [
     "ring_info", "ring_angles", "ring_skip_table", "recursion_constants",
     "plm_T", "plm_pol", "OracleSHT", "alm_square_to_healpy", "alm_healpy_to_square",
-    "gaussian_alm", "lm_count", "plm_c", "c_recursion",
+    "gaussian_alm", "lm_count", "plm_c", "c_recursion", "alm2cl", "filt_alm", "norm_alm",
 ]
 
 PI = math.pi
@@ -384,6 +384,47 @@ def gaussian_alm(cl: np.ndarray, lmax: int, nsim: int, rng: np.random.Generator,
                     alm[:, ll - m, L - m] = 0
     del l
     return alm
+
+
+def alm2cl(alm1: np.ndarray, alm2: np.ndarray | None = None, lmin: int = 0) -> np.ndarray:
+    """Cross spectrum of square-real alm (nsim, L, L) -> (nsim, L): restates the loops of
+    alm2cl_TEB1 / alm2cl_T1 (src/alm2cl_TEB.f90:22-110): sum over m of fac (Re Re + Im Im)
+    / (2l+1), fac = 1 at m = 0 and 2 above; zero below lmin."""
+    if alm2 is None:
+        alm2 = alm1
+    nsim, L, _ = alm1.shape
+    cl = np.zeros((nsim, L))
+    for m in range(L):
+        fac = 1.0 if m == 0 else 2.0
+        for l in range(max(m, lmin), L):
+            t = alm1[:, l, m] * alm2[:, l, m]
+            if m > 0:
+                t = t + alm1[:, l - m, L - m] * alm2[:, l - m, L - m]
+            cl[:, l] += t * fac / (2 * l + 1)
+    return cl
+
+
+def filt_alm(alm: np.ndarray, win: np.ndarray) -> np.ndarray:
+    """alm(l, m) *= win(l) (filt_alm1, src/filt_alm.f90:16-37), returned as a new array."""
+    out = np.array(alm, order="F", copy=True)
+    nsim, L, _ = out.shape
+    out[:, :, 0] *= win[None, :L]
+    for m in range(1, L):
+        out[:, m:, m] *= win[None, m:L]
+        out[:, 0:L - m, L - m] *= win[None, m:L]
+    return out
+
+
+def norm_alm(alm: np.ndarray, fac: np.ndarray, shift: np.ndarray, m0: float) -> np.ndarray:
+    """alm * fac(l) + shift(l), the m = 0 column also times m0 (norm_alm1,
+    src/norm_alm.f90:14-35)."""
+    out = np.empty_like(alm, order="F")
+    nsim, L, _ = alm.shape
+    out[:, :, 0] = alm[:, :, 0] * (fac[:L] * m0)[None, :] + shift[None, :L]
+    for m in range(1, L):
+        out[:, m:, m] = alm[:, m:, m] * fac[None, m:L] + shift[None, m:L]
+        out[:, 0:L - m, L - m] = alm[:, 0:L - m, L - m] * fac[None, m:L] + shift[None, m:L]
+    return out
 
 
 # ---------------------------------------------------------------------------
@@ -774,6 +815,27 @@ class OracleSHT:
         self._zero_unused_bins(bq)
         self._zero_unused_bins(bu)
         return self.fft2map(bq), self.fft2map(bu)
+
+    def fix_eb(self, Q, U, mask, niter):
+        """EB-leakage cleaning (fix_eb, sht_main.f90:801-941; lin_resi_mini,
+        sht_core.f90:232-253): mask Q/U, iterate to E/B, synthesise Q/U from E alone, mask
+        again, iterate to the leakage template's B, take both B alm to pixels with the
+        spin-0 synthesis, and on the pixels where mask == 1 return the residual of the
+        per-map linear fit of the B map on the template (zero elsewhere)."""
+        m = np.asarray(mask, dtype=np.float64)[:, None]
+        almE, almB = self.qu2eb_iter_old(Q * m, U * m, niter)
+        q2, u2 = self.eb2qu(almE, np.zeros_like(almE))
+        _, btpl_alm = self.qu2eb_iter_old(q2 * m, u2 * m, niter)
+        bmap = self.alm2t(almB)
+        btpl = self.alm2t(btpl_alm)
+        vid = np.flatnonzero(np.asarray(mask) == 1)
+        out = np.zeros_like(bmap)
+        x, y = btpl[vid], bmap[vid]
+        mx, my = x.mean(axis=0), y.mean(axis=0)
+        a1 = ((y - my) * (x - mx)).sum(axis=0) / ((x - mx) ** 2).sum(axis=0)
+        a0 = my - mx * a1
+        out[vid] = y - a0 - a1 * x
+        return out
 
     def qu2eb_iter_old(self, Q, U, niter):
         """qu2eb_iter_old (sht_main.f90:563-673)."""

@@ -245,3 +245,24 @@ def test_nside_2048_lmax_4096_roundtrip_and_split():
     assert rel_alm_err(a16, a64) <= 1e-7
     # niter = 0 quadrature error only (lmax = 2 nside): bounded, not exact
     assert rel_alm_err(a64, alm) < 0.5
+
+
+@pytest.mark.parametrize("niter", [0, 2])
+def test_fix_eb_matches_oracle(niter):
+    """EB-leakage cleaning (SHT.fix_eb) against the oracle's restatement of fix_eb, and the
+    reference's in-place masking of Q/U."""
+    ns, lmax, nsim = 16, 40, 3
+    rng = np.random.default_rng(5)
+    l = np.arange(lmax + 1, dtype=float)
+    cl = np.where(l >= 2, 1.0 / np.maximum(l * (l + 1), 1.0), 0.0)
+    E = gaussian_alm(cl, lmax, nsim, rng)
+    B = gaussian_alm(0.01 * cl, lmax, nsim, rng)
+    sht = SHT(ns, lmax, nsim, niter=niter, pol=True)
+    Q, U = sht.eb2qu(E, B)
+    th = np.arccos(np.linspace(1, -1, 12 * ns * ns))           # a band mask, not healpy
+    mask = (np.abs(np.cos(th)) > 0.3).astype(float)
+    Qo, Uo = np.array(Q, order="F", copy=True), np.array(U, order="F", copy=True)
+    want = OracleSHT(ns, lmax, ring_tab=sht.ring_skip()).fix_eb(Qo, Uo, mask, niter)
+    got = sht.fix_eb(Q, U, mask)
+    assert rel_map_err(got, want) <= 1e-10
+    assert np.array_equal(Q, Qo * mask[:, None])               # masked in place

@@ -175,3 +175,36 @@ def test_oracle_c_and_numpy_paths_agree():
     e1, b1 = OracleSHT(ns, lmax, use_c=True).qu2eb(Q, maps)
     e2, b2 = OracleSHT(ns, lmax, use_c=False).qu2eb(Q, maps)
     assert rel_alm_err(e1, e2) < 1e-13 and rel_alm_err(b1, b2) < 1e-13
+
+
+def test_alm2cl_of_one_mode_and_linearity():
+    """alm2cl restatement: a single Re a_lm = 1 at m > 0 gives C_l = 2/(2l+1); the m = 0
+    mode gives 1/(2l+1); cross spectra are bilinear."""
+    from oracle import alm2cl
+    L = 9
+    a = np.zeros((1, L, L), order="F")
+    a[0, 5, 3] = 1.0                       # Re a_{5,3}
+    cl = alm2cl(a)
+    assert np.allclose(cl[0], np.where(np.arange(L) == 5, 2.0 / 11, 0.0))
+    b = np.zeros((1, L, L), order="F")
+    b[0, 4, 0] = 3.0                       # a_{4,0}
+    assert np.isclose(alm2cl(b)[0, 4], 9.0 / 9)
+    rng = np.random.default_rng(0)
+    x = np.asfortranarray(rng.standard_normal((2, L, L)))
+    y = np.asfortranarray(rng.standard_normal((2, L, L)))
+    assert np.allclose(alm2cl(x + y), alm2cl(x) + 2 * alm2cl(x, y) + alm2cl(y))
+    assert np.allclose(alm2cl(x, lmin=4)[:, :4], 0.0)
+
+
+def test_filt_and_norm_restatements():
+    from oracle import filt_alm, norm_alm
+    L = 7
+    rng = np.random.default_rng(1)
+    a = np.asfortranarray(rng.standard_normal((3, L, L)))
+    win = np.linspace(0.5, 1.5, L)
+    f = filt_alm(a, win)
+    assert np.isclose(f[1, 5, 2], a[1, 5, 2] * win[5])            # Re a_{5,2}
+    assert np.isclose(f[1, 5 - 2, L - 2], a[1, 5 - 2, L - 2] * win[5])   # Im a_{5,2}
+    n = norm_alm(a, win, np.full(L, 0.25), 3.0)
+    assert np.isclose(n[0, 4, 0], a[0, 4, 0] * win[4] * 3.0 + 0.25)
+    assert np.isclose(n[0, 4, 1], a[0, 4, 1] * win[4] + 0.25)
