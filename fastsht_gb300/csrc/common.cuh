@@ -117,7 +117,11 @@ struct fsht_plan {
   double2* d_work;
   size_t work_bytes;
   int nbuf;
-  size_t fft_smem;                 // dynamic smem of the ring FFT kernels
+  size_t fft_smem;                 // dynamic smem of the ring FFT kernels (largest segment)
+  // ring segments launched separately so rings with small transforms get 2 CTAs per SM:
+  // {first ring, end ring, dynamic smem bytes} per segment
+  int fft_nseg;
+  long long fft_seg[3 * 8];
   int fft_mpb, fft_threads;        // ring-FFT launch shape (0: heuristic), set by the autotuner
   struct FshtProfile* prof;        // non-null while per-kernel timing is on
   int* d_err;                      // device error word (bounded waits that expired)

@@ -195,6 +195,10 @@ extern "C" int fsht_t2alm_noalloc(int nside, int lmax, const double* maps, doubl
   p.logTmax = f.logTmax;
   p.P3max = f.P3max;
   p.fft_smem = f.smem;
+  p.fft_nseg = 1;
+  p.fft_seg[0] = 0;
+  p.fft_seg[1] = 2 * nside;
+  p.fft_seg[2] = (long long)f.smem;
   p.nbuf = 1;
   int* blue = reinterpret_cast<int*>(base + L.blue);
 

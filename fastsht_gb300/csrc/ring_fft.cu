@@ -715,6 +715,27 @@ int fsht_fft_tables_init(fsht_plan* p) {
   FshtFftLayout lay;
   int rc = fsht_fft_layout(p->nside, p->lmax, &lay, rfs.data(), blue_rings.data());
   if (rc) return rc;
+  {
+    // consecutive rings whose (P + lmax + 1) double2 fit twice per SM form one launch segment
+    const size_t two_per_sm = 112 * 1024;
+    p->fft_nseg = 0;
+    int cls_prev = -1;
+    for (int i = 0; i < nn; ++i) {
+      const size_t sm = (size_t)(rfs[i].P + p->lmax + 1) * sizeof(double2);
+      const int cls = sm <= two_per_sm ? 0 : 1;
+      if (cls != cls_prev && p->fft_nseg < 8) {
+        long long* sg = p->fft_seg + 3 * p->fft_nseg++;
+        sg[0] = i;
+        sg[1] = i + 1;
+        sg[2] = (long long)sm;
+        cls_prev = cls;
+      } else {
+        long long* sg = p->fft_seg + 3 * (p->fft_nseg - 1);
+        sg[1] = i + 1;
+        if ((long long)sm > sg[2]) sg[2] = (long long)sm;
+      }
+    }
+  }
   p->Pmax = lay.Pmax;
   p->Tmax = lay.Tmax;
   p->logTmax = lay.logTmax;
@@ -780,11 +801,15 @@ int fsht_launch_ring_fft_fwd(fsht_plan* p, const double* maps, long long map_str
   a.ring_i0 = p->d_ring_i0;
   a.W = W;
   a.maps_per_block = p->fft_mpb > 0 ? p->fft_mpb : maps_per_block_for(kc, p->nnorth);
-  dim3 grid(p->nnorth, (kc + a.maps_per_block - 1) / a.maps_per_block);
   FSHT_CUDA_TRY(cudaFuncSetAttribute(k_ring_fft_fwd, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      (int)p->fft_smem));
-  k_ring_fft_fwd<<<grid, p->fft_threads > 0 ? p->fft_threads : 512, p->fft_smem, s>>>(a);
-  FSHT_LAUNCH_CHECK();
+  for (int sgi = 0; sgi < p->fft_nseg; ++sgi) {
+    const long long* sg = p->fft_seg + 3 * sgi;
+    a.ring_base = (int)sg[0];
+    dim3 grid((unsigned)(sg[1] - sg[0]), (kc + a.maps_per_block - 1) / a.maps_per_block);
+    k_ring_fft_fwd<<<grid, p->fft_threads > 0 ? p->fft_threads : 512, (size_t)sg[2], s>>>(a);
+    FSHT_LAUNCH_CHECK();
+  }
   return FSHT_OK;
 }
 
@@ -807,11 +832,15 @@ int fsht_launch_ring_fft_inv(fsht_plan* p, const double2* W, double* maps, long 
   a.bhat = p->d_bhat;
   a.ring_i0 = p->d_ring_i0;
   a.maps_per_block = p->fft_mpb > 0 ? p->fft_mpb : maps_per_block_for(kc, p->nnorth);
-  dim3 grid(p->nnorth, (kc + a.maps_per_block - 1) / a.maps_per_block);
   FSHT_CUDA_TRY(cudaFuncSetAttribute(k_ring_fft_inv, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      (int)p->fft_smem));
-  k_ring_fft_inv<<<grid, p->fft_threads > 0 ? p->fft_threads : 512, p->fft_smem, s>>>(a);
-  FSHT_LAUNCH_CHECK();
+  for (int sgi = 0; sgi < p->fft_nseg; ++sgi) {
+    const long long* sg = p->fft_seg + 3 * sgi;
+    a.ring_base = (int)sg[0];
+    dim3 grid((unsigned)(sg[1] - sg[0]), (kc + a.maps_per_block - 1) / a.maps_per_block);
+    k_ring_fft_inv<<<grid, p->fft_threads > 0 ? p->fft_threads : 512, (size_t)sg[2], s>>>(a);
+    FSHT_LAUNCH_CHECK();
+  }
   return FSHT_OK;
 }
 
