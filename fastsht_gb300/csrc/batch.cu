@@ -56,8 +56,9 @@ JobLayout job_layout(const fsht_plan* p, const fsht_job& j, int kc) {
   L.eb_off = L.ws_off;
   L.lb_off = L.ws_off;
   L.total = L.ws_off;
-  if (p->precision == FSHT_PREC_SPLIT && j.kind != FSHT_JOB_EB2QU) {
-    const size_t f = j.kind == FSHT_JOB_QU2EB ? 2 : 1;   // spin 2: tiles of Q and U
+  if (p->precision == FSHT_PREC_SPLIT) {
+    const bool pol2 = j.kind == FSHT_JOB_QU2EB || j.kind == FSHT_JOB_EB2QU;
+    const size_t f = pol2 ? 2 : 1;   // spin 2: tiles of Q and U (or E and B)
     L.eb_off = align_up(L.ws_off + f * fsht_split_ws_bytes(p, kc));
     L.lb_off = align_up(L.eb_off + f * fsht_split_eb_bytes(p, kc));
     L.total = align_up(L.lb_off + p->lbuf_bytes);

@@ -225,6 +225,13 @@ int fsht_launch_split_lambdaT(fsht_plan* p, int w, unsigned char* lbuf, cudaStre
 // Split-precision spin-2 analysis: lambda1/lambda2 digit tiles per wave, then the E/B
 // contraction (which: bit0 E, bit1 B) against the Q and U digit tiles of k_slice_phase.
 int fsht_split_pol_tables_init(fsht_plan* p);
+// Split-precision spin-2 synthesis (E/B -> {G_N, G_S} of Q and U) per wave: lambda1/lambda2
+// ring-row tiles, then the four-pass contraction against the E and B alm tiles.
+int fsht_launch_split_lambdaT_pol(fsht_plan* p, int w, unsigned char* lbuf, cudaStream_t s);
+int fsht_launch_split_synth_pol(fsht_plan* p, int w, const unsigned char* WSE, const int* EBE,
+                                const unsigned char* WSB, const int* EBB,
+                                const unsigned char* lbuf, double2* WQ, double2* WU, int kc,
+                                cudaStream_t s);
 int fsht_launch_split_lambda_pol(fsht_plan* p, int w, unsigned char* lbuf, cudaStream_t s);
 int fsht_launch_split_gemm_pol(fsht_plan* p, int w, const unsigned char* WSQ, const int* EBQ,
                                const unsigned char* WSU, const int* EBU,

@@ -863,7 +863,7 @@ int fsht_split_tables_init(fsht_plan* p) {
   // spin-2 plans stage lambda1 and lambda2: twice the analysis tiles
   const long long fa = p->pol ? 2 : 1;
   auto span = [&](int q0, int q1) -> size_t {
-    return (size_t)std::max(fa * (off[q1] - off[q0]), offT[q1] - offT[q0]);
+    return (size_t)std::max(fa * (off[q1] - off[q0]), fa * (offT[q1] - offT[q0]));
   };
   // waves: consecutive q ranges whose tiles (either layout) fit the staging buffer
   std::vector<int> waves;

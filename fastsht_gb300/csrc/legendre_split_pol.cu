@@ -19,6 +19,7 @@
 #include "split_common.cuh"
 
 #include <algorithm>
+#include <cmath>
 #include <vector>
 
 namespace {
@@ -408,6 +409,364 @@ __global__ void __launch_bounds__(kThreads, 1) k_split_gemm_pol(GemmPArgs a) {
   if (tid == 0 && h.abort) atomicOr(a.err, 1);
 }
 
+// ------------------------------------------------------------------ spin-2 synthesis
+// G_Q = -(lambda1 E + i lambda2 B), G_U = i lambda2 E - lambda1 B (sht_main.f90:1079-1147),
+// north = even + odd l-m; south: lambda1 keeps the sign (-1)^(l-m), lambda2 takes the
+// opposite one.  Ring-row tiles of lambda1 and lambda2 against one global scale (as in the
+// spin-0 synthesis), the E and B alm tiles of k_slice_alm (with the 2^-8 planes, level 4
+// folded in).
+
+// grid (q in wave, 128-ring block), 128 threads = rings.  Tiles of m: (part, parity, ring
+// block, l-step) x 4 digits at twice the spin-0 synthesis offset of q.
+struct LamTPArgs {
+  int lmax, nnorth, q0, eag;
+  const double* cth;
+  const double* sth;
+  const double* pref;
+  const int* ring_i0;
+  const FshtLamRow* tab;
+  const FshtPolRow* ptab;
+  const long long* lam_offT;
+  unsigned char* lbuf;
+};
+
+__global__ void __launch_bounds__(128) k_lambda_digits_T_pol(LamTPArgs a) {
+  __shared__ FshtLamRow s_tab[32];
+  __shared__ FshtPolRow s_pc[32];
+  const int q = a.q0 + blockIdx.x;
+  const int m = m_of_q(q, a.lmax);
+  const int i0 = a.ring_i0[m];
+  const int K = a.nnorth - i0;
+  const int rb = blockIdx.y;
+  if (rb * kSCRings >= K) return;
+  const int tid = threadIdx.x;
+  const int r = rb * kSCRings + tid;
+  const bool valid = r < K;
+  const int nrb = (K + kSCRings - 1) / kSCRings;
+  const int nkl = ((a.lmax - m) / 2 + 1 + kKStep - 1) / kKStep;
+  unsigned char* base =
+      a.lbuf + (size_t)(2 * (a.lam_offT[q] - a.lam_offT[a.q0])) * kSlices * kATileBytes +
+      (tid >> 3) * 256 + (tid & 7) * 16;
+  const FshtLamRow* tab = a.tab + tri_off(m, a.lmax);
+  const FshtPolRow* ptab = a.ptab + tri_off(m, a.lmax);
+  double x = 0.0, inv_s2 = 0.0, b_w = 0.0, c_w = 0.0, s1 = 0.0, s2 = 0.0;
+  int et = 0;
+  if (valid) {
+    int e;
+    const double sth = a.sth[i0 + r];
+    x = a.cth[i0 + r];
+    inv_s2 = 1.0 / (sth * sth);
+    b_w = x * inv_s2;
+    c_w = (double)m * inv_s2;
+    rec_seed(sth, a.pref[m], m, s1, e);
+    et = 600 * e;
+  }
+  for (int kl = 0; kl < nkl; ++kl) {
+    __syncthreads();
+    if (tid < 32 && m + kl * 32 + tid <= a.lmax) {
+      s_tab[tid] = tab[kl * 32 + tid];
+      s_pc[tid] = ptab[kl * 32 + tid];
+    }
+    __syncthreads();
+#pragma unroll 1
+    for (int half = 0; half < 2; ++half) {
+      uint32_t pk[2][2][kSlices][4];      // [part][parity][digit][word]
+#pragma unroll
+      for (int a0 = 0; a0 < 2; ++a0)
+#pragma unroll
+        for (int pp = 0; pp < 2; ++pp)
+#pragma unroll
+          for (int d = 0; d < kSlices; ++d)
+#pragma unroll
+            for (int w = 0; w < 4; ++w) pk[a0][pp][d][w] = 0;
+#pragma unroll
+      for (int jj = 0; jj < 16; ++jj) {
+        const int j = kl * 32 + half * 16 + jj;
+        uint16_t d1[4] = {0, 0, 0, 0}, d2[4] = {0, 0, 0, 0};
+        if (m + j <= a.lmax) {
+          const FshtLamRow rw = s_tab[half * 16 + jj];
+          if (j > 0) {
+            const double t = rw.beta * s2;
+            const double nx = fma(x, s1, -t);
+            s2 = s1;
+            s1 = nx;
+          }
+          if (valid) {
+            const FshtPolRow c = s_pc[half * 16 + jj];
+            const double u = s2 * c.c1;
+            const double l1 = fma(u, b_w, -s1 * fma(c.c2, inv_s2, c.c3));
+            const double l2 = fma(-s1, c.c4 * x, u) * c_w;
+            tc::digits4(l1 * rw.dm, a.eag - et - rw.dx, d1);
+            tc::digits4(l2 * rw.dm, a.eag - et - rw.dx, d2);
+          }
+        }
+        const int par = jj & 1, slot = jj >> 1;
+#pragma unroll
+        for (int dd = 0; dd < kSlices; ++dd) {
+          pk[0][par][dd][slot >> 1] |= (uint32_t)d1[dd] << (16 * (slot & 1));
+          pk[1][par][dd][slot >> 1] |= (uint32_t)d2[dd] << (16 * (slot & 1));
+        }
+      }
+#pragma unroll
+      for (int part = 0; part < 2; ++part)
+#pragma unroll
+        for (int par = 0; par < 2; ++par)
+#pragma unroll
+          for (int dd = 0; dd < kSlices; ++dd) {
+            uint4 o;
+            o.x = pk[part][par][dd][0];
+            o.y = pk[part][par][dd][1];
+            o.z = pk[part][par][dd][2];
+            o.w = pk[part][par][dd][3];
+            *reinterpret_cast<uint4*>(
+                base + ((((size_t)(part * 2 + par) * nrb + rb) * nkl + kl) * kSlices + dd) *
+                           kATileBytes +
+                half * 128) = o;
+          }
+    }
+    const double am = fmax(fabs(s1), fabs(s2));
+    if (am > 0x1p300) {
+      s1 *= 0x1p-600;
+      s2 *= 0x1p-600;
+      et += 600;
+    } else if (am > 0.0 && am < 0x1p-300) {
+      s1 *= 0x1p600;
+      s2 *= 0x1p600;
+      et -= 600;
+    }
+  }
+}
+
+// CTA = (group, ring block x l-chunk x field (Q, U), q): four passes through the same TMEM
+// accumulators, each one (lambda part, alm field, parity) product added to G_N and G_S with
+// its factor c in {-1, -i, +i} and south sign.
+struct SynthPArgs {
+  int lmax, nnorth, ngroups, nkcl_glob, q0, nkclmax, eag;
+  size_t row_bytes;
+  const int* ring_i0;
+  const long long* lam_offT;
+  const unsigned char* lbuf;
+  const unsigned char* WSE;
+  const unsigned char* WSB;
+  const int* EBE;
+  const int* EBB;
+  double* WQ;      // double2 {G_N, G_S} as doubles
+  double* WU;
+  int kc;
+  int* err;
+};
+
+constexpr int kStagesSP = 4;
+constexpr uint32_t kStageBytesSP = kSlices * kATileBytes + kSynthBBytes;   // 44 KB
+
+struct __align__(8) SynthPSmemHdr {
+  uint64_t full[kStagesSP], empty[kStagesSP], tfull, tempty, fin;
+  uint32_t tmem;
+  int abort;
+};
+
+// pass t of field f: lambda part, alm field (0 E, 1 B), parity, factor c (0: -1, 1: -i,
+// 2: +i) and south sign
+__device__ __forceinline__ void synth_pol_pass(int f, int t, int& part, int& fld, int& par,
+                                               int& c, int& sgn_s) {
+  par = t & 1;
+  const int second = t >> 1;
+  if (f == 0) {          // G_Q = -(l1 E) - i (l2 B)
+    part = second;       // l1 then l2
+    fld = second;        // E then B
+    c = second ? 1 : 0;
+  } else {               // G_U = i (l2 E) - (l1 B)
+    part = 1 - second;   // l2 then l1
+    fld = second;        // E then B
+    c = second ? 0 : 2;
+  }
+  const int s1 = par ? -1 : 1;              // lambda1: (-1)^(l-m)
+  sgn_s = (part == 0) ? s1 : -s1;           // lambda2: the opposite sign
+}
+
+__global__ void __launch_bounds__(kThreads, 1) k_split_synth_pol(SynthPArgs a) {
+  extern __shared__ __align__(1024) unsigned char smem[];
+  __shared__ SynthPSmemHdr h;
+  __shared__ double s_cs[4][kCols];
+
+  const int g = blockIdx.x;
+  const int f = blockIdx.y & 1;
+  const int rest = blockIdx.y >> 1;
+  const int rb = rest / a.nkclmax;
+  const int kcl = rest % a.nkclmax;
+  const int q = a.q0 + blockIdx.z;
+  const int m = m_of_q(q, a.lmax);
+  const int i0 = a.ring_i0[m];
+  const int K = a.nnorth - i0;
+  const int nrb = (K + kSCRings - 1) / kSCRings;
+  const int nkl = ((a.lmax - m) / 2 + 1 + kKStep - 1) / kKStep;
+  const int kl0 = kcl * (kKChunk / kKStep);
+  const int kl1 = min(nkl, kl0 + kKChunk / kKStep);
+  if (rb >= nrb || kl0 >= kl1) return;            // uniform: before any barrier or TMEM
+  const int nk = kl1 - kl0;
+
+  const int tid = threadIdx.x;
+  const int warp = tid >> 5;
+  volatile int* abort = &h.abort;
+  if (tid == 0) {
+    for (int s = 0; s < kStagesSP; ++s) {
+      tc::mbar_init(&h.full[s], 1);
+      tc::mbar_init(&h.empty[s], 1);
+    }
+    tc::mbar_init(&h.tfull, 1);
+    tc::mbar_init(&h.tempty, 128);
+    tc::mbar_init(&h.fin, 1);
+    h.abort = 0;
+    tc::mbar_fence_init();
+  }
+  if (tid < kCols) {
+    for (int t = 0; t < 4; ++t) {
+      int part, fld, par, c, sg;
+      synth_pol_pass(f, t, part, fld, par, c, sg);
+      const int* eb = fld ? a.EBB : a.EBE;
+      const int e = eb[(((long long)blockIdx.z * 2 + par) * a.ngroups + g) * kCols + tid];
+      s_cs[t][tid] = (e == kEmptyExp) ? 0.0 : ldexp(1.0, a.eag + e - 12);
+    }
+  }
+  if (warp == 0) tc::tmem_alloc(&h.tmem, 512);
+  tc::tc_fence_before();
+  __syncthreads();
+  tc::tc_fence_after();
+  const uint32_t tmem = h.tmem;
+
+  uint32_t n_loaded = 0;
+  if (tid == 128) {
+    const unsigned char* lam =
+        a.lbuf + (size_t)(2 * (a.lam_offT[q] - a.lam_offT[a.q0])) * kSlices * kATileBytes;
+    for (int i = 0; i < 4 * nk; ++i) {
+      int part, fld, par, c, sg;
+      synth_pol_pass(f, i / nk, part, fld, par, c, sg);
+      const int kk = kl0 + i % nk;
+      const uint32_t st = i % kStagesSP;
+      if (!tc::mbar_wait(&h.empty[st], ((i / kStagesSP) & 1) ^ 1, abort)) break;
+      unsigned char* dst = smem + st * kStageBytesSP;
+      const unsigned char* asrc =
+          lam + ((((size_t)(part * 2 + par) * nrb + rb) * nkl + kk) * kSlices) * kATileBytes;
+      const unsigned char* bsrc = (fld ? a.WSB : a.WSE) +
+                                  (((size_t)blockIdx.z * 2 + par) * a.ngroups + g) * a.row_bytes +
+                                  (size_t)kk * kSynthBBytes;
+      tc::mbar_arrive_expect_tx(&h.full[st], kStageBytesSP);
+      tc::bulk_g2s(dst, asrc, kSlices * kATileBytes, &h.full[st]);
+      tc::bulk_g2s(dst + kSlices * kATileBytes, bsrc, kSynthBBytes, &h.full[st]);
+      ++n_loaded;
+    }
+  } else if (tid == 160) {
+    const uint32_t idesc = tc::umma_idesc_bf16(kRows, kCols);
+    const uint32_t s_u = tc::smem_u32(smem);
+    for (int i = 0; i < 4 * nk; ++i) {
+      if (i > 0 && i % nk == 0) {
+        // a pass is complete: hand TMEM to the epilogue, take it back for the next one
+        tc::umma_commit(&h.tfull);
+        if (!tc::mbar_wait(&h.tempty, ((i / nk) - 1) & 1, abort)) break;
+        tc::tc_fence_after();
+      }
+      const uint32_t st = i % kStagesSP;
+      if (!tc::mbar_wait(&h.full[st], (i / kStagesSP) & 1, abort)) break;
+      tc::tc_fence_after();
+      const uint32_t abase = s_u + st * kStageBytesSP;
+      const uint32_t bbase = abase + kSlices * kATileBytes;
+      const bool first = (i % nk) == 0;
+#pragma unroll
+      for (int lev = 0; lev <= 3; ++lev) {
+#pragma unroll
+        for (int aa = 0; aa <= lev; ++aa) {
+          const uint64_t ad = tc::umma_desc(abase + aa * kATileBytes, 128, 256);
+          const uint64_t bd = tc::umma_desc(bbase + (lev - aa) * kBTileBytes, 128, 256);
+          tc::umma_bf16(tmem + lev * kCols, ad, bd, idesc, (!first || aa > 0) ? 1u : 0u);
+        }
+      }
+#pragma unroll
+      for (int aa = 1; aa <= 3; ++aa) {
+        const uint64_t ad = tc::umma_desc(abase + aa * kATileBytes, 128, 256);
+        const uint64_t bd = tc::umma_desc(bbase + (kSlices - 1 + (4 - aa)) * kBTileBytes, 128, 256);
+        tc::umma_bf16(tmem + 3 * kCols, ad, bd, idesc, 1u);
+      }
+      tc::umma_commit(&h.empty[st]);
+    }
+    tc::umma_commit(&h.tfull);
+  }
+  if (tid < 128) {
+    const int row = (warp << 5) + (tid & 31);
+    const int rr = rb * kSCRings + row;
+    const bool rowok = rr < K;
+    const int i = i0 + rr;
+    double* Wf = f ? a.WU : a.WQ;
+    for (int t = 0; t < 4; ++t) {
+      int part, fld, par, c, sg;
+      synth_pol_pass(f, t, part, fld, par, c, sg);
+      bool ok = tc::mbar_wait(&h.tfull, t & 1, abort);
+      ok = __all_sync(0xffffffffu, ok);
+      tc::tc_fence_after();
+      if (!ok) break;
+      const uint32_t lane_base = tmem + ((uint32_t)(warp << 5) << 16);
+      for (int c0 = 0; c0 < kCols; c0 += 16) {
+        uint32_t v0[16], v1[16], v2[16], v3[16];
+        tc::tmem_ld16(lane_base + 0 * kCols + c0, v0);
+        tc::tmem_ld16(lane_base + 1 * kCols + c0, v1);
+        tc::tmem_ld16(lane_base + 2 * kCols + c0, v2);
+        tc::tmem_ld16(lane_base + 3 * kCols + c0, v3);
+        tc::tmem_wait_ld();
+        const int comp = c0 >> 6;
+        // c D: -1: (-D.x, -D.y);  -i: (D.y, -D.x);  +i: (-D.y, D.x)
+        int tgt = comp;
+        double sgn = -1.0;
+        if (c == 1) {
+          tgt = 1 - comp;
+          sgn = comp ? 1.0 : -1.0;
+        } else if (c == 2) {
+          tgt = 1 - comp;
+          sgn = comp ? -1.0 : 1.0;
+        }
+        if (!rowok) continue;
+#pragma unroll
+        for (int j = 0; j < 16; ++j) {
+          const int cc = c0 + j;
+          const int k = g * kGroupMaps + (cc & 63);
+          if (k < a.kc) {
+            const double v = sgn * combine_levels(v0[j], v1[j], v2[j], v3[j]) * s_cs[t][cc];
+            double* gn = Wf + ((((long long)m * a.nnorth + i) * a.kc + k) * 2) * 2 + tgt;
+            double* gs = gn + 2;
+            const double vs = sg * v;
+            if (a.nkcl_glob > 1) {
+              atomicAdd(gn, v);
+              atomicAdd(gs, vs);
+            } else if (t == 0) {     // pass 0 writes both components of G_N and G_S
+              *gn = v;
+              *gs = vs;
+            } else {
+              *gn += v;
+              *gs += vs;
+            }
+          }
+        }
+      }
+      tc::tc_fence_before();
+      if (t < 3) tc::mbar_arrive(&h.tempty);
+    }
+  }
+  if (tid == 160) {
+    tc::umma_commit(&h.fin);
+    for (uint32_t it = 0; it < tc::kWaitLimit; ++it)
+      if (tc::mbar_try_wait(&h.fin, 0)) break;
+  }
+  if (tid == 128) {
+    for (uint32_t d = 0; d < (uint32_t)kStagesSP && d < n_loaded; ++d) {
+      const uint32_t i = n_loaded - 1 - d;
+      for (uint32_t it = 0; it < tc::kWaitLimit; ++it)
+        if (tc::mbar_try_wait(&h.full[i % kStagesSP], (i / kStagesSP) & 1)) break;
+    }
+  }
+  tc::tc_fence_before();
+  __syncthreads();
+  if (warp == 0) tc::tmem_dealloc(tmem, 512);
+  if (tid == 0 && h.abort) atomicOr(a.err, 1);
+}
+
 }  // namespace
 
 int fsht_split_pol_tables_init(fsht_plan* p) {
@@ -479,6 +838,61 @@ int fsht_launch_split_gemm_pol(fsht_plan* p, int w, const unsigned char* WSQ, co
   FSHT_CUDA_TRY(cudaFuncSetAttribute(k_split_gemm_pol,
                                      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
   k_split_gemm_pol<<<dim3(a.ngroups, 4 * a.ntmax * a.nkcmax, wv[1] - wv[0]), kThreads, sm, s>>>(a);
+  FSHT_LAUNCH_CHECK();
+  return FSHT_OK;
+}
+
+int fsht_launch_split_lambdaT_pol(fsht_plan* p, int w, unsigned char* lbuf, cudaStream_t s) {
+  const int* wv = p->h_waves + kWaveInts * w;
+  if (wv[4] == 0) return FSHT_OK;
+  LamTPArgs a;
+  a.lmax = p->lmax;
+  a.nnorth = p->nnorth;
+  a.q0 = wv[0];
+  a.eag = std::ilogb(std::sqrt((2.0 * p->lmax + 1.0) / (4.0 * M_PI)) * (1.0 + 0x1p-30)) + 1;
+  a.cth = p->d_cth;
+  a.sth = p->d_sth;
+  a.pref = p->d_pref;
+  a.ring_i0 = p->d_ring_i0;
+  a.tab = p->d_lamtab;
+  a.ptab = p->d_poltab;
+  a.lam_offT = p->d_lam_offT;
+  a.lbuf = lbuf;
+  k_lambda_digits_T_pol<<<dim3(wv[1] - wv[0], wv[4]), 128, 0, s>>>(a);
+  FSHT_LAUNCH_CHECK();
+  return FSHT_OK;
+}
+
+int fsht_launch_split_synth_pol(fsht_plan* p, int w, const unsigned char* WSE, const int* EBE,
+                                const unsigned char* WSB, const int* EBB,
+                                const unsigned char* lbuf, double2* WQ, double2* WU, int kc,
+                                cudaStream_t s) {
+  const int* wv = p->h_waves + kWaveInts * w;
+  if (wv[4] == 0 || wv[6] == 0) return FSHT_OK;
+  SynthPArgs a;
+  a.lmax = p->lmax;
+  a.nnorth = p->nnorth;
+  a.ngroups = (kc + kGroupMaps - 1) / kGroupMaps;
+  a.nkcl_glob = ((p->lmax / 2 + 1 + kKStep - 1) / kKStep * kKStep + kKChunk - 1) / kKChunk;
+  a.q0 = wv[0];
+  a.nkclmax = wv[6];
+  a.eag = std::ilogb(std::sqrt((2.0 * p->lmax + 1.0) / (4.0 * M_PI)) * (1.0 + 0x1p-30)) + 1;
+  a.row_bytes = ws_row_bytes(p->lmax, p->nnorth);
+  a.ring_i0 = p->d_ring_i0;
+  a.lam_offT = p->d_lam_offT;
+  a.lbuf = lbuf;
+  a.WSE = WSE;
+  a.WSB = WSB;
+  a.EBE = EBE;
+  a.EBB = EBB;
+  a.WQ = reinterpret_cast<double*>(WQ);
+  a.WU = reinterpret_cast<double*>(WU);
+  a.kc = kc;
+  a.err = p->d_err;
+  const size_t sm = (size_t)kStagesSP * kStageBytesSP;
+  FSHT_CUDA_TRY(cudaFuncSetAttribute(k_split_synth_pol,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+  k_split_synth_pol<<<dim3(a.ngroups, 2 * wv[4] * wv[6], wv[1] - wv[0]), kThreads, sm, s>>>(a);
   FSHT_LAUNCH_CHECK();
   return FSHT_OK;
 }

@@ -608,6 +608,43 @@ static int pol_analysis(fsht_plan* p, const double2* WQ, const double2* WU, doub
   return FSHT_OK;
 }
 
+// One chunk's spin-2 synthesis of E/B into {G_N, G_S} of Q and U: the FP64 kernel, or the
+// split form's tiles and waves.
+static int pol_synthesis(fsht_plan* p, const double* almE, const double* almB, double2* WQ,
+                         double2* WU, int nmaps, int c0, int kc) {
+  if (p->precision != FSHT_PREC_SPLIT) {
+    FSHT_PROF(FSHT_KCAT_SYNTHESIS);
+    return fsht_launch_synthesis_fp64(p, 2, almE, almB, WQ, WU, nmaps, c0, kc, p->stream);
+  }
+  if (!p->d_poltab) {
+    fsht_set_error("spin-2 split synthesis needs a plan created with FSHT_FLAG_POL");
+    return FSHT_EUNSUPPORTED;
+  }
+  unsigned char* wse = p->d_ws;
+  unsigned char* wsb = p->d_ws + fsht_split_ws_bytes(p, kc);
+  int* ebe = p->d_eb;
+  int* ebb = p->d_eb + fsht_split_eb_bytes(p, kc) / sizeof(int);
+  FSHT_TRY(fsht_split_clear_w(p, WQ, kc, p->stream));
+  FSHT_TRY(fsht_split_clear_w(p, WU, kc, p->stream));
+  for (int w = 0; w < p->nwaves; ++w) {
+    {
+      FSHT_PROF(FSHT_KCAT_SLICE);
+      FSHT_TRY(fsht_launch_split_slice_alm(p, w, almE, wse, ebe, nmaps, c0, kc, p->stream));
+      FSHT_TRY(fsht_launch_split_slice_alm(p, w, almB, wsb, ebb, nmaps, c0, kc, p->stream));
+    }
+    {
+      FSHT_PROF(FSHT_KCAT_LAMBDA);
+      FSHT_TRY(fsht_launch_split_lambdaT_pol(p, w, p->d_lbuf, p->stream));
+    }
+    {
+      FSHT_PROF(FSHT_KCAT_SYNTHESIS);
+      FSHT_TRY(fsht_launch_split_synth_pol(p, w, wse, ebe, wsb, ebb, p->d_lbuf, WQ, WU, kc,
+                                           p->stream));
+    }
+  }
+  return FSHT_OK;
+}
+
 static int qu_analysis(fsht_plan* p, const double* Q, const double* U, double* almE,
                        double* almB, int nmaps, int niter, int method, int which) {
   FSHT_TRY(need_bufs(p, niter > 0 ? 4 : 2));
@@ -625,14 +662,10 @@ static int qu_analysis(fsht_plan* p, const double* Q, const double* U, double* a
     }
     FSHT_TRY(pol_analysis(p, WQ, WU, almE, almB, nmaps, c0, kc, 0, which));
     if (niter > 0) {
-      // the split form refines with the FP64 spin-2 synthesis and residual
       double2* RQ = work_buf(p, 2, kc);
       double2* RU = work_buf(p, 3, kc);
       for (int it = 0; it < niter; ++it) {
-        {
-          FSHT_PROF(FSHT_KCAT_SYNTHESIS);
-          FSHT_TRY(fsht_launch_synthesis_fp64(p, 2, almE, almB, RQ, RU, nmaps, c0, kc, p->stream));
-        }
+        FSHT_TRY(pol_synthesis(p, almE, almB, RQ, RU, nmaps, c0, kc));
         {
           FSHT_PROF(FSHT_KCAT_RESIDUAL);
           FSHT_TRY(fsht_launch_fourier_residual(p, WQ, RQ, kc, method, p->stream));
@@ -688,10 +721,7 @@ int fsht_eb2qu(fsht_plan* p, const double* almE, const double* almB, double* Q, 
     const int kc = nmaps - c0 < p->kchunk ? nmaps - c0 : p->kchunk;
     double2* WQ = work_buf(p, 0, kc);
     double2* WU = work_buf(p, 1, kc);
-    {
-      FSHT_PROF(FSHT_KCAT_SYNTHESIS);
-      FSHT_TRY(fsht_launch_synthesis_fp64(p, 2, almE, almB, WQ, WU, nmaps, c0, kc, p->stream));
-    }
+    FSHT_TRY(pol_synthesis(p, almE, almB, WQ, WU, nmaps, c0, kc));
     {
       FSHT_PROF(FSHT_KCAT_FFT_INV);
       FSHT_TRY(fsht_launch_ring_fft_inv(p, WQ, Q + (size_t)c0 * p->npix, p->npix, kc, p->stream));

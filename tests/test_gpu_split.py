@@ -170,3 +170,18 @@ def test_split_qu2eb_refinement():
     E16, B16 = SHT(ns, lmax, nsim, niter=1, pol=True, precision="split").qu2eb(Q, U)
     assert rel_alm_err(E16, E64) <= SPLIT_TOL
     assert rel_alm_err(B16, B64) <= SPLIT_TOL
+
+
+@pytest.mark.parametrize("ns,lmax,nsim", [(4, 11, 2), (16, 47, 5), (64, 191, 70), (512, 2048, 1)])
+def test_split_eb2qu_matches_fp64(ns, lmax, nsim):
+    """Spin-2 split synthesis (lambda1/lambda2 ring-row tiles, four passes with the factors
+    -1, -i, +i and the south signs) against the plain path; lmax 2048 adds l-chunks."""
+    rng = np.random.default_rng(ns)
+    l = np.arange(lmax + 1, dtype=float)
+    cl = np.where(l >= 2, 1.0 / np.maximum(l * (l + 1), 1.0), 0.0)
+    E = gaussian_alm(cl, lmax, nsim, rng)
+    B = gaussian_alm(0.1 * cl, lmax, nsim, rng)
+    Q64, U64 = SHT(ns, lmax, nsim, pol=True).eb2qu(E, B)
+    Q16, U16 = SHT(ns, lmax, nsim, pol=True, precision="split").eb2qu(E, B)
+    assert rel_map_err(Q16, Q64) <= SPLIT_TOL
+    assert rel_map_err(U16, U64) <= SPLIT_TOL
