@@ -244,7 +244,7 @@ struct FwdArgs {
   double2* W;
 };
 
-__global__ void __launch_bounds__(512) k_ring_fft_fwd(FwdArgs a) {
+__global__ void __launch_bounds__(512, 2) k_ring_fft_fwd(FwdArgs a) {
   extern __shared__ double2 smem[];
   const int i = a.ring_base + blockIdx.x;      // north ring index
   const FshtRingFFT rf = a.rfs[i];
@@ -404,7 +404,7 @@ __device__ __forceinline__ double2 spectrum_bin(const double2* ph, const double2
   return y;
 }
 
-__global__ void __launch_bounds__(512) k_ring_fft_inv(InvArgs a) {
+__global__ void __launch_bounds__(512, 2) k_ring_fft_inv(InvArgs a) {
   extern __shared__ double2 smem[];
   const int i = a.ring_base + blockIdx.x;
   const FshtRingFFT rf = a.rfs[i];
