@@ -32,6 +32,12 @@ struct FftTw {
 
 constexpr double kSqrt3Half = 0.86602540378443864676;
 
+// Shared-memory position of transform element i: the low three bits of the index (eight
+// 16-byte elements = one 128-byte bank row) are XORed with the next three, so the strided
+// accesses of the radix-4 passes with small spans spread over the banks; a bijection within
+// every block of 64 elements.
+__device__ __forceinline__ int sw(int i) { return i ^ ((i >> 3) & 7); }
+
 // In-place decimation-in-frequency FFT of rf.P points in shared memory, natural order in,
 // transform order out: an optional radix-3 pass (P = 3 T) splits the data into three
 // blocks of T = 2^logT, then radix-4 passes (radix-2^2 butterflies: three twiddles, none
@@ -46,15 +52,15 @@ __device__ void fft_dif(double2* buf, const FshtRingFFT& rf, const FftTw& tw) {
   if (rf.r3) {
     const int sc = tw.P3max / rf.P;
     for (int j = tid; j < T; j += nt) {
-      const double2 a = buf[j], b = buf[j + T], c = buf[j + 2 * T];
+      const double2 a = buf[sw(j)], b = buf[sw(j + T)], c = buf[sw(j + 2 * T)];
       const double2 sm = cadd(b, c), df = csub(b, c);
       const double2 t = make_double2(fma(-0.5, sm.x, a.x), fma(-0.5, sm.y, a.y));
       // w3 = exp(-2 pi i / 3): a + w3 b + w3^2 c = t - i (sqrt3/2) df, the other t + i ...
       const double2 y1 = make_double2(fma(kSqrt3Half, df.y, t.x), fma(-kSqrt3Half, df.x, t.y));
       const double2 y2 = make_double2(fma(-kSqrt3Half, df.y, t.x), fma(kSqrt3Half, df.x, t.y));
-      buf[j] = cadd(a, sm);
-      buf[j + T] = cmul(y1, __ldg(&tw.tw3[j * sc]));
-      buf[j + 2 * T] = cmul(y2, __ldg(&tw.tw3[2 * j * sc]));
+      buf[sw(j)] = cadd(a, sm);
+      buf[sw(j + T)] = cmul(y1, __ldg(&tw.tw3[j * sc]));
+      buf[sw(j + 2 * T)] = cmul(y2, __ldg(&tw.tw3[2 * j * sc]));
     }
     __syncthreads();
   }
@@ -68,29 +74,29 @@ __device__ void fft_dif(double2* buf, const FshtRingFFT& rf, const FftTw& tw) {
       const int r = idx & (per_blk - 1);
       const int j = r & (h - 1);
       const int i0 = (blk << logT) + ((r >> lh) << logspan) + j;
-      const double2 a = buf[i0], b = buf[i0 + h], c = buf[i0 + 2 * h], d = buf[i0 + 3 * h];
+      const double2 a = buf[sw(i0)], b = buf[sw(i0 + h)], c = buf[sw(i0 + 2 * h)], d = buf[sw(i0 + 3 * h)];
       const double2 apc = cadd(a, c), amc = csub(a, c), bpd = cadd(b, d), bmd = csub(b, d);
       const double2 y1 = csub(apc, bpd);
       const double2 y2 = make_double2(amc.x + bmd.y, amc.y - bmd.x);   // (a-c) - i(b-d)
       const double2 y3 = make_double2(amc.x - bmd.y, amc.y + bmd.x);   // (a-c) + i(b-d)
-      buf[i0] = cadd(apc, bpd);
+      buf[sw(i0)] = cadd(apc, bpd);
       if (h == 1) {
-        buf[i0 + h] = y1;
-        buf[i0 + 2 * h] = y2;
-        buf[i0 + 3 * h] = y3;
+        buf[sw(i0 + h)] = y1;
+        buf[sw(i0 + 2 * h)] = y2;
+        buf[sw(i0 + 3 * h)] = y3;
       } else {
-        buf[i0 + h] = cmul(y1, __ldg(&tw.tw2[(2 * j) << sh]));
-        buf[i0 + 2 * h] = cmul(y2, __ldg(&tw.tw2[j << sh]));
-        buf[i0 + 3 * h] = cmul(y3, __ldg(&tw.tw2[(3 * j) << sh]));
+        buf[sw(i0 + h)] = cmul(y1, __ldg(&tw.tw2[(2 * j) << sh]));
+        buf[sw(i0 + 2 * h)] = cmul(y2, __ldg(&tw.tw2[j << sh]));
+        buf[sw(i0 + 3 * h)] = cmul(y3, __ldg(&tw.tw2[(3 * j) << sh]));
       }
     }
     __syncthreads();
   }
   if (logspan == 1) {
     for (int idx = tid; idx < nblk << (logT - 1); idx += nt) {
-      const double2 a = buf[2 * idx], b = buf[2 * idx + 1];
-      buf[2 * idx] = cadd(a, b);
-      buf[2 * idx + 1] = csub(a, b);
+      const double2 a = buf[sw(2 * idx)], b = buf[sw(2 * idx + 1)];
+      buf[sw(2 * idx)] = cadd(a, b);
+      buf[sw(2 * idx + 1)] = csub(a, b);
     }
     __syncthreads();
   }
@@ -106,9 +112,9 @@ __device__ void fft_dit_inv(double2* buf, const FshtRingFFT& rf, const FftTw& tw
   int logspan = 2;
   if (logT & 1) {
     for (int idx = tid; idx < nblk << (logT - 1); idx += nt) {
-      const double2 a = buf[2 * idx], b = buf[2 * idx + 1];
-      buf[2 * idx] = cadd(a, b);
-      buf[2 * idx + 1] = csub(a, b);
+      const double2 a = buf[sw(2 * idx)], b = buf[sw(2 * idx + 1)];
+      buf[sw(2 * idx)] = cadd(a, b);
+      buf[sw(2 * idx + 1)] = csub(a, b);
     }
     __syncthreads();
     logspan = 3;
@@ -122,32 +128,32 @@ __device__ void fft_dit_inv(double2* buf, const FshtRingFFT& rf, const FftTw& tw
       const int r = idx & (per_blk - 1);
       const int j = r & (h - 1);
       const int i0 = (blk << logT) + ((r >> lh) << logspan) + j;
-      const double2 y0 = buf[i0];
-      double2 z1 = buf[i0 + h], z2 = buf[i0 + 2 * h], z3 = buf[i0 + 3 * h];
+      const double2 y0 = buf[sw(i0)];
+      double2 z1 = buf[sw(i0 + h)], z2 = buf[sw(i0 + 2 * h)], z3 = buf[sw(i0 + 3 * h)];
       if (h > 1) {
         z1 = cmul(z1, cconj(__ldg(&tw.tw2[(2 * j) << sh])));
         z2 = cmul(z2, cconj(__ldg(&tw.tw2[j << sh])));
         z3 = cmul(z3, cconj(__ldg(&tw.tw2[(3 * j) << sh])));
       }
       const double2 sp = cadd(y0, z1), dm = csub(y0, z1), e = cadd(z2, z3), f = csub(z2, z3);
-      buf[i0] = cadd(sp, e);
-      buf[i0 + 2 * h] = csub(sp, e);
-      buf[i0 + h] = make_double2(dm.x - f.y, dm.y + f.x);       // d + i f
-      buf[i0 + 3 * h] = make_double2(dm.x + f.y, dm.y - f.x);   // d - i f
+      buf[sw(i0)] = cadd(sp, e);
+      buf[sw(i0 + 2 * h)] = csub(sp, e);
+      buf[sw(i0 + h)] = make_double2(dm.x - f.y, dm.y + f.x);       // d + i f
+      buf[sw(i0 + 3 * h)] = make_double2(dm.x + f.y, dm.y - f.x);   // d - i f
     }
     __syncthreads();
   }
   if (rf.r3) {
     const int sc = tw.P3max / rf.P;
     for (int j = tid; j < T; j += nt) {
-      const double2 a = buf[j];
-      const double2 b = cmul(buf[j + T], cconj(__ldg(&tw.tw3[j * sc])));
-      const double2 c = cmul(buf[j + 2 * T], cconj(__ldg(&tw.tw3[2 * j * sc])));
+      const double2 a = buf[sw(j)];
+      const double2 b = cmul(buf[sw(j + T)], cconj(__ldg(&tw.tw3[j * sc])));
+      const double2 c = cmul(buf[sw(j + 2 * T)], cconj(__ldg(&tw.tw3[2 * j * sc])));
       const double2 sm = cadd(b, c), df = csub(b, c);
       const double2 t = make_double2(fma(-0.5, sm.x, a.x), fma(-0.5, sm.y, a.y));
-      buf[j] = cadd(a, sm);
-      buf[j + T] = make_double2(fma(-kSqrt3Half, df.y, t.x), fma(kSqrt3Half, df.x, t.y));
-      buf[j + 2 * T] = make_double2(fma(kSqrt3Half, df.y, t.x), fma(-kSqrt3Half, df.x, t.y));
+      buf[sw(j)] = cadd(a, sm);
+      buf[sw(j + T)] = make_double2(fma(-kSqrt3Half, df.y, t.x), fma(kSqrt3Half, df.x, t.y));
+      buf[sw(j + 2 * T)] = make_double2(fma(kSqrt3Half, df.y, t.x), fma(-kSqrt3Half, df.x, t.y));
     }
     __syncthreads();
   }
@@ -171,13 +177,13 @@ __device__ void ring_dft(double2* buf, const FshtRingFFT& rf, const FftTw& tw,
   }
   const int n = rf.nd, P = rf.P;
   for (int j = tid; j < P; j += nt) {
-    if (j < n) buf[j] = cmul(buf[j], __ldg(&chirp[j]));
-    else buf[j] = make_double2(0.0, 0.0);
+    if (j < n) buf[sw(j)] = cmul(buf[sw(j)], __ldg(&chirp[j]));
+    else buf[sw(j)] = make_double2(0.0, 0.0);
   }
   fft_dif(buf, rf, tw);
-  for (int j = tid; j < P; j += nt) buf[j] = cmul(buf[j], __ldg(&bhat[j]));
+  for (int j = tid; j < P; j += nt) buf[sw(j)] = cmul(buf[sw(j)], __ldg(&bhat[j]));
   fft_dit_inv(buf, rf, tw);
-  for (int j = tid; j < n; j += nt) buf[j] = cmul(buf[j], __ldg(&chirp[j]));
+  for (int j = tid; j < n; j += nt) buf[sw(j)] = cmul(buf[sw(j)], __ldg(&chirp[j]));
   __syncthreads();
 }
 
@@ -221,11 +227,11 @@ __global__ void k_bluestein_tables(const FshtRingFFT* rfs, const int* rings, dou
     double2 v = make_double2(0.0, 0.0);
     if (j < n) v = cconj(w[j]);
     else if (P - j < n) v = cconj(w[P - j]);
-    sbuf[j] = v;
+    sbuf[sw(j)] = v;
   }
   fft_dif(sbuf, rf, tw);
   const double invP = 1.0 / (double)P;
-  for (int j = threadIdx.x; j < P; j += blockDim.x) bhat[rf.bhat_off + j] = cscale(sbuf[j], invP);
+  for (int j = threadIdx.x; j < P; j += blockDim.x) bhat[rf.bhat_off + j] = cscale(sbuf[sw(j)], invP);
 }
 
 // ------------------------------------------------------------------ forward
@@ -285,15 +291,15 @@ __global__ void __launch_bounds__(512, 2) k_ring_fft_fwd(FwdArgs a) {
         const double* x = a.maps + (long long)k * a.map_stride + (side ? off_s : off_n);
         __syncthreads();
         for (int j = tid; j < nd; j += nt)
-          buf[j] = make_double2(__ldg(&x[2 * j]), __ldg(&x[2 * j + 1]));
+          buf[sw(j)] = make_double2(__ldg(&x[2 * j]), __ldg(&x[2 * j + 1]));
         __syncthreads();
         ring_dft(buf, rf, a.tw, chirp, bhat);
         for (int m = tid; m <= mtop; m += nt) {
           const int q = m % n;
           const bool cj = q > nd;
           const int kk = cj ? n - q : q;
-          const double2 za = buf[dft_bin(rf, kk == nd ? 0 : kk)];
-          const double2 zb = cconj(buf[dft_bin(rf, kk == 0 ? 0 : nd - kk)]);
+          const double2 za = buf[sw(dft_bin(rf, kk == nd ? 0 : kk))];
+          const double2 zb = cconj(buf[sw(dft_bin(rf, kk == 0 ? 0 : nd - kk))]);
           const double2 e = cscale(cadd(za, zb), 0.5);
           const double2 dd = csub(za, zb);
           const double2 o = make_double2(0.5 * dd.y, -0.5 * dd.x);
@@ -318,15 +324,15 @@ __global__ void __launch_bounds__(512, 2) k_ring_fft_fwd(FwdArgs a) {
     const double* xs = a.maps + (long long)k * a.map_stride + off_s;
     __syncthreads();
     for (int j = tid; j < n; j += nt)
-      buf[j] = make_double2(__ldg(&xn[j]), equator ? 0.0 : __ldg(&xs[j]));
+      buf[sw(j)] = make_double2(__ldg(&xn[j]), equator ? 0.0 : __ldg(&xs[j]));
     __syncthreads();
     ring_dft(buf, rf, a.tw, chirp, bhat);
     // Z = FFT(x_N + i x_S): X_N[q] = (Z[q] + conj Z[-q])/2, X_S[q] = (Z[q] - conj Z[-q])/(2i)
     for (int m = tid; m <= mtop; m += nt) {
       const int q = m % n;
       const int qn = (q == 0) ? 0 : n - q;
-      const double2 zq = buf[dft_bin(rf, q)];
-      const double2 zn = cconj(buf[dft_bin(rf, qn)]);
+      const double2 zq = buf[sw(dft_bin(rf, q))];
+      const double2 zn = cconj(buf[sw(dft_bin(rf, qn))]);
       const double2 xN = cscale(cadd(zq, zn), 0.5);
       const double2 dd = csub(zq, zn);
       const double2 xS = make_double2(0.5 * dd.y, -0.5 * dd.x);
@@ -382,7 +388,7 @@ __device__ void build_spectrum(double2* buf, const double2* ph, const double2* _
       yN = cadd(yN, cscale(cconj(cmul(ph[m], w[0])), c));
       if (!equator) yS = cadd(yS, cscale(cconj(cmul(ph[m], w[1])), c));
     }
-    buf[q] = make_double2(yN.x - yS.y, yN.y + yS.x);   // Y_N + i Y_S
+    buf[sw(q)] = make_double2(yN.x - yS.y, yN.y + yS.x);   // Y_N + i Y_S
   }
 }
 
@@ -446,13 +452,13 @@ __global__ void __launch_bounds__(512, 2) k_ring_fft_inv(InvArgs a) {
           const double2 y1 = spectrum_bin(ph, Wk, stride_m, n, mtop, side, kk + nd);
           const double2 b = cmul(csub(y0, y1), cconj(__ldg(&rtw[kk])));
           const double2 sa = cadd(y0, y1);
-          buf[kk] = cconj(make_double2(sa.x - b.y, sa.y + b.x));   // conj(A + i B)
+          buf[sw(kk)] = cconj(make_double2(sa.x - b.y, sa.y + b.x));   // conj(A + i B)
         }
         __syncthreads();
         ring_dft(buf, rf, a.tw, chirp, bhat);
         double* x = a.maps + (long long)k * a.map_stride + (side ? off_s : off_n);
         for (int j = tid; j < nd; j += nt) {
-          const double2 z = buf[dft_bin(rf, j)];   // conj(z): x_{2j} = Re, x_{2j+1} = -Im
+          const double2 z = buf[sw(dft_bin(rf, j))];   // conj(z): x_{2j} = Re, x_{2j+1} = -Im
           x[2 * j] = z.x;
           x[2 * j + 1] = -z.y;
         }
@@ -465,13 +471,13 @@ __global__ void __launch_bounds__(512, 2) k_ring_fft_inv(InvArgs a) {
     build_spectrum(buf, ph, a.W + ((long long)i * a.kc + k) * 2, stride_m, n, mtop, equator);
     __syncthreads();
     // inverse DFT = conj(DFT(conj Z))
-    for (int j = tid; j < n; j += nt) buf[j] = cconj(buf[j]);
+    for (int j = tid; j < n; j += nt) buf[sw(j)] = cconj(buf[sw(j)]);
     __syncthreads();
     ring_dft(buf, rf, a.tw, chirp, bhat);
     double* xn = a.maps + (long long)k * a.map_stride + off_n;
     double* xs = a.maps + (long long)k * a.map_stride + off_s;
     for (int j = tid; j < n; j += nt) {
-      const double2 z = buf[dft_bin(rf, j)];   // conj applied: x_N = Re, x_S = -Im of the DFT
+      const double2 z = buf[sw(dft_bin(rf, j))];   // conj applied: x_N = Re, x_S = -Im of the DFT
       xn[j] = z.x;
       if (!equator) xs[j] = -z.y;
     }
