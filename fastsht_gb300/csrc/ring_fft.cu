@@ -272,7 +272,7 @@ __global__ void __launch_bounds__(512, 2) k_ring_fft_fwd(FwdArgs a) {
       long long r = (long long)m % (2LL * n);
       sincospi(-(double)r / (double)n, &s, &c);
     }
-    ph[m] = make_double2(c, s);
+    ph[m] = make_double2(0.5 * c, 0.5 * s);    // the 1/2 of the N/S (even/odd) split folded in
   }
   const int k_begin = blockIdx.y * a.maps_per_block;
   const int k_end = min(a.kc, k_begin + a.maps_per_block);
@@ -300,10 +300,10 @@ __global__ void __launch_bounds__(512, 2) k_ring_fft_fwd(FwdArgs a) {
           const int kk = cj ? n - q : q;
           const double2 za = buf[sw(dft_bin(rf, kk == nd ? 0 : kk))];
           const double2 zb = cconj(buf[sw(dft_bin(rf, kk == 0 ? 0 : nd - kk))]);
-          const double2 e = cscale(cadd(za, zb), 0.5);
+          const double2 e = cadd(za, zb);                      // 2 E
           const double2 dd = csub(za, zb);
-          const double2 o = make_double2(0.5 * dd.y, -0.5 * dd.x);
-          double2 xq = cadd(e, cmul(__ldg(&rtw[kk]), o));
+          const double2 o = make_double2(dd.y, -dd.x);         // 2 O
+          double2 xq = cadd(e, cmul(__ldg(&rtw[kk]), o));      // 2 X
           if (cj) xq = cconj(xq);
           const double2 f = cmul(ph[m], xq);
           double2* w = a.W + (((long long)m * a.nnorth + i) * a.kc + k) * 2;
@@ -333,19 +333,18 @@ __global__ void __launch_bounds__(512, 2) k_ring_fft_fwd(FwdArgs a) {
       const int qn = (q == 0) ? 0 : n - q;
       const double2 zq = buf[sw(dft_bin(rf, q))];
       const double2 zn = cconj(buf[sw(dft_bin(rf, qn))]);
-      const double2 xN = cscale(cadd(zq, zn), 0.5);
+      const double2 xN = cadd(zq, zn);                         // 2 X_N
       const double2 dd = csub(zq, zn);
-      const double2 xS = make_double2(0.5 * dd.y, -0.5 * dd.x);
-      const double2 p = ph[m];
-      const double2 fN = cmul(p, xN);
+      const double2 xS = make_double2(dd.y, -dd.x);            // 2 X_S
+      const double2 p = ph[m];                                 // e^{-i m phi0} / 2
       double2* w = a.W + (((long long)m * a.nnorth + i) * a.kc + k) * 2;
       if (equator) {
+        const double2 fN = cmul(p, xN);
         w[0] = fN;
         w[1] = fN;
       } else {
-        const double2 fS = cmul(p, xS);
-        w[0] = cadd(fN, fS);
-        w[1] = csub(fN, fS);
+        w[0] = cmul(p, cadd(xN, xS));                          // F_N + F_S
+        w[1] = cmul(p, csub(xN, xS));                          // F_N - F_S
       }
     }
   }
