@@ -61,7 +61,18 @@ __global__ void __launch_bounds__(256) k_slice_phase(SliceArgs a) {
   const long long rstride = (long long)a.kc * 4;
   auto val = [&](int r) -> double { return (valid && r < K) ? col[r * rstride] : 0.0; };
   double mx = 0.0;
-  for (int r = 0; r < K; ++r) mx = fmax(mx, fabs(val(r)));
+  if (valid) {
+    // eight independent loads in flight per thread
+    int r = 0;
+    for (; r + 8 <= K; r += 8) {
+      double v[8];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) v[u] = col[(long long)(r + u) * rstride];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) mx = fmax(mx, fabs(v[u]));
+    }
+    for (; r < K; ++r) mx = fmax(mx, fabs(col[(long long)r * rstride]));
+  }
   const int E = (mx > 0.0) ? ilogb(mx) + 1 : kEmptyExp;
   a.EB[(((long long)qi * 2 + p) * a.ngroups + g) * kCols + c] = E;
   const int nks = (K + kKStep - 1) / kKStep;

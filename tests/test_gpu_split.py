@@ -185,3 +185,23 @@ def test_split_eb2qu_matches_fp64(ns, lmax, nsim):
     Q16, U16 = SHT(ns, lmax, nsim, pol=True, precision="split").eb2qu(E, B)
     assert rel_map_err(Q16, Q64) <= SPLIT_TOL
     assert rel_map_err(U16, U64) <= SPLIT_TOL
+
+
+@pytest.mark.parametrize("ns,lmax", [(1, 0), (1, 2), (2, 1), (2, 5), (4, 0), (4, 16), (8, 32)])
+def test_split_small_and_edge_sizes(ns, lmax):
+    """Tiny rings, lmax 0 and lmax = 4 nside in every split transform (T and Q/U, both
+    directions), against the plain path."""
+    nsim = 3
+    rng = np.random.default_rng(ns * 100 + lmax)
+    maps = np.asfortranarray(rng.standard_normal((12 * ns * ns, nsim)))
+    p64, p16 = SHT(ns, lmax, nsim, pol=True), SHT(ns, lmax, nsim, pol=True, precision="split")
+    assert rel_alm_err(p16.t2alm(maps), p64.t2alm(maps)) <= SPLIT_TOL
+    alm = p64.t2alm(maps)
+    assert rel_map_err(p16.alm2t(alm), p64.alm2t(alm)) <= SPLIT_TOL
+    if lmax >= 2:
+        E64, B64 = p64.qu2eb(maps, maps[:, ::-1].copy(order="F"))
+        E16, B16 = p16.qu2eb(maps, maps[:, ::-1].copy(order="F"))
+        assert rel_alm_err(E16, E64) <= SPLIT_TOL and rel_alm_err(B16, B64) <= SPLIT_TOL
+        Q64, U64 = p64.eb2qu(E64, B64)
+        Q16, U16 = p16.eb2qu(E64, B64)
+        assert rel_map_err(Q16, Q64) <= SPLIT_TOL and rel_map_err(U16, U64) <= SPLIT_TOL
