@@ -663,10 +663,12 @@ class OracleSHT:
             mat1, mat2 = self.fft2mat(buff, m)
             self.mat2alm(alm2, mat1, mat2, self.plm(m), m, 0, beta)
 
-    def t2alm_timed(self, maps):
+    def t2alm_timed(self, maps, m_stride=1):
         """t2alm with wall-clock phase times (seconds): ring FFT, recursion (which
         the reference computes once per m for the whole batch) and the per-m
-        gather + DGEMMs.  Used by the CPU baseline to scale a map sample to a batch."""
+        gather + DGEMMs.  Used by the CPU baseline to scale a map sample to a batch.
+        m_stride > 1 times every m_stride-th order only and scales the recursion and
+        GEMM times by m_stride (the alm of the other orders stay zero)."""
         import time
         t0 = time.perf_counter()
         nsim = maps.shape[1]
@@ -675,7 +677,7 @@ class OracleSHT:
         alm, alm2 = self._new_alm(nsim)
         t_plm = 0.0
         t_gemm = 0.0
-        for m in range(self.lmax + 1):
+        for m in range(0, self.lmax + 1, m_stride):
             ta = time.perf_counter()
             plm = self.plm(m)
             tb = time.perf_counter()
@@ -684,7 +686,7 @@ class OracleSHT:
             tc = time.perf_counter()
             t_plm += tb - ta
             t_gemm += tc - tb
-        return alm, {"fft": t1 - t0, "plm": t_plm, "gemm": t_gemm}
+        return alm, {"fft": t1 - t0, "plm": t_plm * m_stride, "gemm": t_gemm * m_stride}
 
     def t2alm(self, maps):
         """t2alm (sht_main.f90:38-89)."""
