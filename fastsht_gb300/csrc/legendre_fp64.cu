@@ -156,6 +156,9 @@ __global__ void __launch_bounds__(NT) k_analysis_fp64(AnaArgs a) {
   const int par = lg & 1;
   const int kt0 = blockIdx.y * MT;
   const int npair = (a.lmax + 2) / 2;
+  // map slots q with a map behind them: small batches skip the padding's FMAs (warps
+  // whose lanes all lack slot q skip it entirely)
+  const int nq = max(0, min(4, (a.kc - kt0 - mg + 15) / 16));
 
   for (int pass = 0; pass < 2; ++pass) {
     const int m = pass == 0 ? (int)blockIdx.x : a.lmax - (int)blockIdx.x;
@@ -252,6 +255,7 @@ __global__ void __launch_bounds__(NT) k_analysis_fp64(AnaArgs a) {
             const double2* pp = P + (par * RC + rr) * MT + mg;
 #pragma unroll
             for (int q = 0; q < 4; ++q) {
+              if (q >= nq) break;
               const double2 v = pp[16 * q];
               accE[0][q].x = fma(la, v.x, accE[0][q].x);
               accE[0][q].y = fma(la, v.y, accE[0][q].y);
@@ -268,6 +272,7 @@ __global__ void __launch_bounds__(NT) k_analysis_fp64(AnaArgs a) {
             const double2* u2 = P + ((1 * 2 + (1 - par)) * RC + rr) * MT + mg;
 #pragma unroll
             for (int q = 0; q < 4; ++q) {
+              if (q >= nq) break;
               const double2 Q1 = q1[16 * q], Q2 = q2[16 * q], U1 = u1[16 * q], U2 = u2[16 * q];
               // E += l1 P1Q + i l2 P2U ;  B += l1 P1U - i l2 P2Q
               accE[0][q].x = fma(l1a, Q1.x, fma(-l2a, U2.y, accE[0][q].x));
@@ -355,6 +360,7 @@ __global__ void __launch_bounds__(NT) k_synthesis_fp64(SynArgs a) {
   const int ib = blockIdx.y * RCS;
   const int kt0 = blockIdx.z * MT;
   const long long L1 = a.lmax + 1;
+  const int nq = max(0, min(MQ, (a.kc - kt0 - mg + 15) / 16));   // map slots with a map
 
   for (int pass = 0; pass < 2; ++pass) {
     const int m = pass == 0 ? (int)blockIdx.x : a.lmax - (int)blockIdx.x;
@@ -440,6 +446,7 @@ __global__ void __launch_bounds__(NT) k_synthesis_fp64(SynArgs a) {
             const double r0 = lam1[rg][jj], r1 = lam1[rg + 16][jj];
 #pragma unroll
             for (int q = 0; q < MQ; ++q) {
+              if (q >= nq) break;
               const double2 v = A[0][jj][mg + 16 * q];
               acc[s][0][q][0].x = fma(r0, v.x, acc[s][0][q][0].x);
               acc[s][0][q][0].y = fma(r0, v.y, acc[s][0][q][0].y);
@@ -451,6 +458,7 @@ __global__ void __launch_bounds__(NT) k_synthesis_fp64(SynArgs a) {
             const double a20 = lam2[rg][jj], a21 = lam2[rg + 16][jj];
 #pragma unroll
             for (int q = 0; q < MQ; ++q) {
+              if (q >= nq) break;
               const double2 E = A[0][jj][mg + 16 * q];
               const double2 B = A[1][jj][mg + 16 * q];
               // t=0: l1 E, t=1: l2 B, t=2: l2 E, t=3: l1 B
