@@ -366,6 +366,7 @@ extern "C" int fsht_batch_sync(fsht_batch* b) {
     return FSHT_EINVAL;
   }
   FSHT_CUDA_TRY(cudaStreamSynchronize(b->stream));
+  for (fsht_plan* p : b->plans) FSHT_TRY(fsht_plan_check(p));   // expired device-side waits
   return FSHT_OK;
 }
 

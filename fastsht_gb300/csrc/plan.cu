@@ -396,6 +396,11 @@ int fsht_profile_read(fsht_plan* p, int ncat, int* launches, double* total_ms) {
 int fsht_plan_sync(fsht_plan* p) {
   FSHT_TRY(check_plan(p));
   FSHT_CUDA_TRY(cudaStreamSynchronize(p->stream));
+  return fsht_plan_check(p);
+}
+
+int fsht_plan_check(fsht_plan* p) {
+  FSHT_TRY(check_plan(p));
   int err = 0;
   FSHT_CUDA_TRY(cudaMemcpy(&err, p->d_err, sizeof(int), cudaMemcpyDeviceToHost));
   if (err) {

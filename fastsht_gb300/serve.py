@@ -333,6 +333,16 @@ class Server:
     def _finish(self, part: _Part):
         self._used -= part.nbytes
         self._free_slots.append(part.slot)
+        head = part.members[0][0]
+        rc = _lib.load().fsht_plan_check(self._plan(head.nside, head.lmax, head.precision))
+        if rc:          # a bounded device-side wait expired: these results are invalid
+            err = _lib.FshtError(rc, "fsht_plan_check", _lib.last_error())
+            for r, *_ in part.members:
+                if not r.future.done():
+                    r.future.set_exception(err)
+                if r in self._pending:
+                    self._pending.remove(r)
+            return
         for r, m0, m1, off in part.members:
             if len(part.members) == 1 and m0 == 0 and m1 == r.nmaps:
                 piece = part.outputs

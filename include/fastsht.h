@@ -221,8 +221,14 @@ int fsht_run_job(const fsht_plan* tables, const fsht_job* job, void* workspace,
 int fsht_plan_autotune(fsht_plan* plan, int sample_maps);
 int fsht_plan_tuning(const fsht_plan* plan, int* maps_per_block, int* threads);
 
-/* Blocks until the plan's stream is idle; returns FSHT_ECUDA on an async error. */
+/* Blocks until the plan's stream is idle; returns FSHT_ECUDA on an async error and
+ * FSHT_ETIMEOUT when a bounded device-side wait (split-precision kernels) expired since
+ * the last check (the error word is then cleared). */
 int fsht_plan_sync(fsht_plan* plan);
+/* The error-word check of fsht_plan_sync without synchronising any stream: call it after
+ * the work of interest is known to be complete (an event, fsht_batch_sync).  No
+ * counterpart in the reference. */
+int fsht_plan_check(fsht_plan* plan);
 
 /* Copies the calling thread's last error message into buf (NUL-terminated);
  * returns its full length. */
