@@ -46,3 +46,37 @@ extern "C" int fsht_measure_fp64_peak(double* tflops) {
   *tflops = 2.0 * 8 * (double)iters * blocks * threads / (best * 1e-3) / 1e12;
   return FSHT_OK;
 }
+
+// ---------------------------------------------------------------- wait self-test
+// One thread waits, with the kernels' bounded mbarrier wait, on a barrier that nothing
+// arrives on: the wait gives up after its iteration limit (about a second), and the
+// kernel raises the plan's error word exactly as an expired wait in the split-precision
+// kernels does.  No fault, no trap, no unbounded loop.
+#include "tcgen05.cuh"
+
+namespace {
+__global__ void k_wait_selftest(int* err) {
+  __shared__ uint64_t bar;
+  __shared__ int abort_flag;
+  if (threadIdx.x == 0) {
+    tc::mbar_init(&bar, 1);
+    abort_flag = 0;
+    tc::mbar_fence_init();
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    if (!tc::mbar_wait(&bar, 0, &abort_flag)) atomicOr(err, 1);
+    tc::mbar_arrive(&bar);   // leave the barrier completed before the CTA exits
+  }
+}
+}  // namespace
+
+extern "C" int fsht_selftest_wait_timeout(fsht_plan* p) {
+  if (!p) {
+    fsht_set_error("null plan");
+    return FSHT_EINVAL;
+  }
+  k_wait_selftest<<<1, 32, 0, p->stream>>>(p->d_err);
+  FSHT_LAUNCH_CHECK();
+  return FSHT_OK;
+}

@@ -229,6 +229,11 @@ int fsht_plan_sync(fsht_plan* plan);
  * the work of interest is known to be complete (an event, fsht_batch_sync).  No
  * counterpart in the reference. */
 int fsht_plan_check(fsht_plan* plan);
+/* Failure-detection self-test: enqueues on the plan's stream one bounded device-side wait
+ * that nothing satisfies; the wait expires (about a second), the plan's error word is
+ * raised, and the next fsht_plan_sync returns FSHT_ETIMEOUT.  No counterpart in the
+ * reference. */
+int fsht_selftest_wait_timeout(fsht_plan* plan);
 
 /* Copies the calling thread's last error message into buf (NUL-terminated);
  * returns its full length. */
