@@ -129,13 +129,27 @@ __device__ void fft_dit_inv(double2* buf, const FshtRingFFT& rf, const FftTw& tw
       const int j = r & (h - 1);
       const int i0 = (blk << logT) + ((r >> lh) << logspan) + j;
       const double2 y0 = buf[sw(i0)];
-      double2 z1 = buf[sw(i0 + h)], z2 = buf[sw(i0 + 2 * h)], z3 = buf[sw(i0 + 3 * h)];
+      const double2 y1 = buf[sw(i0 + h)], y2 = buf[sw(i0 + 2 * h)], y3 = buf[sw(i0 + 3 * h)];
+      double2 sp, dm, e, f;
       if (h > 1) {
-        z1 = cmul(z1, cconj(__ldg(&tw.tw2[(2 * j) << sh])));
-        z2 = cmul(z2, cconj(__ldg(&tw.tw2[j << sh])));
-        z3 = cmul(z3, cconj(__ldg(&tw.tw2[(3 * j) << sh])));
+        // twiddles folded into the adds: sp = y0 + conj(w2) y1 and e = conj(w1) y2 +
+        // conj(w3) y3 as FMA chains, dm = 2 y0 - sp, f = 2 z2 - e (24 FP64 ops, not 28)
+        const double2 w1 = __ldg(&tw.tw2[j << sh]);
+        const double2 w2 = __ldg(&tw.tw2[(2 * j) << sh]);
+        const double2 w3 = __ldg(&tw.tw2[(3 * j) << sh]);
+        sp = make_double2(fma(w2.x, y1.x, fma(w2.y, y1.y, y0.x)),
+                          fma(w2.x, y1.y, fma(-w2.y, y1.x, y0.y)));
+        dm = make_double2(fma(2.0, y0.x, -sp.x), fma(2.0, y0.y, -sp.y));
+        const double2 z2 = cmul(y2, cconj(w1));
+        e = make_double2(fma(w3.x, y3.x, fma(w3.y, y3.y, z2.x)),
+                         fma(w3.x, y3.y, fma(-w3.y, y3.x, z2.y)));
+        f = make_double2(fma(2.0, z2.x, -e.x), fma(2.0, z2.y, -e.y));
+      } else {
+        sp = cadd(y0, y1);
+        dm = csub(y0, y1);
+        e = cadd(y2, y3);
+        f = csub(y2, y3);
       }
-      const double2 sp = cadd(y0, z1), dm = csub(y0, z1), e = cadd(z2, z3), f = csub(z2, z3);
       buf[sw(i0)] = cadd(sp, e);
       buf[sw(i0 + 2 * h)] = csub(sp, e);
       buf[sw(i0 + h)] = make_double2(dm.x - f.y, dm.y + f.x);       // d + i f
