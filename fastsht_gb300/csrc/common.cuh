@@ -111,6 +111,13 @@ struct fsht_plan {
   double2* d_rtw;                  // half-length rings: exp(-2 pi i k / n)
   double2* d_bhat;                 // Bluestein filter spectra
   double2* d_tw;                   // [exp(-2 pi i t / Tmax), t < Tmax][exp(-2 pi i t / P3max), t < P3max]
+  long long fft_chirp_total, fft_bhat_total, fft_rtw_total;   // entries of the three tables
+  // df64 copies (float4 = {re hi, im hi, re lo, im lo}) of the twiddle, chirp, filter and
+  // half-ring tables: split-precision plans only (their forward FFT runs in df64)
+  float4* d_tw_df;
+  float4* d_chirp_df;
+  float4* d_bhat_df;
+  float4* d_rtw_df;
   int Pmax;                        // largest transform size (shared-memory sizing)
   int Tmax, logTmax, P3max;        // twiddle tables: largest power-of-two factor, largest 3*2^k size
   // workspace: phase matrices [m][i][k] x 2 complex, one per buffer
@@ -187,6 +194,13 @@ int fsht_fft_tables_fill(fsht_plan* p, const int* d_blue_rings, int nblue, cudaS
 int fsht_fft_tables_init(fsht_plan* p);
 int fsht_launch_ring_fft_fwd(fsht_plan* p, const double* maps, long long map_stride,
                              int kc, double2* W, cudaStream_t s);
+// df64 tables of a split-precision plan (after fsht_fft_tables_init) and the df64 forward
+// transform, which fsht_launch_ring_fft_fwd selects when they exist.
+int fsht_fft_df_tables_init(fsht_plan* p);
+int fsht_launch_ring_fft_fwd_df(fsht_plan* p, const double* maps, long long map_stride,
+                                int kc, double2* W, cudaStream_t s);
+// Maps per CTA of the ring-FFT launches when the autotuner has not set one.
+int fsht_fft_maps_per_block(int kc, int nrings);
 int fsht_launch_ring_fft_inv(fsht_plan* p, const double2* W, double* maps,
                              long long map_stride, int kc, cudaStream_t s);
 int fsht_launch_fourier_residual(fsht_plan* p, const double2* X, double2* GR, int kc,

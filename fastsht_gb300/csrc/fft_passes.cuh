@@ -1,0 +1,239 @@
+// Shared-memory ring DFT passes, written once for two element types:
+//   double2 - FP64 complex (the plain path; every FP64 operation of the earlier FP64-only
+//             kernels is kept, including the FMA-folded inverse butterflies)
+//   cdd     - df64 complex (df64.cuh), FP64-class accuracy on the FP32 pipe
+// Both are 16 bytes, so shared-memory layouts and sizes do not depend on the type.
+#pragma once
+#include <type_traits>
+
+#include "common.cuh"
+#include "df64.cuh"
+
+// Twiddle tables of one element type: tw2[t] = exp(-2 pi i t / Tmax), t < Tmax (full circle,
+// Tmax the largest power-of-two factor of any transform size), tw3[t] = exp(-2 pi i t / P3max)
+// for the 3*2^k sizes.
+template <class E>
+struct FftTwT {
+  const E* tw2;
+  const E* tw3;
+  int logTmax, P3max;
+};
+using FftTw = FftTwT<double2>;
+
+namespace fftp {
+
+constexpr double kSqrt3Half = 0.86602540378443864676;
+constexpr float kSqrt3HalfHi = (float)kSqrt3Half;
+constexpr float kSqrt3HalfLo = (float)(kSqrt3Half - (double)kSqrt3HalfHi);
+
+__device__ __forceinline__ double2 ldg_e(const double2* p) { return __ldg(p); }
+__device__ __forceinline__ cdd ldg_e(const cdd* p) { return ldg_cdd(p); }
+__device__ __forceinline__ double2 cmulc(double2 a, double2 w) { return cmul(a, cconj(w)); }
+__device__ __forceinline__ double2 cmul_mi(double2 a) { return make_double2(a.y, -a.x); }
+template <class E> __device__ __forceinline__ E zero_e();
+template <> __device__ __forceinline__ double2 zero_e<double2>() { return make_double2(0.0, 0.0); }
+template <> __device__ __forceinline__ cdd zero_e<cdd>() { return cdd_zero(); }
+
+}  // namespace fftp
+
+// Shared-memory position of transform element i: the low three bits of the index (eight
+// 16-byte elements = one 128-byte bank row) are XORed with the next three, so the strided
+// accesses of the radix-4 passes with small spans spread over the banks; a bijection within
+// every block of 64 elements.
+__device__ __forceinline__ int sw(int i) { return i ^ ((i >> 3) & 7); }
+
+// In-place decimation-in-frequency FFT of rf.P points in shared memory, natural order in,
+// transform order out: an optional radix-3 pass (P = 3 T) splits the data into three
+// blocks of T = 2^logT, then radix-4 passes (radix-2^2 butterflies: three twiddles, none
+// in the last pass) and a radix-2 pass when logT is odd.  A power-of-two transform
+// leaves bin q at bit-reverse(q).  All threads of the block call it; it synchronises on
+// entry and after every pass.
+template <class E>
+__device__ void fft_dif(E* buf, const FshtRingFFT& rf, const FftTwT<E>& tw) {
+  using namespace fftp;
+  constexpr bool kF64 = std::is_same<E, double2>::value;
+  const int tid = threadIdx.x, nt = blockDim.x;
+  const int logT = rf.logT, T = 1 << logT;
+  const int nblk = rf.r3 ? 3 : 1;
+  __syncthreads();   // the caller's writes to buf must land first
+  if (rf.r3) {
+    const int sc = tw.P3max / rf.P;
+    for (int j = tid; j < T; j += nt) {
+      const E a = buf[sw(j)], b = buf[sw(j + T)], c = buf[sw(j + 2 * T)];
+      const E sm = cadd(b, c), df = csub(b, c);
+      E y1, y2;
+      // w3 = exp(-2 pi i / 3): a + w3 b + w3^2 c = t - i (sqrt3/2) df, the other t + i ...
+      if constexpr (kF64) {
+        const double2 t = make_double2(fma(-0.5, sm.x, a.x), fma(-0.5, sm.y, a.y));
+        y1 = make_double2(fma(kSqrt3Half, df.y, t.x), fma(-kSqrt3Half, df.x, t.y));
+        y2 = make_double2(fma(-kSqrt3Half, df.y, t.x), fma(kSqrt3Half, df.x, t.y));
+      } else {
+        const cdd t = csub(a, cscale_p2(sm, 0.5f));
+        const cdd u = cmul_pi(cscale_dd(df, kSqrt3HalfHi, kSqrt3HalfLo));
+        y1 = csub(t, u);
+        y2 = cadd(t, u);
+      }
+      buf[sw(j)] = cadd(a, sm);
+      buf[sw(j + T)] = cmul(y1, ldg_e(&tw.tw3[j * sc]));
+      buf[sw(j + 2 * T)] = cmul(y2, ldg_e(&tw.tw3[2 * j * sc]));
+    }
+    __syncthreads();
+  }
+  int logspan = logT;
+  for (; logspan >= 2; logspan -= 2) {
+    const int lh = logspan - 2, h = 1 << lh;
+    const int per_blk = 1 << (logT - 2);
+    const int sh = tw.logTmax - logspan;
+    for (int idx = tid; idx < nblk * per_blk; idx += nt) {
+      const int blk = idx >> (logT - 2);
+      const int r = idx & (per_blk - 1);
+      const int j = r & (h - 1);
+      const int i0 = (blk << logT) + ((r >> lh) << logspan) + j;
+      const E a = buf[sw(i0)], b = buf[sw(i0 + h)], c = buf[sw(i0 + 2 * h)], d = buf[sw(i0 + 3 * h)];
+      const E apc = cadd(a, c), amc = csub(a, c), bpd = cadd(b, d), bmd = csub(b, d);
+      const E y1 = csub(apc, bpd);
+      const E mib = cmul_mi(bmd);
+      const E y2 = cadd(amc, mib);   // (a-c) - i(b-d)
+      const E y3 = csub(amc, mib);   // (a-c) + i(b-d)
+      buf[sw(i0)] = cadd(apc, bpd);
+      if (h == 1) {
+        buf[sw(i0 + h)] = y1;
+        buf[sw(i0 + 2 * h)] = y2;
+        buf[sw(i0 + 3 * h)] = y3;
+      } else {
+        buf[sw(i0 + h)] = cmul(y1, ldg_e(&tw.tw2[(2 * j) << sh]));
+        buf[sw(i0 + 2 * h)] = cmul(y2, ldg_e(&tw.tw2[j << sh]));
+        buf[sw(i0 + 3 * h)] = cmul(y3, ldg_e(&tw.tw2[(3 * j) << sh]));
+      }
+    }
+    __syncthreads();
+  }
+  if (logspan == 1) {
+    for (int idx = tid; idx < nblk << (logT - 1); idx += nt) {
+      const E a = buf[sw(2 * idx)], b = buf[sw(2 * idx + 1)];
+      buf[sw(2 * idx)] = cadd(a, b);
+      buf[sw(2 * idx + 1)] = csub(a, b);
+    }
+    __syncthreads();
+  }
+}
+
+// The inverse of fft_dif without normalisation (P times the inverse DFT): transform order
+// in, natural order out; the passes of fft_dif in reverse with conjugate twiddles.
+template <class E>
+__device__ void fft_dit_inv(E* buf, const FshtRingFFT& rf, const FftTwT<E>& tw) {
+  using namespace fftp;
+  constexpr bool kF64 = std::is_same<E, double2>::value;
+  const int tid = threadIdx.x, nt = blockDim.x;
+  const int logT = rf.logT, T = 1 << logT;
+  const int nblk = rf.r3 ? 3 : 1;
+  __syncthreads();
+  int logspan = 2;
+  if (logT & 1) {
+    for (int idx = tid; idx < nblk << (logT - 1); idx += nt) {
+      const E a = buf[sw(2 * idx)], b = buf[sw(2 * idx + 1)];
+      buf[sw(2 * idx)] = cadd(a, b);
+      buf[sw(2 * idx + 1)] = csub(a, b);
+    }
+    __syncthreads();
+    logspan = 3;
+  }
+  for (; logspan <= logT; logspan += 2) {
+    const int lh = logspan - 2, h = 1 << lh;
+    const int per_blk = 1 << (logT - 2);
+    const int sh = tw.logTmax - logspan;
+    for (int idx = tid; idx < nblk * per_blk; idx += nt) {
+      const int blk = idx >> (logT - 2);
+      const int r = idx & (per_blk - 1);
+      const int j = r & (h - 1);
+      const int i0 = (blk << logT) + ((r >> lh) << logspan) + j;
+      const E y0 = buf[sw(i0)];
+      const E y1 = buf[sw(i0 + h)], y2 = buf[sw(i0 + 2 * h)], y3 = buf[sw(i0 + 3 * h)];
+      E sp, dm, e, f;
+      if (h > 1) {
+        const E w1 = ldg_e(&tw.tw2[j << sh]);
+        const E w2 = ldg_e(&tw.tw2[(2 * j) << sh]);
+        const E w3 = ldg_e(&tw.tw2[(3 * j) << sh]);
+        if constexpr (kF64) {
+          // twiddles folded into the adds: sp = y0 + conj(w2) y1 and e = conj(w1) y2 +
+          // conj(w3) y3 as FMA chains, dm = 2 y0 - sp, f = 2 z2 - e (24 FP64 ops, not 28)
+          sp = make_double2(fma(w2.x, y1.x, fma(w2.y, y1.y, y0.x)),
+                            fma(w2.x, y1.y, fma(-w2.y, y1.x, y0.y)));
+          dm = make_double2(fma(2.0, y0.x, -sp.x), fma(2.0, y0.y, -sp.y));
+          const double2 z2 = cmul(y2, cconj(w1));
+          e = make_double2(fma(w3.x, y3.x, fma(w3.y, y3.y, z2.x)),
+                           fma(w3.x, y3.y, fma(-w3.y, y3.x, z2.y)));
+          f = make_double2(fma(2.0, z2.x, -e.x), fma(2.0, z2.y, -e.y));
+        } else {
+          const E z1 = cmulc(y1, w2), z2 = cmulc(y2, w1), z3 = cmulc(y3, w3);
+          sp = cadd(y0, z1);
+          dm = csub(y0, z1);
+          e = cadd(z2, z3);
+          f = csub(z2, z3);
+        }
+      } else {
+        sp = cadd(y0, y1);
+        dm = csub(y0, y1);
+        e = cadd(y2, y3);
+        f = csub(y2, y3);
+      }
+      const E mif = cmul_mi(f);
+      buf[sw(i0)] = cadd(sp, e);
+      buf[sw(i0 + 2 * h)] = csub(sp, e);
+      buf[sw(i0 + h)] = csub(dm, mif);       // d + i f
+      buf[sw(i0 + 3 * h)] = cadd(dm, mif);   // d - i f
+    }
+    __syncthreads();
+  }
+  if (rf.r3) {
+    const int sc = tw.P3max / rf.P;
+    for (int j = tid; j < T; j += nt) {
+      const E a = buf[sw(j)];
+      const E b = cmulc(buf[sw(j + T)], ldg_e(&tw.tw3[j * sc]));
+      const E c = cmulc(buf[sw(j + 2 * T)], ldg_e(&tw.tw3[2 * j * sc]));
+      const E sm = cadd(b, c), df = csub(b, c);
+      buf[sw(j)] = cadd(a, sm);
+      if constexpr (kF64) {
+        const double2 t = make_double2(fma(-0.5, sm.x, a.x), fma(-0.5, sm.y, a.y));
+        buf[sw(j + T)] = make_double2(fma(-kSqrt3Half, df.y, t.x), fma(kSqrt3Half, df.x, t.y));
+        buf[sw(j + 2 * T)] = make_double2(fma(kSqrt3Half, df.y, t.x), fma(-kSqrt3Half, df.x, t.y));
+      } else {
+        const cdd t = csub(a, cscale_p2(sm, 0.5f));
+        const cdd u = cmul_pi(cscale_dd(df, kSqrt3HalfHi, kSqrt3HalfLo));
+        buf[sw(j + T)] = cadd(t, u);
+        buf[sw(j + 2 * T)] = csub(t, u);
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// Where bin q of ring_dft's output sits in buf.
+__device__ __forceinline__ int dft_bin(const FshtRingFFT& rf, int q) {
+  return rf.bluestein ? q : (int)(__brev((unsigned)q) >> (32 - rf.logT));
+}
+
+// DFT of rf.nd points (in buf[0..nd)), forward (e^{-2 pi i jk/nd}); bin q lands at
+// buf[dft_bin(rf, q)].  A power-of-two ring is one fft_dif; any other length uses
+// Bluestein with the ring's chirp and filter spectrum (transform order, divided by P):
+// chirp, fft_dif, filter, fft_dit_inv, chirp, natural order out.
+template <class E>
+__device__ void ring_dft(E* buf, const FshtRingFFT& rf, const FftTwT<E>& tw,
+                         const E* __restrict__ chirp, const E* __restrict__ bhat) {
+  using namespace fftp;
+  const int tid = threadIdx.x, nt = blockDim.x;
+  if (!rf.bluestein) {
+    fft_dif(buf, rf, tw);
+    return;
+  }
+  const int n = rf.nd, P = rf.P;
+  for (int j = tid; j < P; j += nt) {
+    if (j < n) buf[sw(j)] = cmul(buf[sw(j)], ldg_e(&chirp[j]));
+    else buf[sw(j)] = zero_e<E>();
+  }
+  fft_dif(buf, rf, tw);
+  for (int j = tid; j < P; j += nt) buf[sw(j)] = cmul(buf[sw(j)], ldg_e(&bhat[j]));
+  fft_dit_inv(buf, rf, tw);
+  for (int j = tid; j < n; j += nt) buf[sw(j)] = cmul(buf[sw(j)], ldg_e(&chirp[j]));
+  __syncthreads();
+}

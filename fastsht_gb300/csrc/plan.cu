@@ -83,6 +83,10 @@ void free_plan_memory(fsht_plan* p) {
   cudaFree(p->d_rtw);
   cudaFree(p->d_bhat);
   cudaFree(p->d_tw);
+  cudaFree(p->d_tw_df);
+  cudaFree(p->d_chirp_df);
+  cudaFree(p->d_bhat_df);
+  cudaFree(p->d_rtw_df);
   cudaFree(p->d_work);
   cudaFree(p->d_err);
   cudaFree(p->d_ws);
@@ -266,6 +270,7 @@ int fsht_plan_create(int nside, int lmax, int nmaps_max, int flags, int precisio
   }
   if ((rc = fsht_launch_ring_skip(p, p->stream))) return fail(rc);
   if ((rc = fsht_fft_tables_init(p))) return fail(rc);
+  if (precision == FSHT_PREC_SPLIT && (rc = fsht_fft_df_tables_init(p))) return fail(rc);
   if (precision == FSHT_PREC_SPLIT && (rc = fsht_split_tables_init(p))) return fail(rc);
   if (precision == FSHT_PREC_SPLIT && p->pol && (rc = fsht_split_pol_tables_init(p)))
     return fail(rc);

@@ -15,191 +15,12 @@
 // The equator ring (i = 2 nside - 1) is its own mirror: S = D = F_m, and only
 // G_m(i) is used.
 #include "common.cuh"
+#include "fft_passes.cuh"
 #include <cmath>
 #include <vector>
 #include <climits>
 
 namespace {
-
-// Twiddle tables: tw2[t] = exp(-2 pi i t / Tmax), t < Tmax (full circle, Tmax the largest
-// power-of-two factor of any transform size), tw3[t] = exp(-2 pi i t / P3max) for the
-// 3*2^k sizes.
-struct FftTw {
-  const double2* tw2;
-  const double2* tw3;
-  int logTmax, P3max;
-};
-
-constexpr double kSqrt3Half = 0.86602540378443864676;
-
-// Shared-memory position of transform element i: the low three bits of the index (eight
-// 16-byte elements = one 128-byte bank row) are XORed with the next three, so the strided
-// accesses of the radix-4 passes with small spans spread over the banks; a bijection within
-// every block of 64 elements.
-__device__ __forceinline__ int sw(int i) { return i ^ ((i >> 3) & 7); }
-
-// In-place decimation-in-frequency FFT of rf.P points in shared memory, natural order in,
-// transform order out: an optional radix-3 pass (P = 3 T) splits the data into three
-// blocks of T = 2^logT, then radix-4 passes (radix-2^2 butterflies: three twiddles, none
-// in the last pass) and a radix-2 pass when logT is odd.  A power-of-two transform
-// leaves bin q at bit-reverse(q).  All threads of the block call it; it synchronises on
-// entry and after every pass.
-__device__ void fft_dif(double2* buf, const FshtRingFFT& rf, const FftTw& tw) {
-  const int tid = threadIdx.x, nt = blockDim.x;
-  const int logT = rf.logT, T = 1 << logT;
-  const int nblk = rf.r3 ? 3 : 1;
-  __syncthreads();   // the caller's writes to buf must land first
-  if (rf.r3) {
-    const int sc = tw.P3max / rf.P;
-    for (int j = tid; j < T; j += nt) {
-      const double2 a = buf[sw(j)], b = buf[sw(j + T)], c = buf[sw(j + 2 * T)];
-      const double2 sm = cadd(b, c), df = csub(b, c);
-      const double2 t = make_double2(fma(-0.5, sm.x, a.x), fma(-0.5, sm.y, a.y));
-      // w3 = exp(-2 pi i / 3): a + w3 b + w3^2 c = t - i (sqrt3/2) df, the other t + i ...
-      const double2 y1 = make_double2(fma(kSqrt3Half, df.y, t.x), fma(-kSqrt3Half, df.x, t.y));
-      const double2 y2 = make_double2(fma(-kSqrt3Half, df.y, t.x), fma(kSqrt3Half, df.x, t.y));
-      buf[sw(j)] = cadd(a, sm);
-      buf[sw(j + T)] = cmul(y1, __ldg(&tw.tw3[j * sc]));
-      buf[sw(j + 2 * T)] = cmul(y2, __ldg(&tw.tw3[2 * j * sc]));
-    }
-    __syncthreads();
-  }
-  int logspan = logT;
-  for (; logspan >= 2; logspan -= 2) {
-    const int lh = logspan - 2, h = 1 << lh;
-    const int per_blk = 1 << (logT - 2);
-    const int sh = tw.logTmax - logspan;
-    for (int idx = tid; idx < nblk * per_blk; idx += nt) {
-      const int blk = idx >> (logT - 2);
-      const int r = idx & (per_blk - 1);
-      const int j = r & (h - 1);
-      const int i0 = (blk << logT) + ((r >> lh) << logspan) + j;
-      const double2 a = buf[sw(i0)], b = buf[sw(i0 + h)], c = buf[sw(i0 + 2 * h)], d = buf[sw(i0 + 3 * h)];
-      const double2 apc = cadd(a, c), amc = csub(a, c), bpd = cadd(b, d), bmd = csub(b, d);
-      const double2 y1 = csub(apc, bpd);
-      const double2 y2 = make_double2(amc.x + bmd.y, amc.y - bmd.x);   // (a-c) - i(b-d)
-      const double2 y3 = make_double2(amc.x - bmd.y, amc.y + bmd.x);   // (a-c) + i(b-d)
-      buf[sw(i0)] = cadd(apc, bpd);
-      if (h == 1) {
-        buf[sw(i0 + h)] = y1;
-        buf[sw(i0 + 2 * h)] = y2;
-        buf[sw(i0 + 3 * h)] = y3;
-      } else {
-        buf[sw(i0 + h)] = cmul(y1, __ldg(&tw.tw2[(2 * j) << sh]));
-        buf[sw(i0 + 2 * h)] = cmul(y2, __ldg(&tw.tw2[j << sh]));
-        buf[sw(i0 + 3 * h)] = cmul(y3, __ldg(&tw.tw2[(3 * j) << sh]));
-      }
-    }
-    __syncthreads();
-  }
-  if (logspan == 1) {
-    for (int idx = tid; idx < nblk << (logT - 1); idx += nt) {
-      const double2 a = buf[sw(2 * idx)], b = buf[sw(2 * idx + 1)];
-      buf[sw(2 * idx)] = cadd(a, b);
-      buf[sw(2 * idx + 1)] = csub(a, b);
-    }
-    __syncthreads();
-  }
-}
-
-// The inverse of fft_dif without normalisation (P times the inverse DFT): transform order
-// in, natural order out; the passes of fft_dif in reverse with conjugate twiddles.
-__device__ void fft_dit_inv(double2* buf, const FshtRingFFT& rf, const FftTw& tw) {
-  const int tid = threadIdx.x, nt = blockDim.x;
-  const int logT = rf.logT, T = 1 << logT;
-  const int nblk = rf.r3 ? 3 : 1;
-  __syncthreads();
-  int logspan = 2;
-  if (logT & 1) {
-    for (int idx = tid; idx < nblk << (logT - 1); idx += nt) {
-      const double2 a = buf[sw(2 * idx)], b = buf[sw(2 * idx + 1)];
-      buf[sw(2 * idx)] = cadd(a, b);
-      buf[sw(2 * idx + 1)] = csub(a, b);
-    }
-    __syncthreads();
-    logspan = 3;
-  }
-  for (; logspan <= logT; logspan += 2) {
-    const int lh = logspan - 2, h = 1 << lh;
-    const int per_blk = 1 << (logT - 2);
-    const int sh = tw.logTmax - logspan;
-    for (int idx = tid; idx < nblk * per_blk; idx += nt) {
-      const int blk = idx >> (logT - 2);
-      const int r = idx & (per_blk - 1);
-      const int j = r & (h - 1);
-      const int i0 = (blk << logT) + ((r >> lh) << logspan) + j;
-      const double2 y0 = buf[sw(i0)];
-      const double2 y1 = buf[sw(i0 + h)], y2 = buf[sw(i0 + 2 * h)], y3 = buf[sw(i0 + 3 * h)];
-      double2 sp, dm, e, f;
-      if (h > 1) {
-        // twiddles folded into the adds: sp = y0 + conj(w2) y1 and e = conj(w1) y2 +
-        // conj(w3) y3 as FMA chains, dm = 2 y0 - sp, f = 2 z2 - e (24 FP64 ops, not 28)
-        const double2 w1 = __ldg(&tw.tw2[j << sh]);
-        const double2 w2 = __ldg(&tw.tw2[(2 * j) << sh]);
-        const double2 w3 = __ldg(&tw.tw2[(3 * j) << sh]);
-        sp = make_double2(fma(w2.x, y1.x, fma(w2.y, y1.y, y0.x)),
-                          fma(w2.x, y1.y, fma(-w2.y, y1.x, y0.y)));
-        dm = make_double2(fma(2.0, y0.x, -sp.x), fma(2.0, y0.y, -sp.y));
-        const double2 z2 = cmul(y2, cconj(w1));
-        e = make_double2(fma(w3.x, y3.x, fma(w3.y, y3.y, z2.x)),
-                         fma(w3.x, y3.y, fma(-w3.y, y3.x, z2.y)));
-        f = make_double2(fma(2.0, z2.x, -e.x), fma(2.0, z2.y, -e.y));
-      } else {
-        sp = cadd(y0, y1);
-        dm = csub(y0, y1);
-        e = cadd(y2, y3);
-        f = csub(y2, y3);
-      }
-      buf[sw(i0)] = cadd(sp, e);
-      buf[sw(i0 + 2 * h)] = csub(sp, e);
-      buf[sw(i0 + h)] = make_double2(dm.x - f.y, dm.y + f.x);       // d + i f
-      buf[sw(i0 + 3 * h)] = make_double2(dm.x + f.y, dm.y - f.x);   // d - i f
-    }
-    __syncthreads();
-  }
-  if (rf.r3) {
-    const int sc = tw.P3max / rf.P;
-    for (int j = tid; j < T; j += nt) {
-      const double2 a = buf[sw(j)];
-      const double2 b = cmul(buf[sw(j + T)], cconj(__ldg(&tw.tw3[j * sc])));
-      const double2 c = cmul(buf[sw(j + 2 * T)], cconj(__ldg(&tw.tw3[2 * j * sc])));
-      const double2 sm = cadd(b, c), df = csub(b, c);
-      const double2 t = make_double2(fma(-0.5, sm.x, a.x), fma(-0.5, sm.y, a.y));
-      buf[sw(j)] = cadd(a, sm);
-      buf[sw(j + T)] = make_double2(fma(-kSqrt3Half, df.y, t.x), fma(kSqrt3Half, df.x, t.y));
-      buf[sw(j + 2 * T)] = make_double2(fma(kSqrt3Half, df.y, t.x), fma(-kSqrt3Half, df.x, t.y));
-    }
-    __syncthreads();
-  }
-}
-
-// Where bin q of ring_dft's output sits in buf.
-__device__ __forceinline__ int dft_bin(const FshtRingFFT& rf, int q) {
-  return rf.bluestein ? q : (int)(__brev((unsigned)q) >> (32 - rf.logT));
-}
-
-// DFT of rf.nd points (in buf[0..nd)), forward (e^{-2 pi i jk/nd}); bin q lands at
-// buf[dft_bin(rf, q)].  A power-of-two ring is one fft_dif; any other length uses
-// Bluestein with the ring's chirp and filter spectrum (transform order, divided by P):
-// chirp, fft_dif, filter, fft_dit_inv, chirp, natural order out.
-__device__ void ring_dft(double2* buf, const FshtRingFFT& rf, const FftTw& tw,
-                         const double2* __restrict__ chirp, const double2* __restrict__ bhat) {
-  const int tid = threadIdx.x, nt = blockDim.x;
-  if (!rf.bluestein) {
-    fft_dif(buf, rf, tw);
-    return;
-  }
-  const int n = rf.nd, P = rf.P;
-  for (int j = tid; j < P; j += nt) {
-    if (j < n) buf[sw(j)] = cmul(buf[sw(j)], __ldg(&chirp[j]));
-    else buf[sw(j)] = make_double2(0.0, 0.0);
-  }
-  fft_dif(buf, rf, tw);
-  for (int j = tid; j < P; j += nt) buf[sw(j)] = cmul(buf[sw(j)], __ldg(&bhat[j]));
-  fft_dit_inv(buf, rf, tw);
-  for (int j = tid; j < n; j += nt) buf[sw(j)] = cmul(buf[sw(j)], __ldg(&chirp[j]));
-  __syncthreads();
-}
 
 // ------------------------------------------------------------------ tables
 __global__ void k_twiddles(double2* tw, int Tmax, int P3max) {
@@ -650,6 +471,8 @@ int maps_per_block_for(int kc, int nrings_launched) {
 
 }  // namespace
 
+int fsht_fft_maps_per_block(int kc, int nrings) { return maps_per_block_for(kc, nrings); }
+
 // ================================================================== host side
 int fsht_fft_layout(int nside, int lmax, FshtFftLayout* lay, FshtRingFFT* rfs, int* blue_rings) {
   const int nn = 2 * nside;
@@ -760,6 +583,9 @@ int fsht_fft_tables_init(fsht_plan* p) {
   p->logTmax = lay.logTmax;
   p->P3max = lay.P3max;
   p->fft_smem = lay.smem;
+  p->fft_chirp_total = lay.chirp_total;
+  p->fft_bhat_total = lay.bhat_total;
+  p->fft_rtw_total = lay.rtw_total;
   FSHT_CUDA_TRY(cudaMalloc(&p->d_rfft, sizeof(FshtRingFFT) * nn));
   FSHT_CUDA_TRY(cudaMemcpyAsync(p->d_rfft, rfs.data(), sizeof(FshtRingFFT) * nn,
                                 cudaMemcpyHostToDevice, p->stream));
@@ -803,6 +629,7 @@ int fsht_launch_ring_skip(fsht_plan* p, cudaStream_t s) {
 
 int fsht_launch_ring_fft_fwd(fsht_plan* p, const double* maps, long long map_stride, int kc,
                              double2* W, cudaStream_t s) {
+  if (p->d_tw_df) return fsht_launch_ring_fft_fwd_df(p, maps, map_stride, kc, W, s);
   FwdArgs a;
   a.maps = maps;
   a.map_stride = map_stride;

@@ -1,0 +1,240 @@
+// Ring FFTs of the split-precision form in df64 arithmetic (df64.cuh).
+//
+// Same transform, layout and output as the FP64 kernels of ring_fft.cu (the reference's
+// map2fft + fft2mat_fast, src/compute_fft.f90:15-280 and src/fft_mapping.f90:19-140): per ring
+// pair the packed N + iS DFT, then per m the aliased bin times e^{-i m phi0}, written as
+// {S, D} = {F_N + F_S, F_N - F_S} in FP64.  Only the arithmetic differs: each (ring pair, map)
+// is scaled by a power of two so that its largest value lies in [1, 2), converted to df64 by
+// bit manipulation, transformed on the FP32 pipe (GB300: 64 times the FP64 instruction rate)
+// with df64 twiddles, chirps and filter spectra, and converted back with one FP64 addition per
+// output value.  The transform's error is about 2^-44 of the ring's largest value, far below
+// the split contraction's digit resolution (2^-31 of the column maximum).
+#include "common.cuh"
+#include "fft_passes.cuh"
+
+#include <cmath>
+
+namespace {
+
+struct FwdDfArgs {
+  const double* maps;       // chunk base: map k at maps + k * map_stride
+  long long map_stride;
+  int kc, maps_per_block;
+  int nside, lmax, nnorth, nring, ring_base;
+  const FshtRingFFT* rfs;
+  FftTwT<cdd> tw;
+  const cdd* chirp;
+  const cdd* bhat;
+  const cdd* rtw;
+  const int* ring_i0;
+  double2* W;
+};
+
+__device__ __forceinline__ cdd cdd_from_fp64(double re, double im) {
+  cdd r;
+  r.h.x = __double2float_rn(re);
+  r.h.y = __double2float_rn(im);
+  r.l.x = __double2float_rn(re - (double)r.h.x);
+  r.l.y = __double2float_rn(im - (double)r.h.y);
+  return r;
+}
+
+__device__ __forceinline__ cdd cdd_from_raw(double2 v, int sh) {
+  const float2 re = dd_from_double(v.x, sh), im = dd_from_double(v.y, sh);
+  cdd r;
+  r.h = make_float2(re.x, im.x);
+  r.l = make_float2(re.y, im.y);
+  return r;
+}
+
+__device__ __forceinline__ double2 cdd_to_fp64(cdd v, int sh) {
+  return make_double2(dd_to_double(v.h.x, v.l.x, sh), dd_to_double(v.h.y, v.l.y, sh));
+}
+
+// Loads one ring pair (or one half-length ring) of map values into the FFT buffer's slots as
+// raw FP64 pairs, takes the block-wide largest exponent field, then converts every slot to
+// df64 scaled by 2^-sh (sh = that exponent, unbiased; 0 for an all-zero ring).  Thread t owns
+// slots t, t + nt, ... in both passes, so only the exponent needs a barrier.  emax is a
+// shared slot that is zero on entry.  Returns sh.
+__device__ __forceinline__ int load_scaled(cdd* buf, int cnt, const double* xa, const double* xb,
+                                           int stride, int* emax) {
+  double2* raw = reinterpret_cast<double2*>(buf);
+  const int tid = threadIdx.x, nt = blockDim.x;
+  int em = 0;
+  for (int j = tid; j < cnt; j += nt) {
+    const double va = __ldg(&xa[(long long)stride * j]);
+    const double vb = xb ? __ldg(&xb[(long long)stride * j]) : 0.0;
+    em = max(em, max(dd_exp_field(va), dd_exp_field(vb)));
+    raw[sw(j)] = make_double2(va, vb);
+  }
+  em = __reduce_max_sync(0xffffffffu, em);
+  if ((tid & 31) == 0) atomicMax(emax, em);
+  __syncthreads();
+  const int e = *emax;
+  const int sh = (e == 0 || e == 0x7ff) ? 0 : e - 1023;
+  for (int j = tid; j < cnt; j += nt) buf[sw(j)] = cdd_from_raw(raw[sw(j)], sh);
+  return sh;
+}
+
+__global__ void __launch_bounds__(512, 2) k_ring_fft_fwd_df(FwdDfArgs a) {
+  extern __shared__ float4 smem4[];
+  __shared__ int s_emax[2];
+  const int i = a.ring_base + blockIdx.x;      // north ring index
+  const FshtRingFFT rf = a.rfs[i];
+  const int n = rf.n;
+  cdd* buf = reinterpret_cast<cdd*>(smem4);    // rf.P entries
+  cdd* ph = buf + rf.P;                        // lmax+1 phase factors exp(-i m phi0) / 2
+  const int tid = threadIdx.x, nt = blockDim.x;
+  const bool equator = (i == a.nnorth - 1);
+  const int ip = a.nring - 1 - i;
+  const long long off_n = ring_start(a.nside, i);
+  const long long off_s = ring_start(a.nside, ip);
+  const int sflag = ring_phase_flag(a.nside, i);
+  int mtop = a.lmax;
+  while (mtop >= 0 && a.ring_i0[mtop] > i) --mtop;
+  for (int m = tid; m <= mtop; m += nt) {
+    double s = 0.0, c = 1.0;
+    if (sflag) {
+      long long r = (long long)m % (2LL * n);
+      sincospi(-(double)r / (double)n, &s, &c);
+    }
+    ph[m] = cdd_from_fp64(0.5 * c, 0.5 * s);   // the 1/2 of the N/S split folded in
+  }
+  if (tid < 2) s_emax[tid] = 0;
+  const int k_begin = blockIdx.y * a.maps_per_block;
+  const int k_end = min(a.kc, k_begin + a.maps_per_block);
+  const cdd* chirp = a.chirp + rf.chirp_off;
+  const cdd* bhat = a.bhat + rf.bhat_off;
+  int it = 0;   // exponent slot parity: slot it & 1 collects, the other is reset
+  if (rf.nd != n) {
+    // Half-length ring (never the equator): each ring as z_j = x_{2j} + i x_{2j+1},
+    // Z = DFT_nd(z), X_q = E_q + e^{-2 pi i q/n} O_q (see the FP64 kernel); the north ring
+    // writes {F_N, F_N}, the south ring adds +-F_S in FP64.
+    const int nd = rf.nd;
+    const cdd* rtw = a.rtw + rf.rtw_off;
+    for (int k = k_begin; k < k_end; ++k) {
+      for (int side = 0; side < 2; ++side, ++it) {
+        const double* x = a.maps + (long long)k * a.map_stride + (side ? off_s : off_n);
+        __syncthreads();
+        if (tid == 0) s_emax[(it & 1) ^ 1] = 0;
+        const int sh = load_scaled(buf, nd, x, x + 1, 2, &s_emax[it & 1]);
+        ring_dft(buf, rf, a.tw, chirp, bhat);
+        for (int m = tid; m <= mtop; m += nt) {
+          const int q = m % n;
+          const bool cj = q > nd;
+          const int kk = cj ? n - q : q;
+          const cdd za = buf[sw(dft_bin(rf, kk == nd ? 0 : kk))];
+          const cdd zb = cconj(buf[sw(dft_bin(rf, kk == 0 ? 0 : nd - kk))]);
+          const cdd e = cadd(za, zb);                          // 2 E
+          const cdd o = cmul_mi(csub(za, zb));                 // 2 O
+          cdd xq = cadd(e, cmul(o, ldg_cdd(&rtw[kk])));        // 2 X
+          if (cj) xq = cconj(xq);
+          const double2 f = cdd_to_fp64(cmul(xq, ph[m]), sh);
+          double2* w = a.W + (((long long)m * a.nnorth + i) * a.kc + k) * 2;
+          if (side == 0) {
+            w[0] = f;
+            w[1] = f;
+          } else {
+            w[0] = cadd(w[0], f);
+            w[1] = csub(w[1], f);
+          }
+        }
+      }
+    }
+    return;
+  }
+  for (int k = k_begin; k < k_end; ++k, ++it) {
+    const double* xn = a.maps + (long long)k * a.map_stride + off_n;
+    const double* xs = a.maps + (long long)k * a.map_stride + off_s;
+    __syncthreads();   // the previous map's readers of buf and of the other slot are done
+    if (tid == 0) s_emax[(it & 1) ^ 1] = 0;
+    const int sh = load_scaled(buf, n, xn, equator ? nullptr : xs, 1, &s_emax[it & 1]);
+    ring_dft(buf, rf, a.tw, chirp, bhat);
+    // Z = FFT(x_N + i x_S): X_N[q] = (Z[q] + conj Z[-q])/2, X_S[q] = (Z[q] - conj Z[-q])/(2i)
+    for (int m = tid; m <= mtop; m += nt) {
+      const int q = m % n;
+      const int qn = (q == 0) ? 0 : n - q;
+      const cdd zq = buf[sw(dft_bin(rf, q))];
+      const cdd zn = cconj(buf[sw(dft_bin(rf, qn))]);
+      const cdd xN = cadd(zq, zn);                             // 2 X_N
+      const cdd xS = cmul_mi(csub(zq, zn));                    // 2 X_S
+      const cdd p = ph[m];
+      double2* w = a.W + (((long long)m * a.nnorth + i) * a.kc + k) * 2;
+      if (equator) {
+        const double2 fN = cdd_to_fp64(cmul(xN, p), sh);
+        w[0] = fN;
+        w[1] = fN;
+      } else {
+        w[0] = cdd_to_fp64(cmul(cadd(xN, xS), p), sh);        // F_N + F_S
+        w[1] = cdd_to_fp64(cmul(csub(xN, xS), p), sh);        // F_N - F_S
+      }
+    }
+  }
+}
+
+__global__ void k_to_cdd(const double2* __restrict__ in, float4* out, long long n) {
+  for (long long j = blockIdx.x * (long long)blockDim.x + threadIdx.x; j < n;
+       j += (long long)gridDim.x * blockDim.x) {
+    const double2 v = in[j];
+    const cdd c = cdd_from_fp64(v.x, v.y);
+    out[j] = make_float4(c.h.x, c.h.y, c.l.x, c.l.y);
+  }
+}
+
+int to_cdd(const double2* in, float4** out, long long n, cudaStream_t s) {
+  const long long cnt = n > 0 ? n : 1;
+  FSHT_CUDA_TRY(cudaMalloc(out, sizeof(float4) * cnt));
+  if (n > 0) {
+    long long g = (n + 255) / 256;
+    if (g > 4096) g = 4096;
+    k_to_cdd<<<(unsigned)g, 256, 0, s>>>(in, *out, n);
+    FSHT_LAUNCH_CHECK();
+  }
+  return FSHT_OK;
+}
+
+}  // namespace
+
+int fsht_fft_df_tables_init(fsht_plan* p) {
+  FSHT_TRY(to_cdd(p->d_tw, &p->d_tw_df, (long long)p->Tmax + p->P3max, p->stream));
+  FSHT_TRY(to_cdd(p->d_chirp, &p->d_chirp_df, p->fft_chirp_total, p->stream));
+  FSHT_TRY(to_cdd(p->d_bhat, &p->d_bhat_df, p->fft_bhat_total, p->stream));
+  FSHT_TRY(to_cdd(p->d_rtw, &p->d_rtw_df, p->fft_rtw_total, p->stream));
+  FSHT_CUDA_TRY(cudaStreamSynchronize(p->stream));
+  return FSHT_OK;
+}
+
+int fsht_launch_ring_fft_fwd_df(fsht_plan* p, const double* maps, long long map_stride, int kc,
+                                double2* W, cudaStream_t s) {
+  FwdDfArgs a;
+  a.maps = maps;
+  a.map_stride = map_stride;
+  a.kc = kc;
+  a.nside = p->nside;
+  a.lmax = p->lmax;
+  a.nnorth = p->nnorth;
+  a.nring = p->nring;
+  a.ring_base = 0;
+  a.rfs = p->d_rfft;
+  a.tw.tw2 = reinterpret_cast<const cdd*>(p->d_tw_df);
+  a.tw.tw3 = reinterpret_cast<const cdd*>(p->d_tw_df) + p->Tmax;
+  a.tw.logTmax = p->logTmax;
+  a.tw.P3max = p->P3max;
+  a.chirp = reinterpret_cast<const cdd*>(p->d_chirp_df);
+  a.bhat = reinterpret_cast<const cdd*>(p->d_bhat_df);
+  a.rtw = reinterpret_cast<const cdd*>(p->d_rtw_df);
+  a.ring_i0 = p->d_ring_i0;
+  a.W = W;
+  a.maps_per_block = p->fft_mpb > 0 ? p->fft_mpb : fsht_fft_maps_per_block(kc, p->nnorth);
+  FSHT_CUDA_TRY(cudaFuncSetAttribute(k_ring_fft_fwd_df,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)p->fft_smem));
+  for (int sgi = 0; sgi < p->fft_nseg; ++sgi) {
+    const long long* sg = p->fft_seg + 3 * sgi;
+    a.ring_base = (int)sg[0];
+    dim3 grid((unsigned)(sg[1] - sg[0]), (kc + a.maps_per_block - 1) / a.maps_per_block);
+    k_ring_fft_fwd_df<<<grid, p->fft_threads > 0 ? p->fft_threads : 512, (size_t)sg[2], s>>>(a);
+    FSHT_LAUNCH_CHECK();
+  }
+  return FSHT_OK;
+}
