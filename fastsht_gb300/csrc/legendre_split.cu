@@ -79,11 +79,17 @@ __global__ void __launch_bounds__(256) k_slice_phase(SliceArgs a) {
   unsigned char* base = a.WS + ((size_t)(qi * 2 + p) * a.ngroups + g) * a.row_bytes +
                         (c >> 3) * 256 + (c & 7) * 16;
   for (int ts = 0; ts < nks; ++ts) {
+    // the k-step's 16 loads issued together (the column is not in L2 any more)
+    double v[kKStep];
+#pragma unroll
+    for (int u = 0; u < kKStep; ++u) v[u] = val(ts * kKStep + u);
+#pragma unroll
     for (int half = 0; half < 2; ++half) {
       uint16_t sl[kSlices][8];
+#pragma unroll
       for (int j = 0; j < 8; ++j) {
         uint16_t q4[4] = {0, 0, 0, 0};
-        if (E != kEmptyExp) tc::digits4(val(ts * kKStep + half * 8 + j), E, q4);
+        if (E != kEmptyExp) tc::digits4(v[half * 8 + j], E, q4);
         for (int d = 0; d < kSlices; ++d) sl[d][j] = q4[d];
       }
       for (int d = 0; d < kSlices; ++d) {
