@@ -104,6 +104,66 @@ def fft_dp_ops_per_map(nside):
     return total
 
 
+def fft_df_instr_per_map(nside):
+    """FP32-pipe instructions (FADD / FMUL / FFMA) of the df64 arithmetic one forward ring FFT
+    pass executes per map in the split form (k_ring_fft_fwd_df), counted from the kernel's
+    operations: a lazy df64 complex addition 16, a lazy complex product 32, the
+    renormalisation of a stored value 6.  Radix-4 butterfly 248 (152 without twiddles, 184 in
+    Bluestein's zero-padded first pass, 204 in its last inverse pass that keeps two outputs);
+    radix-2 44; radix-3 196 (164 / 174 in the pruned first / last passes); Bluestein chirps
+    and filter 38 per point.  Load/store, index and FP64<->df64 conversion instructions are
+    left out, as are the fold and phase (the same scope as fft_dp_ops_per_map)."""
+    def size(n):
+        if n & (n - 1) == 0:
+            return n, 0
+        need = 2 * n - 1
+        p2 = 1 << (need - 1).bit_length()
+        p3 = 3
+        while p3 < need:
+            p3 *= 2
+        return (p3, 1) if p3 < p2 else (p2, 0)
+
+    def dif(P, r3, pruned):
+        T = P // 3 if r3 else P
+        nblk = 3 if r3 else 1
+        ops = (164 if pruned else 196) * T if r3 else 0
+        L = T.bit_length() - 1
+        first = True
+        while L >= 2:
+            bf = 152 if L == 2 else (184 if (pruned and first and not r3) else 248)
+            ops += nblk * (T // 4) * bf
+            L -= 2
+            first = False
+        if L == 1:
+            ops += nblk * (T // 2) * 44
+        return ops
+
+    def dit(P, r3):
+        T = P // 3 if r3 else P
+        nblk = 3 if r3 else 1
+        L = T.bit_length() - 1
+        ops = nblk * (T // 2) * 44 if L & 1 else 0
+        span = 3 if L & 1 else 2
+        while span <= L:
+            last = span == L and not r3
+            bf = 152 if span == 2 else (204 if last else 248)
+            ops += nblk * (T // 4) * bf
+            span += 2
+        if r3:
+            ops += 174 * T
+        return ops
+
+    total = 0
+    for i in range(2 * nside):
+        n = 4 * (i + 1) if i < nside else 4 * nside
+        P, r3 = size(n)
+        if P == n:
+            total += dif(P, 0, False)
+        else:
+            total += dif(P, r3, True) + dit(P, r3) + 38 * P + 2 * 38 * n
+    return total
+
+
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -281,7 +341,8 @@ def reference_arm(args, rank, world):
 
 
 def workload_config(args):
-    method = ("split-precision form (BF16 digit UMMAs on tcgen05, FP64 recursion and FFT)"
+    method = ("split-precision form (BF16 digit UMMAs on tcgen05, FP64 recursion, "
+              "ring FFT in df64 = FP32-pair arithmetic)"
               if getattr(args, "precision", "fp64") == "split" else "plain FP64 method")
     return {"workload": (f"t2alm (map2alm) of {args.nmaps} T maps per GPU, nside {args.nside}, "
                          f"lmax {args.lmax}, {method}"),
@@ -361,6 +422,8 @@ def ours(args, rank, world, local):
     npix = 12 * nside * nside
     peak64 = C.c_double()
     _lib.call("fsht_measure_fp64_peak", C.byref(peak64))
+    peak32 = C.c_double()
+    _lib.call("fsht_measure_fp32_peak", C.byref(peak32))
     peaks = {}
     pk = ROOT / "MEASURED_PEAKS.json"
     if pk.exists():
@@ -392,7 +455,8 @@ def ours(args, rank, world, local):
     fft_traffic = None
     tf_fft = ROOT / "profiles" / "traffic.json"
     if tf_fft.exists():
-        tr = json.loads(tf_fft.read_text()).get("ring_fft_fwd")
+        tr = json.loads(tf_fft.read_text()).get(
+            "ring_fft_fwd_df" if args.precision == "split" else "ring_fft_fwd")
         if tr and tr.get("bytes_per_map"):
             fft_traffic = tr["bytes_per_map"] * kchunk
     roof_fft = {"bound": "fp64", "kernel": "k_ring_fft_fwd",
@@ -406,7 +470,27 @@ def ours(args, rank, world, local):
                 "hbm": {"achieved_gbs": fft_bytes / (fft_ms / 1000.0) / 1e9 if fft_ms > 0 else None,
                         "peak_gbs": peaks.get("hbm_gbs", 6800.0),
                         "algorithmic_bytes_per_map": 16.0 * npix}}
-    if roof_fft["achieved"]:
+    if roof_fft["achieved"] and args.precision == "split":
+        # The split form's FFT runs in df64 arithmetic on the FP32 pipe: its roofline is the
+        # FP32 instruction rate (FFMA loop measured in this run), its work the modelled df64
+        # FP32 instructions; the FP64-equivalent rate is kept beside it.
+        fp64_equiv = roof_fft["achieved"]
+        ins = fft_df_instr_per_map(nside) * nmaps * args.steps / (fft_ms / 1000.0)
+        roof_fft.update({
+            "bound": "fp32", "kernel": "k_ring_fft_fwd_df (df64 arithmetic)",
+            "achieved": ins / 1e12, "peak": peak32.value / 2, "unit": "Tinstr/s (FP32 pipe)",
+            "frac": ins / 1e12 / (peak32.value / 2),
+            "peak_source": ("FFMA loop measured by bench.py on this GPU "
+                            "(fsht_measure_fp32_peak, TFLOP/s / 2 = FP32 instructions/s); "
+                            "MEASURED_PEAKS.json holds HBM and BF16 figures only"),
+            "fp32_instr_per_map": fft_df_instr_per_map(nside),
+            "fp64_equivalent_tflops": fp64_equiv,
+            "note": ("achieved = df64 FP32 instructions of the radix passes, Bluestein chirps "
+                     "and filter (model: 16 per lazy complex df64 add, 32 per lazy complex "
+                     "product, 6 per renormalised store) / CUDA-event time; loads, stores, "
+                     "index math, conversions and the fold are extra issue slots not counted")})
+        roof_fft["hbm"]["frac"] = roof_fft["hbm"]["achieved_gbs"] / roof_fft["hbm"]["peak_gbs"]
+    elif roof_fft["achieved"]:
         roof_fft["frac"] = roof_fft["achieved"] / roof_fft["peak"]
         roof_fft["hbm"]["frac"] = roof_fft["hbm"]["achieved_gbs"] / roof_fft["hbm"]["peak_gbs"]
         dp = fft_dp_ops_per_map(nside) * nmaps * args.steps / (fft_ms / 1000.0)
@@ -460,7 +544,7 @@ def ours(args, rank, world, local):
             "data": "synthetic", "config": workload_config(args), "clocks": clk,
             "gpu_launches": launches, "per_kernel": per_kernel, "roofline": roof,
             "roofline_fft": roof_fft, "roofline_contraction": roof_ana,
-            "fp64_peak_tflops": peak64.value}
+            "fp64_peak_tflops": peak64.value, "fp32_peak_tflops": peak32.value}
 
     # -------- the plain FP64 path on the same maps (precision reference + speed ratio)
     if args.precision == "split" and not args.no_fp64:

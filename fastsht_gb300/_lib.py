@@ -65,6 +65,7 @@ SIGNATURES = {
     "fsht_profile_enable": [_vp, _i],
     "fsht_profile_read": [_vp, _i, C.POINTER(_i), C.POINTER(C.c_double)],
     "fsht_measure_fp64_peak": [C.POINTER(C.c_double)],
+    "fsht_measure_fp32_peak": [C.POINTER(C.c_double)],
     "fsht_last_error": [C.c_char_p, _sz],
     "fsht_batch_create": [C.c_void_p, _i, _i, _sz, _i, _vp, C.POINTER(_vp)],
     "fsht_batch_run": [_vp],

@@ -106,7 +106,8 @@ int run_job(const fsht_plan* base, const fsht_job& j, unsigned char* arena, size
 
 // ------------------------------------------------------------------ autotuner
 std::mutex g_tune_mu;
-std::map<std::tuple<int, int, int>, std::pair<int, int>> g_tune;   // (nside, lmax bucket, maps)
+// (nside, lmax bucket, maps, df64 FFT) -> (maps per CTA, threads; 0 = per-segment default)
+std::map<std::tuple<int, int, int, int>, std::pair<int, int>> g_tune;
 
 }  // namespace
 
@@ -116,7 +117,8 @@ extern "C" int fsht_plan_autotune(fsht_plan* p, int sample_maps) {
     return FSHT_EINVAL;
   }
   if (sample_maps < 1) sample_maps = 1;
-  const auto key = std::make_tuple(p->nside, (p->lmax + 255) / 256, sample_maps);
+  const auto key = std::make_tuple(p->nside, (p->lmax + 255) / 256, sample_maps,
+                                   p->d_tw_df ? 1 : 0);
   {
     std::lock_guard<std::mutex> lk(g_tune_mu);
     auto it = g_tune.find(key);
@@ -143,7 +145,7 @@ extern "C" int fsht_plan_autotune(fsht_plan* p, int sample_maps) {
   float best = 1e30f;
   int best_mpb = 0, best_thr = 0;
   const int mpbs[] = {1, 2, 4, 8, 16};
-  const int thrs[] = {256, 512};
+  const int thrs[] = {256, 512, 0};
   int rc = FSHT_OK;
   for (int thr : thrs) {
     for (int mpb : mpbs) {

@@ -1,6 +1,5 @@
-// Measurement helper: FP64 FMA throughput of the current device, the roofline
-// denominator for the plain-FP64 kernels (the measured peaks cover HBM and
-// BF16 only).
+// Measurement helpers: FP64 and FP32 FMA throughput of the current device, the roofline
+// denominators of the plain-FP64 kernels and of the df64 ring FFT.
 #include "common.cuh"
 
 namespace {
@@ -33,6 +32,52 @@ extern "C" int fsht_measure_fp64_peak(double* tflops) {
   for (int rep = 0; rep < 3; ++rep) {
     FSHT_CUDA_TRY(cudaEventRecord(e0, 0));
     k_dfma_loop<<<blocks, threads>>>(out, iters, 0.999, 1e-3);
+    FSHT_LAUNCH_CHECK();
+    FSHT_CUDA_TRY(cudaEventRecord(e1, 0));
+    FSHT_CUDA_TRY(cudaEventSynchronize(e1));
+    float ms = 0.f;
+    FSHT_CUDA_TRY(cudaEventElapsedTime(&ms, e0, e1));
+    if (ms < best) best = ms;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(out);
+  *tflops = 2.0 * 8 * (double)iters * blocks * threads / (best * 1e-3) / 1e12;
+  return FSHT_OK;
+}
+
+// FP32 FMA throughput (TFLOP/s): the roofline denominator of the df64 kernels, which run on
+// the FP32 pipe.
+namespace {
+__global__ void k_ffma_loop(float* out, int iters, float a, float b) {
+  float x0 = threadIdx.x, x1 = x0 + 1, x2 = x0 + 2, x3 = x0 + 3;
+  float x4 = x0 + 4, x5 = x0 + 5, x6 = x0 + 6, x7 = x0 + 7;
+  for (int i = 0; i < iters; ++i) {
+    x0 = fmaf(x0, a, b); x1 = fmaf(x1, a, b); x2 = fmaf(x2, a, b); x3 = fmaf(x3, a, b);
+    x4 = fmaf(x4, a, b); x5 = fmaf(x5, a, b); x6 = fmaf(x6, a, b); x7 = fmaf(x7, a, b);
+  }
+  out[blockIdx.x * blockDim.x + threadIdx.x] = x0 + x1 + x2 + x3 + x4 + x5 + x6 + x7;
+}
+}  // namespace
+
+extern "C" int fsht_measure_fp32_peak(double* tflops) {
+  if (!tflops) {
+    fsht_set_error("null output");
+    return FSHT_EINVAL;
+  }
+  int dev = 0, nsm = 0;
+  FSHT_CUDA_TRY(cudaGetDevice(&dev));
+  FSHT_CUDA_TRY(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+  const int blocks = nsm * 8, threads = 256, iters = 40000;
+  float* out = nullptr;
+  FSHT_CUDA_TRY(cudaMalloc(&out, sizeof(float) * blocks * threads));
+  cudaEvent_t e0, e1;
+  FSHT_CUDA_TRY(cudaEventCreate(&e0));
+  FSHT_CUDA_TRY(cudaEventCreate(&e1));
+  float best = 1e30f;
+  for (int rep = 0; rep < 3; ++rep) {
+    FSHT_CUDA_TRY(cudaEventRecord(e0, 0));
+    k_ffma_loop<<<blocks, threads>>>(out, iters, 0.999f, 1e-3f);
     FSHT_LAUNCH_CHECK();
     FSHT_CUDA_TRY(cudaEventRecord(e1, 0));
     FSHT_CUDA_TRY(cudaEventSynchronize(e1));

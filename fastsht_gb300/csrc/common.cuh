@@ -144,6 +144,12 @@ struct fsht_plan {
   int nwaves;
   unsigned char* d_lbuf;
   size_t lbuf_bytes;
+  // plans that own their workspace: lambda-digit tiles one wave ahead on an auxiliary
+  // stream, alternating between d_lbuf and d_lbuf2 (ev: fork, join, tiles ready x2,
+  // contraction done x2); null / unused in table-only plans and their job views
+  cudaStream_t aux;
+  unsigned char* d_lbuf2;
+  cudaEvent_t ev[6];
   int wave_qmax;                   // most orders in one wave
   FshtPolRow* d_poltab;            // spin-2 plans only, same triangular index as d_lamtab
 };
@@ -194,11 +200,13 @@ int fsht_fft_tables_fill(fsht_plan* p, const int* d_blue_rings, int nblue, cudaS
 int fsht_fft_tables_init(fsht_plan* p);
 int fsht_launch_ring_fft_fwd(fsht_plan* p, const double* maps, long long map_stride,
                              int kc, double2* W, cudaStream_t s);
-// df64 tables of a split-precision plan (after fsht_fft_tables_init) and the df64 forward
-// transform, which fsht_launch_ring_fft_fwd selects when they exist.
+// df64 tables of a split-precision plan (after fsht_fft_tables_init) and the df64 forward and
+// inverse transforms, which fsht_launch_ring_fft_fwd / _inv select when they exist.
 int fsht_fft_df_tables_init(fsht_plan* p);
 int fsht_launch_ring_fft_fwd_df(fsht_plan* p, const double* maps, long long map_stride,
                                 int kc, double2* W, cudaStream_t s);
+int fsht_launch_ring_fft_inv_df(fsht_plan* p, const double2* W, double* maps,
+                                long long map_stride, int kc, cudaStream_t s);
 // Maps per CTA of the ring-FFT launches when the autotuner has not set one.
 int fsht_fft_maps_per_block(int kc, int nrings);
 int fsht_launch_ring_fft_inv(fsht_plan* p, const double2* W, double* maps,

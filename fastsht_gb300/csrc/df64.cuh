@@ -68,6 +68,33 @@ __device__ __forceinline__ void mul(float xh, float xl, float yh, float yl, floa
   fast_two_sum(p, e, h, l);
 }
 
+// Lazy forms: the same sums and products without the final fast_two_sum, so the low part
+// is not renormalised (|lo| may reach a few ulp(hi); hi + lo still carries the value to about
+// 2^-46 of the operands).  Chains of at most a few lazy operations are renormalised when they
+// are stored (norm) or converted to FP64.
+__device__ __forceinline__ void add_lazy(float ah, float al, float bh, float bl, float& h,
+                                         float& l) {
+  float e;
+  two_sum(ah, bh, h, e);
+  l = __fadd_rn(e, __fadd_rn(al, bl));
+}
+
+__device__ __forceinline__ void dot2_lazy(float x1h, float x1l, float y1h, float y1l, float x2h,
+                                          float x2l, float y2h, float y2l, float& h, float& l) {
+  const float p1 = __fmul_rn(x1h, y1h);
+  const float e1 = __fmaf_rn(x1h, y1h, -p1);
+  const float p2 = __fmul_rn(x2h, y2h);
+  const float e2 = __fmaf_rn(x2h, y2h, -p2);
+  float e;
+  two_sum(p1, p2, h, e);
+  float t = __fadd_rn(e1, e2);
+  t = __fmaf_rn(x1h, y1l, t);
+  t = __fmaf_rn(x1l, y1h, t);
+  t = __fmaf_rn(x2h, y2l, t);
+  t = __fmaf_rn(x2l, y2h, t);
+  l = __fadd_rn(e, t);
+}
+
 }  // namespace dd
 
 __device__ __forceinline__ cdd cadd(cdd a, cdd b) {
@@ -96,6 +123,38 @@ __device__ __forceinline__ cdd cmulc(cdd a, cdd w) {
   dd::dot2(a.h.y, a.l.y, w.h.x, w.l.x, -a.h.x, -a.l.x, w.h.y, w.l.y, r.h.y, r.l.y);
   return r;
 }
+// lazy complex forms (see dd::add_lazy) and the renormalisation
+__device__ __forceinline__ cdd cadd_lz(cdd a, cdd b) {
+  cdd r;
+  dd::add_lazy(a.h.x, a.l.x, b.h.x, b.l.x, r.h.x, r.l.x);
+  dd::add_lazy(a.h.y, a.l.y, b.h.y, b.l.y, r.h.y, r.l.y);
+  return r;
+}
+__device__ __forceinline__ cdd csub_lz(cdd a, cdd b) {
+  cdd r;
+  dd::add_lazy(a.h.x, a.l.x, -b.h.x, -b.l.x, r.h.x, r.l.x);
+  dd::add_lazy(a.h.y, a.l.y, -b.h.y, -b.l.y, r.h.y, r.l.y);
+  return r;
+}
+__device__ __forceinline__ cdd cmul_lz(cdd a, cdd w) {
+  cdd r;
+  dd::dot2_lazy(a.h.x, a.l.x, w.h.x, w.l.x, -a.h.y, -a.l.y, w.h.y, w.l.y, r.h.x, r.l.x);
+  dd::dot2_lazy(a.h.x, a.l.x, w.h.y, w.l.y, a.h.y, a.l.y, w.h.x, w.l.x, r.h.y, r.l.y);
+  return r;
+}
+__device__ __forceinline__ cdd cmulc_lz(cdd a, cdd w) {
+  cdd r;
+  dd::dot2_lazy(a.h.x, a.l.x, w.h.x, w.l.x, a.h.y, a.l.y, w.h.y, w.l.y, r.h.x, r.l.x);
+  dd::dot2_lazy(a.h.y, a.l.y, w.h.x, w.l.x, -a.h.x, -a.l.x, w.h.y, w.l.y, r.h.y, r.l.y);
+  return r;
+}
+__device__ __forceinline__ cdd cnorm(cdd a) {
+  cdd r;
+  dd::fast_two_sum(a.h.x, a.l.x, r.h.x, r.l.x);
+  dd::fast_two_sum(a.h.y, a.l.y, r.h.y, r.l.y);
+  return r;
+}
+
 __device__ __forceinline__ cdd cconj(cdd a) {
   cdd r;
   r.h = make_float2(a.h.x, -a.h.y);

@@ -30,6 +30,18 @@ __device__ __forceinline__ double2 ldg_e(const double2* p) { return __ldg(p); }
 __device__ __forceinline__ cdd ldg_e(const cdd* p) { return ldg_cdd(p); }
 __device__ __forceinline__ double2 cmulc(double2 a, double2 w) { return cmul(a, cconj(w)); }
 __device__ __forceinline__ double2 cmul_mi(double2 a) { return make_double2(a.y, -a.x); }
+// Operations inside one butterfly: exact FP64 for double2; lazy df64 (no renormalisation,
+// at most four in a chain) for cdd, renormalised once when the butterfly stores (fin).
+__device__ __forceinline__ double2 ladd(double2 a, double2 b) { return cadd(a, b); }
+__device__ __forceinline__ double2 lsub(double2 a, double2 b) { return csub(a, b); }
+__device__ __forceinline__ double2 lmul(double2 a, double2 w) { return cmul(a, w); }
+__device__ __forceinline__ double2 lmulc(double2 a, double2 w) { return cmulc(a, w); }
+__device__ __forceinline__ double2 fin(double2 a) { return a; }
+__device__ __forceinline__ cdd ladd(cdd a, cdd b) { return cadd_lz(a, b); }
+__device__ __forceinline__ cdd lsub(cdd a, cdd b) { return csub_lz(a, b); }
+__device__ __forceinline__ cdd lmul(cdd a, cdd w) { return cmul_lz(a, w); }
+__device__ __forceinline__ cdd lmulc(cdd a, cdd w) { return cmulc_lz(a, w); }
+__device__ __forceinline__ cdd fin(cdd a) { return cnorm(a); }
 template <class E> __device__ __forceinline__ E zero_e();
 template <> __device__ __forceinline__ double2 zero_e<double2>() { return make_double2(0.0, 0.0); }
 template <> __device__ __forceinline__ cdd zero_e<cdd>() { return cdd_zero(); }
@@ -46,10 +58,11 @@ __device__ __forceinline__ int sw(int i) { return i ^ ((i >> 3) & 7); }
 // transform order out: an optional radix-3 pass (P = 3 T) splits the data into three
 // blocks of T = 2^logT, then radix-4 passes (radix-2^2 butterflies: three twiddles, none
 // in the last pass) and a radix-2 pass when logT is odd.  A power-of-two transform
-// leaves bin q at bit-reverse(q).  All threads of the block call it; it synchronises on
-// entry and after every pass.
+// leaves bin q at bit-reverse(q).  Inputs at nz and above are zero (Bluestein's padding):
+// the first pass then skips the products with them (exact, the same results).  All threads of
+// the block call it; it synchronises on entry and after every pass.
 template <class E>
-__device__ void fft_dif(E* buf, const FshtRingFFT& rf, const FftTwT<E>& tw) {
+__device__ void fft_dif(E* buf, const FshtRingFFT& rf, const FftTwT<E>& tw, int nz) {
   using namespace fftp;
   constexpr bool kF64 = std::is_same<E, double2>::value;
   const int tid = threadIdx.x, nt = blockDim.x;
@@ -58,9 +71,11 @@ __device__ void fft_dif(E* buf, const FshtRingFFT& rf, const FftTwT<E>& tw) {
   __syncthreads();   // the caller's writes to buf must land first
   if (rf.r3) {
     const int sc = tw.P3max / rf.P;
+    const bool c_zero = nz <= 2 * T;   // the third input of every butterfly is padding
     for (int j = tid; j < T; j += nt) {
-      const E a = buf[sw(j)], b = buf[sw(j + T)], c = buf[sw(j + 2 * T)];
-      const E sm = cadd(b, c), df = csub(b, c);
+      const E a = buf[sw(j)], b = buf[sw(j + T)];
+      const E c = c_zero ? zero_e<E>() : buf[sw(j + 2 * T)];
+      const E sm = c_zero ? b : ladd(b, c), df = c_zero ? b : lsub(b, c);
       E y1, y2;
       // w3 = exp(-2 pi i / 3): a + w3 b + w3^2 c = t - i (sqrt3/2) df, the other t + i ...
       if constexpr (kF64) {
@@ -68,14 +83,14 @@ __device__ void fft_dif(E* buf, const FshtRingFFT& rf, const FftTwT<E>& tw) {
         y1 = make_double2(fma(kSqrt3Half, df.y, t.x), fma(-kSqrt3Half, df.x, t.y));
         y2 = make_double2(fma(-kSqrt3Half, df.y, t.x), fma(kSqrt3Half, df.x, t.y));
       } else {
-        const cdd t = csub(a, cscale_p2(sm, 0.5f));
+        const cdd t = lsub(a, cscale_p2(sm, 0.5f));
         const cdd u = cmul_pi(cscale_dd(df, kSqrt3HalfHi, kSqrt3HalfLo));
-        y1 = csub(t, u);
-        y2 = cadd(t, u);
+        y1 = lsub(t, u);
+        y2 = ladd(t, u);
       }
-      buf[sw(j)] = cadd(a, sm);
-      buf[sw(j + T)] = cmul(y1, ldg_e(&tw.tw3[j * sc]));
-      buf[sw(j + 2 * T)] = cmul(y2, ldg_e(&tw.tw3[2 * j * sc]));
+      buf[sw(j)] = fin(ladd(a, sm));
+      buf[sw(j + T)] = fin(lmul(y1, ldg_e(&tw.tw3[j * sc])));
+      buf[sw(j + 2 * T)] = fin(lmul(y2, ldg_e(&tw.tw3[2 * j * sc])));
     }
     __syncthreads();
   }
@@ -84,26 +99,38 @@ __device__ void fft_dif(E* buf, const FshtRingFFT& rf, const FftTwT<E>& tw) {
     const int lh = logspan - 2, h = 1 << lh;
     const int per_blk = 1 << (logT - 2);
     const int sh = tw.logTmax - logspan;
+    // first pass over zero-padded data: the inputs at i0 + 2h, i0 + 3h are all padding
+    const bool cd_zero = !rf.r3 && logspan == logT && nz <= 2 * h;
     for (int idx = tid; idx < nblk * per_blk; idx += nt) {
       const int blk = idx >> (logT - 2);
       const int r = idx & (per_blk - 1);
       const int j = r & (h - 1);
       const int i0 = (blk << logT) + ((r >> lh) << logspan) + j;
-      const E a = buf[sw(i0)], b = buf[sw(i0 + h)], c = buf[sw(i0 + 2 * h)], d = buf[sw(i0 + 3 * h)];
-      const E apc = cadd(a, c), amc = csub(a, c), bpd = cadd(b, d), bmd = csub(b, d);
-      const E y1 = csub(apc, bpd);
-      const E mib = cmul_mi(bmd);
-      const E y2 = cadd(amc, mib);   // (a-c) - i(b-d)
-      const E y3 = csub(amc, mib);   // (a-c) + i(b-d)
-      buf[sw(i0)] = cadd(apc, bpd);
-      if (h == 1) {
-        buf[sw(i0 + h)] = y1;
-        buf[sw(i0 + 2 * h)] = y2;
-        buf[sw(i0 + 3 * h)] = y3;
+      E apc, amc, bpd, bmd;
+      if (cd_zero) {
+        apc = amc = buf[sw(i0)];
+        bpd = bmd = buf[sw(i0 + h)];
       } else {
-        buf[sw(i0 + h)] = cmul(y1, ldg_e(&tw.tw2[(2 * j) << sh]));
-        buf[sw(i0 + 2 * h)] = cmul(y2, ldg_e(&tw.tw2[j << sh]));
-        buf[sw(i0 + 3 * h)] = cmul(y3, ldg_e(&tw.tw2[(3 * j) << sh]));
+        const E a = buf[sw(i0)], b = buf[sw(i0 + h)], c = buf[sw(i0 + 2 * h)],
+                d = buf[sw(i0 + 3 * h)];
+        apc = ladd(a, c);
+        amc = lsub(a, c);
+        bpd = ladd(b, d);
+        bmd = lsub(b, d);
+      }
+      const E y1 = lsub(apc, bpd);
+      const E mib = cmul_mi(bmd);
+      const E y2 = ladd(amc, mib);   // (a-c) - i(b-d)
+      const E y3 = lsub(amc, mib);   // (a-c) + i(b-d)
+      buf[sw(i0)] = fin(ladd(apc, bpd));
+      if (h == 1) {
+        buf[sw(i0 + h)] = fin(y1);
+        buf[sw(i0 + 2 * h)] = fin(y2);
+        buf[sw(i0 + 3 * h)] = fin(y3);
+      } else {
+        buf[sw(i0 + h)] = fin(lmul(y1, ldg_e(&tw.tw2[(2 * j) << sh])));
+        buf[sw(i0 + 2 * h)] = fin(lmul(y2, ldg_e(&tw.tw2[j << sh])));
+        buf[sw(i0 + 3 * h)] = fin(lmul(y3, ldg_e(&tw.tw2[(3 * j) << sh])));
       }
     }
     __syncthreads();
@@ -111,17 +138,18 @@ __device__ void fft_dif(E* buf, const FshtRingFFT& rf, const FftTwT<E>& tw) {
   if (logspan == 1) {
     for (int idx = tid; idx < nblk << (logT - 1); idx += nt) {
       const E a = buf[sw(2 * idx)], b = buf[sw(2 * idx + 1)];
-      buf[sw(2 * idx)] = cadd(a, b);
-      buf[sw(2 * idx + 1)] = csub(a, b);
+      buf[sw(2 * idx)] = fin(ladd(a, b));
+      buf[sw(2 * idx + 1)] = fin(lsub(a, b));
     }
     __syncthreads();
   }
 }
 
 // The inverse of fft_dif without normalisation (P times the inverse DFT): transform order
-// in, natural order out; the passes of fft_dif in reverse with conjugate twiddles.
+// in, natural order out; the passes of fft_dif in reverse with conjugate twiddles.  Only the
+// outputs below nout are wanted (Bluestein keeps nd of P): the last pass skips the others.
 template <class E>
-__device__ void fft_dit_inv(E* buf, const FshtRingFFT& rf, const FftTwT<E>& tw) {
+__device__ void fft_dit_inv(E* buf, const FshtRingFFT& rf, const FftTwT<E>& tw, int nout) {
   using namespace fftp;
   constexpr bool kF64 = std::is_same<E, double2>::value;
   const int tid = threadIdx.x, nt = blockDim.x;
@@ -132,8 +160,8 @@ __device__ void fft_dit_inv(E* buf, const FshtRingFFT& rf, const FftTwT<E>& tw) 
   if (logT & 1) {
     for (int idx = tid; idx < nblk << (logT - 1); idx += nt) {
       const E a = buf[sw(2 * idx)], b = buf[sw(2 * idx + 1)];
-      buf[sw(2 * idx)] = cadd(a, b);
-      buf[sw(2 * idx + 1)] = csub(a, b);
+      buf[sw(2 * idx)] = fin(ladd(a, b));
+      buf[sw(2 * idx + 1)] = fin(lsub(a, b));
     }
     __syncthreads();
     logspan = 3;
@@ -142,6 +170,7 @@ __device__ void fft_dit_inv(E* buf, const FshtRingFFT& rf, const FftTwT<E>& tw) 
     const int lh = logspan - 2, h = 1 << lh;
     const int per_blk = 1 << (logT - 2);
     const int sh = tw.logTmax - logspan;
+    const bool low_half = !rf.r3 && logspan == logT && nout <= 2 * h;   // outputs < 2h only
     for (int idx = tid; idx < nblk * per_blk; idx += nt) {
       const int blk = idx >> (logT - 2);
       const int r = idx & (per_blk - 1);
@@ -165,43 +194,47 @@ __device__ void fft_dit_inv(E* buf, const FshtRingFFT& rf, const FftTwT<E>& tw) 
                            fma(w3.x, y3.y, fma(-w3.y, y3.x, z2.y)));
           f = make_double2(fma(2.0, z2.x, -e.x), fma(2.0, z2.y, -e.y));
         } else {
-          const E z1 = cmulc(y1, w2), z2 = cmulc(y2, w1), z3 = cmulc(y3, w3);
-          sp = cadd(y0, z1);
-          dm = csub(y0, z1);
-          e = cadd(z2, z3);
-          f = csub(z2, z3);
+          const E z1 = lmulc(y1, w2), z2 = lmulc(y2, w1), z3 = lmulc(y3, w3);
+          sp = ladd(y0, z1);
+          dm = lsub(y0, z1);
+          e = ladd(z2, z3);
+          f = lsub(z2, z3);
         }
       } else {
-        sp = cadd(y0, y1);
-        dm = csub(y0, y1);
-        e = cadd(y2, y3);
-        f = csub(y2, y3);
+        sp = ladd(y0, y1);
+        dm = lsub(y0, y1);
+        e = ladd(y2, y3);
+        f = lsub(y2, y3);
       }
       const E mif = cmul_mi(f);
-      buf[sw(i0)] = cadd(sp, e);
-      buf[sw(i0 + 2 * h)] = csub(sp, e);
-      buf[sw(i0 + h)] = csub(dm, mif);       // d + i f
-      buf[sw(i0 + 3 * h)] = cadd(dm, mif);   // d - i f
+      buf[sw(i0)] = fin(ladd(sp, e));
+      buf[sw(i0 + h)] = fin(lsub(dm, mif));         // d + i f
+      if (!low_half) {
+        buf[sw(i0 + 2 * h)] = fin(lsub(sp, e));
+        buf[sw(i0 + 3 * h)] = fin(ladd(dm, mif));   // d - i f
+      }
     }
     __syncthreads();
   }
   if (rf.r3) {
     const int sc = tw.P3max / rf.P;
+    const bool two_blocks = nout <= 2 * T;   // the third block is not wanted
     for (int j = tid; j < T; j += nt) {
       const E a = buf[sw(j)];
-      const E b = cmulc(buf[sw(j + T)], ldg_e(&tw.tw3[j * sc]));
-      const E c = cmulc(buf[sw(j + 2 * T)], ldg_e(&tw.tw3[2 * j * sc]));
-      const E sm = cadd(b, c), df = csub(b, c);
-      buf[sw(j)] = cadd(a, sm);
+      const E b = lmulc(buf[sw(j + T)], ldg_e(&tw.tw3[j * sc]));
+      const E c = lmulc(buf[sw(j + 2 * T)], ldg_e(&tw.tw3[2 * j * sc]));
+      const E sm = ladd(b, c), df = lsub(b, c);
+      buf[sw(j)] = fin(ladd(a, sm));
       if constexpr (kF64) {
         const double2 t = make_double2(fma(-0.5, sm.x, a.x), fma(-0.5, sm.y, a.y));
         buf[sw(j + T)] = make_double2(fma(-kSqrt3Half, df.y, t.x), fma(kSqrt3Half, df.x, t.y));
-        buf[sw(j + 2 * T)] = make_double2(fma(kSqrt3Half, df.y, t.x), fma(-kSqrt3Half, df.x, t.y));
+        if (!two_blocks)
+          buf[sw(j + 2 * T)] = make_double2(fma(kSqrt3Half, df.y, t.x), fma(-kSqrt3Half, df.x, t.y));
       } else {
-        const cdd t = csub(a, cscale_p2(sm, 0.5f));
+        const cdd t = lsub(a, cscale_p2(sm, 0.5f));
         const cdd u = cmul_pi(cscale_dd(df, kSqrt3HalfHi, kSqrt3HalfLo));
-        buf[sw(j + T)] = cadd(t, u);
-        buf[sw(j + 2 * T)] = csub(t, u);
+        buf[sw(j + T)] = fin(ladd(t, u));
+        if (!two_blocks) buf[sw(j + 2 * T)] = fin(lsub(t, u));
       }
     }
     __syncthreads();
@@ -223,17 +256,63 @@ __device__ void ring_dft(E* buf, const FshtRingFFT& rf, const FftTwT<E>& tw,
   using namespace fftp;
   const int tid = threadIdx.x, nt = blockDim.x;
   if (!rf.bluestein) {
-    fft_dif(buf, rf, tw);
+    fft_dif(buf, rf, tw, rf.P);
     return;
   }
   const int n = rf.nd, P = rf.P;
   for (int j = tid; j < P; j += nt) {
-    if (j < n) buf[sw(j)] = cmul(buf[sw(j)], ldg_e(&chirp[j]));
+    if (j < n) buf[sw(j)] = fin(lmul(buf[sw(j)], ldg_e(&chirp[j])));
     else buf[sw(j)] = zero_e<E>();
   }
-  fft_dif(buf, rf, tw);
-  for (int j = tid; j < P; j += nt) buf[sw(j)] = cmul(buf[sw(j)], ldg_e(&bhat[j]));
-  fft_dit_inv(buf, rf, tw);
-  for (int j = tid; j < n; j += nt) buf[sw(j)] = cmul(buf[sw(j)], ldg_e(&chirp[j]));
+  fft_dif(buf, rf, tw, n);
+  for (int j = tid; j < P; j += nt) buf[sw(j)] = fin(lmul(buf[sw(j)], ldg_e(&bhat[j])));
+  fft_dit_inv(buf, rf, tw, n);
+  for (int j = tid; j < n; j += nt) buf[sw(j)] = fin(lmul(buf[sw(j)], ldg_e(&chirp[j])));
   __syncthreads();
+}
+
+// ------------------------------------------------------------------ synthesis spectra (FP64)
+// Bin q of the packed spectrum Z[q] = Y_N[q] + i Y_S[q] of a ring pair from G_m (north, W[0])
+// and G_m(i') (south, W[1]), m <= mtop, with ph[m] = e^{i m phi0}:
+//   Y[q] = sum_{m = q mod n} (c_m/2) G_m e^{i m phi0} + sum_{m = -q mod n} (c_m/2) conj(G_m e^{i m phi0}),
+// c_0 = 1, c_{m>0} = 2 (the reference's mat2fft_fast, src/fft_mapping.f90:84-128).
+__device__ __forceinline__ double2 packed_spectrum_bin(const double2* ph,
+                                                       const double2* __restrict__ W,
+                                                       long long stride_m, int n, int mtop,
+                                                       bool equator, int q) {
+  double2 yN = make_double2(0.0, 0.0), yS = make_double2(0.0, 0.0);
+  // m = q (mod n)
+  for (int m = q; m <= mtop; m += n) {
+    const double2* w = W + (long long)m * stride_m;
+    const double c = (m == 0) ? 0.5 : 1.0;
+    yN = cadd(yN, cscale(cmul(ph[m], w[0]), c));
+    if (!equator) yS = cadd(yS, cscale(cmul(ph[m], w[1]), c));
+  }
+  // m = -q (mod n)
+  const int q2 = (q == 0) ? 0 : n - q;
+  for (int m = q2; m <= mtop; m += n) {
+    const double2* w = W + (long long)m * stride_m;
+    const double c = (m == 0) ? 0.5 : 1.0;
+    yN = cadd(yN, cscale(cconj(cmul(ph[m], w[0])), c));
+    if (!equator) yS = cadd(yS, cscale(cconj(cmul(ph[m], w[1])), c));
+  }
+  return make_double2(yN.x - yS.y, yN.y + yS.x);   // Y_N + i Y_S
+}
+
+// Bin q of one ring's Hermitian spectrum (side 0: north from G_N, side 1: south from G_S),
+// the aliased sum packed_spectrum_bin forms for both rings at once.
+__device__ __forceinline__ double2 spectrum_bin(const double2* ph, const double2* __restrict__ W,
+                                                long long stride_m, int n, int mtop, int side,
+                                                int q) {
+  double2 y = make_double2(0.0, 0.0);
+  for (int m = q; m <= mtop; m += n) {
+    const double c = (m == 0) ? 0.5 : 1.0;
+    y = cadd(y, cscale(cmul(ph[m], W[(long long)m * stride_m + side]), c));
+  }
+  const int q2 = (q == 0) ? 0 : n - q;
+  for (int m = q2; m <= mtop; m += n) {
+    const double c = (m == 0) ? 0.5 : 1.0;
+    y = cadd(y, cscale(cconj(cmul(ph[m], W[(long long)m * stride_m + side])), c));
+  }
+  return y;
 }

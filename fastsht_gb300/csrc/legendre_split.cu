@@ -302,8 +302,9 @@ struct __align__(8) GemmSmemHdr {
 __global__ void __launch_bounds__(kThreads, 1) k_split_gemm(GemmArgs a) {
   extern __shared__ __align__(1024) unsigned char smem[];
   __shared__ GemmSmemHdr h;
-  __shared__ double s_cs[kCols];
-  __shared__ double s_rs[kRows];
+  __shared__ int s_ce[kCols];          // column exponents (eb - 12)
+  __shared__ float s_rh[kRows], s_rl[kRows];   // row factors Dm_l pa as df64
+  __shared__ int s_re[kRows];          // row exponents EA(l)
 
   const int g = blockIdx.x;
   const int p = blockIdx.y & 1;
@@ -336,14 +337,18 @@ __global__ void __launch_bounds__(kThreads, 1) k_split_gemm(GemmArgs a) {
   }
   if (tid < kCols) {
     const int eb = a.EB[(((long long)blockIdx.z * 2 + p) * a.ngroups + g) * kCols + tid];
-    s_cs[tid] = (eb == kEmptyExp) ? 0.0 : ldexp(a.pa, eb - 12);
+    s_ce[tid] = (eb == kEmptyExp) ? kEmptyExp : eb - 12;
     const int l = lt0 + p + 2 * tid;
+    float fh = 0.f, fl = 0.f;
+    int re = 0;
     if (l <= a.lmax) {
       const FshtLamRow rw = a.tab[tri_off(m, a.lmax) + (l - m)];
-      s_rs[tid] = ldexp(rw.dm, rw.erow + rw.dx);
-    } else {
-      s_rs[tid] = 0.0;
+      factor_pair(rw.dm * a.pa, fh, fl);
+      re = rw.erow + rw.dx;
     }
+    s_rh[tid] = fh;
+    s_rl[tid] = fl;
+    s_re[tid] = re;
   }
   if (warp == 0) tc::tmem_alloc(&h.tmem, 512);
   tc::tc_fence_before();
@@ -401,7 +406,8 @@ __global__ void __launch_bounds__(kThreads, 1) k_split_gemm(GemmArgs a) {
     const int l = lt0 + p + 2 * row;
     const bool rowok = l <= a.lmax;
     if (ok) {
-      const double rs = s_rs[row];
+      const float rh = s_rh[row], rl = s_rl[row];
+      const int re = s_re[row];
       const long long L1 = a.lmax + 1;
       const uint32_t lane_base = tmem + ((uint32_t)(warp << 5) << 16);
       for (int c0 = 0; c0 < kCols; c0 += 16) {
@@ -419,7 +425,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_split_gemm(GemmArgs a) {
           const int c = c0 + j;
           const int k = g * kGroupMaps + (c & 63);
           if (store && k < a.kc) {
-            const double v = combine_levels(v0[j], v1[j], v2[j], v3[j]) * rs * s_cs[c];
+            const double v = levels_scaled(v0[j], v1[j], v2[j], v3[j], rh, rl, re + s_ce[c]);
             double* dst = a.alm + rowidx * a.ld + a.k0 + k;
             if (a.nkc_glob > 1) atomicAdd(dst, v);
             else if (a.accumulate) *dst += v;
@@ -639,7 +645,7 @@ struct __align__(8) SynthSmemHdr {
 __global__ void __launch_bounds__(kThreads, 1) k_split_synth(SynthArgs a) {
   extern __shared__ __align__(1024) unsigned char smem[];
   __shared__ SynthSmemHdr h;
-  __shared__ double s_cs[2][kCols];
+  __shared__ int s_ce[2][kCols];       // column exponents EAG + eb - 12
 
   const int g = blockIdx.x;
   const int rb = blockIdx.y / a.nkclmax;
@@ -672,7 +678,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_split_synth(SynthArgs a) {
   if (tid < kCols) {
     for (int pp = 0; pp < 2; ++pp) {
       const int eb = a.EB[(((long long)blockIdx.z * 2 + pp) * a.ngroups + g) * kCols + tid];
-      s_cs[pp][tid] = (eb == kEmptyExp) ? 0.0 : ldexp(1.0, a.eag + eb - 12);
+      s_ce[pp][tid] = (eb == kEmptyExp) ? kEmptyExp : a.eag + eb - 12;
     }
   }
   if (warp == 0) tc::tmem_alloc(&h.tmem, 512);
@@ -761,7 +767,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_split_synth(SynthArgs a) {
           const int c = c0 + j;
           const int k = g * kGroupMaps + (c & 63);
           if (rowok && k < a.kc) {
-            const double v = combine_levels(v0[j], v1[j], v2[j], v3[j]) * s_cs[par][c];
+            const double v = levels_scaled(v0[j], v1[j], v2[j], v3[j], 1.f, 0.f, s_ce[par][c]);
             double* gn = a.W + ((((long long)m * a.nnorth + i) * a.kc + k) * 2) * 2 + comp;
             double* gs = gn + 2;
             if (a.nkcl_glob > 1) {

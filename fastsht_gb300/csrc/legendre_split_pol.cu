@@ -231,8 +231,9 @@ struct __align__(8) GemmPSmemHdr {
 __global__ void __launch_bounds__(kThreads, 1) k_split_gemm_pol(GemmPArgs a) {
   extern __shared__ __align__(1024) unsigned char smem[];
   __shared__ GemmPSmemHdr h;
-  __shared__ double s_cs[2][kCols];
-  __shared__ double s_rs[kRows];
+  __shared__ int s_ce[2][kCols];       // column exponents (e - 12) per part
+  __shared__ float s_rh[kRows], s_rl[kRows];   // row factors -Dm_l pa as df64
+  __shared__ int s_re[kRows];          // row exponents EA(l)
 
   const int g = blockIdx.x;
   const int field = blockIdx.y & 1;            // 0: E, 1: B
@@ -278,15 +279,19 @@ __global__ void __launch_bounds__(kThreads, 1) k_split_gemm_pol(GemmPArgs a) {
   if (tid < kCols) {
     for (int part = 0; part < 2; ++part) {
       const int e = eb[part][(((long long)blockIdx.z * 2 + bpar[part]) * a.ngroups + g) * kCols + tid];
-      s_cs[part][tid] = (e == kEmptyExp) ? 0.0 : ldexp(-a.pa, e - 12);
+      s_ce[part][tid] = (e == kEmptyExp) ? kEmptyExp : e - 12;
     }
     const int l = lt0 + p + 2 * tid;
+    float fh = 0.f, fl = 0.f;
+    int re = 0;
     if (l <= a.lmax) {
       const FshtLamRow rw = a.tab[tri_off(m, a.lmax) + (l - m)];
-      s_rs[tid] = ldexp(rw.dm, rw.erow + rw.dx);
-    } else {
-      s_rs[tid] = 0.0;
+      factor_pair(-rw.dm * a.pa, fh, fl);
+      re = rw.erow + rw.dx;
     }
+    s_rh[tid] = fh;
+    s_rl[tid] = fl;
+    s_re[tid] = re;
   }
   if (warp == 0) tc::tmem_alloc(&h.tmem, 512);
   tc::tc_fence_before();
@@ -349,7 +354,8 @@ __global__ void __launch_bounds__(kThreads, 1) k_split_gemm_pol(GemmPArgs a) {
     const long long re_row = (long long)m * L1 + l;
     const long long im_row = (L1 - m) * L1 + (l - m);
     double* alm = field == 0 ? a.almE : a.almB;
-    const double rs = s_rs[row];
+    const float rh = s_rh[row], rl = s_rl[row];
+    const int re = s_re[row];
     for (int part = 0; part < 2; ++part) {
       bool ok = tc::mbar_wait(&h.tfull, part, abort);
       ok = __all_sync(0xffffffffu, ok);
@@ -379,7 +385,8 @@ __global__ void __launch_bounds__(kThreads, 1) k_split_gemm_pol(GemmPArgs a) {
           const int c = c0 + j;
           const int k = g * kGroupMaps + (c & 63);
           if (k < a.kc) {
-            const double v = sgn * combine_levels(v0[j], v1[j], v2[j], v3[j]) * rs * s_cs[part][c];
+            const double u = levels_scaled(v0[j], v1[j], v2[j], v3[j], rh, rl, re + s_ce[part][c]);
+            const double v = sgn < 0.0 ? -u : u;
             double* dst = alm + rowidx * a.ld + a.k0 + k;
             if (a.nkc_glob > 1) atomicAdd(dst, v);
             else if (part == 0 && !a.accumulate) *dst = v;
@@ -587,7 +594,7 @@ __device__ __forceinline__ void synth_pol_pass(int f, int t, int& part, int& fld
 __global__ void __launch_bounds__(kThreads, 1) k_split_synth_pol(SynthPArgs a) {
   extern __shared__ __align__(1024) unsigned char smem[];
   __shared__ SynthPSmemHdr h;
-  __shared__ double s_cs[4][kCols];
+  __shared__ int s_ce[4][kCols];       // column exponents EAG + e - 12 per pass
 
   const int g = blockIdx.x;
   const int f = blockIdx.y & 1;
@@ -625,7 +632,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_split_synth_pol(SynthPArgs a) {
       synth_pol_pass(f, t, part, fld, par, c, sg);
       const int* eb = fld ? a.EBB : a.EBE;
       const int e = eb[(((long long)blockIdx.z * 2 + par) * a.ngroups + g) * kCols + tid];
-      s_cs[t][tid] = (e == kEmptyExp) ? 0.0 : ldexp(1.0, a.eag + e - 12);
+      s_ce[t][tid] = (e == kEmptyExp) ? kEmptyExp : a.eag + e - 12;
     }
   }
   if (warp == 0) tc::tmem_alloc(&h.tmem, 512);
@@ -728,10 +735,11 @@ __global__ void __launch_bounds__(kThreads, 1) k_split_synth_pol(SynthPArgs a) {
           const int cc = c0 + j;
           const int k = g * kGroupMaps + (cc & 63);
           if (k < a.kc) {
-            const double v = sgn * combine_levels(v0[j], v1[j], v2[j], v3[j]) * s_cs[t][cc];
+            const double u = levels_scaled(v0[j], v1[j], v2[j], v3[j], 1.f, 0.f, s_ce[t][cc]);
+            const double v = sgn < 0.0 ? -u : u;
             double* gn = Wf + ((((long long)m * a.nnorth + i) * a.kc + k) * 2) * 2 + tgt;
             double* gs = gn + 2;
-            const double vs = sg * v;
+            const double vs = sg < 0 ? -v : v;
             if (a.nkcl_glob > 1) {
               atomicAdd(gn, v);
               atomicAdd(gs, vs);

@@ -43,23 +43,26 @@ namespace {
 struct ProfScope {
   fsht_plan* p;
   int cat;
-  ProfScope(fsht_plan* pp, int c) : p(pp), cat(c) {
+  cudaStream_t st;
+  ProfScope(fsht_plan* pp, int c, cudaStream_t s) : p(pp), cat(c), st(s) {
     if (p->prof) {
       cudaEvent_t e = p->prof->get();
-      cudaEventRecord(e, p->stream);
+      cudaEventRecord(e, st);
       p->prof->pending[cat].push_back(e);
     }
   }
+  ProfScope(fsht_plan* pp, int c) : ProfScope(pp, c, pp->stream) {}
   ~ProfScope() {
     if (p->prof) {
       cudaEvent_t e = p->prof->get();
-      cudaEventRecord(e, p->stream);
+      cudaEventRecord(e, st);
       p->prof->pending[cat].push_back(e);
     }
   }
 };
 }  // namespace
 #define FSHT_PROF(cat) ProfScope _prof_scope_##__LINE__(p, cat)
+#define FSHT_PROF_ON(cat, st) ProfScope _prof_scope_##__LINE__(p, cat, st)
 
 void fsht_set_error(const char* fmt, ...) {
   char buf[1024];
@@ -94,6 +97,10 @@ void free_plan_memory(fsht_plan* p) {
   cudaFree(p->d_lamtab);
   cudaFree(p->d_lam_off);
   cudaFree(p->d_lbuf);
+  cudaFree(p->d_lbuf2);
+  for (int i = 0; i < 6; ++i)
+    if (p->ev[i]) cudaEventDestroy(p->ev[i]);
+  if (p->aux) cudaStreamDestroy(p->aux);
   cudaFree(p->d_poltab);
   delete[] p->h_waves;
   delete[] p->h_ring_i0;
@@ -282,9 +289,9 @@ int fsht_plan_create(int nside, int lmax, int nmaps_max, int flags, int precisio
   const size_t per_map = per_map_buffer_bytes(p) * p->nbuf;
   auto need = [&](size_t k) -> size_t {
     size_t b = per_map * k;
-    if (precision == FSHT_PREC_SPLIT)   // spin 2: digit tiles of Q and U
+    if (precision == FSHT_PREC_SPLIT)   // spin 2: digit tiles of Q and U; two lambda buffers
       b += (p->pol ? 2 : 1) * (fsht_split_ws_bytes(p, (int)k) + fsht_split_eb_bytes(p, (int)k)) +
-           p->lbuf_bytes;
+           2 * p->lbuf_bytes;
     return b;
   };
   const bool tables_only = (flags & FSHT_FLAG_TABLES_ONLY) != 0;
@@ -308,6 +315,17 @@ int fsht_plan_create(int nside, int lmax, int nmaps_max, int flags, int precisio
     if ((rc = dalloc((void**)&p->d_ws, p->ws_bytes))) return fail(rc);
     if ((rc = dalloc((void**)&p->d_eb, f * fsht_split_eb_bytes(p, p->kchunk)))) return fail(rc);
     if ((rc = dalloc((void**)&p->d_lbuf, p->lbuf_bytes))) return fail(rc);
+    if ((rc = dalloc((void**)&p->d_lbuf2, p->lbuf_bytes))) return fail(rc);
+    if ((ce = cudaStreamCreateWithFlags(&p->aux, cudaStreamNonBlocking)) != cudaSuccess) {
+      fsht_set_error("auxiliary stream: %s", cudaGetErrorString(ce));
+      return fail(FSHT_ECUDA);
+    }
+    for (int i = 0; i < 6; ++i) {
+      if ((ce = cudaEventCreateWithFlags(&p->ev[i], cudaEventDisableTiming)) != cudaSuccess) {
+        fsht_set_error("event: %s", cudaGetErrorString(ce));
+        return fail(FSHT_ECUDA);
+      }
+    }
   }
   if ((ce = cudaStreamSynchronize(p->stream)) != cudaSuccess) {
     fsht_set_error("plan setup: %s", cudaGetErrorString(ce));
@@ -334,7 +352,7 @@ int fsht_plan_set_stream(fsht_plan* p, void* stream) {
 int fsht_plan_info(const fsht_plan* p, size_t* device_bytes, int* maps_per_chunk) {
   FSHT_TRY(check_plan(p));
   if (device_bytes) {
-    size_t b = p->work_bytes;
+    size_t b = p->work_bytes + p->ws_bytes + p->lbuf_bytes * (p->aux ? 2 : 1);
     b += sizeof(double) * (2 * p->nnorth + p->lmax + 1) + sizeof(int) * (p->lmax + 1);
     *device_bytes = b;
   }
@@ -418,48 +436,114 @@ int fsht_plan_check(fsht_plan* p) {
 }
 
 // ----------------------------------------------------------------- split form
+// Wave pipeline of the lambda-digit tiles.  The tiles depend on the plan only, so a plan
+// that owns its workspace computes them on its auxiliary stream two waves ahead of the
+// contraction, alternating between two staging buffers: the recursion (FP64 pipe) overlaps
+// the ring FFT (FP32 pipe; wave 0 and 1 start before it) and the slicing / tensor-core
+// contraction of earlier waves.  Events order each contraction after its tiles and each
+// refill after the contraction that read the buffer.  Job views of table-only plans (the
+// batched and serving forms, which already run several jobs concurrently) have no
+// auxiliary stream and run the kernels in turn on one stream.
+typedef int (*LamLaunch)(fsht_plan*, int, unsigned char*, cudaStream_t);
+enum { kEvFork = 0, kEvJoin = 1, kEvTiles = 2, kEvDone = 4 };
+
+static unsigned char* lam_buf(fsht_plan* p, int w) {
+  return (p->aux && (w & 1)) ? p->d_lbuf2 : p->d_lbuf;
+}
+
+static int lam_ahead(fsht_plan* p, LamLaunch f, int w) {
+  if (w >= 2) FSHT_CUDA_TRY(cudaStreamWaitEvent(p->aux, p->ev[kEvDone + (w & 1)], 0));
+  {
+    FSHT_PROF_ON(FSHT_KCAT_LAMBDA, p->aux);
+    FSHT_TRY(f(p, w, lam_buf(p, w), p->aux));
+  }
+  FSHT_CUDA_TRY(cudaEventRecord(p->ev[kEvTiles + (w & 1)], p->aux));
+  return FSHT_OK;
+}
+
+// Forks the auxiliary stream off the plan's stream and starts waves 0 and 1.
+static int lam_start(fsht_plan* p, LamLaunch f) {
+  if (!p->aux) return FSHT_OK;
+  FSHT_CUDA_TRY(cudaEventRecord(p->ev[kEvFork], p->stream));
+  FSHT_CUDA_TRY(cudaStreamWaitEvent(p->aux, p->ev[kEvFork], 0));
+  FSHT_TRY(lam_ahead(p, f, 0));
+  if (p->nwaves > 1) FSHT_TRY(lam_ahead(p, f, 1));
+  return FSHT_OK;
+}
+
+// Before wave w's contraction: its tiles, in the returned buffer, are ready for the plan's
+// stream (computed there now when the plan has no auxiliary stream).
+static int lam_ready(fsht_plan* p, LamLaunch f, int w, unsigned char** buf) {
+  if (!p->aux) {
+    FSHT_PROF(FSHT_KCAT_LAMBDA);
+    FSHT_TRY(f(p, w, p->d_lbuf, p->stream));
+    *buf = p->d_lbuf;
+    return FSHT_OK;
+  }
+  FSHT_CUDA_TRY(cudaStreamWaitEvent(p->stream, p->ev[kEvTiles + (w & 1)], 0));
+  *buf = lam_buf(p, w);
+  return FSHT_OK;
+}
+
+// After wave w's contraction: its buffer may be refilled with wave w + 2.
+static int lam_done(fsht_plan* p, LamLaunch f, int w) {
+  if (!p->aux) return FSHT_OK;
+  FSHT_CUDA_TRY(cudaEventRecord(p->ev[kEvDone + (w & 1)], p->stream));
+  if (w + 2 < p->nwaves) FSHT_TRY(lam_ahead(p, f, w + 2));
+  return FSHT_OK;
+}
+
+// Joins the auxiliary stream back into the plan's stream.
+static int lam_finish(fsht_plan* p) {
+  if (!p->aux) return FSHT_OK;
+  FSHT_CUDA_TRY(cudaEventRecord(p->ev[kEvJoin], p->aux));
+  FSHT_CUDA_TRY(cudaStreamWaitEvent(p->stream, p->ev[kEvJoin], 0));
+  return FSHT_OK;
+}
+
 // One chunk's split-precision analysis of the {S, D} matrix W into alm (added when
-// accumulate), and synthesis of alm into W = {G_N, G_S}.
+// accumulate), and synthesis of alm into W = {G_N, G_S}.  started: lam_start already ran
+// (before the FFT).
 static int split_analysis(fsht_plan* p, const double2* W, double* alm, int nmaps, int c0, int kc,
-                          int accumulate) {
+                          int accumulate, bool started = false) {
   if (!accumulate) FSHT_TRY(fsht_split_clear_alm(p, alm, nmaps, c0, kc, p->stream));
+  if (!started) FSHT_TRY(lam_start(p, fsht_launch_split_lambda));
   for (int w = 0; w < p->nwaves; ++w) {
     {
       FSHT_PROF(FSHT_KCAT_SLICE);
       FSHT_TRY(fsht_launch_split_slice(p, w, W, p->d_ws, p->d_eb, kc, p->stream));
     }
-    {
-      FSHT_PROF(FSHT_KCAT_LAMBDA);
-      FSHT_TRY(fsht_launch_split_lambda(p, w, p->d_lbuf, p->stream));
-    }
+    unsigned char* lb = nullptr;
+    FSHT_TRY(lam_ready(p, fsht_launch_split_lambda, w, &lb));
     {
       FSHT_PROF(FSHT_KCAT_ANALYSIS);
-      FSHT_TRY(fsht_launch_split_gemm(p, w, p->d_ws, p->d_eb, p->d_lbuf, alm, nmaps, c0, kc,
+      FSHT_TRY(fsht_launch_split_gemm(p, w, p->d_ws, p->d_eb, lb, alm, nmaps, c0, kc,
                                       accumulate, p->stream));
     }
+    FSHT_TRY(lam_done(p, fsht_launch_split_lambda, w));
   }
-  return FSHT_OK;
+  return lam_finish(p);
 }
 
 static int split_synthesis(fsht_plan* p, const double* alm, double2* W, int nmaps, int c0,
                            int kc) {
   FSHT_TRY(fsht_split_clear_w(p, W, kc, p->stream));
+  FSHT_TRY(lam_start(p, fsht_launch_split_lambdaT));
   for (int w = 0; w < p->nwaves; ++w) {
     {
       FSHT_PROF(FSHT_KCAT_SLICE);
       FSHT_TRY(fsht_launch_split_slice_alm(p, w, alm, p->d_ws, p->d_eb, nmaps, c0, kc,
                                            p->stream));
     }
-    {
-      FSHT_PROF(FSHT_KCAT_LAMBDA);
-      FSHT_TRY(fsht_launch_split_lambdaT(p, w, p->d_lbuf, p->stream));
-    }
+    unsigned char* lb = nullptr;
+    FSHT_TRY(lam_ready(p, fsht_launch_split_lambdaT, w, &lb));
     {
       FSHT_PROF(FSHT_KCAT_SYNTHESIS);
-      FSHT_TRY(fsht_launch_split_synth(p, w, p->d_ws, p->d_eb, p->d_lbuf, W, kc, p->stream));
+      FSHT_TRY(fsht_launch_split_synth(p, w, p->d_ws, p->d_eb, lb, W, kc, p->stream));
     }
+    FSHT_TRY(lam_done(p, fsht_launch_split_lambdaT, w));
   }
-  return FSHT_OK;
+  return lam_finish(p);
 }
 
 int fsht_run_stage(fsht_plan* p, int stage, const void* in, void* out, int nmaps) {
@@ -504,12 +588,14 @@ int fsht_t2alm(fsht_plan* p, const double* maps, double* alm, int nmaps, int nit
     for (int c0 = 0; c0 < nmaps; c0 += p->kchunk) {
       const int kc = nmaps - c0 < p->kchunk ? nmaps - c0 : p->kchunk;
       double2* W0 = work_buf(p, 0, kc);
+      // the first lambda tiles are computed on the auxiliary stream during the FFT
+      FSHT_TRY(lam_start(p, fsht_launch_split_lambda));
       {
         FSHT_PROF(FSHT_KCAT_FFT_FWD);
         FSHT_TRY(fsht_launch_ring_fft_fwd(p, maps + (size_t)c0 * p->npix, p->npix, kc, W0,
                                           p->stream));
       }
-      FSHT_TRY(split_analysis(p, W0, alm, nmaps, c0, kc, 0));
+      FSHT_TRY(split_analysis(p, W0, alm, nmaps, c0, kc, 0, true));
       // Jacobi refinement: FP64 Fourier-space residual of a split synthesis, analysed
       // in split precision and added
       for (int it = 0; it < niter; ++it) {
@@ -581,7 +667,8 @@ int fsht_alm2t(fsht_plan* p, const double* alm, double* maps, int nmaps) {
 // One chunk's spin-2 analysis of {S, D}(Q), {S, D}(U) into E/B (which: bit0 E, bit1 B),
 // added when accumulate: the FP64 kernel, or the split form's tiles and waves.
 static int pol_analysis(fsht_plan* p, const double2* WQ, const double2* WU, double* almE,
-                        double* almB, int nmaps, int c0, int kc, int accumulate, int which) {
+                        double* almB, int nmaps, int c0, int kc, int accumulate, int which,
+                        bool started = false) {
   if (p->precision != FSHT_PREC_SPLIT) {
     FSHT_PROF(FSHT_KCAT_ANALYSIS);
     return fsht_launch_analysis_fp64(p, 2, WQ, WU, almE, almB, nmaps, c0, kc, accumulate, which,
@@ -599,23 +686,23 @@ static int pol_analysis(fsht_plan* p, const double2* WQ, const double2* WU, doub
     if (which & 1) FSHT_TRY(fsht_split_clear_alm(p, almE, nmaps, c0, kc, p->stream));
     if (which & 2) FSHT_TRY(fsht_split_clear_alm(p, almB, nmaps, c0, kc, p->stream));
   }
+  if (!started) FSHT_TRY(lam_start(p, fsht_launch_split_lambda_pol));
   for (int w = 0; w < p->nwaves; ++w) {
     {
       FSHT_PROF(FSHT_KCAT_SLICE);
       FSHT_TRY(fsht_launch_split_slice(p, w, WQ, wsq, ebq, kc, p->stream));
       FSHT_TRY(fsht_launch_split_slice(p, w, WU, wsu, ebu, kc, p->stream));
     }
-    {
-      FSHT_PROF(FSHT_KCAT_LAMBDA);
-      FSHT_TRY(fsht_launch_split_lambda_pol(p, w, p->d_lbuf, p->stream));
-    }
+    unsigned char* lb = nullptr;
+    FSHT_TRY(lam_ready(p, fsht_launch_split_lambda_pol, w, &lb));
     {
       FSHT_PROF(FSHT_KCAT_ANALYSIS);
-      FSHT_TRY(fsht_launch_split_gemm_pol(p, w, wsq, ebq, wsu, ebu, p->d_lbuf, almE, almB, nmaps,
+      FSHT_TRY(fsht_launch_split_gemm_pol(p, w, wsq, ebq, wsu, ebu, lb, almE, almB, nmaps,
                                           c0, kc, accumulate, which, p->stream));
     }
+    FSHT_TRY(lam_done(p, fsht_launch_split_lambda_pol, w));
   }
-  return FSHT_OK;
+  return lam_finish(p);
 }
 
 // One chunk's spin-2 synthesis of E/B into {G_N, G_S} of Q and U: the FP64 kernel, or the
@@ -636,23 +723,23 @@ static int pol_synthesis(fsht_plan* p, const double* almE, const double* almB, d
   int* ebb = p->d_eb + fsht_split_eb_bytes(p, kc) / sizeof(int);
   FSHT_TRY(fsht_split_clear_w(p, WQ, kc, p->stream));
   FSHT_TRY(fsht_split_clear_w(p, WU, kc, p->stream));
+  FSHT_TRY(lam_start(p, fsht_launch_split_lambdaT_pol));
   for (int w = 0; w < p->nwaves; ++w) {
     {
       FSHT_PROF(FSHT_KCAT_SLICE);
       FSHT_TRY(fsht_launch_split_slice_alm(p, w, almE, wse, ebe, nmaps, c0, kc, p->stream));
       FSHT_TRY(fsht_launch_split_slice_alm(p, w, almB, wsb, ebb, nmaps, c0, kc, p->stream));
     }
-    {
-      FSHT_PROF(FSHT_KCAT_LAMBDA);
-      FSHT_TRY(fsht_launch_split_lambdaT_pol(p, w, p->d_lbuf, p->stream));
-    }
+    unsigned char* lb = nullptr;
+    FSHT_TRY(lam_ready(p, fsht_launch_split_lambdaT_pol, w, &lb));
     {
       FSHT_PROF(FSHT_KCAT_SYNTHESIS);
-      FSHT_TRY(fsht_launch_split_synth_pol(p, w, wse, ebe, wsb, ebb, p->d_lbuf, WQ, WU, kc,
+      FSHT_TRY(fsht_launch_split_synth_pol(p, w, wse, ebe, wsb, ebb, lb, WQ, WU, kc,
                                            p->stream));
     }
+    FSHT_TRY(lam_done(p, fsht_launch_split_lambdaT_pol, w));
   }
-  return FSHT_OK;
+  return lam_finish(p);
 }
 
 static int qu_analysis(fsht_plan* p, const double* Q, const double* U, double* almE,
@@ -662,6 +749,8 @@ static int qu_analysis(fsht_plan* p, const double* Q, const double* U, double* a
     const int kc = nmaps - c0 < p->kchunk ? nmaps - c0 : p->kchunk;
     double2* WQ = work_buf(p, 0, kc);
     double2* WU = work_buf(p, 1, kc);
+    const bool pre = p->precision == FSHT_PREC_SPLIT && p->d_poltab;
+    if (pre) FSHT_TRY(lam_start(p, fsht_launch_split_lambda_pol));   // overlaps the FFTs
     {
       FSHT_PROF(FSHT_KCAT_FFT_FWD);
       FSHT_TRY(fsht_launch_ring_fft_fwd(p, Q + (size_t)c0 * p->npix, p->npix, kc, WQ, p->stream));
@@ -670,7 +759,7 @@ static int qu_analysis(fsht_plan* p, const double* Q, const double* U, double* a
       FSHT_PROF(FSHT_KCAT_FFT_FWD);
       FSHT_TRY(fsht_launch_ring_fft_fwd(p, U + (size_t)c0 * p->npix, p->npix, kc, WU, p->stream));
     }
-    FSHT_TRY(pol_analysis(p, WQ, WU, almE, almB, nmaps, c0, kc, 0, which));
+    FSHT_TRY(pol_analysis(p, WQ, WU, almE, almB, nmaps, c0, kc, 0, which, pre));
     if (niter > 0) {
       double2* RQ = work_buf(p, 2, kc);
       double2* RU = work_buf(p, 3, kc);

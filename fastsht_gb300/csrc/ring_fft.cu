@@ -64,7 +64,7 @@ __global__ void k_bluestein_tables(const FshtRingFFT* rfs, const int* rings, dou
     else if (P - j < n) v = cconj(w[P - j]);
     sbuf[sw(j)] = v;
   }
-  fft_dif(sbuf, rf, tw);
+  fft_dif(sbuf, rf, tw, rf.P);
   const double invP = 1.0 / (double)P;
   for (int j = threadIdx.x; j < P; j += blockDim.x) bhat[rf.bhat_off + j] = cscale(sbuf[sw(j)], invP);
 }
@@ -201,47 +201,11 @@ struct InvArgs {
 };
 
 // Builds, in buf[0..n), the packed spectrum Z[q] = Y_N[q] + i Y_S[q] of the two
-// real rings from G_m (north) and G_m(i') (south), m <= mtop:
-//   Y[q] = sum_{m = q mod n} (c_m/2) G_m e^{i m phi0} + sum_{m = -q mod n} (c_m/2) conj(G_m e^{i m phi0})
+// real rings from G_m (north) and G_m(i') (south), m <= mtop (packed_spectrum_bin).
 __device__ void build_spectrum(double2* buf, const double2* ph, const double2* __restrict__ W,
                                long long stride_m, int n, int mtop, bool equator) {
-  for (int q = threadIdx.x; q < n; q += blockDim.x) {
-    double2 yN = make_double2(0.0, 0.0), yS = make_double2(0.0, 0.0);
-    // m = q (mod n)
-    for (int m = q; m <= mtop; m += n) {
-      const double2* w = W + (long long)m * stride_m;
-      const double c = (m == 0) ? 0.5 : 1.0;
-      yN = cadd(yN, cscale(cmul(ph[m], w[0]), c));
-      if (!equator) yS = cadd(yS, cscale(cmul(ph[m], w[1]), c));
-    }
-    // m = -q (mod n)
-    const int q2 = (q == 0) ? 0 : n - q;
-    for (int m = q2; m <= mtop; m += n) {
-      const double2* w = W + (long long)m * stride_m;
-      const double c = (m == 0) ? 0.5 : 1.0;
-      yN = cadd(yN, cscale(cconj(cmul(ph[m], w[0])), c));
-      if (!equator) yS = cadd(yS, cscale(cconj(cmul(ph[m], w[1])), c));
-    }
-    buf[sw(q)] = make_double2(yN.x - yS.y, yN.y + yS.x);   // Y_N + i Y_S
-  }
-}
-
-// Bin q of one ring's Hermitian spectrum (side 0: north from G_N, side 1: south from G_S),
-// the aliased sum build_spectrum forms for both rings at once.
-__device__ __forceinline__ double2 spectrum_bin(const double2* ph, const double2* __restrict__ W,
-                                                long long stride_m, int n, int mtop, int side,
-                                                int q) {
-  double2 y = make_double2(0.0, 0.0);
-  for (int m = q; m <= mtop; m += n) {
-    const double c = (m == 0) ? 0.5 : 1.0;
-    y = cadd(y, cscale(cmul(ph[m], W[(long long)m * stride_m + side]), c));
-  }
-  const int q2 = (q == 0) ? 0 : n - q;
-  for (int m = q2; m <= mtop; m += n) {
-    const double c = (m == 0) ? 0.5 : 1.0;
-    y = cadd(y, cscale(cconj(cmul(ph[m], W[(long long)m * stride_m + side])), c));
-  }
-  return y;
+  for (int q = threadIdx.x; q < n; q += blockDim.x)
+    buf[sw(q)] = packed_spectrum_bin(ph, W, stride_m, n, mtop, equator, q);
 }
 
 __global__ void __launch_bounds__(512, 2) k_ring_fft_inv(InvArgs a) {
@@ -661,6 +625,7 @@ int fsht_launch_ring_fft_fwd(fsht_plan* p, const double* maps, long long map_str
 
 int fsht_launch_ring_fft_inv(fsht_plan* p, const double2* W, double* maps, long long map_stride,
                              int kc, cudaStream_t s) {
+  if (p->d_tw_df) return fsht_launch_ring_fft_inv_df(p, W, maps, map_stride, kc, s);
   InvArgs a;
   a.W = W;
   a.maps = maps;

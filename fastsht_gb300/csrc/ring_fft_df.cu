@@ -76,7 +76,7 @@ __device__ __forceinline__ int load_scaled(cdd* buf, int cnt, const double* xa, 
   return sh;
 }
 
-__global__ void __launch_bounds__(512, 2) k_ring_fft_fwd_df(FwdDfArgs a) {
+__global__ void __launch_bounds__(1024, 1) k_ring_fft_fwd_df(FwdDfArgs a) {
   extern __shared__ float4 smem4[];
   __shared__ int s_emax[2];
   const int i = a.ring_base + blockIdx.x;      // north ring index
@@ -125,11 +125,11 @@ __global__ void __launch_bounds__(512, 2) k_ring_fft_fwd_df(FwdDfArgs a) {
           const int kk = cj ? n - q : q;
           const cdd za = buf[sw(dft_bin(rf, kk == nd ? 0 : kk))];
           const cdd zb = cconj(buf[sw(dft_bin(rf, kk == 0 ? 0 : nd - kk))]);
-          const cdd e = cadd(za, zb);                          // 2 E
-          const cdd o = cmul_mi(csub(za, zb));                 // 2 O
-          cdd xq = cadd(e, cmul(o, ldg_cdd(&rtw[kk])));        // 2 X
+          const cdd e = cadd_lz(za, zb);                       // 2 E
+          const cdd o = cmul_mi(csub_lz(za, zb));              // 2 O
+          cdd xq = cadd_lz(e, cmul_lz(o, ldg_cdd(&rtw[kk])));  // 2 X
           if (cj) xq = cconj(xq);
-          const double2 f = cdd_to_fp64(cmul(xq, ph[m]), sh);
+          const double2 f = cdd_to_fp64(cmul_lz(xq, ph[m]), sh);
           double2* w = a.W + (((long long)m * a.nnorth + i) * a.kc + k) * 2;
           if (side == 0) {
             w[0] = f;
@@ -151,23 +151,156 @@ __global__ void __launch_bounds__(512, 2) k_ring_fft_fwd_df(FwdDfArgs a) {
     const int sh = load_scaled(buf, n, xn, equator ? nullptr : xs, 1, &s_emax[it & 1]);
     ring_dft(buf, rf, a.tw, chirp, bhat);
     // Z = FFT(x_N + i x_S): X_N[q] = (Z[q] + conj Z[-q])/2, X_S[q] = (Z[q] - conj Z[-q])/(2i)
-    for (int m = tid; m <= mtop; m += nt) {
-      const int q = m % n;
+    // q = m mod n and the output pointer advance by fixed steps (no division per m)
+    const int qstep = nt % n;
+    const long long wstep = (long long)nt * a.nnorth * a.kc * 2;
+    int q = tid % n;
+    double2* w = a.W + (((long long)tid * a.nnorth + i) * a.kc + k) * 2;
+    for (int m = tid; m <= mtop; m += nt, w += wstep) {
       const int qn = (q == 0) ? 0 : n - q;
       const cdd zq = buf[sw(dft_bin(rf, q))];
       const cdd zn = cconj(buf[sw(dft_bin(rf, qn))]);
-      const cdd xN = cadd(zq, zn);                             // 2 X_N
-      const cdd xS = cmul_mi(csub(zq, zn));                    // 2 X_S
+      q += qstep;
+      if (q >= n) q -= n;
+      const cdd xN = cadd_lz(zq, zn);                          // 2 X_N
+      const cdd xS = cmul_mi(csub_lz(zq, zn));                 // 2 X_S
       const cdd p = ph[m];
-      double2* w = a.W + (((long long)m * a.nnorth + i) * a.kc + k) * 2;
       if (equator) {
-        const double2 fN = cdd_to_fp64(cmul(xN, p), sh);
+        const double2 fN = cdd_to_fp64(cmul_lz(xN, p), sh);
         w[0] = fN;
         w[1] = fN;
       } else {
-        w[0] = cdd_to_fp64(cmul(cadd(xN, xS), p), sh);        // F_N + F_S
-        w[1] = cdd_to_fp64(cmul(csub(xN, xS), p), sh);        // F_N - F_S
+        w[0] = cdd_to_fp64(cmul_lz(cadd_lz(xN, xS), p), sh);  // F_N + F_S
+        w[1] = cdd_to_fp64(cmul_lz(csub_lz(xN, xS), p), sh);  // F_N - F_S
       }
+    }
+  }
+}
+
+// ------------------------------------------------------------------ inverse
+struct InvDfArgs {
+  const double2* W;
+  double* maps;
+  long long map_stride;
+  int kc, maps_per_block;
+  int nside, lmax, nnorth, nring, ring_base;
+  const FshtRingFFT* rfs;
+  FftTwT<cdd> tw;
+  const cdd* chirp;
+  const cdd* bhat;
+  const double2* rtw;       // FP64: the half-ring combination runs before the conversion
+  const int* ring_i0;
+};
+
+// The FP64 values the calling thread left in buf's slots [0, cnt) (its own slots t, t + nt,
+// ...) become df64 scaled by 2^-sh, sh from the block-wide largest exponent field (em = the
+// thread's own largest); conj: store the conjugate.  emax is a shared slot that is zero on
+// entry.  Returns sh.
+__device__ __forceinline__ int convert_scaled(cdd* buf, int cnt, int em, int* emax, bool conj) {
+  const double2* raw = reinterpret_cast<const double2*>(buf);
+  const int tid = threadIdx.x, nt = blockDim.x;
+  em = __reduce_max_sync(0xffffffffu, em);
+  if ((tid & 31) == 0) atomicMax(emax, em);
+  __syncthreads();
+  const int e = *emax;
+  const int sh = (e == 0 || e == 0x7ff) ? 0 : e - 1023;
+  for (int j = tid; j < cnt; j += nt) {
+    const double2 v = raw[sw(j)];
+    buf[sw(j)] = cdd_from_raw(conj ? make_double2(v.x, -v.y) : v, sh);
+  }
+  return sh;
+}
+
+__device__ __forceinline__ int exp2f64(double2 v) {
+  return max(dd_exp_field(v.x), dd_exp_field(v.y));
+}
+
+// Synthesis side of the split form: the spectrum of each ring pair is formed from G in FP64
+// (aliasing, x2, e^{+i m phi0}: O(lmax) per ring), scaled and converted to df64, transformed
+// as conj(DFT(conj Z)) in df64, and written to the maps with one FP64 addition per pixel.
+__global__ void __launch_bounds__(1024, 1) k_ring_fft_inv_df(InvDfArgs a) {
+  extern __shared__ float4 smem4[];
+  __shared__ int s_emax[2];
+  const int i = a.ring_base + blockIdx.x;
+  const FshtRingFFT rf = a.rfs[i];
+  const int n = rf.n;
+  cdd* buf = reinterpret_cast<cdd*>(smem4);
+  double2* raw = reinterpret_cast<double2*>(smem4);
+  double2* ph = reinterpret_cast<double2*>(smem4 + rf.P);   // e^{+i m phi0}, FP64
+  const int tid = threadIdx.x, nt = blockDim.x;
+  const bool equator = (i == a.nnorth - 1);
+  const int ip = a.nring - 1 - i;
+  const long long off_n = ring_start(a.nside, i);
+  const long long off_s = ring_start(a.nside, ip);
+  const int sflag = ring_phase_flag(a.nside, i);
+  int mtop = a.lmax;
+  while (mtop >= 0 && a.ring_i0[mtop] > i) --mtop;
+  for (int m = tid; m <= mtop; m += nt) {
+    double s = 0.0, c = 1.0;
+    if (sflag) {
+      long long r = (long long)m % (2LL * n);
+      sincospi((double)r / (double)n, &s, &c);
+    }
+    ph[m] = make_double2(c, s);
+  }
+  if (tid < 2) s_emax[tid] = 0;
+  const int k_begin = blockIdx.y * a.maps_per_block;
+  const int k_end = min(a.kc, k_begin + a.maps_per_block);
+  const cdd* chirp = a.chirp + rf.chirp_off;
+  const cdd* bhat = a.bhat + rf.bhat_off;
+  const long long stride_m = (long long)a.nnorth * a.kc * 2;
+  int it = 0;
+  if (rf.nd != n) {
+    // Half-length ring: x_{2j} + i x_{2j+1} = sum_k Z_k e^{2 pi i jk/nd} with
+    // Z_k = (Y_k + Y_{k+nd}) + i (Y_k - Y_{k+nd}) e^{2 pi i k/n}, one ring at a time.
+    const int nd = rf.nd;
+    const double2* rtw = a.rtw + rf.rtw_off;
+    for (int k = k_begin; k < k_end; ++k) {
+      const double2* Wk = a.W + ((long long)i * a.kc + k) * 2;
+      for (int side = 0; side < 2; ++side, ++it) {
+        __syncthreads();
+        if (tid == 0) s_emax[(it & 1) ^ 1] = 0;
+        int em = 0;
+        for (int kk = tid; kk < nd; kk += nt) {
+          const double2 y0 = spectrum_bin(ph, Wk, stride_m, n, mtop, side, kk);
+          const double2 y1 = spectrum_bin(ph, Wk, stride_m, n, mtop, side, kk + nd);
+          const double2 b = cmul(csub(y0, y1), cconj(__ldg(&rtw[kk])));
+          const double2 sa = cadd(y0, y1);
+          const double2 v = cconj(make_double2(sa.x - b.y, sa.y + b.x));   // conj(A + i B)
+          raw[sw(kk)] = v;
+          em = max(em, exp2f64(v));
+        }
+        const int sh = convert_scaled(buf, nd, em, &s_emax[it & 1], false);
+        ring_dft(buf, rf, a.tw, chirp, bhat);
+        double* x = a.maps + (long long)k * a.map_stride + (side ? off_s : off_n);
+        for (int j = tid; j < nd; j += nt) {
+          const cdd z = buf[sw(dft_bin(rf, j))];   // conj(z): x_{2j} = Re, x_{2j+1} = -Im
+          x[2 * j] = dd_to_double(z.h.x, z.l.x, sh);
+          x[2 * j + 1] = -dd_to_double(z.h.y, z.l.y, sh);
+        }
+      }
+    }
+    return;
+  }
+  for (int k = k_begin; k < k_end; ++k, ++it) {
+    const double2* Wk = a.W + ((long long)i * a.kc + k) * 2;
+    __syncthreads();
+    if (tid == 0) s_emax[(it & 1) ^ 1] = 0;
+    int em = 0;
+    for (int q = tid; q < n; q += nt) {
+      const double2 z = packed_spectrum_bin(ph, Wk, stride_m, n, mtop, equator, q);
+      raw[sw(q)] = z;
+      em = max(em, exp2f64(z));
+    }
+    // inverse DFT = conj(DFT(conj Z))
+    const int sh = convert_scaled(buf, n, em, &s_emax[it & 1], true);
+    ring_dft(buf, rf, a.tw, chirp, bhat);
+    double* xn = a.maps + (long long)k * a.map_stride + off_n;
+    double* xs = a.maps + (long long)k * a.map_stride + off_s;
+    for (int j = tid; j < n; j += nt) {
+      const cdd z = buf[sw(dft_bin(rf, j))];   // x_N = Re, x_S = -Im of the DFT
+      xn[j] = dd_to_double(z.h.x, z.l.x, sh);
+      if (!equator) xs[j] = -dd_to_double(z.h.y, z.l.y, sh);
     }
   }
 }
@@ -179,6 +312,13 @@ __global__ void k_to_cdd(const double2* __restrict__ in, float4* out, long long 
     const cdd c = cdd_from_fp64(v.x, v.y);
     out[j] = make_float4(c.h.x, c.h.y, c.l.x, c.l.y);
   }
+}
+
+// Threads per CTA: the autotuned shape, else 1024 for segments whose shared memory allows one
+// CTA per SM (32 warps to hide the pass barriers and twiddle loads) and 512 for two per SM.
+int df_threads(const fsht_plan* p, long long smem) {
+  if (p->fft_threads > 0) return p->fft_threads;
+  return smem > 112 * 1024 ? 1024 : 512;
 }
 
 int to_cdd(const double2* in, float4** out, long long n, cudaStream_t s) {
@@ -233,7 +373,42 @@ int fsht_launch_ring_fft_fwd_df(fsht_plan* p, const double* maps, long long map_
     const long long* sg = p->fft_seg + 3 * sgi;
     a.ring_base = (int)sg[0];
     dim3 grid((unsigned)(sg[1] - sg[0]), (kc + a.maps_per_block - 1) / a.maps_per_block);
-    k_ring_fft_fwd_df<<<grid, p->fft_threads > 0 ? p->fft_threads : 512, (size_t)sg[2], s>>>(a);
+    k_ring_fft_fwd_df<<<grid, df_threads(p, sg[2]), (size_t)sg[2], s>>>(a);
+    FSHT_LAUNCH_CHECK();
+  }
+  return FSHT_OK;
+}
+
+int fsht_launch_ring_fft_inv_df(fsht_plan* p, const double2* W, double* maps,
+                                long long map_stride, int kc, cudaStream_t s) {
+  InvDfArgs a;
+  a.W = W;
+  a.maps = maps;
+  a.map_stride = map_stride;
+  a.kc = kc;
+  a.nside = p->nside;
+  a.lmax = p->lmax;
+  a.nnorth = p->nnorth;
+  a.nring = p->nring;
+  a.ring_base = 0;
+  a.rfs = p->d_rfft;
+  a.tw.tw2 = reinterpret_cast<const cdd*>(p->d_tw_df);
+  a.tw.tw3 = reinterpret_cast<const cdd*>(p->d_tw_df) + p->Tmax;
+  a.tw.logTmax = p->logTmax;
+  a.tw.P3max = p->P3max;
+  a.chirp = reinterpret_cast<const cdd*>(p->d_chirp_df);
+  a.bhat = reinterpret_cast<const cdd*>(p->d_bhat_df);
+  a.rtw = p->d_rtw;
+  a.ring_i0 = p->d_ring_i0;
+  a.maps_per_block = p->fft_mpb > 0 ? p->fft_mpb : fsht_fft_maps_per_block(kc, p->nnorth);
+  FSHT_CUDA_TRY(cudaFuncSetAttribute(k_ring_fft_inv_df,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)p->fft_smem));
+  for (int sgi = 0; sgi < p->fft_nseg; ++sgi) {
+    const long long* sg = p->fft_seg + 3 * sgi;
+    a.ring_base = (int)sg[0];
+    dim3 grid((unsigned)(sg[1] - sg[0]), (kc + a.maps_per_block - 1) / a.maps_per_block);
+    k_ring_fft_inv_df<<<grid, df_threads(p, sg[2]), (size_t)sg[2], s>>>(a);
     FSHT_LAUNCH_CHECK();
   }
   return FSHT_OK;

@@ -3,6 +3,7 @@
 // pair order of m, the triangular (l, m) table index and the WS row size.
 #pragma once
 #include "common.cuh"
+#include "df64.cuh"
 #include "tcgen05.cuh"
 
 #include <cmath>
@@ -81,15 +82,37 @@ size_t ws_row_bytes(int lmax, int nnorth) {
 // Levels 0..3 of one output element (FP32 accumulators, weights 1, 2^-8, 2^-16, 2^-24):
 // levels 0 and 1 are exact integers, so their weighted sum is exact as an FP32 (hi, lo)
 // pair (two-sum); levels 2 and 3 only touch lo.
-__device__ __forceinline__ double combine_levels(uint32_t v0, uint32_t v1, uint32_t v2,
-                                                 uint32_t v3) {
+__device__ __forceinline__ void combine_levels_pair(uint32_t v0, uint32_t v1, uint32_t v2,
+                                                    uint32_t v3, float& hi, float& lo) {
   const float L0 = __uint_as_float(v0);
   const float L1f = __uint_as_float(v1) * 0x1p-8f;
-  const float hi = L0 + L1f;
+  hi = L0 + L1f;
   const float bv = hi - L0;
-  const float lo = ((L0 - (hi - bv)) + (L1f - bv)) +
-                   (__uint_as_float(v2) * 0x1p-16f + __uint_as_float(v3) * 0x1p-24f);
-  return (double)hi + (double)lo;
+  lo = ((L0 - (hi - bv)) + (L1f - bv)) +
+       (__uint_as_float(v2) * 0x1p-16f + __uint_as_float(v3) * 0x1p-24f);
+}
+
+// The element times (fh + fl) 2^e as an FP64.  The product of the (hi, lo) pair with the
+// df64 factor is formed on the FP32 pipe (the high product exact through fmaf, the cross
+// terms in the low part, ~2^-46 relative), the power of two goes into the exponent fields
+// and one FP64 addition joins the two parts: one FP64 instruction per element instead of
+// five (two conversions, an addition, two multiplications).  Exponents below the FP64 range
+// give 0, so an empty column (exponent kEmptyExp) writes zeros.
+__device__ __forceinline__ double levels_scaled(uint32_t v0, uint32_t v1, uint32_t v2,
+                                                uint32_t v3, float fh, float fl, int e) {
+  float hi, lo;
+  combine_levels_pair(v0, v1, v2, v3, hi, lo);
+  const float p = __fmul_rn(hi, fh);
+  float q = __fmaf_rn(hi, fh, -p);
+  q = __fmaf_rn(hi, fl, q);
+  q = __fmaf_rn(lo, fh, q);
+  return dd_to_double(p, q, e);
+}
+
+// A positive or negative FP64 factor as a df64 pair (setup, once per row).
+__device__ __forceinline__ void factor_pair(double x, float& fh, float& fl) {
+  fh = __double2float_rn(x);
+  fl = __double2float_rn(x - (double)fh);
 }
 
 }  // namespace

@@ -156,6 +156,9 @@ int fsht_profile_read(fsht_plan* plan, int ncat, int* launches, double* total_ms
 /* Measures this device's FP64 FMA throughput (TFLOP/s) with a DFMA loop kernel:
  * the roofline denominator for the FP64 kernels. */
 int fsht_measure_fp64_peak(double* tflops);
+/* The same for FP32 FMAs: the roofline denominator of the split form's ring FFT, which
+ * runs in df64 (FP32-pair) arithmetic. */
+int fsht_measure_fp32_peak(double* tflops);
 
 /* Runs one stage of the pipeline on device buffers (testing and profiling hook;
  * no counterpart in the reference, whose stages are internal):
@@ -214,10 +217,11 @@ int fsht_job_workspace(const fsht_plan* tables, const fsht_job* job, int maps_pe
 int fsht_run_job(const fsht_plan* tables, const fsht_job* job, void* workspace,
                  size_t workspace_bytes, void* stream);
 
-/* Autotuner: times the ring-FFT launch shapes (maps per CTA 1..16, 256 or 512
- * threads) on sample_maps maps and keeps the fastest in the plan; results are
- * cached per (nside, lmax bucket of 256, sample_maps) for the process.  No
- * counterpart in the reference. */
+/* Autotuner: times the ring-FFT launch shapes (maps per CTA 1..16; 256 or 512
+ * threads, or 0 = the per-segment default: 512, and 1024 where a segment runs one CTA
+ * per SM in the split form) on sample_maps maps and keeps the fastest in the plan;
+ * results are cached per (nside, lmax bucket of 256, sample_maps, precision) for the
+ * process.  No counterpart in the reference. */
 int fsht_plan_autotune(fsht_plan* plan, int sample_maps);
 int fsht_plan_tuning(const fsht_plan* plan, int* maps_per_block, int* threads);
 
