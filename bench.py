@@ -651,9 +651,25 @@ def e2e(sht, maps_dev, ke, args, world):
         sht.t2alm(maps_np, alms_in=out_np)
     torch.cuda.synchronize()
     dt = time.perf_counter() - t0
+    # the copies alone (pinned host <-> device, the first 64 maps): the host link's rate
+    kc = min(ke, 64)
+    dmaps = torch.empty((kc, npix), dtype=torch.float64, device=maps_dev.device)
+    dalm = torch.empty((kc, L * L), dtype=torch.float64, device=maps_dev.device)
+    halm = out_t.reshape(-1)[: kc * L * L].view(kc, L * L)
+    for _ in range(2):                           # the second pass is the measurement
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        dmaps.copy_(host[:kc], non_blocking=True)
+        torch.cuda.synchronize()
+        t2 = time.perf_counter()
+        halm.copy_(dalm, non_blocking=True)
+        torch.cuda.synchronize()
+        t3 = time.perf_counter()
+    del dmaps, dalm
     return {"value": world * ke * args.steps / dt, "unit": UNIT,
             "h2d_bytes_per_step": ke * npix * 8, "d2h_bytes_per_step": ke * L * L * 8,
-            "maps_per_step": ke}
+            "maps_per_step": ke, "ms_per_step": 1000.0 * dt / args.steps,
+            "h2d_gbs": kc * npix * 8 / (t2 - t1) / 1e9, "d2h_gbs": kc * L * L * 8 / (t3 - t2) / 1e9}
 
 
 # ---------------------------------------------------------------- batched form

@@ -46,6 +46,7 @@ SIGNATURES = {
     "fsht_plan_info": [_vp, C.POINTER(_sz), C.POINTER(_i)],
     "fsht_plan_ring_skip": [_vp, C.POINTER(_i)],
     "fsht_t2alm": [_vp, _vp, _vp, _i, _i, _i],
+    "fsht_t2alm_host": [_vp, _vp, _vp, _vp, _vp, _i, _i, _i],
     "fsht_alm2t": [_vp, _vp, _vp, _i],
     "fsht_t2alm_noalloc": [_i, _i, _vp, _vp, _i, _vp],
     "fsht_qu2eb": [_vp, _vp, _vp, _vp, _vp, _i, _i],

@@ -80,6 +80,16 @@ FSHT_HD void fsht_ring_fft_size(FshtRingFFT& r) {
   }
 }
 
+// Twiddle table, packed per pass so that the threads of a warp read consecutive entries:
+//   radix-4 part: for each span S = 2^s, s = 3..logTmax, at 3 (2^s - 8) / 4 the triples
+//                 (w^j, w^2j, w^3j), w = exp(-2 pi i / S), j < S/4
+//   radix-3 part: for each size P = 3 * 2^k, k = 0..log2(P3max / 3), at R4 + 2 (2^k - 1) the
+//                 pairs (w^j, w^2j), w = exp(-2 pi i / P), j < 2^k
+FSHT_HD long long fsht_tw_r4_entries(int Tmax) { return Tmax >= 8 ? 3LL * (2 * Tmax - 8) / 4 : 0; }
+FSHT_HD long long fsht_tw_entries(int Tmax, int P3max) {
+  return fsht_tw_r4_entries(Tmax) + (P3max > 0 ? 2LL * (2 * (P3max / 3) - 1) : 0);
+}
+
 // Split-precision form: per (l, m) row of the scaled recursion (legendre_split.cu).
 struct FshtLamRow {
   double beta;   // mu_l = x mu_{l-1} - beta mu_{l-2}
@@ -110,7 +120,7 @@ struct fsht_plan {
   double2* d_chirp;                // Bluestein chirps
   double2* d_rtw;                  // half-length rings: exp(-2 pi i k / n)
   double2* d_bhat;                 // Bluestein filter spectra
-  double2* d_tw;                   // [exp(-2 pi i t / Tmax), t < Tmax][exp(-2 pi i t / P3max), t < P3max]
+  double2* d_tw;                   // twiddles, packed per pass (fsht_tw_entries)
   long long fft_chirp_total, fft_bhat_total, fft_rtw_total;   // entries of the three tables
   // df64 copies (float4 = {re hi, im hi, re lo, im lo}) of the twiddle, chirp, filter and
   // half-ring tables: split-precision plans only (their forward FFT runs in df64)
@@ -150,6 +160,9 @@ struct fsht_plan {
   cudaStream_t aux;
   unsigned char* d_lbuf2;
   cudaEvent_t ev[6];
+  // host-buffer entry points: copy stream and its events (fork, maps landed, wave done, join)
+  cudaStream_t xfer;
+  cudaEvent_t evx[4];
   int wave_qmax;                   // most orders in one wave
   FshtPolRow* d_poltab;            // spin-2 plans only, same triangular index as d_lamtab
 };
@@ -204,7 +217,13 @@ int fsht_launch_ring_fft_fwd(fsht_plan* p, const double* maps, long long map_str
 // inverse transforms, which fsht_launch_ring_fft_fwd / _inv select when they exist.
 int fsht_fft_df_tables_init(fsht_plan* p);
 int fsht_launch_ring_fft_fwd_df(fsht_plan* p, const double* maps, long long map_stride,
-                                int kc, double2* W, cudaStream_t s);
+                                int kc, int k0, int kb, double2* W, cudaStream_t s);
+// The forward transform of maps [k0, k0 + kb) of a chunk of kc maps (W keeps the chunk's
+// map stride kc), for transfers that land in parts.
+int fsht_launch_ring_fft_fwd_part(fsht_plan* p, const double* maps, long long map_stride,
+                                  int kc, int k0, int kb, double2* W, cudaStream_t s);
+// Pair-order range [q0, q1) of the orders in wave w of a split-precision plan.
+void fsht_split_wave_range(const fsht_plan* p, int w, int* q0, int* q1);
 int fsht_launch_ring_fft_inv_df(fsht_plan* p, const double2* W, double* maps,
                                 long long map_stride, int kc, cudaStream_t s);
 // Maps per CTA of the ring-FFT launches when the autotuner has not set one.

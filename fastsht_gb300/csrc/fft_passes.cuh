@@ -9,14 +9,12 @@
 #include "common.cuh"
 #include "df64.cuh"
 
-// Twiddle tables of one element type: tw2[t] = exp(-2 pi i t / Tmax), t < Tmax (full circle,
-// Tmax the largest power-of-two factor of any transform size), tw3[t] = exp(-2 pi i t / P3max)
-// for the 3*2^k sizes.
+// Twiddle tables of one element type, packed per pass (fsht_tw_entries in common.cuh): r4 the
+// radix-4 triples of each span, r3 the radix-3 pairs of each 3*2^k size.
 template <class E>
 struct FftTwT {
-  const E* tw2;
-  const E* tw3;
-  int logTmax, P3max;
+  const E* r4;
+  const E* r3;
 };
 using FftTw = FftTwT<double2>;
 
@@ -48,11 +46,25 @@ template <> __device__ __forceinline__ cdd zero_e<cdd>() { return cdd_zero(); }
 
 }  // namespace fftp
 
-// Shared-memory position of transform element i: the low three bits of the index (eight
-// 16-byte elements = one 128-byte bank row) are XORed with the next three, so the strided
-// accesses of the radix-4 passes with small spans spread over the banks; a bijection within
-// every block of 64 elements.
-__device__ __forceinline__ int sw(int i) { return i ^ ((i >> 3) & 7); }
+// Shared-memory position of transform element i of a ring's buffer: the low three bits (eight
+// 16-byte elements = one 128-byte bank row) are XORed with a function of the row r = i >> 3,
+// so every group of eight threads of a warp touches eight different 16-byte bank groups:
+//   r ^ ((r & 2) << 1)  - the strided passes with spans 4 and 16 (rows r, r + 2 and
+//                         r .. r + 3 of one group of eight rows map to disjoint halves),
+//   r >> hs             - the top three bits of a 2^logT-point index, so bins read in
+//                         bit-reversed order (the fold after a power-of-two transform) spread
+//                         too (hs = logT - 6, at least 3 so the term is constant within a
+//                         group of eight rows).
+// A bijection: the XOR term depends on i >> 3 only.
+struct Swz {
+  int hs;
+  __device__ __forceinline__ explicit Swz(const FshtRingFFT& rf)
+      : hs(rf.logT > 9 ? rf.logT - 6 : 3) {}
+  __device__ __forceinline__ int operator()(int i) const {
+    const int r = i >> 3;
+    return i ^ ((r ^ ((r & 2) << 1) ^ (r >> hs)) & 7);
+  }
+};
 
 // In-place decimation-in-frequency FFT of rf.P points in shared memory, natural order in,
 // transform order out: an optional radix-3 pass (P = 3 T) splits the data into three
@@ -64,17 +76,18 @@ __device__ __forceinline__ int sw(int i) { return i ^ ((i >> 3) & 7); }
 template <class E>
 __device__ void fft_dif(E* buf, const FshtRingFFT& rf, const FftTwT<E>& tw, int nz) {
   using namespace fftp;
+  const Swz S(rf);
   constexpr bool kF64 = std::is_same<E, double2>::value;
   const int tid = threadIdx.x, nt = blockDim.x;
   const int logT = rf.logT, T = 1 << logT;
   const int nblk = rf.r3 ? 3 : 1;
   __syncthreads();   // the caller's writes to buf must land first
   if (rf.r3) {
-    const int sc = tw.P3max / rf.P;
+    const E* t3 = tw.r3 + 2 * (T - 1);
     const bool c_zero = nz <= 2 * T;   // the third input of every butterfly is padding
     for (int j = tid; j < T; j += nt) {
-      const E a = buf[sw(j)], b = buf[sw(j + T)];
-      const E c = c_zero ? zero_e<E>() : buf[sw(j + 2 * T)];
+      const E a = buf[S(j)], b = buf[S(j + T)];
+      const E c = c_zero ? zero_e<E>() : buf[S(j + 2 * T)];
       const E sm = c_zero ? b : ladd(b, c), df = c_zero ? b : lsub(b, c);
       E y1, y2;
       // w3 = exp(-2 pi i / 3): a + w3 b + w3^2 c = t - i (sqrt3/2) df, the other t + i ...
@@ -88,9 +101,9 @@ __device__ void fft_dif(E* buf, const FshtRingFFT& rf, const FftTwT<E>& tw, int 
         y1 = lsub(t, u);
         y2 = ladd(t, u);
       }
-      buf[sw(j)] = fin(ladd(a, sm));
-      buf[sw(j + T)] = fin(lmul(y1, ldg_e(&tw.tw3[j * sc])));
-      buf[sw(j + 2 * T)] = fin(lmul(y2, ldg_e(&tw.tw3[2 * j * sc])));
+      buf[S(j)] = fin(ladd(a, sm));
+      buf[S(j + T)] = fin(lmul(y1, ldg_e(&t3[2 * j])));
+      buf[S(j + 2 * T)] = fin(lmul(y2, ldg_e(&t3[2 * j + 1])));
     }
     __syncthreads();
   }
@@ -98,7 +111,7 @@ __device__ void fft_dif(E* buf, const FshtRingFFT& rf, const FftTwT<E>& tw, int 
   for (; logspan >= 2; logspan -= 2) {
     const int lh = logspan - 2, h = 1 << lh;
     const int per_blk = 1 << (logT - 2);
-    const int sh = tw.logTmax - logspan;
+    const E* t4 = tw.r4 + 3 * ((1 << logspan) - 8) / 4;   // used when h > 1
     // first pass over zero-padded data: the inputs at i0 + 2h, i0 + 3h are all padding
     const bool cd_zero = !rf.r3 && logspan == logT && nz <= 2 * h;
     for (int idx = tid; idx < nblk * per_blk; idx += nt) {
@@ -108,11 +121,11 @@ __device__ void fft_dif(E* buf, const FshtRingFFT& rf, const FftTwT<E>& tw, int 
       const int i0 = (blk << logT) + ((r >> lh) << logspan) + j;
       E apc, amc, bpd, bmd;
       if (cd_zero) {
-        apc = amc = buf[sw(i0)];
-        bpd = bmd = buf[sw(i0 + h)];
+        apc = amc = buf[S(i0)];
+        bpd = bmd = buf[S(i0 + h)];
       } else {
-        const E a = buf[sw(i0)], b = buf[sw(i0 + h)], c = buf[sw(i0 + 2 * h)],
-                d = buf[sw(i0 + 3 * h)];
+        const E a = buf[S(i0)], b = buf[S(i0 + h)], c = buf[S(i0 + 2 * h)],
+                d = buf[S(i0 + 3 * h)];
         apc = ladd(a, c);
         amc = lsub(a, c);
         bpd = ladd(b, d);
@@ -122,24 +135,24 @@ __device__ void fft_dif(E* buf, const FshtRingFFT& rf, const FftTwT<E>& tw, int 
       const E mib = cmul_mi(bmd);
       const E y2 = ladd(amc, mib);   // (a-c) - i(b-d)
       const E y3 = lsub(amc, mib);   // (a-c) + i(b-d)
-      buf[sw(i0)] = fin(ladd(apc, bpd));
+      buf[S(i0)] = fin(ladd(apc, bpd));
       if (h == 1) {
-        buf[sw(i0 + h)] = fin(y1);
-        buf[sw(i0 + 2 * h)] = fin(y2);
-        buf[sw(i0 + 3 * h)] = fin(y3);
+        buf[S(i0 + h)] = fin(y1);
+        buf[S(i0 + 2 * h)] = fin(y2);
+        buf[S(i0 + 3 * h)] = fin(y3);
       } else {
-        buf[sw(i0 + h)] = fin(lmul(y1, ldg_e(&tw.tw2[(2 * j) << sh])));
-        buf[sw(i0 + 2 * h)] = fin(lmul(y2, ldg_e(&tw.tw2[j << sh])));
-        buf[sw(i0 + 3 * h)] = fin(lmul(y3, ldg_e(&tw.tw2[(3 * j) << sh])));
+        buf[S(i0 + h)] = fin(lmul(y1, ldg_e(&t4[3 * j + 1])));
+        buf[S(i0 + 2 * h)] = fin(lmul(y2, ldg_e(&t4[3 * j])));
+        buf[S(i0 + 3 * h)] = fin(lmul(y3, ldg_e(&t4[3 * j + 2])));
       }
     }
     __syncthreads();
   }
   if (logspan == 1) {
     for (int idx = tid; idx < nblk << (logT - 1); idx += nt) {
-      const E a = buf[sw(2 * idx)], b = buf[sw(2 * idx + 1)];
-      buf[sw(2 * idx)] = fin(ladd(a, b));
-      buf[sw(2 * idx + 1)] = fin(lsub(a, b));
+      const E a = buf[S(2 * idx)], b = buf[S(2 * idx + 1)];
+      buf[S(2 * idx)] = fin(ladd(a, b));
+      buf[S(2 * idx + 1)] = fin(lsub(a, b));
     }
     __syncthreads();
   }
@@ -151,6 +164,7 @@ __device__ void fft_dif(E* buf, const FshtRingFFT& rf, const FftTwT<E>& tw, int 
 template <class E>
 __device__ void fft_dit_inv(E* buf, const FshtRingFFT& rf, const FftTwT<E>& tw, int nout) {
   using namespace fftp;
+  const Swz S(rf);
   constexpr bool kF64 = std::is_same<E, double2>::value;
   const int tid = threadIdx.x, nt = blockDim.x;
   const int logT = rf.logT, T = 1 << logT;
@@ -159,9 +173,9 @@ __device__ void fft_dit_inv(E* buf, const FshtRingFFT& rf, const FftTwT<E>& tw, 
   int logspan = 2;
   if (logT & 1) {
     for (int idx = tid; idx < nblk << (logT - 1); idx += nt) {
-      const E a = buf[sw(2 * idx)], b = buf[sw(2 * idx + 1)];
-      buf[sw(2 * idx)] = fin(ladd(a, b));
-      buf[sw(2 * idx + 1)] = fin(lsub(a, b));
+      const E a = buf[S(2 * idx)], b = buf[S(2 * idx + 1)];
+      buf[S(2 * idx)] = fin(ladd(a, b));
+      buf[S(2 * idx + 1)] = fin(lsub(a, b));
     }
     __syncthreads();
     logspan = 3;
@@ -169,20 +183,20 @@ __device__ void fft_dit_inv(E* buf, const FshtRingFFT& rf, const FftTwT<E>& tw, 
   for (; logspan <= logT; logspan += 2) {
     const int lh = logspan - 2, h = 1 << lh;
     const int per_blk = 1 << (logT - 2);
-    const int sh = tw.logTmax - logspan;
+    const E* t4 = tw.r4 + 3 * ((1 << logspan) - 8) / 4;   // used when h > 1
     const bool low_half = !rf.r3 && logspan == logT && nout <= 2 * h;   // outputs < 2h only
     for (int idx = tid; idx < nblk * per_blk; idx += nt) {
       const int blk = idx >> (logT - 2);
       const int r = idx & (per_blk - 1);
       const int j = r & (h - 1);
       const int i0 = (blk << logT) + ((r >> lh) << logspan) + j;
-      const E y0 = buf[sw(i0)];
-      const E y1 = buf[sw(i0 + h)], y2 = buf[sw(i0 + 2 * h)], y3 = buf[sw(i0 + 3 * h)];
+      const E y0 = buf[S(i0)];
+      const E y1 = buf[S(i0 + h)], y2 = buf[S(i0 + 2 * h)], y3 = buf[S(i0 + 3 * h)];
       E sp, dm, e, f;
       if (h > 1) {
-        const E w1 = ldg_e(&tw.tw2[j << sh]);
-        const E w2 = ldg_e(&tw.tw2[(2 * j) << sh]);
-        const E w3 = ldg_e(&tw.tw2[(3 * j) << sh]);
+        const E w1 = ldg_e(&t4[3 * j]);
+        const E w2 = ldg_e(&t4[3 * j + 1]);
+        const E w3 = ldg_e(&t4[3 * j + 2]);
         if constexpr (kF64) {
           // twiddles folded into the adds: sp = y0 + conj(w2) y1 and e = conj(w1) y2 +
           // conj(w3) y3 as FMA chains, dm = 2 y0 - sp, f = 2 z2 - e (24 FP64 ops, not 28)
@@ -207,34 +221,34 @@ __device__ void fft_dit_inv(E* buf, const FshtRingFFT& rf, const FftTwT<E>& tw, 
         f = lsub(y2, y3);
       }
       const E mif = cmul_mi(f);
-      buf[sw(i0)] = fin(ladd(sp, e));
-      buf[sw(i0 + h)] = fin(lsub(dm, mif));         // d + i f
+      buf[S(i0)] = fin(ladd(sp, e));
+      buf[S(i0 + h)] = fin(lsub(dm, mif));         // d + i f
       if (!low_half) {
-        buf[sw(i0 + 2 * h)] = fin(lsub(sp, e));
-        buf[sw(i0 + 3 * h)] = fin(ladd(dm, mif));   // d - i f
+        buf[S(i0 + 2 * h)] = fin(lsub(sp, e));
+        buf[S(i0 + 3 * h)] = fin(ladd(dm, mif));   // d - i f
       }
     }
     __syncthreads();
   }
   if (rf.r3) {
-    const int sc = tw.P3max / rf.P;
+    const E* t3 = tw.r3 + 2 * (T - 1);
     const bool two_blocks = nout <= 2 * T;   // the third block is not wanted
     for (int j = tid; j < T; j += nt) {
-      const E a = buf[sw(j)];
-      const E b = lmulc(buf[sw(j + T)], ldg_e(&tw.tw3[j * sc]));
-      const E c = lmulc(buf[sw(j + 2 * T)], ldg_e(&tw.tw3[2 * j * sc]));
+      const E a = buf[S(j)];
+      const E b = lmulc(buf[S(j + T)], ldg_e(&t3[2 * j]));
+      const E c = lmulc(buf[S(j + 2 * T)], ldg_e(&t3[2 * j + 1]));
       const E sm = ladd(b, c), df = lsub(b, c);
-      buf[sw(j)] = fin(ladd(a, sm));
+      buf[S(j)] = fin(ladd(a, sm));
       if constexpr (kF64) {
         const double2 t = make_double2(fma(-0.5, sm.x, a.x), fma(-0.5, sm.y, a.y));
-        buf[sw(j + T)] = make_double2(fma(-kSqrt3Half, df.y, t.x), fma(kSqrt3Half, df.x, t.y));
+        buf[S(j + T)] = make_double2(fma(-kSqrt3Half, df.y, t.x), fma(kSqrt3Half, df.x, t.y));
         if (!two_blocks)
-          buf[sw(j + 2 * T)] = make_double2(fma(kSqrt3Half, df.y, t.x), fma(-kSqrt3Half, df.x, t.y));
+          buf[S(j + 2 * T)] = make_double2(fma(kSqrt3Half, df.y, t.x), fma(-kSqrt3Half, df.x, t.y));
       } else {
         const cdd t = lsub(a, cscale_p2(sm, 0.5f));
         const cdd u = cmul_pi(cscale_dd(df, kSqrt3HalfHi, kSqrt3HalfLo));
-        buf[sw(j + T)] = fin(ladd(t, u));
-        if (!two_blocks) buf[sw(j + 2 * T)] = fin(lsub(t, u));
+        buf[S(j + T)] = fin(ladd(t, u));
+        if (!two_blocks) buf[S(j + 2 * T)] = fin(lsub(t, u));
       }
     }
     __syncthreads();
@@ -254,6 +268,7 @@ template <class E>
 __device__ void ring_dft(E* buf, const FshtRingFFT& rf, const FftTwT<E>& tw,
                          const E* __restrict__ chirp, const E* __restrict__ bhat) {
   using namespace fftp;
+  const Swz S(rf);
   const int tid = threadIdx.x, nt = blockDim.x;
   if (!rf.bluestein) {
     fft_dif(buf, rf, tw, rf.P);
@@ -261,13 +276,13 @@ __device__ void ring_dft(E* buf, const FshtRingFFT& rf, const FftTwT<E>& tw,
   }
   const int n = rf.nd, P = rf.P;
   for (int j = tid; j < P; j += nt) {
-    if (j < n) buf[sw(j)] = fin(lmul(buf[sw(j)], ldg_e(&chirp[j])));
-    else buf[sw(j)] = zero_e<E>();
+    if (j < n) buf[S(j)] = fin(lmul(buf[S(j)], ldg_e(&chirp[j])));
+    else buf[S(j)] = zero_e<E>();
   }
   fft_dif(buf, rf, tw, n);
-  for (int j = tid; j < P; j += nt) buf[sw(j)] = fin(lmul(buf[sw(j)], ldg_e(&bhat[j])));
+  for (int j = tid; j < P; j += nt) buf[S(j)] = fin(lmul(buf[S(j)], ldg_e(&bhat[j])));
   fft_dit_inv(buf, rf, tw, n);
-  for (int j = tid; j < n; j += nt) buf[sw(j)] = fin(lmul(buf[sw(j)], ldg_e(&chirp[j])));
+  for (int j = tid; j < n; j += nt) buf[S(j)] = fin(lmul(buf[S(j)], ldg_e(&chirp[j])));
   __syncthreads();
 }
 

@@ -923,6 +923,12 @@ int fsht_split_tables_init(fsht_plan* p) {
   return FSHT_OK;
 }
 
+void fsht_split_wave_range(const fsht_plan* p, int w, int* q0, int* q1) {
+  const int* wv = p->h_waves + kWaveInts * w;
+  *q0 = wv[0];
+  *q1 = wv[1];
+}
+
 int fsht_launch_split_lambda(fsht_plan* p, int w, unsigned char* lbuf, cudaStream_t s) {
   const int* wv = p->h_waves + kWaveInts * w;
   LamArgs a;

@@ -50,7 +50,7 @@ ScratchLayout layout_for(int nside, int lmax, const FshtFftLayout& f) {
   L.ring_i0 = o; o = align256(o + sizeof(int) * (lmax + 1));
   L.rfs = o;     o = align256(o + sizeof(FshtRingFFT) * nn);
   L.blue = o;    o = align256(o + sizeof(int) * nn);
-  L.tw = o;      o = align256(o + sizeof(double2) * (f.Tmax + f.P3max));
+  L.tw = o;      o = align256(o + sizeof(double2) * (size_t)(fsht_tw_entries(f.Tmax, f.P3max) + 1));
   L.chirp = o;   o = align256(o + sizeof(double2) * (size_t)(f.chirp_total > 0 ? f.chirp_total : 1));
   L.bhat = o;    o = align256(o + sizeof(double2) * (size_t)(f.bhat_total > 0 ? f.bhat_total : 1));
   L.work = o;

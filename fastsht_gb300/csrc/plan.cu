@@ -101,6 +101,9 @@ void free_plan_memory(fsht_plan* p) {
   for (int i = 0; i < 6; ++i)
     if (p->ev[i]) cudaEventDestroy(p->ev[i]);
   if (p->aux) cudaStreamDestroy(p->aux);
+  for (int i = 0; i < 4; ++i)
+    if (p->evx[i]) cudaEventDestroy(p->evx[i]);
+  if (p->xfer) cudaStreamDestroy(p->xfer);
   cudaFree(p->d_poltab);
   delete[] p->h_waves;
   delete[] p->h_ring_i0;
@@ -327,6 +330,18 @@ int fsht_plan_create(int nside, int lmax, int nmaps_max, int flags, int precisio
       }
     }
   }
+  if (!tables_only) {
+    if ((ce = cudaStreamCreateWithFlags(&p->xfer, cudaStreamNonBlocking)) != cudaSuccess) {
+      fsht_set_error("copy stream: %s", cudaGetErrorString(ce));
+      return fail(FSHT_ECUDA);
+    }
+    for (int i = 0; i < 4; ++i) {
+      if ((ce = cudaEventCreateWithFlags(&p->evx[i], cudaEventDisableTiming)) != cudaSuccess) {
+        fsht_set_error("event: %s", cudaGetErrorString(ce));
+        return fail(FSHT_ECUDA);
+      }
+    }
+  }
   if ((ce = cudaStreamSynchronize(p->stream)) != cudaSuccess) {
     fsht_set_error("plan setup: %s", cudaGetErrorString(ce));
     return fail(FSHT_ECUDA);
@@ -501,11 +516,62 @@ static int lam_finish(fsht_plan* p) {
   return FSHT_OK;
 }
 
+// Host-buffer transfers of fsht_t2alm_host on the plan's copy stream: the maps land in
+// sub-batches, each forward-transformed as soon as it is on the device, and alm columns go
+// back as soon as every order they hold is final (after each wave of the split form when
+// niter = 0, else at the end of the chunk).  Column c holds Re a_lm of m = c and Im a_lm of
+// m = lmax + 1 - c, so it is final once both orders are.
+struct HostXfer {
+  const double* hmaps;
+  double* halm;
+  std::vector<char> mdone, cdone;
+};
+
+static int xfer_wait_main(fsht_plan* p, int ev) {
+  FSHT_CUDA_TRY(cudaEventRecord(p->evx[ev], p->stream));
+  FSHT_CUDA_TRY(cudaStreamWaitEvent(p->xfer, p->evx[ev], 0));
+  return FSHT_OK;
+}
+
+static int xfer_join(fsht_plan* p) {
+  FSHT_CUDA_TRY(cudaEventRecord(p->evx[3], p->xfer));
+  FSHT_CUDA_TRY(cudaStreamWaitEvent(p->stream, p->evx[3], 0));
+  return FSHT_OK;
+}
+
+// Orders of pair-order range [q0, q1) are final in the device alm of maps [c0, c0 + kc):
+// copy the columns that became complete (runs of adjacent columns as 2D copies).
+static int xfer_orders_done(fsht_plan* p, HostXfer& x, const double* dalm, int nmaps, int q0,
+                            int q1, int c0, int kc) {
+  const int lmax = p->lmax;
+  for (int q = q0; q < q1; ++q) x.mdone[(q & 1) ? lmax - (q >> 1) : (q >> 1)] = 1;
+  FSHT_TRY(xfer_wait_main(p, 2));
+  const size_t L1 = (size_t)lmax + 1, pitch = sizeof(double) * nmaps;
+  int c = 0;
+  while (c <= lmax) {
+    auto ready = [&](int cc) {
+      return !x.cdone[cc] && x.mdone[cc] && (cc == 0 || x.mdone[lmax + 1 - cc]);
+    };
+    if (!ready(c)) {
+      ++c;
+      continue;
+    }
+    int e = c;
+    while (e <= lmax && ready(e)) x.cdone[e++] = 1;
+    const size_t off = (size_t)c * L1 * nmaps + c0;
+    FSHT_CUDA_TRY(cudaMemcpy2DAsync(x.halm + off, pitch, dalm + off, pitch,
+                                    sizeof(double) * kc, (size_t)(e - c) * L1,
+                                    cudaMemcpyDeviceToHost, p->xfer));
+    c = e;
+  }
+  return FSHT_OK;
+}
+
 // One chunk's split-precision analysis of the {S, D} matrix W into alm (added when
 // accumulate), and synthesis of alm into W = {G_N, G_S}.  started: lam_start already ran
-// (before the FFT).
+// (before the FFT).  hx: copy each wave's finished alm columns to the host.
 static int split_analysis(fsht_plan* p, const double2* W, double* alm, int nmaps, int c0, int kc,
-                          int accumulate, bool started = false) {
+                          int accumulate, bool started = false, HostXfer* hx = nullptr) {
   if (!accumulate) FSHT_TRY(fsht_split_clear_alm(p, alm, nmaps, c0, kc, p->stream));
   if (!started) FSHT_TRY(lam_start(p, fsht_launch_split_lambda));
   for (int w = 0; w < p->nwaves; ++w) {
@@ -521,6 +587,11 @@ static int split_analysis(fsht_plan* p, const double2* W, double* alm, int nmaps
                                       accumulate, p->stream));
     }
     FSHT_TRY(lam_done(p, fsht_launch_split_lambda, w));
+    if (hx) {
+      int q0, q1;
+      fsht_split_wave_range(p, w, &q0, &q1);
+      FSHT_TRY(xfer_orders_done(p, *hx, alm, nmaps, q0, q1, c0, kc));
+    }
   }
   return lam_finish(p);
 }
@@ -576,26 +647,44 @@ int fsht_run_stage(fsht_plan* p, int stage, const void* in, void* out, int nmaps
 }
 
 // ----------------------------------------------------------------- temperature
-int fsht_t2alm(fsht_plan* p, const double* maps, double* alm, int nmaps, int niter, int method) {
-  FSHT_TRY(check_call(p, nmaps, maps, alm));
-  if (niter < 0 || method < 0 || method > 1) {
-    fsht_set_error("niter = %d, method = %d: need niter >= 0 and method 0 (old) or 1 (new)",
-                   niter, method);
-    return FSHT_EINVAL;
-  }
+// hx: the maps come from host memory (copied in sub-batches that the FFT consumes as they
+// land) and the alm go back to it; null: device buffers only.
+static int t2alm_impl(fsht_plan* p, const double* maps, double* alm, int nmaps, int niter,
+                      int method, HostXfer* hx) {
   FSHT_TRY(need_bufs(p, niter > 0 ? 2 : 1));
-  if (p->precision == FSHT_PREC_SPLIT) {
-    for (int c0 = 0; c0 < nmaps; c0 += p->kchunk) {
-      const int kc = nmaps - c0 < p->kchunk ? nmaps - c0 : p->kchunk;
-      double2* W0 = work_buf(p, 0, kc);
-      // the first lambda tiles are computed on the auxiliary stream during the FFT
-      FSHT_TRY(lam_start(p, fsht_launch_split_lambda));
-      {
+  const bool split = p->precision == FSHT_PREC_SPLIT;
+  if (hx) FSHT_TRY(xfer_wait_main(p, 0));   // the device buffers' earlier users are done
+  for (int c0 = 0; c0 < nmaps; c0 += p->kchunk) {
+    const int kc = nmaps - c0 < p->kchunk ? nmaps - c0 : p->kchunk;
+    double2* W0 = work_buf(p, 0, kc);
+    if (hx) {
+      hx->mdone.assign(p->lmax + 1, 0);
+      hx->cdone.assign(p->lmax + 1, 0);
+    }
+    // the first lambda tiles are computed on the auxiliary stream during the FFT
+    if (split) FSHT_TRY(lam_start(p, fsht_launch_split_lambda));
+    const double* cmaps = maps + (size_t)c0 * p->npix;
+    if (!hx) {
+      FSHT_PROF(FSHT_KCAT_FFT_FWD);
+      FSHT_TRY(fsht_launch_ring_fft_fwd(p, cmaps, p->npix, kc, W0, p->stream));
+    } else {
+      // sub-batches of a multiple of 16 maps, at most 8
+      int kb = (kc + 7) / 8;
+      kb = (kb + 15) / 16 * 16;
+      for (int k0 = 0; k0 < kc; k0 += kb) {
+        const int cnt = kc - k0 < kb ? kc - k0 : kb;
+        const size_t off = (size_t)(c0 + k0) * p->npix;
+        FSHT_CUDA_TRY(cudaMemcpyAsync(const_cast<double*>(maps) + off, hx->hmaps + off,
+                                      sizeof(double) * p->npix * cnt, cudaMemcpyHostToDevice,
+                                      p->xfer));
+        FSHT_CUDA_TRY(cudaEventRecord(p->evx[1], p->xfer));
+        FSHT_CUDA_TRY(cudaStreamWaitEvent(p->stream, p->evx[1], 0));
         FSHT_PROF(FSHT_KCAT_FFT_FWD);
-        FSHT_TRY(fsht_launch_ring_fft_fwd(p, maps + (size_t)c0 * p->npix, p->npix, kc, W0,
-                                          p->stream));
+        FSHT_TRY(fsht_launch_ring_fft_fwd_part(p, cmaps, p->npix, kc, k0, cnt, W0, p->stream));
       }
-      FSHT_TRY(split_analysis(p, W0, alm, nmaps, c0, kc, 0, true));
+    }
+    if (split) {
+      FSHT_TRY(split_analysis(p, W0, alm, nmaps, c0, kc, 0, true, niter == 0 ? hx : nullptr));
       // Jacobi refinement: FP64 Fourier-space residual of a split synthesis, analysed
       // in split precision and added
       for (int it = 0; it < niter; ++it) {
@@ -607,40 +696,67 @@ int fsht_t2alm(fsht_plan* p, const double* maps, double* alm, int nmaps, int nit
         }
         FSHT_TRY(split_analysis(p, W1, alm, nmaps, c0, kc, 1));
       }
-    }
-    return FSHT_OK;
-  }
-  for (int c0 = 0; c0 < nmaps; c0 += p->kchunk) {
-    const int kc = nmaps - c0 < p->kchunk ? nmaps - c0 : p->kchunk;
-    double2* W0 = work_buf(p, 0, kc);
-    double2* W1 = work_buf(p, 1, kc);
-    {
-      FSHT_PROF(FSHT_KCAT_FFT_FWD);
-      FSHT_TRY(fsht_launch_ring_fft_fwd(p, maps + (size_t)c0 * p->npix, p->npix, kc, W0, p->stream));
-    }
-    {
-      FSHT_PROF(FSHT_KCAT_ANALYSIS);
-      FSHT_TRY(fsht_launch_analysis_fp64(p, 0, W0, nullptr, alm, nullptr, nmaps, c0, kc, 0, 1,
-                                         p->stream));
-    }
-    for (int it = 0; it < niter; ++it) {
-      {
-        FSHT_PROF(FSHT_KCAT_SYNTHESIS);
-        FSHT_TRY(fsht_launch_synthesis_fp64(p, 0, alm, nullptr, W1, nullptr, nmaps, c0, kc,
-                                            p->stream));
-      }
-      {
-        FSHT_PROF(FSHT_KCAT_RESIDUAL);
-        FSHT_TRY(fsht_launch_fourier_residual(p, W0, W1, kc, method, p->stream));
-      }
+    } else {
+      double2* W1 = work_buf(p, 1, kc);
       {
         FSHT_PROF(FSHT_KCAT_ANALYSIS);
-        FSHT_TRY(fsht_launch_analysis_fp64(p, 0, W1, nullptr, alm, nullptr, nmaps, c0, kc, 1, 1,
+        FSHT_TRY(fsht_launch_analysis_fp64(p, 0, W0, nullptr, alm, nullptr, nmaps, c0, kc, 0, 1,
                                            p->stream));
       }
+      for (int it = 0; it < niter; ++it) {
+        {
+          FSHT_PROF(FSHT_KCAT_SYNTHESIS);
+          FSHT_TRY(fsht_launch_synthesis_fp64(p, 0, alm, nullptr, W1, nullptr, nmaps, c0, kc,
+                                              p->stream));
+        }
+        {
+          FSHT_PROF(FSHT_KCAT_RESIDUAL);
+          FSHT_TRY(fsht_launch_fourier_residual(p, W0, W1, kc, method, p->stream));
+        }
+        {
+          FSHT_PROF(FSHT_KCAT_ANALYSIS);
+          FSHT_TRY(fsht_launch_analysis_fp64(p, 0, W1, nullptr, alm, nullptr, nmaps, c0, kc, 1,
+                                             1, p->stream));
+        }
+      }
     }
+    // whatever the waves did not return yet (all of it for FP64 or niter > 0)
+    if (hx) FSHT_TRY(xfer_orders_done(p, *hx, alm, nmaps, 0, p->lmax + 1, c0, kc));
   }
+  if (hx) FSHT_TRY(xfer_join(p));
   return FSHT_OK;
+}
+
+int fsht_t2alm(fsht_plan* p, const double* maps, double* alm, int nmaps, int niter, int method) {
+  FSHT_TRY(check_call(p, nmaps, maps, alm));
+  if (niter < 0 || method < 0 || method > 1) {
+    fsht_set_error("niter = %d, method = %d: need niter >= 0 and method 0 (old) or 1 (new)",
+                   niter, method);
+    return FSHT_EINVAL;
+  }
+  return t2alm_impl(p, maps, alm, nmaps, niter, method, nullptr);
+}
+
+int fsht_t2alm_host(fsht_plan* p, const double* host_maps, double* host_alm, double* dev_maps,
+                    double* dev_alm, int nmaps, int niter, int method) {
+  FSHT_TRY(check_call(p, nmaps, dev_maps, dev_alm));
+  if (!host_maps || !host_alm) {
+    fsht_set_error("t2alm_host: null host buffer");
+    return FSHT_EINVAL;
+  }
+  if (niter < 0 || method < 0 || method > 1) {
+    fsht_set_error("niter = %d, method = %d: need niter >= 0 and method 0 (old) or 1 (new)",
+                   niter, method);
+    return FSHT_EINVAL;
+  }
+  if (!p->xfer) {
+    fsht_set_error("t2alm_host needs a plan that owns its workspace (not FSHT_FLAG_TABLES_ONLY)");
+    return FSHT_EUNSUPPORTED;
+  }
+  HostXfer hx;
+  hx.hmaps = host_maps;
+  hx.halm = host_alm;
+  return t2alm_impl(p, dev_maps, dev_alm, nmaps, niter, method, &hx);
 }
 
 int fsht_alm2t(fsht_plan* p, const double* alm, double* maps, int nmaps) {

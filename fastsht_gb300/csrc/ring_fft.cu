@@ -23,17 +23,30 @@
 namespace {
 
 // ------------------------------------------------------------------ tables
+// The packed twiddle table (fsht_tw_entries): thread per entry, FP64 sincospi of the exact
+// fraction.
 __global__ void k_twiddles(double2* tw, int Tmax, int P3max) {
-  const int j = blockIdx.x * blockDim.x + threadIdx.x;
-  double s, c;
-  if (j < Tmax) {
-    sincospi(-2.0 * (double)j / (double)Tmax, &s, &c);
-    tw[j] = make_double2(c, s);
-  } else if (j < Tmax + P3max) {
-    const int t = j - Tmax;
-    sincospi(-2.0 * (double)t / (double)P3max, &s, &c);
-    tw[j] = make_double2(c, s);
+  const long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  const long long n4 = fsht_tw_r4_entries(Tmax);
+  if (e >= fsht_tw_entries(Tmax, P3max)) return;
+  long long num, den;
+  if (e < n4) {
+    int s = 3;
+    while (3LL * ((2LL << s) - 8) / 4 <= e) ++s;       // span 2^s holds entry e
+    const long long r = e - 3LL * ((1LL << s) - 8) / 4;
+    num = (r / 3) * (r % 3 + 1);
+    den = 1LL << s;
+  } else {
+    const long long r0 = e - n4;
+    int k = 0;
+    while (2LL * ((2LL << k) - 1) <= r0) ++k;          // size 3 * 2^k holds entry e
+    const long long r = r0 - 2LL * ((1LL << k) - 1);
+    num = (r / 2) * (r % 2 + 1);
+    den = 3LL << k;
   }
+  double sn, cs;
+  sincospi(-2.0 * (double)(num % den) / (double)den, &sn, &cs);
+  tw[e] = make_double2(cs, sn);
 }
 
 // chirp w_j = exp(-i pi j^2 / nd) and the filter spectrum (fft_dif of the wrapped conj
@@ -42,6 +55,7 @@ __global__ void k_bluestein_tables(const FshtRingFFT* rfs, const int* rings, dou
                                    double2* bhat, double2* rtw, FftTw tw) {
   extern __shared__ double2 sbuf[];
   const FshtRingFFT rf = rfs[rings[blockIdx.x]];
+  const Swz S(rf);
   const int n = rf.nd, P = rf.P;
   if (rf.nd != rf.n) {     // half-length ring: exp(-2 pi i k / n_ring), k <= nd
     for (int k = threadIdx.x; k <= n; k += blockDim.x) {
@@ -62,18 +76,19 @@ __global__ void k_bluestein_tables(const FshtRingFFT* rfs, const int* rings, dou
     double2 v = make_double2(0.0, 0.0);
     if (j < n) v = cconj(w[j]);
     else if (P - j < n) v = cconj(w[P - j]);
-    sbuf[sw(j)] = v;
+    sbuf[S(j)] = v;
   }
   fft_dif(sbuf, rf, tw, rf.P);
   const double invP = 1.0 / (double)P;
-  for (int j = threadIdx.x; j < P; j += blockDim.x) bhat[rf.bhat_off + j] = cscale(sbuf[sw(j)], invP);
+  for (int j = threadIdx.x; j < P; j += blockDim.x) bhat[rf.bhat_off + j] = cscale(sbuf[S(j)], invP);
 }
 
 // ------------------------------------------------------------------ forward
 struct FwdArgs {
   const double* maps;       // chunk base: map k at maps + k * map_stride
   long long map_stride;
-  int kc;                   // maps in this chunk
+  int kc;                   // maps in this chunk (the map stride of W)
+  int k_off, k_cnt;         // the maps of this launch: [k_off, k_off + k_cnt)
   int maps_per_block;
   int nside, lmax, nnorth, nring, ring_base;
   const FshtRingFFT* rfs;
@@ -89,6 +104,7 @@ __global__ void __launch_bounds__(512, 2) k_ring_fft_fwd(FwdArgs a) {
   extern __shared__ double2 smem[];
   const int i = a.ring_base + blockIdx.x;      // north ring index
   const FshtRingFFT rf = a.rfs[i];
+  const Swz S(rf);
   const int n = rf.n;
   double2* buf = smem;                          // rf.P entries
   double2* ph = smem + rf.P;                    // lmax+1 phase factors exp(-i m phi0)
@@ -109,8 +125,8 @@ __global__ void __launch_bounds__(512, 2) k_ring_fft_fwd(FwdArgs a) {
     }
     ph[m] = make_double2(0.5 * c, 0.5 * s);    // the 1/2 of the N/S (even/odd) split folded in
   }
-  const int k_begin = blockIdx.y * a.maps_per_block;
-  const int k_end = min(a.kc, k_begin + a.maps_per_block);
+  const int k_begin = a.k_off + blockIdx.y * a.maps_per_block;
+  const int k_end = min(a.k_off + a.k_cnt, k_begin + a.maps_per_block);
   const double2* chirp = a.chirp + rf.chirp_off;
   const double2* bhat = a.bhat + rf.bhat_off;
   if (rf.nd != n) {
@@ -126,15 +142,15 @@ __global__ void __launch_bounds__(512, 2) k_ring_fft_fwd(FwdArgs a) {
         const double* x = a.maps + (long long)k * a.map_stride + (side ? off_s : off_n);
         __syncthreads();
         for (int j = tid; j < nd; j += nt)
-          buf[sw(j)] = make_double2(__ldg(&x[2 * j]), __ldg(&x[2 * j + 1]));
+          buf[S(j)] = make_double2(__ldg(&x[2 * j]), __ldg(&x[2 * j + 1]));
         __syncthreads();
         ring_dft(buf, rf, a.tw, chirp, bhat);
         for (int m = tid; m <= mtop; m += nt) {
           const int q = m % n;
           const bool cj = q > nd;
           const int kk = cj ? n - q : q;
-          const double2 za = buf[sw(dft_bin(rf, kk == nd ? 0 : kk))];
-          const double2 zb = cconj(buf[sw(dft_bin(rf, kk == 0 ? 0 : nd - kk))]);
+          const double2 za = buf[S(dft_bin(rf, kk == nd ? 0 : kk))];
+          const double2 zb = cconj(buf[S(dft_bin(rf, kk == 0 ? 0 : nd - kk))]);
           const double2 e = cadd(za, zb);                      // 2 E
           const double2 dd = csub(za, zb);
           const double2 o = make_double2(dd.y, -dd.x);         // 2 O
@@ -159,15 +175,15 @@ __global__ void __launch_bounds__(512, 2) k_ring_fft_fwd(FwdArgs a) {
     const double* xs = a.maps + (long long)k * a.map_stride + off_s;
     __syncthreads();
     for (int j = tid; j < n; j += nt)
-      buf[sw(j)] = make_double2(__ldg(&xn[j]), equator ? 0.0 : __ldg(&xs[j]));
+      buf[S(j)] = make_double2(__ldg(&xn[j]), equator ? 0.0 : __ldg(&xs[j]));
     __syncthreads();
     ring_dft(buf, rf, a.tw, chirp, bhat);
     // Z = FFT(x_N + i x_S): X_N[q] = (Z[q] + conj Z[-q])/2, X_S[q] = (Z[q] - conj Z[-q])/(2i)
     for (int m = tid; m <= mtop; m += nt) {
       const int q = m % n;
       const int qn = (q == 0) ? 0 : n - q;
-      const double2 zq = buf[sw(dft_bin(rf, q))];
-      const double2 zn = cconj(buf[sw(dft_bin(rf, qn))]);
+      const double2 zq = buf[S(dft_bin(rf, q))];
+      const double2 zn = cconj(buf[S(dft_bin(rf, qn))]);
       const double2 xN = cadd(zq, zn);                         // 2 X_N
       const double2 dd = csub(zq, zn);
       const double2 xS = make_double2(dd.y, -dd.x);            // 2 X_S
@@ -202,16 +218,18 @@ struct InvArgs {
 
 // Builds, in buf[0..n), the packed spectrum Z[q] = Y_N[q] + i Y_S[q] of the two
 // real rings from G_m (north) and G_m(i') (south), m <= mtop (packed_spectrum_bin).
-__device__ void build_spectrum(double2* buf, const double2* ph, const double2* __restrict__ W,
-                               long long stride_m, int n, int mtop, bool equator) {
+__device__ void build_spectrum(double2* buf, const Swz& S, const double2* ph,
+                               const double2* __restrict__ W, long long stride_m, int n, int mtop,
+                               bool equator) {
   for (int q = threadIdx.x; q < n; q += blockDim.x)
-    buf[sw(q)] = packed_spectrum_bin(ph, W, stride_m, n, mtop, equator, q);
+    buf[S(q)] = packed_spectrum_bin(ph, W, stride_m, n, mtop, equator, q);
 }
 
 __global__ void __launch_bounds__(512, 2) k_ring_fft_inv(InvArgs a) {
   extern __shared__ double2 smem[];
   const int i = a.ring_base + blockIdx.x;
   const FshtRingFFT rf = a.rfs[i];
+  const Swz S(rf);
   const int n = rf.n;
   double2* buf = smem;
   double2* ph = smem + rf.P;
@@ -250,13 +268,13 @@ __global__ void __launch_bounds__(512, 2) k_ring_fft_inv(InvArgs a) {
           const double2 y1 = spectrum_bin(ph, Wk, stride_m, n, mtop, side, kk + nd);
           const double2 b = cmul(csub(y0, y1), cconj(__ldg(&rtw[kk])));
           const double2 sa = cadd(y0, y1);
-          buf[sw(kk)] = cconj(make_double2(sa.x - b.y, sa.y + b.x));   // conj(A + i B)
+          buf[S(kk)] = cconj(make_double2(sa.x - b.y, sa.y + b.x));   // conj(A + i B)
         }
         __syncthreads();
         ring_dft(buf, rf, a.tw, chirp, bhat);
         double* x = a.maps + (long long)k * a.map_stride + (side ? off_s : off_n);
         for (int j = tid; j < nd; j += nt) {
-          const double2 z = buf[sw(dft_bin(rf, j))];   // conj(z): x_{2j} = Re, x_{2j+1} = -Im
+          const double2 z = buf[S(dft_bin(rf, j))];   // conj(z): x_{2j} = Re, x_{2j+1} = -Im
           x[2 * j] = z.x;
           x[2 * j + 1] = -z.y;
         }
@@ -266,16 +284,16 @@ __global__ void __launch_bounds__(512, 2) k_ring_fft_inv(InvArgs a) {
   }
   for (int k = k_begin; k < k_end; ++k) {
     __syncthreads();
-    build_spectrum(buf, ph, a.W + ((long long)i * a.kc + k) * 2, stride_m, n, mtop, equator);
+    build_spectrum(buf, S, ph, a.W + ((long long)i * a.kc + k) * 2, stride_m, n, mtop, equator);
     __syncthreads();
     // inverse DFT = conj(DFT(conj Z))
-    for (int j = tid; j < n; j += nt) buf[sw(j)] = cconj(buf[sw(j)]);
+    for (int j = tid; j < n; j += nt) buf[S(j)] = cconj(buf[S(j)]);
     __syncthreads();
     ring_dft(buf, rf, a.tw, chirp, bhat);
     double* xn = a.maps + (long long)k * a.map_stride + off_n;
     double* xs = a.maps + (long long)k * a.map_stride + off_s;
     for (int j = tid; j < n; j += nt) {
-      const double2 z = buf[sw(dft_bin(rf, j))];   // conj applied: x_N = Re, x_S = -Im of the DFT
+      const double2 z = buf[S(dft_bin(rf, j))];   // conj applied: x_N = Re, x_S = -Im of the DFT
       xn[j] = z.x;
       if (!equator) xs[j] = -z.y;
     }
@@ -491,17 +509,17 @@ int fsht_fft_layout(int nside, int lmax, FshtFftLayout* lay, FshtRingFFT* rfs, i
 namespace {
 FftTw plan_tw(const fsht_plan* p) {
   FftTw t;
-  t.tw2 = p->d_tw;
-  t.tw3 = p->d_tw + p->Tmax;
-  t.logTmax = p->logTmax;
-  t.P3max = p->P3max;
+  t.r4 = p->d_tw;
+  t.r3 = p->d_tw + fsht_tw_r4_entries(p->Tmax);
   return t;
 }
 }  // namespace
 
 int fsht_fft_tables_fill(fsht_plan* p, const int* d_blue_rings, int nblue, cudaStream_t s) {
-  const int ntw = p->Tmax + p->P3max;
-  k_twiddles<<<(ntw + 255) / 256, 256, 0, s>>>(p->d_tw, p->Tmax, p->P3max);
+  const long long ntw = fsht_tw_entries(p->Tmax, p->P3max);
+  if (ntw > 0) {
+    k_twiddles<<<(unsigned)((ntw + 255) / 256), 256, 0, s>>>(p->d_tw, p->Tmax, p->P3max);
+  }
   FSHT_LAUNCH_CHECK();
   if (nblue > 0) {
     const size_t sm = (size_t)p->Pmax * sizeof(double2);
@@ -553,7 +571,8 @@ int fsht_fft_tables_init(fsht_plan* p) {
   FSHT_CUDA_TRY(cudaMalloc(&p->d_rfft, sizeof(FshtRingFFT) * nn));
   FSHT_CUDA_TRY(cudaMemcpyAsync(p->d_rfft, rfs.data(), sizeof(FshtRingFFT) * nn,
                                 cudaMemcpyHostToDevice, p->stream));
-  FSHT_CUDA_TRY(cudaMalloc(&p->d_tw, sizeof(double2) * (lay.Tmax + lay.P3max)));
+  const long long ntw = fsht_tw_entries(lay.Tmax, lay.P3max);
+  FSHT_CUDA_TRY(cudaMalloc(&p->d_tw, sizeof(double2) * (ntw > 0 ? ntw : 1)));
   FSHT_CUDA_TRY(cudaMalloc(&p->d_chirp, sizeof(double2) * (lay.chirp_total > 0 ? lay.chirp_total : 1)));
   FSHT_CUDA_TRY(cudaMalloc(&p->d_bhat, sizeof(double2) * (lay.bhat_total > 0 ? lay.bhat_total : 1)));
   FSHT_CUDA_TRY(cudaMalloc(&p->d_rtw, sizeof(double2) * (lay.rtw_total > 0 ? lay.rtw_total : 1)));
@@ -593,11 +612,18 @@ int fsht_launch_ring_skip(fsht_plan* p, cudaStream_t s) {
 
 int fsht_launch_ring_fft_fwd(fsht_plan* p, const double* maps, long long map_stride, int kc,
                              double2* W, cudaStream_t s) {
-  if (p->d_tw_df) return fsht_launch_ring_fft_fwd_df(p, maps, map_stride, kc, W, s);
+  return fsht_launch_ring_fft_fwd_part(p, maps, map_stride, kc, 0, kc, W, s);
+}
+
+int fsht_launch_ring_fft_fwd_part(fsht_plan* p, const double* maps, long long map_stride, int kc,
+                                  int k0, int kb, double2* W, cudaStream_t s) {
+  if (p->d_tw_df) return fsht_launch_ring_fft_fwd_df(p, maps, map_stride, kc, k0, kb, W, s);
   FwdArgs a;
   a.maps = maps;
   a.map_stride = map_stride;
   a.kc = kc;
+  a.k_off = k0;
+  a.k_cnt = kb;
   a.nside = p->nside;
   a.lmax = p->lmax;
   a.nnorth = p->nnorth;
@@ -610,13 +636,13 @@ int fsht_launch_ring_fft_fwd(fsht_plan* p, const double* maps, long long map_str
   a.bhat = p->d_bhat;
   a.ring_i0 = p->d_ring_i0;
   a.W = W;
-  a.maps_per_block = p->fft_mpb > 0 ? p->fft_mpb : maps_per_block_for(kc, p->nnorth);
+  a.maps_per_block = p->fft_mpb > 0 ? p->fft_mpb : maps_per_block_for(kb, p->nnorth);
   FSHT_CUDA_TRY(cudaFuncSetAttribute(k_ring_fft_fwd, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      (int)p->fft_smem));
   for (int sgi = 0; sgi < p->fft_nseg; ++sgi) {
     const long long* sg = p->fft_seg + 3 * sgi;
     a.ring_base = (int)sg[0];
-    dim3 grid((unsigned)(sg[1] - sg[0]), (kc + a.maps_per_block - 1) / a.maps_per_block);
+    dim3 grid((unsigned)(sg[1] - sg[0]), (kb + a.maps_per_block - 1) / a.maps_per_block);
     k_ring_fft_fwd<<<grid, p->fft_threads > 0 ? p->fft_threads : 512, (size_t)sg[2], s>>>(a);
     FSHT_LAUNCH_CHECK();
   }

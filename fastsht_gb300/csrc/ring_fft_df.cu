@@ -19,7 +19,8 @@ namespace {
 struct FwdDfArgs {
   const double* maps;       // chunk base: map k at maps + k * map_stride
   long long map_stride;
-  int kc, maps_per_block;
+  int kc, maps_per_block;   // kc: maps in the chunk (the map stride of W)
+  int k_off, k_cnt;         // the maps of this launch: [k_off, k_off + k_cnt)
   int nside, lmax, nnorth, nring, ring_base;
   const FshtRingFFT* rfs;
   FftTwT<cdd> tw;
@@ -56,8 +57,8 @@ __device__ __forceinline__ double2 cdd_to_fp64(cdd v, int sh) {
 // df64 scaled by 2^-sh (sh = that exponent, unbiased; 0 for an all-zero ring).  Thread t owns
 // slots t, t + nt, ... in both passes, so only the exponent needs a barrier.  emax is a
 // shared slot that is zero on entry.  Returns sh.
-__device__ __forceinline__ int load_scaled(cdd* buf, int cnt, const double* xa, const double* xb,
-                                           int stride, int* emax) {
+__device__ __forceinline__ int load_scaled(cdd* buf, const Swz& S, int cnt, const double* xa,
+                                           const double* xb, int stride, int* emax) {
   double2* raw = reinterpret_cast<double2*>(buf);
   const int tid = threadIdx.x, nt = blockDim.x;
   int em = 0;
@@ -65,14 +66,14 @@ __device__ __forceinline__ int load_scaled(cdd* buf, int cnt, const double* xa, 
     const double va = __ldg(&xa[(long long)stride * j]);
     const double vb = xb ? __ldg(&xb[(long long)stride * j]) : 0.0;
     em = max(em, max(dd_exp_field(va), dd_exp_field(vb)));
-    raw[sw(j)] = make_double2(va, vb);
+    raw[S(j)] = make_double2(va, vb);
   }
   em = __reduce_max_sync(0xffffffffu, em);
   if ((tid & 31) == 0) atomicMax(emax, em);
   __syncthreads();
   const int e = *emax;
   const int sh = (e == 0 || e == 0x7ff) ? 0 : e - 1023;
-  for (int j = tid; j < cnt; j += nt) buf[sw(j)] = cdd_from_raw(raw[sw(j)], sh);
+  for (int j = tid; j < cnt; j += nt) buf[S(j)] = cdd_from_raw(raw[S(j)], sh);
   return sh;
 }
 
@@ -81,6 +82,7 @@ __global__ void __launch_bounds__(1024, 1) k_ring_fft_fwd_df(FwdDfArgs a) {
   __shared__ int s_emax[2];
   const int i = a.ring_base + blockIdx.x;      // north ring index
   const FshtRingFFT rf = a.rfs[i];
+  const Swz S(rf);
   const int n = rf.n;
   cdd* buf = reinterpret_cast<cdd*>(smem4);    // rf.P entries
   cdd* ph = buf + rf.P;                        // lmax+1 phase factors exp(-i m phi0) / 2
@@ -101,8 +103,8 @@ __global__ void __launch_bounds__(1024, 1) k_ring_fft_fwd_df(FwdDfArgs a) {
     ph[m] = cdd_from_fp64(0.5 * c, 0.5 * s);   // the 1/2 of the N/S split folded in
   }
   if (tid < 2) s_emax[tid] = 0;
-  const int k_begin = blockIdx.y * a.maps_per_block;
-  const int k_end = min(a.kc, k_begin + a.maps_per_block);
+  const int k_begin = a.k_off + blockIdx.y * a.maps_per_block;
+  const int k_end = min(a.k_off + a.k_cnt, k_begin + a.maps_per_block);
   const cdd* chirp = a.chirp + rf.chirp_off;
   const cdd* bhat = a.bhat + rf.bhat_off;
   int it = 0;   // exponent slot parity: slot it & 1 collects, the other is reset
@@ -117,14 +119,14 @@ __global__ void __launch_bounds__(1024, 1) k_ring_fft_fwd_df(FwdDfArgs a) {
         const double* x = a.maps + (long long)k * a.map_stride + (side ? off_s : off_n);
         __syncthreads();
         if (tid == 0) s_emax[(it & 1) ^ 1] = 0;
-        const int sh = load_scaled(buf, nd, x, x + 1, 2, &s_emax[it & 1]);
+        const int sh = load_scaled(buf, S, nd, x, x + 1, 2, &s_emax[it & 1]);
         ring_dft(buf, rf, a.tw, chirp, bhat);
         for (int m = tid; m <= mtop; m += nt) {
           const int q = m % n;
           const bool cj = q > nd;
           const int kk = cj ? n - q : q;
-          const cdd za = buf[sw(dft_bin(rf, kk == nd ? 0 : kk))];
-          const cdd zb = cconj(buf[sw(dft_bin(rf, kk == 0 ? 0 : nd - kk))]);
+          const cdd za = buf[S(dft_bin(rf, kk == nd ? 0 : kk))];
+          const cdd zb = cconj(buf[S(dft_bin(rf, kk == 0 ? 0 : nd - kk))]);
           const cdd e = cadd_lz(za, zb);                       // 2 E
           const cdd o = cmul_mi(csub_lz(za, zb));              // 2 O
           cdd xq = cadd_lz(e, cmul_lz(o, ldg_cdd(&rtw[kk])));  // 2 X
@@ -148,7 +150,7 @@ __global__ void __launch_bounds__(1024, 1) k_ring_fft_fwd_df(FwdDfArgs a) {
     const double* xs = a.maps + (long long)k * a.map_stride + off_s;
     __syncthreads();   // the previous map's readers of buf and of the other slot are done
     if (tid == 0) s_emax[(it & 1) ^ 1] = 0;
-    const int sh = load_scaled(buf, n, xn, equator ? nullptr : xs, 1, &s_emax[it & 1]);
+    const int sh = load_scaled(buf, S, n, xn, equator ? nullptr : xs, 1, &s_emax[it & 1]);
     ring_dft(buf, rf, a.tw, chirp, bhat);
     // Z = FFT(x_N + i x_S): X_N[q] = (Z[q] + conj Z[-q])/2, X_S[q] = (Z[q] - conj Z[-q])/(2i)
     // q = m mod n and the output pointer advance by fixed steps (no division per m)
@@ -158,8 +160,8 @@ __global__ void __launch_bounds__(1024, 1) k_ring_fft_fwd_df(FwdDfArgs a) {
     double2* w = a.W + (((long long)tid * a.nnorth + i) * a.kc + k) * 2;
     for (int m = tid; m <= mtop; m += nt, w += wstep) {
       const int qn = (q == 0) ? 0 : n - q;
-      const cdd zq = buf[sw(dft_bin(rf, q))];
-      const cdd zn = cconj(buf[sw(dft_bin(rf, qn))]);
+      const cdd zq = buf[S(dft_bin(rf, q))];
+      const cdd zn = cconj(buf[S(dft_bin(rf, qn))]);
       q += qstep;
       if (q >= n) q -= n;
       const cdd xN = cadd_lz(zq, zn);                          // 2 X_N
@@ -196,7 +198,8 @@ struct InvDfArgs {
 // ...) become df64 scaled by 2^-sh, sh from the block-wide largest exponent field (em = the
 // thread's own largest); conj: store the conjugate.  emax is a shared slot that is zero on
 // entry.  Returns sh.
-__device__ __forceinline__ int convert_scaled(cdd* buf, int cnt, int em, int* emax, bool conj) {
+__device__ __forceinline__ int convert_scaled(cdd* buf, const Swz& S, int cnt, int em, int* emax,
+                                              bool conj) {
   const double2* raw = reinterpret_cast<const double2*>(buf);
   const int tid = threadIdx.x, nt = blockDim.x;
   em = __reduce_max_sync(0xffffffffu, em);
@@ -205,8 +208,8 @@ __device__ __forceinline__ int convert_scaled(cdd* buf, int cnt, int em, int* em
   const int e = *emax;
   const int sh = (e == 0 || e == 0x7ff) ? 0 : e - 1023;
   for (int j = tid; j < cnt; j += nt) {
-    const double2 v = raw[sw(j)];
-    buf[sw(j)] = cdd_from_raw(conj ? make_double2(v.x, -v.y) : v, sh);
+    const double2 v = raw[S(j)];
+    buf[S(j)] = cdd_from_raw(conj ? make_double2(v.x, -v.y) : v, sh);
   }
   return sh;
 }
@@ -223,6 +226,7 @@ __global__ void __launch_bounds__(1024, 1) k_ring_fft_inv_df(InvDfArgs a) {
   __shared__ int s_emax[2];
   const int i = a.ring_base + blockIdx.x;
   const FshtRingFFT rf = a.rfs[i];
+  const Swz S(rf);
   const int n = rf.n;
   cdd* buf = reinterpret_cast<cdd*>(smem4);
   double2* raw = reinterpret_cast<double2*>(smem4);
@@ -267,14 +271,14 @@ __global__ void __launch_bounds__(1024, 1) k_ring_fft_inv_df(InvDfArgs a) {
           const double2 b = cmul(csub(y0, y1), cconj(__ldg(&rtw[kk])));
           const double2 sa = cadd(y0, y1);
           const double2 v = cconj(make_double2(sa.x - b.y, sa.y + b.x));   // conj(A + i B)
-          raw[sw(kk)] = v;
+          raw[S(kk)] = v;
           em = max(em, exp2f64(v));
         }
-        const int sh = convert_scaled(buf, nd, em, &s_emax[it & 1], false);
+        const int sh = convert_scaled(buf, S, nd, em, &s_emax[it & 1], false);
         ring_dft(buf, rf, a.tw, chirp, bhat);
         double* x = a.maps + (long long)k * a.map_stride + (side ? off_s : off_n);
         for (int j = tid; j < nd; j += nt) {
-          const cdd z = buf[sw(dft_bin(rf, j))];   // conj(z): x_{2j} = Re, x_{2j+1} = -Im
+          const cdd z = buf[S(dft_bin(rf, j))];   // conj(z): x_{2j} = Re, x_{2j+1} = -Im
           x[2 * j] = dd_to_double(z.h.x, z.l.x, sh);
           x[2 * j + 1] = -dd_to_double(z.h.y, z.l.y, sh);
         }
@@ -289,16 +293,16 @@ __global__ void __launch_bounds__(1024, 1) k_ring_fft_inv_df(InvDfArgs a) {
     int em = 0;
     for (int q = tid; q < n; q += nt) {
       const double2 z = packed_spectrum_bin(ph, Wk, stride_m, n, mtop, equator, q);
-      raw[sw(q)] = z;
+      raw[S(q)] = z;
       em = max(em, exp2f64(z));
     }
     // inverse DFT = conj(DFT(conj Z))
-    const int sh = convert_scaled(buf, n, em, &s_emax[it & 1], true);
+    const int sh = convert_scaled(buf, S, n, em, &s_emax[it & 1], true);
     ring_dft(buf, rf, a.tw, chirp, bhat);
     double* xn = a.maps + (long long)k * a.map_stride + off_n;
     double* xs = a.maps + (long long)k * a.map_stride + off_s;
     for (int j = tid; j < n; j += nt) {
-      const cdd z = buf[sw(dft_bin(rf, j))];   // x_N = Re, x_S = -Im of the DFT
+      const cdd z = buf[S(dft_bin(rf, j))];   // x_N = Re, x_S = -Im of the DFT
       xn[j] = dd_to_double(z.h.x, z.l.x, sh);
       if (!equator) xs[j] = -dd_to_double(z.h.y, z.l.y, sh);
     }
@@ -336,7 +340,7 @@ int to_cdd(const double2* in, float4** out, long long n, cudaStream_t s) {
 }  // namespace
 
 int fsht_fft_df_tables_init(fsht_plan* p) {
-  FSHT_TRY(to_cdd(p->d_tw, &p->d_tw_df, (long long)p->Tmax + p->P3max, p->stream));
+  FSHT_TRY(to_cdd(p->d_tw, &p->d_tw_df, fsht_tw_entries(p->Tmax, p->P3max), p->stream));
   FSHT_TRY(to_cdd(p->d_chirp, &p->d_chirp_df, p->fft_chirp_total, p->stream));
   FSHT_TRY(to_cdd(p->d_bhat, &p->d_bhat_df, p->fft_bhat_total, p->stream));
   FSHT_TRY(to_cdd(p->d_rtw, &p->d_rtw_df, p->fft_rtw_total, p->stream));
@@ -345,34 +349,34 @@ int fsht_fft_df_tables_init(fsht_plan* p) {
 }
 
 int fsht_launch_ring_fft_fwd_df(fsht_plan* p, const double* maps, long long map_stride, int kc,
-                                double2* W, cudaStream_t s) {
+                                int k0, int kb, double2* W, cudaStream_t s) {
   FwdDfArgs a;
   a.maps = maps;
   a.map_stride = map_stride;
   a.kc = kc;
+  a.k_off = k0;
+  a.k_cnt = kb;
   a.nside = p->nside;
   a.lmax = p->lmax;
   a.nnorth = p->nnorth;
   a.nring = p->nring;
   a.ring_base = 0;
   a.rfs = p->d_rfft;
-  a.tw.tw2 = reinterpret_cast<const cdd*>(p->d_tw_df);
-  a.tw.tw3 = reinterpret_cast<const cdd*>(p->d_tw_df) + p->Tmax;
-  a.tw.logTmax = p->logTmax;
-  a.tw.P3max = p->P3max;
+  a.tw.r4 = reinterpret_cast<const cdd*>(p->d_tw_df);
+  a.tw.r3 = reinterpret_cast<const cdd*>(p->d_tw_df) + fsht_tw_r4_entries(p->Tmax);
   a.chirp = reinterpret_cast<const cdd*>(p->d_chirp_df);
   a.bhat = reinterpret_cast<const cdd*>(p->d_bhat_df);
   a.rtw = reinterpret_cast<const cdd*>(p->d_rtw_df);
   a.ring_i0 = p->d_ring_i0;
   a.W = W;
-  a.maps_per_block = p->fft_mpb > 0 ? p->fft_mpb : fsht_fft_maps_per_block(kc, p->nnorth);
+  a.maps_per_block = p->fft_mpb > 0 ? p->fft_mpb : fsht_fft_maps_per_block(kb, p->nnorth);
   FSHT_CUDA_TRY(cudaFuncSetAttribute(k_ring_fft_fwd_df,
                                      cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      (int)p->fft_smem));
   for (int sgi = 0; sgi < p->fft_nseg; ++sgi) {
     const long long* sg = p->fft_seg + 3 * sgi;
     a.ring_base = (int)sg[0];
-    dim3 grid((unsigned)(sg[1] - sg[0]), (kc + a.maps_per_block - 1) / a.maps_per_block);
+    dim3 grid((unsigned)(sg[1] - sg[0]), (kb + a.maps_per_block - 1) / a.maps_per_block);
     k_ring_fft_fwd_df<<<grid, df_threads(p, sg[2]), (size_t)sg[2], s>>>(a);
     FSHT_LAUNCH_CHECK();
   }
@@ -392,10 +396,8 @@ int fsht_launch_ring_fft_inv_df(fsht_plan* p, const double2* W, double* maps,
   a.nring = p->nring;
   a.ring_base = 0;
   a.rfs = p->d_rfft;
-  a.tw.tw2 = reinterpret_cast<const cdd*>(p->d_tw_df);
-  a.tw.tw3 = reinterpret_cast<const cdd*>(p->d_tw_df) + p->Tmax;
-  a.tw.logTmax = p->logTmax;
-  a.tw.P3max = p->P3max;
+  a.tw.r4 = reinterpret_cast<const cdd*>(p->d_tw_df);
+  a.tw.r3 = reinterpret_cast<const cdd*>(p->d_tw_df) + fsht_tw_r4_entries(p->Tmax);
   a.chirp = reinterpret_cast<const cdd*>(p->d_chirp_df);
   a.bhat = reinterpret_cast<const cdd*>(p->d_bhat_df);
   a.rtw = p->d_rtw;

@@ -211,6 +211,8 @@ class SHT:
                              'set_maps(maps_in)!')
         with torch.cuda.device(self.device):
             self._stream()
+            if get_alm and not _is_torch(maps) and self._host_alm_ok(alms_in):
+                return self._t2alm_host(maps, alms_in, method)
             dmaps, as_torch = self._dev_maps(maps, "maps")
             dalm = self._new_dev_alm()
             _lib.call("fsht_t2alm", self._plan, C.c_void_p(dmaps.data_ptr()),
@@ -222,6 +224,35 @@ class SHT:
             if not get_alm:
                 return None
             return self._alm_out(dalm, alms_in, as_torch)
+
+    def _host_alm_ok(self, alms_in):
+        if alms_in is None:
+            return True
+        if _is_torch(alms_in):
+            return False
+        a = np.asarray(alms_in)
+        L = self.lmax + 1
+        return a.dtype == np.float64 and a.flags.f_contiguous and a.shape == (self.nsim, L, L)
+
+    def _t2alm_host(self, maps, alms_in, method):
+        """Host maps -> host alm through fsht_t2alm_host: the maps go to the device in
+        sub-batches that the FFT consumes as they land, finished alm columns come back while
+        later waves run (copies overlap the transform)."""
+        a = np.asarray(maps)
+        if a.shape != (self.npix, self.nsim):
+            raise ValueError(f"maps: expected shape ({self.npix}, {self.nsim}), got {a.shape}")
+        a = np.asfortranarray(a, dtype=np.float64)
+        L = self.lmax + 1
+        out = np.asarray(alms_in) if alms_in is not None else _pinned_empty_fortran((self.nsim, L, L))
+        dmaps = self._new_dev_maps()
+        dalm = self._new_dev_alm()
+        _lib.call("fsht_t2alm_host", self._plan, C.c_void_p(a.ctypes.data),
+                  C.c_void_p(out.ctypes.data), C.c_void_p(dmaps.data_ptr()),
+                  C.c_void_p(dalm.data_ptr()), self.nsim, self.niter,
+                  0 if method == 'old' else 1)
+        _lib.call("fsht_plan_sync", self._plan)
+        self._dev_alm = dalm
+        return 0 if alms_in is not None else out
 
     def alm2t(self, alms, maps_in=None):
         """alm -> temperature maps (reference SHT.alm2t, SHT.py:109-122)."""

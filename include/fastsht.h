@@ -75,6 +75,18 @@ int fsht_plan_ring_skip(const fsht_plan* plan, int* out);
  * method 1: t2alm_iter (src/sht_main.f90:171-264). */
 int fsht_t2alm(fsht_plan* plan, const double* maps, double* alm, int nmaps,
                int niter, int method);
+/* fsht_t2alm from and to host memory, with the transfers overlapped with the transform: the
+ * maps go to dev_maps in sub-batches on the plan's copy stream and each is forward-transformed
+ * as soon as it lands; alm columns go from dev_alm back to host_alm as soon as they are final
+ * (after each wave of the split form when niter = 0, else after the chunk).  Replaces the
+ * reference's host-side SHT.t2alm call (SHT.py:72-107 over sht_main.f90:38-89, whose maps
+ * and alm live in host memory).  dev_maps / dev_alm: device buffers of the same layouts,
+ * provided by the caller (nothing is allocated here).  Host buffers should be pinned for
+ * the copies to run asynchronously.  Results equal fsht_t2alm's; when the call returns the
+ * work is enqueued on the plan's stream (fsht_plan_sync waits for it).  Needs a plan that
+ * owns its workspace. */
+int fsht_t2alm_host(fsht_plan* plan, const double* host_maps, double* host_alm,
+                    double* dev_maps, double* dev_alm, int nmaps, int niter, int method);
 /* Temperature synthesis: reference alm2t (src/sht_main.f90:96-155). */
 int fsht_alm2t(fsht_plan* plan, const double* alm, double* maps, int nmaps);
 /* Temperature analysis that allocates no device memory and needs no plan

@@ -1,0 +1,63 @@
+"""Host-buffer analysis (fsht_t2alm_host, used by SHT.t2alm for NumPy inputs): the maps go to
+the device in sub-batches that the FFT consumes as they land and alm columns come back as waves
+finish.  The results must equal the device-buffer path bit for bit, for both precisions, with
+refinement, with several workspace chunks, into a caller's output array and from pageable
+(not pinned) input."""
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _cuda():
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from fastsht_gb300 import build
+    build.build()
+
+
+def _maps(ns, nsim, seed):
+    rng = np.random.default_rng(seed)
+    return np.asfortranarray(rng.standard_normal((12 * ns * ns, nsim)))
+
+
+@pytest.mark.parametrize("precision", ["fp64", "split"])
+@pytest.mark.parametrize("niter", [0, 1])
+def test_host_path_equals_device_path(precision, niter):
+    from fastsht_gb300 import SHT
+    ns, lmax, nsim = 64, 191, 70
+    maps = _maps(ns, nsim, 1)
+    sht = SHT(ns, lmax, nsim, niter=niter, precision=precision)
+    got = sht.t2alm(maps)                                     # host in, host out
+    dev = torch.from_numpy(maps.T.copy()).cuda().T            # (npix, nsim) Fortran view
+    want = sht.t2alm(dev).cpu().numpy()
+    assert isinstance(got, np.ndarray) and got.shape == (nsim, lmax + 1, lmax + 1)
+    assert np.array_equal(got, want)
+    assert np.array_equal(sht.get_alms(), want)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "split"])
+def test_host_path_several_chunks_and_caller_output(precision):
+    from fastsht_gb300 import SHT
+    ns, lmax, nsim = 64, 191, 150
+    maps = _maps(ns, nsim, 2)
+    sht = SHT(ns, lmax, nsim, precision=precision, workspace_limit=60 << 20)
+    assert sht.plan_info()["maps_per_chunk"] < nsim
+    out = np.zeros((nsim, lmax + 1, lmax + 1), order="F")
+    assert sht.t2alm(maps, alms_in=out) == 0
+    want = sht.t2alm(torch.from_numpy(maps.T.copy()).cuda().T).cpu().numpy()
+    assert np.array_equal(out, want)
+
+
+def test_host_path_split_nside_1024():
+    """The headline shape class (17 waves, per-wave column returns), 3 maps."""
+    from fastsht_gb300 import SHT
+    ns, lmax, nsim = 1024, 2047, 3
+    maps = _maps(ns, nsim, 3)
+    sht = SHT(ns, lmax, nsim, precision="split")
+    got = sht.t2alm(maps)
+    want = sht.t2alm(torch.from_numpy(maps.T.copy()).cuda().T).cpu().numpy()
+    assert np.array_equal(got, want)
