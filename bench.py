@@ -633,9 +633,49 @@ def ours(args, rank, world, local):
         dist.destroy_process_group()
 
 
+def gpu_local_cpus(dev):
+    """Host cores of the GPU's own NUMA node (sysfs local_cpulist of its PCI device, found
+    through the device UUID in nvidia-smi), or None."""
+    import torch
+    try:
+        uuid = str(torch.cuda.get_device_properties(dev).uuid)
+        out = subprocess.run(["nvidia-smi", "--query-gpu=uuid,pci.bus_id", "--format=csv,noheader"],
+                             capture_output=True, text=True, timeout=30).stdout
+        for line in out.splitlines():
+            u, bus = [x.strip() for x in line.split(",")]
+            if u.lower().endswith(uuid.lower()) or uuid.lower() in u.lower():
+                dom, rest = bus.split(":", 1)
+                path = f"/sys/bus/pci/devices/{int(dom, 16):04x}:{rest.lower()}/local_cpulist"
+                cpus = set()
+                for part in Path(path).read_text().strip().split(","):
+                    lo, _, hi = part.partition("-")
+                    cpus.update(range(int(lo), int(hi or lo) + 1))
+                return cpus or None
+    except Exception:
+        return None
+    return None
+
+
 def e2e(sht, maps_dev, ke, args, world):
     """Same metric through SHT.t2alm with host buffers: every step copies the maps
-    host->device and the alm device->host (pinned buffers, reused)."""
+    host->device and the alm device->host (pinned buffers, reused).  The process runs on the
+    GPU's own NUMA node's cores while it allocates them (first touch places the pinned pages
+    there), as a NUMA-aware user would."""
+    import torch
+    local = gpu_local_cpus(maps_dev.device)
+    saved = os.sched_getaffinity(0)
+    if local:
+        try:
+            os.sched_setaffinity(0, local)
+        except OSError:
+            local = None
+    try:
+        return _e2e_run(sht, maps_dev, ke, args, world, local)
+    finally:
+        os.sched_setaffinity(0, saved)
+
+
+def _e2e_run(sht, maps_dev, ke, args, world, local):
     import torch
     npix = sht.npix
     L = sht.lmax + 1
@@ -669,6 +709,7 @@ def e2e(sht, maps_dev, ke, args, world):
     return {"value": world * ke * args.steps / dt, "unit": UNIT,
             "h2d_bytes_per_step": ke * npix * 8, "d2h_bytes_per_step": ke * L * L * 8,
             "maps_per_step": ke, "ms_per_step": 1000.0 * dt / args.steps,
+            "host_cpus": ("the GPU's NUMA-local cores (%d)" % len(local)) if local else "default",
             "h2d_gbs": kc * npix * 8 / (t2 - t1) / 1e9, "d2h_gbs": kc * L * L * 8 / (t3 - t2) / 1e9}
 
 

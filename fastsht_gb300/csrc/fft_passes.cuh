@@ -74,7 +74,8 @@ struct Swz {
 // the first pass then skips the products with them (exact, the same results).  All threads of
 // the block call it; it synchronises on entry and after every pass.
 template <class E>
-__device__ void fft_dif(E* buf, const FshtRingFFT& rf, const FftTwT<E>& tw, int nz) {
+__device__ void fft_dif(E* buf, const FshtRingFFT& rf, const FftTwT<E>& tw, int nz,
+                        bool last = true) {
   using namespace fftp;
   const Swz S(rf);
   constexpr bool kF64 = std::is_same<E, double2>::value;
@@ -108,7 +109,10 @@ __device__ void fft_dif(E* buf, const FshtRingFFT& rf, const FftTwT<E>& tw, int 
     __syncthreads();
   }
   int logspan = logT;
-  for (; logspan >= 2; logspan -= 2) {
+  // last = false: stop before the twiddle-free last pass (span 4 or 2), which the caller
+  // fuses with what follows
+  const int stop = (last || (logT & 1)) ? 2 : 4;
+  for (; logspan >= stop; logspan -= 2) {
     const int lh = logspan - 2, h = 1 << lh;
     const int per_blk = 1 << (logT - 2);
     const E* t4 = tw.r4 + 3 * ((1 << logspan) - 8) / 4;   // used when h > 1
@@ -148,7 +152,7 @@ __device__ void fft_dif(E* buf, const FshtRingFFT& rf, const FftTwT<E>& tw, int 
     }
     __syncthreads();
   }
-  if (logspan == 1) {
+  if (logspan == 1 && last) {
     for (int idx = tid; idx < nblk << (logT - 1); idx += nt) {
       const E a = buf[S(2 * idx)], b = buf[S(2 * idx + 1)];
       buf[S(2 * idx)] = fin(ladd(a, b));
@@ -162,7 +166,8 @@ __device__ void fft_dif(E* buf, const FshtRingFFT& rf, const FftTwT<E>& tw, int 
 // in, natural order out; the passes of fft_dif in reverse with conjugate twiddles.  Only the
 // outputs below nout are wanted (Bluestein keeps nd of P): the last pass skips the others.
 template <class E>
-__device__ void fft_dit_inv(E* buf, const FshtRingFFT& rf, const FftTwT<E>& tw, int nout) {
+__device__ void fft_dit_inv(E* buf, const FshtRingFFT& rf, const FftTwT<E>& tw, int nout,
+                            bool first = true) {
   using namespace fftp;
   const Swz S(rf);
   constexpr bool kF64 = std::is_same<E, double2>::value;
@@ -170,15 +175,21 @@ __device__ void fft_dit_inv(E* buf, const FshtRingFFT& rf, const FftTwT<E>& tw, 
   const int logT = rf.logT, T = 1 << logT;
   const int nblk = rf.r3 ? 3 : 1;
   __syncthreads();
+  // first = false: the twiddle-free first pass (span 2 or 4) was fused into the caller's
+  // previous step
   int logspan = 2;
   if (logT & 1) {
-    for (int idx = tid; idx < nblk << (logT - 1); idx += nt) {
-      const E a = buf[S(2 * idx)], b = buf[S(2 * idx + 1)];
-      buf[S(2 * idx)] = fin(ladd(a, b));
-      buf[S(2 * idx + 1)] = fin(lsub(a, b));
+    if (first) {
+      for (int idx = tid; idx < nblk << (logT - 1); idx += nt) {
+        const E a = buf[S(2 * idx)], b = buf[S(2 * idx + 1)];
+        buf[S(2 * idx)] = fin(ladd(a, b));
+        buf[S(2 * idx + 1)] = fin(lsub(a, b));
+      }
+      __syncthreads();
     }
-    __syncthreads();
     logspan = 3;
+  } else if (!first) {
+    logspan = 4;
   }
   for (; logspan <= logT; logspan += 2) {
     const int lh = logspan - 2, h = 1 << lh;
@@ -279,9 +290,37 @@ __device__ void ring_dft(E* buf, const FshtRingFFT& rf, const FftTwT<E>& tw,
     if (j < n) buf[S(j)] = fin(lmul(buf[S(j)], ldg_e(&chirp[j])));
     else buf[S(j)] = zero_e<E>();
   }
-  fft_dif(buf, rf, tw, n);
-  for (int j = tid; j < P; j += nt) buf[S(j)] = fin(lmul(buf[S(j)], ldg_e(&bhat[j])));
-  fft_dit_inv(buf, rf, tw, n);
+  fft_dif(buf, rf, tw, n, false);
+  // the forward transform's twiddle-free last pass, the filter and the inverse's
+  // twiddle-free first pass, on the same 4 (odd log2: 2) elements in registers
+  if (!(rf.logT & 1)) {
+    for (int idx = tid; idx < (P >> 2); idx += nt) {
+      const int i0 = 4 * idx;
+      const E a = buf[S(i0)], b = buf[S(i0 + 1)], c = buf[S(i0 + 2)], d = buf[S(i0 + 3)];
+      const E apc = ladd(a, c), amc = lsub(a, c), bpd = ladd(b, d), bmd = lsub(b, d);
+      const E mib = cmul_mi(bmd);
+      const E y0 = fin(lmul(ladd(apc, bpd), ldg_e(&bhat[i0])));
+      const E y1 = fin(lmul(lsub(apc, bpd), ldg_e(&bhat[i0 + 1])));
+      const E y2 = fin(lmul(ladd(amc, mib), ldg_e(&bhat[i0 + 2])));
+      const E y3 = fin(lmul(lsub(amc, mib), ldg_e(&bhat[i0 + 3])));
+      const E sp = ladd(y0, y1), dm = lsub(y0, y1), e = ladd(y2, y3), f = lsub(y2, y3);
+      const E mif = cmul_mi(f);
+      buf[S(i0)] = fin(ladd(sp, e));
+      buf[S(i0 + 1)] = fin(lsub(dm, mif));
+      buf[S(i0 + 2)] = fin(lsub(sp, e));
+      buf[S(i0 + 3)] = fin(ladd(dm, mif));
+    }
+  } else {
+    for (int idx = tid; idx < (P >> 1); idx += nt) {
+      const int i0 = 2 * idx;
+      const E a = buf[S(i0)], b = buf[S(i0 + 1)];
+      const E y0 = fin(lmul(ladd(a, b), ldg_e(&bhat[i0])));
+      const E y1 = fin(lmul(lsub(a, b), ldg_e(&bhat[i0 + 1])));
+      buf[S(i0)] = fin(ladd(y0, y1));
+      buf[S(i0 + 1)] = fin(lsub(y0, y1));
+    }
+  }
+  fft_dit_inv(buf, rf, tw, n, false);
   for (int j = tid; j < n; j += nt) buf[S(j)] = fin(lmul(buf[S(j)], ldg_e(&chirp[j])));
   __syncthreads();
 }

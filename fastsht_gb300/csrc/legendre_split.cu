@@ -44,18 +44,25 @@ struct SliceArgs {
   int* EB;
 };
 
-// grid (q in wave, group), 256 threads = (map, parity, Re/Im) with Re/Im fastest, so a warp
-// reads 8 maps' whole 32-byte {S, D} entries of one ring: every W sector is read once per
-// pass (two passes: the column maximum, then the digits).
-__global__ void __launch_bounds__(256) k_slice_phase(SliceArgs a) {
+// grid (q in wave, group), 512 threads = (ring half, map, parity, Re/Im) with Re/Im fastest, so
+// a warp reads 8 maps' whole 32-byte {S, D} entries of one ring: every W sector is read once per
+// pass (two passes: the column maximum, then the digits).  The two halves of a column's
+// k-steps go to two threads (shorter serial chains, twice the loads in flight); their maxima
+// meet in shared memory.
+__global__ void __launch_bounds__(512, 2) k_slice_phase(SliceArgs a) {
+  __shared__ double s_mx[256];
   const int qi = blockIdx.x, g = blockIdx.y;
   const int m = m_of_q(a.q0 + qi, a.lmax);
-  const int t = threadIdx.x;
+  const int t = threadIdx.x & 255, half = threadIdx.x >> 8;
   const int comp = t & 1, p = (t >> 1) & 1, kl = t >> 2;
   const int k = g * kGroupMaps + kl;
   const int c = comp * kGroupMaps + kl;
   const int i0 = a.ring_i0[m];
   const int K = a.nnorth - i0;
+  const int nks = (K + kKStep - 1) / kKStep;
+  const int ksh = (nks + 1) / 2;                   // k-steps of the first half
+  const int ks_begin = half ? ksh : 0, ks_end = half ? nks : ksh;
+  const int r_begin = ks_begin * kKStep, r_end = min(K, ks_end * kKStep);
   const bool valid = k < a.kc;
   const double* col = a.W + ((((long long)m * a.nnorth + i0) * a.kc + k) * 2 + p) * 2 + comp;
   const long long rstride = (long long)a.kc * 4;
@@ -63,33 +70,37 @@ __global__ void __launch_bounds__(256) k_slice_phase(SliceArgs a) {
   double mx = 0.0;
   if (valid) {
     // eight independent loads in flight per thread
-    int r = 0;
-    for (; r + 8 <= K; r += 8) {
+    int r = r_begin;
+    for (; r + 8 <= r_end; r += 8) {
       double v[8];
 #pragma unroll
       for (int u = 0; u < 8; ++u) v[u] = col[(long long)(r + u) * rstride];
 #pragma unroll
       for (int u = 0; u < 8; ++u) mx = fmax(mx, fabs(v[u]));
     }
-    for (; r < K; ++r) mx = fmax(mx, fabs(col[(long long)r * rstride]));
+    for (; r < r_end; ++r) mx = fmax(mx, fabs(col[(long long)r * rstride]));
   }
+  if (half) s_mx[t] = mx;
+  __syncthreads();
+  if (!half) s_mx[t] = fmax(mx, s_mx[t]);
+  __syncthreads();
+  mx = s_mx[t];
   const int E = (mx > 0.0) ? ilogb(mx) + 1 : kEmptyExp;
-  a.EB[(((long long)qi * 2 + p) * a.ngroups + g) * kCols + c] = E;
-  const int nks = (K + kKStep - 1) / kKStep;
+  if (!half) a.EB[(((long long)qi * 2 + p) * a.ngroups + g) * kCols + c] = E;
   unsigned char* base = a.WS + ((size_t)(qi * 2 + p) * a.ngroups + g) * a.row_bytes +
                         (c >> 3) * 256 + (c & 7) * 16;
-  for (int ts = 0; ts < nks; ++ts) {
+  for (int ts = ks_begin; ts < ks_end; ++ts) {
     // the k-step's 16 loads issued together (the column is not in L2 any more)
     double v[kKStep];
 #pragma unroll
     for (int u = 0; u < kKStep; ++u) v[u] = val(ts * kKStep + u);
 #pragma unroll
-    for (int half = 0; half < 2; ++half) {
+    for (int hh = 0; hh < 2; ++hh) {
       uint16_t sl[kSlices][8];
 #pragma unroll
       for (int j = 0; j < 8; ++j) {
         uint16_t q4[4] = {0, 0, 0, 0};
-        if (E != kEmptyExp) tc::digits4(v[half * 8 + j], E, q4);
+        if (E != kEmptyExp) tc::digits4(v[hh * 8 + j], E, q4);
         for (int d = 0; d < kSlices; ++d) sl[d][j] = q4[d];
       }
       for (int d = 0; d < kSlices; ++d) {
@@ -98,7 +109,7 @@ __global__ void __launch_bounds__(256) k_slice_phase(SliceArgs a) {
         pk.y = sl[d][2] | ((uint32_t)sl[d][3] << 16);
         pk.z = sl[d][4] | ((uint32_t)sl[d][5] << 16);
         pk.w = sl[d][6] | ((uint32_t)sl[d][7] << 16);
-        *reinterpret_cast<uint4*>(base + ((size_t)ts * kSlices + d) * kBTileBytes + half * 128) = pk;
+        *reinterpret_cast<uint4*>(base + ((size_t)ts * kSlices + d) * kBTileBytes + hh * 128) = pk;
       }
     }
   }
@@ -271,15 +282,20 @@ __global__ void __launch_bounds__(128) k_lambda_digits(LamArgs a) {
 }
 
 // ------------------------------------------------------------------ split GEMM
-// CTA = (64-map group, parity x l-tile x K-chunk, q): one 128-row x 128-column output tile
-// over <= 64 k-steps of 16 rings.  Warp 4 lane 0 streams lambda and P digit tiles (bulk
-// async copies, kStagesG deep), warp 5 lane 0 issues the ten level-ordered UMMAs per k-step,
-// warps 0-3 run the epilogue.
+// Persistent: one CTA per SM walks the wave's work units u = blockIdx.x, + gridDim.x, ...;
+// a unit is (q, parity, l-tile, K-chunk, 64-map group), the group fastest, so CTAs running
+// at the same time share lambda tiles in L2.  A unit is one 128-row x 128-column output tile
+// over <= 64 k-steps of 16 rings.  Warp 4 lane 0 streams lambda and P digit tiles (bulk async
+// copies) through a kStagesG-deep ring that runs on across units, so the next unit's tiles
+// load while the current one's epilogue drains the accumulators; warp 5 lane 0 issues the
+// ten level-ordered UMMAs per k-step; warps 0-3 run the epilogue.  TMEM (four 128-column
+// level accumulators) is allocated once per CTA; tfull / tempty hand it between the UMMA
+// issuer and the epilogue for every unit.
 constexpr int kStagesG = 6;
 constexpr uint32_t kStageBytesG = 2 * kSlices * kATileBytes;    // 32 KB: A then B
 
 struct GemmArgs {
-  int lmax, nnorth, ngroups, nkc_glob, q0, ntmax, nkcmax, accumulate;
+  int lmax, nnorth, ngroups, nkc_glob, q0, ntmax, nkcmax, accumulate, nunits;
   size_t row_bytes;
   const int* ring_i0;
   const long long* lam_off;
@@ -294,33 +310,42 @@ struct GemmArgs {
 };
 
 struct __align__(8) GemmSmemHdr {
-  uint64_t full[kStagesG], empty[kStagesG], tfull, fin;
+  uint64_t full[kStagesG], empty[kStagesG], tfull, tempty, fin;
   uint32_t tmem;
   int abort;
 };
 
+// One work unit, decoded from its index; nk = 0: nothing to do (l-tile beyond lmax - m, or a
+// K-chunk past the kept rings).
+struct GemmUnit {
+  int g, p, kci, t, qi, m, nks, ntiles, ks0, nk, lt0;
+};
+
+__device__ __forceinline__ GemmUnit gemm_unit(const GemmArgs& a, int u) {
+  GemmUnit w;
+  w.g = u % a.ngroups;
+  int r = u / a.ngroups;
+  w.p = r & 1;
+  r >>= 1;
+  w.kci = r % a.nkcmax;
+  r /= a.nkcmax;
+  w.t = r % a.ntmax;
+  w.qi = r / a.ntmax;
+  w.m = m_of_q(a.q0 + w.qi, a.lmax);
+  const int K = a.nnorth - a.ring_i0[w.m];
+  w.nks = (K + kKStep - 1) / kKStep;
+  w.ntiles = (a.lmax - w.m + 1 + 2 * kRows - 1) / (2 * kRows);
+  w.ks0 = w.kci * (kKChunk / kKStep);
+  const int ks1 = min(w.nks, w.ks0 + kKChunk / kKStep);
+  w.nk = (w.t < w.ntiles && w.ks0 < ks1) ? ks1 - w.ks0 : 0;
+  w.lt0 = w.m + w.t * 2 * kRows;
+  return w;
+}
+
 __global__ void __launch_bounds__(kThreads, 1) k_split_gemm(GemmArgs a) {
   extern __shared__ __align__(1024) unsigned char smem[];
   __shared__ GemmSmemHdr h;
-  __shared__ int s_ce[kCols];          // column exponents (eb - 12)
-  __shared__ float s_rh[kRows], s_rl[kRows];   // row factors Dm_l pa as df64
-  __shared__ int s_re[kRows];          // row exponents EA(l)
-
-  const int g = blockIdx.x;
-  const int p = blockIdx.y & 1;
-  const int kci = (blockIdx.y >> 1) % a.nkcmax;
-  const int t = (blockIdx.y >> 1) / a.nkcmax;
-  const int q = a.q0 + blockIdx.z;
-  const int m = m_of_q(q, a.lmax);
-  const int i0 = a.ring_i0[m];
-  const int K = a.nnorth - i0;
-  const int nks = (K + kKStep - 1) / kKStep;
-  const int ntiles = (a.lmax - m + 1 + 2 * kRows - 1) / (2 * kRows);
-  const int ks0 = kci * (kKChunk / kKStep);
-  const int ks1 = min(nks, ks0 + kKChunk / kKStep);
-  if (t >= ntiles || ks0 >= ks1) return;          // uniform: before any barrier or TMEM
-  const int nk = ks1 - ks0;
-  const int lt0 = m + t * 2 * kRows;
+  __shared__ int s_ce[kCols];          // column exponents (eb - 12) of the current unit
 
   const int tid = threadIdx.x;
   const int warp = tid >> 5;
@@ -331,24 +356,10 @@ __global__ void __launch_bounds__(kThreads, 1) k_split_gemm(GemmArgs a) {
       tc::mbar_init(&h.empty[s], 1);
     }
     tc::mbar_init(&h.tfull, 1);
+    tc::mbar_init(&h.tempty, 128);
     tc::mbar_init(&h.fin, 1);
     h.abort = 0;
     tc::mbar_fence_init();
-  }
-  if (tid < kCols) {
-    const int eb = a.EB[(((long long)blockIdx.z * 2 + p) * a.ngroups + g) * kCols + tid];
-    s_ce[tid] = (eb == kEmptyExp) ? kEmptyExp : eb - 12;
-    const int l = lt0 + p + 2 * tid;
-    float fh = 0.f, fl = 0.f;
-    int re = 0;
-    if (l <= a.lmax) {
-      const FshtLamRow rw = a.tab[tri_off(m, a.lmax) + (l - m)];
-      factor_pair(rw.dm * a.pa, fh, fl);
-      re = rw.erow + rw.dx;
-    }
-    s_rh[tid] = fh;
-    s_rl[tid] = fl;
-    s_re[tid] = re;
   }
   if (warp == 0) tc::tmem_alloc(&h.tmem, 512);
   tc::tc_fence_before();
@@ -358,58 +369,103 @@ __global__ void __launch_bounds__(kThreads, 1) k_split_gemm(GemmArgs a) {
 
   uint32_t n_loaded = 0;
   if (tid == 128) {
-    const unsigned char* asrc =
-        a.lbuf + (size_t)(a.lam_off[q] - a.lam_off[a.q0]) * kSlices * kATileBytes +
-        ((size_t)(p * ntiles + t) * nks + ks0) * kSlices * kATileBytes;
-    const unsigned char* bsrc =
-        a.WS + (((size_t)blockIdx.z * 2 + p) * a.ngroups + g) * a.row_bytes +
-        (size_t)ks0 * kSlices * kBTileBytes;
-    for (int i = 0; i < nk; ++i) {
-      const uint32_t st = i % kStagesG;
-      if (!tc::mbar_wait(&h.empty[st], ((i / kStagesG) & 1) ^ 1, abort)) break;
-      unsigned char* dst = smem + st * kStageBytesG;
-      tc::mbar_arrive_expect_tx(&h.full[st], kStageBytesG);
-      tc::bulk_g2s(dst, asrc + (size_t)i * kSlices * kATileBytes, kSlices * kATileBytes,
-                   &h.full[st]);
-      tc::bulk_g2s(dst + kSlices * kATileBytes, bsrc + (size_t)i * kSlices * kBTileBytes,
-                   kSlices * kBTileBytes, &h.full[st]);
-      ++n_loaded;
+    // producer: the k-step ring runs on across units
+    uint32_t i = 0;
+    for (int u = blockIdx.x; u < a.nunits && !*abort; u += gridDim.x) {
+      const GemmUnit w = gemm_unit(a, u);
+      if (w.nk == 0) continue;
+      const unsigned char* asrc =
+          a.lbuf + (size_t)(a.lam_off[a.q0 + w.qi] - a.lam_off[a.q0]) * kSlices * kATileBytes +
+          ((size_t)(w.p * w.ntiles + w.t) * w.nks + w.ks0) * kSlices * kATileBytes;
+      const unsigned char* bsrc =
+          a.WS + (((size_t)w.qi * 2 + w.p) * a.ngroups + w.g) * a.row_bytes +
+          (size_t)w.ks0 * kSlices * kBTileBytes;
+      bool ok = true;
+      for (int k = 0; k < w.nk; ++k, ++i) {
+        const uint32_t st = i % kStagesG;
+        if (!tc::mbar_wait(&h.empty[st], ((i / kStagesG) & 1) ^ 1, abort)) {
+          ok = false;
+          break;
+        }
+        unsigned char* dst = smem + st * kStageBytesG;
+        tc::mbar_arrive_expect_tx(&h.full[st], kStageBytesG);
+        tc::bulk_g2s(dst, asrc + (size_t)k * kSlices * kATileBytes, kSlices * kATileBytes,
+                     &h.full[st]);
+        tc::bulk_g2s(dst + kSlices * kATileBytes, bsrc + (size_t)k * kSlices * kBTileBytes,
+                     kSlices * kBTileBytes, &h.full[st]);
+        ++n_loaded;
+      }
+      if (!ok) break;
     }
   } else if (tid == 160) {
+    // UMMA issuer
     const uint32_t idesc = tc::umma_idesc_bf16(kRows, kCols);
     const uint32_t s_u = tc::smem_u32(smem);
-    for (int i = 0; i < nk; ++i) {
-      const uint32_t st = i % kStagesG;
-      if (!tc::mbar_wait(&h.full[st], (i / kStagesG) & 1, abort)) break;
+    uint32_t i = 0, nu = 0;
+    for (int u = blockIdx.x; u < a.nunits && !*abort; u += gridDim.x) {
+      const GemmUnit w = gemm_unit(a, u);
+      if (w.nk == 0) continue;
+      // the epilogue of the previous unit has read the accumulators
+      if (nu > 0 && !tc::mbar_wait(&h.tempty, (nu - 1) & 1, abort)) break;
       tc::tc_fence_after();
-      const uint32_t abase = s_u + st * kStageBytesG;
-      const uint32_t bbase = abase + kSlices * kATileBytes;
-#pragma unroll
-      for (int lev = 0; lev <= 3; ++lev) {
-#pragma unroll
-        for (int aa = 0; aa <= lev; ++aa) {
-          const uint64_t ad = tc::umma_desc(abase + aa * kATileBytes, 128, 256);
-          const uint64_t bd = tc::umma_desc(bbase + (lev - aa) * kBTileBytes, 128, 256);
-          tc::umma_bf16(tmem + lev * kCols, ad, bd, idesc, (i > 0 || aa > 0) ? 1u : 0u);
+      bool ok = true;
+      for (int k = 0; k < w.nk; ++k, ++i) {
+        const uint32_t st = i % kStagesG;
+        if (!tc::mbar_wait(&h.full[st], (i / kStagesG) & 1, abort)) {
+          ok = false;
+          break;
         }
+        tc::tc_fence_after();
+        const uint32_t abase = s_u + st * kStageBytesG;
+        const uint32_t bbase = abase + kSlices * kATileBytes;
+#pragma unroll
+        for (int lev = 0; lev <= 3; ++lev) {
+#pragma unroll
+          for (int aa = 0; aa <= lev; ++aa) {
+            const uint64_t ad = tc::umma_desc(abase + aa * kATileBytes, 128, 256);
+            const uint64_t bd = tc::umma_desc(bbase + (lev - aa) * kBTileBytes, 128, 256);
+            tc::umma_bf16(tmem + lev * kCols, ad, bd, idesc, (k > 0 || aa > 0) ? 1u : 0u);
+          }
+        }
+        tc::umma_commit(&h.empty[st]);
       }
-      tc::umma_commit(&h.empty[st]);
+      if (!ok) break;
+      tc::umma_commit(&h.tfull);
+      ++nu;
     }
-    tc::umma_commit(&h.tfull);
-  }
-  // ---------------- epilogue (warps 0-3): TMEM -> alm
-  if (tid < 128) {
-    bool ok = tc::mbar_wait(&h.tfull, 0, abort);
-    ok = __all_sync(0xffffffffu, ok);      // tcgen05.ld below is warp-collective
-    tc::tc_fence_after();
+  } else if (tid < 128) {
+    // epilogue (warps 0-3): TMEM -> alm, row = TMEM lane
     const int row = (warp << 5) + (tid & 31);
-    const int l = lt0 + p + 2 * row;
-    const bool rowok = l <= a.lmax;
-    if (ok) {
-      const float rh = s_rh[row], rl = s_rl[row];
-      const int re = s_re[row];
-      const long long L1 = a.lmax + 1;
-      const uint32_t lane_base = tmem + ((uint32_t)(warp << 5) << 16);
+    const long long L1 = a.lmax + 1;
+    const uint32_t lane_base = tmem + ((uint32_t)(warp << 5) << 16);
+    uint32_t nu = 0;
+    for (int u = blockIdx.x; u < a.nunits; u += gridDim.x) {
+      const GemmUnit w = gemm_unit(a, u);
+      if (w.nk == 0) continue;
+      // this unit's column exponents and this thread's row factor
+      {
+        const int eb = a.EB[(((long long)w.qi * 2 + w.p) * a.ngroups + w.g) * kCols + tid];
+        // the previous unit's readers of s_ce are done (named barrier of the 128 threads)
+        asm volatile("bar.sync 1, 128;" ::: "memory");
+        s_ce[tid] = (eb == kEmptyExp) ? kEmptyExp : eb - 12;
+        asm volatile("bar.sync 1, 128;" ::: "memory");
+      }
+      const int l = w.lt0 + w.p + 2 * row;
+      const bool rowok = l <= a.lmax;
+      float rh = 0.f, rl = 0.f;
+      int re = 0;
+      if (rowok) {
+        const FshtLamRow rw = a.tab[tri_off(w.m, a.lmax) + (l - w.m)];
+        factor_pair(rw.dm * a.pa, rh, rl);
+        re = rw.erow + rw.dx;
+      }
+      // No early exit from this loop: the 128 threads must meet at every named barrier, so
+      // after an expired wait (abort) the remaining units are walked without work.
+      bool ok = tc::mbar_wait(&h.tfull, nu & 1, abort);
+      ok = __all_sync(0xffffffffu, ok);      // tcgen05.ld below is warp-collective
+      ++nu;
+      if (!ok) continue;
+      tc::tc_fence_after();
       for (int c0 = 0; c0 < kCols; c0 += 16) {
         uint32_t v0[16], v1[16], v2[16], v3[16];
         tc::tmem_ld16(lane_base + 0 * kCols + c0, v0);
@@ -417,13 +473,19 @@ __global__ void __launch_bounds__(kThreads, 1) k_split_gemm(GemmArgs a) {
         tc::tmem_ld16(lane_base + 2 * kCols + c0, v2);
         tc::tmem_ld16(lane_base + 3 * kCols + c0, v3);
         tc::tmem_wait_ld();
+        if (c0 == kCols - 16) {
+          // every accumulator column of this unit is in registers: hand TMEM back
+          tc::tc_fence_before();
+          tc::mbar_arrive(&h.tempty);
+        }
         const int comp = c0 >> 6;
-        const bool store = rowok && !(comp == 1 && m == 0);
-        const long long rowidx = comp == 0 ? ((long long)m * L1 + l) : ((L1 - m) * L1 + (l - m));
+        const bool store = rowok && !(comp == 1 && w.m == 0);
+        const long long rowidx =
+            comp == 0 ? ((long long)w.m * L1 + l) : ((L1 - w.m) * L1 + (l - w.m));
 #pragma unroll
         for (int j = 0; j < 16; ++j) {
           const int c = c0 + j;
-          const int k = g * kGroupMaps + (c & 63);
+          const int k = w.g * kGroupMaps + (c & 63);
           if (store && k < a.kc) {
             const double v = levels_scaled(v0[j], v1[j], v2[j], v3[j], rh, rl, re + s_ce[c]);
             double* dst = a.alm + rowidx * a.ld + a.k0 + k;
@@ -844,7 +906,7 @@ int fsht_launch_split_slice(fsht_plan* p, int w, const double2* W, unsigned char
   sa.ring_i0 = p->d_ring_i0;
   sa.WS = WS;
   sa.EB = EB;
-  k_slice_phase<<<dim3(wv[1] - wv[0], sa.ngroups), 256, 0, s>>>(sa);
+  k_slice_phase<<<dim3(wv[1] - wv[0], sa.ngroups), 512, 0, s>>>(sa);
   FSHT_LAUNCH_CHECK();
   return FSHT_OK;
 }
@@ -975,10 +1037,15 @@ int fsht_launch_split_gemm(fsht_plan* p, int w, const unsigned char* WS, const i
   a.kc = kc;
   a.pa = p->pa;
   a.err = p->d_err;
+  a.nunits = a.ngroups * 2 * a.ntmax * a.nkcmax * (wv[1] - wv[0]);
   const size_t sm = (size_t)kStagesG * kStageBytesG;
   FSHT_CUDA_TRY(
       cudaFuncSetAttribute(k_split_gemm, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-  k_split_gemm<<<dim3(a.ngroups, 2 * a.ntmax * a.nkcmax, wv[1] - wv[0]), kThreads, sm, s>>>(a);
+  int dev = 0, nsm = 0;
+  FSHT_CUDA_TRY(cudaGetDevice(&dev));
+  FSHT_CUDA_TRY(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+  const int grid = a.nunits < nsm ? a.nunits : nsm;
+  if (grid > 0) k_split_gemm<<<grid, kThreads, sm, s>>>(a);
   FSHT_LAUNCH_CHECK();
   return FSHT_OK;
 }
