@@ -677,13 +677,15 @@ def e2e(sht, maps_dev, ke, args, world):
 
 def _e2e_run(sht, maps_dev, ke, args, world, local):
     import torch
+    from fastsht_gb300 import pinned_empty
     npix = sht.npix
     L = sht.lmax + 1
-    host = torch.empty((ke, npix), dtype=torch.float64, pin_memory=True)
+    # page-locked host buffers from the library (cudaHostAlloc), as a user of the host API
+    maps_np = pinned_empty((npix, ke))           # Fortran order
+    host = torch.from_numpy(maps_np.T)           # (ke, npix) view of the same memory
     host.copy_(maps_dev.T[:ke])
-    maps_np = host.numpy().T                     # (npix, ke) Fortran order
-    out_t = torch.empty((L, L, ke), dtype=torch.float64, pin_memory=True)
-    out_np = out_t.numpy().T                     # (ke, L, L) Fortran order
+    out_np = pinned_empty((ke, L, L))            # Fortran order
+    out_t = torch.from_numpy(out_np.T)           # (L, L, ke) view
     sht.t2alm(maps_np, alms_in=out_np)           # warm-up
     torch.cuda.synchronize()
     t0 = time.perf_counter()

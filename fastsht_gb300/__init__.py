@@ -4,6 +4,6 @@ A from-scratch sm_103a implementation of the batched SHT path of
 liuhao-cn/fastSHT behind the same ``SHT`` class surface (see ``sht.SHT``), with
 the transforms in a C-ABI CUDA library (``include/fastsht.h``).
 """
-from .sht import SHT  # noqa: F401
+from .sht import SHT, pinned_empty  # noqa: F401
 
-__all__ = ["SHT"]
+__all__ = ["SHT", "pinned_empty"]

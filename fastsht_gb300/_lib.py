@@ -62,6 +62,8 @@ SIGNATURES = {
     "fsht_plan_sync": [_vp],
     "fsht_plan_check": [_vp],
     "fsht_selftest_wait_timeout": [_vp],
+    "fsht_host_alloc": [_sz, C.POINTER(_vp)],
+    "fsht_host_free": [_vp],
     "fsht_run_stage": [_vp, _i, _vp, _vp, _i],
     "fsht_profile_enable": [_vp, _i],
     "fsht_profile_read": [_vp, _i, C.POINTER(_i), C.POINTER(C.c_double)],

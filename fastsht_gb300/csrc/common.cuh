@@ -243,13 +243,11 @@ int fsht_launch_analysis_fp64(fsht_plan* p, int spin, const double2* WQ,
 size_t fsht_split_ws_bytes(const fsht_plan* p, int kc);
 size_t fsht_split_eb_bytes(const fsht_plan* p, int kc);
 // Spin-0 analysis of one chunk (BF16 digits on tcgen05).  Tables (plan creation): recursion
-// rows, per-m tile offsets, waves of m and the staging size.  Per chunk: clear alm's chunk
-// columns when ring K-chunks will add into it; per wave w: slice cuts the {S, D} matrix W of
-// the wave's orders into digit tiles WS and column exponents EB, lambda writes the wave's
-// lambda digit tiles into lbuf, gemm contracts them into alm.
+// rows, per-m tile offsets, waves of m and the staging size.  Per wave w: slice cuts the
+// {S, D} matrix W of the wave's orders into digit tiles WS and column exponents EB, lambda
+// writes the wave's lambda digit tiles into lbuf, gemm contracts them into alm (stores, or
+// adds when accumulate).
 int fsht_split_tables_init(fsht_plan* p);
-int fsht_split_clear_alm(fsht_plan* p, double* alm, int nmaps_total, int k0, int kc,
-                         cudaStream_t s);
 int fsht_launch_split_slice(fsht_plan* p, int w, const double2* W, unsigned char* WS, int* EB,
                             int kc, cudaStream_t s);
 int fsht_launch_split_lambda(fsht_plan* p, int w, unsigned char* lbuf, cudaStream_t s);

@@ -283,19 +283,22 @@ __global__ void __launch_bounds__(128) k_lambda_digits(LamArgs a) {
 
 // ------------------------------------------------------------------ split GEMM
 // Persistent: one CTA per SM walks the wave's work units u = blockIdx.x, + gridDim.x, ...;
-// a unit is (q, parity, l-tile, K-chunk, 64-map group), the group fastest, so CTAs running
-// at the same time share lambda tiles in L2.  A unit is one 128-row x 128-column output tile
-// over <= 64 k-steps of 16 rings.  Warp 4 lane 0 streams lambda and P digit tiles (bulk async
-// copies) through a kStagesG-deep ring that runs on across units, so the next unit's tiles
-// load while the current one's epilogue drains the accumulators; warp 5 lane 0 issues the
-// ten level-ordered UMMAs per k-step; warps 0-3 run the epilogue.  TMEM (four 128-column
-// level accumulators) is allocated once per CTA; tfull / tempty hand it between the UMMA
-// issuer and the epilogue for every unit.
+// a unit is (q, parity, l-tile, 64-map group), the group fastest, so CTAs running at the same
+// time share lambda tiles in L2.  A unit is one 128-row x 128-column output tile over all of
+// its k-steps of 16 rings, accumulated in parts of <= 64 k-steps (1024 rings keep levels 0
+// and 1 exact in FP32): the first part's epilogue stores, later parts add as fire-and-forget
+// reductions (one thread owns each element, so the result is deterministic).  Warp 8 lane 0 streams lambda and P digit tiles (bulk async copies) through a
+// kStagesG-deep ring that runs on across parts and units, so the next tiles load while an
+// epilogue drains the accumulators; warp 9 lane 0 issues the ten level-ordered UMMAs per
+// k-step; warps 0-7 run the epilogue.  TMEM (four 128-column level accumulators) is
+// allocated once per CTA; tfull / tempty hand it between the UMMA issuer and the epilogue for
+// every part.
 constexpr int kStagesG = 6;
 constexpr uint32_t kStageBytesG = 2 * kSlices * kATileBytes;    // 32 KB: A then B
+constexpr int kPartSteps = kKChunk / kKStep;                    // k-steps per part
 
 struct GemmArgs {
-  int lmax, nnorth, ngroups, nkc_glob, q0, ntmax, nkcmax, accumulate, nunits;
+  int lmax, nnorth, ngroups, q0, ntmax, accumulate, nunits;
   size_t row_bytes;
   const int* ring_i0;
   const long long* lam_off;
@@ -315,10 +318,9 @@ struct __align__(8) GemmSmemHdr {
   int abort;
 };
 
-// One work unit, decoded from its index; nk = 0: nothing to do (l-tile beyond lmax - m, or a
-// K-chunk past the kept rings).
+// One work unit, decoded from its index; nks = 0: nothing to do (l-tile beyond lmax - m).
 struct GemmUnit {
-  int g, p, kci, t, qi, m, nks, ntiles, ks0, nk, lt0;
+  int g, p, t, qi, m, nks, ntiles, lt0;
 };
 
 __device__ __forceinline__ GemmUnit gemm_unit(const GemmArgs& a, int u) {
@@ -327,22 +329,17 @@ __device__ __forceinline__ GemmUnit gemm_unit(const GemmArgs& a, int u) {
   int r = u / a.ngroups;
   w.p = r & 1;
   r >>= 1;
-  w.kci = r % a.nkcmax;
-  r /= a.nkcmax;
   w.t = r % a.ntmax;
   w.qi = r / a.ntmax;
   w.m = m_of_q(a.q0 + w.qi, a.lmax);
   const int K = a.nnorth - a.ring_i0[w.m];
-  w.nks = (K + kKStep - 1) / kKStep;
   w.ntiles = (a.lmax - w.m + 1 + 2 * kRows - 1) / (2 * kRows);
-  w.ks0 = w.kci * (kKChunk / kKStep);
-  const int ks1 = min(w.nks, w.ks0 + kKChunk / kKStep);
-  w.nk = (w.t < w.ntiles && w.ks0 < ks1) ? ks1 - w.ks0 : 0;
+  w.nks = w.t < w.ntiles ? (K + kKStep - 1) / kKStep : 0;
   w.lt0 = w.m + w.t * 2 * kRows;
   return w;
 }
 
-__global__ void __launch_bounds__(kThreads, 1) k_split_gemm(GemmArgs a) {
+__global__ void __launch_bounds__(kThreadsG, 1) k_split_gemm(GemmArgs a) {
   extern __shared__ __align__(1024) unsigned char smem[];
   __shared__ GemmSmemHdr h;
   __shared__ int s_ce[kCols];          // column exponents (eb - 12) of the current unit
@@ -356,7 +353,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_split_gemm(GemmArgs a) {
       tc::mbar_init(&h.empty[s], 1);
     }
     tc::mbar_init(&h.tfull, 1);
-    tc::mbar_init(&h.tempty, 128);
+    tc::mbar_init(&h.tempty, kEpiThreads);
     tc::mbar_init(&h.fin, 1);
     h.abort = 0;
     tc::mbar_fence_init();
@@ -368,20 +365,19 @@ __global__ void __launch_bounds__(kThreads, 1) k_split_gemm(GemmArgs a) {
   const uint32_t tmem = h.tmem;
 
   uint32_t n_loaded = 0;
-  if (tid == 128) {
-    // producer: the k-step ring runs on across units
+  if (tid == kEpiThreads) {
+    // producer: the k-step ring runs on across parts and units
     uint32_t i = 0;
     for (int u = blockIdx.x; u < a.nunits && !*abort; u += gridDim.x) {
       const GemmUnit w = gemm_unit(a, u);
-      if (w.nk == 0) continue;
+      if (w.nks == 0) continue;
       const unsigned char* asrc =
           a.lbuf + (size_t)(a.lam_off[a.q0 + w.qi] - a.lam_off[a.q0]) * kSlices * kATileBytes +
-          ((size_t)(w.p * w.ntiles + w.t) * w.nks + w.ks0) * kSlices * kATileBytes;
+          (size_t)(w.p * w.ntiles + w.t) * w.nks * kSlices * kATileBytes;
       const unsigned char* bsrc =
-          a.WS + (((size_t)w.qi * 2 + w.p) * a.ngroups + w.g) * a.row_bytes +
-          (size_t)w.ks0 * kSlices * kBTileBytes;
+          a.WS + (((size_t)w.qi * 2 + w.p) * a.ngroups + w.g) * a.row_bytes;
       bool ok = true;
-      for (int k = 0; k < w.nk; ++k, ++i) {
+      for (int k = 0; k < w.nks; ++k, ++i) {
         const uint32_t st = i % kStagesG;
         if (!tc::mbar_wait(&h.empty[st], ((i / kStagesG) & 1) ^ 1, abort)) {
           ok = false;
@@ -397,58 +393,66 @@ __global__ void __launch_bounds__(kThreads, 1) k_split_gemm(GemmArgs a) {
       }
       if (!ok) break;
     }
-  } else if (tid == 160) {
+  } else if (tid == kEpiThreads + 32) {
     // UMMA issuer
     const uint32_t idesc = tc::umma_idesc_bf16(kRows, kCols);
     const uint32_t s_u = tc::smem_u32(smem);
-    uint32_t i = 0, nu = 0;
-    for (int u = blockIdx.x; u < a.nunits && !*abort; u += gridDim.x) {
+    uint32_t i = 0, np = 0;
+    bool ok = true;
+    for (int u = blockIdx.x; u < a.nunits && ok && !*abort; u += gridDim.x) {
       const GemmUnit w = gemm_unit(a, u);
-      if (w.nk == 0) continue;
-      // the epilogue of the previous unit has read the accumulators
-      if (nu > 0 && !tc::mbar_wait(&h.tempty, (nu - 1) & 1, abort)) break;
-      tc::tc_fence_after();
-      bool ok = true;
-      for (int k = 0; k < w.nk; ++k, ++i) {
-        const uint32_t st = i % kStagesG;
-        if (!tc::mbar_wait(&h.full[st], (i / kStagesG) & 1, abort)) {
+      for (int ks0 = 0; ks0 < w.nks && ok; ks0 += kPartSteps, ++np) {
+        // the epilogue of the previous part has read the accumulators
+        if (np > 0 && !tc::mbar_wait(&h.tempty, (np - 1) & 1, abort)) {
           ok = false;
           break;
         }
         tc::tc_fence_after();
-        const uint32_t abase = s_u + st * kStageBytesG;
-        const uint32_t bbase = abase + kSlices * kATileBytes;
-#pragma unroll
-        for (int lev = 0; lev <= 3; ++lev) {
-#pragma unroll
-          for (int aa = 0; aa <= lev; ++aa) {
-            const uint64_t ad = tc::umma_desc(abase + aa * kATileBytes, 128, 256);
-            const uint64_t bd = tc::umma_desc(bbase + (lev - aa) * kBTileBytes, 128, 256);
-            tc::umma_bf16(tmem + lev * kCols, ad, bd, idesc, (k > 0 || aa > 0) ? 1u : 0u);
+        const int nk = min(w.nks - ks0, kPartSteps);
+        for (int k = 0; k < nk; ++k, ++i) {
+          const uint32_t st = i % kStagesG;
+          if (!tc::mbar_wait(&h.full[st], (i / kStagesG) & 1, abort)) {
+            ok = false;
+            break;
           }
+          tc::tc_fence_after();
+          const uint32_t abase = s_u + st * kStageBytesG;
+          const uint32_t bbase = abase + kSlices * kATileBytes;
+#pragma unroll
+          for (int lev = 0; lev <= 3; ++lev) {
+#pragma unroll
+            for (int aa = 0; aa <= lev; ++aa) {
+              const uint64_t ad = tc::umma_desc(abase + aa * kATileBytes, 128, 256);
+              const uint64_t bd = tc::umma_desc(bbase + (lev - aa) * kBTileBytes, 128, 256);
+              tc::umma_bf16(tmem + lev * kCols, ad, bd, idesc, (k > 0 || aa > 0) ? 1u : 0u);
+            }
+          }
+          tc::umma_commit(&h.empty[st]);
         }
-        tc::umma_commit(&h.empty[st]);
+        if (ok) tc::umma_commit(&h.tfull);
       }
-      if (!ok) break;
-      tc::umma_commit(&h.tfull);
-      ++nu;
     }
-  } else if (tid < 128) {
-    // epilogue (warps 0-3): TMEM -> alm, row = TMEM lane
-    const int row = (warp << 5) + (tid & 31);
+  } else if (tid < kEpiThreads) {
+    // epilogue (warps 0-7): TMEM -> alm, row = TMEM lane (warp % 4 picks the lane quarter,
+    // warp / 4 the half of the columns).  No early exit: the epilogue threads must meet at
+    // every named barrier, so after an expired wait (abort) the remaining parts are walked
+    // without work.
+    const int row = ((warp & 3) << 5) + (tid & 31);
+    const int cbeg = (warp >> 2) * (kCols / 2);   // this warp's half of the columns
     const long long L1 = a.lmax + 1;
-    const uint32_t lane_base = tmem + ((uint32_t)(warp << 5) << 16);
-    uint32_t nu = 0;
+    const uint32_t lane_base = tmem + ((uint32_t)((warp & 3) << 5) << 16);
+    uint32_t np = 0;
     for (int u = blockIdx.x; u < a.nunits; u += gridDim.x) {
       const GemmUnit w = gemm_unit(a, u);
-      if (w.nk == 0) continue;
+      if (w.nks == 0) continue;
       // this unit's column exponents and this thread's row factor
       {
-        const int eb = a.EB[(((long long)w.qi * 2 + w.p) * a.ngroups + w.g) * kCols + tid];
-        // the previous unit's readers of s_ce are done (named barrier of the 128 threads)
-        asm volatile("bar.sync 1, 128;" ::: "memory");
-        s_ce[tid] = (eb == kEmptyExp) ? kEmptyExp : eb - 12;
-        asm volatile("bar.sync 1, 128;" ::: "memory");
+        const int eb =
+            tid < kCols ? a.EB[(((long long)w.qi * 2 + w.p) * a.ngroups + w.g) * kCols + tid] : 0;
+        // the previous unit's readers of s_ce are done (named barrier of the epilogue threads)
+        asm volatile("bar.sync 1, %0;" ::"n"(kEpiThreads) : "memory");
+        if (tid < kCols) s_ce[tid] = (eb == kEmptyExp) ? kEmptyExp : eb - 12;
+        asm volatile("bar.sync 1, %0;" ::"n"(kEpiThreads) : "memory");
       }
       const int l = w.lt0 + w.p + 2 * row;
       const bool rowok = l <= a.lmax;
@@ -459,39 +463,42 @@ __global__ void __launch_bounds__(kThreads, 1) k_split_gemm(GemmArgs a) {
         factor_pair(rw.dm * a.pa, rh, rl);
         re = rw.erow + rw.dx;
       }
-      // No early exit from this loop: the 128 threads must meet at every named barrier, so
-      // after an expired wait (abort) the remaining units are walked without work.
-      bool ok = tc::mbar_wait(&h.tfull, nu & 1, abort);
-      ok = __all_sync(0xffffffffu, ok);      // tcgen05.ld below is warp-collective
-      ++nu;
-      if (!ok) continue;
-      tc::tc_fence_after();
-      for (int c0 = 0; c0 < kCols; c0 += 16) {
-        uint32_t v0[16], v1[16], v2[16], v3[16];
-        tc::tmem_ld16(lane_base + 0 * kCols + c0, v0);
-        tc::tmem_ld16(lane_base + 1 * kCols + c0, v1);
-        tc::tmem_ld16(lane_base + 2 * kCols + c0, v2);
-        tc::tmem_ld16(lane_base + 3 * kCols + c0, v3);
-        tc::tmem_wait_ld();
-        if (c0 == kCols - 16) {
-          // every accumulator column of this unit is in registers: hand TMEM back
-          tc::tc_fence_before();
-          tc::mbar_arrive(&h.tempty);
-        }
-        const int comp = c0 >> 6;
-        const bool store = rowok && !(comp == 1 && w.m == 0);
-        const long long rowidx =
-            comp == 0 ? ((long long)w.m * L1 + l) : ((L1 - w.m) * L1 + (l - w.m));
+      for (int ks0 = 0; ks0 < w.nks; ks0 += kPartSteps) {
+        bool ok = tc::mbar_wait(&h.tfull, np & 1, abort);
+        ok = __all_sync(0xffffffffu, ok);      // tcgen05.ld below is warp-collective
+        ++np;
+        if (!ok) continue;
+        tc::tc_fence_after();
+        const bool add = ks0 > 0 || a.accumulate;
+        for (int c0 = cbeg; c0 < cbeg + kCols / 2; c0 += 16) {
+          uint32_t v0[16], v1[16], v2[16], v3[16];
+          tc::tmem_ld16(lane_base + 0 * kCols + c0, v0);
+          tc::tmem_ld16(lane_base + 1 * kCols + c0, v1);
+          tc::tmem_ld16(lane_base + 2 * kCols + c0, v2);
+          tc::tmem_ld16(lane_base + 3 * kCols + c0, v3);
+          tc::tmem_wait_ld();
+          if (c0 == cbeg + kCols / 2 - 16) {
+            // every accumulator column of this part is in registers: hand TMEM back
+            tc::tc_fence_before();
+            tc::mbar_arrive(&h.tempty);
+          }
+          const int comp = c0 >> 6;
+          const bool store = rowok && !(comp == 1 && w.m == 0);
+          const long long rowidx =
+              comp == 0 ? ((long long)w.m * L1 + l) : ((L1 - w.m) * L1 + (l - w.m));
 #pragma unroll
-        for (int j = 0; j < 16; ++j) {
-          const int c = c0 + j;
-          const int k = w.g * kGroupMaps + (c & 63);
-          if (store && k < a.kc) {
-            const double v = levels_scaled(v0[j], v1[j], v2[j], v3[j], rh, rl, re + s_ce[c]);
-            double* dst = a.alm + rowidx * a.ld + a.k0 + k;
-            if (a.nkc_glob > 1) atomicAdd(dst, v);
-            else if (a.accumulate) *dst += v;
-            else *dst = v;
+          for (int j = 0; j < 16; ++j) {
+            const int c = c0 + j;
+            const int k = w.g * kGroupMaps + (c & 63);
+            if (store && k < a.kc) {
+              const double v = levels_scaled(v0[j], v1[j], v2[j], v3[j], rh, rl, re + s_ce[c]);
+              double* dst = a.alm + rowidx * a.ld + a.k0 + k;
+              // adds go out as fire-and-forget reductions (no load latency in the epilogue);
+              // one thread owns each element, so the order (store, then adds) is its program
+              // order and the result is deterministic
+              if (add) atomicAdd(dst, v);
+              else *dst = v;
+            }
           }
         }
       }
@@ -499,12 +506,12 @@ __global__ void __launch_bounds__(kThreads, 1) k_split_gemm(GemmArgs a) {
   }
   // drain: the UMMA issuer waits for its last products before TMEM is released, and the
   // loader for its last copies
-  if (tid == 160) {
+  if (tid == kEpiThreads + 32) {
     tc::umma_commit(&h.fin);
     for (uint32_t it = 0; it < tc::kWaitLimit; ++it)
       if (tc::mbar_try_wait(&h.fin, 0)) break;
   }
-  if (tid == 128) {
+  if (tid == kEpiThreads) {
     for (uint32_t d = 0; d < (uint32_t)kStagesG && d < n_loaded; ++d) {
       const uint32_t i = n_loaded - 1 - d;
       for (uint32_t it = 0; it < tc::kWaitLimit; ++it)
@@ -880,18 +887,6 @@ size_t fsht_split_eb_bytes(const fsht_plan* p, int kc) {
   return (size_t)p->wave_qmax * 2 * ngroups * kCols * sizeof(int);
 }
 
-int fsht_split_clear_alm(fsht_plan* p, double* alm, int nmaps_total, int k0, int kc,
-                         cudaStream_t s) {
-  const int nkc = (p->nnorth + kKChunk - 1) / kKChunk;
-  if (nkc > 1 && alm) {
-    // K-chunks add into alm: clear this chunk's columns first
-    const size_t L1 = (size_t)p->lmax + 1;
-    FSHT_CUDA_TRY(cudaMemset2DAsync(alm + k0, sizeof(double) * nmaps_total, 0,
-                                    sizeof(double) * kc, L1 * L1, s));
-  }
-  return FSHT_OK;
-}
-
 int fsht_launch_split_slice(fsht_plan* p, int w, const double2* W, unsigned char* WS, int* EB,
                             int kc, cudaStream_t s) {
   const int* wv = p->h_waves + kWaveInts * w;
@@ -1020,11 +1015,9 @@ int fsht_launch_split_gemm(fsht_plan* p, int w, const unsigned char* WS, const i
   a.nnorth = p->nnorth;
   a.ngroups = (kc + kGroupMaps - 1) / kGroupMaps;
   a.row_bytes = ws_row_bytes(p->lmax, p->nnorth);
-  a.nkc_glob = (p->nnorth + kKChunk - 1) / kKChunk;
   a.accumulate = accumulate;
   a.q0 = wv[0];
   a.ntmax = wv[2];
-  a.nkcmax = wv[3];
   a.ring_i0 = p->d_ring_i0;
   a.lam_off = p->d_lam_off;
   a.tab = p->d_lamtab;
@@ -1037,7 +1030,7 @@ int fsht_launch_split_gemm(fsht_plan* p, int w, const unsigned char* WS, const i
   a.kc = kc;
   a.pa = p->pa;
   a.err = p->d_err;
-  a.nunits = a.ngroups * 2 * a.ntmax * a.nkcmax * (wv[1] - wv[0]);
+  a.nunits = a.ngroups * 2 * a.ntmax * (wv[1] - wv[0]);
   const size_t sm = (size_t)kStagesG * kStageBytesG;
   FSHT_CUDA_TRY(
       cudaFuncSetAttribute(k_split_gemm, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
@@ -1045,7 +1038,7 @@ int fsht_launch_split_gemm(fsht_plan* p, int w, const unsigned char* WS, const i
   FSHT_CUDA_TRY(cudaGetDevice(&dev));
   FSHT_CUDA_TRY(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
   const int grid = a.nunits < nsm ? a.nunits : nsm;
-  if (grid > 0) k_split_gemm<<<grid, kThreads, sm, s>>>(a);
+  if (grid > 0) k_split_gemm<<<grid, kThreadsG, sm, s>>>(a);
   FSHT_LAUNCH_CHECK();
   return FSHT_OK;
 }

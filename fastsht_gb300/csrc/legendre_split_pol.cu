@@ -199,13 +199,17 @@ __global__ void __launch_bounds__(128) k_lambda_digits_pol(LamPArgs a) {
   }
 }
 
-// CTA = (group, field x parity x l-tile x K-chunk, q): the lambda1 pass then the lambda2
-// pass through the same TMEM accumulators.
+// Persistent, like k_split_gemm: one CTA per SM walks work units (q, l-tile, parity, field
+// E|B, 64-map group), the group fastest.  A unit runs, per part of <= 64 k-steps (1024 rings
+// keep levels 0 and 1 exact), the lambda1 pass then the lambda2 pass through the same TMEM
+// accumulators; the epilogue of each pass stores or adds (fire-and-forget reductions; the same
+// thread handles every pass of an element, so the result is deterministic).
 constexpr int kStagesP = 6;
 constexpr uint32_t kStageBytesP = 2 * kSlices * kATileBytes;    // 32 KB: A then B
+constexpr int kPartStepsP = kKChunk / kKStep;
 
 struct GemmPArgs {
-  int lmax, nnorth, ngroups, nkc_glob, q0, ntmax, nkcmax, accumulate, which;
+  int lmax, nnorth, ngroups, q0, ntmax, accumulate, which, nunits;
   size_t row_bytes;
   const int* ring_i0;
   const long long* lam_off;
@@ -228,39 +232,33 @@ struct __align__(8) GemmPSmemHdr {
   int abort;
 };
 
-__global__ void __launch_bounds__(kThreads, 1) k_split_gemm_pol(GemmPArgs a) {
+// One work unit; nks = 0: nothing to do (l-tile beyond lmax - m, or a field not asked for).
+struct GemmPUnit {
+  int g, field, p, t, qi, m, nks, ntiles, lt0;
+};
+
+__device__ __forceinline__ GemmPUnit gemm_pol_unit(const GemmPArgs& a, int u) {
+  GemmPUnit w;
+  w.g = u % a.ngroups;
+  int r = u / a.ngroups;
+  w.field = r & 1;               // 0: E, 1: B
+  r >>= 1;
+  w.p = r & 1;
+  r >>= 1;
+  w.t = r % a.ntmax;
+  w.qi = r / a.ntmax;
+  w.m = m_of_q(a.q0 + w.qi, a.lmax);
+  const int K = a.nnorth - a.ring_i0[w.m];
+  w.ntiles = (a.lmax - w.m + 1 + 2 * kRows - 1) / (2 * kRows);
+  w.nks = (w.t < w.ntiles && (a.which & (1 << w.field))) ? (K + kKStep - 1) / kKStep : 0;
+  w.lt0 = w.m + w.t * 2 * kRows;
+  return w;
+}
+
+__global__ void __launch_bounds__(kThreadsG, 1) k_split_gemm_pol(GemmPArgs a) {
   extern __shared__ __align__(1024) unsigned char smem[];
   __shared__ GemmPSmemHdr h;
-  __shared__ int s_ce[2][kCols];       // column exponents (e - 12) per part
-  __shared__ float s_rh[kRows], s_rl[kRows];   // row factors -Dm_l pa as df64
-  __shared__ int s_re[kRows];          // row exponents EA(l)
-
-  const int g = blockIdx.x;
-  const int field = blockIdx.y & 1;            // 0: E, 1: B
-  const int p = (blockIdx.y >> 1) & 1;
-  const int rest = blockIdx.y >> 2;
-  const int kci = rest % a.nkcmax;
-  const int t = rest / a.nkcmax;
-  if (!(a.which & (1 << field))) return;
-  const int q = a.q0 + blockIdx.z;
-  const int m = m_of_q(q, a.lmax);
-  const int i0 = a.ring_i0[m];
-  const int K = a.nnorth - i0;
-  const int nks = (K + kKStep - 1) / kKStep;
-  const int ntiles = (a.lmax - m + 1 + 2 * kRows - 1) / (2 * kRows);
-  const int ks0 = kci * (kKChunk / kKStep);
-  const int ks1 = min(nks, ks0 + kKChunk / kKStep);
-  if (t >= ntiles || ks0 >= ks1) return;          // uniform: before any barrier or TMEM
-  const int nk = ks1 - ks0;
-  const int lt0 = m + t * 2 * kRows;
-  // B operands and their column exponents: part 0 multiplies lambda1, part 1 lambda2
-  const unsigned char* ws[2];
-  const int* eb[2];
-  int bpar[2] = {p, 1 - p};
-  ws[0] = field == 0 ? a.WSQ : a.WSU;
-  eb[0] = field == 0 ? a.EBQ : a.EBU;
-  ws[1] = field == 0 ? a.WSU : a.WSQ;
-  eb[1] = field == 0 ? a.EBU : a.EBQ;
+  __shared__ int s_ce[2][kCols];       // column exponents (e - 12) per pass of the unit
 
   const int tid = threadIdx.x;
   const int warp = tid >> 5;
@@ -271,27 +269,10 @@ __global__ void __launch_bounds__(kThreads, 1) k_split_gemm_pol(GemmPArgs a) {
       tc::mbar_init(&h.empty[s], 1);
     }
     tc::mbar_init(&h.tfull, 1);
-    tc::mbar_init(&h.tempty, 128);
+    tc::mbar_init(&h.tempty, kEpiThreads);
     tc::mbar_init(&h.fin, 1);
     h.abort = 0;
     tc::mbar_fence_init();
-  }
-  if (tid < kCols) {
-    for (int part = 0; part < 2; ++part) {
-      const int e = eb[part][(((long long)blockIdx.z * 2 + bpar[part]) * a.ngroups + g) * kCols + tid];
-      s_ce[part][tid] = (e == kEmptyExp) ? kEmptyExp : e - 12;
-    }
-    const int l = lt0 + p + 2 * tid;
-    float fh = 0.f, fl = 0.f;
-    int re = 0;
-    if (l <= a.lmax) {
-      const FshtLamRow rw = a.tab[tri_off(m, a.lmax) + (l - m)];
-      factor_pair(-rw.dm * a.pa, fh, fl);
-      re = rw.erow + rw.dx;
-    }
-    s_rh[tid] = fh;
-    s_rl[tid] = fl;
-    s_re[tid] = re;
   }
   if (warp == 0) tc::tmem_alloc(&h.tmem, 512);
   tc::tc_fence_before();
@@ -300,110 +281,176 @@ __global__ void __launch_bounds__(kThreads, 1) k_split_gemm_pol(GemmPArgs a) {
   const uint32_t tmem = h.tmem;
 
   uint32_t n_loaded = 0;
-  if (tid == 128) {
-    const unsigned char* lam =
-        a.lbuf + (size_t)(2 * (a.lam_off[q] - a.lam_off[a.q0])) * kSlices * kATileBytes;
-    for (int i = 0; i < 2 * nk; ++i) {
-      const int part = i / nk, ks = ks0 + i % nk;
-      const uint32_t st = i % kStagesP;
-      if (!tc::mbar_wait(&h.empty[st], ((i / kStagesP) & 1) ^ 1, abort)) break;
-      unsigned char* dst = smem + st * kStageBytesP;
-      const unsigned char* asrc =
-          lam + (((size_t)(p * ntiles + t) * 2 + part) * nks + ks) * kSlices * kATileBytes;
-      const unsigned char* bsrc =
-          ws[part] + (((size_t)blockIdx.z * 2 + bpar[part]) * a.ngroups + g) * a.row_bytes +
-          (size_t)ks * kSlices * kBTileBytes;
-      tc::mbar_arrive_expect_tx(&h.full[st], kStageBytesP);
-      tc::bulk_g2s(dst, asrc, kSlices * kATileBytes, &h.full[st]);
-      tc::bulk_g2s(dst + kSlices * kATileBytes, bsrc, kSlices * kBTileBytes, &h.full[st]);
-      ++n_loaded;
-    }
-  } else if (tid == 160) {
-    const uint32_t idesc = tc::umma_idesc_bf16(kRows, kCols);
-    const uint32_t s_u = tc::smem_u32(smem);
-    for (int i = 0; i < 2 * nk; ++i) {
-      if (i == nk) {
-        tc::umma_commit(&h.tfull);
-        if (!tc::mbar_wait(&h.tempty, 0, abort)) break;
-        tc::tc_fence_after();
-      }
-      const uint32_t st = i % kStagesP;
-      if (!tc::mbar_wait(&h.full[st], (i / kStagesP) & 1, abort)) break;
-      tc::tc_fence_after();
-      const uint32_t abase = s_u + st * kStageBytesP;
-      const uint32_t bbase = abase + kSlices * kATileBytes;
-      const bool first = (i % nk) == 0;
-#pragma unroll
-      for (int lev = 0; lev <= 3; ++lev) {
-#pragma unroll
-        for (int aa = 0; aa <= lev; ++aa) {
-          const uint64_t ad = tc::umma_desc(abase + aa * kATileBytes, 128, 256);
-          const uint64_t bd = tc::umma_desc(bbase + (lev - aa) * kBTileBytes, 128, 256);
-          tc::umma_bf16(tmem + lev * kCols, ad, bd, idesc, (!first || aa > 0) ? 1u : 0u);
-        }
-      }
-      tc::umma_commit(&h.empty[st]);
-    }
-    tc::umma_commit(&h.tfull);
-  }
-  if (tid < 128) {
-    const int row = (warp << 5) + (tid & 31);
-    const int l = lt0 + p + 2 * row;
-    const bool rowok = l <= a.lmax;
-    const long long L1 = a.lmax + 1;
-    const long long re_row = (long long)m * L1 + l;
-    const long long im_row = (L1 - m) * L1 + (l - m);
-    double* alm = field == 0 ? a.almE : a.almB;
-    const float rh = s_rh[row], rl = s_rl[row];
-    const int re = s_re[row];
-    for (int part = 0; part < 2; ++part) {
-      bool ok = tc::mbar_wait(&h.tfull, part, abort);
-      ok = __all_sync(0xffffffffu, ok);
-      tc::tc_fence_after();
-      if (!ok) break;
-      const uint32_t lane_base = tmem + ((uint32_t)(warp << 5) << 16);
-      for (int c0 = 0; c0 < kCols; c0 += 16) {
-        uint32_t v0[16], v1[16], v2[16], v3[16];
-        tc::tmem_ld16(lane_base + 0 * kCols + c0, v0);
-        tc::tmem_ld16(lane_base + 1 * kCols + c0, v1);
-        tc::tmem_ld16(lane_base + 2 * kCols + c0, v2);
-        tc::tmem_ld16(lane_base + 3 * kCols + c0, v3);
-        tc::tmem_wait_ld();
-        const int comp = c0 >> 6;
-        // part 0: (Re, Im) -> (Re, Im).  part 1 (factor +i for E, -i for B):
-        //   E: Re <- -Im, Im <- +Re;   B: Re <- +Im, Im <- -Re
-        int tgt = comp;
-        double sgn = 1.0;
-        if (part == 1) {
-          tgt = 1 - comp;
-          sgn = (field == 0) == (comp == 1) ? -1.0 : 1.0;
-        }
-        if (!rowok || (tgt == 1 && m == 0)) continue;
-        const long long rowidx = tgt == 0 ? re_row : im_row;
-#pragma unroll
-        for (int j = 0; j < 16; ++j) {
-          const int c = c0 + j;
-          const int k = g * kGroupMaps + (c & 63);
-          if (k < a.kc) {
-            const double u = levels_scaled(v0[j], v1[j], v2[j], v3[j], rh, rl, re + s_ce[part][c]);
-            const double v = sgn < 0.0 ? -u : u;
-            double* dst = alm + rowidx * a.ld + a.k0 + k;
-            if (a.nkc_glob > 1) atomicAdd(dst, v);
-            else if (part == 0 && !a.accumulate) *dst = v;
-            else *dst += v;
+  if (tid == kEpiThreads) {
+    // producer: per part, the lambda1 k-steps (B = the field's own map) then the lambda2
+    // k-steps (B = the other map, opposite parity)
+    uint32_t i = 0;
+    bool ok = true;
+    for (int u = blockIdx.x; u < a.nunits && ok && !*abort; u += gridDim.x) {
+      const GemmPUnit w = gemm_pol_unit(a, u);
+      if (w.nks == 0) continue;
+      const unsigned char* lam =
+          a.lbuf + (size_t)(2 * (a.lam_off[a.q0 + w.qi] - a.lam_off[a.q0])) * kSlices * kATileBytes;
+      const unsigned char* ws[2] = {w.field == 0 ? a.WSQ : a.WSU, w.field == 0 ? a.WSU : a.WSQ};
+      const int bpar[2] = {w.p, 1 - w.p};
+      for (int ks0 = 0; ks0 < w.nks && ok; ks0 += kPartStepsP) {
+        const int nk = min(w.nks - ks0, kPartStepsP);
+        for (int part = 0; part < 2 && ok; ++part) {
+          for (int k = 0; k < nk; ++k, ++i) {
+            const int ks = ks0 + k;
+            const uint32_t st = i % kStagesP;
+            if (!tc::mbar_wait(&h.empty[st], ((i / kStagesP) & 1) ^ 1, abort)) {
+              ok = false;
+              break;
+            }
+            unsigned char* dst = smem + st * kStageBytesP;
+            const unsigned char* asrc =
+                lam + (((size_t)(w.p * w.ntiles + w.t) * 2 + part) * w.nks + ks) * kSlices *
+                          kATileBytes;
+            const unsigned char* bsrc =
+                ws[part] + (((size_t)w.qi * 2 + bpar[part]) * a.ngroups + w.g) * a.row_bytes +
+                (size_t)ks * kSlices * kBTileBytes;
+            tc::mbar_arrive_expect_tx(&h.full[st], kStageBytesP);
+            tc::bulk_g2s(dst, asrc, kSlices * kATileBytes, &h.full[st]);
+            tc::bulk_g2s(dst + kSlices * kATileBytes, bsrc, kSlices * kBTileBytes, &h.full[st]);
+            ++n_loaded;
           }
         }
       }
-      tc::tc_fence_before();
-      if (part == 0) tc::mbar_arrive(&h.tempty);
+    }
+  } else if (tid == kEpiThreads + 32) {
+    // UMMA issuer: one accumulation pass per (part of k-steps, lambda1 | lambda2)
+    const uint32_t idesc = tc::umma_idesc_bf16(kRows, kCols);
+    const uint32_t s_u = tc::smem_u32(smem);
+    uint32_t i = 0, np = 0;
+    bool ok = true;
+    for (int u = blockIdx.x; u < a.nunits && ok && !*abort; u += gridDim.x) {
+      const GemmPUnit w = gemm_pol_unit(a, u);
+      for (int ks0 = 0; ks0 < w.nks && ok; ks0 += kPartStepsP) {
+        const int nk = min(w.nks - ks0, kPartStepsP);
+        for (int part = 0; part < 2 && ok; ++part, ++np) {
+          if (np > 0 && !tc::mbar_wait(&h.tempty, (np - 1) & 1, abort)) {
+            ok = false;
+            break;
+          }
+          tc::tc_fence_after();
+          for (int k = 0; k < nk; ++k, ++i) {
+            const uint32_t st = i % kStagesP;
+            if (!tc::mbar_wait(&h.full[st], (i / kStagesP) & 1, abort)) {
+              ok = false;
+              break;
+            }
+            tc::tc_fence_after();
+            const uint32_t abase = s_u + st * kStageBytesP;
+            const uint32_t bbase = abase + kSlices * kATileBytes;
+#pragma unroll
+            for (int lev = 0; lev <= 3; ++lev) {
+#pragma unroll
+              for (int aa = 0; aa <= lev; ++aa) {
+                const uint64_t ad = tc::umma_desc(abase + aa * kATileBytes, 128, 256);
+                const uint64_t bd = tc::umma_desc(bbase + (lev - aa) * kBTileBytes, 128, 256);
+                tc::umma_bf16(tmem + lev * kCols, ad, bd, idesc, (k > 0 || aa > 0) ? 1u : 0u);
+              }
+            }
+            tc::umma_commit(&h.empty[st]);
+          }
+          if (ok) tc::umma_commit(&h.tfull);
+        }
+      }
+    }
+  } else if (tid < kEpiThreads) {
+    // epilogue (warps 0-7), row = TMEM lane (warp % 4: lane quarter, warp / 4: half of the
+    // columns).  No early exit: the epilogue threads must meet at every named barrier, so
+    // after an expired wait (abort) the remaining passes are walked idle.
+    const int row = ((warp & 3) << 5) + (tid & 31);
+    const int cbeg = (warp >> 2) * (kCols / 2);   // this warp's half of the columns
+    const long long L1 = a.lmax + 1;
+    const uint32_t lane_base = tmem + ((uint32_t)((warp & 3) << 5) << 16);
+    uint32_t np = 0;
+    for (int u = blockIdx.x; u < a.nunits; u += gridDim.x) {
+      const GemmPUnit w = gemm_pol_unit(a, u);
+      if (w.nks == 0) continue;
+      {
+        const int* eb[2] = {w.field == 0 ? a.EBQ : a.EBU, w.field == 0 ? a.EBU : a.EBQ};
+        const int bpar[2] = {w.p, 1 - w.p};
+        int e[2] = {0, 0};
+        if (tid < kCols)
+          for (int part = 0; part < 2; ++part)
+            e[part] =
+                eb[part][(((long long)w.qi * 2 + bpar[part]) * a.ngroups + w.g) * kCols + tid];
+        asm volatile("bar.sync 1, %0;" ::"n"(kEpiThreads) : "memory");
+        if (tid < kCols)
+          for (int part = 0; part < 2; ++part)
+            s_ce[part][tid] = (e[part] == kEmptyExp) ? kEmptyExp : e[part] - 12;
+        asm volatile("bar.sync 1, %0;" ::"n"(kEpiThreads) : "memory");
+      }
+      const int l = w.lt0 + w.p + 2 * row;
+      const bool rowok = l <= a.lmax;
+      float rh = 0.f, rl = 0.f;
+      int re = 0;
+      if (rowok) {
+        const FshtLamRow rw = a.tab[tri_off(w.m, a.lmax) + (l - w.m)];
+        factor_pair(-rw.dm * a.pa, rh, rl);
+        re = rw.erow + rw.dx;
+      }
+      const long long re_row = (long long)w.m * L1 + l;
+      const long long im_row = (L1 - w.m) * L1 + (l - w.m);
+      double* alm = w.field == 0 ? a.almE : a.almB;
+      for (int ks0 = 0; ks0 < w.nks; ks0 += kPartStepsP) {
+        for (int part = 0; part < 2; ++part) {
+          bool ok = tc::mbar_wait(&h.tfull, np & 1, abort);
+          ok = __all_sync(0xffffffffu, ok);
+          ++np;
+          if (!ok) continue;
+          tc::tc_fence_after();
+          const bool add = ks0 > 0 || part > 0 || a.accumulate;
+          for (int c0 = cbeg; c0 < cbeg + kCols / 2; c0 += 16) {
+            uint32_t v0[16], v1[16], v2[16], v3[16];
+            tc::tmem_ld16(lane_base + 0 * kCols + c0, v0);
+            tc::tmem_ld16(lane_base + 1 * kCols + c0, v1);
+            tc::tmem_ld16(lane_base + 2 * kCols + c0, v2);
+            tc::tmem_ld16(lane_base + 3 * kCols + c0, v3);
+            tc::tmem_wait_ld();
+            if (c0 == cbeg + kCols / 2 - 16) {
+              tc::tc_fence_before();
+              tc::mbar_arrive(&h.tempty);
+            }
+            const int comp = c0 >> 6;
+            // part 0: (Re, Im) -> (Re, Im).  part 1 (factor +i for E, -i for B):
+            //   E: Re <- -Im, Im <- +Re;   B: Re <- +Im, Im <- -Re
+            int tgt = comp;
+            bool neg = false;
+            if (part == 1) {
+              tgt = 1 - comp;
+              neg = (w.field == 0) == (comp == 1);
+            }
+            if (!rowok || (tgt == 1 && w.m == 0)) continue;
+            const long long rowidx = tgt == 0 ? re_row : im_row;
+#pragma unroll
+            for (int j = 0; j < 16; ++j) {
+              const int c = c0 + j;
+              const int k = w.g * kGroupMaps + (c & 63);
+              if (k < a.kc) {
+                const double uu =
+                    levels_scaled(v0[j], v1[j], v2[j], v3[j], rh, rl, re + s_ce[part][c]);
+                const double v = neg ? -uu : uu;
+                double* dst = alm + rowidx * a.ld + a.k0 + k;
+                // adds as fire-and-forget reductions; one thread owns each element
+                if (add) atomicAdd(dst, v);
+                else *dst = v;
+              }
+            }
+          }
+        }
+      }
     }
   }
-  if (tid == 160) {
+  if (tid == kEpiThreads + 32) {
     tc::umma_commit(&h.fin);
     for (uint32_t it = 0; it < tc::kWaitLimit; ++it)
       if (tc::mbar_try_wait(&h.fin, 0)) break;
   }
-  if (tid == 128) {
+  if (tid == kEpiThreads) {
     for (uint32_t d = 0; d < (uint32_t)kStagesP && d < n_loaded; ++d) {
       const uint32_t i = n_loaded - 1 - d;
       for (uint32_t it = 0; it < tc::kWaitLimit; ++it)
@@ -820,12 +867,11 @@ int fsht_launch_split_gemm_pol(fsht_plan* p, int w, const unsigned char* WSQ, co
   a.lmax = p->lmax;
   a.nnorth = p->nnorth;
   a.ngroups = (kc + kGroupMaps - 1) / kGroupMaps;
-  a.nkc_glob = (p->nnorth + kKChunk - 1) / kKChunk;
   a.q0 = wv[0];
   a.ntmax = wv[2];
-  a.nkcmax = wv[3];
   a.accumulate = accumulate;
   a.which = which;
+  a.nunits = a.ngroups * 4 * a.ntmax * (wv[1] - wv[0]);
   a.row_bytes = ws_row_bytes(p->lmax, p->nnorth);
   a.ring_i0 = p->d_ring_i0;
   a.lam_off = p->d_lam_off;
@@ -845,7 +891,11 @@ int fsht_launch_split_gemm_pol(fsht_plan* p, int w, const unsigned char* WSQ, co
   const size_t sm = (size_t)kStagesP * kStageBytesP;
   FSHT_CUDA_TRY(cudaFuncSetAttribute(k_split_gemm_pol,
                                      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-  k_split_gemm_pol<<<dim3(a.ngroups, 4 * a.ntmax * a.nkcmax, wv[1] - wv[0]), kThreads, sm, s>>>(a);
+  int dev = 0, nsm = 0;
+  FSHT_CUDA_TRY(cudaGetDevice(&dev));
+  FSHT_CUDA_TRY(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+  const int grid = a.nunits < nsm ? a.nunits : nsm;
+  if (grid > 0) k_split_gemm_pol<<<grid, kThreadsG, sm, s>>>(a);
   FSHT_LAUNCH_CHECK();
   return FSHT_OK;
 }

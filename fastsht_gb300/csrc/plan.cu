@@ -437,6 +437,26 @@ int fsht_plan_sync(fsht_plan* p) {
   return fsht_plan_check(p);
 }
 
+int fsht_host_alloc(size_t bytes, void** ptr) {
+  if (!ptr) {
+    fsht_set_error("host_alloc: null output pointer");
+    return FSHT_EINVAL;
+  }
+  *ptr = nullptr;
+  cudaError_t e = cudaHostAlloc(ptr, bytes > 0 ? bytes : 1, cudaHostAllocPortable);
+  if (e != cudaSuccess) {
+    fsht_set_error("cudaHostAlloc(%zu): %s", bytes, cudaGetErrorString(e));
+    *ptr = nullptr;
+    return e == cudaErrorMemoryAllocation ? FSHT_ENOMEM : FSHT_ECUDA;
+  }
+  return FSHT_OK;
+}
+
+int fsht_host_free(void* ptr) {
+  if (ptr) FSHT_CUDA_TRY(cudaFreeHost(ptr));
+  return FSHT_OK;
+}
+
 int fsht_plan_check(fsht_plan* p) {
   FSHT_TRY(check_plan(p));
   int err = 0;
@@ -572,7 +592,8 @@ static int xfer_orders_done(fsht_plan* p, HostXfer& x, const double* dalm, int n
 // (before the FFT).  hx: copy each wave's finished alm columns to the host.
 static int split_analysis(fsht_plan* p, const double2* W, double* alm, int nmaps, int c0, int kc,
                           int accumulate, bool started = false, HostXfer* hx = nullptr) {
-  if (!accumulate) FSHT_TRY(fsht_split_clear_alm(p, alm, nmaps, c0, kc, p->stream));
+  // every alm element of the chunk is written by exactly one unit of the contraction (its
+  // first ring part stores, later parts add), so alm needs no clearing
   if (!started) FSHT_TRY(lam_start(p, fsht_launch_split_lambda));
   for (int w = 0; w < p->nwaves; ++w) {
     {
@@ -798,10 +819,8 @@ static int pol_analysis(fsht_plan* p, const double2* WQ, const double2* WU, doub
   unsigned char* wsu = p->d_ws + fsht_split_ws_bytes(p, kc);
   int* ebq = p->d_eb;
   int* ebu = p->d_eb + fsht_split_eb_bytes(p, kc) / sizeof(int);
-  if (!accumulate) {
-    if (which & 1) FSHT_TRY(fsht_split_clear_alm(p, almE, nmaps, c0, kc, p->stream));
-    if (which & 2) FSHT_TRY(fsht_split_clear_alm(p, almB, nmaps, c0, kc, p->stream));
-  }
+  // every alm element of the chunk is written by one unit of the contraction (its first pass
+  // stores, later passes add), so alm needs no clearing
   if (!started) FSHT_TRY(lam_start(p, fsht_launch_split_lambda_pol));
   for (int w = 0; w < p->nwaves; ++w) {
     {

@@ -24,6 +24,10 @@ constexpr uint32_t kBTileBytes = kCols * kKStep * 2;    // 4 KB per (k-step, dig
 constexpr int kSynthPlanes = 7;
 constexpr uint32_t kSynthBBytes = kSynthPlanes * kBTileBytes;   // 28 KB per l-step
 constexpr int kThreads = 192;
+// persistent analysis contractions: eight epilogue warps (two per TMEM lane quarter, one per
+// half of the columns), then the copy thread's warp and the UMMA thread's warp
+constexpr int kEpiThreads = 256;
+constexpr int kThreadsG = kEpiThreads + 64;
 constexpr int kEmptyExp = -4000;    // column exponent of an all-zero column
 
 struct RecConst {

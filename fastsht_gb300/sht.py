@@ -14,6 +14,7 @@ the same logical shape and Fortran strides (results stay on the device).
 from __future__ import annotations
 
 import ctypes as C
+import weakref
 
 import numpy as np
 import torch
@@ -32,14 +33,24 @@ def _fortran_view_ok(t: torch.Tensor) -> bool:
     return t.permute(*reversed(range(t.dim()))).is_contiguous()
 
 
+def pinned_empty(shape, order="F"):
+    """float64 NumPy array in page-locked host memory (fsht_host_alloc), freed with the array;
+    host buffers of this kind let SHT.t2alm overlap its copies with the transform."""
+    n = int(np.prod(shape)) if len(shape) else 1
+    ptr = C.c_void_p()
+    try:
+        _lib.call("fsht_host_alloc", C.c_size_t(8 * max(n, 1)), C.byref(ptr))
+    except Exception:
+        return np.empty(shape, dtype=np.float64, order=order)
+    buf = (C.c_double * max(n, 1)).from_address(ptr.value)
+    arr = np.frombuffer(buf, dtype=np.float64, count=n).reshape(shape, order=order)
+    weakref.finalize(buf, _lib.load().fsht_host_free, C.c_void_p(ptr.value))
+    return arr
+
+
 def _pinned_empty_fortran(shape, dtype=torch.float64):
     """Pinned host array with Fortran layout, returned as a NumPy array."""
-    rev = tuple(reversed(shape))
-    try:
-        t = torch.empty(rev, dtype=dtype, pin_memory=True)
-    except RuntimeError:
-        t = torch.empty(rev, dtype=dtype)
-    return t.numpy().T
+    return pinned_empty(shape, order="F")
 
 
 class SHT:

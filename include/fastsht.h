@@ -251,6 +251,12 @@ int fsht_plan_check(fsht_plan* plan);
  * reference. */
 int fsht_selftest_wait_timeout(fsht_plan* plan);
 
+/* Page-locked host memory (cudaHostAlloc, portable to every device) for host buffers of
+ * fsht_t2alm_host and the SHT class's NumPy outputs, so the copies run asynchronously at the
+ * host link's rate.  No counterpart in the reference. */
+int fsht_host_alloc(size_t bytes, void** ptr);
+int fsht_host_free(void* ptr);
+
 /* Copies the calling thread's last error message into buf (NUL-terminated);
  * returns its full length. */
 int fsht_last_error(char* buf, size_t len);

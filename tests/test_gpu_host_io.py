@@ -63,3 +63,18 @@ def test_host_path_split_nside_1024():
     got = sht.t2alm(maps)
     want = sht.t2alm(torch.from_numpy(maps.T.copy()).cuda().T).cpu().numpy()
     assert np.array_equal(got, want)
+
+
+def test_pinned_empty_buffers():
+    """Library-allocated page-locked buffers (fsht_host_alloc) as t2alm input and output."""
+    from fastsht_gb300 import SHT, pinned_empty
+    ns, lmax, nsim = 32, 95, 5
+    sht = SHT(ns, lmax, nsim, precision="split")
+    maps = pinned_empty((12 * ns * ns, nsim))
+    maps[...] = _maps(ns, nsim, 4)
+    out = pinned_empty((nsim, lmax + 1, lmax + 1))
+    assert out.flags.f_contiguous and maps.flags.f_contiguous
+    assert sht.t2alm(maps, alms_in=out) == 0
+    want = sht.t2alm(torch.from_numpy(np.asarray(maps).T.copy()).cuda().T).cpu().numpy()
+    assert np.array_equal(out, want)
+    del maps, out                                  # freed through fsht_host_free
