@@ -546,6 +546,14 @@ def ours(args, rank, world, local):
             "roofline_fft": roof_fft, "roofline_contraction": roof_ana,
             "fp64_peak_tflops": peak64.value, "fp32_peak_tflops": peak32.value}
 
+    # -------- e2e through the public API with host (pinned) buffers (first, while the
+    # device holds only this form's buffers)
+    if not args.no_e2e:
+        ke = args.e2e_maps or nmaps
+        sh = sht if ke == nmaps else SHT(nside, lmax, ke, device=local, precision=args.precision)
+        line["e2e"] = e2e(sh, maps, ke, args, world)
+        sh.release_staging()
+        torch.cuda.empty_cache()
     # -------- the plain FP64 path on the same maps (precision reference + speed ratio)
     if args.precision == "split" and not args.no_fp64:
         ms64, out64, pk64, kms64, _, _ = timed_steps(lib, sht64, maps, 1, 1, world, dist, dev,
@@ -609,11 +617,6 @@ def ours(args, rank, world, local):
         s64r.close()
         del out_r, out64r
         torch.cuda.empty_cache()
-    # -------- e2e through the public API with host (pinned) buffers
-    if not args.no_e2e:
-        ke = args.e2e_maps or nmaps
-        sh = sht if ke == nmaps else SHT(nside, lmax, ke, device=local, precision=args.precision)
-        line["e2e"] = e2e(sh, maps, ke, args, world)
     # -------- CPU baseline and parity sample (rank 0, N = 1)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         k = min(args.cpu_maps, nmaps)

@@ -251,6 +251,22 @@ __device__ __forceinline__ double dd_to_double(float h, float l, int sh) {
   return dd_float_to_double(h, sh) + dd_float_to_double(l, sh);
 }
 
+// dd_float_to_double for |sh| <= 896, where no exponent can leave the FP64 range: the double's
+// high word is the float's bits shifted right by three with the exponent rebiased by one
+// addition (e896 = (896 + sh) << 20) and the sign put back; zero, subnormal and non-finite f
+// take the checked path.
+__device__ __forceinline__ double dd_float_to_double_near(float f, int sh, unsigned e896) {
+  const unsigned b = __float_as_uint(f);
+  if ((((b >> 23) & 0xffu) - 1u) >= 254u) return dd_float_to_double(f, sh);
+  const unsigned hw = (((b >> 3) & 0x0fffffffu) + e896) | (b & 0x80000000u);
+  return __hiloint2double((int)hw, (int)(b << 29));
+}
+
+// dd_to_double for |sh| <= 896 (see dd_float_to_double_near)
+__device__ __forceinline__ double dd_to_double_near(float h, float l, int sh, unsigned e896) {
+  return dd_float_to_double_near(h, sh, e896) + dd_float_to_double_near(l, sh, e896);
+}
+
 // the largest biased FP64 exponent field of x (0 for zero / subnormal)
 __device__ __forceinline__ int dd_exp_field(double x) {
   return (int)(((unsigned)(__double_as_longlong(x) >> 32) >> 20) & 0x7ff);

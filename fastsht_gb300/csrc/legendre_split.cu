@@ -690,7 +690,7 @@ __global__ void __launch_bounds__(128) k_slice_alm(SliceAArgs a) {
 // TMEM accumulators (E first, written as G_N = G_S = E; then O, added to G_N and subtracted
 // from G_S by the same threads).  Roles as in k_split_gemm.
 struct SynthArgs {
-  int lmax, nnorth, ngroups, nkcl_glob, q0, nkclmax, eag;
+  int lmax, nnorth, ngroups, q0, nrbmax, eag, nunits;
   size_t row_bytes;
   const int* ring_i0;
   const long long* lam_offT;
@@ -704,6 +704,7 @@ struct SynthArgs {
 
 constexpr int kStagesS = 4;
 constexpr uint32_t kStageBytesS = kSlices * kATileBytes + kSynthBBytes;   // 44 KB
+constexpr int kPartStepsS = kKChunk / kKStep;
 
 struct __align__(8) SynthSmemHdr {
   uint64_t full[kStagesS], empty[kStagesS], tfull, tempty, fin;
@@ -711,24 +712,36 @@ struct __align__(8) SynthSmemHdr {
   int abort;
 };
 
-__global__ void __launch_bounds__(kThreads, 1) k_split_synth(SynthArgs a) {
+// One work unit (q, 128-ring block, 64-map group), the group fastest; nkl = 0: nothing to do.
+struct SynthUnit {
+  int g, rb, qi, m, i0, K, nrb, nkl;
+};
+
+__device__ __forceinline__ SynthUnit synth_unit(const SynthArgs& a, int u) {
+  SynthUnit w;
+  w.g = u % a.ngroups;
+  int r = u / a.ngroups;
+  w.rb = r % a.nrbmax;
+  w.qi = r / a.nrbmax;
+  w.m = m_of_q(a.q0 + w.qi, a.lmax);
+  w.i0 = a.ring_i0[w.m];
+  w.K = a.nnorth - w.i0;
+  w.nrb = (w.K + kSCRings - 1) / kSCRings;
+  w.nkl = w.rb < w.nrb ? ((a.lmax - w.m) / 2 + 1 + kKStep - 1) / kKStep : 0;
+  return w;
+}
+
+// Persistent like k_split_gemm: one CTA per SM walks the units; per part of <= 64 l-steps
+// (1024 l keep levels 0 and 1 exact) the even-l pass then the odd-l pass run through the same
+// TMEM accumulators.  The first even pass of a unit writes G_N = G_S = E, every later pass adds
+// (+E, or +O to G_N and -O to G_S) as fire-and-forget reductions from the thread that owns the
+// element, so W needs no clearing and the result is deterministic.  Warps 0-7: epilogue (two
+// per TMEM lane quarter, one per half of the columns), warp 8 lane 0: copies, warp 9 lane 0:
+// UMMAs (13 per l-step: levels 0-3 and the level-4 fold).
+__global__ void __launch_bounds__(kThreadsG, 1) k_split_synth(SynthArgs a) {
   extern __shared__ __align__(1024) unsigned char smem[];
   __shared__ SynthSmemHdr h;
-  __shared__ int s_ce[2][kCols];       // column exponents EAG + eb - 12
-
-  const int g = blockIdx.x;
-  const int rb = blockIdx.y / a.nkclmax;
-  const int kcl = blockIdx.y % a.nkclmax;
-  const int q = a.q0 + blockIdx.z;
-  const int m = m_of_q(q, a.lmax);
-  const int i0 = a.ring_i0[m];
-  const int K = a.nnorth - i0;
-  const int nrb = (K + kSCRings - 1) / kSCRings;
-  const int nkl = ((a.lmax - m) / 2 + 1 + kKStep - 1) / kKStep;
-  const int kl0 = kcl * (kKChunk / kKStep);
-  const int kl1 = min(nkl, kl0 + kKChunk / kKStep);
-  if (rb >= nrb || kl0 >= kl1) return;            // uniform: before any barrier or TMEM
-  const int nk = kl1 - kl0;
+  __shared__ int s_ce[2][kCols];       // column exponents EAG + eb - 12 per parity
 
   const int tid = threadIdx.x;
   const int warp = tid >> 5;
@@ -739,16 +752,10 @@ __global__ void __launch_bounds__(kThreads, 1) k_split_synth(SynthArgs a) {
       tc::mbar_init(&h.empty[s], 1);
     }
     tc::mbar_init(&h.tfull, 1);
-    tc::mbar_init(&h.tempty, 128);
+    tc::mbar_init(&h.tempty, kEpiThreads);
     tc::mbar_init(&h.fin, 1);
     h.abort = 0;
     tc::mbar_fence_init();
-  }
-  if (tid < kCols) {
-    for (int pp = 0; pp < 2; ++pp) {
-      const int eb = a.EB[(((long long)blockIdx.z * 2 + pp) * a.ngroups + g) * kCols + tid];
-      s_ce[pp][tid] = (eb == kEmptyExp) ? kEmptyExp : a.eag + eb - 12;
-    }
   }
   if (warp == 0) tc::tmem_alloc(&h.tmem, 512);
   tc::tc_fence_before();
@@ -757,111 +764,158 @@ __global__ void __launch_bounds__(kThreads, 1) k_split_synth(SynthArgs a) {
   const uint32_t tmem = h.tmem;
 
   uint32_t n_loaded = 0;
-  if (tid == 128) {
-    const unsigned char* abase =
-        a.lbuf + (size_t)(a.lam_offT[q] - a.lam_offT[a.q0]) * kSlices * kATileBytes;
-    for (int i = 0; i < 2 * nk; ++i) {
-      const int par = i / nk, kk = kl0 + i % nk;
-      const uint32_t st = i % kStagesS;
-      if (!tc::mbar_wait(&h.empty[st], ((i / kStagesS) & 1) ^ 1, abort)) break;
-      unsigned char* dst = smem + st * kStageBytesS;
-      const unsigned char* asrc =
-          abase + ((size_t)(par * nrb + rb) * nkl + kk) * kSlices * kATileBytes;
-      const unsigned char* bsrc = a.WS + (((size_t)blockIdx.z * 2 + par) * a.ngroups + g) * a.row_bytes +
-                                  (size_t)kk * kSynthBBytes;
-      tc::mbar_arrive_expect_tx(&h.full[st], kStageBytesS);
-      tc::bulk_g2s(dst, asrc, kSlices * kATileBytes, &h.full[st]);
-      tc::bulk_g2s(dst + kSlices * kATileBytes, bsrc, kSynthBBytes, &h.full[st]);
-      ++n_loaded;
-    }
-  } else if (tid == 160) {
-    const uint32_t idesc = tc::umma_idesc_bf16(kRows, kCols);
-    const uint32_t s_u = tc::smem_u32(smem);
-    for (int i = 0; i < 2 * nk; ++i) {
-      if (i == nk) {
-        // E is complete: hand TMEM to the epilogue, take it back for O
-        tc::umma_commit(&h.tfull);
-        if (!tc::mbar_wait(&h.tempty, 0, abort)) break;
-        tc::tc_fence_after();
-      }
-      const uint32_t st = i % kStagesS;
-      if (!tc::mbar_wait(&h.full[st], (i / kStagesS) & 1, abort)) break;
-      tc::tc_fence_after();
-      const uint32_t abase = s_u + st * kStageBytesS;
-      const uint32_t bbase = abase + kSlices * kATileBytes;
-      const bool first = (i % nk) == 0;
-#pragma unroll
-      for (int lev = 0; lev <= 3; ++lev) {
-#pragma unroll
-        for (int aa = 0; aa <= lev; ++aa) {
-          const uint64_t ad = tc::umma_desc(abase + aa * kATileBytes, 128, 256);
-          const uint64_t bd = tc::umma_desc(bbase + (lev - aa) * kBTileBytes, 128, 256);
-          tc::umma_bf16(tmem + lev * kCols, ad, bd, idesc, (!first || aa > 0) ? 1u : 0u);
+  if (tid == kEpiThreads) {
+    uint32_t i = 0;
+    bool ok = true;
+    for (int u = blockIdx.x; u < a.nunits && ok && !*abort; u += gridDim.x) {
+      const SynthUnit w = synth_unit(a, u);
+      if (w.nkl == 0) continue;
+      const unsigned char* abase =
+          a.lbuf + (size_t)(a.lam_offT[a.q0 + w.qi] - a.lam_offT[a.q0]) * kSlices * kATileBytes;
+      for (int kl0 = 0; kl0 < w.nkl && ok; kl0 += kPartStepsS) {
+        const int nk = min(w.nkl - kl0, kPartStepsS);
+        for (int par = 0; par < 2 && ok; ++par) {
+          for (int kk = kl0; kk < kl0 + nk; ++kk, ++i) {
+            const uint32_t st = i % kStagesS;
+            if (!tc::mbar_wait(&h.empty[st], ((i / kStagesS) & 1) ^ 1, abort)) {
+              ok = false;
+              break;
+            }
+            unsigned char* dst = smem + st * kStageBytesS;
+            const unsigned char* asrc =
+                abase + ((size_t)(par * w.nrb + w.rb) * w.nkl + kk) * kSlices * kATileBytes;
+            const unsigned char* bsrc =
+                a.WS + (((size_t)w.qi * 2 + par) * a.ngroups + w.g) * a.row_bytes +
+                (size_t)kk * kSynthBBytes;
+            tc::mbar_arrive_expect_tx(&h.full[st], kStageBytesS);
+            tc::bulk_g2s(dst, asrc, kSlices * kATileBytes, &h.full[st]);
+            tc::bulk_g2s(dst + kSlices * kATileBytes, bsrc, kSynthBBytes, &h.full[st]);
+            ++n_loaded;
+          }
         }
       }
-      // level 4 (a1 b3, a2 b2, a3 b1) into the level-3 accumulator via the 2^-8 planes:
-      // with lambda against one scale its digits are often small, and dropping level 4
-      // would cost ~2e-7
-#pragma unroll
-      for (int aa = 1; aa <= 3; ++aa) {
-        const uint64_t ad = tc::umma_desc(abase + aa * kATileBytes, 128, 256);
-        const uint64_t bd = tc::umma_desc(bbase + (kSlices - 1 + (4 - aa)) * kBTileBytes, 128, 256);
-        tc::umma_bf16(tmem + 3 * kCols, ad, bd, idesc, 1u);
-      }
-      tc::umma_commit(&h.empty[st]);
     }
-    tc::umma_commit(&h.tfull);
-  }
-  if (tid < 128) {
-    const int row = (warp << 5) + (tid & 31);
-    const int rr = rb * kSCRings + row;
-    const bool rowok = rr < K;
-    const int i = i0 + rr;
-    for (int par = 0; par < 2; ++par) {
-      bool ok = tc::mbar_wait(&h.tfull, par, abort);
-      ok = __all_sync(0xffffffffu, ok);
-      tc::tc_fence_after();
-      if (!ok) break;
-      const uint32_t lane_base = tmem + ((uint32_t)(warp << 5) << 16);
-      for (int c0 = 0; c0 < kCols; c0 += 16) {
-        uint32_t v0[16], v1[16], v2[16], v3[16];
-        tc::tmem_ld16(lane_base + 0 * kCols + c0, v0);
-        tc::tmem_ld16(lane_base + 1 * kCols + c0, v1);
-        tc::tmem_ld16(lane_base + 2 * kCols + c0, v2);
-        tc::tmem_ld16(lane_base + 3 * kCols + c0, v3);
-        tc::tmem_wait_ld();
-        const int comp = c0 >> 6;
+  } else if (tid == kEpiThreads + 32) {
+    const uint32_t idesc = tc::umma_idesc_bf16(kRows, kCols);
+    const uint32_t s_u = tc::smem_u32(smem);
+    uint32_t i = 0, np = 0;
+    bool ok = true;
+    for (int u = blockIdx.x; u < a.nunits && ok && !*abort; u += gridDim.x) {
+      const SynthUnit w = synth_unit(a, u);
+      for (int kl0 = 0; kl0 < w.nkl && ok; kl0 += kPartStepsS) {
+        const int nk = min(w.nkl - kl0, kPartStepsS);
+        for (int par = 0; par < 2 && ok; ++par, ++np) {
+          if (np > 0 && !tc::mbar_wait(&h.tempty, (np - 1) & 1, abort)) {
+            ok = false;
+            break;
+          }
+          tc::tc_fence_after();
+          for (int k = 0; k < nk; ++k, ++i) {
+            const uint32_t st = i % kStagesS;
+            if (!tc::mbar_wait(&h.full[st], (i / kStagesS) & 1, abort)) {
+              ok = false;
+              break;
+            }
+            tc::tc_fence_after();
+            const uint32_t abase = s_u + st * kStageBytesS;
+            const uint32_t bbase = abase + kSlices * kATileBytes;
 #pragma unroll
-        for (int j = 0; j < 16; ++j) {
-          const int c = c0 + j;
-          const int k = g * kGroupMaps + (c & 63);
-          if (rowok && k < a.kc) {
-            const double v = levels_scaled(v0[j], v1[j], v2[j], v3[j], 1.f, 0.f, s_ce[par][c]);
-            double* gn = a.W + ((((long long)m * a.nnorth + i) * a.kc + k) * 2) * 2 + comp;
-            double* gs = gn + 2;
-            if (a.nkcl_glob > 1) {
-              atomicAdd(gn, v);
-              atomicAdd(gs, par ? -v : v);
-            } else if (par == 0) {
-              *gn = v;
-              *gs = v;
-            } else {
-              *gn += v;
-              *gs -= v;
+            for (int lev = 0; lev <= 3; ++lev) {
+#pragma unroll
+              for (int aa = 0; aa <= lev; ++aa) {
+                const uint64_t ad = tc::umma_desc(abase + aa * kATileBytes, 128, 256);
+                const uint64_t bd = tc::umma_desc(bbase + (lev - aa) * kBTileBytes, 128, 256);
+                tc::umma_bf16(tmem + lev * kCols, ad, bd, idesc, (k > 0 || aa > 0) ? 1u : 0u);
+              }
+            }
+            // level 4 (a1 b3, a2 b2, a3 b1) into the level-3 accumulator via the 2^-8 planes:
+            // with lambda against one scale its digits are often small, and dropping level 4
+            // would cost ~2e-7
+#pragma unroll
+            for (int aa = 1; aa <= 3; ++aa) {
+              const uint64_t ad = tc::umma_desc(abase + aa * kATileBytes, 128, 256);
+              const uint64_t bd =
+                  tc::umma_desc(bbase + (kSlices - 1 + (4 - aa)) * kBTileBytes, 128, 256);
+              tc::umma_bf16(tmem + 3 * kCols, ad, bd, idesc, 1u);
+            }
+            tc::umma_commit(&h.empty[st]);
+          }
+          if (ok) tc::umma_commit(&h.tfull);
+        }
+      }
+    }
+  } else if (tid < kEpiThreads) {
+    // No early exit: the epilogue threads must meet at every named barrier.
+    const int row = ((warp & 3) << 5) + (tid & 31);
+    const int cbeg = (warp >> 2) * (kCols / 2);
+    const uint32_t lane_base = tmem + ((uint32_t)((warp & 3) << 5) << 16);
+    uint32_t np = 0;
+    for (int u = blockIdx.x; u < a.nunits; u += gridDim.x) {
+      const SynthUnit w = synth_unit(a, u);
+      if (w.nkl == 0) continue;
+      {
+        int e[2] = {0, 0};
+        if (tid < kCols)
+          for (int pp = 0; pp < 2; ++pp)
+            e[pp] = a.EB[(((long long)w.qi * 2 + pp) * a.ngroups + w.g) * kCols + tid];
+        asm volatile("bar.sync 1, %0;" ::"n"(kEpiThreads) : "memory");
+        if (tid < kCols)
+          for (int pp = 0; pp < 2; ++pp)
+            s_ce[pp][tid] = (e[pp] == kEmptyExp) ? kEmptyExp : a.eag + e[pp] - 12;
+        asm volatile("bar.sync 1, %0;" ::"n"(kEpiThreads) : "memory");
+      }
+      const int rr = w.rb * kSCRings + row;
+      const bool rowok = rr < w.K;
+      const int i = w.i0 + rr;
+      for (int kl0 = 0; kl0 < w.nkl; kl0 += kPartStepsS) {
+        for (int par = 0; par < 2; ++par) {
+          bool ok = tc::mbar_wait(&h.tfull, np & 1, abort);
+          ok = __all_sync(0xffffffffu, ok);
+          ++np;
+          if (!ok) continue;
+          tc::tc_fence_after();
+          const bool first = kl0 == 0 && par == 0;
+          for (int c0 = cbeg; c0 < cbeg + kCols / 2; c0 += 16) {
+            uint32_t v0[16], v1[16], v2[16], v3[16];
+            tc::tmem_ld16(lane_base + 0 * kCols + c0, v0);
+            tc::tmem_ld16(lane_base + 1 * kCols + c0, v1);
+            tc::tmem_ld16(lane_base + 2 * kCols + c0, v2);
+            tc::tmem_ld16(lane_base + 3 * kCols + c0, v3);
+            tc::tmem_wait_ld();
+            if (c0 == cbeg + kCols / 2 - 16) {
+              tc::tc_fence_before();
+              tc::mbar_arrive(&h.tempty);
+            }
+            const int comp = c0 >> 6;
+#pragma unroll
+            for (int j = 0; j < 16; ++j) {
+              const int c = c0 + j;
+              const int k = w.g * kGroupMaps + (c & 63);
+              if (rowok && k < a.kc) {
+                const double v =
+                    levels_scaled(v0[j], v1[j], v2[j], v3[j], 1.f, 0.f, s_ce[par][c]);
+                double* gn = a.W + ((((long long)w.m * a.nnorth + i) * a.kc + k) * 2) * 2 + comp;
+                double* gs = gn + 2;
+                if (first) {
+                  *gn = v;
+                  *gs = v;
+                } else {
+                  atomicAdd(gn, v);
+                  atomicAdd(gs, par ? -v : v);
+                }
+              }
             }
           }
         }
       }
-      tc::tc_fence_before();
-      if (par == 0) tc::mbar_arrive(&h.tempty);
     }
   }
-  if (tid == 160) {
+  if (tid == kEpiThreads + 32) {
     tc::umma_commit(&h.fin);
     for (uint32_t it = 0; it < tc::kWaitLimit; ++it)
       if (tc::mbar_try_wait(&h.fin, 0)) break;
   }
-  if (tid == 128) {
+  if (tid == kEpiThreads) {
     for (uint32_t d = 0; d < (uint32_t)kStagesS && d < n_loaded; ++d) {
       const uint32_t i = n_loaded - 1 - d;
       for (uint32_t it = 0; it < tc::kWaitLimit; ++it)
@@ -1101,10 +1155,10 @@ int fsht_launch_split_synth(fsht_plan* p, int w, const unsigned char* WS, const 
   a.nnorth = p->nnorth;
   a.ngroups = (kc + kGroupMaps - 1) / kGroupMaps;
   a.row_bytes = ws_row_bytes(p->lmax, p->nnorth);
-  a.nkcl_glob = ((p->lmax / 2 + 1 + kKStep - 1) / kKStep * kKStep + kKChunk - 1) / kKChunk;
   a.q0 = wv[0];
-  a.nkclmax = wv[6];
+  a.nrbmax = wv[4];
   a.eag = eag_of(p->lmax);
+  a.nunits = a.ngroups * a.nrbmax * (wv[1] - wv[0]);
   a.ring_i0 = p->d_ring_i0;
   a.lam_offT = p->d_lam_offT;
   a.lbuf = lbuf;
@@ -1116,7 +1170,11 @@ int fsht_launch_split_synth(fsht_plan* p, int w, const unsigned char* WS, const 
   const size_t sm = (size_t)kStagesS * kStageBytesS;
   FSHT_CUDA_TRY(
       cudaFuncSetAttribute(k_split_synth, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-  k_split_synth<<<dim3(a.ngroups, wv[4] * wv[6], wv[1] - wv[0]), kThreads, sm, s>>>(a);
+  int dev = 0, nsm = 0;
+  FSHT_CUDA_TRY(cudaGetDevice(&dev));
+  FSHT_CUDA_TRY(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+  const int grid = a.nunits < nsm ? a.nunits : nsm;
+  if (grid > 0) k_split_synth<<<grid, kThreadsG, sm, s>>>(a);
   FSHT_LAUNCH_CHECK();
   return FSHT_OK;
 }

@@ -619,7 +619,7 @@ static int split_analysis(fsht_plan* p, const double2* W, double* alm, int nmaps
 
 static int split_synthesis(fsht_plan* p, const double* alm, double2* W, int nmaps, int c0,
                            int kc) {
-  FSHT_TRY(fsht_split_clear_w(p, W, kc, p->stream));
+  // the first even-l pass of every unit stores G_N and G_S, later passes add: no clearing
   FSHT_TRY(lam_start(p, fsht_launch_split_lambdaT));
   for (int w = 0; w < p->nwaves; ++w) {
     {

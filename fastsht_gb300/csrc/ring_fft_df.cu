@@ -49,7 +49,17 @@ __device__ __forceinline__ cdd cdd_from_raw(double2 v, int sh) {
 }
 
 __device__ __forceinline__ double2 cdd_to_fp64(cdd v, int sh) {
+  if (sh >= -896 && sh <= 896) {   // uniform per (ring pair, map): the short conversion
+    const unsigned e896 = (unsigned)(896 + sh) << 20;
+    return make_double2(dd_to_double_near(v.h.x, v.l.x, sh, e896),
+                        dd_to_double_near(v.h.y, v.l.y, sh, e896));
+  }
   return make_double2(dd_to_double(v.h.x, v.l.x, sh), dd_to_double(v.h.y, v.l.y, sh));
+}
+
+__device__ __forceinline__ double dd_out(float h, float l, int sh) {
+  if (sh >= -896 && sh <= 896) return dd_to_double_near(h, l, sh, (unsigned)(896 + sh) << 20);
+  return dd_to_double(h, l, sh);
 }
 
 // Loads one ring pair (or one half-length ring) of map values into the FFT buffer's slots as
@@ -279,8 +289,8 @@ __global__ void __launch_bounds__(1024, 1) k_ring_fft_inv_df(InvDfArgs a) {
         double* x = a.maps + (long long)k * a.map_stride + (side ? off_s : off_n);
         for (int j = tid; j < nd; j += nt) {
           const cdd z = buf[S(dft_bin(rf, j))];   // conj(z): x_{2j} = Re, x_{2j+1} = -Im
-          x[2 * j] = dd_to_double(z.h.x, z.l.x, sh);
-          x[2 * j + 1] = -dd_to_double(z.h.y, z.l.y, sh);
+          x[2 * j] = dd_out(z.h.x, z.l.x, sh);
+          x[2 * j + 1] = -dd_out(z.h.y, z.l.y, sh);
         }
       }
     }
@@ -303,8 +313,8 @@ __global__ void __launch_bounds__(1024, 1) k_ring_fft_inv_df(InvDfArgs a) {
     double* xs = a.maps + (long long)k * a.map_stride + off_s;
     for (int j = tid; j < n; j += nt) {
       const cdd z = buf[S(dft_bin(rf, j))];   // x_N = Re, x_S = -Im of the DFT
-      xn[j] = dd_to_double(z.h.x, z.l.x, sh);
-      if (!equator) xs[j] = -dd_to_double(z.h.y, z.l.y, sh);
+      xn[j] = dd_out(z.h.x, z.l.x, sh);
+      if (!equator) xs[j] = -dd_out(z.h.y, z.l.y, sh);
     }
   }
 }

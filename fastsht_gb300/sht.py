@@ -236,6 +236,14 @@ class SHT:
                 return None
             return self._alm_out(dalm, alms_in, as_torch)
 
+    def release_staging(self):
+        """Frees the device buffers that t2alm keeps between calls for NumPy (host) inputs
+        (maps and alm of nsim maps); the next host-buffer call allocates them again."""
+        hd = getattr(self, "_host_dev", None)
+        if hd is not None and self._dev_alm is hd[1]:
+            self._dev_alm = None          # get_alms() has nothing to read any more
+        self._host_dev = None
+
     def _host_alm_ok(self, alms_in):
         if alms_in is None:
             return True
@@ -255,8 +263,11 @@ class SHT:
         a = np.asfortranarray(a, dtype=np.float64)
         L = self.lmax + 1
         out = np.asarray(alms_in) if alms_in is not None else _pinned_empty_fortran((self.nsim, L, L))
-        dmaps = self._new_dev_maps()
-        dalm = self._new_dev_alm()
+        # device staging buffers of the host path, kept between calls (like the reference's
+        # persistent device arrays); the alm buffer is also what get_alms() reads
+        if getattr(self, "_host_dev", None) is None:
+            self._host_dev = (self._new_dev_maps(), self._new_dev_alm())
+        dmaps, dalm = self._host_dev
         _lib.call("fsht_t2alm_host", self._plan, C.c_void_p(a.ctypes.data),
                   C.c_void_p(out.ctypes.data), C.c_void_p(dmaps.data_ptr()),
                   C.c_void_p(dalm.data_ptr()), self.nsim, self.niter,
