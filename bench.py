@@ -696,7 +696,9 @@ def _e2e_run(sht, maps_dev, ke, args, world, local):
         sht.t2alm(maps_np, alms_in=out_np)
     torch.cuda.synchronize()
     dt = time.perf_counter() - t0
-    # the copies alone (pinned host <-> device, the first 64 maps): the host link's rate
+    # the same pinned buffers copied by torch (first 64 maps): a reference for the host link's
+    # rate; the library's own copies are cudaMemcpyAsync calls on its copy stream, which on
+    # some boxes run several times faster than torch's copy of the same memory
     kc = min(ke, 64)
     dmaps = torch.empty((kc, npix), dtype=torch.float64, device=maps_dev.device)
     dalm = torch.empty((kc, L * L), dtype=torch.float64, device=maps_dev.device)
@@ -715,7 +717,8 @@ def _e2e_run(sht, maps_dev, ke, args, world, local):
             "h2d_bytes_per_step": ke * npix * 8, "d2h_bytes_per_step": ke * L * L * 8,
             "maps_per_step": ke, "ms_per_step": 1000.0 * dt / args.steps,
             "host_cpus": ("the GPU's NUMA-local cores (%d)" % len(local)) if local else "default",
-            "h2d_gbs": kc * npix * 8 / (t2 - t1) / 1e9, "d2h_gbs": kc * L * L * 8 / (t3 - t2) / 1e9}
+            "torch_copy_h2d_gbs": kc * npix * 8 / (t2 - t1) / 1e9,
+            "torch_copy_d2h_gbs": kc * L * L * 8 / (t3 - t2) / 1e9}
 
 
 # ---------------------------------------------------------------- batched form
