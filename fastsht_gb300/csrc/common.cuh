@@ -256,8 +256,7 @@ int fsht_launch_split_gemm(fsht_plan* p, int w, const unsigned char* WS, const i
                            int kc, int accumulate, cudaStream_t s);
 // Split-precision synthesis of one chunk into W = {G_N, G_S}: per wave, slice_alm cuts alm
 // into digit tiles WS / exponents EB, lambdaT writes ring-row lambda tiles, synth contracts
-// them.  clear_w zeroes W for the spin-2 synthesis, whose l-chunks add into it.
-int fsht_split_clear_w(fsht_plan* p, double2* W, int kc, cudaStream_t s);
+// them.
 int fsht_launch_split_slice_alm(fsht_plan* p, int w, const double* alm, unsigned char* WS,
                                 int* EB, int nmaps_total, int k0, int kc, cudaStream_t s);
 int fsht_launch_split_lambdaT(fsht_plan* p, int w, unsigned char* lbuf, cudaStream_t s);

@@ -1097,16 +1097,6 @@ int fsht_launch_split_gemm(fsht_plan* p, int w, const unsigned char* WS, const i
   return FSHT_OK;
 }
 
-int fsht_split_clear_w(fsht_plan* p, double2* W, int kc, cudaStream_t s) {
-  const int nkl0 = (p->lmax / 2 + 1 + kKStep - 1) / kKStep;
-  if (nkl0 * kKStep > kKChunk) {
-    // l-chunks add into W: clear it first
-    FSHT_CUDA_TRY(cudaMemsetAsync(W, 0, sizeof(double2) * 2 * (size_t)(p->lmax + 1) * p->nnorth * kc,
-                                  s));
-  }
-  return FSHT_OK;
-}
-
 int fsht_launch_split_slice_alm(fsht_plan* p, int w, const double* alm, unsigned char* WS,
                                 int* EB, int nmaps_total, int k0, int kc, cudaStream_t s) {
   const int* wv = p->h_waves + kWaveInts * w;

@@ -595,7 +595,7 @@ __global__ void __launch_bounds__(128) k_lambda_digits_T_pol(LamTPArgs a) {
 // accumulators, each one (lambda part, alm field, parity) product added to G_N and G_S with
 // its factor c in {-1, -i, +i} and south sign.
 struct SynthPArgs {
-  int lmax, nnorth, ngroups, nkcl_glob, q0, nkclmax, eag;
+  int lmax, nnorth, ngroups, q0, nrbmax, eag, nunits;
   size_t row_bytes;
   const int* ring_i0;
   const long long* lam_offT;
@@ -612,12 +612,35 @@ struct SynthPArgs {
 
 constexpr int kStagesSP = 4;
 constexpr uint32_t kStageBytesSP = kSlices * kATileBytes + kSynthBBytes;   // 44 KB
+constexpr int kPartStepsSP = kKChunk / kKStep;
 
 struct __align__(8) SynthPSmemHdr {
   uint64_t full[kStagesSP], empty[kStagesSP], tfull, tempty, fin;
   uint32_t tmem;
   int abort;
 };
+
+// One work unit (q, 128-ring block, field Q|U, 64-map group), the group fastest; nkl = 0:
+// nothing to do.
+struct SynthPUnit {
+  int g, f, rb, qi, m, i0, K, nrb, nkl;
+};
+
+__device__ __forceinline__ SynthPUnit synth_pol_unit(const SynthPArgs& a, int u) {
+  SynthPUnit w;
+  w.g = u % a.ngroups;
+  int r = u / a.ngroups;
+  w.f = r & 1;
+  r >>= 1;
+  w.rb = r % a.nrbmax;
+  w.qi = r / a.nrbmax;
+  w.m = m_of_q(a.q0 + w.qi, a.lmax);
+  w.i0 = a.ring_i0[w.m];
+  w.K = a.nnorth - w.i0;
+  w.nrb = (w.K + kSCRings - 1) / kSCRings;
+  w.nkl = w.rb < w.nrb ? ((a.lmax - w.m) / 2 + 1 + kKStep - 1) / kKStep : 0;
+  return w;
+}
 
 // pass t of field f: lambda part, alm field (0 E, 1 B), parity, factor c (0: -1, 1: -i,
 // 2: +i) and south sign
@@ -638,26 +661,16 @@ __device__ __forceinline__ void synth_pol_pass(int f, int t, int& part, int& fld
   sgn_s = (part == 0) ? s1 : -s1;           // lambda2: the opposite sign
 }
 
-__global__ void __launch_bounds__(kThreads, 1) k_split_synth_pol(SynthPArgs a) {
+// Persistent like the analysis contractions: one CTA per SM walks the units; per part of
+// <= 64 l-steps the four passes (lambda part x alm field x parity, synth_pol_pass) run through
+// the same TMEM accumulators.  The first pass of a unit writes both components of G_N and G_S,
+// every later pass adds as fire-and-forget reductions from the thread that owns the element
+// (deterministic, no clearing of W).  Warps 0-7: epilogue, warp 8 lane 0: copies, warp 9
+// lane 0: UMMAs.
+__global__ void __launch_bounds__(kThreadsG, 1) k_split_synth_pol(SynthPArgs a) {
   extern __shared__ __align__(1024) unsigned char smem[];
   __shared__ SynthPSmemHdr h;
   __shared__ int s_ce[4][kCols];       // column exponents EAG + e - 12 per pass
-
-  const int g = blockIdx.x;
-  const int f = blockIdx.y & 1;
-  const int rest = blockIdx.y >> 1;
-  const int rb = rest / a.nkclmax;
-  const int kcl = rest % a.nkclmax;
-  const int q = a.q0 + blockIdx.z;
-  const int m = m_of_q(q, a.lmax);
-  const int i0 = a.ring_i0[m];
-  const int K = a.nnorth - i0;
-  const int nrb = (K + kSCRings - 1) / kSCRings;
-  const int nkl = ((a.lmax - m) / 2 + 1 + kKStep - 1) / kKStep;
-  const int kl0 = kcl * (kKChunk / kKStep);
-  const int kl1 = min(nkl, kl0 + kKChunk / kKStep);
-  if (rb >= nrb || kl0 >= kl1) return;            // uniform: before any barrier or TMEM
-  const int nk = kl1 - kl0;
 
   const int tid = threadIdx.x;
   const int warp = tid >> 5;
@@ -668,19 +681,10 @@ __global__ void __launch_bounds__(kThreads, 1) k_split_synth_pol(SynthPArgs a) {
       tc::mbar_init(&h.empty[s], 1);
     }
     tc::mbar_init(&h.tfull, 1);
-    tc::mbar_init(&h.tempty, 128);
+    tc::mbar_init(&h.tempty, kEpiThreads);
     tc::mbar_init(&h.fin, 1);
     h.abort = 0;
     tc::mbar_fence_init();
-  }
-  if (tid < kCols) {
-    for (int t = 0; t < 4; ++t) {
-      int part, fld, par, c, sg;
-      synth_pol_pass(f, t, part, fld, par, c, sg);
-      const int* eb = fld ? a.EBB : a.EBE;
-      const int e = eb[(((long long)blockIdx.z * 2 + par) * a.ngroups + g) * kCols + tid];
-      s_ce[t][tid] = (e == kEmptyExp) ? kEmptyExp : a.eag + e - 12;
-    }
   }
   if (warp == 0) tc::tmem_alloc(&h.tmem, 512);
   tc::tc_fence_before();
@@ -689,127 +693,179 @@ __global__ void __launch_bounds__(kThreads, 1) k_split_synth_pol(SynthPArgs a) {
   const uint32_t tmem = h.tmem;
 
   uint32_t n_loaded = 0;
-  if (tid == 128) {
-    const unsigned char* lam =
-        a.lbuf + (size_t)(2 * (a.lam_offT[q] - a.lam_offT[a.q0])) * kSlices * kATileBytes;
-    for (int i = 0; i < 4 * nk; ++i) {
-      int part, fld, par, c, sg;
-      synth_pol_pass(f, i / nk, part, fld, par, c, sg);
-      const int kk = kl0 + i % nk;
-      const uint32_t st = i % kStagesSP;
-      if (!tc::mbar_wait(&h.empty[st], ((i / kStagesSP) & 1) ^ 1, abort)) break;
-      unsigned char* dst = smem + st * kStageBytesSP;
-      const unsigned char* asrc =
-          lam + ((((size_t)(part * 2 + par) * nrb + rb) * nkl + kk) * kSlices) * kATileBytes;
-      const unsigned char* bsrc = (fld ? a.WSB : a.WSE) +
-                                  (((size_t)blockIdx.z * 2 + par) * a.ngroups + g) * a.row_bytes +
-                                  (size_t)kk * kSynthBBytes;
-      tc::mbar_arrive_expect_tx(&h.full[st], kStageBytesSP);
-      tc::bulk_g2s(dst, asrc, kSlices * kATileBytes, &h.full[st]);
-      tc::bulk_g2s(dst + kSlices * kATileBytes, bsrc, kSynthBBytes, &h.full[st]);
-      ++n_loaded;
+  if (tid == kEpiThreads) {
+    uint32_t i = 0;
+    bool ok = true;
+    for (int u = blockIdx.x; u < a.nunits && ok && !*abort; u += gridDim.x) {
+      const SynthPUnit w = synth_pol_unit(a, u);
+      if (w.nkl == 0) continue;
+      const unsigned char* lam =
+          a.lbuf + (size_t)(2 * (a.lam_offT[a.q0 + w.qi] - a.lam_offT[a.q0])) * kSlices * kATileBytes;
+      for (int kl0 = 0; kl0 < w.nkl && ok; kl0 += kPartStepsSP) {
+        const int nk = min(w.nkl - kl0, kPartStepsSP);
+        for (int t = 0; t < 4 && ok; ++t) {
+          int part, fld, par, c, sg;
+          synth_pol_pass(w.f, t, part, fld, par, c, sg);
+          for (int kk = kl0; kk < kl0 + nk; ++kk, ++i) {
+            const uint32_t st = i % kStagesSP;
+            if (!tc::mbar_wait(&h.empty[st], ((i / kStagesSP) & 1) ^ 1, abort)) {
+              ok = false;
+              break;
+            }
+            unsigned char* dst = smem + st * kStageBytesSP;
+            const unsigned char* asrc =
+                lam + ((((size_t)(part * 2 + par) * w.nrb + w.rb) * w.nkl + kk) * kSlices) *
+                          kATileBytes;
+            const unsigned char* bsrc =
+                (fld ? a.WSB : a.WSE) +
+                (((size_t)w.qi * 2 + par) * a.ngroups + w.g) * a.row_bytes +
+                (size_t)kk * kSynthBBytes;
+            tc::mbar_arrive_expect_tx(&h.full[st], kStageBytesSP);
+            tc::bulk_g2s(dst, asrc, kSlices * kATileBytes, &h.full[st]);
+            tc::bulk_g2s(dst + kSlices * kATileBytes, bsrc, kSynthBBytes, &h.full[st]);
+            ++n_loaded;
+          }
+        }
+      }
     }
-  } else if (tid == 160) {
+  } else if (tid == kEpiThreads + 32) {
     const uint32_t idesc = tc::umma_idesc_bf16(kRows, kCols);
     const uint32_t s_u = tc::smem_u32(smem);
-    for (int i = 0; i < 4 * nk; ++i) {
-      if (i > 0 && i % nk == 0) {
-        // a pass is complete: hand TMEM to the epilogue, take it back for the next one
-        tc::umma_commit(&h.tfull);
-        if (!tc::mbar_wait(&h.tempty, ((i / nk) - 1) & 1, abort)) break;
-        tc::tc_fence_after();
-      }
-      const uint32_t st = i % kStagesSP;
-      if (!tc::mbar_wait(&h.full[st], (i / kStagesSP) & 1, abort)) break;
-      tc::tc_fence_after();
-      const uint32_t abase = s_u + st * kStageBytesSP;
-      const uint32_t bbase = abase + kSlices * kATileBytes;
-      const bool first = (i % nk) == 0;
+    uint32_t i = 0, np = 0;
+    bool ok = true;
+    for (int u = blockIdx.x; u < a.nunits && ok && !*abort; u += gridDim.x) {
+      const SynthPUnit w = synth_pol_unit(a, u);
+      for (int kl0 = 0; kl0 < w.nkl && ok; kl0 += kPartStepsSP) {
+        const int nk = min(w.nkl - kl0, kPartStepsSP);
+        for (int t = 0; t < 4 && ok; ++t, ++np) {
+          if (np > 0 && !tc::mbar_wait(&h.tempty, (np - 1) & 1, abort)) {
+            ok = false;
+            break;
+          }
+          tc::tc_fence_after();
+          for (int k = 0; k < nk; ++k, ++i) {
+            const uint32_t st = i % kStagesSP;
+            if (!tc::mbar_wait(&h.full[st], (i / kStagesSP) & 1, abort)) {
+              ok = false;
+              break;
+            }
+            tc::tc_fence_after();
+            const uint32_t abase = s_u + st * kStageBytesSP;
+            const uint32_t bbase = abase + kSlices * kATileBytes;
 #pragma unroll
-      for (int lev = 0; lev <= 3; ++lev) {
+            for (int lev = 0; lev <= 3; ++lev) {
 #pragma unroll
-        for (int aa = 0; aa <= lev; ++aa) {
-          const uint64_t ad = tc::umma_desc(abase + aa * kATileBytes, 128, 256);
-          const uint64_t bd = tc::umma_desc(bbase + (lev - aa) * kBTileBytes, 128, 256);
-          tc::umma_bf16(tmem + lev * kCols, ad, bd, idesc, (!first || aa > 0) ? 1u : 0u);
+              for (int aa = 0; aa <= lev; ++aa) {
+                const uint64_t ad = tc::umma_desc(abase + aa * kATileBytes, 128, 256);
+                const uint64_t bd = tc::umma_desc(bbase + (lev - aa) * kBTileBytes, 128, 256);
+                tc::umma_bf16(tmem + lev * kCols, ad, bd, idesc, (k > 0 || aa > 0) ? 1u : 0u);
+              }
+            }
+#pragma unroll
+            for (int aa = 1; aa <= 3; ++aa) {
+              const uint64_t ad = tc::umma_desc(abase + aa * kATileBytes, 128, 256);
+              const uint64_t bd =
+                  tc::umma_desc(bbase + (kSlices - 1 + (4 - aa)) * kBTileBytes, 128, 256);
+              tc::umma_bf16(tmem + 3 * kCols, ad, bd, idesc, 1u);
+            }
+            tc::umma_commit(&h.empty[st]);
+          }
+          if (ok) tc::umma_commit(&h.tfull);
         }
       }
-#pragma unroll
-      for (int aa = 1; aa <= 3; ++aa) {
-        const uint64_t ad = tc::umma_desc(abase + aa * kATileBytes, 128, 256);
-        const uint64_t bd = tc::umma_desc(bbase + (kSlices - 1 + (4 - aa)) * kBTileBytes, 128, 256);
-        tc::umma_bf16(tmem + 3 * kCols, ad, bd, idesc, 1u);
-      }
-      tc::umma_commit(&h.empty[st]);
     }
-    tc::umma_commit(&h.tfull);
-  }
-  if (tid < 128) {
-    const int row = (warp << 5) + (tid & 31);
-    const int rr = rb * kSCRings + row;
-    const bool rowok = rr < K;
-    const int i = i0 + rr;
-    double* Wf = f ? a.WU : a.WQ;
-    for (int t = 0; t < 4; ++t) {
-      int part, fld, par, c, sg;
-      synth_pol_pass(f, t, part, fld, par, c, sg);
-      bool ok = tc::mbar_wait(&h.tfull, t & 1, abort);
-      ok = __all_sync(0xffffffffu, ok);
-      tc::tc_fence_after();
-      if (!ok) break;
-      const uint32_t lane_base = tmem + ((uint32_t)(warp << 5) << 16);
-      for (int c0 = 0; c0 < kCols; c0 += 16) {
-        uint32_t v0[16], v1[16], v2[16], v3[16];
-        tc::tmem_ld16(lane_base + 0 * kCols + c0, v0);
-        tc::tmem_ld16(lane_base + 1 * kCols + c0, v1);
-        tc::tmem_ld16(lane_base + 2 * kCols + c0, v2);
-        tc::tmem_ld16(lane_base + 3 * kCols + c0, v3);
-        tc::tmem_wait_ld();
-        const int comp = c0 >> 6;
-        // c D: -1: (-D.x, -D.y);  -i: (D.y, -D.x);  +i: (-D.y, D.x)
-        int tgt = comp;
-        double sgn = -1.0;
-        if (c == 1) {
-          tgt = 1 - comp;
-          sgn = comp ? 1.0 : -1.0;
-        } else if (c == 2) {
-          tgt = 1 - comp;
-          sgn = comp ? -1.0 : 1.0;
-        }
-        if (!rowok) continue;
+  } else if (tid < kEpiThreads) {
+    // No early exit: the epilogue threads must meet at every named barrier.
+    const int row = ((warp & 3) << 5) + (tid & 31);
+    const int cbeg = (warp >> 2) * (kCols / 2);
+    const uint32_t lane_base = tmem + ((uint32_t)((warp & 3) << 5) << 16);
+    uint32_t np = 0;
+    for (int u = blockIdx.x; u < a.nunits; u += gridDim.x) {
+      const SynthPUnit w = synth_pol_unit(a, u);
+      if (w.nkl == 0) continue;
+      {
+        int e[4] = {0, 0, 0, 0};
+        if (tid < kCols)
+          for (int t = 0; t < 4; ++t) {
+            int part, fld, par, c, sg;
+            synth_pol_pass(w.f, t, part, fld, par, c, sg);
+            const int* eb = fld ? a.EBB : a.EBE;
+            e[t] = eb[(((long long)w.qi * 2 + par) * a.ngroups + w.g) * kCols + tid];
+          }
+        asm volatile("bar.sync 1, %0;" ::"n"(kEpiThreads) : "memory");
+        if (tid < kCols)
+          for (int t = 0; t < 4; ++t)
+            s_ce[t][tid] = (e[t] == kEmptyExp) ? kEmptyExp : a.eag + e[t] - 12;
+        asm volatile("bar.sync 1, %0;" ::"n"(kEpiThreads) : "memory");
+      }
+      const int rr = w.rb * kSCRings + row;
+      const bool rowok = rr < w.K;
+      const int i = w.i0 + rr;
+      double* Wf = w.f ? a.WU : a.WQ;
+      for (int kl0 = 0; kl0 < w.nkl; kl0 += kPartStepsSP) {
+        for (int t = 0; t < 4; ++t) {
+          int part, fld, par, c, sg;
+          synth_pol_pass(w.f, t, part, fld, par, c, sg);
+          bool ok = tc::mbar_wait(&h.tfull, np & 1, abort);
+          ok = __all_sync(0xffffffffu, ok);
+          ++np;
+          if (!ok) continue;
+          tc::tc_fence_after();
+          const bool first = kl0 == 0 && t == 0;   // pass 0 writes both components
+          for (int c0 = cbeg; c0 < cbeg + kCols / 2; c0 += 16) {
+            uint32_t v0[16], v1[16], v2[16], v3[16];
+            tc::tmem_ld16(lane_base + 0 * kCols + c0, v0);
+            tc::tmem_ld16(lane_base + 1 * kCols + c0, v1);
+            tc::tmem_ld16(lane_base + 2 * kCols + c0, v2);
+            tc::tmem_ld16(lane_base + 3 * kCols + c0, v3);
+            tc::tmem_wait_ld();
+            if (c0 == cbeg + kCols / 2 - 16) {
+              tc::tc_fence_before();
+              tc::mbar_arrive(&h.tempty);
+            }
+            const int comp = c0 >> 6;
+            // c D: -1: (-D.x, -D.y);  -i: (D.y, -D.x);  +i: (-D.y, D.x)
+            int tgt = comp;
+            bool neg = true;
+            if (c == 1) {
+              tgt = 1 - comp;
+              neg = comp == 0;
+            } else if (c == 2) {
+              tgt = 1 - comp;
+              neg = comp == 1;
+            }
+            if (!rowok) continue;
 #pragma unroll
-        for (int j = 0; j < 16; ++j) {
-          const int cc = c0 + j;
-          const int k = g * kGroupMaps + (cc & 63);
-          if (k < a.kc) {
-            const double u = levels_scaled(v0[j], v1[j], v2[j], v3[j], 1.f, 0.f, s_ce[t][cc]);
-            const double v = sgn < 0.0 ? -u : u;
-            double* gn = Wf + ((((long long)m * a.nnorth + i) * a.kc + k) * 2) * 2 + tgt;
-            double* gs = gn + 2;
-            const double vs = sg < 0 ? -v : v;
-            if (a.nkcl_glob > 1) {
-              atomicAdd(gn, v);
-              atomicAdd(gs, vs);
-            } else if (t == 0) {     // pass 0 writes both components of G_N and G_S
-              *gn = v;
-              *gs = vs;
-            } else {
-              *gn += v;
-              *gs += vs;
+            for (int j = 0; j < 16; ++j) {
+              const int cc = c0 + j;
+              const int k = w.g * kGroupMaps + (cc & 63);
+              if (k < a.kc) {
+                const double uu =
+                    levels_scaled(v0[j], v1[j], v2[j], v3[j], 1.f, 0.f, s_ce[t][cc]);
+                const double v = neg ? -uu : uu;
+                double* gn = Wf + ((((long long)w.m * a.nnorth + i) * a.kc + k) * 2) * 2 + tgt;
+                double* gs = gn + 2;
+                const double vs = sg < 0 ? -v : v;
+                if (first) {
+                  *gn = v;
+                  *gs = vs;
+                } else {
+                  atomicAdd(gn, v);
+                  atomicAdd(gs, vs);
+                }
+              }
             }
           }
         }
       }
-      tc::tc_fence_before();
-      if (t < 3) tc::mbar_arrive(&h.tempty);
     }
   }
-  if (tid == 160) {
+  if (tid == kEpiThreads + 32) {
     tc::umma_commit(&h.fin);
     for (uint32_t it = 0; it < tc::kWaitLimit; ++it)
       if (tc::mbar_try_wait(&h.fin, 0)) break;
   }
-  if (tid == 128) {
+  if (tid == kEpiThreads) {
     for (uint32_t d = 0; d < (uint32_t)kStagesSP && d < n_loaded; ++d) {
       const uint32_t i = n_loaded - 1 - d;
       for (uint32_t it = 0; it < tc::kWaitLimit; ++it)
@@ -931,9 +987,9 @@ int fsht_launch_split_synth_pol(fsht_plan* p, int w, const unsigned char* WSE, c
   a.lmax = p->lmax;
   a.nnorth = p->nnorth;
   a.ngroups = (kc + kGroupMaps - 1) / kGroupMaps;
-  a.nkcl_glob = ((p->lmax / 2 + 1 + kKStep - 1) / kKStep * kKStep + kKChunk - 1) / kKChunk;
   a.q0 = wv[0];
-  a.nkclmax = wv[6];
+  a.nrbmax = wv[4];
+  a.nunits = a.ngroups * 2 * a.nrbmax * (wv[1] - wv[0]);
   a.eag = std::ilogb(std::sqrt((2.0 * p->lmax + 1.0) / (4.0 * M_PI)) * (1.0 + 0x1p-30)) + 1;
   a.row_bytes = ws_row_bytes(p->lmax, p->nnorth);
   a.ring_i0 = p->d_ring_i0;
@@ -950,7 +1006,11 @@ int fsht_launch_split_synth_pol(fsht_plan* p, int w, const unsigned char* WSE, c
   const size_t sm = (size_t)kStagesSP * kStageBytesSP;
   FSHT_CUDA_TRY(cudaFuncSetAttribute(k_split_synth_pol,
                                      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-  k_split_synth_pol<<<dim3(a.ngroups, 2 * wv[4] * wv[6], wv[1] - wv[0]), kThreads, sm, s>>>(a);
+  int dev = 0, nsm = 0;
+  FSHT_CUDA_TRY(cudaGetDevice(&dev));
+  FSHT_CUDA_TRY(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+  const int grid = a.nunits < nsm ? a.nunits : nsm;
+  if (grid > 0) k_split_synth_pol<<<grid, kThreadsG, sm, s>>>(a);
   FSHT_LAUNCH_CHECK();
   return FSHT_OK;
 }

@@ -856,8 +856,7 @@ static int pol_synthesis(fsht_plan* p, const double* almE, const double* almB, d
   unsigned char* wsb = p->d_ws + fsht_split_ws_bytes(p, kc);
   int* ebe = p->d_eb;
   int* ebb = p->d_eb + fsht_split_eb_bytes(p, kc) / sizeof(int);
-  FSHT_TRY(fsht_split_clear_w(p, WQ, kc, p->stream));
-  FSHT_TRY(fsht_split_clear_w(p, WU, kc, p->stream));
+  // the first pass of every unit stores G_N and G_S, later passes add: no clearing
   FSHT_TRY(lam_start(p, fsht_launch_split_lambdaT_pol));
   for (int w = 0; w < p->nwaves; ++w) {
     {
