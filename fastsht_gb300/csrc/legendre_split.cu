@@ -9,18 +9,21 @@
 // exactly, so every UMMA product is an exact integer.  The ten digit products of level
 // a+b <= 3 run as BF16 UMMAs with FP32 accumulation, one TMEM accumulator per level:
 //   level 0 and level 1 sums stay below 2^24 over <= 1024 rings, so they are exact
-//   (rings beyond 1024 go to another CTA: K-chunks, combined with FP64 atomics);
+//   (a tile with more rings is accumulated in parts of <= 1024, each drained and added);
 //   levels 2 and 3 carry weights 2^-16 and 2^-24, so FP32 rounding there is far
 //   below the ~2^-31 representation error.
-// The epilogue combines the four levels and applies the scales in FP64.
+// The epilogue combines the four levels on the FP32 pipe and applies the scales with one
+// FP64 addition per element (levels_scaled).
 //
-// Three kernels per chunk of maps:
+// Three kernels per wave of m:
 //   k_slice_phase    P -> digit tiles WS and column exponents EB (per 64-map group);
 //   k_lambda_digits  the FP64 exponent-rescaled recursion, once per (m, ring) for all
 //                    map groups, written as lambda digit tiles into a staging buffer that
 //                    holds one wave of m (a few GB at most: no P_lm table is kept);
-//   k_split_gemm     one 128 x 128 output tile per CTA, both operands streamed by bulk
-//                    async copies (TMA engine) into a 6-stage ring, UMMAs into TMEM.
+//   k_split_gemm     persistent, one CTA per SM walking 128 x 128 output tiles, both
+//                    operands streamed by bulk async copies (TMA engine) into a 6-stage
+//                    ring, UMMAs into TMEM, eight epilogue warps.
+// The synthesis counterparts (k_slice_alm, k_lambda_digits_T, k_split_synth) follow below.
 // Max relative alm error against FP64: ~3e-8 (tests/test_gpu_split.py).
 #include "split_common.cuh"
 

@@ -12,10 +12,11 @@
 //   k_pol_table          per (l, m): c1..c4 of the scaled lambda1/lambda2 formulas;
 //   k_lambda_digits_pol  the FP64 recursion (mu form) once per (m, ring), lambda1 and
 //                        lambda2 digit tiles into the wave's staging buffer;
-//   k_split_gemm_pol     CTA = (64-map group, field, parity, l-tile, ring K-chunk): the
-//                        lambda1 product then the lambda2 product through the same TMEM
-//                        accumulators, each with its own column scales; the epilogue routes
-//                        (Re, Im) of the second product by the factor +-i.
+//   k_split_gemm_pol     persistent; unit = (q, l-tile, parity, field, 64-map group): per
+//                        ring part the lambda1 product then the lambda2 product through the
+//                        same TMEM accumulators, each with its own column scales; the
+//                        epilogue routes (Re, Im) of the second product by the factor +-i.
+// and the spin-2 synthesis (k_lambda_digits_T_pol, k_split_synth_pol) below.
 #include "split_common.cuh"
 
 #include <algorithm>
