@@ -163,6 +163,10 @@ struct fsht_plan {
   // host-buffer entry points: copy stream and its events (fork, maps landed, wave done, join)
   cudaStream_t xfer;
   cudaEvent_t evx[4];
+  // spin-0 split analysis: slicing one wave ahead on a second auxiliary stream into the other
+  // half of d_ws / d_eb (events: fork, join, slice done x2); null in job views
+  cudaStream_t aux2;
+  cudaEvent_t evs[4];
   int wave_qmax;                   // most orders in one wave
   FshtPolRow* d_poltab;            // spin-2 plans only, same triangular index as d_lamtab
 };

@@ -47,17 +47,18 @@ struct SliceArgs {
   int* EB;
 };
 
-// grid (q in wave, group), 512 threads = (ring half, map, parity, Re/Im) with Re/Im fastest, so
-// a warp reads 8 maps' whole 32-byte {S, D} entries of one ring: every W sector is read once per
-// pass (two passes: the column maximum, then the digits).  The two halves of a column's
-// k-steps go to two threads (shorter serial chains, twice the loads in flight); their maxima
-// meet in shared memory.
-__global__ void __launch_bounds__(512, 2) k_slice_phase(SliceArgs a) {
-  __shared__ double s_mx[256];
-  const int qi = blockIdx.x, g = blockIdx.y;
+// grid (q in wave, 2 x group), 256 threads = (ring half, map, parity, Re/Im) over one half
+// (32 maps) of a 64-map group, Re/Im fastest, so a warp reads 8 maps' whole 32-byte {S, D}
+// entries of one ring: every W sector is read once per pass (two passes: the column maximum,
+// then the digits).  The two halves of a column's k-steps go to two threads (shorter serial
+// chains, twice the loads in flight); their maxima meet in shared memory.  256 threads at <= 64
+// registers let a CTA share an SM with the persistent contraction of the previous wave.
+__global__ void __launch_bounds__(256, 4) k_slice_phase(SliceArgs a) {
+  __shared__ double s_mx[128];
+  const int qi = blockIdx.x, g = blockIdx.y >> 1;
   const int m = m_of_q(a.q0 + qi, a.lmax);
-  const int t = threadIdx.x & 255, half = threadIdx.x >> 8;
-  const int comp = t & 1, p = (t >> 1) & 1, kl = t >> 2;
+  const int t = threadIdx.x & 127, half = threadIdx.x >> 7;
+  const int comp = t & 1, p = (t >> 1) & 1, kl = (t >> 2) + 32 * (blockIdx.y & 1);
   const int k = g * kGroupMaps + kl;
   const int c = comp * kGroupMaps + kl;
   const int i0 = a.ring_i0[m];
@@ -958,7 +959,7 @@ int fsht_launch_split_slice(fsht_plan* p, int w, const double2* W, unsigned char
   sa.ring_i0 = p->d_ring_i0;
   sa.WS = WS;
   sa.EB = EB;
-  k_slice_phase<<<dim3(wv[1] - wv[0], sa.ngroups), 512, 0, s>>>(sa);
+  k_slice_phase<<<dim3(wv[1] - wv[0], 2 * sa.ngroups), 256, 0, s>>>(sa);
   FSHT_LAUNCH_CHECK();
   return FSHT_OK;
 }

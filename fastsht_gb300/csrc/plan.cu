@@ -104,6 +104,9 @@ void free_plan_memory(fsht_plan* p) {
   for (int i = 0; i < 4; ++i)
     if (p->evx[i]) cudaEventDestroy(p->evx[i]);
   if (p->xfer) cudaStreamDestroy(p->xfer);
+  for (int i = 0; i < 4; ++i)
+    if (p->evs[i]) cudaEventDestroy(p->evs[i]);
+  if (p->aux2) cudaStreamDestroy(p->aux2);
   cudaFree(p->d_poltab);
   delete[] p->h_waves;
   delete[] p->h_ring_i0;
@@ -292,9 +295,9 @@ int fsht_plan_create(int nside, int lmax, int nmaps_max, int flags, int precisio
   const size_t per_map = per_map_buffer_bytes(p) * p->nbuf;
   auto need = [&](size_t k) -> size_t {
     size_t b = per_map * k;
-    if (precision == FSHT_PREC_SPLIT)   // spin 2: digit tiles of Q and U; two lambda buffers
-      b += (p->pol ? 2 : 1) * (fsht_split_ws_bytes(p, (int)k) + fsht_split_eb_bytes(p, (int)k)) +
-           2 * p->lbuf_bytes;
+    if (precision == FSHT_PREC_SPLIT)   // two digit-tile buffers (Q and U, or two waves of T);
+      b += 2 * (fsht_split_ws_bytes(p, (int)k) + fsht_split_eb_bytes(p, (int)k)) +   // two
+           2 * p->lbuf_bytes;                                                          // lambda
     return b;
   };
   const bool tables_only = (flags & FSHT_FLAG_TABLES_ONLY) != 0;
@@ -313,7 +316,7 @@ int fsht_plan_create(int nside, int lmax, int nmaps_max, int flags, int precisio
     return fail(FSHT_ECUDA);
   }
   if (precision == FSHT_PREC_SPLIT && !tables_only) {
-    const size_t f = p->pol ? 2 : 1;
+    const size_t f = 2;   // Q and U digit tiles, or (spin 0) two waves in flight
     p->ws_bytes = f * fsht_split_ws_bytes(p, p->kchunk);
     if ((rc = dalloc((void**)&p->d_ws, p->ws_bytes))) return fail(rc);
     if ((rc = dalloc((void**)&p->d_eb, f * fsht_split_eb_bytes(p, p->kchunk)))) return fail(rc);
@@ -325,6 +328,16 @@ int fsht_plan_create(int nside, int lmax, int nmaps_max, int flags, int precisio
     }
     for (int i = 0; i < 6; ++i) {
       if ((ce = cudaEventCreateWithFlags(&p->ev[i], cudaEventDisableTiming)) != cudaSuccess) {
+        fsht_set_error("event: %s", cudaGetErrorString(ce));
+        return fail(FSHT_ECUDA);
+      }
+    }
+    if ((ce = cudaStreamCreateWithFlags(&p->aux2, cudaStreamNonBlocking)) != cudaSuccess) {
+      fsht_set_error("auxiliary stream: %s", cudaGetErrorString(ce));
+      return fail(FSHT_ECUDA);
+    }
+    for (int i = 0; i < 4; ++i) {
+      if ((ce = cudaEventCreateWithFlags(&p->evs[i], cudaEventDisableTiming)) != cudaSuccess) {
         fsht_set_error("event: %s", cudaGetErrorString(ce));
         return fail(FSHT_ECUDA);
       }
@@ -595,16 +608,43 @@ static int split_analysis(fsht_plan* p, const double2* W, double* alm, int nmaps
   // every alm element of the chunk is written by exactly one unit of the contraction (its
   // first ring part stores, later parts add), so alm needs no clearing
   if (!started) FSHT_TRY(lam_start(p, fsht_launch_split_lambda));
+  // Slicing runs one wave ahead on the second auxiliary stream, alternating between the two
+  // halves of d_ws / d_eb: the HBM-bound slicing of wave w + 1 shares the SMs with the
+  // tensor-core contraction of wave w.  The slice of wave w + 1 waits for the contraction of
+  // wave w - 1 (the "contraction done" events of the lambda pipeline), the contraction of
+  // wave w for its slice.
+  const bool ahead = p->aux2 != nullptr && p->aux != nullptr;
+  const size_t ws1 = fsht_split_ws_bytes(p, kc);
+  const size_t eb1 = fsht_split_eb_bytes(p, kc) / sizeof(int);
+  auto ws_of = [&](int w) { return p->d_ws + (ahead ? (size_t)(w & 1) * ws1 : 0); };
+  auto eb_of = [&](int w) { return p->d_eb + (ahead ? (size_t)(w & 1) * eb1 : 0); };
+  auto slice_on = [&](int w, cudaStream_t st) -> int {
+    FSHT_PROF_ON(FSHT_KCAT_SLICE, st);
+    return fsht_launch_split_slice(p, w, W, ws_of(w), eb_of(w), kc, st);
+  };
+  if (ahead) {
+    FSHT_CUDA_TRY(cudaEventRecord(p->evs[0], p->stream));
+    FSHT_CUDA_TRY(cudaStreamWaitEvent(p->aux2, p->evs[0], 0));
+    FSHT_TRY(slice_on(0, p->aux2));
+    FSHT_CUDA_TRY(cudaEventRecord(p->evs[2], p->aux2));
+  }
   for (int w = 0; w < p->nwaves; ++w) {
-    {
-      FSHT_PROF(FSHT_KCAT_SLICE);
-      FSHT_TRY(fsht_launch_split_slice(p, w, W, p->d_ws, p->d_eb, kc, p->stream));
+    if (!ahead) {
+      FSHT_TRY(slice_on(w, p->stream));
+    } else {
+      if (w + 1 < p->nwaves) {
+        if (w >= 1)
+          FSHT_CUDA_TRY(cudaStreamWaitEvent(p->aux2, p->ev[kEvDone + ((w + 1) & 1)], 0));
+        FSHT_TRY(slice_on(w + 1, p->aux2));
+        FSHT_CUDA_TRY(cudaEventRecord(p->evs[2 + ((w + 1) & 1)], p->aux2));
+      }
+      FSHT_CUDA_TRY(cudaStreamWaitEvent(p->stream, p->evs[2 + (w & 1)], 0));
     }
     unsigned char* lb = nullptr;
     FSHT_TRY(lam_ready(p, fsht_launch_split_lambda, w, &lb));
     {
       FSHT_PROF(FSHT_KCAT_ANALYSIS);
-      FSHT_TRY(fsht_launch_split_gemm(p, w, p->d_ws, p->d_eb, lb, alm, nmaps, c0, kc,
+      FSHT_TRY(fsht_launch_split_gemm(p, w, ws_of(w), eb_of(w), lb, alm, nmaps, c0, kc,
                                       accumulate, p->stream));
     }
     FSHT_TRY(lam_done(p, fsht_launch_split_lambda, w));
@@ -613,6 +653,10 @@ static int split_analysis(fsht_plan* p, const double2* W, double* alm, int nmaps
       fsht_split_wave_range(p, w, &q0, &q1);
       FSHT_TRY(xfer_orders_done(p, *hx, alm, nmaps, q0, q1, c0, kc));
     }
+  }
+  if (ahead) {
+    FSHT_CUDA_TRY(cudaEventRecord(p->evs[1], p->aux2));
+    FSHT_CUDA_TRY(cudaStreamWaitEvent(p->stream, p->evs[1], 0));
   }
   return lam_finish(p);
 }
