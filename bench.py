@@ -660,8 +660,10 @@ def gpu_local_cpus(dev):
 
 
 def e2e(sht, maps_dev, ke, args, world):
-    """Same metric through SHT.t2alm with host buffers: every step copies the maps
-    host->device and the alm device->host (pinned buffers, reused).  The process runs on the
+    """Same metric through SHT.t2alm with host buffers: every step moves the maps
+    host->device (read in place by the FFT over the host link, the API's default for pinned
+    buffers; the staged copy is timed beside it) and the alm device->host (pinned buffers,
+    reused).  The process runs on the
     GPU's own NUMA node's cores while it allocates them (first touch places the pinned pages
     there), as a NUMA-aware user would."""
     import torch
@@ -689,13 +691,29 @@ def _e2e_run(sht, maps_dev, ke, args, world, local):
     host.copy_(maps_dev.T[:ke])
     out_np = pinned_empty((ke, L, L))            # Fortran order
     out_t = torch.from_numpy(out_np.T)           # (L, L, ke) view
-    sht.t2alm(maps_np, alms_in=out_np)           # warm-up
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    for _ in range(args.steps):
-        sht.t2alm(maps_np, alms_in=out_np)
-    torch.cuda.synchronize()
-    dt = time.perf_counter() - t0
+
+    def timed(mode):
+        # host_read: "direct" = the FFT reads the pinned maps in place over the host link,
+        # "staged" = the maps are copied to device memory in sub-batches first
+        from fastsht_gb300 import _lib
+        _lib.call("fsht_plan_set_host_read", sht._plan, 1 if mode == "direct" else 0)
+        sht.host_read = mode
+        sht.t2alm(maps_np, alms_in=out_np)       # warm-up
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            sht.t2alm(maps_np, alms_in=out_np)
+        torch.cuda.synchronize()
+        return time.perf_counter() - t0
+
+    mode0 = sht.host_read
+    try:
+        dt_staged = timed("staged")
+        dt = timed("direct")
+    finally:
+        from fastsht_gb300 import _lib
+        _lib.call("fsht_plan_set_host_read", sht._plan, 1 if mode0 == "direct" else 0)
+        sht.host_read = mode0
     # the same pinned buffers copied by torch (first 64 maps): a reference for the host link's
     # rate; the library's own copies are cudaMemcpyAsync calls on its copy stream, which on
     # some boxes run several times faster than torch's copy of the same memory
@@ -716,6 +734,12 @@ def _e2e_run(sht, maps_dev, ke, args, world, local):
     return {"value": world * ke * args.steps / dt, "unit": UNIT,
             "h2d_bytes_per_step": ke * npix * 8, "d2h_bytes_per_step": ke * L * L * 8,
             "maps_per_step": ke, "ms_per_step": 1000.0 * dt / args.steps,
+            "host_read": ("direct: the forward FFT reads the pinned maps in place over the "
+                          "host link (the API's default for pinned_empty buffers)"),
+            "staged": {"value": world * ke * args.steps / dt_staged, "unit": UNIT,
+                       "ms_per_step": 1000.0 * dt_staged / args.steps,
+                       "note": "host_read='staged': maps copied to device memory in "
+                               "sub-batches, each transformed as it lands"},
             "host_cpus": ("the GPU's NUMA-local cores (%d)" % len(local)) if local else "default",
             "torch_copy_h2d_gbs": kc * npix * 8 / (t2 - t1) / 1e9,
             "torch_copy_d2h_gbs": kc * L * L * 8 / (t3 - t2) / 1e9}

@@ -47,6 +47,7 @@ SIGNATURES = {
     "fsht_plan_ring_skip": [_vp, C.POINTER(_i)],
     "fsht_t2alm": [_vp, _vp, _vp, _i, _i, _i],
     "fsht_t2alm_host": [_vp, _vp, _vp, _vp, _vp, _i, _i, _i],
+    "fsht_plan_set_host_read": [_vp, _i],
     "fsht_alm2t": [_vp, _vp, _vp, _i],
     "fsht_t2alm_noalloc": [_i, _i, _vp, _vp, _i, _vp],
     "fsht_qu2eb": [_vp, _vp, _vp, _vp, _vp, _i, _i],
@@ -64,6 +65,7 @@ SIGNATURES = {
     "fsht_selftest_wait_timeout": [_vp],
     "fsht_host_alloc": [_sz, C.POINTER(_vp)],
     "fsht_host_free": [_vp],
+    "fsht_host_mapped": [_vp, _sz, C.POINTER(_i)],
     "fsht_run_stage": [_vp, _i, _vp, _vp, _i],
     "fsht_profile_enable": [_vp, _i],
     "fsht_profile_read": [_vp, _i, C.POINTER(_i), C.POINTER(C.c_double)],

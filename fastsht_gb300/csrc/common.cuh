@@ -163,6 +163,9 @@ struct fsht_plan {
   // host-buffer entry points: copy stream and its events (fork, maps landed, wave done, join)
   cudaStream_t xfer;
   cudaEvent_t evx[4];
+  // fsht_t2alm_host: 0 = maps that lie in one fsht_host_alloc block are read in place by the
+  // forward FFT over the host link (no staging copy), 1 = maps are always copied first
+  int host_staged;
   // spin-0 split analysis: slicing one wave ahead on a second auxiliary stream into the other
   // half of d_ws / d_eb (events: fork, join, slice done x2); null in job views
   cudaStream_t aux2;

@@ -11,12 +11,18 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <map>
+#include <mutex>
 #include <new>
 #include <string>
 #include <vector>
 
 namespace {
 thread_local std::string g_last_error;
+// Page-locked blocks from fsht_host_alloc (start -> bytes): fsht_t2alm_host reads maps that
+// lie inside one of them in place.
+std::mutex g_host_mu;
+std::map<const char*, size_t> g_host_blocks;
 constexpr size_t kDefaultWorkspace = 16ull << 30;
 constexpr size_t kDefaultWorkspaceSplit = 80ull << 30;   // 500 maps at nside 1024 in one chunk
 }  // namespace
@@ -456,17 +462,64 @@ int fsht_host_alloc(size_t bytes, void** ptr) {
     return FSHT_EINVAL;
   }
   *ptr = nullptr;
-  cudaError_t e = cudaHostAlloc(ptr, bytes > 0 ? bytes : 1, cudaHostAllocPortable);
+  const size_t n = bytes > 0 ? bytes : 1;
+  cudaError_t e = cudaHostAlloc(ptr, n, cudaHostAllocPortable | cudaHostAllocMapped);
   if (e != cudaSuccess) {
     fsht_set_error("cudaHostAlloc(%zu): %s", bytes, cudaGetErrorString(e));
     *ptr = nullptr;
     return e == cudaErrorMemoryAllocation ? FSHT_ENOMEM : FSHT_ECUDA;
   }
+  std::lock_guard<std::mutex> lk(g_host_mu);
+  g_host_blocks[static_cast<const char*>(*ptr)] = n;
   return FSHT_OK;
 }
 
 int fsht_host_free(void* ptr) {
-  if (ptr) FSHT_CUDA_TRY(cudaFreeHost(ptr));
+  if (!ptr) return FSHT_OK;
+  {
+    std::lock_guard<std::mutex> lk(g_host_mu);
+    g_host_blocks.erase(static_cast<const char*>(ptr));
+  }
+  FSHT_CUDA_TRY(cudaFreeHost(ptr));
+  return FSHT_OK;
+}
+
+namespace {
+// The device address of host bytes [ptr, ptr + bytes) when they lie inside one
+// fsht_host_alloc block (mapped into the device's address space), else null.
+const double* host_direct(const void* ptr, size_t bytes) {
+  const char* c = static_cast<const char*>(ptr);
+  const char* base = nullptr;
+  {
+    std::lock_guard<std::mutex> lk(g_host_mu);
+    auto it = g_host_blocks.upper_bound(c);
+    if (it == g_host_blocks.begin()) return nullptr;
+    --it;
+    const size_t off = (size_t)(c - it->first);
+    if (off >= it->second || bytes > it->second - off) return nullptr;
+    base = it->first;
+  }
+  void* d = nullptr;
+  if (cudaHostGetDevicePointer(&d, const_cast<char*>(base), 0) != cudaSuccess || !d) {
+    cudaGetLastError();   // not mapped for this device: the caller stages the maps
+    return nullptr;
+  }
+  return reinterpret_cast<const double*>(static_cast<const char*>(d) + (c - base));
+}
+}  // namespace
+
+int fsht_host_mapped(const void* ptr, size_t bytes, int* mapped) {
+  if (!mapped) {
+    fsht_set_error("host_mapped: null output pointer");
+    return FSHT_EINVAL;
+  }
+  *mapped = (ptr && host_direct(ptr, bytes)) ? 1 : 0;
+  return FSHT_OK;
+}
+
+int fsht_plan_set_host_read(fsht_plan* p, int direct) {
+  FSHT_TRY(check_plan(p));
+  p->host_staged = direct ? 0 : 1;
   return FSHT_OK;
 }
 
@@ -556,6 +609,7 @@ static int lam_finish(fsht_plan* p) {
 // m = lmax + 1 - c, so it is final once both orders are.
 struct HostXfer {
   const double* hmaps;
+  const double* direct;   // device address of hmaps when the FFT reads them in place, or null
   double* halm;
   std::vector<char> mdone, cdone;
 };
@@ -728,9 +782,12 @@ static int t2alm_impl(fsht_plan* p, const double* maps, double* alm, int nmaps, 
     }
     // the first lambda tiles are computed on the auxiliary stream during the FFT
     if (split) FSHT_TRY(lam_start(p, fsht_launch_split_lambda));
-    const double* cmaps = maps + (size_t)c0 * p->npix;
-    if (!hx) {
+    // the chunk's maps as the FFT reads them: device buffer, or host memory read in place
+    const double* cmaps = (hx && hx->direct ? hx->direct : maps) + (size_t)c0 * p->npix;
+    if (!hx || hx->direct) {
       FSHT_PROF(FSHT_KCAT_FFT_FWD);
+      // (page-locked maps mapped into the device's address space are read over the host link
+      // as the transform goes, every value once, with no staging copy)
       FSHT_TRY(fsht_launch_ring_fft_fwd(p, cmaps, p->npix, kc, W0, p->stream));
     } else {
       // sub-batches of a multiple of 16 maps, at most 8
@@ -804,9 +861,16 @@ int fsht_t2alm(fsht_plan* p, const double* maps, double* alm, int nmaps, int nit
 
 int fsht_t2alm_host(fsht_plan* p, const double* host_maps, double* host_alm, double* dev_maps,
                     double* dev_alm, int nmaps, int niter, int method) {
-  FSHT_TRY(check_call(p, nmaps, dev_maps, dev_alm));
+  FSHT_TRY(check_call(p, nmaps, dev_alm, dev_alm));
   if (!host_maps || !host_alm) {
     fsht_set_error("t2alm_host: null host buffer");
+    return FSHT_EINVAL;
+  }
+  const double* direct =
+      p->host_staged ? nullptr : host_direct(host_maps, sizeof(double) * (size_t)p->npix * nmaps);
+  if (!direct && !dev_maps) {
+    fsht_set_error("t2alm_host: dev_maps is null and the maps are not read in place "
+                   "(not inside one fsht_host_alloc block, or staged reads requested)");
     return FSHT_EINVAL;
   }
   if (niter < 0 || method < 0 || method > 1) {
@@ -820,6 +884,7 @@ int fsht_t2alm_host(fsht_plan* p, const double* host_maps, double* host_alm, dou
   }
   HostXfer hx;
   hx.hmaps = host_maps;
+  hx.direct = direct;
   hx.halm = host_alm;
   return t2alm_impl(p, dev_maps, dev_alm, nmaps, niter, method, &hx);
 }

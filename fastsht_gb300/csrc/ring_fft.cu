@@ -141,7 +141,8 @@ __global__ void __launch_bounds__(512, 2) k_ring_fft_fwd(FwdArgs a) {
       for (int side = 0; side < 2; ++side) {
         const double* x = a.maps + (long long)k * a.map_stride + (side ? off_s : off_n);
         __syncthreads();
-        for (int j = tid; j < nd; j += nt)
+#pragma unroll 4
+        for (int j = tid; j < nd; j += nt)   // unrolled: several loads in flight per thread
           buf[S(j)] = make_double2(__ldg(&x[2 * j]), __ldg(&x[2 * j + 1]));
         __syncthreads();
         ring_dft(buf, rf, a.tw, chirp, bhat);
@@ -174,7 +175,8 @@ __global__ void __launch_bounds__(512, 2) k_ring_fft_fwd(FwdArgs a) {
     const double* xn = a.maps + (long long)k * a.map_stride + off_n;
     const double* xs = a.maps + (long long)k * a.map_stride + off_s;
     __syncthreads();
-    for (int j = tid; j < n; j += nt)
+#pragma unroll 4
+    for (int j = tid; j < n; j += nt)   // unrolled: several loads in flight per thread
       buf[S(j)] = make_double2(__ldg(&xn[j]), equator ? 0.0 : __ldg(&xs[j]));
     __syncthreads();
     ring_dft(buf, rf, a.tw, chirp, bhat);

@@ -72,6 +72,9 @@ __device__ __forceinline__ int load_scaled(cdd* buf, const Swz& S, int cnt, cons
   double2* raw = reinterpret_cast<double2*>(buf);
   const int tid = threadIdx.x, nt = blockDim.x;
   int em = 0;
+  // unrolled so that several loads are in flight per thread (the maps may be host memory read
+  // over the host link, with microseconds of latency)
+#pragma unroll 4
   for (int j = tid; j < cnt; j += nt) {
     const double va = __ldg(&xa[(long long)stride * j]);
     const double vb = xb ? __ldg(&xb[(long long)stride * j]) : 0.0;

@@ -62,10 +62,13 @@ class SHT:
     "fp64" (the plain method, all FP64) or "split" (the temperature Legendre
     contractions of t2alm and alm2t as BF16 digit products on the tensor cores, ~3e-8 max
     relative alm error; niter > 0 refines with the FP64 Fourier-space residual).
+    ``host_read``: how t2alm takes NumPy maps that sit in a ``pinned_empty`` buffer -
+    "direct" (read in place by the FFT over the host link) or "staged" (copied to device
+    memory first); the results are the same.
     """
 
     def __init__(self, nside, lmax, nsim, niter=0, pol=False, all_buff=False, *,
-                 device=None, workspace_limit=0, precision="fp64"):
+                 device=None, workspace_limit=0, precision="fp64", host_read="direct"):
         if not torch.cuda.is_available():
             raise RuntimeError("fastsht_gb300 needs a CUDA device (no CPU fallback)")
         self.nside = int(nside)
@@ -78,7 +81,10 @@ class SHT:
         self.device = torch.device("cuda", torch.cuda.current_device() if device is None else device)
         if precision not in ("fp64", "split"):
             raise ValueError("precision must be 'fp64' or 'split'")
+        if host_read not in ("direct", "staged"):
+            raise ValueError("host_read must be 'direct' or 'staged'")
         self.precision = precision
+        self.host_read = host_read
         # workspace buffers, like the reference's nbuff (SHT.py:52-59)
         flags = 0
         if pol or all_buff:
@@ -96,6 +102,7 @@ class SHT:
                       _lib.FSHT_PREC_SPLIT if precision == "split" else _lib.FSHT_PREC_FP64,
                       int(workspace_limit), C.c_void_p(stream), C.byref(plan))
         self._plan = plan
+        _lib.call("fsht_plan_set_host_read", plan, 1 if host_read == "direct" else 0)
 
     # ------------------------------------------------------------ lifetime
     def close(self):
@@ -254,9 +261,10 @@ class SHT:
         return a.dtype == np.float64 and a.flags.f_contiguous and a.shape == (self.nsim, L, L)
 
     def _t2alm_host(self, maps, alms_in, method):
-        """Host maps -> host alm through fsht_t2alm_host: the maps go to the device in
-        sub-batches that the FFT consumes as they land, finished alm columns come back while
-        later waves run (copies overlap the transform)."""
+        """Host maps -> host alm through fsht_t2alm_host.  Maps in a pinned_empty buffer are
+        read in place by the FFT over the host link (host_read="direct"); other maps go to the
+        device in sub-batches that the FFT consumes as they land.  Finished alm columns come
+        back while later waves run (copies overlap the transform)."""
         a = np.asarray(maps)
         if a.shape != (self.npix, self.nsim):
             raise ValueError(f"maps: expected shape ({self.npix}, {self.nsim}), got {a.shape}")
@@ -264,12 +272,21 @@ class SHT:
         L = self.lmax + 1
         out = np.asarray(alms_in) if alms_in is not None else _pinned_empty_fortran((self.nsim, L, L))
         # device staging buffers of the host path, kept between calls (like the reference's
-        # persistent device arrays); the alm buffer is also what get_alms() reads
-        if getattr(self, "_host_dev", None) is None:
-            self._host_dev = (self._new_dev_maps(), self._new_dev_alm())
-        dmaps, dalm = self._host_dev
+        # persistent device arrays); the alm buffer is also what get_alms() reads, the maps
+        # buffer is only made for maps that are not read in place
+        hd = getattr(self, "_host_dev", None)
+        if hd is None:
+            hd = self._host_dev = [None, self._new_dev_alm()]
+        mapped = C.c_int(0)
+        if self.host_read == "direct":
+            _lib.call("fsht_host_mapped", C.c_void_p(a.ctypes.data), C.c_size_t(a.nbytes),
+                      C.byref(mapped))
+        if not mapped.value and hd[0] is None:
+            hd[0] = self._new_dev_maps()
+        dmaps, dalm = hd
         _lib.call("fsht_t2alm_host", self._plan, C.c_void_p(a.ctypes.data),
-                  C.c_void_p(out.ctypes.data), C.c_void_p(dmaps.data_ptr()),
+                  C.c_void_p(out.ctypes.data),
+                  C.c_void_p(dmaps.data_ptr() if dmaps is not None else None),
                   C.c_void_p(dalm.data_ptr()), self.nsim, self.niter,
                   0 if method == 'old' else 1)
         _lib.call("fsht_plan_sync", self._plan)

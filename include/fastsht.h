@@ -16,7 +16,7 @@
  *          the (lmax+1)^2 slots is either a Re or an Im of some a_lm.
  * Transform entry points take DEVICE pointers and run asynchronously on the
  * plan's stream (fsht_plan_set_stream).  The *_host entry points take host
- * pointers and return after the result is in host memory.
+ * pointers and enqueue the copies with the transform on the same stream.
  */
 #ifndef FASTSHT_GB300_H
 #define FASTSHT_GB300_H
@@ -75,18 +75,26 @@ int fsht_plan_ring_skip(const fsht_plan* plan, int* out);
  * method 1: t2alm_iter (src/sht_main.f90:171-264). */
 int fsht_t2alm(fsht_plan* plan, const double* maps, double* alm, int nmaps,
                int niter, int method);
-/* fsht_t2alm from and to host memory, with the transfers overlapped with the transform: the
- * maps go to dev_maps in sub-batches on the plan's copy stream and each is forward-transformed
- * as soon as it lands; alm columns go from dev_alm back to host_alm as soon as they are final
- * (after each wave of the split form when niter = 0, else after the chunk).  Replaces the
- * reference's host-side SHT.t2alm call (SHT.py:72-107 over sht_main.f90:38-89, whose maps
- * and alm live in host memory).  dev_maps / dev_alm: device buffers of the same layouts,
- * provided by the caller (nothing is allocated here).  Host buffers should be pinned for
- * the copies to run asynchronously.  Results equal fsht_t2alm's; when the call returns the
- * work is enqueued on the plan's stream (fsht_plan_sync waits for it).  Needs a plan that
- * owns its workspace. */
+/* fsht_t2alm from and to host memory, with the transfers overlapped with the transform.
+ * Maps inside one fsht_host_alloc block (mapped into the device's address space) are read in
+ * place by the forward FFT over the host link, every value once, with no staging copy (unless
+ * fsht_plan_set_host_read(plan, 0)); other maps go to dev_maps in sub-batches on the plan's
+ * copy stream and each is forward-transformed as soon as it lands.  alm columns go from
+ * dev_alm back to host_alm as soon as they are final (after each wave of the split form when
+ * niter = 0, else after the chunk).  Replaces the reference's host-side SHT.t2alm call
+ * (SHT.py:72-107 over sht_main.f90:38-89, whose maps and alm live in host memory).
+ * dev_maps / dev_alm: device buffers of the same layouts, provided by the caller (nothing is
+ * allocated here); dev_maps may be null when the maps are read in place (fsht_host_mapped).
+ * Host buffers should be pinned for the copies to run asynchronously.  Results equal
+ * fsht_t2alm's; when the call returns the work is enqueued on the plan's stream
+ * (fsht_plan_sync waits for it; the host buffers must stay valid until then).  Needs a plan
+ * that owns its workspace. */
 int fsht_t2alm_host(fsht_plan* plan, const double* host_maps, double* host_alm,
                     double* dev_maps, double* dev_alm, int nmaps, int niter, int method);
+/* How fsht_t2alm_host obtains host maps: direct = 1 (the default) reads maps that lie in one
+ * fsht_host_alloc block in place, direct = 0 always copies them to dev_maps first.  Results
+ * are the same either way.  No counterpart in the reference. */
+int fsht_plan_set_host_read(fsht_plan* plan, int direct);
 /* Temperature synthesis: reference alm2t (src/sht_main.f90:96-155). */
 int fsht_alm2t(fsht_plan* plan, const double* alm, double* maps, int nmaps);
 /* Temperature analysis that allocates no device memory and needs no plan
@@ -251,11 +259,15 @@ int fsht_plan_check(fsht_plan* plan);
  * reference. */
 int fsht_selftest_wait_timeout(fsht_plan* plan);
 
-/* Page-locked host memory (cudaHostAlloc, portable to every device) for host buffers of
- * fsht_t2alm_host and the SHT class's NumPy outputs, so the copies run asynchronously at the
- * host link's rate.  No counterpart in the reference. */
+/* Page-locked host memory (cudaHostAlloc, portable to every device and mapped into their
+ * address spaces) for host buffers of fsht_t2alm_host and the SHT class's NumPy outputs: the
+ * copies run asynchronously at the host link's rate, and maps in such a block are read in
+ * place by fsht_t2alm_host.  No counterpart in the reference. */
 int fsht_host_alloc(size_t bytes, void** ptr);
 int fsht_host_free(void* ptr);
+/* *mapped = 1 when host bytes [ptr, ptr + bytes) lie inside one fsht_host_alloc block that
+ * the current device can read in place (fsht_t2alm_host then needs no dev_maps), else 0. */
+int fsht_host_mapped(const void* ptr, size_t bytes, int* mapped);
 
 /* Copies the calling thread's last error message into buf (NUL-terminated);
  * returns its full length. */

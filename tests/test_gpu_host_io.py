@@ -78,3 +78,64 @@ def test_pinned_empty_buffers():
     want = sht.t2alm(torch.from_numpy(np.asarray(maps).T.copy()).cuda().T).cpu().numpy()
     assert np.array_equal(out, want)
     del maps, out                                  # freed through fsht_host_free
+
+
+def _mapped(ptr, nbytes):
+    import ctypes as C
+    from fastsht_gb300 import _lib
+    m = C.c_int(-1)
+    _lib.call("fsht_host_mapped", C.c_void_p(ptr), C.c_size_t(nbytes), C.byref(m))
+    return m.value
+
+
+def test_host_mapped_ranges():
+    """Only byte ranges inside one fsht_host_alloc block are read in place."""
+    from fastsht_gb300 import pinned_empty
+    buf = pinned_empty((1000,))
+    p = buf.ctypes.data
+    assert _mapped(p, buf.nbytes) == 1
+    assert _mapped(p + 800, 200 * 8) == 1
+    assert _mapped(p + 8, buf.nbytes) == 0          # one double past the block's end
+    assert _mapped(np.zeros(1000).ctypes.data, 8000) == 0   # pageable memory
+    del buf
+    assert _mapped(p, 8000) == 0                    # freed blocks are forgotten
+
+
+@pytest.mark.parametrize("precision", ["fp64", "split"])
+@pytest.mark.parametrize("niter", [0, 1])
+def test_direct_read_equals_staged_and_device_paths(precision, niter):
+    """Maps in a pinned_empty buffer, read in place by the FFT (the default) and copied first
+    (host_read="staged"): both equal the device-buffer path bit for bit."""
+    from fastsht_gb300 import SHT, pinned_empty
+    ns, lmax, nsim = 64, 191, 70
+    maps = pinned_empty((12 * ns * ns, nsim))
+    maps[...] = _maps(ns, nsim, 5)
+    assert _mapped(maps.ctypes.data, maps.nbytes) == 1
+    want = SHT(ns, lmax, nsim, niter=niter, precision=precision).t2alm(
+        torch.from_numpy(np.asarray(maps).T.copy()).cuda().T).cpu().numpy()
+    direct = SHT(ns, lmax, nsim, niter=niter, precision=precision)
+    got = direct.t2alm(maps)
+    assert direct._host_dev[0] is None              # no device staging buffer for the maps
+    staged = SHT(ns, lmax, nsim, niter=niter, precision=precision, host_read="staged")
+    got_s = staged.t2alm(maps)
+    assert staged._host_dev[0] is not None
+    assert np.array_equal(got, want)
+    assert np.array_equal(got_s, want)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "split"])
+def test_direct_read_several_chunks_nside_1024(precision):
+    """In-place reads with several workspace chunks, and the headline shape class."""
+    from fastsht_gb300 import SHT, pinned_empty
+    for ns, lmax, nsim, lim in [(64, 191, 150, (60 << 20) if precision == "fp64" else (300 << 20)),
+                                (1024, 2047, 2, 0)]:
+        maps = pinned_empty((12 * ns * ns, nsim))
+        maps[...] = _maps(ns, nsim, 6)
+        sht = SHT(ns, lmax, nsim, precision=precision, workspace_limit=lim)
+        if lim:
+            assert sht.plan_info()["maps_per_chunk"] < nsim
+        got = sht.t2alm(maps)
+        want = sht.t2alm(torch.from_numpy(np.asarray(maps).T.copy()).cuda().T).cpu().numpy()
+        assert np.array_equal(got, want)
+        sht.close()
+        del maps
