@@ -183,9 +183,12 @@ def parse():
                          "fp64: the plain method")
     ap.add_argument("--no-fp64", action="store_true",
                     help="skip the plain-FP64 comparison run of the split form")
-    ap.add_argument("--workload", choices=["c3", "batched", "serving"], default="c3",
+    ap.add_argument("--workload", choices=["c3", "batched", "serving", "qu2eb"], default="c3",
                     help="c3: the headline 500-map nside-1024 analysis; batched: a mix of map "
-                         "sets in CUDA-graph launches; serving: a Poisson request stream")
+                         "sets in CUDA-graph launches; serving: a Poisson request stream; "
+                         "qu2eb: the spin-2 pair (Q/U -> E/B) in the split form")
+    ap.add_argument("--pol-maps", type=int, default=200,
+                    help="qu2eb: Q/U map pairs per step")
     ap.add_argument("--sets", type=int, default=64, help="batched: map sets in the mix")
     ap.add_argument("--max-maps", type=int, default=None,
                     help="batched/serving: upper end of the uniform nmaps draw")
@@ -851,6 +854,87 @@ def bench_batched(args, rank, world, local):
         dist.destroy_process_group()
 
 
+# ---------------------------------------------------------------- spin-2 pair
+def bench_qu2eb(args, rank, world, local):
+    """qu2eb (Q/U maps -> E/B alm, niter 0) of --pol-maps map pairs resident in HBM in the
+    split form; value counts Q and U as two maps.  Inputs: Q/U synthesised from Gaussian E/B
+    alm (C_l ~ l^-2, seeds 5 and 6).  The plain FP64 path runs the first 16 pairs for the error
+    and the speed ratio."""
+    import ctypes as C
+    import torch
+    import torch.distributed as dist
+    from fastsht_gb300 import SHT, _lib
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    lib = _lib.load(build_if_missing=True)
+    if world > 1:
+        dist.init_process_group("nccl", device_id=dev)
+    nside, lmax, nmaps = args.nside, args.lmax, args.pol_maps
+    sp = SHT(nside, lmax, nmaps, pol=True, device=local, precision="split")
+    E0 = device_alm(nside, lmax, nmaps, 5 + rank, dev)
+    B0 = device_alm(nside, lmax, nmaps, 6 + rank, dev)
+    Q, U = sp.eb2qu(E0.permute(2, 1, 0), B0.permute(2, 1, 0))   # (npix, nmaps) Fortran views
+    del E0, B0
+    torch.cuda.synchronize()
+    for _ in range(args.warmup):
+        E, B = sp.qu2eb(Q, U)
+    torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+    lib.fsht_profile_enable(sp._plan, 1)
+    _lib.call("fsht_profile_read", sp._plan, 0, None, None)
+    clocks = ClockSampler(local)
+    clocks.start()
+    s = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(s)
+    for _ in range(args.steps):
+        E, B = sp.qu2eb(Q, U)
+    e1.record(s)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    ms = e0.elapsed_time(e1)
+    counts = (C.c_int * _lib.KCAT_COUNT)()
+    kms = (C.c_double * _lib.KCAT_COUNT)()
+    _lib.call("fsht_profile_read", sp._plan, _lib.KCAT_COUNT, counts, kms)
+    lib.fsht_profile_enable(sp._plan, 0)
+    if world > 1:
+        ms = max_over_ranks(ms, dist, dev)
+    per_kernel = {name: {"launches": counts[i], "ms_per_step": round(kms[i] / args.steps, 2)}
+                  for i, name in enumerate(_lib.KCAT_NAMES) if counts[i]}
+    ks = min(16, nmaps)
+    p64 = SHT(nside, lmax, ks, pol=True, device=local)
+    p64.qu2eb(Q[:, :ks], U[:, :ks])                      # warm-up
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    E64, B64 = p64.qu2eb(Q[:, :ks], U[:, :ks])
+    torch.cuda.synchronize()
+    t64 = time.perf_counter() - t0
+    err = max(rel_err_per_map(E[:ks], E64), rel_err_per_map(B[:ks], B64))
+    value = world * 2 * nmaps * args.steps / (ms / 1000.0)
+    v64 = 2 * ks / t64
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None,
+        "dtype": "bf16x4-split of f64 (FP32 accum)", "data": "synthetic",
+        "config": {"workload": (f"qu2eb (spin-2 Q/U -> E/B, niter 0) of {nmaps} map pairs at "
+                                f"nside {nside} / lmax {lmax}, split form; Q and U count as two "
+                                f"maps"),
+                   "l2": "inputs resident in HBM, larger than L2, no flush",
+                   "parallelism": f"replicas x{world}"},
+        "clocks": clk, "per_kernel": per_kernel,
+        "fp64_plain": {"value": v64, "unit": UNIT, "maps_timed": 2 * ks,
+                       "split_speedup": value / v64 / world,
+                       "max_rel_alm_err_split_vs_fp64": err, "tolerance": 1e-7},
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+
+
 # ---------------------------------------------------------------- serving form
 def bench_serving(args, rank, world, local):
     """Open-loop Poisson stream into fastsht_gb300.serve.Server: map2alm or alm2map, T or
@@ -955,6 +1039,9 @@ def main():
         return
     if args.workload == "serving":
         bench_serving(args, rank, world, local)
+        return
+    if args.workload == "qu2eb":
+        bench_qu2eb(args, rank, world, local)
         return
     ours(args, rank, world, local)
 

@@ -299,11 +299,13 @@ int fsht_plan_create(int nside, int lmax, int nmaps_max, int flags, int precisio
                            ? workspace_limit_bytes
                            : (precision == FSHT_PREC_SPLIT ? kDefaultWorkspaceSplit : kDefaultWorkspace);
   const size_t per_map = per_map_buffer_bytes(p) * p->nbuf;
+  // digit-tile buffers of the split form: two waves in flight of T, or of Q and U (four)
+  const size_t f_ws = p->pol ? 4 : 2;
   auto need = [&](size_t k) -> size_t {
     size_t b = per_map * k;
-    if (precision == FSHT_PREC_SPLIT)   // two digit-tile buffers (Q and U, or two waves of T);
-      b += 2 * (fsht_split_ws_bytes(p, (int)k) + fsht_split_eb_bytes(p, (int)k)) +   // two
-           2 * p->lbuf_bytes;                                                          // lambda
+    if (precision == FSHT_PREC_SPLIT)   // digit tiles and their exponents, two lambda buffers
+      b += f_ws * (fsht_split_ws_bytes(p, (int)k) + fsht_split_eb_bytes(p, (int)k)) +
+           2 * p->lbuf_bytes;
     return b;
   };
   const bool tables_only = (flags & FSHT_FLAG_TABLES_ONLY) != 0;
@@ -322,7 +324,7 @@ int fsht_plan_create(int nside, int lmax, int nmaps_max, int flags, int precisio
     return fail(FSHT_ECUDA);
   }
   if (precision == FSHT_PREC_SPLIT && !tables_only) {
-    const size_t f = 2;   // Q and U digit tiles, or (spin 0) two waves in flight
+    const size_t f = f_ws;
     p->ws_bytes = f * fsht_split_ws_bytes(p, p->kchunk);
     if ((rc = dalloc((void**)&p->d_ws, p->ws_bytes))) return fail(rc);
     if ((rc = dalloc((void**)&p->d_eb, f * fsht_split_eb_bytes(p, p->kchunk)))) return fail(rc);
@@ -924,27 +926,59 @@ static int pol_analysis(fsht_plan* p, const double2* WQ, const double2* WU, doub
     fsht_set_error("spin-2 split analysis needs a plan created with FSHT_FLAG_POL");
     return FSHT_EUNSUPPORTED;
   }
-  unsigned char* wsq = p->d_ws;
-  unsigned char* wsu = p->d_ws + fsht_split_ws_bytes(p, kc);
-  int* ebq = p->d_eb;
-  int* ebu = p->d_eb + fsht_split_eb_bytes(p, kc) / sizeof(int);
   // every alm element of the chunk is written by one unit of the contraction (its first pass
   // stores, later passes add), so alm needs no clearing
   if (!started) FSHT_TRY(lam_start(p, fsht_launch_split_lambda_pol));
+  // Slicing of Q and U runs one wave ahead on the second auxiliary stream, as in the spin-0
+  // analysis: wave w's tiles of Q and U sit in quarters 2 (w & 1) and 2 (w & 1) + 1 of d_ws /
+  // d_eb (quarters 0 and 1 without the auxiliary streams).
+  const bool ahead = p->aux2 != nullptr && p->aux != nullptr;
+  const size_t ws1 = fsht_split_ws_bytes(p, kc);
+  const size_t eb1 = fsht_split_eb_bytes(p, kc) / sizeof(int);
+  auto quarter = [&](int w, int field) -> size_t {
+    return (ahead ? 2 * (size_t)(w & 1) : 0) + (size_t)field;
+  };
+  auto slice_on = [&](int w, cudaStream_t st) -> int {
+    FSHT_PROF_ON(FSHT_KCAT_SLICE, st);
+    FSHT_TRY(fsht_launch_split_slice(p, w, WQ, p->d_ws + quarter(w, 0) * ws1,
+                                     p->d_eb + quarter(w, 0) * eb1, kc, st));
+    return fsht_launch_split_slice(p, w, WU, p->d_ws + quarter(w, 1) * ws1,
+                                   p->d_eb + quarter(w, 1) * eb1, kc, st);
+  };
+  if (ahead) {
+    FSHT_CUDA_TRY(cudaEventRecord(p->evs[0], p->stream));
+    FSHT_CUDA_TRY(cudaStreamWaitEvent(p->aux2, p->evs[0], 0));
+    FSHT_TRY(slice_on(0, p->aux2));
+    FSHT_CUDA_TRY(cudaEventRecord(p->evs[2], p->aux2));
+  }
   for (int w = 0; w < p->nwaves; ++w) {
-    {
-      FSHT_PROF(FSHT_KCAT_SLICE);
-      FSHT_TRY(fsht_launch_split_slice(p, w, WQ, wsq, ebq, kc, p->stream));
-      FSHT_TRY(fsht_launch_split_slice(p, w, WU, wsu, ebu, kc, p->stream));
+    if (!ahead) {
+      FSHT_TRY(slice_on(w, p->stream));
+    } else {
+      if (w + 1 < p->nwaves) {
+        // the quarters of wave w + 1 were last read by the contraction of wave w - 1
+        if (w >= 1)
+          FSHT_CUDA_TRY(cudaStreamWaitEvent(p->aux2, p->ev[kEvDone + ((w + 1) & 1)], 0));
+        FSHT_TRY(slice_on(w + 1, p->aux2));
+        FSHT_CUDA_TRY(cudaEventRecord(p->evs[2 + ((w + 1) & 1)], p->aux2));
+      }
+      FSHT_CUDA_TRY(cudaStreamWaitEvent(p->stream, p->evs[2 + (w & 1)], 0));
     }
     unsigned char* lb = nullptr;
     FSHT_TRY(lam_ready(p, fsht_launch_split_lambda_pol, w, &lb));
     {
       FSHT_PROF(FSHT_KCAT_ANALYSIS);
-      FSHT_TRY(fsht_launch_split_gemm_pol(p, w, wsq, ebq, wsu, ebu, lb, almE, almB, nmaps,
+      FSHT_TRY(fsht_launch_split_gemm_pol(p, w, p->d_ws + quarter(w, 0) * ws1,
+                                          p->d_eb + quarter(w, 0) * eb1,
+                                          p->d_ws + quarter(w, 1) * ws1,
+                                          p->d_eb + quarter(w, 1) * eb1, lb, almE, almB, nmaps,
                                           c0, kc, accumulate, which, p->stream));
     }
     FSHT_TRY(lam_done(p, fsht_launch_split_lambda_pol, w));
+  }
+  if (ahead) {
+    FSHT_CUDA_TRY(cudaEventRecord(p->evs[1], p->aux2));
+    FSHT_CUDA_TRY(cudaStreamWaitEvent(p->stream, p->evs[1], 0));
   }
   return lam_finish(p);
 }
