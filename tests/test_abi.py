@@ -59,3 +59,21 @@ def test_null_plan_is_an_error(lib):
     rc = lib.fsht_t2alm(None, None, None, 1, 0, 0)
     assert rc == _lib.FSHT_EINVAL
     assert "plan" in _lib.last_error()
+
+
+def test_host_mapped_without_library_blocks(lib):
+    """Memory that fsht_host_alloc did not return is never read in place (no CUDA call is
+    needed to say so); a null output pointer is an argument error."""
+    import numpy as np
+    a = np.zeros(1000)
+    m = C.c_int(-1)
+    assert lib.fsht_host_mapped(C.c_void_p(a.ctypes.data), C.c_size_t(a.nbytes), C.byref(m)) == 0
+    assert m.value == 0
+    assert lib.fsht_host_mapped(None, C.c_size_t(8), C.byref(m)) == 0
+    assert m.value == 0
+    assert lib.fsht_host_mapped(C.c_void_p(a.ctypes.data), C.c_size_t(8), None) == _lib.FSHT_EINVAL
+
+
+def test_host_read_setter_needs_a_plan(lib):
+    assert lib.fsht_plan_set_host_read(None, 1) == _lib.FSHT_EINVAL
+    assert "plan" in _lib.last_error()
