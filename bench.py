@@ -596,9 +596,14 @@ def ours(args, rank, world, local):
         torch.cuda.empty_cache()
     # -------- one refinement step (niter = 1) in the split form, against the plain path
     # with the same niter on the first maps of the batch
+    ring_tab = sht.ring_skip()
     if args.precision == "split" and not args.no_fp64:
-        sr = SHT(nside, lmax, nmaps, niter=1, device=local, precision="split",
-                 workspace_limit=40 << 30)
+        # the refinement plan holds two phase matrices per map: the niter-0 split plan is
+        # released first so that it gets the library's default split workspace (two chunks
+        # of the 500-map batch, the recursion once per chunk and pass)
+        sht.close()
+        torch.cuda.empty_cache()
+        sr = SHT(nside, lmax, nmaps, niter=1, device=local, precision="split")
         ms_r, out_r, pk_r, _, _, _ = timed_steps(lib, sr, maps, 1, 1, world, dist, dev, local,
                                                  sample_clocks=False)
         sr.close()
@@ -624,7 +629,7 @@ def ours(args, rank, world, local):
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         k = min(args.cpu_maps, nmaps)
         maps_np = np.asfortranarray(maps[:, :k].cpu().numpy())
-        cb, alm_ref = cpu_baseline(nside, lmax, nmaps, k, maps_np, sht.ring_skip(),
+        cb, alm_ref = cpu_baseline(nside, lmax, nmaps, k, maps_np, ring_tab,
                                    want_alm=True)
         line["cpu_baseline"] = cb
         got = out[:k].cpu().numpy()
