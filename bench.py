@@ -723,8 +723,8 @@ def _e2e_run(sht, maps_dev, ke, args, world, local):
         _lib.call("fsht_plan_set_host_read", sht._plan, 1 if mode0 == "direct" else 0)
         sht.host_read = mode0
     # the same pinned buffers copied by torch (first 64 maps): a reference for the host link's
-    # rate; the library's own copies are cudaMemcpyAsync calls on its copy stream, which on
-    # some boxes run several times faster than torch's copy of the same memory
+    # rate beside the library's own transfers (in-place reads by the FFT, or cudaMemcpyAsync
+    # calls on its copy stream)
     kc = min(ke, 64)
     dmaps = torch.empty((kc, npix), dtype=torch.float64, device=maps_dev.device)
     dalm = torch.empty((kc, L * L), dtype=torch.float64, device=maps_dev.device)
