@@ -17,6 +17,7 @@ FSHT_ENOMEM = -2
 FSHT_ECUDA = -3
 FSHT_ETIMEOUT = -4
 FSHT_EUNSUPPORTED = -5
+FSHT_ERANGE = -6
 FSHT_PREC_FP64 = 0
 FSHT_PREC_SPLIT = 1
 FSHT_FLAG_POL = 1
@@ -71,6 +72,7 @@ SIGNATURES = {
     "fsht_profile_read": [_vp, _i, C.POINTER(_i), C.POINTER(C.c_double)],
     "fsht_measure_fp64_peak": [C.POINTER(C.c_double)],
     "fsht_measure_fp32_peak": [C.POINTER(C.c_double)],
+    "fsht_measure_dmma_peak": [C.POINTER(C.c_double)],
     "fsht_last_error": [C.c_char_p, _sz],
     "fsht_batch_create": [C.c_void_p, _i, _i, _sz, _i, _vp, C.POINTER(_vp)],
     "fsht_batch_run": [_vp],

@@ -1,5 +1,5 @@
-// Measurement helpers: FP64 and FP32 FMA throughput of the current device, the roofline
-// denominators of the plain-FP64 kernels and of the df64 ring FFT.
+// Measurement helpers: FP64 and FP32 FMA and FP64 tensor-core (DMMA) throughput of the current
+// device, the roofline denominators of the plain-FP64 kernels and of the df64 ring FFT.
 #include "common.cuh"
 
 namespace {
@@ -92,6 +92,68 @@ extern "C" int fsht_measure_fp32_peak(double* tflops) {
   return FSHT_OK;
 }
 
+// FP64 tensor-core (DMMA) throughput (TFLOP/s): a loop of mma.sync.m8n8k4 FP64 products with
+// four independent accumulators per warp.  The plain path's contraction is written for the
+// FP64 FMA pipe because this figure is below fsht_measure_fp64_peak's on GB300; measuring both
+// in every run keeps that choice checkable.
+namespace {
+__global__ void k_dmma_loop(double* out, int iters, double a, double b) {
+  double acc[4][2];
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    acc[j][0] = threadIdx.x + j;
+    acc[j][1] = threadIdx.x - j;
+  }
+  const double fa = a + 1e-9 * threadIdx.x, fb = b;
+  for (int i = 0; i < iters; ++i) {
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+      asm volatile(
+          "mma.sync.aligned.m8n8k4.row.col.f64.f64.f64.f64 {%0, %1}, {%2}, {%3}, {%0, %1};"
+          : "+d"(acc[j][0]), "+d"(acc[j][1])
+          : "d"(fa), "d"(fb));
+  }
+  double s = 0.0;
+#pragma unroll
+  for (int j = 0; j < 4; ++j) s += acc[j][0] + acc[j][1];
+  out[blockIdx.x * blockDim.x + threadIdx.x] = s;
+}
+}  // namespace
+
+extern "C" int fsht_measure_dmma_peak(double* tflops) {
+  if (!tflops) {
+    fsht_set_error("null output");
+    return FSHT_EINVAL;
+  }
+  int dev = 0, nsm = 0;
+  FSHT_CUDA_TRY(cudaGetDevice(&dev));
+  FSHT_CUDA_TRY(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+  const int blocks = nsm * 8, threads = 256, iters = 2000;
+  double* out = nullptr;
+  FSHT_CUDA_TRY(cudaMalloc(&out, sizeof(double) * blocks * threads));
+  cudaEvent_t e0, e1;
+  FSHT_CUDA_TRY(cudaEventCreate(&e0));
+  FSHT_CUDA_TRY(cudaEventCreate(&e1));
+  float best = 1e30f;
+  for (int rep = 0; rep < 3; ++rep) {
+    FSHT_CUDA_TRY(cudaEventRecord(e0, 0));
+    k_dmma_loop<<<blocks, threads>>>(out, iters, 1.0 - 1e-6, 1e-3);
+    FSHT_LAUNCH_CHECK();
+    FSHT_CUDA_TRY(cudaEventRecord(e1, 0));
+    FSHT_CUDA_TRY(cudaEventSynchronize(e1));
+    float ms = 0.f;
+    FSHT_CUDA_TRY(cudaEventElapsedTime(&ms, e0, e1));
+    if (ms < best) best = ms;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(out);
+  // one m8n8k4 product per warp = 8 * 8 * 4 FMAs = 512 flop
+  const double warps = (double)blocks * threads / 32.0;
+  *tflops = 512.0 * 4 * (double)iters * warps / (best * 1e-3) / 1e12;
+  return FSHT_OK;
+}
+
 // ---------------------------------------------------------------- wait self-test
 // One thread waits, with the kernels' bounded mbarrier wait, on a barrier that nothing
 // arrives on: the wait gives up after its iteration limit (about a second), and the
@@ -110,7 +172,7 @@ __global__ void k_wait_selftest(int* err) {
   }
   __syncthreads();
   if (threadIdx.x == 0) {
-    if (!tc::mbar_wait(&bar, 0, &abort_flag)) atomicOr(err, 1);
+    if (!tc::mbar_wait(&bar, 0, &abort_flag)) atomicOr(err, tc::kErrTimeout);
     tc::mbar_arrive(&bar);   // leave the barrier completed before the CTA exits
   }
 }

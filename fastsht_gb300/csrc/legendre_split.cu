@@ -45,6 +45,7 @@ struct SliceArgs {
   const int* ring_i0;
   unsigned char* WS;
   int* EB;
+  int* err;              // plan error word (kErrRange when a value misses its scale)
 };
 
 // grid (q in wave, 2 x group), 256 threads = (ring half, map, parity, Re/Im) over one half
@@ -93,6 +94,7 @@ __global__ void __launch_bounds__(256, 4) k_slice_phase(SliceArgs a) {
   if (!half) a.EB[(((long long)qi * 2 + p) * a.ngroups + g) * kCols + c] = E;
   unsigned char* base = a.WS + ((size_t)(qi * 2 + p) * a.ngroups + g) * a.row_bytes +
                         (c >> 3) * 256 + (c & 7) * 16;
+  bool bad = false;
   for (int ts = ks_begin; ts < ks_end; ++ts) {
     // the k-step's 16 loads issued together (the column is not in L2 any more)
     double v[kKStep];
@@ -104,7 +106,7 @@ __global__ void __launch_bounds__(256, 4) k_slice_phase(SliceArgs a) {
 #pragma unroll
       for (int j = 0; j < 8; ++j) {
         uint16_t q4[4] = {0, 0, 0, 0};
-        if (E != kEmptyExp) tc::digits4(v[hh * 8 + j], E, q4);
+        if (E != kEmptyExp) bad |= tc::digits4(v[hh * 8 + j], E, q4);
         for (int d = 0; d < kSlices; ++d) sl[d][j] = q4[d];
       }
       for (int d = 0; d < kSlices; ++d) {
@@ -117,6 +119,7 @@ __global__ void __launch_bounds__(256, 4) k_slice_phase(SliceArgs a) {
       }
     }
   }
+  if (bad) atomicOr(a.err, tc::kErrRange);
 }
 
 // ------------------------------------------------------------------ lambda digits
@@ -167,6 +170,7 @@ struct LamArgs {
   const FshtLamRow* tab;
   const long long* lam_off;
   unsigned char* lbuf;
+  int* err;
 };
 
 constexpr int kLamBlock = 32;                 // l per staging block (16 rows per parity)
@@ -206,6 +210,7 @@ __global__ void __launch_bounds__(128) k_lambda_digits(LamArgs a) {
   }
   __syncthreads();
   const int lend = ntiles * 2 * kRows;
+  bool bad = false;
   for (int lb = 0; lb < lend; lb += kLamBlock) {
 #pragma unroll 4
     for (int jj = 0; jj < kLamBlock; ++jj) {
@@ -222,7 +227,7 @@ __global__ void __launch_bounds__(128) k_lambda_digits(LamArgs a) {
         }
         if (valid) {
           uint16_t d[4];
-          tc::digits4(s1, erow - et, d);
+          bad |= tc::digits4(s1, erow - et, d);
           pk = (unsigned long long)d[0] | ((unsigned long long)d[1] << 16) |
                ((unsigned long long)d[2] << 32) | ((unsigned long long)d[3] << 48);
         }
@@ -283,6 +288,7 @@ __global__ void __launch_bounds__(128) k_lambda_digits(LamArgs a) {
     }
     __syncthreads();
   }
+  if (bad) atomicOr(a.err, tc::kErrRange);
 }
 
 // ------------------------------------------------------------------ split GEMM
@@ -525,7 +531,7 @@ __global__ void __launch_bounds__(kThreadsG, 1) k_split_gemm(GemmArgs a) {
   tc::tc_fence_before();
   __syncthreads();
   if (warp == 0) tc::tmem_dealloc(tmem, 512);
-  if (tid == 0 && h.abort) atomicOr(a.err, 1);
+  if (tid == 0 && h.abort) atomicOr(a.err, tc::kErrTimeout);
 }
 
 
@@ -548,6 +554,7 @@ struct LamTArgs {
   const FshtLamRow* tab;
   const long long* lam_offT;
   unsigned char* lbuf;
+  int* err;
 };
 
 __global__ void __launch_bounds__(128) k_lambda_digits_T(LamTArgs a) {
@@ -575,6 +582,7 @@ __global__ void __launch_bounds__(128) k_lambda_digits_T(LamTArgs a) {
     et = 600 * e;
   }
   __shared__ FshtLamRow s_tab[32];
+  bool bad = false;
   for (int kl = 0; kl < nkl; ++kl) {
     __syncthreads();                      // the previous block's rows are no longer read
     if (tid < 32 && m + kl * 32 + tid <= a.lmax) s_tab[tid] = tab[kl * 32 + tid];
@@ -600,7 +608,7 @@ __global__ void __launch_bounds__(128) k_lambda_digits_T(LamTArgs a) {
             s2 = s1;
             s1 = nx;
           }
-          if (valid) tc::digits4(s1 * rw.dm, a.eag - et - rw.dx, d);
+          if (valid) bad |= tc::digits4(s1 * rw.dm, a.eag - et - rw.dx, d);
         }
         const int par = jj & 1, slot = jj >> 1;
 #pragma unroll
@@ -632,6 +640,7 @@ __global__ void __launch_bounds__(128) k_lambda_digits_T(LamTArgs a) {
       et -= 600;
     }
   }
+  if (bad) atomicOr(a.err, tc::kErrRange);
 }
 
 // alm -> digit tiles: grid (m, parity, group), 128 threads = columns (map = c & 63,
@@ -642,6 +651,7 @@ struct SliceAArgs {
   size_t row_bytes;
   unsigned char* WS;
   int* EB;
+  int* err;
 };
 
 __global__ void __launch_bounds__(128) k_slice_alm(SliceAArgs a) {
@@ -668,12 +678,13 @@ __global__ void __launch_bounds__(128) k_slice_alm(SliceAArgs a) {
   unsigned char* base = a.WS +
                         ((size_t)(qi * 2 + p) * a.ngroups + g) * a.row_bytes +
                         (c >> 3) * 256 + (c & 7) * 16;
+  bool bad = false;
   for (int kl = 0; kl < nkl; ++kl) {
     for (int half = 0; half < 2; ++half) {
       uint16_t sl[kSynthPlanes][8];
       for (int j = 0; j < 8; ++j) {
         uint16_t q4[4] = {0, 0, 0, 0};
-        if (E != kEmptyExp) tc::digits4(val(kl * kKStep + half * 8 + j), E, q4);
+        if (E != kEmptyExp) bad |= tc::digits4(val(kl * kKStep + half * 8 + j), E, q4);
         for (int d = 0; d < kSlices; ++d) sl[d][j] = q4[d];
         for (int d = 1; d < kSlices; ++d) sl[kSlices - 1 + d][j] = tc::bf16_scale_2m8(q4[d]);
       }
@@ -688,6 +699,7 @@ __global__ void __launch_bounds__(128) k_slice_alm(SliceAArgs a) {
       }
     }
   }
+  if (bad) atomicOr(a.err, tc::kErrRange);
 }
 
 // CTA = (64-map group, 128-ring block x l-chunk, q): both parities in turn through the same
@@ -929,7 +941,7 @@ __global__ void __launch_bounds__(kThreadsG, 1) k_split_synth(SynthArgs a) {
   tc::tc_fence_before();
   __syncthreads();
   if (warp == 0) tc::tmem_dealloc(tmem, 512);
-  if (tid == 0 && h.abort) atomicOr(a.err, 1);
+  if (tid == 0 && h.abort) atomicOr(a.err, tc::kErrTimeout);
 }
 
 }  // namespace
@@ -959,6 +971,7 @@ int fsht_launch_split_slice(fsht_plan* p, int w, const double2* W, unsigned char
   sa.ring_i0 = p->d_ring_i0;
   sa.WS = WS;
   sa.EB = EB;
+  sa.err = p->d_err;
   k_slice_phase<<<dim3(wv[1] - wv[0], 2 * sa.ngroups), 256, 0, s>>>(sa);
   FSHT_LAUNCH_CHECK();
   return FSHT_OK;
@@ -1057,6 +1070,7 @@ int fsht_launch_split_lambda(fsht_plan* p, int w, unsigned char* lbuf, cudaStrea
   a.tab = p->d_lamtab;
   a.lam_off = p->d_lam_off;
   a.lbuf = lbuf;
+  a.err = p->d_err;
   if (wv[4] == 0) return FSHT_OK;
   k_lambda_digits<<<dim3(wv[1] - wv[0], wv[4]), 128, 0, s>>>(a);
   FSHT_LAUNCH_CHECK();
@@ -1115,6 +1129,7 @@ int fsht_launch_split_slice_alm(fsht_plan* p, int w, const double* alm, unsigned
   a.row_bytes = ws_row_bytes(p->lmax, p->nnorth);
   a.WS = WS;
   a.EB = EB;
+  a.err = p->d_err;
   k_slice_alm<<<dim3(wv[1] - wv[0], 2, a.ngroups), 128, 0, s>>>(a);
   FSHT_LAUNCH_CHECK();
   return FSHT_OK;
@@ -1135,6 +1150,7 @@ int fsht_launch_split_lambdaT(fsht_plan* p, int w, unsigned char* lbuf, cudaStre
   a.tab = p->d_lamtab;
   a.lam_offT = p->d_lam_offT;
   a.lbuf = lbuf;
+  a.err = p->d_err;
   k_lambda_digits_T<<<dim3(wv[1] - wv[0], wv[4]), 128, 0, s>>>(a);
   FSHT_LAUNCH_CHECK();
   return FSHT_OK;

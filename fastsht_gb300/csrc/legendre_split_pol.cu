@@ -68,6 +68,7 @@ struct LamPArgs {
   const FshtPolRow* ptab;
   const long long* lam_off;
   unsigned char* lbuf;
+  int* err;
 };
 
 constexpr int kPolBlock = 32;                 // l per staging block
@@ -120,6 +121,7 @@ __global__ void __launch_bounds__(128) k_lambda_digits_pol(LamPArgs a) {
   auto Sidx = [&](int part, int par, int row, int col) -> unsigned long long& {
     return S[((part * 2 + par) * (kPolBlock / 2) + row) * kPolStride + col];
   };
+  bool bad = false;
   for (int lb = 0; lb < lend; lb += kPolBlock) {
 #pragma unroll 2
     for (int jj = 0; jj < kPolBlock; ++jj) {
@@ -138,10 +140,10 @@ __global__ void __launch_bounds__(128) k_lambda_digits_pol(LamPArgs a) {
           const double l1 = fma(u, b_w, -s1 * fma(c.c2, inv_s2, c.c3));
           const double l2 = fma(-s1, c.c4 * x, u) * c_w;
           uint16_t d[4];
-          tc::digits4(l1, s_erow[jj] - et, d);
+          bad |= tc::digits4(l1, s_erow[jj] - et, d);
           pk1 = (unsigned long long)d[0] | ((unsigned long long)d[1] << 16) |
                 ((unsigned long long)d[2] << 32) | ((unsigned long long)d[3] << 48);
-          tc::digits4(l2, s_erow[jj] - et, d);
+          bad |= tc::digits4(l2, s_erow[jj] - et, d);
           pk2 = (unsigned long long)d[0] | ((unsigned long long)d[1] << 16) |
                 ((unsigned long long)d[2] << 32) | ((unsigned long long)d[3] << 48);
         }
@@ -198,6 +200,7 @@ __global__ void __launch_bounds__(128) k_lambda_digits_pol(LamPArgs a) {
     stage(lb + kPolBlock);
     __syncthreads();
   }
+  if (bad) atomicOr(a.err, tc::kErrRange);
 }
 
 // Persistent, like k_split_gemm: one CTA per SM walks work units (q, l-tile, parity, field
@@ -461,7 +464,7 @@ __global__ void __launch_bounds__(kThreadsG, 1) k_split_gemm_pol(GemmPArgs a) {
   tc::tc_fence_before();
   __syncthreads();
   if (warp == 0) tc::tmem_dealloc(tmem, 512);
-  if (tid == 0 && h.abort) atomicOr(a.err, 1);
+  if (tid == 0 && h.abort) atomicOr(a.err, tc::kErrTimeout);
 }
 
 // ------------------------------------------------------------------ spin-2 synthesis
@@ -483,6 +486,7 @@ struct LamTPArgs {
   const FshtPolRow* ptab;
   const long long* lam_offT;
   unsigned char* lbuf;
+  int* err;
 };
 
 __global__ void __launch_bounds__(128) k_lambda_digits_T_pol(LamTPArgs a) {
@@ -516,6 +520,7 @@ __global__ void __launch_bounds__(128) k_lambda_digits_T_pol(LamTPArgs a) {
     rec_seed(sth, a.pref[m], m, s1, e);
     et = 600 * e;
   }
+  bool bad = false;
   for (int kl = 0; kl < nkl; ++kl) {
     __syncthreads();
     if (tid < 32 && m + kl * 32 + tid <= a.lmax) {
@@ -551,8 +556,8 @@ __global__ void __launch_bounds__(128) k_lambda_digits_T_pol(LamTPArgs a) {
             const double u = s2 * c.c1;
             const double l1 = fma(u, b_w, -s1 * fma(c.c2, inv_s2, c.c3));
             const double l2 = fma(-s1, c.c4 * x, u) * c_w;
-            tc::digits4(l1 * rw.dm, a.eag - et - rw.dx, d1);
-            tc::digits4(l2 * rw.dm, a.eag - et - rw.dx, d2);
+            bad |= tc::digits4(l1 * rw.dm, a.eag - et - rw.dx, d1);
+            bad |= tc::digits4(l2 * rw.dm, a.eag - et - rw.dx, d2);
           }
         }
         const int par = jj & 1, slot = jj >> 1;
@@ -590,6 +595,7 @@ __global__ void __launch_bounds__(128) k_lambda_digits_T_pol(LamTPArgs a) {
       et -= 600;
     }
   }
+  if (bad) atomicOr(a.err, tc::kErrRange);
 }
 
 // CTA = (group, ring block x l-chunk x field (Q, U), q): four passes through the same TMEM
@@ -876,7 +882,7 @@ __global__ void __launch_bounds__(kThreadsG, 1) k_split_synth_pol(SynthPArgs a) 
   tc::tc_fence_before();
   __syncthreads();
   if (warp == 0) tc::tmem_dealloc(tmem, 512);
-  if (tid == 0 && h.abort) atomicOr(a.err, 1);
+  if (tid == 0 && h.abort) atomicOr(a.err, tc::kErrTimeout);
 }
 
 }  // namespace
@@ -905,6 +911,7 @@ int fsht_launch_split_lambda_pol(fsht_plan* p, int w, unsigned char* lbuf, cudaS
   a.ptab = p->d_poltab;
   a.lam_off = p->d_lam_off;
   a.lbuf = lbuf;
+  a.err = p->d_err;
   FSHT_CUDA_TRY(cudaFuncSetAttribute(k_lambda_digits_pol,
                                      cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      (int)kPolStageBytes));
@@ -973,6 +980,7 @@ int fsht_launch_split_lambdaT_pol(fsht_plan* p, int w, unsigned char* lbuf, cuda
   a.ptab = p->d_poltab;
   a.lam_offT = p->d_lam_offT;
   a.lbuf = lbuf;
+  a.err = p->d_err;
   k_lambda_digits_T_pol<<<dim3(wv[1] - wv[0], wv[4]), 128, 0, s>>>(a);
   FSHT_LAUNCH_CHECK();
   return FSHT_OK;

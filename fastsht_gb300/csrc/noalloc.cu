@@ -25,8 +25,10 @@
 
 namespace {
 
-// 32 MiB: enough for nside <= 128 at lmax = 4 nside (one map per pass) and for
-// many maps per pass at the sizes below that.
+// 32 MiB: enough for every nside <= 256 at any lmax <= 4 nside (nside 256 at lmax 1024
+// runs one map per pass, about 6.7 MiB of tables plus 16 MiB of phase matrix), for many
+// maps per pass below that, and for nside 512 up to lmax 167 (the FFT tables alone take
+// about 26.7 MiB there).  Every other size is rejected with FSHT_EUNSUPPORTED.
 constexpr size_t kNoAllocScratchBytes = 32ull << 20;
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
 
@@ -136,8 +138,8 @@ int scratch_address(void** out) {
 
 extern "C" int fsht_t2alm_noalloc(int nside, int lmax, const double* maps, double* alm,
                                   int nmaps, void* stream) {
-  if (nside < 1 || (nside & (nside - 1)) || nside > 1024) {
-    fsht_set_error("t2alm_noalloc: nside = %d must be a power of two in [1, 1024]", nside);
+  if (nside < 1 || (nside & (nside - 1)) || nside > 2048) {
+    fsht_set_error("t2alm_noalloc: nside = %d must be a power of two in [1, 2048]", nside);
     return FSHT_EINVAL;
   }
   if (lmax < 0 || lmax > 4 * nside) {

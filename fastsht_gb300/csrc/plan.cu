@@ -6,6 +6,7 @@
 // FFT tables and the phase-matrix workspace all live in one object bound to a
 // CUDA stream, so independent plans can run concurrently.
 #include "common.cuh"
+#include "tcgen05.cuh"
 
 #include <cmath>
 #include <cstdarg>
@@ -531,9 +532,14 @@ int fsht_plan_check(fsht_plan* p) {
   FSHT_CUDA_TRY(cudaMemcpy(&err, p->d_err, sizeof(int), cudaMemcpyDeviceToHost));
   if (err) {
     FSHT_CUDA_TRY(cudaMemset(p->d_err, 0, sizeof(int)));
-    fsht_set_error("a bounded device-side wait expired (error word %d); results are invalid",
-                   err);
-    return FSHT_ETIMEOUT;
+    if (err & tc::kErrTimeout) {
+      fsht_set_error("a bounded device-side wait expired (error word %d); results are invalid",
+                     err);
+      return FSHT_ETIMEOUT;
+    }
+    fsht_set_error("a value fell outside its digit scale in the split form (error word %d: "
+                   "non-finite input?); results are invalid", err);
+    return FSHT_ERANGE;
   }
   return FSHT_OK;
 }

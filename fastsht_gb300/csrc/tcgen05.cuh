@@ -147,15 +147,25 @@ __device__ __forceinline__ uint16_t bf16_of_int(int d) {
 __device__ __forceinline__ uint16_t bf16_scale_2m8(uint16_t h) {
   return (h & 0x7FFF) ? (uint16_t)(h - (8u << 7)) : h;
 }
-__device__ __forceinline__ void digits4(double v, int E, uint16_t (&s)[4]) {
+// Returns true when v does not fit its scale (|v| >= 2^E, or v is not finite): the digits
+// are then saturated (or zero for a non-finite v) and the caller raises the plan's error
+// word (kErrRange), so a wrong result never passes silently.
+constexpr int kErrTimeout = 1;   // error-word bit: a bounded wait expired
+constexpr int kErrRange = 2;     // error-word bit: a value fell outside its digit scale
+__device__ __forceinline__ bool digits4(double v, int E, uint16_t (&s)[4]) {
   const unsigned long long bits = (unsigned long long)__double_as_longlong(v);
   const int eb = (int)((bits >> 52) & 0x7FF);
   long long T = 0;
+  bool out_of_range = eb == 0x7FF;
   if (eb != 0 && eb != 0x7FF) {
     const unsigned long long mant = (bits & ((1ull << 52) - 1)) | (1ull << 52);
     const int sh = E - (eb - 1023) + 22;      // >= 23 when |v| < 2^E
-    if (sh < 23) T = 1ll << 30;               // out of range: saturate (never for valid scales)
-    else if (sh < 64) T = (long long)((mant + (1ull << (sh - 1))) >> sh);
+    if (sh < 23) {                            // out of range: saturate and report
+      T = 1ll << 30;
+      out_of_range = true;
+    } else if (sh < 64) {
+      T = (long long)((mant + (1ull << (sh - 1))) >> sh);
+    }
   }
   const int neg = (bits >> 63) ? -1 : 1;
   int d[4];
@@ -168,6 +178,7 @@ __device__ __forceinline__ void digits4(double v, int E, uint16_t (&s)[4]) {
   d[0] = (int)T;
 #pragma unroll
   for (int j = 0; j < 4; ++j) s[j] = bf16_of_int(neg * d[j]);
+  return out_of_range;
 }
 
 }  // namespace tc

@@ -48,20 +48,15 @@ def pinned_empty(shape, order="F"):
     return arr
 
 
-def _pinned_empty_fortran(shape, dtype=torch.float64):
-    """Pinned host array with Fortran layout, returned as a NumPy array."""
-    return pinned_empty(shape, order="F")
-
-
 class SHT:
     """Batched spherical-harmonic transforms of ``nsim`` HEALPix maps.
 
     SHT(nside, lmax, nsim, niter=0, pol=False, all_buff=False) as in the
     reference (SHT.py:17).  Extra keywords: ``device`` (CUDA device index),
     ``workspace_limit`` (bytes of workspace, 0 = library default) and ``precision``:
-    "fp64" (the plain method, all FP64) or "split" (the temperature Legendre
-    contractions of t2alm and alm2t as BF16 digit products on the tensor cores, ~3e-8 max
-    relative alm error; niter > 0 refines with the FP64 Fourier-space residual).
+    "fp64" (the plain method, all FP64) or "split" (the Legendre contractions of t2alm,
+    alm2t, qu2eb / qu2e / qu2b and eb2qu as BF16 digit products on the tensor cores, ~3e-8
+    max relative alm error; niter > 0 refines with the FP64 Fourier-space residual).
     ``host_read``: how t2alm takes NumPy maps that sit in a ``pinned_empty`` buffer -
     "direct" (read in place by the FFT over the host link) or "staged" (copied to device
     memory first); the results are the same.
@@ -189,7 +184,7 @@ class SHT:
             return 0
         if as_torch:
             return dev.permute(2, 1, 0)
-        out = _pinned_empty_fortran((self.nsim, self.lmax + 1, self.lmax + 1))
+        out = pinned_empty((self.nsim, self.lmax + 1, self.lmax + 1))
         torch.from_numpy(out.T).copy_(dev, non_blocking=False)
         return out
 
@@ -204,7 +199,7 @@ class SHT:
             return 0
         if as_torch:
             return dev.T
-        out = _pinned_empty_fortran((self.npix, self.nsim))
+        out = pinned_empty((self.npix, self.nsim))
         torch.from_numpy(out.T).copy_(dev, non_blocking=False)
         return out
 
@@ -270,7 +265,7 @@ class SHT:
             raise ValueError(f"maps: expected shape ({self.npix}, {self.nsim}), got {a.shape}")
         a = np.asfortranarray(a, dtype=np.float64)
         L = self.lmax + 1
-        out = np.asarray(alms_in) if alms_in is not None else _pinned_empty_fortran((self.nsim, L, L))
+        out = np.asarray(alms_in) if alms_in is not None else pinned_empty((self.nsim, L, L))
         # device staging buffers of the host path, kept between calls (like the reference's
         # persistent device arrays); the alm buffer is also what get_alms() reads, the maps
         # buffer is only made for maps that are not read in place
@@ -431,6 +426,6 @@ class SHT:
             out[vid] = y - a0 - a1 * x
             if as_torch:
                 return out
-            res = _pinned_empty_fortran((self.npix, self.nsim))
+            res = pinned_empty((self.npix, self.nsim))
             torch.from_numpy(res.T).copy_(out.T)
             return res

@@ -35,7 +35,9 @@ enum {
   FSHT_ENOMEM = -2,       /* device allocation failed                          */
   FSHT_ECUDA = -3,        /* CUDA runtime error (message in fsht_last_error)   */
   FSHT_ETIMEOUT = -4,     /* a bounded device-side wait expired                */
-  FSHT_EUNSUPPORTED = -5  /* size or mode outside what this build supports     */
+  FSHT_EUNSUPPORTED = -5, /* size or mode outside what this build supports     */
+  FSHT_ERANGE = -6        /* split form: a value missed its digit scale (e.g. a
+                             non-finite input); the results of that work are invalid */
 };
 
 enum { FSHT_PREC_FP64 = 0, FSHT_PREC_SPLIT = 1 };
@@ -53,9 +55,10 @@ enum { FSHT_FLAG_POL = 1, FSHT_FLAG_ITER = 2, FSHT_FLAG_TABLES_ONLY = 4 };
  *   nmaps_max  largest nmaps a transform call on this plan will pass
  *   flags      FSHT_FLAG_POL for spin-2 (Q/U) transforms, FSHT_FLAG_ITER for
  *              niter > 0 (each doubles the workspace, like the reference's nbuff)
- *   precision  FSHT_PREC_FP64 (plain, all FP64) or FSHT_PREC_SPLIT (t2alm's Legendre
- *              contraction as BF16 slice products on the tensor cores, max relative
- *              alm error ~1e-9..1e-8 against FP64; other transforms stay FP64)
+ *   precision  FSHT_PREC_FP64 (plain, all FP64) or FSHT_PREC_SPLIT (the Legendre
+ *              contractions of t2alm, alm2t, qu2eb / qu2e / qu2b and eb2qu as BF16 slice
+ *              products on the tensor cores, the ring FFTs of t2alm in df64; max relative
+ *              alm error ~1e-9..3e-8 against FP64)
  *   workspace_limit_bytes  upper bound for the plan's workspace (0 = default 16 GiB,
  *              40 GiB for FSHT_PREC_SPLIT); maps are processed in chunks that fit.
  *   stream     cudaStream_t (NULL = legacy default stream) */
@@ -104,8 +107,10 @@ int fsht_alm2t(fsht_plan* plan, const double* alm, double* maps, int nmaps);
  * device memory for its own pool and gives plug-ins buffers but no right to
  * allocate, or a latency-critical loop where an allocation would synchronise the
  * device.  Scratch comes from one fixed 32 MiB array of device memory inside the
- * library (every GPU that loads the library holds it until exit), which covers
- * nside <= 256 at any lmax <= 4 nside; larger sizes return FSHT_EUNSUPPORTED.
+ * library (every GPU that loads the library holds it until exit).  A size is
+ * accepted when its tables plus one map's phase matrix fit in that array: every
+ * nside <= 256 at any lmax <= 4 nside, and nside 512 up to lmax 167; larger lmax
+ * at nside 512, and nside 1024 and 2048, return FSHT_EUNSUPPORTED.
  * maps / alm are device pointers (layouts as above); stream is a cudaStream_t.
  * The first call on a device looks up the scratch address with that device
  * current: make it before any stream capture.  Calls share the scratch, so calls
@@ -179,6 +184,10 @@ int fsht_measure_fp64_peak(double* tflops);
 /* The same for FP32 FMAs: the roofline denominator of the split form's ring FFT, which
  * runs in df64 (FP32-pair) arithmetic. */
 int fsht_measure_fp32_peak(double* tflops);
+/* The same for FP64 tensor-core products (mma.sync m8n8k4 f64, DMMA), the unit the reference's
+ * cuBLAS DGEMMs run on (src/sht_core.f90:51-57): on GB300 it is slower than the FP64 FMA
+ * pipe, which is why the plain contraction uses DFMA.  No counterpart in the reference. */
+int fsht_measure_dmma_peak(double* tflops);
 
 /* Runs one stage of the pipeline on device buffers (testing and profiling hook;
  * no counterpart in the reference, whose stages are internal):
@@ -245,9 +254,10 @@ int fsht_run_job(const fsht_plan* tables, const fsht_job* job, void* workspace,
 int fsht_plan_autotune(fsht_plan* plan, int sample_maps);
 int fsht_plan_tuning(const fsht_plan* plan, int* maps_per_block, int* threads);
 
-/* Blocks until the plan's stream is idle; returns FSHT_ECUDA on an async error and
+/* Blocks until the plan's stream is idle; returns FSHT_ECUDA on an async error,
  * FSHT_ETIMEOUT when a bounded device-side wait (split-precision kernels) expired since
- * the last check (the error word is then cleared). */
+ * the last check, and FSHT_ERANGE when a split-form kernel met a value outside its digit
+ * scale (a non-finite input) since the last check (the error word is then cleared). */
 int fsht_plan_sync(fsht_plan* plan);
 /* The error-word check of fsht_plan_sync without synchronising any stream: call it after
  * the work of interest is known to be complete (an event, fsht_batch_sync).  No

@@ -152,3 +152,29 @@ void oracle_plm_sphere(int m, int lmax, int nside, int i0, const double* cc_all,
   }
   (void)out0;
 }
+
+/*
+ * fft2mat_fast (src/fft_mapping.f90:19-68) in the reference's memory order, for the timed
+ * CPU baseline: the FFT bins b are (npix, nsim) with the map index fastest (the reference's
+ * fft(1:nsim, i1:i2) after its transposing FFT), and for each kept ring r the pair of bins
+ * (j[r], j[r] + 1) becomes one row of the FFT matrix:
+ *   mat1[r][k] = b[j[r]][k] f1[r] + b[j[r]+1][k] f2[r],
+ *   mat2[r][k] = b[j[r]][k] f3[r] + b[j[r]+1][k] f4[r].
+ * OpenMP over rings, like the reference's parallel loop (fft_mapping.f90:41).
+ */
+void oracle_fft2mat(int nsim, int rlen, const double* b, const long long* j, const double* f1,
+                    const double* f2, const double* f3, const double* f4, double* mat1,
+                    double* mat2) {
+#pragma omp parallel for schedule(static)
+  for (int r = 0; r < rlen; ++r) {
+    const double* x0 = b + (size_t)j[r] * nsim;
+    const double* x1 = x0 + nsim;
+    double* o1 = mat1 + (size_t)r * nsim;
+    double* o2 = mat2 + (size_t)r * nsim;
+    const double a1 = f1[r], a2 = f2[r], a3 = f3[r], a4 = f4[r];
+    for (int k = 0; k < nsim; ++k) {
+      o1[k] = x0[k] * a1 + x1[k] * a2;
+      o2[k] = x0[k] * a3 + x1[k] * a4;
+    }
+  }
+}

@@ -55,6 +55,9 @@ def c_recursion():
                                           dp, dp, ctypes.c_double, ctypes.c_int, ctypes.c_int,
                                           dp, dp, dp]
         lib.oracle_plm_sphere.restype = None
+        lib.oracle_fft2mat.argtypes = [ctypes.c_int, ctypes.c_int, dp,
+                                       ctypes.POINTER(ctypes.c_longlong), dp, dp, dp, dp, dp, dp]
+        lib.oracle_fft2mat.restype = None
         _CLIB = lib
     return _CLIB or None
 
@@ -581,6 +584,37 @@ class OracleSHT:
         mat1 = x0 * f1[jf] + x1 * f2[jf]
         mat2 = x0 * f3[jf] + x1 * f4[jf]
         return mat1, mat2                                   # (nsim, rlen), rings i0..i1
+
+    def fft2mat_tables(self, m):
+        """Per kept ring of order m: the first PERM bin and the four phase factors of
+        fft2mat_fast (the reference computes these once, fft2mat_compute_table,
+        sht_data_init.f90:438-492)."""
+        n, i0, rlen, i1, p1, p2 = self.locations(m)
+        tab, f1, f2, f3, f4 = self._fwd_table(m)
+        rings = np.arange(i0, self.nring - i0)
+        jf = self._mirror_index(rings)
+        j = np.ascontiguousarray(tab[rings], dtype=np.int64)
+        return j, [np.ascontiguousarray(f[jf], dtype=np.float64) for f in (f1, f2, f3, f4)]
+
+    def fft2mat_c(self, buffT, m, tables=None):
+        """fft2mat with the bins in the reference's memory order, buffT (npix, nsim) with the
+        map index fastest, by oracle/plm.c (OpenMP over rings, like fft_mapping.f90:41).
+        Returns (mat1, mat2) as (rlen, nsim) arrays: the transposes of fft2mat's.  `tables`:
+        fft2mat_tables(m), when computed beforehand."""
+        import ctypes
+        lib = c_recursion()
+        j, fs = tables if tables is not None else self.fft2mat_tables(m)
+        rlen = len(j)
+        nsim = buffT.shape[1]
+        b = np.ascontiguousarray(buffT)
+        mat1 = np.empty((rlen, nsim))
+        mat2 = np.empty((rlen, nsim))
+        dp = ctypes.POINTER(ctypes.c_double)
+        lib.oracle_fft2mat(nsim, rlen, b.ctypes.data_as(dp),
+                           j.ctypes.data_as(ctypes.POINTER(ctypes.c_longlong)),
+                           *[f.ctypes.data_as(dp) for f in fs],
+                           mat1.ctypes.data_as(dp), mat2.ctypes.data_as(dp))
+        return mat1, mat2
 
     # --- mat2fft_fast (src/fft_mapping.f90:84-128)
     def mat2fft(self, buff, mat1, mat2, m):

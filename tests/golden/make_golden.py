@@ -16,7 +16,9 @@ from pathlib import Path
 
 import numpy as np
 
-ref = Path(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+if len(sys.argv) != 2:
+    sys.exit("usage: make_golden.py <path of the reference tree>")
+ref = Path(sys.argv[1])
 out = Path(__file__).resolve().parent
 
 plm = {}

@@ -77,3 +77,23 @@ def test_host_mapped_without_library_blocks(lib):
 def test_host_read_setter_needs_a_plan(lib):
     assert lib.fsht_plan_set_host_read(None, 1) == _lib.FSHT_EINVAL
     assert "plan" in _lib.last_error()
+
+
+@pytest.mark.parametrize("nside,lmax,code", [
+    (512, 168, _lib.FSHT_EUNSUPPORTED),    # tables + one map above the fixed scratch
+    (1024, 64, _lib.FSHT_EUNSUPPORTED),
+    (2048, 64, _lib.FSHT_EUNSUPPORTED),    # half-length ring transforms: plan path only
+    (3, 8, _lib.FSHT_EINVAL),              # not a power of two
+    (8, 33, _lib.FSHT_EINVAL),             # lmax > 4 nside
+])
+def test_noalloc_rejects_sizes_before_any_device_work(lib, nside, lmax, code):
+    """The allocation-free analysis checks its size rule on the host first: these sizes are
+    refused without touching a device (the pointers are never used)."""
+    rc = lib.fsht_t2alm_noalloc(nside, lmax, C.c_void_p(16), C.c_void_p(16), 1, None)
+    assert rc == code
+    assert len(_lib.last_error()) > 0
+
+
+def test_range_status_is_declared():
+    assert "FSHT_ERANGE = -6" in HEADER.read_text()
+    assert _lib.FSHT_ERANGE == -6

@@ -208,3 +208,16 @@ def test_filt_and_norm_restatements():
     n = norm_alm(a, win, np.full(L, 0.25), 3.0)
     assert np.isclose(n[0, 4, 0], a[0, 4, 0] * win[4] * 3.0 + 0.25)
     assert np.isclose(n[0, 4, 1], a[0, 4, 1] * win[4] + 0.25)
+
+
+@pytest.mark.parametrize("ns,lmax,m", [(8, 23, 0), (8, 23, 5), (16, 47, 30), (32, 95, 95)])
+def test_c_gather_matches_numpy_fft2mat(ns, lmax, m):
+    """The C gather the CPU baseline times (reference memory order, map index fastest)
+    forms the same FFT matrix as the NumPy restatement of fft2mat_fast."""
+    o = OracleSHT(ns, lmax)
+    rng = np.random.default_rng(m)
+    maps = np.asfortranarray(rng.standard_normal((12 * ns * ns, 5)))
+    buff = o.map2fft(maps)                          # (nsim, npix)
+    m1, m2 = o.fft2mat(buff, m)                     # (nsim, rlen)
+    c1, c2 = o.fft2mat_c(np.ascontiguousarray(buff.T), m)
+    assert np.array_equal(c1, m1.T) and np.array_equal(c2, m2.T)

@@ -37,7 +37,8 @@ def lib():
     return _lib
 
 
-@pytest.mark.parametrize("nside,lmax,nmaps", [(8, 23, 3), (64, 191, 12), (256, 1024, 3)])
+@pytest.mark.parametrize("nside,lmax,nmaps", [(8, 23, 3), (64, 191, 12), (256, 1024, 3),
+                                              (512, 167, 2)])
 def test_noalloc_matches_plan_path_twice(lib, nside, lmax, nmaps):
     from fastsht_gb300 import SHT
     rng = np.random.default_rng(nside)
@@ -49,9 +50,15 @@ def test_noalloc_matches_plan_path_twice(lib, nside, lmax, nmaps):
     stream = torch.cuda.current_stream().cuda_stream
     for call in range(2):
         alm = torch.full((L, L, nmaps), float("nan"), dtype=torch.float64, device="cuda")
+        torch.cuda.synchronize()
+        free_before = torch.cuda.mem_get_info()[0]
         lib.call("fsht_t2alm_noalloc", nside, lmax, C.c_void_p(maps.data_ptr()),
                  C.c_void_p(alm.data_ptr()), nmaps, C.c_void_p(stream))
         torch.cuda.synchronize()
+        if call == 1:
+            # the point of the entry point: once its kernels are loaded (first call), a call
+            # takes no device memory at all
+            assert torch.cuda.mem_get_info()[0] == free_before
         got = alm.cpu().numpy()
         assert np.isfinite(got).all()
         err = _rel(np.moveaxis(got, 2, 0), np.moveaxis(want, 2, 0))
@@ -65,6 +72,10 @@ def test_noalloc_rejects_sizes_above_its_scratch(lib):
                  C.c_void_p(x.data_ptr()), 1, None)
     assert ei.value.code == lib.FSHT_EUNSUPPORTED
     assert "static scratch" in str(ei.value)
+    with pytest.raises(lib.FshtError) as ei:
+        lib.call("fsht_t2alm_noalloc", 2048, 64, C.c_void_p(x.data_ptr()),
+                 C.c_void_p(x.data_ptr()), 1, None)
+    assert ei.value.code == lib.FSHT_EUNSUPPORTED
     with pytest.raises(ValueError):
         lib.call("fsht_t2alm_noalloc", 12, 8, C.c_void_p(x.data_ptr()),
                  C.c_void_p(x.data_ptr()), 1, None)
