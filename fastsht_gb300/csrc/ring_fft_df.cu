@@ -179,6 +179,18 @@ __global__ void __launch_bounds__(1024, 1) k_ring_fft_fwd_df(FwdDfArgs a) {
       if (q >= n) q -= n;
       const cdd xN = cadd_lz(zq, zn);                          // 2 X_N
       const cdd xS = cmul_mi(csub_lz(zq, zn));                 // 2 X_S
+      if (!sflag) {
+        // phi0 = 0: the phase factor is the real 1/2, folded into the output exponent
+        if (equator) {
+          const double2 fN = cdd_to_fp64(xN, sh - 1);
+          w[0] = fN;
+          w[1] = fN;
+        } else {
+          w[0] = cdd_to_fp64(cadd_lz(xN, xS), sh - 1);
+          w[1] = cdd_to_fp64(csub_lz(xN, xS), sh - 1);
+        }
+        continue;
+      }
       const cdd p = ph[m];
       if (equator) {
         const double2 fN = cdd_to_fp64(cmul_lz(xN, p), sh);
