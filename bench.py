@@ -802,24 +802,38 @@ def _e2e_run(sht, maps_dev, ke, args, world, local):
     out_np = pinned_empty((ke, L, L))            # Fortran order
     out_t = torch.from_numpy(out_np.T)           # (L, L, ke) view
 
-    def timed(mode):
+    def timed(mode, detail):
         # host_read: "direct" = the FFT reads the pinned maps in place over the host link,
         # "staged" = the maps are copied to device memory in sub-batches first
+        import ctypes as C
         from fastsht_gb300 import _lib
         _lib.call("fsht_plan_set_host_read", sht._plan, 1 if mode == "direct" else 0)
         sht.host_read = mode
         sht.t2alm(maps_np, alms_in=out_np)       # warm-up
         torch.cuda.synchronize()
+        detail["device_free_gb"] = round(torch.cuda.mem_get_info()[0] / 1e9, 1)
         t0 = time.perf_counter()
         for _ in range(args.steps):
             sht.t2alm(maps_np, alms_in=out_np)
         torch.cuda.synchronize()
-        return time.perf_counter() - t0
+        dt = time.perf_counter() - t0
+        # one more step with the per-kernel CUDA-event profiler: where the step's time goes
+        _lib.load().fsht_profile_enable(sht._plan, 1)
+        _lib.call("fsht_profile_read", sht._plan, 0, None, None)
+        sht.t2alm(maps_np, alms_in=out_np)
+        cnt = (C.c_int * _lib.KCAT_COUNT)()
+        kms = (C.c_double * _lib.KCAT_COUNT)()
+        _lib.call("fsht_profile_read", sht._plan, _lib.KCAT_COUNT, cnt, kms)
+        _lib.load().fsht_profile_enable(sht._plan, 0)
+        detail["per_kernel_ms"] = {n: round(kms[i], 1) for i, n in enumerate(_lib.KCAT_NAMES)
+                                   if cnt[i]}
+        return dt
 
     mode0 = sht.host_read
+    det_staged, det_direct = {}, {}
     try:
-        dt_staged = timed("staged")
-        dt = timed("direct")
+        dt_staged = timed("staged", det_staged)
+        dt = timed("direct", det_direct)
     finally:
         from fastsht_gb300 import _lib
         _lib.call("fsht_plan_set_host_read", sht._plan, 1 if mode0 == "direct" else 0)
@@ -846,8 +860,10 @@ def _e2e_run(sht, maps_dev, ke, args, world, local):
             "maps_per_step": ke, "ms_per_step": 1000.0 * dt / args.steps,
             "host_read": ("direct: the forward FFT reads the pinned maps in place over the "
                           "host link (the API's default for pinned_empty buffers)"),
+            "detail": det_direct,
             "staged": {"value": world * ke * args.steps / dt_staged, "unit": UNIT,
                        "ms_per_step": 1000.0 * dt_staged / args.steps,
+                       "detail": det_staged,
                        "note": "host_read='staged': maps copied to device memory in "
                                "sub-batches, each transformed as it lands"},
             "host_cpus": ("the GPU's NUMA-local cores (%d)" % len(local)) if local else "default",

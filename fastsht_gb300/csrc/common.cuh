@@ -128,6 +128,7 @@ struct fsht_plan {
   float4* d_chirp_df;
   float4* d_bhat_df;
   float4* d_rtw_df;
+  float4* d_tw16_df;               // the df64 radix-16 passes' twiddles (fft_r16.cuh)
   int Pmax;                        // largest transform size (shared-memory sizing)
   int Tmax, logTmax, P3max;        // twiddle tables: largest power-of-two factor, largest 3*2^k size
   // workspace: phase matrices [m][i][k] x 2 complex, one per buffer

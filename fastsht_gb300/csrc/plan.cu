@@ -97,6 +97,7 @@ void free_plan_memory(fsht_plan* p) {
   cudaFree(p->d_chirp_df);
   cudaFree(p->d_bhat_df);
   cudaFree(p->d_rtw_df);
+  cudaFree(p->d_tw16_df);
   cudaFree(p->d_work);
   cudaFree(p->d_err);
   cudaFree(p->d_ws);

@@ -484,6 +484,12 @@ int fsht_fft_layout(int nside, int lmax, FshtFftLayout* lay, FshtRingFFT* rfs, i
       if (blue_rings) blue_rings[nblue] = i;
       ++nblue;
     }
+    if (r.P >= 8 && (r.P & 7)) {
+      // the df64 kernels' shared-memory swizzle permutes rows of eight elements; ring lengths
+      // 4 (i + 1) and 4 nside never give such a size (the smallest Bluestein size is 24)
+      fsht_set_error("ring %d: transform size %d is not a multiple of 8", i, r.P);
+      return FSHT_EUNSUPPORTED;
+    }
     if (r.P > Pmax) Pmax = r.P;
     if (r.logT > logTmax) logTmax = r.logT;
     if (r.r3 && r.P > P3max) P3max = r.P;

@@ -11,6 +11,7 @@
 // the split contraction's digit resolution (2^-31 of the column maximum).
 #include "common.cuh"
 #include "fft_passes.cuh"
+#include "fft_r16.cuh"
 
 #include <cmath>
 
@@ -23,7 +24,8 @@ struct FwdDfArgs {
   int k_off, k_cnt;         // the maps of this launch: [k_off, k_off + k_cnt)
   int nside, lmax, nnorth, nring, ring_base;
   const FshtRingFFT* rfs;
-  FftTwT<cdd> tw;
+  FftTwT<cdd> tw;            // tw.r3: the radix-3 twiddles
+  const cdd* tw16;           // the radix-16 passes' twiddles (fft_r16.cuh)
   const cdd* chirp;
   const cdd* bhat;
   const cdd* rtw;
@@ -67,7 +69,8 @@ __device__ __forceinline__ double dd_out(float h, float l, int sh) {
 // df64 scaled by 2^-sh (sh = that exponent, unbiased; 0 for an all-zero ring).  Thread t owns
 // slots t, t + nt, ... in both passes, so only the exponent needs a barrier.  emax is a
 // shared slot that is zero on entry.  Returns sh.
-__device__ __forceinline__ int load_scaled(cdd* buf, const Swz& S, int cnt, const double* xa,
+template <class Sw>
+__device__ __forceinline__ int load_scaled(cdd* buf, const Sw& S, int cnt, const double* xa,
                                            const double* xb, int stride, int* emax) {
   double2* raw = reinterpret_cast<double2*>(buf);
   const int tid = threadIdx.x, nt = blockDim.x;
@@ -90,12 +93,15 @@ __device__ __forceinline__ int load_scaled(cdd* buf, const Swz& S, int cnt, cons
   return sh;
 }
 
-__global__ void __launch_bounds__(1024, 1) k_ring_fft_fwd_df(FwdDfArgs a) {
+// NT threads per CTA (256: two CTAs per SM, 512: one), 128 registers a thread for the
+// radix-16 butterflies' sixteen df64 values.
+template <int NT>
+__global__ void __launch_bounds__(NT, 512 / NT) k_ring_fft_fwd_df(FwdDfArgs a) {
   extern __shared__ float4 smem4[];
   __shared__ int s_emax[2];
   const int i = a.ring_base + blockIdx.x;      // north ring index
   const FshtRingFFT rf = a.rfs[i];
-  const Swz S(rf);
+  const Swz16 S(rf);
   const int n = rf.n;
   cdd* buf = reinterpret_cast<cdd*>(smem4);    // rf.P entries
   cdd* ph = buf + rf.P;                        // lmax+1 phase factors exp(-i m phi0) / 2
@@ -133,7 +139,7 @@ __global__ void __launch_bounds__(1024, 1) k_ring_fft_fwd_df(FwdDfArgs a) {
         __syncthreads();
         if (tid == 0) s_emax[(it & 1) ^ 1] = 0;
         const int sh = load_scaled(buf, S, nd, x, x + 1, 2, &s_emax[it & 1]);
-        ring_dft(buf, rf, a.tw, chirp, bhat);
+        ring_dft16(buf, rf, S, a.tw16, a.tw.r3, chirp, bhat);
         for (int m = tid; m <= mtop; m += nt) {
           const int q = m % n;
           const bool cj = q > nd;
@@ -164,7 +170,7 @@ __global__ void __launch_bounds__(1024, 1) k_ring_fft_fwd_df(FwdDfArgs a) {
     __syncthreads();   // the previous map's readers of buf and of the other slot are done
     if (tid == 0) s_emax[(it & 1) ^ 1] = 0;
     const int sh = load_scaled(buf, S, n, xn, equator ? nullptr : xs, 1, &s_emax[it & 1]);
-    ring_dft(buf, rf, a.tw, chirp, bhat);
+    ring_dft16(buf, rf, S, a.tw16, a.tw.r3, chirp, bhat);
     // Z = FFT(x_N + i x_S): X_N[q] = (Z[q] + conj Z[-q])/2, X_S[q] = (Z[q] - conj Z[-q])/(2i)
     // q = m mod n and the output pointer advance by fixed steps (no division per m)
     const int qstep = nt % n;
@@ -212,7 +218,8 @@ struct InvDfArgs {
   int kc, maps_per_block;
   int nside, lmax, nnorth, nring, ring_base;
   const FshtRingFFT* rfs;
-  FftTwT<cdd> tw;
+  FftTwT<cdd> tw;           // tw.r3: the radix-3 twiddles
+  const cdd* tw16;          // the radix-16 passes' twiddles (fft_r16.cuh)
   const cdd* chirp;
   const cdd* bhat;
   const double2* rtw;       // FP64: the half-ring combination runs before the conversion
@@ -223,7 +230,8 @@ struct InvDfArgs {
 // ...) become df64 scaled by 2^-sh, sh from the block-wide largest exponent field (em = the
 // thread's own largest); conj: store the conjugate.  emax is a shared slot that is zero on
 // entry.  Returns sh.
-__device__ __forceinline__ int convert_scaled(cdd* buf, const Swz& S, int cnt, int em, int* emax,
+template <class Sw>
+__device__ __forceinline__ int convert_scaled(cdd* buf, const Sw& S, int cnt, int em, int* emax,
                                               bool conj) {
   const double2* raw = reinterpret_cast<const double2*>(buf);
   const int tid = threadIdx.x, nt = blockDim.x;
@@ -246,12 +254,13 @@ __device__ __forceinline__ int exp2f64(double2 v) {
 // Synthesis side of the split form: the spectrum of each ring pair is formed from G in FP64
 // (aliasing, x2, e^{+i m phi0}: O(lmax) per ring), scaled and converted to df64, transformed
 // as conj(DFT(conj Z)) in df64, and written to the maps with one FP64 addition per pixel.
-__global__ void __launch_bounds__(1024, 1) k_ring_fft_inv_df(InvDfArgs a) {
+template <int NT>
+__global__ void __launch_bounds__(NT, 512 / NT) k_ring_fft_inv_df(InvDfArgs a) {
   extern __shared__ float4 smem4[];
   __shared__ int s_emax[2];
   const int i = a.ring_base + blockIdx.x;
   const FshtRingFFT rf = a.rfs[i];
-  const Swz S(rf);
+  const Swz16 S(rf);
   const int n = rf.n;
   cdd* buf = reinterpret_cast<cdd*>(smem4);
   double2* raw = reinterpret_cast<double2*>(smem4);
@@ -300,7 +309,7 @@ __global__ void __launch_bounds__(1024, 1) k_ring_fft_inv_df(InvDfArgs a) {
           em = max(em, exp2f64(v));
         }
         const int sh = convert_scaled(buf, S, nd, em, &s_emax[it & 1], false);
-        ring_dft(buf, rf, a.tw, chirp, bhat);
+        ring_dft16(buf, rf, S, a.tw16, a.tw.r3, chirp, bhat);
         double* x = a.maps + (long long)k * a.map_stride + (side ? off_s : off_n);
         for (int j = tid; j < nd; j += nt) {
           const cdd z = buf[S(dft_bin(rf, j))];   // conj(z): x_{2j} = Re, x_{2j+1} = -Im
@@ -323,7 +332,7 @@ __global__ void __launch_bounds__(1024, 1) k_ring_fft_inv_df(InvDfArgs a) {
     }
     // inverse DFT = conj(DFT(conj Z))
     const int sh = convert_scaled(buf, S, n, em, &s_emax[it & 1], true);
-    ring_dft(buf, rf, a.tw, chirp, bhat);
+    ring_dft16(buf, rf, S, a.tw16, a.tw.r3, chirp, bhat);
     double* xn = a.maps + (long long)k * a.map_stride + off_n;
     double* xs = a.maps + (long long)k * a.map_stride + off_s;
     for (int j = tid; j < n; j += nt) {
@@ -343,11 +352,30 @@ __global__ void k_to_cdd(const double2* __restrict__ in, float4* out, long long 
   }
 }
 
-// Threads per CTA: the autotuned shape, else 1024 for segments whose shared memory allows one
-// CTA per SM (32 warps to hide the pass barriers and twiddle loads) and 512 for two per SM.
+// Threads per CTA: the autotuned shape (256 or 512), else 512 for segments whose shared memory
+// allows one CTA per SM and 256 for two per SM (sixteen warps an SM either way).
 int df_threads(const fsht_plan* p, long long smem) {
-  if (p->fft_threads > 0) return p->fft_threads;
-  return smem > 112 * 1024 ? 1024 : 512;
+  if (p->fft_threads > 0) return p->fft_threads > 256 ? 512 : 256;
+  return smem > 112 * 1024 ? 512 : 256;
+}
+
+// The radix-16 twiddle table (fft_r16.cuh layout), FP64 sincospi of the exactly reduced
+// argument, stored as df64
+__global__ void k_twiddles16(float4* out, int logTmax) {
+  const long long n = fsht_tw16_entries(1 << logTmax);
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n;
+       e += (long long)gridDim.x * blockDim.x) {
+    int s = 5;
+    while (s < logTmax && e >= fsht_tw16_off(s + 1)) ++s;
+    const long long loc = e - fsht_tw16_off(s);
+    const long long h = 1LL << (s - 4);
+    const long long k = loc / h + 1, j = loc % h;
+    const long long r = (j * k) & ((1LL << s) - 1);   // j k mod 2^s
+    double sn, cs;
+    sincospi(-2.0 * (double)r / (double)(1LL << s), &sn, &cs);
+    const cdd c = cdd_from_fp64(cs, sn);
+    out[e] = make_float4(c.h.x, c.h.y, c.l.x, c.l.y);
+  }
 }
 
 int to_cdd(const double2* in, float4** out, long long n, cudaStream_t s) {
@@ -369,6 +397,14 @@ int fsht_fft_df_tables_init(fsht_plan* p) {
   FSHT_TRY(to_cdd(p->d_chirp, &p->d_chirp_df, p->fft_chirp_total, p->stream));
   FSHT_TRY(to_cdd(p->d_bhat, &p->d_bhat_df, p->fft_bhat_total, p->stream));
   FSHT_TRY(to_cdd(p->d_rtw, &p->d_rtw_df, p->fft_rtw_total, p->stream));
+  const long long n16 = fsht_tw16_entries(p->Tmax);
+  FSHT_CUDA_TRY(cudaMalloc(&p->d_tw16_df, sizeof(float4) * (n16 > 0 ? n16 : 1)));
+  if (n16 > 0) {
+    long long g = (n16 + 255) / 256;
+    if (g > 4096) g = 4096;
+    k_twiddles16<<<(unsigned)g, 256, 0, p->stream>>>(p->d_tw16_df, p->logTmax);
+    FSHT_LAUNCH_CHECK();
+  }
   FSHT_CUDA_TRY(cudaStreamSynchronize(p->stream));
   return FSHT_OK;
 }
@@ -392,17 +428,24 @@ int fsht_launch_ring_fft_fwd_df(fsht_plan* p, const double* maps, long long map_
   a.chirp = reinterpret_cast<const cdd*>(p->d_chirp_df);
   a.bhat = reinterpret_cast<const cdd*>(p->d_bhat_df);
   a.rtw = reinterpret_cast<const cdd*>(p->d_rtw_df);
+  a.tw16 = reinterpret_cast<const cdd*>(p->d_tw16_df);
   a.ring_i0 = p->d_ring_i0;
   a.W = W;
   a.maps_per_block = p->fft_mpb > 0 ? p->fft_mpb : fsht_fft_maps_per_block(kb, p->nnorth);
-  FSHT_CUDA_TRY(cudaFuncSetAttribute(k_ring_fft_fwd_df,
+  FSHT_CUDA_TRY(cudaFuncSetAttribute(k_ring_fft_fwd_df<256>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)p->fft_smem));
+  FSHT_CUDA_TRY(cudaFuncSetAttribute(k_ring_fft_fwd_df<512>,
                                      cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      (int)p->fft_smem));
   for (int sgi = 0; sgi < p->fft_nseg; ++sgi) {
     const long long* sg = p->fft_seg + 3 * sgi;
     a.ring_base = (int)sg[0];
     dim3 grid((unsigned)(sg[1] - sg[0]), (kb + a.maps_per_block - 1) / a.maps_per_block);
-    k_ring_fft_fwd_df<<<grid, df_threads(p, sg[2]), (size_t)sg[2], s>>>(a);
+    if (df_threads(p, sg[2]) == 256)
+      k_ring_fft_fwd_df<256><<<grid, 256, (size_t)sg[2], s>>>(a);
+    else
+      k_ring_fft_fwd_df<512><<<grid, 512, (size_t)sg[2], s>>>(a);
     FSHT_LAUNCH_CHECK();
   }
   return FSHT_OK;
@@ -426,16 +469,23 @@ int fsht_launch_ring_fft_inv_df(fsht_plan* p, const double2* W, double* maps,
   a.chirp = reinterpret_cast<const cdd*>(p->d_chirp_df);
   a.bhat = reinterpret_cast<const cdd*>(p->d_bhat_df);
   a.rtw = p->d_rtw;
+  a.tw16 = reinterpret_cast<const cdd*>(p->d_tw16_df);
   a.ring_i0 = p->d_ring_i0;
   a.maps_per_block = p->fft_mpb > 0 ? p->fft_mpb : fsht_fft_maps_per_block(kc, p->nnorth);
-  FSHT_CUDA_TRY(cudaFuncSetAttribute(k_ring_fft_inv_df,
+  FSHT_CUDA_TRY(cudaFuncSetAttribute(k_ring_fft_inv_df<256>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)p->fft_smem));
+  FSHT_CUDA_TRY(cudaFuncSetAttribute(k_ring_fft_inv_df<512>,
                                      cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      (int)p->fft_smem));
   for (int sgi = 0; sgi < p->fft_nseg; ++sgi) {
     const long long* sg = p->fft_seg + 3 * sgi;
     a.ring_base = (int)sg[0];
     dim3 grid((unsigned)(sg[1] - sg[0]), (kc + a.maps_per_block - 1) / a.maps_per_block);
-    k_ring_fft_inv_df<<<grid, df_threads(p, sg[2]), (size_t)sg[2], s>>>(a);
+    if (df_threads(p, sg[2]) == 256)
+      k_ring_fft_inv_df<256><<<grid, 256, (size_t)sg[2], s>>>(a);
+    else
+      k_ring_fft_inv_df<512><<<grid, 512, (size_t)sg[2], s>>>(a);
     FSHT_LAUNCH_CHECK();
   }
   return FSHT_OK;
