@@ -200,6 +200,9 @@ def parse():
     ap.add_argument("--requests", type=int, default=2000, help="serving: requests")
     ap.add_argument("--rate", type=float, default=200.0, help="serving: mean arrivals per s")
     ap.add_argument("--budget-gb", type=float, default=150.0, help="serving: HBM budget")
+    ap.add_argument("--nside2048-maps", type=int, default=16,
+                    help="serving: cap on nmaps at nside 2048 (a 256-map Q/U request there is "
+                         "206 GB of input maps, more than the device or host holds)")
     a = ap.parse_args()
     if a.lmax is None:
         a.lmax = 2 * a.nside - 1
@@ -1078,22 +1081,24 @@ def bench_serving(args, rank, world, local):
     rng = np.random.default_rng(4)
     hi = int(round(math.log2(args.max_nside)))
     kinds = ["t2alm", "alm2t", "qu2eb", "eb2qu"]
+    cap = {2048: args.nside2048_maps}
     reqs = []
     t = 0.0
     for _ in range(args.requests):
         t += rng.exponential(1.0 / args.rate)
         ns = int(2 ** rng.integers(6, hi + 1))
-        reqs.append((t, kinds[int(rng.integers(0, 4))], ns, 2 * ns,
-                     int(rng.integers(1, max_maps + 1)),
+        nm = int(rng.integers(1, max_maps + 1))
+        reqs.append((t, kinds[int(rng.integers(0, 4))], ns, 2 * ns, min(nm, cap.get(ns, nm)),
                      "split" if rng.integers(0, 2) else "fp64"))
     pools = {}
     for ns in sorted({r[2] for r in reqs}):
         L = 2 * ns + 1
+        pm = max(r[4] for r in reqs if r[2] == ns)
         gm = torch.Generator(device=dev)
         gm.manual_seed(ns)
-        pools[ns] = (torch.randn((2, max_maps, 12 * ns * ns), dtype=torch.float64, device=dev,
+        pools[ns] = (torch.randn((2, pm, 12 * ns * ns), dtype=torch.float64, device=dev,
                                  generator=gm),
-                     torch.randn((2, L, L, max_maps), dtype=torch.float64, device=dev,
+                     torch.randn((2, L, L, pm), dtype=torch.float64, device=dev,
                                  generator=gm))
 
     def inputs(kind, ns, nm):
@@ -1109,8 +1114,7 @@ def bench_serving(args, rank, world, local):
     for kind in kinds:
         for ns in pools:
             for prec in ("fp64", "split"):
-                srv.submit(kind, ns, 2 * ns, inputs(kind, ns, 1),
-                           precision=prec if kind != "eb2qu" else "fp64")
+                srv.submit(kind, ns, 2 * ns, inputs(kind, ns, 1), precision=prec)
     srv.drain()
     srv.completed.clear()
     clocks = ClockSampler(local)
@@ -1120,8 +1124,11 @@ def bench_serving(args, rank, world, local):
         now = time.perf_counter() - t0
         if ta > now:
             time.sleep(ta - now)
-        srv.submit(kind, ns, lmax, inputs(kind, ns, nm),
-                   precision=prec if kind != "eb2qu" else "fp64", t_arrival=t0 + ta)
+        srv.submit(kind, ns, lmax, inputs(kind, ns, nm), precision=prec, t_arrival=t0 + ta)
+    # requests still queued or running when the last one arrives: a server that keeps up with
+    # the offered rate has only the most recent few
+    with srv._lock:
+        backlog = len(srv._pending) + sum(len(p.members) for p in srv._inflight)
     srv.drain()
     torch.cuda.synchronize()
     wall = time.perf_counter() - t0
@@ -1137,13 +1144,18 @@ def bench_serving(args, rank, world, local):
         "data": "synthetic",
         "config": {"workload": (f"serving form: Poisson stream of {args.requests} requests "
                                 f"(mean {args.rate}/s), map2alm or alm2map x T or Q/U, nside "
-                                f"2^U{{6..{hi}}}, lmax = 2 nside, nmaps ~ U[1, {max_maps}], "
-                                f"FP64 or split per request, seed 4; HBM budget "
-                                f"{args.budget_gb} GB"),
+                                f"2^U{{6..{hi}}}, lmax = 2 nside, nmaps ~ U[1, {max_maps}] "
+                                f"(at most {args.nside2048_maps} at nside 2048), FP64 or split "
+                                f"per request, seed 4; HBM budget {args.budget_gb} GB"),
                    "offered_s": reqs[-1][0], "nslots": 8},
         "clocks": clk,
         "latency_ms": {"p50": st.get("p50_ms"), "p99": st.get("p99_ms"),
                        "mean": st.get("mean_ms")},
+        "latency_by_precision_ms": st.get("by_precision"),
+        "latency_by_nside_ms": st.get("by_nside"),
+        "backlog_at_last_arrival": backlog,
+        "offered_requests_per_s": args.requests / reqs[-1][0],
+        "max_parts_per_request": st.get("max_parts"),
         "requests_per_s": args.requests / wall,
         "max_inflight": st.get("max_inflight"),
         "high_water_bytes": st.get("high_water_bytes"),

@@ -306,6 +306,7 @@ __global__ void __launch_bounds__(128) k_lambda_digits(LamArgs a) {
 constexpr int kStagesG = 6;
 constexpr uint32_t kStageBytesG = 2 * kSlices * kATileBytes;    // 32 KB: A then B
 constexpr int kPartSteps = kKChunk / kKStep;                    // k-steps per part
+constexpr size_t kSmemG = (size_t)kStagesG * kStageBytesG + kStgBytes;
 
 struct GemmArgs {
   int lmax, nnorth, ngroups, q0, ntmax, accumulate, nunits;
@@ -447,10 +448,15 @@ __global__ void __launch_bounds__(kThreadsG, 1) k_split_gemm(GemmArgs a) {
     // warp / 4 the half of the columns).  No early exit: the epilogue threads must meet at
     // every named barrier, so after an expired wait (abort) the remaining parts are walked
     // without work.
-    const int row = ((warp & 3) << 5) + (tid & 31);
+    const int lane = tid & 31;
+    const int row0 = (warp & 3) << 5;              // this warp's 32 rows (its TMEM lane quarter)
+    const int row = row0 + lane;
     const int cbeg = (warp >> 2) * (kCols / 2);   // this warp's half of the columns
+    const int comp = cbeg >> 6;                    // Re (0) or Im (1) of its 64 maps
     const long long L1 = a.lmax + 1;
-    const uint32_t lane_base = tmem + ((uint32_t)((warp & 3) << 5) << 16);
+    const uint32_t lane_base = tmem + ((uint32_t)row0 << 16);
+    double* stg = reinterpret_cast<double*>(smem + (size_t)kStagesG * kStageBytesG) +
+                  (size_t)warp * kStgWarpDoubles;
     uint32_t np = 0;
     for (int u = blockIdx.x; u < a.nunits; u += gridDim.x) {
       const GemmUnit w = gemm_unit(a, u);
@@ -480,6 +486,8 @@ __global__ void __launch_bounds__(kThreadsG, 1) k_split_gemm(GemmArgs a) {
         if (!ok) continue;
         tc::tc_fence_after();
         const bool add = ks0 > 0 || a.accumulate;
+        // Im of m = 0 does not exist
+        const bool comp_ok = !(comp == 1 && w.m == 0);
         for (int c0 = cbeg; c0 < cbeg + kCols / 2; c0 += 16) {
           uint32_t v0[16], v1[16], v2[16], v3[16];
           tc::tmem_ld16(lane_base + 0 * kCols + c0, v0);
@@ -492,24 +500,34 @@ __global__ void __launch_bounds__(kThreadsG, 1) k_split_gemm(GemmArgs a) {
             tc::tc_fence_before();
             tc::mbar_arrive(&h.tempty);
           }
-          const int comp = c0 >> 6;
-          const bool store = rowok && !(comp == 1 && w.m == 0);
-          const long long rowidx =
-              comp == 0 ? ((long long)w.m * L1 + l) : ((L1 - w.m) * L1 + (l - w.m));
+          // this lane's row of the block, staged
 #pragma unroll
-          for (int j = 0; j < 16; ++j) {
-            const int c = c0 + j;
-            const int k = w.g * kGroupMaps + (c & 63);
-            if (store && k < a.kc) {
-              const double v = levels_scaled(v0[j], v1[j], v2[j], v3[j], rh, rl, re + s_ce[c]);
-              double* dst = a.alm + rowidx * a.ld + a.k0 + k;
-              // adds go out as fire-and-forget reductions (no load latency in the epilogue);
-              // one thread owns each element, so the order (store, then adds) is its program
-              // order and the result is deterministic
-              if (add) atomicAdd(dst, v);
-              else *dst = v;
+          for (int j = 0; j < 16; ++j)
+            stg[stg_at(lane, j)] =
+                rowok ? levels_scaled(v0[j], v1[j], v2[j], v3[j], rh, rl, re + s_ce[c0 + j]) : 0.0;
+          __syncwarp();
+          // the block back out by rows: lanes 0-15 one row, 16-31 the next, 16 maps each.
+          // Adds go out as fire-and-forget reductions (no load latency in the epilogue); one
+          // thread owns each element within a part and parts are ordered by the TMEM hand-over,
+          // so the order (store, then adds) is fixed and the result is deterministic.
+          const int cc = lane & 15;
+          const int k = w.g * kGroupMaps + ((c0 + cc) & 63);
+          if (comp_ok && k < a.kc) {
+#pragma unroll 4
+            for (int i = 0; i < 16; ++i) {
+              const int r = 2 * i + (lane >> 4);
+              const int lr = w.lt0 + w.p + 2 * (row0 + r);
+              if (lr <= a.lmax) {
+                const long long rowidx =
+                    comp == 0 ? ((long long)w.m * L1 + lr) : ((L1 - w.m) * L1 + (lr - w.m));
+                double* dst = a.alm + rowidx * a.ld + a.k0 + k;
+                const double v = stg[stg_at(r, cc)];
+                if (add) atomicAdd(dst, v);
+                else *dst = v;
+              }
             }
           }
+          __syncwarp();
         }
       }
     }
@@ -1103,7 +1121,7 @@ int fsht_launch_split_gemm(fsht_plan* p, int w, const unsigned char* WS, const i
   a.pa = p->pa;
   a.err = p->d_err;
   a.nunits = a.ngroups * 2 * a.ntmax * (wv[1] - wv[0]);
-  const size_t sm = (size_t)kStagesG * kStageBytesG;
+  const size_t sm = kSmemG;
   FSHT_CUDA_TRY(
       cudaFuncSetAttribute(k_split_gemm, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
   int dev = 0, nsm = 0;

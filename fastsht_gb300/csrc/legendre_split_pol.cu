@@ -366,10 +366,18 @@ __global__ void __launch_bounds__(kThreadsG, 1) k_split_gemm_pol(GemmPArgs a) {
     // epilogue (warps 0-7), row = TMEM lane (warp % 4: lane quarter, warp / 4: half of the
     // columns).  No early exit: the epilogue threads must meet at every named barrier, so
     // after an expired wait (abort) the remaining passes are walked idle.
-    const int row = ((warp & 3) << 5) + (tid & 31);
-    const int cbeg = (warp >> 2) * (kCols / 2);   // this warp's half of the columns
+    const int lane = tid & 31;
+    const int row0 = (warp & 3) << 5;              // this warp's 32 rows (its TMEM lane quarter)
+    const int row = row0 + lane;
+    // tgt: the alm component (Re 0, Im 1) this warp writes, in every pass.  The first pass
+    // maps accumulator columns (Re, Im) to (Re, Im), the second (factor +-i) to (Im, Re), so in
+    // the second pass the warp reads the other half of the columns: every element then has one
+    // writer, whose store (first pass) and adds (later passes) are in its program order.
+    const int tgt = warp >> 2;
     const long long L1 = a.lmax + 1;
-    const uint32_t lane_base = tmem + ((uint32_t)((warp & 3) << 5) << 16);
+    const uint32_t lane_base = tmem + ((uint32_t)row0 << 16);
+    double* stg = reinterpret_cast<double*>(smem + (size_t)kStagesP * kStageBytesP) +
+                  (size_t)warp * kStgWarpDoubles;
     uint32_t np = 0;
     for (int u = blockIdx.x; u < a.nunits; u += gridDim.x) {
       const GemmPUnit w = gemm_pol_unit(a, u);
@@ -397,8 +405,6 @@ __global__ void __launch_bounds__(kThreadsG, 1) k_split_gemm_pol(GemmPArgs a) {
         factor_pair(-rw.dm * a.pa, rh, rl);
         re = rw.erow + rw.dx;
       }
-      const long long re_row = (long long)w.m * L1 + l;
-      const long long im_row = (L1 - w.m) * L1 + (l - w.m);
       double* alm = w.field == 0 ? a.almE : a.almB;
       for (int ks0 = 0; ks0 < w.nks; ks0 += kPartStepsP) {
         for (int part = 0; part < 2; ++part) {
@@ -408,6 +414,12 @@ __global__ void __launch_bounds__(kThreadsG, 1) k_split_gemm_pol(GemmPArgs a) {
           if (!ok) continue;
           tc::tc_fence_after();
           const bool add = ks0 > 0 || part > 0 || a.accumulate;
+          // part 0: (Re, Im) -> (Re, Im).  part 1 (factor +i for E, -i for B):
+          //   E: Re <- -Im, Im <- +Re;   B: Re <- +Im, Im <- -Re
+          const int comp = part == 0 ? tgt : 1 - tgt;     // the accumulator half read
+          const bool neg = part == 1 && ((w.field == 0) == (comp == 1));
+          const int cbeg = comp * (kCols / 2);
+          const bool tgt_ok = !(tgt == 1 && w.m == 0);    // Im of m = 0 does not exist
           for (int c0 = cbeg; c0 < cbeg + kCols / 2; c0 += 16) {
             uint32_t v0[16], v1[16], v2[16], v3[16];
             tc::tmem_ld16(lane_base + 0 * kCols + c0, v0);
@@ -419,31 +431,34 @@ __global__ void __launch_bounds__(kThreadsG, 1) k_split_gemm_pol(GemmPArgs a) {
               tc::tc_fence_before();
               tc::mbar_arrive(&h.tempty);
             }
-            const int comp = c0 >> 6;
-            // part 0: (Re, Im) -> (Re, Im).  part 1 (factor +i for E, -i for B):
-            //   E: Re <- -Im, Im <- +Re;   B: Re <- +Im, Im <- -Re
-            int tgt = comp;
-            bool neg = false;
-            if (part == 1) {
-              tgt = 1 - comp;
-              neg = (w.field == 0) == (comp == 1);
-            }
-            if (!rowok || (tgt == 1 && w.m == 0)) continue;
-            const long long rowidx = tgt == 0 ? re_row : im_row;
 #pragma unroll
             for (int j = 0; j < 16; ++j) {
-              const int c = c0 + j;
-              const int k = w.g * kGroupMaps + (c & 63);
-              if (k < a.kc) {
-                const double uu =
-                    levels_scaled(v0[j], v1[j], v2[j], v3[j], rh, rl, re + s_ce[part][c]);
-                const double v = neg ? -uu : uu;
-                double* dst = alm + rowidx * a.ld + a.k0 + k;
-                // adds as fire-and-forget reductions; one thread owns each element
-                if (add) atomicAdd(dst, v);
-                else *dst = v;
+              const double uu =
+                  rowok ? levels_scaled(v0[j], v1[j], v2[j], v3[j], rh, rl, re + s_ce[part][c0 + j])
+                        : 0.0;
+              stg[stg_at(lane, j)] = neg ? -uu : uu;
+            }
+            __syncwarp();
+            // the block back out by rows (lanes 0-15 one row, 16-31 the next), as fire-and-forget
+            // stores / reductions
+            const int cc = lane & 15;
+            const int k = w.g * kGroupMaps + ((c0 + cc) & 63);
+            if (tgt_ok && k < a.kc) {
+#pragma unroll 4
+              for (int i = 0; i < 16; ++i) {
+                const int r = 2 * i + (lane >> 4);
+                const int lr = w.lt0 + w.p + 2 * (row0 + r);
+                if (lr <= a.lmax) {
+                  const long long rowidx =
+                      tgt == 0 ? ((long long)w.m * L1 + lr) : ((L1 - w.m) * L1 + (lr - w.m));
+                  double* dst = alm + rowidx * a.ld + a.k0 + k;
+                  const double v = stg[stg_at(r, cc)];
+                  if (add) atomicAdd(dst, v);
+                  else *dst = v;
+                }
               }
             }
+            __syncwarp();
           }
         }
       }
@@ -952,7 +967,7 @@ int fsht_launch_split_gemm_pol(fsht_plan* p, int w, const unsigned char* WSQ, co
   a.kc = kc;
   a.pa = p->pa;
   a.err = p->d_err;
-  const size_t sm = (size_t)kStagesP * kStageBytesP;
+  const size_t sm = (size_t)kStagesP * kStageBytesP + kStgBytes;
   FSHT_CUDA_TRY(cudaFuncSetAttribute(k_split_gemm_pol,
                                      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
   int dev = 0, nsm = 0;

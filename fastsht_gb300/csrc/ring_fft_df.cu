@@ -93,15 +93,41 @@ __device__ __forceinline__ int load_scaled(cdd* buf, const Sw& S, int cnt, const
   return sh;
 }
 
-// NT threads per CTA (256: two CTAs per SM, 512: one), 128 registers a thread for the
-// radix-16 butterflies' sixteen df64 values.
-template <int NT>
-__global__ void __launch_bounds__(NT, 512 / NT) k_ring_fft_fwd_df(FwdDfArgs a) {
+// The pass flavour of a df64 ring-FFT kernel.  Radix-16 register passes (fft_r16.cuh) execute
+// about a fifth fewer instructions but need 128 registers a thread and give a transform P/16
+// butterflies per pass: they pay where transforms are large (the belt's 4096 points and the
+// large Bluestein sizes).  Segments of small transforms keep the radix-4 passes
+// (fft_passes.cuh), whose four times more butterflies per pass keep 512 threads busy at 64
+// registers.
+template <bool R16>
+struct DfPasses {
+  using Sw = Swz16;
+  static __device__ __forceinline__ void dft(cdd* buf, const FshtRingFFT& rf, const Sw& S,
+                                             const FftTwT<cdd>& tw, const cdd* tw16,
+                                             const cdd* chirp, const cdd* bhat) {
+    ring_dft16(buf, rf, S, tw16, tw.r3, chirp, bhat);
+  }
+};
+template <>
+struct DfPasses<false> {
+  using Sw = Swz;
+  static __device__ __forceinline__ void dft(cdd* buf, const FshtRingFFT& rf, const Sw&,
+                                             const FftTwT<cdd>& tw, const cdd*,
+                                             const cdd* chirp, const cdd* bhat) {
+    ring_dft(buf, rf, tw, chirp, bhat);
+  }
+};
+
+// NT threads per CTA, at least MINB CTAs per SM (which sets the register budget: 128 a
+// thread for <256, 2> and <512, 1>, 64 for <512, 2> and <1024, 1>).
+template <int NT, int MINB, bool R16>
+__global__ void __launch_bounds__(NT, MINB) k_ring_fft_fwd_df(FwdDfArgs a) {
+  using DP = DfPasses<R16>;
   extern __shared__ float4 smem4[];
   __shared__ int s_emax[2];
   const int i = a.ring_base + blockIdx.x;      // north ring index
   const FshtRingFFT rf = a.rfs[i];
-  const Swz16 S(rf);
+  const typename DP::Sw S(rf);
   const int n = rf.n;
   cdd* buf = reinterpret_cast<cdd*>(smem4);    // rf.P entries
   cdd* ph = buf + rf.P;                        // lmax+1 phase factors exp(-i m phi0) / 2
@@ -139,7 +165,7 @@ __global__ void __launch_bounds__(NT, 512 / NT) k_ring_fft_fwd_df(FwdDfArgs a) {
         __syncthreads();
         if (tid == 0) s_emax[(it & 1) ^ 1] = 0;
         const int sh = load_scaled(buf, S, nd, x, x + 1, 2, &s_emax[it & 1]);
-        ring_dft16(buf, rf, S, a.tw16, a.tw.r3, chirp, bhat);
+        DP::dft(buf, rf, S, a.tw, a.tw16, chirp, bhat);
         for (int m = tid; m <= mtop; m += nt) {
           const int q = m % n;
           const bool cj = q > nd;
@@ -170,7 +196,7 @@ __global__ void __launch_bounds__(NT, 512 / NT) k_ring_fft_fwd_df(FwdDfArgs a) {
     __syncthreads();   // the previous map's readers of buf and of the other slot are done
     if (tid == 0) s_emax[(it & 1) ^ 1] = 0;
     const int sh = load_scaled(buf, S, n, xn, equator ? nullptr : xs, 1, &s_emax[it & 1]);
-    ring_dft16(buf, rf, S, a.tw16, a.tw.r3, chirp, bhat);
+    DP::dft(buf, rf, S, a.tw, a.tw16, chirp, bhat);
     // Z = FFT(x_N + i x_S): X_N[q] = (Z[q] + conj Z[-q])/2, X_S[q] = (Z[q] - conj Z[-q])/(2i)
     // q = m mod n and the output pointer advance by fixed steps (no division per m)
     const int qstep = nt % n;
@@ -254,13 +280,14 @@ __device__ __forceinline__ int exp2f64(double2 v) {
 // Synthesis side of the split form: the spectrum of each ring pair is formed from G in FP64
 // (aliasing, x2, e^{+i m phi0}: O(lmax) per ring), scaled and converted to df64, transformed
 // as conj(DFT(conj Z)) in df64, and written to the maps with one FP64 addition per pixel.
-template <int NT>
-__global__ void __launch_bounds__(NT, 512 / NT) k_ring_fft_inv_df(InvDfArgs a) {
+template <int NT, int MINB, bool R16>
+__global__ void __launch_bounds__(NT, MINB) k_ring_fft_inv_df(InvDfArgs a) {
+  using DP = DfPasses<R16>;
   extern __shared__ float4 smem4[];
   __shared__ int s_emax[2];
   const int i = a.ring_base + blockIdx.x;
   const FshtRingFFT rf = a.rfs[i];
-  const Swz16 S(rf);
+  const typename DP::Sw S(rf);
   const int n = rf.n;
   cdd* buf = reinterpret_cast<cdd*>(smem4);
   double2* raw = reinterpret_cast<double2*>(smem4);
@@ -309,7 +336,7 @@ __global__ void __launch_bounds__(NT, 512 / NT) k_ring_fft_inv_df(InvDfArgs a) {
           em = max(em, exp2f64(v));
         }
         const int sh = convert_scaled(buf, S, nd, em, &s_emax[it & 1], false);
-        ring_dft16(buf, rf, S, a.tw16, a.tw.r3, chirp, bhat);
+        DP::dft(buf, rf, S, a.tw, a.tw16, chirp, bhat);
         double* x = a.maps + (long long)k * a.map_stride + (side ? off_s : off_n);
         for (int j = tid; j < nd; j += nt) {
           const cdd z = buf[S(dft_bin(rf, j))];   // conj(z): x_{2j} = Re, x_{2j+1} = -Im
@@ -332,7 +359,7 @@ __global__ void __launch_bounds__(NT, 512 / NT) k_ring_fft_inv_df(InvDfArgs a) {
     }
     // inverse DFT = conj(DFT(conj Z))
     const int sh = convert_scaled(buf, S, n, em, &s_emax[it & 1], true);
-    ring_dft16(buf, rf, S, a.tw16, a.tw.r3, chirp, bhat);
+    DP::dft(buf, rf, S, a.tw, a.tw16, chirp, bhat);
     double* xn = a.maps + (long long)k * a.map_stride + off_n;
     double* xs = a.maps + (long long)k * a.map_stride + off_s;
     for (int j = tid; j < n; j += nt) {
@@ -352,11 +379,34 @@ __global__ void k_to_cdd(const double2* __restrict__ in, float4* out, long long 
   }
 }
 
-// Threads per CTA: the autotuned shape (256 or 512), else 512 for segments whose shared memory
-// allows one CTA per SM and 256 for two per SM (sixteen warps an SM either way).
-int df_threads(const fsht_plan* p, long long smem) {
-  if (p->fft_threads > 0) return p->fft_threads > 256 ? 512 : 256;
-  return smem > 112 * 1024 ? 512 : 256;
+// Kernel variant of a ring segment: radix-16 passes when its largest transform has at least
+// 4096 points, with the autotuned thread count (256 or 512) or else 512 for one CTA per SM and
+// 256 for two (sixteen warps an SM either way); radix-4 passes below that, 1024 threads for one
+// CTA per SM and 512 for two (32 warps).
+enum DfVariant { kR16T256, kR16T512, kR4T512, kR4T1024 };
+DfVariant df_variant(const fsht_plan* p, long long smem) {
+  const long long pmax = smem / (long long)sizeof(cdd) - (p->lmax + 1);
+  const bool one_cta = smem > 112 * 1024;
+  if (pmax >= 4096) {
+    if (p->fft_threads > 0) return p->fft_threads > 256 ? kR16T512 : kR16T256;
+    return one_cta ? kR16T512 : kR16T256;
+  }
+  return one_cta ? kR4T1024 : kR4T512;
+}
+
+template <class Args>
+int df_set_smem(void (*k)(Args), size_t smem) {
+  FSHT_CUDA_TRY(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  return FSHT_OK;
+}
+
+template <class Args>
+int df_launch(DfVariant v, void (*const* ks)(Args), dim3 grid, size_t smem, cudaStream_t s,
+              const Args& a) {
+  static const int threads[4] = {256, 512, 512, 1024};
+  ks[v]<<<grid, threads[v], smem, s>>>(a);
+  FSHT_LAUNCH_CHECK();
+  return FSHT_OK;
 }
 
 // The radix-16 twiddle table (fft_r16.cuh layout), FP64 sincospi of the exactly reduced
@@ -432,21 +482,15 @@ int fsht_launch_ring_fft_fwd_df(fsht_plan* p, const double* maps, long long map_
   a.ring_i0 = p->d_ring_i0;
   a.W = W;
   a.maps_per_block = p->fft_mpb > 0 ? p->fft_mpb : fsht_fft_maps_per_block(kb, p->nnorth);
-  FSHT_CUDA_TRY(cudaFuncSetAttribute(k_ring_fft_fwd_df<256>,
-                                     cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     (int)p->fft_smem));
-  FSHT_CUDA_TRY(cudaFuncSetAttribute(k_ring_fft_fwd_df<512>,
-                                     cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     (int)p->fft_smem));
+  void (*const ks[4])(FwdDfArgs) = {k_ring_fft_fwd_df<256, 2, true>, k_ring_fft_fwd_df<512, 1, true>,
+                                    k_ring_fft_fwd_df<512, 2, false>,
+                                    k_ring_fft_fwd_df<1024, 1, false>};
+  for (auto k : ks) FSHT_TRY(df_set_smem(k, p->fft_smem));
   for (int sgi = 0; sgi < p->fft_nseg; ++sgi) {
     const long long* sg = p->fft_seg + 3 * sgi;
     a.ring_base = (int)sg[0];
     dim3 grid((unsigned)(sg[1] - sg[0]), (kb + a.maps_per_block - 1) / a.maps_per_block);
-    if (df_threads(p, sg[2]) == 256)
-      k_ring_fft_fwd_df<256><<<grid, 256, (size_t)sg[2], s>>>(a);
-    else
-      k_ring_fft_fwd_df<512><<<grid, 512, (size_t)sg[2], s>>>(a);
-    FSHT_LAUNCH_CHECK();
+    FSHT_TRY(df_launch(df_variant(p, sg[2]), ks, grid, (size_t)sg[2], s, a));
   }
   return FSHT_OK;
 }
@@ -472,21 +516,15 @@ int fsht_launch_ring_fft_inv_df(fsht_plan* p, const double2* W, double* maps,
   a.tw16 = reinterpret_cast<const cdd*>(p->d_tw16_df);
   a.ring_i0 = p->d_ring_i0;
   a.maps_per_block = p->fft_mpb > 0 ? p->fft_mpb : fsht_fft_maps_per_block(kc, p->nnorth);
-  FSHT_CUDA_TRY(cudaFuncSetAttribute(k_ring_fft_inv_df<256>,
-                                     cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     (int)p->fft_smem));
-  FSHT_CUDA_TRY(cudaFuncSetAttribute(k_ring_fft_inv_df<512>,
-                                     cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     (int)p->fft_smem));
+  void (*const ks[4])(InvDfArgs) = {k_ring_fft_inv_df<256, 2, true>, k_ring_fft_inv_df<512, 1, true>,
+                                    k_ring_fft_inv_df<512, 2, false>,
+                                    k_ring_fft_inv_df<1024, 1, false>};
+  for (auto k : ks) FSHT_TRY(df_set_smem(k, p->fft_smem));
   for (int sgi = 0; sgi < p->fft_nseg; ++sgi) {
     const long long* sg = p->fft_seg + 3 * sgi;
     a.ring_base = (int)sg[0];
     dim3 grid((unsigned)(sg[1] - sg[0]), (kc + a.maps_per_block - 1) / a.maps_per_block);
-    if (df_threads(p, sg[2]) == 256)
-      k_ring_fft_inv_df<256><<<grid, 256, (size_t)sg[2], s>>>(a);
-    else
-      k_ring_fft_inv_df<512><<<grid, 512, (size_t)sg[2], s>>>(a);
-    FSHT_LAUNCH_CHECK();
+    FSHT_TRY(df_launch(df_variant(p, sg[2]), ks, grid, (size_t)sg[2], s, a));
   }
   return FSHT_OK;
 }

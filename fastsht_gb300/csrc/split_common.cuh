@@ -29,6 +29,14 @@ constexpr int kThreads = 192;
 constexpr int kEpiThreads = 256;
 constexpr int kThreadsG = kEpiThreads + 64;
 constexpr int kEmptyExp = -4000;    // column exponent of an all-zero column
+// Epilogue staging of the analysis GEMMs: each epilogue warp turns a 32-row x 16-column block
+// of results around in shared memory, so that its global stores and reductions go out as
+// 128-byte row segments (two rows per instruction) instead of 32 scattered 8-byte values.
+// Column j of row r sits at j ^ (r & 15): both the row-wise writes and the column-wise reads
+// of a warp touch each bank pair at most twice.
+constexpr int kStgWarpDoubles = 32 * 16;
+constexpr size_t kStgBytes = (size_t)(kEpiThreads / 32) * kStgWarpDoubles * sizeof(double);
+__device__ __forceinline__ int stg_at(int r, int c) { return r * 16 + (c ^ (r & 15)); }
 
 struct RecConst {
   double a, b;

@@ -9,7 +9,17 @@ share the per-(l, m, ring) recursion and fill the kernels' 64-map tiles.  A requ
 whose footprint exceeds the whole budget is split along maps.  Inputs and results
 stay resident on the device (CUDA tensors); host arrays are copied in on the job's
 stream.  Each request records arrival, admission and completion times, from which
-the server reports p50 / p99 latency beside throughput.
+the server reports p50 / p99 latency beside throughput, overall and per precision.
+
+Head-of-line blocking: a large request (an FP64 transform at nside 2048 takes tens of
+seconds) must not hold back small ones.  Three rules keep it from doing so:
+  * a job's estimated GPU time (a cost model of its FFT and Legendre work at the
+    precision's rate) is capped at max_job_s: larger requests run as several jobs
+    along maps, so they give their slot and memory back regularly;
+  * jobs estimated below small_s are "small": they run on high-priority streams, so
+    their thread blocks are scheduled ahead of the waiting blocks of large kernels;
+  * `reserved` of the slots (the high-priority ones) only take small jobs, so a burst
+    of large requests cannot occupy every slot.
 
 No counterpart in the reference (one SHT instance, one blocking call at a time,
 SHT.py:16-227); every transform runs through the C ABI's fsht_run_job on a shared
@@ -92,14 +102,20 @@ class Server:
     gather from waiting requests of the same configuration (0 disables fusing).
     """
 
-    def __init__(self, hbm_budget=150e9, nslots=8, device=None, poll_s=5e-5, fuse_maps=128):
+    def __init__(self, hbm_budget=150e9, nslots=8, device=None, poll_s=5e-5, fuse_maps=128,
+                 max_job_s=1.0, small_s=0.05, reserved=2):
         self.device = torch.device("cuda", torch.cuda.current_device() if device is None else device)
         self.budget = int(hbm_budget)
         self.nslots = nslots
         self.poll_s = poll_s
         self.fuse_maps = int(fuse_maps)
+        self.max_job_s = float(max_job_s)
+        self.small_s = float(small_s)
+        self.reserved = max(0, min(int(reserved), nslots - 1))
         with torch.cuda.device(self.device):
-            self.streams = [torch.cuda.Stream(self.device) for _ in range(nslots)]
+            # slots [0, reserved): high-priority streams for small jobs only
+            self.streams = [torch.cuda.Stream(self.device, priority=-1 if i < self.reserved else 0)
+                            for i in range(nslots)]
         self._plans = {}
         self._ws_cache = {}
         self._pending = collections.deque()
@@ -177,13 +193,26 @@ class Server:
         t0 = min(r.t_arrival for r in self.completed)
         t1 = max(r.t_done for r in self.completed)
         mapsht = sum(r.nmaps * r.nfields for r in self.completed)
+
+        def pct(rs):
+            x = np.array([r.t_done - r.t_arrival for r in rs])
+            return {"requests": int(x.size), "p50_ms": float(np.percentile(x, 50) * 1e3),
+                    "p99_ms": float(np.percentile(x, 99) * 1e3)} if x.size else None
+
+        by_prec = {pr: pct([r for r in self.completed if r.precision == pr])
+                   for pr in ("fp64", "split")}
+        by_nside = {ns: pct([r for r in self.completed if r.nside == ns])
+                    for ns in sorted({r.nside for r in self.completed})}
         return {"requests": int(lat.size), "p50_ms": float(np.percentile(lat, 50) * 1e3),
                 "p99_ms": float(np.percentile(lat, 99) * 1e3),
                 "mean_ms": float(lat.mean() * 1e3), "wall_s": t1 - t0,
                 "requests_per_s": lat.size / (t1 - t0),
                 "maps_sht_per_s": mapsht / (t1 - t0),
+                "by_precision": {k: v for k, v in by_prec.items() if v},
+                "by_nside": by_nside,
                 "high_water_bytes": self.high_water, "budget_bytes": self.budget,
-                "max_inflight": self.max_inflight, "max_fused": self.max_fused}
+                "max_inflight": self.max_inflight, "max_fused": self.max_fused,
+                "max_parts": max(r.parts for r in self.completed)}
 
     # ------------------------------------------------------------ internals
     def _plan(self, nside, lmax, precision):
@@ -211,6 +240,21 @@ class Server:
             j.out0 = outs[0].data_ptr()
             j.out1 = outs[1].data_ptr() if len(outs) > 1 else None
         return j
+
+    @staticmethod
+    def cost_s(kind, nside, lmax, precision, n):
+        """Rough GPU seconds of n maps of a request (scheduling only): the ring FFTs at about
+        0.4 ms (df64) / 1.3 ms (FP64) per map per field at nside 1024, scaled by the pixel
+        count, and the Legendre contraction's 4 nside (lmax+1)(lmax+2) flop per map (four times
+        that per Q/U pair) at about 1 TFLOP/s in FP64 and 80 TFLOP/s in the split form."""
+        nf = 2 if kind in ("qu2eb", "eb2qu") else 1
+        split = precision == "split"
+        fft = (0.4e-3 if split else 1.3e-3) * (nside / 1024.0) ** 2 * nf
+        leg = 4.0 * nside * (lmax + 1) * (lmax + 2) * (4 if nf == 2 else 1)
+        return n * (fft + leg / (80e12 if split else 1.0e12))
+
+    def _req_cost(self, req, n):
+        return self.cost_s(req.kind, req.nside, req.lmax, req.precision, n)
 
     def _io_bytes(self, req, n):
         npix = 12 * req.nside ** 2
@@ -256,15 +300,27 @@ class Server:
                 total += r.nmaps
         return group
 
+    def _slot_for(self, small):
+        """A free slot for a job: small jobs prefer the reserved high-priority slots, large
+        jobs only take the others."""
+        free = sorted(self._free_slots)
+        if small:
+            return free[0] if free else None
+        big = [s for s in free if s >= self.reserved]
+        return big[0] if big else None
+
     def _admit(self, head) -> bool:
-        """Admit one job led by `head`: the rest of head's maps (as many as fit), or head
-        fused with waiting requests of the same configuration."""
+        """Admit one job led by `head`: the rest of head's maps (as many as fit the budget and
+        the max_job_s cap), or head fused with waiting requests of the same configuration."""
         if not self._free_slots:
             return False
         avail = self.budget - self._used
+        # maps per job under the duration cap (at least one)
+        per_map = self._req_cost(head, 1)
+        n_cap = max(1, int(self.max_job_s / per_map)) if per_map > 0 else 1 << 30
         group = self._gather(head)
         while True:
-            total = sum(r.nmaps - r.next_map for r in group)
+            total = min(sum(r.nmaps - r.next_map for r in group), n_cap)
             fit = self._fit(head, total, avail)
             if fit is None or fit[0] == total or len(group) == 1:
                 break
@@ -275,6 +331,9 @@ class Server:
                                    f"the {self.budget}-byte budget even for one map")
             return False
         n, kc, need = fit
+        slot = self._slot_for(self._req_cost(head, n) <= self.small_s)
+        if slot is None:
+            return False
         members, off = [], 0
         for r in group:
             k = min(r.nmaps - r.next_map, n - off)
@@ -282,7 +341,7 @@ class Server:
                 break
             members.append((r, r.next_map, r.next_map + k, off))
             off += k
-        slot = self._free_slots.pop()
+        self._free_slots.remove(slot)
         stream = self.streams[slot]
         with torch.cuda.device(self.device), torch.cuda.stream(stream):
             for r, *_ in members:

@@ -121,3 +121,39 @@ def test_waiting_requests_of_one_configuration_are_fused():
         want = _direct("t2alm", ns, lmax, ins, "fp64")[0]
         assert got.shape == want.shape and _close(got, want)
     srv.close()
+
+
+def test_small_requests_are_not_held_behind_a_large_one():
+    """Head-of-line blocking: an FP64 request of 48 maps at nside 1024 (about a second of GPU
+    time) is in flight when small requests arrive.  It runs as several jobs of at most
+    max_job_s, and the small ones run on the reserved high-priority slots, so each small
+    request finishes long before the large one, with its result unchanged."""
+    import time
+    from fastsht_gb300.serve import Server
+    gen = torch.Generator(device="cuda").manual_seed(11)
+    big = _inputs("t2alm", 1024, 2047, 48, gen)
+    small = [_inputs("t2alm", 32, 64, 1, gen) for _ in range(6)]
+    torch.cuda.synchronize()
+    srv = Server(hbm_budget=60e9, nslots=4, max_job_s=0.25)
+    try:
+        # plans and kernels of both configurations in place first
+        srv.submit("t2alm", 1024, 2047, [big[0][:1].contiguous()], "fp64").result(timeout=300)
+        srv.submit("t2alm", 32, 64, small[0], "fp64").result(timeout=60)
+        srv.drain()
+        srv.completed.clear()
+        fb = srv.submit("t2alm", 1024, 2047, big, "fp64")
+        time.sleep(0.05)
+        fs = [srv.submit("t2alm", 32, 64, s, "fp64") for s in small]
+        outs = [f.result(timeout=300) for f in fs]
+        fb.result(timeout=600)
+        st = srv.stats()
+        lat = {}
+        for r in srv.completed:
+            lat.setdefault(r.nside, []).append(r.t_done - r.t_arrival)
+        big_req = [r for r in srv.completed if r.nside == 1024][0]
+    finally:
+        srv.close()
+    assert big_req.parts >= 3, big_req.parts                 # ran as several capped jobs
+    assert max(lat[32]) < 0.3 * lat[1024][0], (lat, st)      # not held behind it
+    want = _direct("t2alm", 32, 64, small[3], "fp64")
+    assert _close(outs[3][0], want[0])
