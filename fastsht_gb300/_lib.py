@@ -83,6 +83,8 @@ SIGNATURES = {
     "fsht_job_workspace": [_vp, _vp, _i, C.POINTER(_sz)],
     "fsht_run_job": [_vp, _vp, _vp, _sz, _vp],
     "fsht_plan_tuning": [_vp, C.POINTER(_i), C.POINTER(_i)],
+    "fsht_plan_set_contraction": [_vp, _i, _i, _i],
+    "fsht_plan_contraction": [_vp, C.POINTER(_i), C.POINTER(_i), C.POINTER(_i)],
 }
 
 _lib = None

@@ -1,6 +1,6 @@
 // Batched form: many map sets of different nside / lmax / nmaps / spin / precision
 // executed as one CUDA-graph launch, plus the autotuner that picks the ring-FFT
-// launch shape per (nside, lmax) bucket.
+// launch shape and the contraction's tile shapes per (nside, lmax) bucket.
 //
 // The reference runs one SHT instance per process and one transform at a time
 // (module-global state, SHT.py:16-62); there it takes one Python call per map set.
@@ -108,6 +108,85 @@ int run_job(const fsht_plan* base, const fsht_job& j, unsigned char* arena, size
 std::mutex g_tune_mu;
 // (nside, lmax bucket, maps, df64 FFT) -> (maps per CTA, threads; 0 = per-segment default)
 std::map<std::tuple<int, int, int, int>, std::pair<int, int>> g_tune;
+// (nside, lmax bucket, maps, precision) -> contraction tile shape (ana_mt, ana_rc, split_part)
+std::map<std::tuple<int, int, int, int>, std::tuple<int, int, int>> g_tune_c;
+
+// Times one T analysis of the sample maps per candidate contraction tile shape and keeps the
+// fastest in the plan.  The ring FFT is the same for every candidate, so the fastest call has
+// the fastest contraction.  Plans that own a workspace run it there; table-only plans through a
+// job view on a temporary arena.
+int tune_contraction(fsht_plan* p, const double* maps, int sample_maps) {
+  struct Cand {
+    int mt, rc, part;
+  };
+  std::vector<Cand> cands;
+  if (p->precision == FSHT_PREC_SPLIT) {
+    for (int part : {64, 32, 16}) cands.push_back({0, 0, part});
+  } else {
+    for (int mt : {64, 32})
+      for (int rc : {16, 32, 8}) cands.push_back({mt, rc, 0});
+  }
+  const size_t L1 = (size_t)p->lmax + 1;
+  fsht_job j{};
+  j.nside = p->nside;
+  j.lmax = p->lmax;
+  j.nmaps = sample_maps;
+  j.kind = FSHT_JOB_T2ALM;
+  j.precision = p->precision;
+  j.in0 = maps;
+  double* alm = nullptr;
+  unsigned char* arena = nullptr;
+  size_t arena_bytes = 0;
+  FSHT_CUDA_TRY(cudaMalloc(&alm, sizeof(double) * L1 * L1 * sample_maps));
+  j.out0 = alm;
+  const bool own = p->d_work != nullptr && sample_maps <= p->kchunk;
+  int rc = FSHT_OK;
+  if (!own) {
+    arena_bytes = job_layout(p, j, sample_maps).total;
+    cudaError_t e = cudaMalloc(&arena, arena_bytes);
+    if (e != cudaSuccess) {
+      cudaFree(alm);
+      fsht_set_error("autotune: cudaMalloc(%zu): %s", arena_bytes, cudaGetErrorString(e));
+      return FSHT_ENOMEM;
+    }
+  }
+  auto run = [&]() -> int {
+    return own ? fsht_t2alm(p, maps, alm, sample_maps, 0, 0)
+               : run_job(p, j, arena, arena_bytes, p->stream);
+  };
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  float best = 1e30f;
+  Cand pick = cands[0];
+  if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) rc = FSHT_ECUDA;
+  for (size_t c = 0; c < cands.size() && !rc; ++c) {
+    p->ana_mt = cands[c].mt;
+    p->ana_rc = cands[c].rc;
+    p->split_part = cands[c].part;
+    if ((rc = run())) break;   // warm-up (kernel loading)
+    cudaEventRecord(e0, p->stream);
+    for (int r = 0; r < 2 && !rc; ++r) rc = run();
+    cudaEventRecord(e1, p->stream);
+    if (rc) break;
+    if (cudaEventSynchronize(e1) != cudaSuccess) {
+      rc = FSHT_ECUDA;
+      break;
+    }
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    if (ms < best) {
+      best = ms;
+      pick = cands[c];
+    }
+  }
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  cudaFree(alm);
+  if (arena) cudaFree(arena);
+  p->ana_mt = pick.mt;
+  p->ana_rc = pick.rc;
+  p->split_part = pick.part;
+  return rc ? rc : fsht_plan_check(p);
+}
 
 }  // namespace
 
@@ -122,13 +201,16 @@ extern "C" int fsht_plan_autotune(fsht_plan* p, int sample_maps) {
   {
     std::lock_guard<std::mutex> lk(g_tune_mu);
     auto it = g_tune.find(key);
-    if (it != g_tune.end()) {
+    auto itc = g_tune_c.find(std::make_tuple(p->nside, (p->lmax + 255) / 256, sample_maps,
+                                             p->precision));
+    if (it != g_tune.end() && itc != g_tune_c.end()) {
       p->fft_mpb = it->second.first;
       p->fft_threads = it->second.second;
+      std::tie(p->ana_mt, p->ana_rc, p->split_part) = itc->second;
       return FSHT_OK;
     }
   }
-  if (sample_maps > p->kchunk && p->kchunk > 0) sample_maps = p->kchunk;
+  if (p->d_work && sample_maps > p->kchunk && p->kchunk > 0) sample_maps = p->kchunk;
   double* maps = nullptr;
   double2* W = p->d_work;
   double2* W_tmp = nullptr;
@@ -174,13 +256,64 @@ extern "C" int fsht_plan_autotune(fsht_plan* p, int sample_maps) {
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
-  cudaFree(maps);
   if (W_tmp) cudaFree(W_tmp);
   p->fft_mpb = best_mpb;
   p->fft_threads = best_thr;
-  if (rc) return rc;
-  std::lock_guard<std::mutex> lk(g_tune_mu);
-  g_tune[key] = std::make_pair(best_mpb, best_thr);
+  if (!rc) {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    g_tune[key] = std::make_pair(best_mpb, best_thr);
+  }
+  // the contraction's tile shapes, with the chosen FFT shape in place
+  const auto ckey = std::make_tuple(p->nside, (p->lmax + 255) / 256, sample_maps, p->precision);
+  bool cached = false;
+  {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    auto it = g_tune_c.find(ckey);
+    if (it != g_tune_c.end()) {
+      std::tie(p->ana_mt, p->ana_rc, p->split_part) = it->second;
+      cached = true;
+    }
+  }
+  if (!rc && !cached) {
+    rc = tune_contraction(p, maps, sample_maps);
+    if (!rc) {
+      std::lock_guard<std::mutex> lk(g_tune_mu);
+      g_tune_c[ckey] = std::make_tuple(p->ana_mt, p->ana_rc, p->split_part);
+    }
+  }
+  cudaFree(maps);
+  return rc;
+}
+
+extern "C" int fsht_plan_set_contraction(fsht_plan* p, int maps_per_cta, int rings_per_chunk,
+                                         int part_steps) {
+  if (!p) {
+    fsht_set_error("null plan");
+    return FSHT_EINVAL;
+  }
+  if ((maps_per_cta != 0 && maps_per_cta != 32 && maps_per_cta != 64) ||
+      (rings_per_chunk != 0 && rings_per_chunk != 8 && rings_per_chunk != 16 &&
+       rings_per_chunk != 32) ||
+      (part_steps != 0 && part_steps != 16 && part_steps != 32 && part_steps != 64)) {
+    fsht_set_error("contraction shape (%d, %d, %d): need maps_per_cta 0|32|64, rings_per_chunk "
+                   "0|8|16|32, part_steps 0|16|32|64", maps_per_cta, rings_per_chunk, part_steps);
+    return FSHT_EINVAL;
+  }
+  p->ana_mt = maps_per_cta;
+  p->ana_rc = rings_per_chunk;
+  p->split_part = part_steps;
+  return FSHT_OK;
+}
+
+extern "C" int fsht_plan_contraction(const fsht_plan* p, int* maps_per_cta, int* rings_per_chunk,
+                                     int* part_steps) {
+  if (!p) {
+    fsht_set_error("null plan");
+    return FSHT_EINVAL;
+  }
+  if (maps_per_cta) *maps_per_cta = p->ana_mt;
+  if (rings_per_chunk) *rings_per_chunk = p->ana_rc;
+  if (part_steps) *part_steps = p->split_part;
   return FSHT_OK;
 }
 
@@ -274,8 +407,12 @@ extern "C" int fsht_batch_create(const fsht_job* jobs, int njobs, int nslots,
     b->job_plan.push_back(it->second);
   }
   if (autotune) {
-    for (fsht_plan* p : b->plans) {
-      int rc = fsht_plan_autotune(p, 1);
+    // each plan tuned at the map count of its largest job (at most one 64-map tile)
+    for (size_t pi = 0; pi < b->plans.size(); ++pi) {
+      int sm = 1;
+      for (int i = 0; i < njobs; ++i)
+        if (b->job_plan[i] == (int)pi) sm = std::max(sm, std::min(jobs[i].nmaps, 64));
+      int rc = fsht_plan_autotune(b->plans[pi], sm);
       if (rc) return fail(rc);
     }
   }

@@ -141,6 +141,10 @@ struct fsht_plan {
   int fft_nseg;
   long long fft_seg[3 * 8];
   int fft_mpb, fft_threads;        // ring-FFT launch shape (0: heuristic), set by the autotuner
+  // contraction tile shapes (0: defaults), set by the autotuner or fsht_plan_set_contraction:
+  // FP64 analysis maps per CTA (32 | 64) and rings per chunk (spin 0: 8 | 16 | 32, spin 2:
+  // 8 | 16); split GEMMs' ring-part length in k-steps of 16 rings (16 | 32 | 64)
+  int ana_mt, ana_rc, split_part;
   struct FshtProfile* prof;        // non-null while per-kernel timing is on
   int* d_err;                      // device error word (bounded waits that expired)
   // split-precision form: sliced phase tiles and their column exponents, the scaled

@@ -127,16 +127,19 @@ struct AnaArgs {
   int which;           // bit0: E/T, bit1: B
 };
 
-template <int SPIN>
+// Tile shape: QN map slots per thread (16 QN maps per CTA: 64 by default, 32 for small
+// batches) and RC rings per chunk (16 for spin 0 and 8 for spin 2 by default); the autotuner
+// picks among the instantiated shapes per (nside, lmax) bucket.
+template <int SPIN, int QN = 4, int RCN = (SPIN == 0 ? 16 : 8)>
 struct AnaCfg {
-  static constexpr int MT = 64;                  // maps per CTA
-  static constexpr int RC = SPIN == 0 ? 16 : 8;  // rings per chunk
+  static constexpr int MT = 16 * QN;             // maps per CTA
+  static constexpr int RC = RCN;                 // rings per chunk
   static constexpr int NF = SPIN == 0 ? 1 : 2;   // fields read
 };
 
-template <int SPIN>
+template <int SPIN, int QN, int RCN>
 __global__ void __launch_bounds__(NT) k_analysis_fp64(AnaArgs a) {
-  using C = AnaCfg<SPIN>;
+  using C = AnaCfg<SPIN, QN, RCN>;
   constexpr int MT = C::MT, RC = C::RC, NF = C::NF;
   extern __shared__ __align__(16) double smem_d[];
   // layout: st_cur[nnorth] st_prev[nnorth] | P[NF][2][RC][MT] double2 | lam1[RC][LC]
@@ -158,7 +161,7 @@ __global__ void __launch_bounds__(NT) k_analysis_fp64(AnaArgs a) {
   const int npair = (a.lmax + 2) / 2;
   // map slots q with a map behind them: small batches skip the padding's FMAs (warps
   // whose lanes all lack slot q skip it entirely)
-  const int nq = max(0, min(4, (a.kc - kt0 - mg + 15) / 16));
+  const int nq = max(0, min(QN, (a.kc - kt0 - mg + 15) / 16));
 
   for (int pass = 0; pass < 2; ++pass) {
     const int m = pass == 0 ? (int)blockIdx.x : a.lmax - (int)blockIdx.x;
@@ -188,11 +191,11 @@ __global__ void __launch_bounds__(NT) k_analysis_fp64(AnaArgs a) {
           s_nl[tid] = (l <= a.lmax) ? normal_l(l) : 0.0;
         }
       }
-      double2 accE[2][4], accB[2][4];
+      double2 accE[2][QN], accB[2][QN];
 #pragma unroll
       for (int s = 0; s < 2; ++s)
 #pragma unroll
-        for (int q = 0; q < 4; ++q) {
+        for (int q = 0; q < QN; ++q) {
           accE[s][q] = make_double2(0.0, 0.0);
           accB[s][q] = make_double2(0.0, 0.0);
         }
@@ -254,7 +257,7 @@ __global__ void __launch_bounds__(NT) k_analysis_fp64(AnaArgs a) {
             const double lb = lam1[rr * LC + lg + 16];
             const double2* pp = P + (par * RC + rr) * MT + mg;
 #pragma unroll
-            for (int q = 0; q < 4; ++q) {
+            for (int q = 0; q < QN; ++q) {
               if (q >= nq) break;
               const double2 v = pp[16 * q];
               accE[0][q].x = fma(la, v.x, accE[0][q].x);
@@ -271,7 +274,7 @@ __global__ void __launch_bounds__(NT) k_analysis_fp64(AnaArgs a) {
             const double2* u1 = P + ((1 * 2 + par) * RC + rr) * MT + mg;
             const double2* u2 = P + ((1 * 2 + (1 - par)) * RC + rr) * MT + mg;
 #pragma unroll
-            for (int q = 0; q < 4; ++q) {
+            for (int q = 0; q < QN; ++q) {
               if (q >= nq) break;
               const double2 Q1 = q1[16 * q], Q2 = q2[16 * q], U1 = u1[16 * q], U2 = u2[16 * q];
               // E += l1 P1Q + i l2 P2U ;  B += l1 P1U - i l2 P2Q
@@ -295,7 +298,7 @@ __global__ void __launch_bounds__(NT) k_analysis_fp64(AnaArgs a) {
         const int l = l0 + j;
         if (j >= nl) continue;
 #pragma unroll
-        for (int q = 0; q < 4; ++q) {
+        for (int q = 0; q < QN; ++q) {
           const int k = kt0 + mg + 16 * q;
           if (k >= a.kc) continue;
           const long long kk = a.k0 + k;
@@ -525,12 +528,24 @@ size_t syn_smem() {
   return sizeof(double2) * NF * LC * C::MT + sizeof(double) * C::RCS * (LC + 1) * (SPIN == 2 ? 2 : 1);
 }
 
-template <int SPIN>
+template <int SPIN, int QN, int RCN>
 size_t ana_smem(int nnorth) {
-  using C = AnaCfg<SPIN>;
+  using C = AnaCfg<SPIN, QN, RCN>;
   return (size_t)nnorth * (2 * sizeof(double) + sizeof(int)) +
          sizeof(double2) * C::NF * 2 * C::RC * C::MT +
          sizeof(double) * C::RC * LC * (SPIN == 2 ? 2 : 1);
+}
+
+template <int SPIN, int QN, int RCN>
+int launch_ana(const AnaArgs& a, int npair, int nnorth, int kc, cudaStream_t s) {
+  using C = AnaCfg<SPIN, QN, RCN>;
+  const size_t sm = ana_smem<SPIN, QN, RCN>(nnorth);
+  FSHT_CUDA_TRY(cudaFuncSetAttribute(k_analysis_fp64<SPIN, QN, RCN>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+  dim3 grid(npair, (kc + C::MT - 1) / C::MT);
+  k_analysis_fp64<SPIN, QN, RCN><<<grid, NT, sm, s>>>(a);
+  FSHT_LAUNCH_CHECK();
+  return FSHT_OK;
 }
 
 }  // namespace
@@ -557,21 +572,23 @@ int fsht_launch_analysis_fp64(fsht_plan* p, int spin, const double2* WQ, const d
   a.accumulate = accumulate;
   a.which = which;
   const int npair = (p->lmax + 2) / 2;
+  // tile shape: the plan's (autotuned) choice, else the default 64 maps per CTA
+  const bool q2 = p->ana_mt == 32;
   if (spin == 0) {
-    const size_t sm = ana_smem<0>(p->nnorth);
-    FSHT_CUDA_TRY(cudaFuncSetAttribute(k_analysis_fp64<0>,
-                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-    dim3 grid(npair, (kc + AnaCfg<0>::MT - 1) / AnaCfg<0>::MT);
-    k_analysis_fp64<0><<<grid, NT, sm, s>>>(a);
-  } else {
-    const size_t sm = ana_smem<2>(p->nnorth);
-    FSHT_CUDA_TRY(cudaFuncSetAttribute(k_analysis_fp64<2>,
-                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-    dim3 grid(npair, (kc + AnaCfg<2>::MT - 1) / AnaCfg<2>::MT);
-    k_analysis_fp64<2><<<grid, NT, sm, s>>>(a);
+    if (p->ana_rc == 32)
+      return q2 ? launch_ana<0, 2, 32>(a, npair, p->nnorth, kc, s)
+                : launch_ana<0, 4, 32>(a, npair, p->nnorth, kc, s);
+    if (p->ana_rc == 8)
+      return q2 ? launch_ana<0, 2, 8>(a, npair, p->nnorth, kc, s)
+                : launch_ana<0, 4, 8>(a, npair, p->nnorth, kc, s);
+    return q2 ? launch_ana<0, 2, 16>(a, npair, p->nnorth, kc, s)
+              : launch_ana<0, 4, 16>(a, npair, p->nnorth, kc, s);
   }
-  FSHT_LAUNCH_CHECK();
-  return FSHT_OK;
+  if (p->ana_rc == 16)
+    return q2 ? launch_ana<2, 2, 16>(a, npair, p->nnorth, kc, s)
+              : launch_ana<2, 4, 16>(a, npair, p->nnorth, kc, s);
+  return q2 ? launch_ana<2, 2, 8>(a, npair, p->nnorth, kc, s)
+            : launch_ana<2, 4, 8>(a, npair, p->nnorth, kc, s);
 }
 
 int fsht_launch_synthesis_fp64(fsht_plan* p, int spin, const double* almE, const double* almB,

@@ -305,11 +305,12 @@ __global__ void __launch_bounds__(128) k_lambda_digits(LamArgs a) {
 // every part.
 constexpr int kStagesG = 6;
 constexpr uint32_t kStageBytesG = 2 * kSlices * kATileBytes;    // 32 KB: A then B
-constexpr int kPartSteps = kKChunk / kKStep;                    // k-steps per part
+constexpr int kPartSteps = kKChunk / kKStep;   // most k-steps per part (levels 0, 1 exact)
 constexpr size_t kSmemG = (size_t)kStagesG * kStageBytesG + kStgBytes;
 
 struct GemmArgs {
   int lmax, nnorth, ngroups, q0, ntmax, accumulate, nunits;
+  int part_steps;        // k-steps per ring part, <= kPartSteps (the plan's tile choice)
   size_t row_bytes;
   const int* ring_i0;
   const long long* lam_off;
@@ -412,14 +413,14 @@ __global__ void __launch_bounds__(kThreadsG, 1) k_split_gemm(GemmArgs a) {
     bool ok = true;
     for (int u = blockIdx.x; u < a.nunits && ok && !*abort; u += gridDim.x) {
       const GemmUnit w = gemm_unit(a, u);
-      for (int ks0 = 0; ks0 < w.nks && ok; ks0 += kPartSteps, ++np) {
+      for (int ks0 = 0; ks0 < w.nks && ok; ks0 += a.part_steps, ++np) {
         // the epilogue of the previous part has read the accumulators
         if (np > 0 && !tc::mbar_wait(&h.tempty, (np - 1) & 1, abort)) {
           ok = false;
           break;
         }
         tc::tc_fence_after();
-        const int nk = min(w.nks - ks0, kPartSteps);
+        const int nk = min(w.nks - ks0, a.part_steps);
         for (int k = 0; k < nk; ++k, ++i) {
           const uint32_t st = i % kStagesG;
           if (!tc::mbar_wait(&h.full[st], (i / kStagesG) & 1, abort)) {
@@ -479,7 +480,7 @@ __global__ void __launch_bounds__(kThreadsG, 1) k_split_gemm(GemmArgs a) {
         factor_pair(rw.dm * a.pa, rh, rl);
         re = rw.erow + rw.dx;
       }
-      for (int ks0 = 0; ks0 < w.nks; ks0 += kPartSteps) {
+      for (int ks0 = 0; ks0 < w.nks; ks0 += a.part_steps) {
         bool ok = tc::mbar_wait(&h.tfull, np & 1, abort);
         ok = __all_sync(0xffffffffu, ok);      // tcgen05.ld below is warp-collective
         ++np;
@@ -1120,6 +1121,7 @@ int fsht_launch_split_gemm(fsht_plan* p, int w, const unsigned char* WS, const i
   a.kc = kc;
   a.pa = p->pa;
   a.err = p->d_err;
+  a.part_steps = (p->split_part > 0 && p->split_part < kPartSteps) ? p->split_part : kPartSteps;
   a.nunits = a.ngroups * 2 * a.ntmax * (wv[1] - wv[0]);
   const size_t sm = kSmemG;
   FSHT_CUDA_TRY(

@@ -214,6 +214,7 @@ constexpr int kPartStepsP = kKChunk / kKStep;
 
 struct GemmPArgs {
   int lmax, nnorth, ngroups, q0, ntmax, accumulate, which, nunits;
+  int part_steps;        // k-steps per ring part, <= kPartStepsP (the plan's tile choice)
   size_t row_bytes;
   const int* ring_i0;
   const long long* lam_off;
@@ -297,8 +298,8 @@ __global__ void __launch_bounds__(kThreadsG, 1) k_split_gemm_pol(GemmPArgs a) {
           a.lbuf + (size_t)(2 * (a.lam_off[a.q0 + w.qi] - a.lam_off[a.q0])) * kSlices * kATileBytes;
       const unsigned char* ws[2] = {w.field == 0 ? a.WSQ : a.WSU, w.field == 0 ? a.WSU : a.WSQ};
       const int bpar[2] = {w.p, 1 - w.p};
-      for (int ks0 = 0; ks0 < w.nks && ok; ks0 += kPartStepsP) {
-        const int nk = min(w.nks - ks0, kPartStepsP);
+      for (int ks0 = 0; ks0 < w.nks && ok; ks0 += a.part_steps) {
+        const int nk = min(w.nks - ks0, a.part_steps);
         for (int part = 0; part < 2 && ok; ++part) {
           for (int k = 0; k < nk; ++k, ++i) {
             const int ks = ks0 + k;
@@ -330,8 +331,8 @@ __global__ void __launch_bounds__(kThreadsG, 1) k_split_gemm_pol(GemmPArgs a) {
     bool ok = true;
     for (int u = blockIdx.x; u < a.nunits && ok && !*abort; u += gridDim.x) {
       const GemmPUnit w = gemm_pol_unit(a, u);
-      for (int ks0 = 0; ks0 < w.nks && ok; ks0 += kPartStepsP) {
-        const int nk = min(w.nks - ks0, kPartStepsP);
+      for (int ks0 = 0; ks0 < w.nks && ok; ks0 += a.part_steps) {
+        const int nk = min(w.nks - ks0, a.part_steps);
         for (int part = 0; part < 2 && ok; ++part, ++np) {
           if (np > 0 && !tc::mbar_wait(&h.tempty, (np - 1) & 1, abort)) {
             ok = false;
@@ -406,7 +407,7 @@ __global__ void __launch_bounds__(kThreadsG, 1) k_split_gemm_pol(GemmPArgs a) {
         re = rw.erow + rw.dx;
       }
       double* alm = w.field == 0 ? a.almE : a.almB;
-      for (int ks0 = 0; ks0 < w.nks; ks0 += kPartStepsP) {
+      for (int ks0 = 0; ks0 < w.nks; ks0 += a.part_steps) {
         for (int part = 0; part < 2; ++part) {
           bool ok = tc::mbar_wait(&h.tfull, np & 1, abort);
           ok = __all_sync(0xffffffffu, ok);
@@ -967,6 +968,8 @@ int fsht_launch_split_gemm_pol(fsht_plan* p, int w, const unsigned char* WSQ, co
   a.kc = kc;
   a.pa = p->pa;
   a.err = p->d_err;
+  a.part_steps =
+      (p->split_part > 0 && p->split_part < kPartStepsP) ? p->split_part : kPartStepsP;
   const size_t sm = (size_t)kStagesP * kStageBytesP + kStgBytes;
   FSHT_CUDA_TRY(cudaFuncSetAttribute(k_split_gemm_pol,
                                      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));

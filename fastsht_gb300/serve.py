@@ -20,6 +20,9 @@ seconds) must not hold back small ones.  Three rules keep it from doing so:
     their thread blocks are scheduled ahead of the waiting blocks of large kernels;
   * `reserved` of the slots (the high-priority ones) only take small jobs, so a burst
     of large requests cannot occupy every slot.
+Kernels are not preempted: a small job can still wait for the large jobs' kernels that are
+running when it arrives, so its latency is bounded by a few max_job_s, not by the size of the
+large requests.
 
 No counterpart in the reference (one SHT instance, one blocking call at a time,
 SHT.py:16-227); every transform runs through the C ABI's fsht_run_job on a shared

@@ -246,13 +246,24 @@ int fsht_job_workspace(const fsht_plan* tables, const fsht_job* job, int maps_pe
 int fsht_run_job(const fsht_plan* tables, const fsht_job* job, void* workspace,
                  size_t workspace_bytes, void* stream);
 
-/* Autotuner: times the ring-FFT launch shapes (maps per CTA 1..16; 256 or 512
- * threads, or 0 = the per-segment default: 512, and 1024 where a segment runs one CTA
- * per SM in the split form) on sample_maps maps and keeps the fastest in the plan;
- * results are cached per (nside, lmax bucket of 256, sample_maps, precision) for the
- * process.  No counterpart in the reference. */
+/* Autotuner: times the ring-FFT launch shapes (maps per CTA 1..16; 256 or 512 threads, or
+ * 0 = the per-segment default) on sample_maps maps and keeps the fastest in the plan, then the
+ * contraction's tile shapes (fsht_plan_set_contraction); results are cached per (nside, lmax
+ * bucket of 256, sample_maps, precision) for the process.  No counterpart in the reference. */
 int fsht_plan_autotune(fsht_plan* plan, int sample_maps);
 int fsht_plan_tuning(const fsht_plan* plan, int* maps_per_block, int* threads);
+/* Contraction tile shapes (0 = the default): the FP64 analysis kernel's maps per CTA (32 or
+ * 64) and rings per chunk (8, 16 or 32 for spin 0; 8 or 16 for spin 2), and the split GEMMs'
+ * ring-part length in k-steps of 16 rings (16, 32 or 64; 64 keeps the exact levels' sums below
+ * 2^24).  fsht_plan_autotune times the candidates on sample_maps maps after the FFT shape and
+ * keeps the fastest, cached per (nside, lmax bucket of 256, sample_maps, precision); the
+ * setter fixes them by hand.  Every shape gives the same transform (the FP64 sums in another
+ * order, the split form's exact levels unchanged).  No counterpart in the reference, whose
+ * contraction is one cuBLAS DGEMM per m (src/sht_core.f90:30-89). */
+int fsht_plan_set_contraction(fsht_plan* plan, int maps_per_cta, int rings_per_chunk,
+                              int part_steps);
+int fsht_plan_contraction(const fsht_plan* plan, int* maps_per_cta, int* rings_per_chunk,
+                          int* part_steps);
 
 /* Blocks until the plan's stream is idle; returns FSHT_ECUDA on an async error,
  * FSHT_ETIMEOUT when a bounded device-side wait (split-precision kernels) expired since

@@ -107,3 +107,76 @@ def test_config4_style_batch_runs_and_is_deterministic():
     again = [t for j in b.jobs for t in j.outputs]
     for x, y in zip(first, again):
         assert torch.equal(x, y)
+
+
+def _rel(a, b):
+    a = np.asarray(a)
+    b = np.asarray(b)
+    n = b.shape[0]
+    return float((np.abs(a - b).reshape(n, -1).max(axis=1) /
+                  np.abs(b).reshape(n, -1).max(axis=1)).max())
+
+
+@pytest.mark.parametrize("mt,rc", [(32, 16), (64, 32), (32, 8), (64, 8)])
+def test_fp64_contraction_shapes_give_the_same_transform(mt, rc):
+    """Every FP64 analysis tile shape the autotuner may pick (maps per CTA, rings per chunk)
+    gives the default shape's alm, T and Q/U, to FP64 rounding (the ring sums run in another
+    order only when the rings per chunk change)."""
+    import ctypes as C
+    from fastsht_gb300 import SHT, _lib
+    ns, lmax, nsim = 32, 80, 40
+    rng = np.random.default_rng(mt + rc)
+    T = np.asfortranarray(rng.standard_normal((12 * ns * ns, nsim)))
+    Q = np.asfortranarray(rng.standard_normal((12 * ns * ns, nsim)))
+    sht = SHT(ns, lmax, nsim, pol=True)
+    a0 = sht.t2alm(T)
+    e0, b0 = sht.qu2eb(Q, T)
+    _lib.call("fsht_plan_set_contraction", sht._plan, mt, rc, 0)
+    got = (C.c_int(), C.c_int(), C.c_int())
+    _lib.call("fsht_plan_contraction", sht._plan, *[C.byref(x) for x in got])
+    assert (got[0].value, got[1].value) == (mt, rc)
+    assert _rel(sht.t2alm(T), a0) <= 1e-13
+    e1, b1 = sht.qu2eb(Q, T)
+    assert _rel(e1, e0) <= 1e-13 and _rel(b1, b0) <= 1e-13
+
+
+@pytest.mark.parametrize("part", [16, 32])
+def test_split_part_lengths_give_the_same_transform(part):
+    """The split GEMMs' ring-part length (k-steps accumulated in TMEM before an FP64 add)
+    changes only where the FP32 lower levels are rounded: T and E/B alm agree with the default
+    64-step parts far inside the split form's 1e-7 bar."""
+    from fastsht_gb300 import SHT, _lib
+    ns, lmax, nsim = 512, 600, 9      # up to 1024 kept rings: 2 parts at 32 steps, 4 at 16
+    rng = np.random.default_rng(part)
+    T = np.asfortranarray(rng.standard_normal((12 * ns * ns, nsim)))
+    Q = np.asfortranarray(rng.standard_normal((12 * ns * ns, nsim)))
+    sht = SHT(ns, lmax, nsim, pol=True, precision="split")
+    a0 = sht.t2alm(T)
+    e0, b0 = sht.qu2eb(Q, T)
+    _lib.call("fsht_plan_set_contraction", sht._plan, 0, 0, part)
+    assert _rel(sht.t2alm(T), a0) <= 1e-9
+    e1, b1 = sht.qu2eb(Q, T)
+    assert _rel(e1, e0) <= 1e-9 and _rel(b1, b0) <= 1e-9
+
+
+@pytest.mark.parametrize("precision", ["fp64", "split"])
+def test_autotune_picks_a_contraction_shape(precision):
+    """The autotuner times the FFT launch shapes and then the contraction's tile shapes, keeps
+    one of the candidates and the transform stays the same."""
+    import ctypes as C
+    from fastsht_gb300 import SHT, _lib
+    ns, lmax, nsim = 64, 160, 24
+    rng = np.random.default_rng(7)
+    T = np.asfortranarray(rng.standard_normal((12 * ns * ns, nsim)))
+    sht = SHT(ns, lmax, nsim, precision=precision)
+    a0 = sht.t2alm(T)
+    _lib.call("fsht_plan_autotune", sht._plan, nsim)
+    got = (C.c_int(), C.c_int(), C.c_int())
+    _lib.call("fsht_plan_contraction", sht._plan, *[C.byref(x) for x in got])
+    mt, rc, part = (x.value for x in got)
+    if precision == "fp64":
+        assert mt in (32, 64) and rc in (8, 16, 32) and part == 0
+    else:
+        assert part in (16, 32, 64) and mt == 0 and rc == 0
+    tol = 1e-13 if precision == "fp64" else 1e-9
+    assert _rel(sht.t2alm(T), a0) <= tol

@@ -124,14 +124,16 @@ def test_waiting_requests_of_one_configuration_are_fused():
 
 
 def test_small_requests_are_not_held_behind_a_large_one():
-    """Head-of-line blocking: an FP64 request of 48 maps at nside 1024 (about a second of GPU
+    """Head-of-line blocking: an FP64 request of 96 maps at nside 1024 (a few seconds of GPU
     time) is in flight when small requests arrive.  It runs as several jobs of at most
-    max_job_s, and the small ones run on the reserved high-priority slots, so each small
-    request finishes long before the large one, with its result unchanged."""
+    max_job_s, and the small ones run on the reserved high-priority slots.  Kernels are not
+    preempted, so a small request can still wait for the large job's running kernels (a few
+    max_job_s), but not for the large request: each finishes within that bound and long before
+    the large one, with its result unchanged."""
     import time
     from fastsht_gb300.serve import Server
     gen = torch.Generator(device="cuda").manual_seed(11)
-    big = _inputs("t2alm", 1024, 2047, 48, gen)
+    big = _inputs("t2alm", 1024, 2047, 96, gen)
     small = [_inputs("t2alm", 32, 64, 1, gen) for _ in range(6)]
     torch.cuda.synchronize()
     srv = Server(hbm_budget=60e9, nslots=4, max_job_s=0.25)
@@ -153,7 +155,8 @@ def test_small_requests_are_not_held_behind_a_large_one():
         big_req = [r for r in srv.completed if r.nside == 1024][0]
     finally:
         srv.close()
-    assert big_req.parts >= 3, big_req.parts                 # ran as several capped jobs
-    assert max(lat[32]) < 0.3 * lat[1024][0], (lat, st)      # not held behind it
+    assert big_req.parts >= 4, big_req.parts                 # ran as several capped jobs
+    assert max(lat[32]) < 4 * 0.25, (lat, st)                # within a few job lengths
+    assert max(lat[32]) < 0.35 * lat[1024][0], (lat, st)     # not held behind the request
     want = _direct("t2alm", 32, 64, small[3], "fp64")
     assert _close(outs[3][0], want[0])
