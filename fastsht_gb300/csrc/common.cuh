@@ -140,6 +140,7 @@ struct fsht_plan {
   // {first ring, end ring, dynamic smem bytes} per segment
   int fft_nseg;
   long long fft_seg[3 * 8];
+  int fft_seg_pmin[8];             // smallest transform size of each segment
   int fft_mpb, fft_threads;        // ring-FFT launch shape (0: heuristic), set by the autotuner
   // contraction tile shapes (0: defaults), set by the autotuner or fsht_plan_set_contraction:
   // FP64 analysis maps per CTA (32 | 64) and rings per chunk (spin 0: 8 | 16 | 32, spin 2:
@@ -183,6 +184,11 @@ struct fsht_plan {
 #include "../../include/fastsht.h"
 
 void fsht_set_error(const char* fmt, ...);
+// Lets kernel `func` take at least `bytes` of dynamic shared memory on the current device.  The
+// attribute is set only when the limit has to grow (once per kernel and device in practice):
+// changing a function's attributes is not a launch-path operation and can wait for that
+// function's launches in flight, which would tie the enqueueing thread to the GPU.
+int fsht_smem_limit(const void* func, size_t bytes);
 
 #define FSHT_CUDA_TRY(expr)                                                   \
   do {                                                                        \

@@ -540,8 +540,7 @@ template <int SPIN, int QN, int RCN>
 int launch_ana(const AnaArgs& a, int npair, int nnorth, int kc, cudaStream_t s) {
   using C = AnaCfg<SPIN, QN, RCN>;
   const size_t sm = ana_smem<SPIN, QN, RCN>(nnorth);
-  FSHT_CUDA_TRY(cudaFuncSetAttribute(k_analysis_fp64<SPIN, QN, RCN>,
-                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+  FSHT_TRY(fsht_smem_limit((const void*)k_analysis_fp64<SPIN, QN, RCN>, sm));
   dim3 grid(npair, (kc + C::MT - 1) / C::MT);
   k_analysis_fp64<SPIN, QN, RCN><<<grid, NT, sm, s>>>(a);
   FSHT_LAUNCH_CHECK();
@@ -612,15 +611,13 @@ int fsht_launch_synthesis_fp64(fsht_plan* p, int spin, const double* almE, const
   const int npair = (p->lmax + 2) / 2;
   if (spin == 0) {
     const size_t sm = syn_smem<0>();
-    FSHT_CUDA_TRY(cudaFuncSetAttribute(k_synthesis_fp64<0>,
-                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    FSHT_TRY(fsht_smem_limit((const void*)k_synthesis_fp64<0>, (size_t)(sm)));
     dim3 grid(npair, (p->nnorth + SynCfg<0>::RCS - 1) / SynCfg<0>::RCS,
               (kc + SynCfg<0>::MT - 1) / SynCfg<0>::MT);
     k_synthesis_fp64<0><<<grid, NT, sm, s>>>(a);
   } else {
     const size_t sm = syn_smem<2>();
-    FSHT_CUDA_TRY(cudaFuncSetAttribute(k_synthesis_fp64<2>,
-                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    FSHT_TRY(fsht_smem_limit((const void*)k_synthesis_fp64<2>, (size_t)(sm)));
     dim3 grid(npair, (p->nnorth + SynCfg<2>::RCS - 1) / SynCfg<2>::RCS,
               (kc + SynCfg<2>::MT - 1) / SynCfg<2>::MT);
     k_synthesis_fp64<2><<<grid, NT, sm, s>>>(a);

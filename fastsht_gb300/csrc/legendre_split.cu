@@ -1124,8 +1124,7 @@ int fsht_launch_split_gemm(fsht_plan* p, int w, const unsigned char* WS, const i
   a.part_steps = (p->split_part > 0 && p->split_part < kPartSteps) ? p->split_part : kPartSteps;
   a.nunits = a.ngroups * 2 * a.ntmax * (wv[1] - wv[0]);
   const size_t sm = kSmemG;
-  FSHT_CUDA_TRY(
-      cudaFuncSetAttribute(k_split_gemm, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+  FSHT_TRY(fsht_smem_limit((const void*)k_split_gemm, (size_t)(sm)));
   int dev = 0, nsm = 0;
   FSHT_CUDA_TRY(cudaGetDevice(&dev));
   FSHT_CUDA_TRY(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
@@ -1198,8 +1197,7 @@ int fsht_launch_split_synth(fsht_plan* p, int w, const unsigned char* WS, const 
   a.kc = kc;
   a.err = p->d_err;
   const size_t sm = (size_t)kStagesS * kStageBytesS;
-  FSHT_CUDA_TRY(
-      cudaFuncSetAttribute(k_split_synth, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+  FSHT_TRY(fsht_smem_limit((const void*)k_split_synth, (size_t)(sm)));
   int dev = 0, nsm = 0;
   FSHT_CUDA_TRY(cudaGetDevice(&dev));
   FSHT_CUDA_TRY(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));

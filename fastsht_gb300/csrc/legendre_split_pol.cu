@@ -928,9 +928,7 @@ int fsht_launch_split_lambda_pol(fsht_plan* p, int w, unsigned char* lbuf, cudaS
   a.lam_off = p->d_lam_off;
   a.lbuf = lbuf;
   a.err = p->d_err;
-  FSHT_CUDA_TRY(cudaFuncSetAttribute(k_lambda_digits_pol,
-                                     cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     (int)kPolStageBytes));
+  FSHT_TRY(fsht_smem_limit((const void*)k_lambda_digits_pol, (size_t)(kPolStageBytes)));
   k_lambda_digits_pol<<<dim3(wv[1] - wv[0], wv[4]), 128, kPolStageBytes, s>>>(a);
   FSHT_LAUNCH_CHECK();
   return FSHT_OK;
@@ -971,8 +969,7 @@ int fsht_launch_split_gemm_pol(fsht_plan* p, int w, const unsigned char* WSQ, co
   a.part_steps =
       (p->split_part > 0 && p->split_part < kPartStepsP) ? p->split_part : kPartStepsP;
   const size_t sm = (size_t)kStagesP * kStageBytesP + kStgBytes;
-  FSHT_CUDA_TRY(cudaFuncSetAttribute(k_split_gemm_pol,
-                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+  FSHT_TRY(fsht_smem_limit((const void*)k_split_gemm_pol, (size_t)(sm)));
   int dev = 0, nsm = 0;
   FSHT_CUDA_TRY(cudaGetDevice(&dev));
   FSHT_CUDA_TRY(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
@@ -1031,8 +1028,7 @@ int fsht_launch_split_synth_pol(fsht_plan* p, int w, const unsigned char* WSE, c
   a.kc = kc;
   a.err = p->d_err;
   const size_t sm = (size_t)kStagesSP * kStageBytesSP;
-  FSHT_CUDA_TRY(cudaFuncSetAttribute(k_split_synth_pol,
-                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+  FSHT_TRY(fsht_smem_limit((const void*)k_split_synth_pol, (size_t)(sm)));
   int dev = 0, nsm = 0;
   FSHT_CUDA_TRY(cudaGetDevice(&dev));
   FSHT_CUDA_TRY(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));

@@ -16,6 +16,7 @@
 #include <mutex>
 #include <new>
 #include <string>
+#include <utility>
 #include <vector>
 
 namespace {
@@ -70,6 +71,21 @@ struct ProfScope {
 }  // namespace
 #define FSHT_PROF(cat) ProfScope _prof_scope_##__LINE__(p, cat)
 #define FSHT_PROF_ON(cat, st) ProfScope _prof_scope_##__LINE__(p, cat, st)
+
+int fsht_smem_limit(const void* func, size_t bytes) {
+  static std::mutex mu;
+  static std::map<std::pair<int, const void*>, size_t> done;
+  int dev = 0;
+  FSHT_CUDA_TRY(cudaGetDevice(&dev));
+  std::lock_guard<std::mutex> lk(mu);
+  size_t& cur = done[std::make_pair(dev, func)];
+  if (bytes > cur) {
+    FSHT_CUDA_TRY(cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)bytes));
+    cur = bytes;
+  }
+  return FSHT_OK;
+}
 
 void fsht_set_error(const char* fmt, ...) {
   char buf[1024];

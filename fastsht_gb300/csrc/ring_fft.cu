@@ -531,8 +531,7 @@ int fsht_fft_tables_fill(fsht_plan* p, const int* d_blue_rings, int nblue, cudaS
   FSHT_LAUNCH_CHECK();
   if (nblue > 0) {
     const size_t sm = (size_t)p->Pmax * sizeof(double2);
-    FSHT_CUDA_TRY(cudaFuncSetAttribute(k_bluestein_tables,
-                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    FSHT_TRY(fsht_smem_limit((const void*)k_bluestein_tables, (size_t)(sm)));
     k_bluestein_tables<<<(unsigned)nblue, 512, sm, s>>>(p->d_rfft, d_blue_rings, p->d_chirp,
                                                          p->d_bhat, p->d_rtw, plan_tw(p));
     FSHT_LAUNCH_CHECK();
@@ -556,6 +555,7 @@ int fsht_fft_tables_init(fsht_plan* p) {
       const size_t sm = (size_t)(rfs[i].P + p->lmax + 1) * sizeof(double2);
       const int cls = sm <= two_per_sm ? 0 : 1;
       if (cls != cls_prev && p->fft_nseg < 8) {
+        p->fft_seg_pmin[p->fft_nseg] = rfs[i].P;
         long long* sg = p->fft_seg + 3 * p->fft_nseg++;
         sg[0] = i;
         sg[1] = i + 1;
@@ -565,6 +565,7 @@ int fsht_fft_tables_init(fsht_plan* p) {
         long long* sg = p->fft_seg + 3 * (p->fft_nseg - 1);
         sg[1] = i + 1;
         if ((long long)sm > sg[2]) sg[2] = (long long)sm;
+        if (rfs[i].P < p->fft_seg_pmin[p->fft_nseg - 1]) p->fft_seg_pmin[p->fft_nseg - 1] = rfs[i].P;
       }
     }
   }
@@ -645,8 +646,7 @@ int fsht_launch_ring_fft_fwd_part(fsht_plan* p, const double* maps, long long ma
   a.ring_i0 = p->d_ring_i0;
   a.W = W;
   a.maps_per_block = p->fft_mpb > 0 ? p->fft_mpb : maps_per_block_for(kb, p->nnorth);
-  FSHT_CUDA_TRY(cudaFuncSetAttribute(k_ring_fft_fwd, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     (int)p->fft_smem));
+  FSHT_TRY(fsht_smem_limit((const void*)k_ring_fft_fwd, (size_t)(p->fft_smem)));
   for (int sgi = 0; sgi < p->fft_nseg; ++sgi) {
     const long long* sg = p->fft_seg + 3 * sgi;
     a.ring_base = (int)sg[0];
@@ -677,8 +677,7 @@ int fsht_launch_ring_fft_inv(fsht_plan* p, const double2* W, double* maps, long 
   a.bhat = p->d_bhat;
   a.ring_i0 = p->d_ring_i0;
   a.maps_per_block = p->fft_mpb > 0 ? p->fft_mpb : maps_per_block_for(kc, p->nnorth);
-  FSHT_CUDA_TRY(cudaFuncSetAttribute(k_ring_fft_inv, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     (int)p->fft_smem));
+  FSHT_TRY(fsht_smem_limit((const void*)k_ring_fft_inv, (size_t)(p->fft_smem)));
   for (int sgi = 0; sgi < p->fft_nseg; ++sgi) {
     const long long* sg = p->fft_seg + 3 * sgi;
     a.ring_base = (int)sg[0];
@@ -704,8 +703,7 @@ int fsht_launch_fourier_residual(fsht_plan* p, const double2* X, double2* GR, in
   a.ring_i0 = p->d_ring_i0;
   a.maps_per_block = p->fft_mpb > 0 ? p->fft_mpb : maps_per_block_for(kc, p->nnorth);
   dim3 grid(p->nnorth, (kc + a.maps_per_block - 1) / a.maps_per_block);
-  FSHT_CUDA_TRY(cudaFuncSetAttribute(k_fourier_residual,
-                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p->fft_smem));
+  FSHT_TRY(fsht_smem_limit((const void*)k_fourier_residual, (size_t)(p->fft_smem)));
   k_fourier_residual<<<grid, p->fft_threads > 0 ? p->fft_threads : 512, p->fft_smem, s>>>(a);
   FSHT_LAUNCH_CHECK();
   return FSHT_OK;

@@ -379,15 +379,16 @@ __global__ void k_to_cdd(const double2* __restrict__ in, float4* out, long long 
   }
 }
 
-// Kernel variant of a ring segment: radix-16 passes when its largest transform has at least
-// 4096 points, with the autotuned thread count (256 or 512) or else 512 for one CTA per SM and
-// 256 for two (sixteen warps an SM either way); radix-4 passes below that, 1024 threads for one
-// CTA per SM and 512 for two (32 warps).
+// Kernel variant of ring segment sgi: radix-16 passes when every transform of the segment has
+// at least 4096 points (the belt at nside >= 1024, the large Bluestein caps), with the
+// autotuned thread count (256 or 512) or else 512 for one CTA per SM and 256 for two (sixteen
+// warps an SM either way); radix-4 passes otherwise, 1024 threads for one CTA per SM and 512
+// for two (32 warps).
 enum DfVariant { kR16T256, kR16T512, kR4T512, kR4T1024 };
-DfVariant df_variant(const fsht_plan* p, long long smem) {
-  const long long pmax = smem / (long long)sizeof(cdd) - (p->lmax + 1);
+DfVariant df_variant(const fsht_plan* p, int sgi) {
+  const long long smem = p->fft_seg[3 * sgi + 2];
   const bool one_cta = smem > 112 * 1024;
-  if (pmax >= 4096) {
+  if (p->fft_seg_pmin[sgi] >= 4096) {
     if (p->fft_threads > 0) return p->fft_threads > 256 ? kR16T512 : kR16T256;
     return one_cta ? kR16T512 : kR16T256;
   }
@@ -396,8 +397,7 @@ DfVariant df_variant(const fsht_plan* p, long long smem) {
 
 template <class Args>
 int df_set_smem(void (*k)(Args), size_t smem) {
-  FSHT_CUDA_TRY(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  return FSHT_OK;
+  return fsht_smem_limit((const void*)k, smem);
 }
 
 template <class Args>
@@ -490,7 +490,7 @@ int fsht_launch_ring_fft_fwd_df(fsht_plan* p, const double* maps, long long map_
     const long long* sg = p->fft_seg + 3 * sgi;
     a.ring_base = (int)sg[0];
     dim3 grid((unsigned)(sg[1] - sg[0]), (kb + a.maps_per_block - 1) / a.maps_per_block);
-    FSHT_TRY(df_launch(df_variant(p, sg[2]), ks, grid, (size_t)sg[2], s, a));
+    FSHT_TRY(df_launch(df_variant(p, sgi), ks, grid, (size_t)sg[2], s, a));
   }
   return FSHT_OK;
 }
@@ -524,7 +524,7 @@ int fsht_launch_ring_fft_inv_df(fsht_plan* p, const double2* W, double* maps,
     const long long* sg = p->fft_seg + 3 * sgi;
     a.ring_base = (int)sg[0];
     dim3 grid((unsigned)(sg[1] - sg[0]), (kc + a.maps_per_block - 1) / a.maps_per_block);
-    FSHT_TRY(df_launch(df_variant(p, sg[2]), ks, grid, (size_t)sg[2], s, a));
+    FSHT_TRY(df_launch(df_variant(p, sgi), ks, grid, (size_t)sg[2], s, a));
   }
   return FSHT_OK;
 }
