@@ -170,12 +170,20 @@ struct fsht_plan {
   cudaStream_t xfer;
   cudaEvent_t evx[4];
   // fsht_t2alm_host: 0 = maps that lie in one fsht_host_alloc block are read in place by the
-  // forward FFT over the host link (no staging copy), 1 = maps are always copied first
-  int host_staged;
+  // forward FFT over the host link (no staging copy), 1 = maps are always copied first;
+  // host_onechunk: read in place without the chunked overlap
+  int host_staged, host_onechunk;
   // spin-0 split analysis: slicing one wave ahead on a second auxiliary stream into the other
   // half of d_ws / d_eb (events: fork, join, slice done x2); null in job views
   cudaStream_t aux2;
   cudaEvent_t evs[4];
+  // fsht_t2alm_host's chunked in-place route (split form): the contraction of a chunk of maps
+  // on high-priority copies of the plan's streams while the next chunk's forward FFT reads the
+  // host link on the plan's stream (events: fork, FFT done x2, contraction done x2); the GEMM's
+  // persistent grid capped at gemm_ctas CTAs meanwhile (0 = one per SM)
+  cudaStream_t hp_main, hp_aux, hp_aux2;
+  cudaEvent_t evh[5];
+  int gemm_ctas;
   int wave_qmax;                   // most orders in one wave
   FshtPolRow* d_poltab;            // spin-2 plans only, same triangular index as d_lamtab
 };

@@ -1128,7 +1128,9 @@ int fsht_launch_split_gemm(fsht_plan* p, int w, const unsigned char* WS, const i
   int dev = 0, nsm = 0;
   FSHT_CUDA_TRY(cudaGetDevice(&dev));
   FSHT_CUDA_TRY(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
-  const int grid = a.nunits < nsm ? a.nunits : nsm;
+  // persistent: one CTA per SM, or fewer while another kernel needs SMs beside it
+  const int cap = (p->gemm_ctas > 0 && p->gemm_ctas < nsm) ? p->gemm_ctas : nsm;
+  const int grid = a.nunits < cap ? a.nunits : cap;
   if (grid > 0) k_split_gemm<<<grid, kThreadsG, sm, s>>>(a);
   FSHT_LAUNCH_CHECK();
   return FSHT_OK;

@@ -131,6 +131,11 @@ void free_plan_memory(fsht_plan* p) {
   for (int i = 0; i < 4; ++i)
     if (p->evs[i]) cudaEventDestroy(p->evs[i]);
   if (p->aux2) cudaStreamDestroy(p->aux2);
+  for (int i = 0; i < 5; ++i)
+    if (p->evh[i]) cudaEventDestroy(p->evh[i]);
+  if (p->hp_main) cudaStreamDestroy(p->hp_main);
+  if (p->hp_aux) cudaStreamDestroy(p->hp_aux);
+  if (p->hp_aux2) cudaStreamDestroy(p->hp_aux2);
   cudaFree(p->d_poltab);
   delete[] p->h_waves;
   delete[] p->h_ring_i0;
@@ -368,6 +373,23 @@ int fsht_plan_create(int nside, int lmax, int nmaps_max, int flags, int precisio
         return fail(FSHT_ECUDA);
       }
     }
+    int least = 0, greatest = 0;
+    if ((ce = cudaDeviceGetStreamPriorityRange(&least, &greatest)) != cudaSuccess ||
+        (ce = cudaStreamCreateWithPriority(&p->hp_main, cudaStreamNonBlocking, greatest)) !=
+            cudaSuccess ||
+        (ce = cudaStreamCreateWithPriority(&p->hp_aux, cudaStreamNonBlocking, greatest)) !=
+            cudaSuccess ||
+        (ce = cudaStreamCreateWithPriority(&p->hp_aux2, cudaStreamNonBlocking, greatest)) !=
+            cudaSuccess) {
+      fsht_set_error("high-priority stream: %s", cudaGetErrorString(ce));
+      return fail(FSHT_ECUDA);
+    }
+    for (int i = 0; i < 5; ++i) {
+      if ((ce = cudaEventCreateWithFlags(&p->evh[i], cudaEventDisableTiming)) != cudaSuccess) {
+        fsht_set_error("event: %s", cudaGetErrorString(ce));
+        return fail(FSHT_ECUDA);
+      }
+    }
   }
   if (!tables_only) {
     if ((ce = cudaStreamCreateWithFlags(&p->xfer, cudaStreamNonBlocking)) != cudaSuccess) {
@@ -539,7 +561,13 @@ int fsht_host_mapped(const void* ptr, size_t bytes, int* mapped) {
 
 int fsht_plan_set_host_read(fsht_plan* p, int direct) {
   FSHT_TRY(check_plan(p));
+  if (direct < 0 || direct > 2) {
+    fsht_set_error("host read mode %d: 0 (staged), 1 (in place) or 2 (in place, one chunk)",
+                   direct);
+    return FSHT_EINVAL;
+  }
   p->host_staged = direct ? 0 : 1;
+  p->host_onechunk = direct == 2 ? 1 : 0;
   return FSHT_OK;
 }
 
@@ -791,6 +819,76 @@ int fsht_run_stage(fsht_plan* p, int stage, const void* in, void* out, int nmaps
 }
 
 // ----------------------------------------------------------------- temperature
+// SMs the persistent GEMM leaves to the next chunk's forward FFT in the chunked host route:
+// reading maps in place is bound by the host link, which about two dozen SMs keep busy.
+constexpr int kFftSms = 24;
+
+// Maps per chunk of the chunked host route (a multiple of the 64-map tile), or 0 when the
+// route does not apply: the split form without iterations, maps read in place, at least two
+// chunks' phase matrices in the workspace.
+static int host_chunk_maps(const fsht_plan* p, int nmaps, int niter, const HostXfer* hx) {
+  if (!hx || !hx->direct || p->host_onechunk || niter != 0 ||
+      p->precision != FSHT_PREC_SPLIT || !p->hp_main || nmaps < 128)
+    return 0;
+  const int nch = nmaps >= 256 ? 4 : 2;
+  int kc = (nmaps + nch - 1) / nch;
+  kc = (kc + 63) / 64 * 64;
+  return 2 * kc <= p->kchunk ? kc : 0;
+}
+
+static void swap_hp(fsht_plan* p) {
+  std::swap(p->stream, p->hp_main);
+  std::swap(p->aux, p->hp_aux);
+  std::swap(p->aux2, p->hp_aux2);
+}
+
+// fsht_t2alm_host, split form, maps read in place: chunks of kc maps whose forward FFT reads
+// the host link on the plan's stream while the previous chunk's contraction (recursion, slicing,
+// tensor-core GEMM, alm copies back) runs on high-priority copies of the plan's streams, two
+// phase-matrix buffers alternating.  The link-bound FFT needs few SMs: the GEMM's persistent
+// grid leaves it kFftSms while a later chunk is pending, and the contraction's kernels, at the
+// higher priority, take the others as the FFT's thread blocks retire.  The recursion runs once
+// per chunk (its digit tiles are not kept between chunks).
+static int t2alm_host_chunked(fsht_plan* p, double* alm, int nmaps, int kc, HostXfer* hx) {
+  const int nch = (nmaps + kc - 1) / kc;
+  const size_t per_map = per_map_buffer_bytes(p) / sizeof(double2);
+  double2* Wb[2] = {p->d_work, p->d_work + per_map * kc};
+  int dev = 0, nsm = 0;
+  FSHT_CUDA_TRY(cudaGetDevice(&dev));
+  FSHT_CUDA_TRY(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+  FSHT_CUDA_TRY(cudaEventRecord(p->evh[0], p->stream));
+  FSHT_CUDA_TRY(cudaStreamWaitEvent(p->hp_main, p->evh[0], 0));
+  for (int c = 0; c < nch; ++c) {
+    const int c0 = c * kc, n = nmaps - c0 < kc ? nmaps - c0 : kc, b = c & 1;
+    // buffer b is free once the contraction of chunk c - 2 has read it
+    if (c >= 2) FSHT_CUDA_TRY(cudaStreamWaitEvent(p->stream, p->evh[3 + b], 0));
+    {
+      FSHT_PROF(FSHT_KCAT_FFT_FWD);
+      FSHT_TRY(fsht_launch_ring_fft_fwd(p, hx->direct + (size_t)c0 * p->npix, p->npix, n, Wb[b],
+                                        p->stream));
+    }
+    FSHT_CUDA_TRY(cudaEventRecord(p->evh[1 + b], p->stream));
+    swap_hp(p);
+    p->gemm_ctas = (c + 1 < nch && nsm > 2 * kFftSms) ? nsm - kFftSms : 0;
+    hx->mdone.assign(p->lmax + 1, 0);
+    hx->cdone.assign(p->lmax + 1, 0);
+    int rc = cudaStreamWaitEvent(p->stream, p->evh[1 + b], 0) == cudaSuccess ? FSHT_OK
+                                                                               : FSHT_ECUDA;
+    if (!rc) rc = split_analysis(p, Wb[b], alm, nmaps, c0, n, 0, false, hx);
+    if (!rc) rc = xfer_orders_done(p, *hx, alm, nmaps, 0, p->lmax + 1, c0, n);
+    if (!rc && cudaEventRecord(p->evh[3 + b], p->stream) != cudaSuccess) rc = FSHT_ECUDA;
+    p->gemm_ctas = 0;
+    swap_hp(p);
+    if (rc) {
+      if (rc == FSHT_ECUDA) fsht_set_error("chunked host route: CUDA error");
+      return rc;
+    }
+  }
+  // the plan's stream resumes after the last contraction
+  FSHT_CUDA_TRY(cudaStreamWaitEvent(p->stream, p->evh[3 + ((nch - 1) & 1)], 0));
+  return FSHT_OK;
+}
+
 // hx: the maps come from host memory (copied in sub-batches that the FFT consumes as they
 // land) and the alm go back to it; null: device buffers only.
 static int t2alm_impl(fsht_plan* p, const double* maps, double* alm, int nmaps, int niter,
@@ -798,6 +896,10 @@ static int t2alm_impl(fsht_plan* p, const double* maps, double* alm, int nmaps, 
   FSHT_TRY(need_bufs(p, niter > 0 ? 2 : 1));
   const bool split = p->precision == FSHT_PREC_SPLIT;
   if (hx) FSHT_TRY(xfer_wait_main(p, 0));   // the device buffers' earlier users are done
+  if (const int kc = host_chunk_maps(p, nmaps, niter, hx)) {
+    FSHT_TRY(t2alm_host_chunked(p, alm, nmaps, kc, hx));
+    return xfer_join(p);
+  }
   for (int c0 = 0; c0 < nmaps; c0 += p->kchunk) {
     const int kc = nmaps - c0 < p->kchunk ? nmaps - c0 : p->kchunk;
     double2* W0 = work_buf(p, 0, kc);

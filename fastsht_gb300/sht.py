@@ -48,6 +48,12 @@ def pinned_empty(shape, order="F"):
     return arr
 
 
+# host_read modes of fsht_plan_set_host_read: maps in a pinned_empty buffer read in place by
+# the forward FFT ("direct"; in the split form with 128 or more maps as overlapped chunks, each
+# chunk's contraction beside the next chunk's reads), in place as one chunk, or copied first
+_HOST_READ = {"staged": 0, "direct": 1, "direct_onechunk": 2}
+
+
 class SHT:
     """Batched spherical-harmonic transforms of ``nsim`` HEALPix maps.
 
@@ -58,7 +64,9 @@ class SHT:
     alm2t, qu2eb / qu2e / qu2b and eb2qu as BF16 digit products on the tensor cores, ~3e-8
     max relative alm error; niter > 0 refines with the FP64 Fourier-space residual).
     ``host_read``: how t2alm takes NumPy maps that sit in a ``pinned_empty`` buffer -
-    "direct" (read in place by the FFT over the host link) or "staged" (copied to device
+    "direct" (read in place by the FFT over the host link; in the split form with 128 or more
+    maps in chunks, each chunk's contraction running beside the next chunk's reads),
+    "direct_onechunk" (in place, all maps before the contraction) or "staged" (copied to device
     memory first); the results are the same.
     """
 
@@ -76,8 +84,8 @@ class SHT:
         self.device = torch.device("cuda", torch.cuda.current_device() if device is None else device)
         if precision not in ("fp64", "split"):
             raise ValueError("precision must be 'fp64' or 'split'")
-        if host_read not in ("direct", "staged"):
-            raise ValueError("host_read must be 'direct' or 'staged'")
+        if host_read not in _HOST_READ:
+            raise ValueError(f"host_read must be one of {sorted(_HOST_READ)}")
         self.precision = precision
         self.host_read = host_read
         # workspace buffers, like the reference's nbuff (SHT.py:52-59)
@@ -97,7 +105,7 @@ class SHT:
                       _lib.FSHT_PREC_SPLIT if precision == "split" else _lib.FSHT_PREC_FP64,
                       int(workspace_limit), C.c_void_p(stream), C.byref(plan))
         self._plan = plan
-        _lib.call("fsht_plan_set_host_read", plan, 1 if host_read == "direct" else 0)
+        _lib.call("fsht_plan_set_host_read", plan, _HOST_READ[host_read])
 
     # ------------------------------------------------------------ lifetime
     def close(self):
@@ -273,7 +281,7 @@ class SHT:
         if hd is None:
             hd = self._host_dev = [None, self._new_dev_alm()]
         mapped = C.c_int(0)
-        if self.host_read == "direct":
+        if self.host_read != "staged":
             _lib.call("fsht_host_mapped", C.c_void_p(a.ctypes.data), C.c_size_t(a.nbytes),
                       C.byref(mapped))
         if not mapped.value and hd[0] is None:
