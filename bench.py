@@ -600,6 +600,8 @@ def ours(args, rank, world, local):
             "legendre_analysis_split" if args.precision == "split" else "legendre_analysis_fp64")
         if tr and tr.get("bytes_per_map"):
             traffic = tr["bytes_per_map"] * kchunk
+        elif tr and tr.get("bytes_per_call") and tr.get("maps") == kchunk:
+            traffic = tr["bytes_per_call"]          # not per map: measured at this chunk size
     if args.precision == "split":
         bf = peaks.get("bf16_tflops", 1900.0)
         ex_tf = 10 * ana_tf if ana_tf else None
