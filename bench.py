@@ -838,7 +838,7 @@ def _e2e_run(sht, maps_dev, ke, args, world, local):
         import ctypes as C
         from fastsht_gb300 import _lib
         _lib.call("fsht_plan_set_host_read", sht._plan,
-                  {"staged": 0, "direct": 1, "direct_onechunk": 2}[mode])
+                  {"staged": 0, "direct": 1, "direct_chunked": 2}[mode])
         sht.host_read = mode
         sht.t2alm(maps_np, alms_in=out_np)       # warm-up
         torch.cuda.synchronize()
@@ -861,15 +861,15 @@ def _e2e_run(sht, maps_dev, ke, args, world, local):
         return dt
 
     mode0 = sht.host_read
-    det_staged, det_direct, det_one = {}, {}, {}
+    det_staged, det_direct, det_chunked = {}, {}, {}
     try:
         dt_staged = timed("staged", det_staged)
-        dt_one = timed("direct_onechunk", det_one)
+        dt_chunked = timed("direct_chunked", det_chunked)
         dt = timed("direct", det_direct)
     finally:
         from fastsht_gb300 import _lib
         _lib.call("fsht_plan_set_host_read", sht._plan,
-                  {"staged": 0, "direct": 1, "direct_onechunk": 2}[mode0])
+                  {"staged": 0, "direct": 1, "direct_chunked": 2}[mode0])
         sht.host_read = mode0
     # the same pinned buffers copied by torch (first 64 maps): a reference for the host link's
     # rate beside the library's own transfers (in-place reads by the FFT, or cudaMemcpyAsync
@@ -892,13 +892,12 @@ def _e2e_run(sht, maps_dev, ke, args, world, local):
             "h2d_bytes_per_step": ke * npix * 8, "d2h_bytes_per_step": ke * L * L * 8,
             "maps_per_step": ke, "ms_per_step": 1000.0 * dt / args.steps,
             "host_read": ("direct: the forward FFT reads the pinned maps in place over the "
-                          "host link (the API's default for pinned_empty buffers), in chunks of "
-                          "128 maps, each chunk's contraction beside the next chunk's reads"),
+                          "host link (the API's default for pinned_empty buffers)"),
             "detail": det_direct,
-            "onechunk": {"value": world * ke * args.steps / dt_one, "unit": UNIT,
-                         "ms_per_step": 1000.0 * dt_one / args.steps, "detail": det_one,
-                         "note": "host_read='direct_onechunk': all maps read in place before "
-                                 "the contraction starts"},
+            "chunked": {"value": world * ke * args.steps / dt_chunked, "unit": UNIT,
+                        "ms_per_step": 1000.0 * dt_chunked / args.steps, "detail": det_chunked,
+                        "note": "host_read='direct_chunked': 128-map chunks read in place, each "
+                                "chunk's contraction beside the next chunk's reads"},
             "staged": {"value": world * ke * args.steps / dt_staged, "unit": UNIT,
                        "ms_per_step": 1000.0 * dt_staged / args.steps,
                        "detail": det_staged,

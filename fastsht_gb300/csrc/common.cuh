@@ -171,8 +171,9 @@ struct fsht_plan {
   cudaEvent_t evx[4];
   // fsht_t2alm_host: 0 = maps that lie in one fsht_host_alloc block are read in place by the
   // forward FFT over the host link (no staging copy), 1 = maps are always copied first;
-  // host_onechunk: read in place without the chunked overlap
-  int host_staged, host_onechunk;
+  // host_chunked: read in place in chunks, each chunk's contraction beside the next chunk's
+  // reads (measured slower than one chunk on GB300; kept as an option)
+  int host_staged, host_chunked;
   // spin-0 split analysis: slicing one wave ahead on a second auxiliary stream into the other
   // half of d_ws / d_eb (events: fork, join, slice done x2); null in job views
   cudaStream_t aux2;

@@ -562,12 +562,12 @@ int fsht_host_mapped(const void* ptr, size_t bytes, int* mapped) {
 int fsht_plan_set_host_read(fsht_plan* p, int direct) {
   FSHT_TRY(check_plan(p));
   if (direct < 0 || direct > 2) {
-    fsht_set_error("host read mode %d: 0 (staged), 1 (in place) or 2 (in place, one chunk)",
+    fsht_set_error("host read mode %d: 0 (staged), 1 (in place) or 2 (in place, in chunks)",
                    direct);
     return FSHT_EINVAL;
   }
   p->host_staged = direct ? 0 : 1;
-  p->host_onechunk = direct == 2 ? 1 : 0;
+  p->host_chunked = direct == 2 ? 1 : 0;
   return FSHT_OK;
 }
 
@@ -827,7 +827,7 @@ constexpr int kFftSms = 24;
 // route does not apply: the split form without iterations, maps read in place, at least two
 // chunks' phase matrices in the workspace.
 static int host_chunk_maps(const fsht_plan* p, int nmaps, int niter, const HostXfer* hx) {
-  if (!hx || !hx->direct || p->host_onechunk || niter != 0 ||
+  if (!hx || !hx->direct || !p->host_chunked || niter != 0 ||
       p->precision != FSHT_PREC_SPLIT || !p->hp_main || nmaps < 128)
     return 0;
   const int nch = nmaps >= 256 ? 4 : 2;

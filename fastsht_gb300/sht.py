@@ -49,9 +49,9 @@ def pinned_empty(shape, order="F"):
 
 
 # host_read modes of fsht_plan_set_host_read: maps in a pinned_empty buffer read in place by
-# the forward FFT ("direct"; in the split form with 128 or more maps as overlapped chunks, each
-# chunk's contraction beside the next chunk's reads), in place as one chunk, or copied first
-_HOST_READ = {"staged": 0, "direct": 1, "direct_onechunk": 2}
+# the forward FFT ("direct"), in place as overlapped chunks (split form, 128 or more maps: each
+# chunk's contraction beside the next chunk's reads), or copied to device memory first
+_HOST_READ = {"staged": 0, "direct": 1, "direct_chunked": 2}
 
 
 class SHT:
@@ -64,10 +64,9 @@ class SHT:
     alm2t, qu2eb / qu2e / qu2b and eb2qu as BF16 digit products on the tensor cores, ~3e-8
     max relative alm error; niter > 0 refines with the FP64 Fourier-space residual).
     ``host_read``: how t2alm takes NumPy maps that sit in a ``pinned_empty`` buffer -
-    "direct" (read in place by the FFT over the host link; in the split form with 128 or more
-    maps in chunks, each chunk's contraction running beside the next chunk's reads),
-    "direct_onechunk" (in place, all maps before the contraction) or "staged" (copied to device
-    memory first); the results are the same.
+    "direct" (read in place by the FFT over the host link), "direct_chunked" (in place, in the
+    split form with 128 or more maps as chunks, each chunk's contraction running beside the next
+    chunk's reads) or "staged" (copied to device memory first); the results are the same.
     """
 
     def __init__(self, nside, lmax, nsim, niter=0, pol=False, all_buff=False, *,

@@ -96,11 +96,11 @@ int fsht_t2alm_host(fsht_plan* plan, const double* host_maps, double* host_alm,
                     double* dev_maps, double* dev_alm, int nmaps, int niter, int method);
 /* How fsht_t2alm_host obtains host maps: direct = 1 (the default) reads maps that lie in one
  * fsht_host_alloc block in place, direct = 0 always copies them to dev_maps first, direct = 2
- * reads them in place as one chunk.  With direct = 1 the split form (niter = 0, 128 or more
- * maps, a workspace of two chunks) runs the maps in chunks of a multiple of 64: each chunk's
- * forward FFT reads the host link while the previous chunk's contraction runs on
- * high-priority streams.  Results are the same in every mode.  No counterpart in the
- * reference. */
+ * reads them in place in chunks: in the split form (niter = 0, 128 or more maps, a workspace
+ * of two chunks) the maps run in chunks of a multiple of 64, each chunk's forward FFT reading
+ * the host link while the previous chunk's contraction runs on high-priority streams (on GB300
+ * this measured slower than one chunk: the FFT needs most SMs to keep the link busy).  Results
+ * are the same in every mode.  No counterpart in the reference. */
 int fsht_plan_set_host_read(fsht_plan* plan, int direct);
 /* Temperature synthesis: reference alm2t (src/sht_main.f90:96-155). */
 int fsht_alm2t(fsht_plan* plan, const double* alm, double* maps, int nmaps);

@@ -144,14 +144,14 @@ def test_direct_read_several_chunks_nside_1024(precision):
 def test_chunked_direct_read_equals_device_path():
     """The split form's chunked in-place route (128-map chunks, each chunk's contraction beside
     the next chunk's host reads, two phase-matrix buffers alternating) gives the device path's
-    alm bit for bit, as does the one-chunk route."""
+    alm bit for bit, as does the one-chunk route (the default)."""
     from fastsht_gb300 import SHT, pinned_empty
     ns, lmax, nsim = 64, 191, 300
     maps = pinned_empty((12 * ns * ns, nsim))
     maps[...] = _maps(ns, nsim, 8)
     want = SHT(ns, lmax, nsim, precision="split").t2alm(
         torch.from_numpy(np.asarray(maps).T.copy()).cuda().T).cpu().numpy()
-    for mode in ("direct", "direct_onechunk"):
+    for mode in ("direct_chunked", "direct"):
         sht = SHT(ns, lmax, nsim, precision="split", host_read=mode)
         got = sht.t2alm(maps)
         got2 = sht.t2alm(maps)                      # buffers reused on a second call
