@@ -515,6 +515,12 @@ def ours(args, rank, world, local):
     _lib.call("fsht_measure_fp32_peak", C.byref(peak32))
     peak_dmma = C.c_double()
     _lib.call("fsht_measure_dmma_peak", C.byref(peak_dmma))
+    umma = {}
+    if args.precision == "split":
+        for ncol in (128, 256):
+            r = C.c_double()
+            _lib.call("fsht_measure_umma_rate", ncol, C.byref(r))
+            umma[ncol] = r.value
     peaks = {}
     pk = ROOT / "MEASURED_PEAKS.json"
     if pk.exists():
@@ -613,6 +619,15 @@ def ours(args, rank, world, local):
                     "algorithmic_flop_per_chunk": flop_per_map(nside, lmax) * kchunk,
                     "executed_tensor_tflops": ex_tf,
                     "executed_frac": ex_tf / bf if ex_tf else None,
+                    "umma_tile_ceiling": {
+                        "n128_tflops": umma.get(128), "n256_tflops": umma.get(256),
+                        "executed_frac_of_n128": (ex_tf / umma[128]
+                                                  if ex_tf and umma.get(128) else None),
+                        "note": ("the contraction's k-step (ten 128 x N x 16 BF16 UMMAs) issued "
+                                 "back to back from shared memory, one CTA per SM "
+                                 "(fsht_measure_umma_rate), measured in this run: the ceiling "
+                                 "of the 128-column tile the kernel uses, and of a 256-column "
+                                 "one")},
                     "traffic": traffic,
                     "note": ("achieved counts algorithmic FLOP (4 nside (lmax+1)(lmax+2) per map); "
                              "the kernel executes 10 BF16 digit products per algorithmic FMA "
@@ -998,6 +1013,7 @@ def bench_batched(args, rank, world, local):
 
     def all_groups(precision, steps, warmup, clocks=None):
         ms, infos, t_build = 0.0, [], 0.0
+        tunings = {}
         if world > 1:
             dist.barrier()
         if clocks:
@@ -1008,20 +1024,26 @@ def bench_batched(args, rank, world, local):
             t_build += time.perf_counter() - t0
             ms += run(b, steps, warmup)
             infos.append(b.info())
+            for t in b.tunings():
+                key = f"{t['precision']} nside {t['nside']} lmax {t['lmax']}"
+                tunings[key] = {k: v for k, v in t.items()
+                                if k not in ("nside", "lmax", "precision")}
             b.close()
             del b
             torch.cuda.empty_cache()
         clk = clocks.stop() if clocks else None
         if world > 1:
             ms = max_over_ranks(ms, dist, dev)
-        return ms, clk, infos, t_build
+        return ms, clk, infos, t_build, tunings
 
-    ms, clk, infos, t_build = all_groups("split", args.steps, args.warmup, ClockSampler(local))
+    ms, clk, infos, t_build, tunings = all_groups("split", args.steps, args.warmup,
+                                                  ClockSampler(local))
     value = world * mapsht * args.steps / (ms / 1000.0)
     fp64 = None
     if not args.no_fp64:
         s64 = max(1, args.steps // 2)
-        ms64, _, _, _ = all_groups("fp64", s64, 1)
+        ms64, _, _, _, tun64 = all_groups("fp64", s64, 1)
+        tunings.update(tun64)
         v64 = world * mapsht * s64 / (ms64 / 1000.0)
         fp64 = {"value": v64, "unit": UNIT, "ms_per_step": ms64 / s64, "split_speedup": value / v64}
     line = {
@@ -1047,6 +1069,9 @@ def bench_batched(args, rank, world, local):
         "clocks": clk,
         "flop_rate_tflops": world * flops * args.steps / (ms / 1000.0) / 1e12,
         "fp64_all": fp64,
+        # launch shapes the autotuner chose per plan (FFT maps per CTA and threads; FP64 maps
+        # per CTA and rings per chunk; split ring-part k-steps; 0 = the kernel's default)
+        "autotuned_shapes": tunings,
     }
     if rank == 0:
         print(json.dumps(line), flush=True)
@@ -1140,8 +1165,8 @@ def bench_serving(args, rank, world, local):
     """Open-loop Poisson stream into fastsht_gb300.serve.Server: map2alm or alm2map, T or
     Q/U with equal odds, nside = 2^U{6..log2 max_nside}, lmax = 2 nside, nmaps ~
     U[1, max_maps], FP64 or split per request (the split form covers map2alm T and Q/U and
-    alm2map T; alm2map Q/U runs FP64), seed 4.  Inputs are device-resident views of pre-generated
-    pools.  value = map.SHT/s over the run; p50/p99 latency from arrival to result."""
+    alm2map T; alm2map Q/U runs FP64), seed 4.  Inputs are device-resident views of one
+    pre-generated N(0,1) pool per nside (no per-request copies).  value = map.SHT/s over the run; p50/p99 latency from arrival to result."""
     import torch
     from fastsht_gb300 import _lib
     from fastsht_gb300.serve import Server
@@ -1164,23 +1189,26 @@ def bench_serving(args, rank, world, local):
         nm = int(rng.integers(1, max_maps + 1))
         reqs.append((t, kinds[int(rng.integers(0, 4))], ns, 2 * ns, min(nm, cap.get(ns, nm)),
                      "split" if rng.integers(0, 2) else "fp64"))
+    # one flat N(0,1) pool per nside and field, large enough for the biggest request of either
+    # direction: a request of nm maps views its first nm maps' (or nm alm sets') worth of
+    # values in the layout it needs, so requests share the pool without copies
     pools = {}
     for ns in sorted({r[2] for r in reqs}):
         L = 2 * ns + 1
         pm = max(r[4] for r in reqs if r[2] == ns)
         gm = torch.Generator(device=dev)
         gm.manual_seed(ns)
-        pools[ns] = (torch.randn((2, pm, 12 * ns * ns), dtype=torch.float64, device=dev,
-                                 generator=gm),
-                     torch.randn((2, L, L, pm), dtype=torch.float64, device=dev,
-                                 generator=gm))
+        pools[ns] = torch.randn((2, pm * max(12 * ns * ns, L * L)), dtype=torch.float64,
+                                device=dev, generator=gm)
 
     def inputs(kind, ns, nm):
-        maps, alm = pools[ns]
+        pool = pools[ns]
         nf = 2 if kind in ("qu2eb", "eb2qu") else 1
         if kind in ("t2alm", "qu2eb"):
-            return [maps[f, :nm] for f in range(nf)]
-        return [alm[f, :, :, :nm].contiguous() for f in range(nf)]
+            npix = 12 * ns * ns
+            return [pool[f, :nm * npix].view(nm, npix) for f in range(nf)]
+        L = 2 * ns + 1
+        return [pool[f, :L * L * nm].view(L, L, nm) for f in range(nf)]
 
     budget = args.budget_gb * 1e9
     srv = Server(hbm_budget=budget, nslots=8, device=local)

@@ -73,11 +73,14 @@ SIGNATURES = {
     "fsht_measure_fp64_peak": [C.POINTER(C.c_double)],
     "fsht_measure_fp32_peak": [C.POINTER(C.c_double)],
     "fsht_measure_dmma_peak": [C.POINTER(C.c_double)],
+    "fsht_measure_umma_rate": [C.c_int, C.POINTER(C.c_double)],
     "fsht_last_error": [C.c_char_p, _sz],
     "fsht_batch_create": [C.c_void_p, _i, _i, _sz, _i, _vp, C.POINTER(_vp)],
     "fsht_batch_run": [_vp],
     "fsht_batch_sync": [_vp],
     "fsht_batch_info": [_vp, C.POINTER(_i), C.POINTER(_i)],
+    "fsht_batch_plan_tuning": [_vp, _i, C.POINTER(_i), C.POINTER(_i), C.POINTER(_i),
+                               C.POINTER(_i)],
     "fsht_batch_destroy": [_vp],
     "fsht_plan_autotune": [_vp, _i],
     "fsht_job_workspace": [_vp, _vp, _i, C.POINTER(_sz)],

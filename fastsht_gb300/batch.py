@@ -105,6 +105,25 @@ class Batch:
         _lib.call("fsht_batch_info", self._b, C.byref(n_plans), C.byref(n_nodes))
         return {"plans": n_plans.value, "graph_nodes": n_nodes.value, "jobs": len(self.jobs)}
 
+    def tunings(self):
+        """Per plan of the built batch: (nside, lmax, precision) and the launch shapes it runs
+        with (FFT maps per CTA and threads, FP64 analysis maps per CTA and rings per chunk,
+        split ring-part k-steps; 0 = the kernel's default)."""
+        n_plans = C.c_int()
+        _lib.call("fsht_batch_info", self._b, C.byref(n_plans), None)
+        out = []
+        for i in range(n_plans.value):
+            ns, lm, pr = C.c_int(), C.c_int(), C.c_int()
+            sh = (C.c_int * 5)()
+            _lib.call("fsht_batch_plan_tuning", self._b, i, C.byref(ns), C.byref(lm),
+                      C.byref(pr), sh)
+            out.append({"nside": ns.value, "lmax": lm.value,
+                        "precision": "split" if pr.value == _lib.FSHT_PREC_SPLIT else "fp64",
+                        "fft_maps_per_cta": sh[0], "fft_threads": sh[1],
+                        "fp64_maps_per_cta": sh[2], "fp64_rings_per_chunk": sh[3],
+                        "split_part_steps": sh[4]})
+        return out
+
     def close(self):
         if self._b.value:
             _lib.load().fsht_batch_destroy(self._b)

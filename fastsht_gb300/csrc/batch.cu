@@ -499,6 +499,26 @@ extern "C" int fsht_batch_info(const fsht_batch* b, int* nplans, int* nnodes) {
   return FSHT_OK;
 }
 
+extern "C" int fsht_batch_plan_tuning(const fsht_batch* b, int i, int* nside, int* lmax,
+                                      int* precision, int* shapes) {
+  if (!b || i < 0 || i >= (int)b->plans.size()) {
+    fsht_set_error("batch_plan_tuning: no plan %d", i);
+    return FSHT_EINVAL;
+  }
+  const fsht_plan* p = b->plans[i];
+  if (nside) *nside = p->nside;
+  if (lmax) *lmax = p->lmax;
+  if (precision) *precision = p->precision;
+  if (shapes) {
+    shapes[0] = p->fft_mpb;
+    shapes[1] = p->fft_threads;
+    shapes[2] = p->ana_mt;
+    shapes[3] = p->ana_rc;
+    shapes[4] = p->split_part;
+  }
+  return FSHT_OK;
+}
+
 extern "C" int fsht_batch_sync(fsht_batch* b) {
   if (!b) {
     fsht_set_error("null batch");

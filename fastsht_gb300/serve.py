@@ -46,7 +46,7 @@ _KINDS = {"t2alm": _lib.FSHT_JOB_T2ALM, "alm2t": _lib.FSHT_JOB_ALM2T,
           "qu2eb": _lib.FSHT_JOB_QU2EB, "eb2qu": _lib.FSHT_JOB_EB2QU}
 
 
-@dataclass
+@dataclass(eq=False)      # identity: requests are found in queues with `in` / remove()
 class Request:
     kind: str
     nside: int
@@ -78,7 +78,7 @@ class Request:
         return self.kind in ("t2alm", "qu2eb")
 
 
-@dataclass
+@dataclass(eq=False)
 class _Part:
     members: list                     # (request, m0, m1, offset of m0 in this job)
     nmaps: int

@@ -192,6 +192,11 @@ int fsht_measure_fp32_peak(double* tflops);
  * cuBLAS DGEMMs run on (src/sht_core.f90:51-57): on GB300 it is slower than the FP64 FMA
  * pipe, which is why the plain contraction uses DFMA.  No counterpart in the reference. */
 int fsht_measure_dmma_peak(double* tflops);
+/* BF16 tcgen05 UMMA throughput (TFLOP/s) of the split contraction's k-step (ten 128 x n_cols x 16
+ * digit products) with its operands already in shared memory, one CTA per SM: the ceiling of
+ * the contraction's tile shape (n_cols 128) and of a wider one (256).  No counterpart in the
+ * reference. */
+int fsht_measure_umma_rate(int n_cols, double* tflops);
 
 /* Runs one stage of the pipeline on device buffers (testing and profiling hook;
  * no counterpart in the reference, whose stages are internal):
@@ -236,6 +241,13 @@ int fsht_batch_create(const fsht_job* jobs, int njobs, int nslots, size_t worksp
 int fsht_batch_run(fsht_batch* batch);
 /* Number of distinct plans and of nodes in the captured graph (0 before the first run). */
 int fsht_batch_info(const fsht_batch* batch, int* nplans, int* nnodes);
+/* The i-th plan of a batch (0 <= i < nplans): its nside, lmax, precision and the launch shapes
+ * it runs with (after autotuning, when the batch was created with it): shapes[0..4] = FFT maps
+ * per CTA (0: sized from the maps of each call), FFT threads (0: the per-segment default),
+ * FP64 analysis maps per CTA, FP64 rings per chunk, split ring-part k-steps (0: the kernel's
+ * default).  No counterpart in the reference. */
+int fsht_batch_plan_tuning(const fsht_batch* batch, int i, int* nside, int* lmax, int* precision,
+                           int* shapes);
 int fsht_batch_sync(fsht_batch* batch);
 int fsht_batch_destroy(fsht_batch* batch);
 

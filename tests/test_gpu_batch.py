@@ -180,3 +180,42 @@ def test_autotune_picks_a_contraction_shape(precision):
         assert part in (16, 32, 64) and mt == 0 and rc == 0
     tol = 1e-13 if precision == "fp64" else 1e-9
     assert _rel(sht.t2alm(T), a0) <= tol
+
+
+def test_batch_reports_each_plans_tuned_shapes():
+    """An autotuned batch of two buckets and both precisions reports one entry per plan with
+    its key and shapes from the candidate sets, and its results equal an untuned batch's to
+    each form's rounding."""
+    from fastsht_gb300.batch import Batch
+    outs = []
+    for tune in (True, False):
+        b = Batch(nslots=2, autotune=tune)
+        for (ns, lmax, prec) in [(32, 80, "fp64"), (64, 160, "fp64"), (64, 160, "split")]:
+            j = b.add("t2alm", ns, lmax, 12, precision=prec)
+            g = torch.Generator(device=j.inputs[0].device)
+            g.manual_seed(ns + lmax)
+            j.inputs[0].copy_(torch.randn(j.inputs[0].shape, dtype=torch.float64,
+                                          device=j.inputs[0].device, generator=g))
+        b.build()
+        b.run()
+        b.sync()
+        outs.append([t.cpu().numpy() for j in b.jobs for t in j.outputs])
+        tun = b.tunings()
+        b.close()
+        assert len(tun) == 3
+        keys = {(t["nside"], t["lmax"], t["precision"]) for t in tun}
+        assert keys == {(32, 80, "fp64"), (64, 160, "fp64"), (64, 160, "split")}
+        for t in tun:
+            assert (1 <= t["fft_maps_per_cta"] <= 16) if tune else t["fft_maps_per_cta"] == 0
+            if t["precision"] == "fp64":
+                assert t["split_part_steps"] == 0
+                if tune:
+                    assert t["fp64_maps_per_cta"] in (32, 64)
+                    assert t["fp64_rings_per_chunk"] in (8, 16, 32)
+            else:
+                assert t["fp64_maps_per_cta"] == 0 and t["fp64_rings_per_chunk"] == 0
+                if tune:
+                    assert t["split_part_steps"] in (16, 32, 64)
+    for k, (x, y) in enumerate(zip(*outs)):
+        tol = 1e-9 if k == 2 else 1e-13
+        assert _rel(x[None], y[None]) <= tol
