@@ -1164,9 +1164,9 @@ def bench_qu2eb(args, rank, world, local):
 def bench_serving(args, rank, world, local):
     """Open-loop Poisson stream into fastsht_gb300.serve.Server: map2alm or alm2map, T or
     Q/U with equal odds, nside = 2^U{6..log2 max_nside}, lmax = 2 nside, nmaps ~
-    U[1, max_maps], FP64 or split per request (the split form covers map2alm T and Q/U and
-    alm2map T; alm2map Q/U runs FP64), seed 4.  Inputs are device-resident views of one
-    pre-generated N(0,1) pool per nside (no per-request copies).  value = map.SHT/s over the run; p50/p99 latency from arrival to result."""
+    U[1, max_maps], FP64 or split per request, seed 4.  Inputs are device-resident views of
+    one pre-generated N(0,1) pool per nside (no per-request copies); the client discards the
+    results.  value = map.SHT/s over the run; p50/p99 latency from arrival to result."""
     import torch
     from fastsht_gb300 import _lib
     from fastsht_gb300.serve import Server
@@ -1211,7 +1211,9 @@ def bench_serving(args, rank, world, local):
         return [pool[f, :L * L * nm].view(L, L, nm) for f in range(nf)]
 
     budget = args.budget_gb * 1e9
-    srv = Server(hbm_budget=budget, nslots=8, device=local)
+    # the client discards results (it measures the service): outputs leave the budget as
+    # soon as their request completes
+    srv = Server(hbm_budget=budget, nslots=8, device=local, discard_outputs=True)
     # warm-up: every (kind, nside, precision) once, so plans and autotuning are in place
     for kind in kinds:
         for ns in pools:
@@ -1222,11 +1224,13 @@ def bench_serving(args, rank, world, local):
     clocks = ClockSampler(local)
     clocks.start()
     t0 = time.perf_counter()
+    futs = []
     for (ta, kind, ns, lmax, nm, prec) in reqs:
         now = time.perf_counter() - t0
         if ta > now:
             time.sleep(ta - now)
-        srv.submit(kind, ns, lmax, inputs(kind, ns, nm), precision=prec, t_arrival=t0 + ta)
+        futs.append(srv.submit(kind, ns, lmax, inputs(kind, ns, nm), precision=prec,
+                               t_arrival=t0 + ta))
     # requests still queued or running when the last one arrives: a server that keeps up with
     # the offered rate has only the most recent few
     with srv._lock:
@@ -1237,7 +1241,14 @@ def bench_serving(args, rank, world, local):
     clk = clocks.stop()
     st = srv.stats()
     srv.close()
-    mapsht = sum(nm * (2 if kind in ("qu2eb", "eb2qu") else 1) for _, kind, _, _, nm, _ in reqs)
+    failed = {}
+    for f, r in zip(futs, reqs):
+        e = f.exception(timeout=0)
+        if e is not None:
+            key = f"{r[1]} nside {r[2]} {r[5]}: {e!r}"[:300]
+            failed[key] = failed.get(key, 0) + 1
+    ok = [r for f, r in zip(futs, reqs) if f.exception(timeout=0) is None]
+    mapsht = sum(nm * (2 if kind in ("qu2eb", "eb2qu") else 1) for _, kind, _, _, nm, _ in ok)
     line = {
         "metric": METRIC, "value": mapsht / wall, "unit": UNIT, "n_gpus": 1,
         "steps": 1, "warmup": 1, "ms_per_step": wall * 1000.0, "higher_is_better": True,
@@ -1258,7 +1269,9 @@ def bench_serving(args, rank, world, local):
         "backlog_at_last_arrival": backlog,
         "offered_requests_per_s": args.requests / reqs[-1][0],
         "max_parts_per_request": st.get("max_parts"),
-        "requests_per_s": args.requests / wall,
+        "requests_per_s": len(ok) / wall,
+        "failed_requests": sum(failed.values()),
+        "failures": failed,
         "max_inflight": st.get("max_inflight"),
         "high_water_bytes": st.get("high_water_bytes"),
     }

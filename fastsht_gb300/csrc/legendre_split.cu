@@ -48,18 +48,20 @@ struct SliceArgs {
   int* err;              // plan error word (kErrRange when a value misses its scale)
 };
 
-// grid (q in wave, 2 x group), 256 threads = (ring half, map, parity, Re/Im) over one half
-// (32 maps) of a 64-map group, Re/Im fastest, so a warp reads 8 maps' whole 32-byte {S, D}
+// grid (q in wave, 4 x group), 128 threads = (ring half, map, parity, Re/Im) over one quarter
+// (16 maps) of a 64-map group, Re/Im fastest, so a warp reads 8 maps' whole 32-byte {S, D}
 // entries of one ring: every W sector is read once per pass (two passes: the column maximum,
 // then the digits).  The two halves of a column's k-steps go to two threads (shorter serial
-// chains, twice the loads in flight); their maxima meet in shared memory.  256 threads at <= 64
-// registers let a CTA share an SM with the persistent contraction of the previous wave.
-__global__ void __launch_bounds__(256, 4) k_slice_phase(SliceArgs a) {
-  __shared__ double s_mx[128];
-  const int qi = blockIdx.x, g = blockIdx.y >> 1;
+// chains, twice the loads in flight); their maxima meet in shared memory.  128 threads at <= 64
+// registers (8 K registers) let a CTA share an SM with the persistent contraction of the
+// previous wave, whose 320 threads hold 168 registers each.
+constexpr int kSliceThreads = 128;
+__global__ void __launch_bounds__(kSliceThreads, 8) k_slice_phase(SliceArgs a) {
+  __shared__ unsigned long long s_mx[kSliceThreads / 2];
+  const int qi = blockIdx.x, g = blockIdx.y >> 2;
   const int m = m_of_q(a.q0 + qi, a.lmax);
-  const int t = threadIdx.x & 127, half = threadIdx.x >> 7;
-  const int comp = t & 1, p = (t >> 1) & 1, kl = (t >> 2) + 32 * (blockIdx.y & 1);
+  const int t = threadIdx.x & (kSliceThreads / 2 - 1), half = threadIdx.x / (kSliceThreads / 2);
+  const int comp = t & 1, p = (t >> 1) & 1, kl = (t >> 2) + 16 * (blockIdx.y & 3);
   const int k = g * kGroupMaps + kl;
   const int c = comp * kGroupMaps + kl;
   const int i0 = a.ring_i0[m];
@@ -72,25 +74,34 @@ __global__ void __launch_bounds__(256, 4) k_slice_phase(SliceArgs a) {
   const double* col = a.W + ((((long long)m * a.nnorth + i0) * a.kc + k) * 2 + p) * 2 + comp;
   const long long rstride = (long long)a.kc * 4;
   auto val = [&](int r) -> double { return (valid && r < K) ? col[r * rstride] : 0.0; };
-  double mx = 0.0;
+  // The column maximum as FP64 bits with the sign cleared: for finite values the unsigned
+  // integer order is the magnitude order, so the maximum takes integer operations only (an FP64
+  // max runs on GB300's FP64 pipe at two per clock per SM, which bound this pass).
+  constexpr unsigned long long kAbs = 0x7FFFFFFFFFFFFFFFull;
+  unsigned long long mx = 0;
   if (valid) {
     // eight independent loads in flight per thread
     int r = r_begin;
     for (; r + 8 <= r_end; r += 8) {
-      double v[8];
+      unsigned long long v[8];
 #pragma unroll
-      for (int u = 0; u < 8; ++u) v[u] = col[(long long)(r + u) * rstride];
+      for (int u = 0; u < 8; ++u)
+        v[u] = (unsigned long long)__double_as_longlong(col[(long long)(r + u) * rstride]) & kAbs;
 #pragma unroll
-      for (int u = 0; u < 8; ++u) mx = fmax(mx, fabs(v[u]));
+      for (int u = 0; u < 8; ++u) mx = max(mx, v[u]);
     }
-    for (; r < r_end; ++r) mx = fmax(mx, fabs(col[(long long)r * rstride]));
+    for (; r < r_end; ++r)
+      mx = max(mx, (unsigned long long)__double_as_longlong(col[(long long)r * rstride]) & kAbs);
   }
   if (half) s_mx[t] = mx;
   __syncthreads();
-  if (!half) s_mx[t] = fmax(mx, s_mx[t]);
+  if (!half) s_mx[t] = max(mx, s_mx[t]);
   __syncthreads();
   mx = s_mx[t];
-  const int E = (mx > 0.0) ? ilogb(mx) + 1 : kEmptyExp;
+  // |v| < 2^E for every value of the column (a subnormal maximum takes E = -1021; a
+  // non-finite one gives an exponent its digits report as out of range)
+  const int ef = (int)(mx >> 52);
+  const int E = mx == 0 ? kEmptyExp : (ef == 0 ? -1021 : ef - 1022);
   if (!half) a.EB[(((long long)qi * 2 + p) * a.ngroups + g) * kCols + c] = E;
   unsigned char* base = a.WS + ((size_t)(qi * 2 + p) * a.ngroups + g) * a.row_bytes +
                         (c >> 3) * 256 + (c & 7) * 16;
@@ -192,20 +203,34 @@ __global__ void __launch_bounds__(128) k_lambda_digits(LamArgs a) {
   unsigned char* base = a.lbuf + (size_t)(a.lam_off[q] - a.lam_off[a.q0]) * kSlices * kATileBytes;
   const FshtLamRow* tab = a.tab + tri_off(m, a.lmax);
 
-  double x = 0.0, s1 = 0.0, s2 = 0.0;
+  // The recursion runs in df64 (FP32 pairs, ~48 significand bits) on the FP32 pipe: the
+  // digits need 2^-31 of each row's scale and the recursion's error stays near l 2^-48, while
+  // GB300's FP64 pipe (two operations per clock per SM) would bound this kernel.  The state
+  // (s1, s2) = (mu_l, mu_{l-1}) 2^-et is kept within 2^-32 .. 2^32 after every step: one step
+  // changes max(|s1|, |s2|) by at most a factor 2 up and beta / 2 >= 2^-14 down, so FP32
+  // exponents (and the low parts, 2^24 below) never leave the normal range.
+  float xh = 0.f, xl = 0.f, s1h = 0.f, s1l = 0.f, s2h = 0.f, s2l = 0.f;
   int et = 0;
   if (valid) {
-    int e;
-    x = a.cth[i0 + r];
+    int e, k;
+    const double x = a.cth[i0 + r];
+    double s1;
     rec_seed(a.sth[i0 + r], a.pref[m], m, s1, e);
-    et = 600 * e;
+    const double f = frexp(s1, &k);           // s1 = f 2^k, |f| in [0.5, 1)
+    et = 600 * e + k;
+    s1h = __double2float_rn(f);
+    s1l = __double2float_rn(f - (double)s1h);
+    xh = __double2float_rn(x);
+    xl = __double2float_rn(x - (double)xh);
   }
   // the 32 recursion rows of the current block, staged in shared memory (uniform reads
-  // off the dependency chain)
-  __shared__ double s_beta[kLamBlock];
+  // off the dependency chain): -beta as a df64 pair
+  __shared__ float2 s_beta[kLamBlock];
   __shared__ int s_erow[kLamBlock];
   if (tid < kLamBlock && m + tid <= a.lmax) {
-    s_beta[tid] = tab[tid].beta;
+    const double b = tab[tid].beta;
+    const float bh = __double2float_rn(b);
+    s_beta[tid] = make_float2(-bh, -__double2float_rn(b - (double)bh));
     s_erow[tid] = tab[tid].erow;
   }
   __syncthreads();
@@ -217,34 +242,32 @@ __global__ void __launch_bounds__(128) k_lambda_digits(LamArgs a) {
       const int j = lb + jj;
       unsigned long long pk = 0;
       if (m + j <= a.lmax) {
-        const double beta = s_beta[jj];
+        const float2 nb = s_beta[jj];
         const int erow = s_erow[jj];
         if (j > 0) {
-          const double t = beta * s2;
-          const double nx = fma(x, s1, -t);
-          s2 = s1;
-          s1 = nx;
+          float nh, nl;
+          dd::dot2(xh, xl, s1h, s1l, nb.x, nb.y, s2h, s2l, nh, nl);   // x mu1 - beta mu2
+          s2h = s1h;
+          s2l = s1l;
+          s1h = nh;
+          s1l = nl;
+          const float am = fmaxf(fabsf(s1h), fabsf(s2h));
+          if (am > 0x1p32f) {
+            s1h *= 0x1p-64f; s1l *= 0x1p-64f; s2h *= 0x1p-64f; s2l *= 0x1p-64f;
+            et += 64;
+          } else if (am < 0x1p-32f && am > 0.f) {
+            s1h *= 0x1p64f; s1l *= 0x1p64f; s2h *= 0x1p64f; s2l *= 0x1p64f;
+            et -= 64;
+          }
         }
         if (valid) {
           uint16_t d[4];
-          bad |= tc::digits4(s1, erow - et, d);
+          bad |= tc::digits4_df(s1h, s1l, erow - et, d);
           pk = (unsigned long long)d[0] | ((unsigned long long)d[1] << 16) |
                ((unsigned long long)d[2] << 32) | ((unsigned long long)d[3] << 48);
         }
       }
       S[jj & 1][jj >> 1][tid] = pk;
-    }
-    {   // keep the state within 2^-300 .. 2^300; growth per block stays far below 2^300
-      const double am = fmax(fabs(s1), fabs(s2));
-      if (am > 0x1p300) {
-        s1 *= 0x1p-600;
-        s2 *= 0x1p-600;
-        et += 600;
-      } else if (am > 0.0 && am < 0x1p-300) {
-        s1 *= 0x1p600;
-        s2 *= 0x1p600;
-        et -= 600;
-      }
     }
     __syncthreads();
     // write-out: unit u = (r8: 3 bits, khalf, rg, ks: 3 bits, parity); a warp stores 512
@@ -283,7 +306,9 @@ __global__ void __launch_bounds__(128) k_lambda_digits(LamArgs a) {
       }
     }
     if (tid < kLamBlock && m + lb + kLamBlock + tid <= a.lmax) {
-      s_beta[tid] = tab[lb + kLamBlock + tid].beta;
+      const double b = tab[lb + kLamBlock + tid].beta;
+      const float bh = __double2float_rn(b);
+      s_beta[tid] = make_float2(-bh, -__double2float_rn(b - (double)bh));
       s_erow[tid] = tab[lb + kLamBlock + tid].erow;
     }
     __syncthreads();
@@ -489,23 +514,34 @@ __global__ void __launch_bounds__(kThreadsG, 1) k_split_gemm(GemmArgs a) {
         const bool add = ks0 > 0 || a.accumulate;
         // Im of m = 0 does not exist
         const bool comp_ok = !(comp == 1 && w.m == 0);
-        for (int c0 = cbeg; c0 < cbeg + kCols / 2; c0 += 16) {
-          uint32_t v0[16], v1[16], v2[16], v3[16];
-          tc::tmem_ld16(lane_base + 0 * kCols + c0, v0);
-          tc::tmem_ld16(lane_base + 1 * kCols + c0, v1);
-          tc::tmem_ld16(lane_base + 2 * kCols + c0, v2);
-          tc::tmem_ld16(lane_base + 3 * kCols + c0, v3);
+        // Drain first: this lane's row of the warp's 64 columns leaves TMEM as FP32 (hi, lo)
+        // pairs (the four levels joined exactly, FP32 pipe only, 128 registers) and TMEM goes
+        // back to the UMMA issuer before any FP64 instruction or global store, so the next
+        // part's products run under the rest of this epilogue (on GB300 the FP64 pipe does two
+        // operations per clock per SM: the joining additions of a whole part take ~4 us).
+        float hh[kCols / 2], ll[kCols / 2];
+#pragma unroll
+        for (int c = 0; c < kCols / 2; c += 8) {
+          uint32_t v0[8], v1[8], v2[8], v3[8];
+          tc::tmem_ld8(lane_base + 0 * kCols + cbeg + c, v0);
+          tc::tmem_ld8(lane_base + 1 * kCols + cbeg + c, v1);
+          tc::tmem_ld8(lane_base + 2 * kCols + cbeg + c, v2);
+          tc::tmem_ld8(lane_base + 3 * kCols + cbeg + c, v3);
           tc::tmem_wait_ld();
-          if (c0 == cbeg + kCols / 2 - 16) {
-            // every accumulator column of this part is in registers: hand TMEM back
-            tc::tc_fence_before();
-            tc::mbar_arrive(&h.tempty);
-          }
+#pragma unroll
+          for (int j = 0; j < 8; ++j)
+            combine_levels_pair(v0[j], v1[j], v2[j], v3[j], hh[c + j], ll[c + j]);
+        }
+        tc::tc_fence_before();
+        tc::mbar_arrive(&h.tempty);
+#pragma unroll
+        for (int cr = 0; cr < kCols / 2; cr += 16) {
+          const int c0 = cbeg + cr;
           // this lane's row of the block, staged
 #pragma unroll
           for (int j = 0; j < 16; ++j)
             stg[stg_at(lane, j)] =
-                rowok ? levels_scaled(v0[j], v1[j], v2[j], v3[j], rh, rl, re + s_ce[c0 + j]) : 0.0;
+                rowok ? pair_scaled(hh[cr + j], ll[cr + j], rh, rl, re + s_ce[c0 + j]) : 0.0;
           __syncwarp();
           // the block back out by rows: lanes 0-15 one row, 16-31 the next, 16 maps each.
           // Adds go out as fire-and-forget reductions (no load latency in the epilogue); one
@@ -592,19 +628,33 @@ __global__ void __launch_bounds__(128) k_lambda_digits_T(LamTArgs a) {
       a.lbuf + (size_t)(a.lam_offT[q] - a.lam_offT[a.q0]) * kSlices * kATileBytes +
       (tid >> 3) * 256 + (tid & 7) * 16;
   const FshtLamRow* tab = a.tab + tri_off(m, a.lmax);
-  double x = 0.0, s1 = 0.0, s2 = 0.0;
+  // df64 recursion with per-step rescaling, as in k_lambda_digits
+  float xh = 0.f, xl = 0.f, s1h = 0.f, s1l = 0.f, s2h = 0.f, s2l = 0.f;
   int et = 0;
   if (valid) {
-    int e;
-    x = a.cth[i0 + r];
+    int e, kx;
+    const double x = a.cth[i0 + r];
+    double s1;
     rec_seed(a.sth[i0 + r], a.pref[m], m, s1, e);
-    et = 600 * e;
+    const double f = frexp(s1, &kx);
+    et = 600 * e + kx;
+    s1h = __double2float_rn(f);
+    s1l = __double2float_rn(f - (double)s1h);
+    xh = __double2float_rn(x);
+    xl = __double2float_rn(x - (double)xh);
   }
-  __shared__ FshtLamRow s_tab[32];
+  __shared__ float4 s_bd[32];             // (-beta, Dm) as df64 pairs
+  __shared__ int s_dx[32];
   bool bad = false;
   for (int kl = 0; kl < nkl; ++kl) {
     __syncthreads();                      // the previous block's rows are no longer read
-    if (tid < 32 && m + kl * 32 + tid <= a.lmax) s_tab[tid] = tab[kl * 32 + tid];
+    if (tid < 32 && m + kl * 32 + tid <= a.lmax) {
+      const FshtLamRow rw = tab[kl * 32 + tid];
+      const float bh = __double2float_rn(rw.beta), dh = __double2float_rn(rw.dm);
+      s_bd[tid] = make_float4(-bh, -__double2float_rn(rw.beta - (double)bh), dh,
+                              __double2float_rn(rw.dm - (double)dh));
+      s_dx[tid] = rw.dx;
+    }
     __syncthreads();
 #pragma unroll
     for (int half = 0; half < 2; ++half) {
@@ -620,14 +670,28 @@ __global__ void __launch_bounds__(128) k_lambda_digits_T(LamTArgs a) {
         const int j = kl * 32 + half * 16 + jj;
         uint16_t d[4] = {0, 0, 0, 0};
         if (m + j <= a.lmax) {
-          const FshtLamRow rw = s_tab[half * 16 + jj];
+          const float4 bd = s_bd[half * 16 + jj];
           if (j > 0) {
-            const double t = rw.beta * s2;
-            const double nx = fma(x, s1, -t);
-            s2 = s1;
-            s1 = nx;
+            float nh, nl;
+            dd::dot2(xh, xl, s1h, s1l, bd.x, bd.y, s2h, s2l, nh, nl);   // x mu1 - beta mu2
+            s2h = s1h;
+            s2l = s1l;
+            s1h = nh;
+            s1l = nl;
+            const float am = fmaxf(fabsf(s1h), fabsf(s2h));
+            if (am > 0x1p32f) {
+              s1h *= 0x1p-64f; s1l *= 0x1p-64f; s2h *= 0x1p-64f; s2l *= 0x1p-64f;
+              et += 64;
+            } else if (am < 0x1p-32f && am > 0.f) {
+              s1h *= 0x1p64f; s1l *= 0x1p64f; s2h *= 0x1p64f; s2l *= 0x1p64f;
+              et -= 64;
+            }
           }
-          if (valid) bad |= tc::digits4(s1 * rw.dm, a.eag - et - rw.dx, d);
+          if (valid) {
+            float vh, vl;
+            dd::mul(s1h, s1l, bd.z, bd.w, vh, vl);                     // mu Dm
+            bad |= tc::digits4_df(vh, vl, a.eag - et - s_dx[half * 16 + jj], d);
+          }
         }
         const int par = jj & 1, slot = jj >> 1;
 #pragma unroll
@@ -647,16 +711,6 @@ __global__ void __launch_bounds__(128) k_lambda_digits_T(LamTArgs a) {
               base + (((size_t)(par * nrb + rb) * nkl + kl) * kSlices + dd) * kATileBytes +
               half * 128) = o;
         }
-    }
-    const double am = fmax(fabs(s1), fabs(s2));
-    if (am > 0x1p300) {
-      s1 *= 0x1p-600;
-      s2 *= 0x1p-600;
-      et += 600;
-    } else if (am > 0.0 && am < 0x1p-300) {
-      s1 *= 0x1p600;
-      s2 *= 0x1p600;
-      et -= 600;
     }
   }
   if (bad) atomicOr(a.err, tc::kErrRange);
@@ -689,9 +743,13 @@ __global__ void __launch_bounds__(128) k_slice_alm(SliceAArgs a) {
     const long long row = comp == 0 ? (long long)m * L1 + l : (L1 - m) * L1 + (l - m);
     return a.alm[row * a.ld + a.k0 + k];
   };
-  double mx = 0.0;
-  for (int idx = 0; idx < cnt; ++idx) mx = fmax(mx, fabs(val(idx)));
-  const int E = (mx > 0.0) ? ilogb(mx) + 1 : kEmptyExp;
+  // column maximum on FP64 bits with the sign cleared (integer operations, as in
+  // k_slice_phase)
+  unsigned long long mx = 0;
+  for (int idx = 0; idx < cnt; ++idx)
+    mx = max(mx, (unsigned long long)__double_as_longlong(val(idx)) & 0x7FFFFFFFFFFFFFFFull);
+  const int ef = (int)(mx >> 52);
+  const int E = mx == 0 ? kEmptyExp : (ef == 0 ? -1021 : ef - 1022);
   a.EB[(((long long)qi * 2 + p) * a.ngroups + g) * kCols + c] = E;
   const int nkl = (cnt0 + kKStep - 1) / kKStep;
   unsigned char* base = a.WS +
@@ -991,7 +1049,7 @@ int fsht_launch_split_slice(fsht_plan* p, int w, const double2* W, unsigned char
   sa.WS = WS;
   sa.EB = EB;
   sa.err = p->d_err;
-  k_slice_phase<<<dim3(wv[1] - wv[0], 2 * sa.ngroups), 256, 0, s>>>(sa);
+  k_slice_phase<<<dim3(wv[1] - wv[0], 4 * sa.ngroups), kSliceThreads, 0, s>>>(sa);
   FSHT_LAUNCH_CHECK();
   return FSHT_OK;
 }

@@ -77,9 +77,10 @@ constexpr size_t kPolStageBytes = (size_t)2 * 2 * (kPolBlock / 2) * kPolStride *
 
 __global__ void __launch_bounds__(128) k_lambda_digits_pol(LamPArgs a) {
   extern __shared__ __align__(16) unsigned long long S[];     // [part][parity][row][ring]
-  __shared__ double s_beta[kPolBlock];
+  // per staged l: -beta, c1, c2, c3, c4 as df64 pairs
+  __shared__ float2 s_beta[kPolBlock];
   __shared__ int s_erow[kPolBlock];
-  __shared__ FshtPolRow s_pc[kPolBlock];
+  __shared__ float2 s_pc[kPolBlock][4];
   const int q = a.q0 + blockIdx.x;
   const int m = m_of_q(q, a.lmax);
   const int i0 = a.ring_i0[m];
@@ -95,25 +96,41 @@ __global__ void __launch_bounds__(128) k_lambda_digits_pol(LamPArgs a) {
       a.lbuf + (size_t)(2 * (a.lam_off[q] - a.lam_off[a.q0])) * kSlices * kATileBytes;
   const FshtLamRow* tab = a.tab + tri_off(m, a.lmax);
   const FshtPolRow* ptab = a.ptab + tri_off(m, a.lmax);
+  auto pair = [](double v) {
+    const float h = __double2float_rn(v);
+    return make_float2(h, __double2float_rn(v - (double)h));
+  };
   auto stage = [&](int j0) {
     if (tid < kPolBlock && m + j0 + tid <= a.lmax) {
-      s_beta[tid] = tab[j0 + tid].beta;
+      s_beta[tid] = pair(-tab[j0 + tid].beta);
       s_erow[tid] = tab[j0 + tid].erow;
-      s_pc[tid] = ptab[j0 + tid];
+      const FshtPolRow c = ptab[j0 + tid];
+      s_pc[tid][0] = pair(c.c1);
+      s_pc[tid][1] = pair(c.c2);
+      s_pc[tid][2] = pair(c.c3);
+      s_pc[tid][3] = pair(c.c4);
     }
   };
 
-  double x = 0.0, inv_s2 = 0.0, b_w = 0.0, c_w = 0.0, s1 = 0.0, s2 = 0.0;
+  // The recursion and the lambda1 / lambda2 forms run in df64 on the FP32 pipe (about 80 FP32
+  // instructions per step against ten FP64 operations, which GB300 runs at two per clock per
+  // SM); the state is rescaled after every step as in k_lambda_digits.
+  float2 x = make_float2(0.f, 0.f), is2 = x, bw = x, cw = x, s1 = x, s2 = x;
   int et = 0;
   if (valid) {
-    int e;
+    int e, kx;
     const double sth = a.sth[i0 + r];
-    x = a.cth[i0 + r];
-    inv_s2 = 1.0 / (sth * sth);
-    b_w = x * inv_s2;
-    c_w = (double)m * inv_s2;
-    rec_seed(sth, a.pref[m], m, s1, e);
-    et = 600 * e;
+    const double xd = a.cth[i0 + r];
+    const double inv_s2 = 1.0 / (sth * sth);
+    double sd;
+    rec_seed(sth, a.pref[m], m, sd, e);
+    const double f = frexp(sd, &kx);
+    et = 600 * e + kx;
+    s1 = pair(f);
+    x = pair(xd);
+    is2 = pair(inv_s2);
+    bw = pair(xd * inv_s2);
+    cw = pair((double)m * inv_s2);
   }
   stage(0);
   __syncthreads();
@@ -129,39 +146,40 @@ __global__ void __launch_bounds__(128) k_lambda_digits_pol(LamPArgs a) {
       unsigned long long pk1 = 0, pk2 = 0;
       if (m + j <= a.lmax) {
         if (j > 0) {
-          const double t = s_beta[jj] * s2;
-          const double nx = fma(x, s1, -t);
+          const float2 nb = s_beta[jj];
+          float2 n;
+          dd::dot2(x.x, x.y, s1.x, s1.y, nb.x, nb.y, s2.x, s2.y, n.x, n.y);   // x mu1 - beta mu2
           s2 = s1;
-          s1 = nx;
+          s1 = n;
+          const float am = fmaxf(fabsf(s1.x), fabsf(s2.x));
+          if (am > 0x1p32f) {
+            s1.x *= 0x1p-64f; s1.y *= 0x1p-64f; s2.x *= 0x1p-64f; s2.y *= 0x1p-64f;
+            et += 64;
+          } else if (am < 0x1p-32f && am > 0.f) {
+            s1.x *= 0x1p64f; s1.y *= 0x1p64f; s2.x *= 0x1p64f; s2.y *= 0x1p64f;
+            et -= 64;
+          }
         }
         if (valid) {
-          const FshtPolRow c = s_pc[jj];
-          const double u = s2 * c.c1;
-          const double l1 = fma(u, b_w, -s1 * fma(c.c2, inv_s2, c.c3));
-          const double l2 = fma(-s1, c.c4 * x, u) * c_w;
+          const float2 c1 = s_pc[jj][0], c2 = s_pc[jj][1], c3 = s_pc[jj][2], c4 = s_pc[jj][3];
+          float2 u, t, c4x, v, l1, l2;
+          dd::mul(s2.x, s2.y, c1.x, c1.y, u.x, u.y);                          // mu2 c1
+          dd::dot2(c2.x, c2.y, is2.x, is2.y, c3.x, c3.y, 1.f, 0.f, t.x, t.y);  // c2/sin^2 + c3
+          dd::dot2(u.x, u.y, bw.x, bw.y, -s1.x, -s1.y, t.x, t.y, l1.x, l1.y);
+          dd::mul(c4.x, c4.y, x.x, x.y, c4x.x, c4x.y);
+          dd::dot2(u.x, u.y, 1.f, 0.f, -s1.x, -s1.y, c4x.x, c4x.y, v.x, v.y);
+          dd::mul(v.x, v.y, cw.x, cw.y, l2.x, l2.y);                          // (..) m/sin^2
           uint16_t d[4];
-          bad |= tc::digits4(l1, s_erow[jj] - et, d);
+          bad |= tc::digits4_df(l1.x, l1.y, s_erow[jj] - et, d);
           pk1 = (unsigned long long)d[0] | ((unsigned long long)d[1] << 16) |
                 ((unsigned long long)d[2] << 32) | ((unsigned long long)d[3] << 48);
-          bad |= tc::digits4(l2, s_erow[jj] - et, d);
+          bad |= tc::digits4_df(l2.x, l2.y, s_erow[jj] - et, d);
           pk2 = (unsigned long long)d[0] | ((unsigned long long)d[1] << 16) |
                 ((unsigned long long)d[2] << 32) | ((unsigned long long)d[3] << 48);
         }
       }
       Sidx(0, jj & 1, jj >> 1, tid) = pk1;
       Sidx(1, jj & 1, jj >> 1, tid) = pk2;
-    }
-    {
-      const double am = fmax(fabs(s1), fabs(s2));
-      if (am > 0x1p300) {
-        s1 *= 0x1p-600;
-        s2 *= 0x1p-600;
-        et += 600;
-      } else if (am > 0.0 && am < 0x1p-300) {
-        s1 *= 0x1p600;
-        s2 *= 0x1p600;
-        et -= 600;
-      }
     }
     __syncthreads();
     const int t = lb / (2 * kRows);
@@ -421,21 +439,30 @@ __global__ void __launch_bounds__(kThreadsG, 1) k_split_gemm_pol(GemmPArgs a) {
           const bool neg = part == 1 && ((w.field == 0) == (comp == 1));
           const int cbeg = comp * (kCols / 2);
           const bool tgt_ok = !(tgt == 1 && w.m == 0);    // Im of m = 0 does not exist
-          for (int c0 = cbeg; c0 < cbeg + kCols / 2; c0 += 16) {
-            uint32_t v0[16], v1[16], v2[16], v3[16];
-            tc::tmem_ld16(lane_base + 0 * kCols + c0, v0);
-            tc::tmem_ld16(lane_base + 1 * kCols + c0, v1);
-            tc::tmem_ld16(lane_base + 2 * kCols + c0, v2);
-            tc::tmem_ld16(lane_base + 3 * kCols + c0, v3);
+          // drain first (as in k_split_gemm): the warp's 64 columns leave TMEM as FP32 (hi, lo)
+          // pairs and TMEM goes back to the UMMA issuer before the FP64 work and the stores
+          float hh[kCols / 2], ll[kCols / 2];
+#pragma unroll
+          for (int c = 0; c < kCols / 2; c += 8) {
+            uint32_t v0[8], v1[8], v2[8], v3[8];
+            tc::tmem_ld8(lane_base + 0 * kCols + cbeg + c, v0);
+            tc::tmem_ld8(lane_base + 1 * kCols + cbeg + c, v1);
+            tc::tmem_ld8(lane_base + 2 * kCols + cbeg + c, v2);
+            tc::tmem_ld8(lane_base + 3 * kCols + cbeg + c, v3);
             tc::tmem_wait_ld();
-            if (c0 == cbeg + kCols / 2 - 16) {
-              tc::tc_fence_before();
-              tc::mbar_arrive(&h.tempty);
-            }
+#pragma unroll
+            for (int j = 0; j < 8; ++j)
+              combine_levels_pair(v0[j], v1[j], v2[j], v3[j], hh[c + j], ll[c + j]);
+          }
+          tc::tc_fence_before();
+          tc::mbar_arrive(&h.tempty);
+#pragma unroll
+          for (int cr = 0; cr < kCols / 2; cr += 16) {
+            const int c0 = cbeg + cr;
 #pragma unroll
             for (int j = 0; j < 16; ++j) {
               const double uu =
-                  rowok ? levels_scaled(v0[j], v1[j], v2[j], v3[j], rh, rl, re + s_ce[part][c0 + j])
+                  rowok ? pair_scaled(hh[cr + j], ll[cr + j], rh, rl, re + s_ce[part][c0 + j])
                         : 0.0;
               stg[stg_at(lane, j)] = neg ? -uu : uu;
             }
@@ -506,8 +533,9 @@ struct LamTPArgs {
 };
 
 __global__ void __launch_bounds__(128) k_lambda_digits_T_pol(LamTPArgs a) {
-  __shared__ FshtLamRow s_tab[32];
-  __shared__ FshtPolRow s_pc[32];
+  __shared__ float2 s_bd[32][2];          // -beta, Dm as df64 pairs
+  __shared__ int s_dx[32];
+  __shared__ float2 s_pc[32][4];          // c1..c4 as df64 pairs
   const int q = a.q0 + blockIdx.x;
   const int m = m_of_q(q, a.lmax);
   const int i0 = a.ring_i0[m];
@@ -524,24 +552,41 @@ __global__ void __launch_bounds__(128) k_lambda_digits_T_pol(LamTPArgs a) {
       (tid >> 3) * 256 + (tid & 7) * 16;
   const FshtLamRow* tab = a.tab + tri_off(m, a.lmax);
   const FshtPolRow* ptab = a.ptab + tri_off(m, a.lmax);
-  double x = 0.0, inv_s2 = 0.0, b_w = 0.0, c_w = 0.0, s1 = 0.0, s2 = 0.0;
+  auto pair = [](double v) {
+    const float h = __double2float_rn(v);
+    return make_float2(h, __double2float_rn(v - (double)h));
+  };
+  // df64 recursion and lambda1 / lambda2 forms, as in k_lambda_digits_pol
+  float2 x = make_float2(0.f, 0.f), is2 = x, bw = x, cw = x, s1 = x, s2 = x;
   int et = 0;
   if (valid) {
-    int e;
+    int e, kx;
     const double sth = a.sth[i0 + r];
-    x = a.cth[i0 + r];
-    inv_s2 = 1.0 / (sth * sth);
-    b_w = x * inv_s2;
-    c_w = (double)m * inv_s2;
-    rec_seed(sth, a.pref[m], m, s1, e);
-    et = 600 * e;
+    const double xd = a.cth[i0 + r];
+    const double inv_s2 = 1.0 / (sth * sth);
+    double sd;
+    rec_seed(sth, a.pref[m], m, sd, e);
+    const double f = frexp(sd, &kx);
+    et = 600 * e + kx;
+    s1 = pair(f);
+    x = pair(xd);
+    is2 = pair(inv_s2);
+    bw = pair(xd * inv_s2);
+    cw = pair((double)m * inv_s2);
   }
   bool bad = false;
   for (int kl = 0; kl < nkl; ++kl) {
     __syncthreads();
     if (tid < 32 && m + kl * 32 + tid <= a.lmax) {
-      s_tab[tid] = tab[kl * 32 + tid];
-      s_pc[tid] = ptab[kl * 32 + tid];
+      const FshtLamRow rw = tab[kl * 32 + tid];
+      const FshtPolRow c = ptab[kl * 32 + tid];
+      s_bd[tid][0] = pair(-rw.beta);
+      s_bd[tid][1] = pair(rw.dm);
+      s_dx[tid] = rw.dx;
+      s_pc[tid][0] = pair(c.c1);
+      s_pc[tid][1] = pair(c.c2);
+      s_pc[tid][2] = pair(c.c3);
+      s_pc[tid][3] = pair(c.c4);
     }
     __syncthreads();
 #pragma unroll 1
@@ -560,20 +605,36 @@ __global__ void __launch_bounds__(128) k_lambda_digits_T_pol(LamTPArgs a) {
         const int j = kl * 32 + half * 16 + jj;
         uint16_t d1[4] = {0, 0, 0, 0}, d2[4] = {0, 0, 0, 0};
         if (m + j <= a.lmax) {
-          const FshtLamRow rw = s_tab[half * 16 + jj];
+          const int jr = half * 16 + jj;
           if (j > 0) {
-            const double t = rw.beta * s2;
-            const double nx = fma(x, s1, -t);
+            const float2 nb = s_bd[jr][0];
+            float2 n;
+            dd::dot2(x.x, x.y, s1.x, s1.y, nb.x, nb.y, s2.x, s2.y, n.x, n.y);
             s2 = s1;
-            s1 = nx;
+            s1 = n;
+            const float am = fmaxf(fabsf(s1.x), fabsf(s2.x));
+            if (am > 0x1p32f) {
+              s1.x *= 0x1p-64f; s1.y *= 0x1p-64f; s2.x *= 0x1p-64f; s2.y *= 0x1p-64f;
+              et += 64;
+            } else if (am < 0x1p-32f && am > 0.f) {
+              s1.x *= 0x1p64f; s1.y *= 0x1p64f; s2.x *= 0x1p64f; s2.y *= 0x1p64f;
+              et -= 64;
+            }
           }
           if (valid) {
-            const FshtPolRow c = s_pc[half * 16 + jj];
-            const double u = s2 * c.c1;
-            const double l1 = fma(u, b_w, -s1 * fma(c.c2, inv_s2, c.c3));
-            const double l2 = fma(-s1, c.c4 * x, u) * c_w;
-            bad |= tc::digits4(l1 * rw.dm, a.eag - et - rw.dx, d1);
-            bad |= tc::digits4(l2 * rw.dm, a.eag - et - rw.dx, d2);
+            const float2 c1 = s_pc[jr][0], c2 = s_pc[jr][1], c3 = s_pc[jr][2], c4 = s_pc[jr][3];
+            const float2 dm = s_bd[jr][1];
+            float2 u, t, c4x, v, l1, l2;
+            dd::mul(s2.x, s2.y, c1.x, c1.y, u.x, u.y);
+            dd::dot2(c2.x, c2.y, is2.x, is2.y, c3.x, c3.y, 1.f, 0.f, t.x, t.y);
+            dd::dot2(u.x, u.y, bw.x, bw.y, -s1.x, -s1.y, t.x, t.y, l1.x, l1.y);
+            dd::mul(c4.x, c4.y, x.x, x.y, c4x.x, c4x.y);
+            dd::dot2(u.x, u.y, 1.f, 0.f, -s1.x, -s1.y, c4x.x, c4x.y, v.x, v.y);
+            dd::mul(v.x, v.y, cw.x, cw.y, l2.x, l2.y);
+            dd::mul(l1.x, l1.y, dm.x, dm.y, l1.x, l1.y);
+            dd::mul(l2.x, l2.y, dm.x, dm.y, l2.x, l2.y);
+            bad |= tc::digits4_df(l1.x, l1.y, a.eag - et - s_dx[jr], d1);
+            bad |= tc::digits4_df(l2.x, l2.y, a.eag - et - s_dx[jr], d2);
           }
         }
         const int par = jj & 1, slot = jj >> 1;
@@ -599,16 +660,6 @@ __global__ void __launch_bounds__(128) k_lambda_digits_T_pol(LamTPArgs a) {
                            kATileBytes +
                 half * 128) = o;
           }
-    }
-    const double am = fmax(fabs(s1), fabs(s2));
-    if (am > 0x1p300) {
-      s1 *= 0x1p-600;
-      s2 *= 0x1p-600;
-      et += 600;
-    } else if (am > 0.0 && am < 0x1p-300) {
-      s1 *= 0x1p600;
-      s2 *= 0x1p600;
-      et -= 600;
     }
   }
   if (bad) atomicOr(a.err, tc::kErrRange);

@@ -110,15 +110,18 @@ __device__ __forceinline__ void combine_levels_pair(uint32_t v0, uint32_t v1, ui
 // and one FP64 addition joins the two parts: one FP64 instruction per element instead of
 // five (two conversions, an addition, two multiplications).  Exponents below the FP64 range
 // give 0, so an empty column (exponent kEmptyExp) writes zeros.
-__device__ __forceinline__ double levels_scaled(uint32_t v0, uint32_t v1, uint32_t v2,
-                                                uint32_t v3, float fh, float fl, int e) {
-  float hi, lo;
-  combine_levels_pair(v0, v1, v2, v3, hi, lo);
+__device__ __forceinline__ double pair_scaled(float hi, float lo, float fh, float fl, int e) {
   const float p = __fmul_rn(hi, fh);
   float q = __fmaf_rn(hi, fh, -p);
   q = __fmaf_rn(hi, fl, q);
   q = __fmaf_rn(lo, fh, q);
   return dd_to_double(p, q, e);
+}
+__device__ __forceinline__ double levels_scaled(uint32_t v0, uint32_t v1, uint32_t v2,
+                                                uint32_t v3, float fh, float fl, int e) {
+  float hi, lo;
+  combine_levels_pair(v0, v1, v2, v3, hi, lo);
+  return pair_scaled(hi, lo, fh, fl, e);
 }
 
 // A positive or negative FP64 factor as a df64 pair (setup, once per row).

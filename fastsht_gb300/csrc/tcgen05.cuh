@@ -124,6 +124,13 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t (&v)[16]) {
       : "r"(taddr)
       : "memory");
 }
+__device__ __forceinline__ void tmem_ld8(uint32_t taddr, uint32_t (&v)[8]) {
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+               : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]),
+                 "=r"(v[6]), "=r"(v[7])
+               : "r"(taddr)
+               : "memory");
+}
 __device__ __forceinline__ void tmem_wait_ld() {
   asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 }
@@ -152,6 +159,20 @@ __device__ __forceinline__ uint16_t bf16_scale_2m8(uint16_t h) {
 // word (kErrRange), so a wrong result never passes silently.
 constexpr int kErrTimeout = 1;   // error-word bit: a bounded wait expired
 constexpr int kErrRange = 2;     // error-word bit: a value fell outside its digit scale
+// The balanced base-256 digits of T (0 <= T <= 2^30), times sgn.
+__device__ __forceinline__ void digits_of_T(long long T, int sgn, uint16_t (&s)[4]) {
+  int d[4];
+#pragma unroll
+  for (int j = 3; j >= 1; --j) {
+    const int dj = (int)((T + 128) & 255) - 128;
+    d[j] = dj;
+    T = (T - dj) >> 8;
+  }
+  d[0] = (int)T;
+#pragma unroll
+  for (int j = 0; j < 4; ++j) s[j] = bf16_of_int(sgn * d[j]);
+}
+
 __device__ __forceinline__ bool digits4(double v, int E, uint16_t (&s)[4]) {
   const unsigned long long bits = (unsigned long long)__double_as_longlong(v);
   const int eb = (int)((bits >> 52) & 0x7FF);
@@ -168,16 +189,37 @@ __device__ __forceinline__ bool digits4(double v, int E, uint16_t (&s)[4]) {
     }
   }
   const int neg = (bits >> 63) ? -1 : 1;
-  int d[4];
-#pragma unroll
-  for (int j = 3; j >= 1; --j) {
-    const int dj = (int)((T + 128) & 255) - 128;
-    d[j] = dj;
-    T = (T - dj) >> 8;
+  digits_of_T(T, neg, s);
+  return out_of_range;
+}
+
+// f 2^(30 - E + 24) as a signed fixed-point integer, toward zero (zero and subnormal f give 0:
+// they are below every digit); saturates far above the 2^54 a value inside its scale reaches.
+__device__ __forceinline__ long long fixed_of_float(float f, int E) {
+  const unsigned b = __float_as_uint(f);
+  const int eb = (int)((b >> 23) & 0xFF);
+  if (eb == 0) return 0;
+  const long long M = (long long)((b & 0x7FFFFFu) | 0x800000u);
+  const int sh = eb - 126 + 30 - E;           // f = M 2^(eb - 150): sh <= 30 when |f| < 2^E
+  const long long X = sh >= 0 ? (M << min(sh, 38)) : (sh > -40 ? (M >> -sh) : 0);
+  return (b >> 31) ? -X : X;
+}
+
+// digits4 of a df64 value hi + lo (|lo| <= ulp(hi)): T = round(|hi + lo| 2^(30 - E)) formed
+// exactly in 64-bit fixed point (hi and lo are 24-bit significands 2^24 ulps apart), integer
+// operations only; the same digits as digits4 of the FP64 value hi + lo except at rounding
+// ties below 2^-24 of a T unit.  Non-finite hi or |hi + lo| >= 2^E report out of range.
+__device__ __forceinline__ bool digits4_df(float hi, float lo, int E, uint16_t (&s)[4]) {
+  const unsigned bh = __float_as_uint(hi);
+  bool out_of_range = ((bh >> 23) & 0xFF) == 0xFF;
+  const long long X = fixed_of_float(hi, E) + fixed_of_float(lo, E);
+  const long long U = X < 0 ? -X : X;
+  long long T = out_of_range ? 0 : ((U + (1ll << 23)) >> 24);
+  if (T > (1ll << 30)) {                      // out of range: saturate and report
+    T = 1ll << 30;
+    out_of_range = true;
   }
-  d[0] = (int)T;
-#pragma unroll
-  for (int j = 0; j < 4; ++j) s[j] = bf16_of_int(neg * d[j]);
+  digits_of_T(T, X < 0 ? -1 : 1, s);
   return out_of_range;
 }
 

@@ -14,8 +14,9 @@ the server reports p50 / p99 latency beside throughput, overall and per precisio
 Head-of-line blocking: a large request (an FP64 transform at nside 2048 takes tens of
 seconds) must not hold back small ones.  Three rules keep it from doing so:
   * a job's estimated GPU time (a cost model of its FFT and Legendre work at the
-    precision's rate) is capped at max_job_s: larger requests run as several jobs
-    along maps, so they give their slot and memory back regularly;
+    precision's rate) is capped at max_job_s, in whole 64-map tiles: larger requests run
+    as several jobs along maps, so they give their slot and memory back regularly (a job
+    of fewer than 64 maps costs a whole tile, so requests are never split below one);
   * jobs estimated below small_s are "small": they run on high-priority streams, so
     their thread blocks are scheduled ahead of the waiting blocks of large kernels;
   * `reserved` of the slots (the high-priority ones) only take small jobs, so a burst
@@ -42,6 +43,8 @@ import torch
 
 from . import _lib
 
+_TILE_MAPS = 64       # maps per contraction tile (FP64 and split kernels alike)
+
 _KINDS = {"t2alm": _lib.FSHT_JOB_T2ALM, "alm2t": _lib.FSHT_JOB_ALM2T,
           "qu2eb": _lib.FSHT_JOB_QU2EB, "eb2qu": _lib.FSHT_JOB_EB2QU}
 
@@ -56,7 +59,6 @@ class Request:
     inputs: list                      # device tensors in the library layout (or host arrays)
     t_arrival: float
     future: Future = field(default_factory=Future)
-    outputs: list = field(default_factory=list)
     t_admit: float = 0.0
     t_done: float = 0.0
     parts: int = 0                    # jobs this request ran in (split along maps)
@@ -64,6 +66,7 @@ class Request:
     ready: torch.cuda.Event = None    # inputs written (submitting thread's stream)
     next_map: int = 0                 # first map not yet admitted
     done_parts: list = field(default_factory=list)   # (m0, outputs) per finished piece
+    held: list = field(default_factory=list)         # jobs whose outputs hold its pieces
 
     @property
     def key(self):
@@ -86,7 +89,9 @@ class _Part:
     keep: list                        # tensors the job reads (kept alive until it ends)
     event: torch.cuda.Event = None
     slot: int = -1
-    nbytes: int = 0
+    nbytes: int = 0                   # budget charged: inputs + outputs + workspace
+    out_bytes: int = 0                # the outputs' share, held until every member completes
+    holders: int = 0                  # members not yet completed
 
 
 def _maps_shape(nside, nmaps):
@@ -101,12 +106,16 @@ class Server:
     """Continuous-batching SHT server on one GPU.
 
     hbm_budget: device bytes the server may hold for in-flight jobs (inputs, outputs and
-    workspaces); nslots: concurrent CUDA streams; fuse_maps: most maps one fused job may
-    gather from waiting requests of the same configuration (0 disables fusing).
+    workspaces); a job's output stays charged until every request with a piece in it has
+    completed (the pieces are views of it), and a request split into several jobs is joined
+    into one output at completion, outside the budget for that moment; nslots: concurrent CUDA
+    streams; fuse_maps: most maps one fused job may gather from waiting requests of the same
+    configuration (0 disables fusing); discard_outputs: complete futures with None and drop
+    the results (a client that only measures the service).
     """
 
     def __init__(self, hbm_budget=150e9, nslots=8, device=None, poll_s=5e-5, fuse_maps=128,
-                 max_job_s=1.0, small_s=0.05, reserved=2):
+                 max_job_s=1.0, small_s=0.05, reserved=2, discard_outputs=False):
         self.device = torch.device("cuda", torch.cuda.current_device() if device is None else device)
         self.budget = int(hbm_budget)
         self.nslots = nslots
@@ -115,6 +124,7 @@ class Server:
         self.max_job_s = float(max_job_s)
         self.small_s = float(small_s)
         self.reserved = max(0, min(int(reserved), nslots - 1))
+        self.discard_outputs = bool(discard_outputs)
         with torch.cuda.device(self.device):
             # slots [0, reserved): high-priority streams for small jobs only
             self.streams = [torch.cuda.Stream(self.device, priority=-1 if i < self.reserved else 0)
@@ -246,15 +256,21 @@ class Server:
 
     @staticmethod
     def cost_s(kind, nside, lmax, precision, n):
-        """Rough GPU seconds of n maps of a request (scheduling only): the ring FFTs at about
-        0.4 ms (df64) / 1.3 ms (FP64) per map per field at nside 1024, scaled by the pixel
-        count, and the Legendre contraction's 4 nside (lmax+1)(lmax+2) flop per map (four times
-        that per Q/U pair) at about 1 TFLOP/s in FP64 and 80 TFLOP/s in the split form."""
+        """Rough GPU seconds of one job of n maps (scheduling only).  The contractions work on
+        tiles of 64 maps, so a job of fewer maps costs a whole tile: the Legendre term counts
+        ceil(n / 64) tiles of 64 maps at 4 nside (lmax+1)(lmax+2) flop per map (four times that
+        per Q/U pair), about 1 TFLOP/s in FP64 and 80 TFLOP/s in the split form, whose
+        recursion also runs once per job (about 30 ms at nside 1024 / lmax 2047, scaled by
+        nside (lmax+1)^2); the ring FFTs cost about 0.4 ms (df64) / 1.3 ms (FP64) per map per
+        field at nside 1024, scaled by the pixel count."""
         nf = 2 if kind in ("qu2eb", "eb2qu") else 1
         split = precision == "split"
-        fft = (0.4e-3 if split else 1.3e-3) * (nside / 1024.0) ** 2 * nf
-        leg = 4.0 * nside * (lmax + 1) * (lmax + 2) * (4 if nf == 2 else 1)
-        return n * (fft + leg / (80e12 if split else 1.0e12))
+        fft = n * (0.4e-3 if split else 1.3e-3) * (nside / 1024.0) ** 2 * nf
+        tiles = -(-n // _TILE_MAPS)
+        leg = (_TILE_MAPS * tiles * 4.0 * nside * (lmax + 1) * (lmax + 2) *
+               (4 if nf == 2 else 1))
+        rec = 0.03 * (nside / 1024.0) * ((lmax + 1) / 2048.0) ** 2 if split else 0.0
+        return fft + leg / (80e12 if split else 1.0e12) + rec
 
     def _req_cost(self, req, n):
         return self.cost_s(req.kind, req.nside, req.lmax, req.precision, n)
@@ -319,8 +335,10 @@ class Server:
             return False
         avail = self.budget - self._used
         # maps per job under the duration cap (at least one)
-        per_map = self._req_cost(head, 1)
-        n_cap = max(1, int(self.max_job_s / per_map)) if per_map > 0 else 1 << 30
+        # maps per job under the duration cap, in whole 64-map tiles: a job of fewer maps
+        # costs a whole tile, so splitting below one only multiplies the work
+        per_tile = self._req_cost(head, _TILE_MAPS)
+        n_cap = _TILE_MAPS * max(1, int(self.max_job_s / per_tile)) if per_tile > 0 else 1 << 30
         group = self._gather(head)
         while True:
             total = min(sum(r.nmaps - r.next_map for r in group), n_cap)
@@ -329,9 +347,16 @@ class Server:
                 break
             group.pop()                 # the fused job does not fit whole: fuse fewer
         if fit is None:
-            if self._used == 0:
-                raise RuntimeError(f"request (nside {head.nside}, lmax {head.lmax}) does not fit "
-                                   f"the {self.budget}-byte budget even for one map")
+            if not self._inflight:
+                # nothing running will free memory: one map of this request (beside the outputs
+                # of its finished pieces) can never fit
+                err = ValueError(f"request (nside {head.nside}, lmax {head.lmax}) does not fit "
+                                 f"the {self.budget}-byte budget even for one map")
+                if not head.future.done():
+                    head.future.set_exception(err)
+                if head in self._pending:
+                    self._pending.remove(head)
+                self._release(head)
             return False
         n, kc, need = fit
         slot = self._slot_for(self._req_cost(head, n) <= self.small_s)
@@ -388,12 +413,26 @@ class Server:
         self.max_fused = max(self.max_fused, len(members))
         self._used += need
         self.high_water = max(self.high_water, self._used)
-        self._inflight.append(_Part(members, n, outs, ins + [ws], ev, slot, need))
+        self._inflight.append(_Part(members, n, outs, ins + [ws], ev, slot, need,
+                                    out_bytes=sum(o.numel() * o.element_size() for o in outs),
+                                    holders=len(members)))
         self.max_inflight = max(self.max_inflight, len(self._inflight))
         return True
 
+    def _release(self, r):
+        """r has completed or failed: the jobs holding its pieces lose a holder, and a job's
+        outputs leave the budget when no request holds a piece of them."""
+        for p in r.held:
+            p.holders -= 1
+            if p.holders == 0:
+                self._used -= p.out_bytes
+                p.outputs = []
+        r.held = []
+        r.done_parts = []
+
     def _finish(self, part: _Part):
-        self._used -= part.nbytes
+        self._used -= part.nbytes - part.out_bytes     # inputs and workspace
+        part.keep = []
         self._free_slots.append(part.slot)
         head = part.members[0][0]
         rc = _lib.load().fsht_plan_check(self._plan(head.nside, head.lmax, head.precision))
@@ -404,6 +443,8 @@ class Server:
                     r.future.set_exception(err)
                 if r in self._pending:
                     self._pending.remove(r)
+                r.held.append(part)
+                self._release(r)
             return
         for r, m0, m1, off in part.members:
             if len(part.members) == 1 and m0 == 0 and m1 == r.nmaps:
@@ -413,21 +454,28 @@ class Server:
             else:
                 piece = [o[off:off + (m1 - m0)] for o in part.outputs]
             r.done_parts.append((m0, piece))
+            r.held.append(part)
+            if r.future.done():           # failed in another job: nothing to assemble
+                self._release(r)
+                continue
             if sum(p[0].shape[-1 if r.analysis else 0] for _, p in r.done_parts) < r.nmaps:
                 continue
-            r.done_parts.sort(key=lambda t: t[0])
-            with torch.cuda.device(self.device):
-                if len(r.done_parts) == 1:
-                    r.outputs = [t.contiguous() for t in r.done_parts[0][1]]
-                else:
-                    dim = -1 if r.analysis else 0
-                    r.outputs = [torch.cat([p[f] for _, p in r.done_parts], dim=dim)
-                                 for f in range(r.nfields)]
-                torch.cuda.current_stream(self.device).synchronize()
-            r.done_parts = []
+            result = None
+            if not self.discard_outputs:
+                r.done_parts.sort(key=lambda t: t[0])
+                with torch.cuda.device(self.device):
+                    if len(r.done_parts) == 1:
+                        result = [t.contiguous() for t in r.done_parts[0][1]]
+                    else:
+                        dim = -1 if r.analysis else 0
+                        result = [torch.cat([p[f] for _, p in r.done_parts], dim=dim)
+                                  for f in range(r.nfields)]
+                    torch.cuda.current_stream(self.device).synchronize()
+            self._release(r)
             r.t_done = time.perf_counter()
+            r.inputs = []                 # the client's tensors: not kept by the statistics
             self.completed.append(r)
-            r.future.set_result(r.outputs)
+            r.future.set_result(result)
 
     def _loop(self):
         try:

@@ -1,0 +1,111 @@
+"""CPU model of the split form's df64 lambda recursion (legendre_split.cu k_lambda_digits and
+its synthesis / spin-2 forms): the same FP32 operation sequence as dd::dot2 (products exact
+through a wider format, as fmaf is), the per-step rescaling of the state into 2^-32 .. 2^32,
+and the integer fixed-point digits of tc::digits4_df.  It checks the two facts the kernels
+rely on: the state never leaves FP32's normal range, and the recursion stays within a small
+part of the 2^-31 digit quantum of the FP64 recursion over thousands of steps."""
+import math
+
+import numpy as np
+import pytest
+
+f32 = np.float32
+
+
+def _two_sum(a, b):
+    s = f32(a + b)
+    v = f32(s - a)
+    return s, f32(f32(a - f32(s - v)) + f32(b - v))
+
+
+def _fmaf(a, b, c):
+    return f32(float(a) * float(b) + float(c))
+
+
+def _dot2(x1h, x1l, y1h, y1l, x2h, x2l, y2h, y2l):
+    p1 = f32(x1h * y1h)
+    e1 = _fmaf(x1h, y1h, -p1)
+    p2 = f32(x2h * y2h)
+    e2 = _fmaf(x2h, y2h, -p2)
+    s, e = _two_sum(p1, p2)
+    t = f32(e1 + e2)
+    for a, b in ((x1h, y1l), (x1l, y1h), (x2h, y2l), (x2l, y2h)):
+        t = _fmaf(a, b, t)
+    h = f32(s + f32(e + t))
+    return h, f32(f32(e + t) - f32(h - s))
+
+
+def _pair(v):
+    h = f32(v)
+    return h, f32(v - float(h))
+
+
+def _coeffs(l, m):
+    a = math.sqrt((2 * l - 1) * (2 * l + 1) / (l * l - m * m))
+    b = math.sqrt(((l - 1) ** 2 - m * m) / ((2 * l - 3) * (2 * l - 1))) * a
+    return a, b
+
+
+def _fixed_of_float(f, E):
+    b = int(np.float32(f).view(np.uint32))
+    eb = (b >> 23) & 0xFF
+    if eb == 0:
+        return 0
+    M = (b & 0x7FFFFF) | 0x800000
+    sh = eb - 126 + 30 - E
+    X = M << min(sh, 38) if sh >= 0 else (M >> -sh if sh > -40 else 0)
+    return -X if b >> 31 else X
+
+
+@pytest.mark.parametrize("m,x,lmax", [(2000, 0.0, 2047), (1000, 0.99, 2047), (3000, 1e-4, 4095),
+                                      (0, 0.01, 2047), (10, 0.5, 2047)])
+def test_df64_recursion_tracks_fp64(m, x, lmax):
+    s1d, s2d, ed = 0.75, 0.0, 0
+    s1h, s1l = _pair(0.75)
+    s2h = s2l = f32(0)
+    et = 0
+    xh, xl = _pair(x)
+    a_prev = None
+    worst = 0.0
+    for l in range(m + 1, lmax + 1):
+        a, b = _coeffs(l, m)
+        beta = 0.0 if l == m + 1 else b / (a * a_prev)
+        a_prev = a
+        s1d, s2d = x * s1d - beta * s2d, s1d
+        am = max(abs(s1d), abs(s2d))
+        if am > 2.0 ** 300:
+            s1d, s2d, ed = s1d * 2.0 ** -600, s2d * 2.0 ** -600, ed + 600
+        elif 0 < am < 2.0 ** -300:
+            s1d, s2d, ed = s1d * 2.0 ** 600, s2d * 2.0 ** 600, ed - 600
+        bh, bl = _pair(-beta)
+        nh, nl = _dot2(xh, xl, s1h, s1l, bh, bl, s2h, s2l)
+        s2h, s2l, s1h, s1l = s1h, s1l, nh, nl
+        amf = max(abs(s1h), abs(s2h))
+        if amf > f32(2.0 ** 32):
+            s1h, s1l, s2h, s2l = (f32(v * f32(2.0 ** -64)) for v in (s1h, s1l, s2h, s2l))
+            et += 64
+        elif 0 < amf < f32(2.0 ** -32):
+            s1h, s1l, s2h, s2l = (f32(v * f32(2.0 ** 64)) for v in (s1h, s1l, s2h, s2l))
+            et -= 64
+        hi = max(abs(s1h), abs(s2h))
+        assert hi == 0 or 2.0 ** -46 <= hi <= 2.0 ** 33     # normal, with room for lo
+        ref = math.ldexp(s1d, ed)
+        got = math.ldexp(float(s1h) + float(s1l), et)
+        scale = math.ldexp(max(abs(s1d), abs(s2d)), ed)
+        if scale > 0:
+            worst = max(worst, abs(got - ref) / scale)
+    assert worst < 2.0 ** -31 / 2, worst
+
+
+def test_fixed_point_digits_round_like_fp64():
+    """T = round(|hi + lo| 2^(30 - E)) from the two floats' bits equals the FP64 rounding."""
+    rng = np.random.default_rng(1)
+    for _ in range(20000):
+        E = int(rng.integers(-90, 90))
+        v = rng.uniform(-1, 1) * 2.0 ** (E - int(rng.integers(0, 40)))
+        hi, lo = _pair(v)
+        X = _fixed_of_float(hi, E) + _fixed_of_float(lo, E)
+        T = (abs(X) + (1 << 23)) >> 24
+        vv = float(hi) + float(lo)
+        assert abs(T - round(abs(vv) * 2.0 ** (30 - E))) <= 1
+        assert T == 0 or (X < 0) == (vv < 0)
