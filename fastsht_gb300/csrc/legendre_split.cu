@@ -12,12 +12,13 @@
 //   (a tile with more rings is accumulated in parts of <= 1024, each drained and added);
 //   levels 2 and 3 carry weights 2^-16 and 2^-24, so FP32 rounding there is far
 //   below the ~2^-31 representation error.
-// The epilogue combines the four levels on the FP32 pipe and applies the scales with one
-// FP64 addition per element (levels_scaled).
+// The epilogue drains TMEM as FP32 (hi, lo) pairs (the levels joined on the FP32 pipe), hands
+// it back to the UMMA issuer, and then applies the scales with one FP64 addition per element
+// (pair_scaled).
 //
 // Three kernels per wave of m:
 //   k_slice_phase    P -> digit tiles WS and column exponents EB (per 64-map group);
-//   k_lambda_digits  the FP64 exponent-rescaled recursion, once per (m, ring) for all
+//   k_lambda_digits  the exponent-rescaled recursion in df64, once per (m, ring) for all
 //                    map groups, written as lambda digit tiles into a staging buffer that
 //                    holds one wave of m (a few GB at most: no P_lm table is kept);
 //   k_split_gemm     persistent, one CTA per SM walking 128 x 128 output tiles, both

@@ -10,7 +10,7 @@
 // (checked against the oracle), so they share the spin-0 row scales.
 //
 //   k_pol_table          per (l, m): c1..c4 of the scaled lambda1/lambda2 formulas;
-//   k_lambda_digits_pol  the FP64 recursion (mu form) once per (m, ring), lambda1 and
+//   k_lambda_digits_pol  the df64 recursion (mu form) once per (m, ring), lambda1 and
 //                        lambda2 digit tiles into the wave's staging buffer;
 //   k_split_gemm_pol     persistent; unit = (q, l-tile, parity, field, 64-map group): per
 //                        ring part the lambda1 product then the lambda2 product through the

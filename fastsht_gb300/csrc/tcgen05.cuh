@@ -193,34 +193,52 @@ __device__ __forceinline__ bool digits4(double v, int E, uint16_t (&s)[4]) {
   return out_of_range;
 }
 
-// f 2^(30 - E + 24) as a signed fixed-point integer, toward zero (zero and subnormal f give 0:
-// they are below every digit); saturates far above the 2^54 a value inside its scale reaches.
-__device__ __forceinline__ long long fixed_of_float(float f, int E) {
+// f 2^k for an FP32 f, by moving its exponent field (no FP64 and no exp2f range limit): values
+// that would leave FP32's normal range below give 0 (far under every digit), above give
+// infinity (reported out of range by the caller).
+__device__ __forceinline__ float scale_pow2(float f, int k) {
   const unsigned b = __float_as_uint(f);
   const int eb = (int)((b >> 23) & 0xFF);
-  if (eb == 0) return 0;
-  const long long M = (long long)((b & 0x7FFFFFu) | 0x800000u);
-  const int sh = eb - 126 + 30 - E;           // f = M 2^(eb - 150): sh <= 30 when |f| < 2^E
-  const long long X = sh >= 0 ? (M << min(sh, 38)) : (sh > -40 ? (M >> -sh) : 0);
-  return (b >> 31) ? -X : X;
+  if (eb == 0) return 0.f;
+  const int ne = eb + k;
+  if (ne <= 0) return 0.f;
+  if (ne >= 255) return __uint_as_float((b & 0x80000000u) | 0x7F800000u);
+  return __uint_as_float((b & 0x807FFFFFu) | ((unsigned)ne << 23));
 }
 
-// digits4 of a df64 value hi + lo (|lo| <= ulp(hi)): T = round(|hi + lo| 2^(30 - E)) formed
-// exactly in 64-bit fixed point (hi and lo are 24-bit significands 2^24 ulps apart), integer
-// operations only; the same digits as digits4 of the FP64 value hi + lo except at rounding
-// ties below 2^-24 of a T unit.  Non-finite hi or |hi + lo| >= 2^E report out of range.
+// BF16 bits of a float that holds an integer of magnitude <= 256 (its low 16 bits are zero).
+__device__ __forceinline__ uint16_t bf16_of_small_int_float(float d) {
+  return (uint16_t)(__float_as_uint(d) >> 16);
+}
+
+// Four balanced base-256 digits of a df64 value hi + lo (|lo| <= ulp(hi)) against 2^E, on the
+// FP32 pipe: w = (hi + lo) 2^(6 - E) (exponent moves, exact), d0 = rint(w_hi), then
+// r = (w_hi - d0) + w_lo (the one rounding, below 2^-26) and d_{j+1} = rint(256 r_j),
+// r_{j+1} = 256 r_j - d_{j+1} (exact).  |d0| <= 64 and |d1..3| <= 128 as for digits4 (the
+// digits may differ in sign: every product stays an exact integer and the level bounds hold),
+// residual below 1.5 2^-25.  Non-finite hi or |hi + lo| > 2^E (beyond rounding) report out of
+// range; the digits are then zero.
 __device__ __forceinline__ bool digits4_df(float hi, float lo, int E, uint16_t (&s)[4]) {
-  const unsigned bh = __float_as_uint(hi);
-  bool out_of_range = ((bh >> 23) & 0xFF) == 0xFF;
-  const long long X = fixed_of_float(hi, E) + fixed_of_float(lo, E);
-  const long long U = X < 0 ? -X : X;
-  long long T = out_of_range ? 0 : ((U + (1ll << 23)) >> 24);
-  if (T > (1ll << 30)) {                      // out of range: saturate and report
-    T = 1ll << 30;
-    out_of_range = true;
+  const int k = 6 - E;
+  const float wh = scale_pow2(hi, k), wl = scale_pow2(lo, k);
+  const bool out_of_range = !(fabsf(wh) <= 64.5f);     // also catches infinity and NaN
+  float d0 = rintf(wh);
+  float r = __fadd_rn(__fsub_rn(wh, d0), wl);
+  float t = __fmul_rn(r, 256.f);
+  const float d1 = rintf(t);
+  t = __fmul_rn(__fsub_rn(t, d1), 256.f);
+  const float d2 = rintf(t);
+  t = __fmul_rn(__fsub_rn(t, d2), 256.f);
+  const float d3 = rintf(t);
+  if (out_of_range) {
+    s[0] = s[1] = s[2] = s[3] = 0;
+    return true;
   }
-  digits_of_T(T, X < 0 ? -1 : 1, s);
-  return out_of_range;
+  s[0] = bf16_of_small_int_float(d0);
+  s[1] = bf16_of_small_int_float(d1);
+  s[2] = bf16_of_small_int_float(d2);
+  s[3] = bf16_of_small_int_float(d3);
+  return false;
 }
 
 }  // namespace tc

@@ -1,7 +1,7 @@
 """CPU model of the split form's df64 lambda recursion (legendre_split.cu k_lambda_digits and
 its synthesis / spin-2 forms): the same FP32 operation sequence as dd::dot2 (products exact
 through a wider format, as fmaf is), the per-step rescaling of the state into 2^-32 .. 2^32,
-and the integer fixed-point digits of tc::digits4_df.  It checks the two facts the kernels
+and the FP32 digit sequence of tc::digits4_df.  It checks the two facts the kernels
 rely on: the state never leaves FP32's normal range, and the recursion stays within a small
 part of the 2^-31 digit quantum of the FP64 recursion over thousands of steps."""
 import math
@@ -46,15 +46,19 @@ def _coeffs(l, m):
     return a, b
 
 
-def _fixed_of_float(f, E):
-    b = int(np.float32(f).view(np.uint32))
-    eb = (b >> 23) & 0xFF
-    if eb == 0:
-        return 0
-    M = (b & 0x7FFFFF) | 0x800000
-    sh = eb - 126 + 30 - E
-    X = M << min(sh, 38) if sh >= 0 else (M >> -sh if sh > -40 else 0)
-    return -X if b >> 31 else X
+def _digits_df(hi, lo, E):
+    """tc::digits4_df: the FP32 operation sequence (exponent moves are exact)."""
+    wh, wl = f32(math.ldexp(float(hi), 6 - E)), f32(math.ldexp(float(lo), 6 - E))
+    assert abs(wh) <= 64.5
+    d0 = f32(np.rint(wh))
+    r = f32(f32(wh - d0) + wl)
+    t = f32(r * f32(256))
+    d1 = f32(np.rint(t))
+    t = f32(f32(t - d1) * f32(256))
+    d2 = f32(np.rint(t))
+    t = f32(f32(t - d2) * f32(256))
+    d3 = f32(np.rint(t))
+    return [float(d) for d in (d0, d1, d2, d3)], float(wh) + float(wl)
 
 
 @pytest.mark.parametrize("m,x,lmax", [(2000, 0.0, 2047), (1000, 0.99, 2047), (3000, 1e-4, 4095),
@@ -97,15 +101,16 @@ def test_df64_recursion_tracks_fp64(m, x, lmax):
     assert worst < 2.0 ** -31 / 2, worst
 
 
-def test_fixed_point_digits_round_like_fp64():
-    """T = round(|hi + lo| 2^(30 - E)) from the two floats' bits equals the FP64 rounding."""
+def test_fp32_digits_reconstruct_the_value():
+    """digits4_df's digits are integers within the bounds the exact UMMA levels need, and
+    d0 + d1 2^-8 + d2 2^-16 + d3 2^-24 is within 1.5 2^-25 of (hi + lo) 2^(6 - E)."""
     rng = np.random.default_rng(1)
     for _ in range(20000):
         E = int(rng.integers(-90, 90))
         v = rng.uniform(-1, 1) * 2.0 ** (E - int(rng.integers(0, 40)))
         hi, lo = _pair(v)
-        X = _fixed_of_float(hi, E) + _fixed_of_float(lo, E)
-        T = (abs(X) + (1 << 23)) >> 24
-        vv = float(hi) + float(lo)
-        assert abs(T - round(abs(vv) * 2.0 ** (30 - E))) <= 1
-        assert T == 0 or (X < 0) == (vv < 0)
+        d, w = _digits_df(hi, lo, E)
+        assert all(x == int(x) for x in d)
+        assert abs(d[0]) <= 64 and all(abs(x) <= 128 for x in d[1:])
+        rec = d[0] + d[1] * 2.0 ** -8 + d[2] * 2.0 ** -16 + d[3] * 2.0 ** -24
+        assert abs(rec - w) <= 1.5 * 2.0 ** -25
