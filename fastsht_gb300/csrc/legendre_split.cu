@@ -53,11 +53,11 @@ struct SliceArgs {
 // (16 maps) of a 64-map group, Re/Im fastest, so a warp reads 8 maps' whole 32-byte {S, D}
 // entries of one ring: every W sector is read once per pass (two passes: the column maximum,
 // then the digits).  The two halves of a column's k-steps go to two threads (shorter serial
-// chains, twice the loads in flight); their maxima meet in shared memory.  128 threads at <= 64
-// registers (8 K registers) let a CTA share an SM with the persistent contraction of the
+// chains, twice the loads in flight); their maxima meet in shared memory.  128 threads at <= 85
+// registers (72 used: 9 K) fit in the register file beside the persistent contraction of the
 // previous wave, whose 320 threads hold 168 registers each.
 constexpr int kSliceThreads = 128;
-__global__ void __launch_bounds__(kSliceThreads, 8) k_slice_phase(SliceArgs a) {
+__global__ void __launch_bounds__(kSliceThreads, 6) k_slice_phase(SliceArgs a) {
   __shared__ unsigned long long s_mx[kSliceThreads / 2];
   const int qi = blockIdx.x, g = blockIdx.y >> 2;
   const int m = m_of_q(a.q0 + qi, a.lmax);
@@ -118,7 +118,7 @@ __global__ void __launch_bounds__(kSliceThreads, 8) k_slice_phase(SliceArgs a) {
 #pragma unroll
       for (int j = 0; j < 8; ++j) {
         uint16_t q4[4] = {0, 0, 0, 0};
-        if (E != kEmptyExp) bad |= tc::digits4(v[hh * 8 + j], E, q4);
+        if (E != kEmptyExp) bad |= tc::digits4_f(v[hh * 8 + j], E, q4);
         for (int d = 0; d < kSlices; ++d) sl[d][j] = q4[d];
       }
       for (int d = 0; d < kSlices; ++d) {
@@ -762,7 +762,7 @@ __global__ void __launch_bounds__(128) k_slice_alm(SliceAArgs a) {
       uint16_t sl[kSynthPlanes][8];
       for (int j = 0; j < 8; ++j) {
         uint16_t q4[4] = {0, 0, 0, 0};
-        if (E != kEmptyExp) bad |= tc::digits4(val(kl * kKStep + half * 8 + j), E, q4);
+        if (E != kEmptyExp) bad |= tc::digits4_f(val(kl * kKStep + half * 8 + j), E, q4);
         for (int d = 0; d < kSlices; ++d) sl[d][j] = q4[d];
         for (int d = 1; d < kSlices; ++d) sl[kSlices - 1 + d][j] = tc::bf16_scale_2m8(q4[d]);
       }

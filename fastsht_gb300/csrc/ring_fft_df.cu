@@ -66,23 +66,51 @@ __device__ __forceinline__ double dd_out(float h, float l, int sh) {
 
 // Loads one ring pair (or one half-length ring) of map values into the FFT buffer's slots as
 // raw FP64 pairs, takes the block-wide largest exponent field, then converts every slot to
-// df64 scaled by 2^-sh (sh = that exponent, unbiased; 0 for an all-zero ring).  Thread t owns
-// slots t, t + nt, ... in both passes, so only the exponent needs a barrier.  emax is a
-// shared slot that is zero on entry.  Returns sh.
+// df64 scaled by 2^-sh (sh = that exponent, unbiased; 0 for an all-zero ring).  The barrier
+// that publishes the exponent also orders the raw stores before the conversion pass, in which
+// thread t converts slots t, t + nt, ... in place.  emax is a shared slot that is zero on
+// entry.  Returns sh.
 template <class Sw>
 __device__ __forceinline__ int load_scaled(cdd* buf, const Sw& S, int cnt, const double* xa,
                                            const double* xb, int stride, int* emax) {
   double2* raw = reinterpret_cast<double2*>(buf);
   const int tid = threadIdx.x, nt = blockDim.x;
   int em = 0;
-  // unrolled so that several loads are in flight per thread (the maps may be host memory read
-  // over the host link, with microseconds of latency)
+  // Loads unrolled so that several are in flight per thread (the maps may be host memory read
+  // over the host link, with microseconds of latency), 16 bytes each where the ring lies on
+  // 16-byte boundaries (ring starts are even pixel indices; a caller's map view may not be).
+  const bool a16 = ((reinterpret_cast<unsigned long long>(xa) |
+                     reinterpret_cast<unsigned long long>(xb)) & 15) == 0;
+  if (stride == 2 && xb == xa + 1 && a16) {
+    // half-length ring: (x[2j], x[2j + 1]) is one 16-byte load
+    const double2* x2 = reinterpret_cast<const double2*>(xa);
 #pragma unroll 4
-  for (int j = tid; j < cnt; j += nt) {
-    const double va = __ldg(&xa[(long long)stride * j]);
-    const double vb = xb ? __ldg(&xb[(long long)stride * j]) : 0.0;
-    em = max(em, max(dd_exp_field(va), dd_exp_field(vb)));
-    raw[S(j)] = make_double2(va, vb);
+    for (int j = tid; j < cnt; j += nt) {
+      const double2 v = __ldg(&x2[j]);
+      em = max(em, max(dd_exp_field(v.x), dd_exp_field(v.y)));
+      raw[S(j)] = v;
+    }
+  } else if (stride == 1 && (cnt & 1) == 0 && a16) {
+    // ring pair: two consecutive samples of each ring per load
+    const double2* a2 = reinterpret_cast<const double2*>(xa);
+    const double2* b2 = reinterpret_cast<const double2*>(xb);
+#pragma unroll 4
+    for (int j = tid; j < cnt / 2; j += nt) {
+      const double2 va = __ldg(&a2[j]);
+      const double2 vb = xb ? __ldg(&b2[j]) : make_double2(0.0, 0.0);
+      em = max(em, max(max(dd_exp_field(va.x), dd_exp_field(va.y)),
+                       max(dd_exp_field(vb.x), dd_exp_field(vb.y))));
+      raw[S(2 * j)] = make_double2(va.x, vb.x);
+      raw[S(2 * j + 1)] = make_double2(va.y, vb.y);
+    }
+  } else {
+#pragma unroll 4
+    for (int j = tid; j < cnt; j += nt) {
+      const double va = __ldg(&xa[(long long)stride * j]);
+      const double vb = xb ? __ldg(&xb[(long long)stride * j]) : 0.0;
+      em = max(em, max(dd_exp_field(va), dd_exp_field(vb)));
+      raw[S(j)] = make_double2(va, vb);
+    }
   }
   em = __reduce_max_sync(0xffffffffu, em);
   if ((tid & 31) == 0) atomicMax(emax, em);

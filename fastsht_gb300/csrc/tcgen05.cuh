@@ -211,33 +211,70 @@ __device__ __forceinline__ uint16_t bf16_of_small_int_float(float d) {
   return (uint16_t)(__float_as_uint(d) >> 16);
 }
 
-// Four balanced base-256 digits of a df64 value hi + lo (|lo| <= ulp(hi)) against 2^E, on the
-// FP32 pipe: w = (hi + lo) 2^(6 - E) (exponent moves, exact), d0 = rint(w_hi), then
-// r = (w_hi - d0) + w_lo (the one rounding, below 2^-26) and d_{j+1} = rint(256 r_j),
-// r_{j+1} = 256 r_j - d_{j+1} (exact).  |d0| <= 64 and |d1..3| <= 128 as for digits4 (the
-// digits may differ in sign: every product stays an exact integer and the level bounds hold),
-// residual below 1.5 2^-25.  Non-finite hi or |hi + lo| > 2^E (beyond rounding) report out of
-// range; the digits are then zero.
-__device__ __forceinline__ bool digits4_df(float hi, float lo, int E, uint16_t (&s)[4]) {
-  const int k = 6 - E;
-  const float wh = scale_pow2(hi, k), wl = scale_pow2(lo, k);
-  const bool out_of_range = !(fabsf(wh) <= 64.5f);     // also catches infinity and NaN
-  float d0 = rintf(wh);
-  float r = __fadd_rn(__fsub_rn(wh, d0), wl);
-  float t = __fmul_rn(r, 256.f);
-  const float d1 = rintf(t);
+// Round to the nearest integer, ties to even, on the FP32 add pipe (|x| <= 2^22): adding and
+// subtracting 1.5 2^23 leaves no fraction bits.
+__device__ __forceinline__ float rint_small(float x) {
+  return __fsub_rn(__fadd_rn(x, 0x1.8p23f), 0x1.8p23f);
+}
+
+// The digits of w = wh + wl (|wl| <= ulp(wh), |w| <= 64.5) on the FP32 pipe: d0 = rint(wh),
+// r = (wh - d0) + wl (the one rounding, below 2^-26), d_{j+1} = rint(256 r_j),
+// r_{j+1} = 256 r_j - d_{j+1} (exact).  |d0| <= 64, |d1..3| <= 128 (digits may differ in sign:
+// every product stays an exact integer and the level bounds of the contraction hold),
+// residual below 1.5 2^-25; the BF16 digits are the high halves of the FP32 digits.
+__device__ __forceinline__ void digits_of_pair(float wh, float wl, uint16_t (&s)[4]) {
+  const float d0 = rint_small(wh);
+  float t = __fmul_rn(__fadd_rn(__fsub_rn(wh, d0), wl), 256.f);
+  const float d1 = rint_small(t);
   t = __fmul_rn(__fsub_rn(t, d1), 256.f);
-  const float d2 = rintf(t);
+  const float d2 = rint_small(t);
   t = __fmul_rn(__fsub_rn(t, d2), 256.f);
-  const float d3 = rintf(t);
-  if (out_of_range) {
-    s[0] = s[1] = s[2] = s[3] = 0;
-    return true;
-  }
+  const float d3 = rint_small(t);
   s[0] = bf16_of_small_int_float(d0);
   s[1] = bf16_of_small_int_float(d1);
   s[2] = bf16_of_small_int_float(d2);
   s[3] = bf16_of_small_int_float(d3);
+}
+
+// Four balanced base-256 digits of a df64 value hi + lo (|lo| <= ulp(hi)) against 2^E:
+// w = (hi + lo) 2^(6 - E) by exponent moves (exact), then digits_of_pair.  Non-finite hi or
+// |hi + lo| > 2^E (beyond rounding) report out of range; the digits are then zero.
+__device__ __forceinline__ bool digits4_df(float hi, float lo, int E, uint16_t (&s)[4]) {
+  const int k = 6 - E;
+  const float wh = scale_pow2(hi, k), wl = scale_pow2(lo, k);
+  if (!(fabsf(wh) <= 64.5f)) {                       // also catches infinity and NaN
+    s[0] = s[1] = s[2] = s[3] = 0;
+    return true;
+  }
+  digits_of_pair(wh, wl, s);
+  return false;
+}
+
+// digits4 of an FP64 value with FP32 and 32-bit integer operations only: w = v 2^(6 - E) is
+// cut from v's bits into an FP32 pair (the top 24 significand bits, then the next 24 of the
+// remaining 29, truncated: below 2^-47 of w), then digits_of_pair.  Zero and subnormal v give
+// zero digits (below every digit of any scale the kernels use); |v| > 2^E (beyond rounding) or
+// a non-finite v report out of range with zero digits.
+__device__ __forceinline__ bool digits4_f(double v, int E, uint16_t (&s)[4]) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(v);
+  const unsigned hw = (unsigned)(b >> 32), lw = (unsigned)b;
+  const int eb = (int)((hw >> 20) & 0x7FF);
+  const int ew = eb - 1023 + 6 - E;                   // exponent of w
+  s[0] = s[1] = s[2] = s[3] = 0;
+  if (eb == 0x7FF || (eb != 0 && ew > 6)) return true;
+  if (eb == 0 || ew < -40) return false;              // |w| < 2^-39: all digits zero
+  const unsigned sign = hw & 0x80000000u;
+  const float wh =
+      __uint_as_float(sign | ((unsigned)(ew + 127) << 23) | ((hw & 0xFFFFFu) << 3) | (lw >> 29));
+  const unsigned r = lw & 0x1FFFFFFFu;
+  float wl = 0.f;
+  if (r) {
+    const int p = 31 - __clz(r);                      // leading bit of the remainder
+    const unsigned mr = p >= 23 ? (r >> (p - 23)) : (r << (23 - p));
+    wl = __uint_as_float(sign | ((unsigned)(ew - 52 + p + 127) << 23) | (mr & 0x7FFFFFu));
+  }
+  if (!(fabsf(wh) <= 64.5f)) return true;
+  digits_of_pair(wh, wl, s);
   return false;
 }
 

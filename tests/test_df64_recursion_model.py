@@ -114,3 +114,43 @@ def test_fp32_digits_reconstruct_the_value():
         assert abs(d[0]) <= 64 and all(abs(x) <= 128 for x in d[1:])
         rec = d[0] + d[1] * 2.0 ** -8 + d[2] * 2.0 ** -16 + d[3] * 2.0 ** -24
         assert abs(rec - w) <= 1.5 * 2.0 ** -25
+
+
+def _digits_f(v, E):
+    """tc::digits4_f: the FP32 pair cut from the FP64 bits, then the FP32 digit sequence."""
+    b = int(np.float64(v).view(np.uint64))
+    hw, lw = b >> 32, b & 0xFFFFFFFF
+    eb = (hw >> 20) & 0x7FF
+    ew = eb - 1023 + 6 - E
+    if eb == 0 or ew < -40:
+        return [0.0] * 4, 0.0
+    sign = hw & 0x80000000
+    wh = np.uint32(sign | ((ew + 127) << 23) | ((hw & 0xFFFFF) << 3) | (lw >> 29)).view(np.float32)
+    r = lw & 0x1FFFFFFF
+    wl = f32(0)
+    if r:
+        pbit = r.bit_length() - 1
+        mr = r >> (pbit - 23) if pbit >= 23 else r << (23 - pbit)
+        wl = np.uint32(sign | ((ew - 52 + pbit + 127) << 23) | (mr & 0x7FFFFF)).view(np.float32)
+    assert abs(wh) <= 64.5
+    rint = lambda x: f32(f32(x + f32(12582912.0)) - f32(12582912.0))
+    d0 = rint(wh)
+    t = f32(f32(f32(wh - d0) + wl) * f32(256))
+    d1 = rint(t)
+    t = f32(f32(t - d1) * f32(256))
+    d2 = rint(t)
+    t = f32(f32(t - d2) * f32(256))
+    d3 = rint(t)
+    return [float(d) for d in (d0, d1, d2, d3)], v * 2.0 ** (6 - E)
+
+
+def test_fp64_digits_on_the_fp32_pipe():
+    """digits4_f reconstructs v 2^(6 - E) to 1.5 2^-25 with digits inside the exact bounds."""
+    rng = np.random.default_rng(2)
+    for _ in range(20000):
+        E = int(rng.integers(-900, 900))
+        v = rng.uniform(-1, 1) * 2.0 ** (E - int(rng.integers(0, 45)))
+        d, w = _digits_f(v, E)
+        assert abs(d[0]) <= 64 and all(abs(x) <= 128 for x in d[1:])
+        rec = d[0] + d[1] * 2.0 ** -8 + d[2] * 2.0 ** -16 + d[3] * 2.0 ** -24
+        assert abs(rec - w) <= 1.5 * 2.0 ** -25, (v, E, d, w)
