@@ -141,6 +141,7 @@ struct fsht_plan {
   int fft_nseg;
   long long fft_seg[3 * 8];
   int fft_seg_pmin[8];             // smallest transform size of each segment
+  int fft_seg_gen[8];              // 1: the segment has Bluestein, radix-3 or half-length rings
   int fft_mpb, fft_threads;        // ring-FFT launch shape (0: heuristic), set by the autotuner
   // contraction tile shapes (0: defaults), set by the autotuner or fsht_plan_set_contraction:
   // FP64 analysis maps per CTA (32 | 64) and rings per chunk (spin 0: 8 | 16 | 32, spin 2:

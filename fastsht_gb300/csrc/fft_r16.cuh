@@ -341,15 +341,18 @@ __device__ __forceinline__ void pass_filter(cdd* buf, const Sw& S, int n_elems,
 // when they fill the upper half of every butterfly.  last = false: stop before the
 // twiddle-free last pass (Bluestein fuses it with the filter).  All threads call it; it
 // synchronises on entry and after every pass.
-template <class Sw>
+// GEN = false: the caller guarantees a power-of-two size (no radix-3 pass), and the code for
+// the other sizes is left out of the kernel (a smaller kernel misses the instruction cache
+// less: the belt segment's largest stall).
+template <class Sw, bool GEN = true>
 __device__ void fft_dif16(cdd* buf, const FshtRingFFT& rf, const Sw& S, const cdd* tw16,
                           const cdd* tw3, int nz, bool last) {
   using namespace fftp;
   const int tid = threadIdx.x, nt = blockDim.x;
   const int logT = rf.logT, T = 1 << logT;
-  const int nblk = rf.r3 ? 3 : 1;
+  const int nblk = GEN && rf.r3 ? 3 : 1;
   __syncthreads();
-  if (rf.r3) {
+  if (GEN && rf.r3) {
     const cdd* t3 = tw3 + 2 * (T - 1);
     const bool c_zero = nz <= 2 * T;   // the third input of every butterfly is padding
     for (int j = tid; j < T; j += nt) {
@@ -367,7 +370,7 @@ __device__ void fft_dif16(cdd* buf, const FshtRingFFT& rf, const Sw& S, const cd
   const int rem = logT & 3;
   const int lstop = rem ? rem : 4;   // span of the twiddle-free last pass
   for (int ls = logT; ls > lstop; ls -= 4) {
-    const bool half_in = !rf.r3 && ls == logT && nz <= (T >> 1);
+    const bool half_in = GEN && !rf.r3 && ls == logT && nz <= (T >> 1);
     r16::pass16_dif(buf, S, logT, nblk, ls, tw16, half_in);
     __syncthreads();
   }
@@ -430,14 +433,15 @@ __device__ void fft_dit16_inv(cdd* buf, const FshtRingFFT& rf, const Sw& S, cons
 
 // DFT of rf.nd points in buf[0..nd), forward; bin q lands at buf[S(dft_bin(rf, q))] (as
 // ring_dft in fft_passes.cuh, with the radix-16 passes).
-template <class Sw>
+// GEN = false: every transform the kernel meets is a power of two (no Bluestein, no radix 3).
+template <class Sw, bool GEN = true>
 __device__ void ring_dft16(cdd* buf, const FshtRingFFT& rf, const Sw& S, const cdd* tw16,
                            const cdd* tw3, const cdd* __restrict__ chirp,
                            const cdd* __restrict__ bhat) {
   using namespace fftp;
   const int tid = threadIdx.x, nt = blockDim.x;
-  if (!rf.bluestein) {
-    fft_dif16(buf, rf, S, tw16, tw3, rf.P, true);
+  if (!GEN || !rf.bluestein) {
+    fft_dif16<Sw, GEN>(buf, rf, S, tw16, tw3, rf.P, true);
     return;
   }
   const int n = rf.nd, P = rf.P;

@@ -556,6 +556,7 @@ int fsht_fft_tables_init(fsht_plan* p) {
       const int cls = sm <= two_per_sm ? 0 : 1;
       if (cls != cls_prev && p->fft_nseg < 8) {
         p->fft_seg_pmin[p->fft_nseg] = rfs[i].P;
+        p->fft_seg_gen[p->fft_nseg] = 0;
         long long* sg = p->fft_seg + 3 * p->fft_nseg++;
         sg[0] = i;
         sg[1] = i + 1;
@@ -567,6 +568,7 @@ int fsht_fft_tables_init(fsht_plan* p) {
         if ((long long)sm > sg[2]) sg[2] = (long long)sm;
         if (rfs[i].P < p->fft_seg_pmin[p->fft_nseg - 1]) p->fft_seg_pmin[p->fft_nseg - 1] = rfs[i].P;
       }
+      if (rfs[i].bluestein || rfs[i].r3 || rfs[i].nd != rfs[i].n) p->fft_seg_gen[p->fft_nseg - 1] = 1;
     }
   }
   p->Pmax = lay.Pmax;

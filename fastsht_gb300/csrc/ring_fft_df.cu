@@ -130,15 +130,17 @@ __device__ __forceinline__ int load_scaled(cdd* buf, const Sw& S, int cnt, const
 template <bool R16>
 struct DfPasses {
   using Sw = Swz16;
+  template <bool GEN = true>
   static __device__ __forceinline__ void dft(cdd* buf, const FshtRingFFT& rf, const Sw& S,
                                              const FftTwT<cdd>& tw, const cdd* tw16,
                                              const cdd* chirp, const cdd* bhat) {
-    ring_dft16(buf, rf, S, tw16, tw.r3, chirp, bhat);
+    ring_dft16<Sw, GEN>(buf, rf, S, tw16, tw.r3, chirp, bhat);
   }
 };
 template <>
 struct DfPasses<false> {
   using Sw = Swz;
+  template <bool GEN = true>
   static __device__ __forceinline__ void dft(cdd* buf, const FshtRingFFT& rf, const Sw&,
                                              const FftTwT<cdd>& tw, const cdd*,
                                              const cdd* chirp, const cdd* bhat) {
@@ -147,8 +149,10 @@ struct DfPasses<false> {
 };
 
 // NT threads per CTA, at least MINB CTAs per SM (which sets the register budget: 128 a
-// thread for <256, 2> and <512, 1>, 64 for <512, 2> and <1024, 1>).
-template <int NT, int MINB, bool R16>
+// thread for <256, 2> and <512, 1>, 64 for <512, 2> and <1024, 1>).  GEN = false: a segment
+// of power-of-two rings only (the belt), built without the Bluestein, radix-3 and half-length
+// paths.
+template <int NT, int MINB, bool R16, bool GEN = true>
 __global__ void __launch_bounds__(NT, MINB) k_ring_fft_fwd_df(FwdDfArgs a) {
   using DP = DfPasses<R16>;
   extern __shared__ float4 smem4[];
@@ -181,7 +185,7 @@ __global__ void __launch_bounds__(NT, MINB) k_ring_fft_fwd_df(FwdDfArgs a) {
   const cdd* chirp = a.chirp + rf.chirp_off;
   const cdd* bhat = a.bhat + rf.bhat_off;
   int it = 0;   // exponent slot parity: slot it & 1 collects, the other is reset
-  if (rf.nd != n) {
+  if (GEN && rf.nd != n) {
     // Half-length ring (never the equator): each ring as z_j = x_{2j} + i x_{2j+1},
     // Z = DFT_nd(z), X_q = E_q + e^{-2 pi i q/n} O_q (see the FP64 kernel); the north ring
     // writes {F_N, F_N}, the south ring adds +-F_S in FP64.
@@ -193,7 +197,7 @@ __global__ void __launch_bounds__(NT, MINB) k_ring_fft_fwd_df(FwdDfArgs a) {
         __syncthreads();
         if (tid == 0) s_emax[(it & 1) ^ 1] = 0;
         const int sh = load_scaled(buf, S, nd, x, x + 1, 2, &s_emax[it & 1]);
-        DP::dft(buf, rf, S, a.tw, a.tw16, chirp, bhat);
+        DP::template dft<GEN>(buf, rf, S, a.tw, a.tw16, chirp, bhat);
         for (int m = tid; m <= mtop; m += nt) {
           const int q = m % n;
           const bool cj = q > nd;
@@ -224,7 +228,7 @@ __global__ void __launch_bounds__(NT, MINB) k_ring_fft_fwd_df(FwdDfArgs a) {
     __syncthreads();   // the previous map's readers of buf and of the other slot are done
     if (tid == 0) s_emax[(it & 1) ^ 1] = 0;
     const int sh = load_scaled(buf, S, n, xn, equator ? nullptr : xs, 1, &s_emax[it & 1]);
-    DP::dft(buf, rf, S, a.tw, a.tw16, chirp, bhat);
+    DP::template dft<GEN>(buf, rf, S, a.tw, a.tw16, chirp, bhat);
     // Z = FFT(x_N + i x_S): X_N[q] = (Z[q] + conj Z[-q])/2, X_S[q] = (Z[q] - conj Z[-q])/(2i)
     // q = m mod n and the output pointer advance by fixed steps (no division per m)
     const int qstep = nt % n;
@@ -239,27 +243,26 @@ __global__ void __launch_bounds__(NT, MINB) k_ring_fft_fwd_df(FwdDfArgs a) {
       if (q >= n) q -= n;
       const cdd xN = cadd_lz(zq, zn);                          // 2 X_N
       const cdd xS = cmul_mi(csub_lz(zq, zn));                 // 2 X_S
+      double2 S, D;
       if (!sflag) {
         // phi0 = 0: the phase factor is the real 1/2, folded into the output exponent
         if (equator) {
-          const double2 fN = cdd_to_fp64(xN, sh - 1);
-          w[0] = fN;
-          w[1] = fN;
+          S = D = cdd_to_fp64(xN, sh - 1);
         } else {
-          w[0] = cdd_to_fp64(cadd_lz(xN, xS), sh - 1);
-          w[1] = cdd_to_fp64(csub_lz(xN, xS), sh - 1);
+          S = cdd_to_fp64(cadd_lz(xN, xS), sh - 1);
+          D = cdd_to_fp64(csub_lz(xN, xS), sh - 1);
         }
-        continue;
-      }
-      const cdd p = ph[m];
-      if (equator) {
-        const double2 fN = cdd_to_fp64(cmul_lz(xN, p), sh);
-        w[0] = fN;
-        w[1] = fN;
       } else {
-        w[0] = cdd_to_fp64(cmul_lz(cadd_lz(xN, xS), p), sh);  // F_N + F_S
-        w[1] = cdd_to_fp64(cmul_lz(csub_lz(xN, xS), p), sh);  // F_N - F_S
+        const cdd p = ph[m];
+        if (equator) {
+          S = D = cdd_to_fp64(cmul_lz(xN, p), sh);
+        } else {
+          S = cdd_to_fp64(cmul_lz(cadd_lz(xN, xS), p), sh);  // F_N + F_S
+          D = cdd_to_fp64(cmul_lz(csub_lz(xN, xS), p), sh);  // F_N - F_S
+        }
       }
+      w[0] = S;
+      w[1] = D;
     }
   }
 }
@@ -412,13 +415,16 @@ __global__ void k_to_cdd(const double2* __restrict__ in, float4* out, long long 
 // autotuned thread count (256 or 512) or else 512 for one CTA per SM and 256 for two (sixteen
 // warps an SM either way); radix-4 passes otherwise, 1024 threads for one CTA per SM and 512
 // for two (32 warps).
-enum DfVariant { kR16T256, kR16T512, kR4T512, kR4T1024 };
-DfVariant df_variant(const fsht_plan* p, int sgi) {
+// pow2_ok: the launcher has the power-of-two-only radix-16 kernels (kR16T*P), used for segments
+// without Bluestein, radix-3 or half-length rings.
+enum DfVariant { kR16T256, kR16T512, kR4T512, kR4T1024, kR16T256P, kR16T512P };
+DfVariant df_variant(const fsht_plan* p, int sgi, bool pow2_ok) {
   const long long smem = p->fft_seg[3 * sgi + 2];
   const bool one_cta = smem > 112 * 1024;
   if (p->fft_seg_pmin[sgi] >= 4096) {
-    if (p->fft_threads > 0) return p->fft_threads > 256 ? kR16T512 : kR16T256;
-    return one_cta ? kR16T512 : kR16T256;
+    const bool t512 = p->fft_threads > 0 ? p->fft_threads > 256 : one_cta;
+    if (pow2_ok && !p->fft_seg_gen[sgi]) return t512 ? kR16T512P : kR16T256P;
+    return t512 ? kR16T512 : kR16T256;
   }
   return one_cta ? kR4T1024 : kR4T512;
 }
@@ -431,7 +437,7 @@ int df_set_smem(void (*k)(Args), size_t smem) {
 template <class Args>
 int df_launch(DfVariant v, void (*const* ks)(Args), dim3 grid, size_t smem, cudaStream_t s,
               const Args& a) {
-  static const int threads[4] = {256, 512, 512, 1024};
+  static const int threads[6] = {256, 512, 512, 1024, 256, 512};
   ks[v]<<<grid, threads[v], smem, s>>>(a);
   FSHT_LAUNCH_CHECK();
   return FSHT_OK;
@@ -510,15 +516,17 @@ int fsht_launch_ring_fft_fwd_df(fsht_plan* p, const double* maps, long long map_
   a.ring_i0 = p->d_ring_i0;
   a.W = W;
   a.maps_per_block = p->fft_mpb > 0 ? p->fft_mpb : fsht_fft_maps_per_block(kb, p->nnorth);
-  void (*const ks[4])(FwdDfArgs) = {k_ring_fft_fwd_df<256, 2, true>, k_ring_fft_fwd_df<512, 1, true>,
+  void (*const ks[6])(FwdDfArgs) = {k_ring_fft_fwd_df<256, 2, true>, k_ring_fft_fwd_df<512, 1, true>,
                                     k_ring_fft_fwd_df<512, 2, false>,
-                                    k_ring_fft_fwd_df<1024, 1, false>};
+                                    k_ring_fft_fwd_df<1024, 1, false>,
+                                    k_ring_fft_fwd_df<256, 2, true, false>,
+                                    k_ring_fft_fwd_df<512, 1, true, false>};
   for (auto k : ks) FSHT_TRY(df_set_smem(k, p->fft_smem));
   for (int sgi = 0; sgi < p->fft_nseg; ++sgi) {
     const long long* sg = p->fft_seg + 3 * sgi;
     a.ring_base = (int)sg[0];
     dim3 grid((unsigned)(sg[1] - sg[0]), (kb + a.maps_per_block - 1) / a.maps_per_block);
-    FSHT_TRY(df_launch(df_variant(p, sgi), ks, grid, (size_t)sg[2], s, a));
+    FSHT_TRY(df_launch(df_variant(p, sgi, true), ks, grid, (size_t)sg[2], s, a));
   }
   return FSHT_OK;
 }
@@ -552,7 +560,7 @@ int fsht_launch_ring_fft_inv_df(fsht_plan* p, const double2* W, double* maps,
     const long long* sg = p->fft_seg + 3 * sgi;
     a.ring_base = (int)sg[0];
     dim3 grid((unsigned)(sg[1] - sg[0]), (kc + a.maps_per_block - 1) / a.maps_per_block);
-    FSHT_TRY(df_launch(df_variant(p, sgi), ks, grid, (size_t)sg[2], s, a));
+    FSHT_TRY(df_launch(df_variant(p, sgi, false), ks, grid, (size_t)sg[2], s, a));
   }
   return FSHT_OK;
 }
