@@ -136,62 +136,22 @@ __device__ __forceinline__ void tmem_wait_ld() {
 }
 
 // ------------------------------------------------------------------ slicing
-// Four balanced base-256 digits of an FP64 value v against a power-of-two scale 2^E
-// (|v| < 2^E):  |v| 2^(6-E) = d0 + d1 2^-8 + d2 2^-16 + d3 2^-24 + r,  |r| <= 2^-25,
-// |d0| <= 64, |d1..3| <= 128, every digit carrying the sign of v.  Each digit is an
-// integer that BF16 holds exactly, so slice products are exact integers.  Integer
-// operations only.
-__device__ __forceinline__ uint16_t bf16_of_int(int d) {
-  if (d == 0) return 0;
-  const uint32_t sign = d < 0 ? 0x8000u : 0u;
-  const uint32_t b = (uint32_t)(d < 0 ? -d : d);   // 1..255
-  const int msb = 31 - __clz(b);
-  const uint32_t mant = (b << (7 - msb)) & 0x7F;
-  return (uint16_t)(sign | ((uint32_t)(127 + msb) << 7) | mant);
-}
+// Operands are cut into four balanced base-256 digits against a power-of-two scale 2^E
+// (|v| < 2^E):  v 2^(6-E) = d0 + d1 2^-8 + d2 2^-16 + d3 2^-24 + r,  |r| < 1.5 2^-25,
+// |d0| <= 64, |d1..3| <= 128.  Each digit is an integer that BF16 holds exactly, so the
+// products of two digits are exact integers; the digit functions below work on the FP32 pipe
+// and with 32-bit integer operations (no FP64 instruction).
+
 // The BF16 digit h times 2^-8 (exact: only the exponent moves; digits are >= 1 in
 // magnitude, so the result stays normal).
 __device__ __forceinline__ uint16_t bf16_scale_2m8(uint16_t h) {
   return (h & 0x7FFF) ? (uint16_t)(h - (8u << 7)) : h;
 }
-// Returns true when v does not fit its scale (|v| >= 2^E, or v is not finite): the digits
-// are then saturated (or zero for a non-finite v) and the caller raises the plan's error
-// word (kErrRange), so a wrong result never passes silently.
+// A digit function returns true when its value does not fit the scale (|v| > 2^E beyond
+// rounding, or v is not finite): the digits are then zero and the caller raises the plan's
+// error word (kErrRange), so a wrong result never passes silently.
 constexpr int kErrTimeout = 1;   // error-word bit: a bounded wait expired
 constexpr int kErrRange = 2;     // error-word bit: a value fell outside its digit scale
-// The balanced base-256 digits of T (0 <= T <= 2^30), times sgn.
-__device__ __forceinline__ void digits_of_T(long long T, int sgn, uint16_t (&s)[4]) {
-  int d[4];
-#pragma unroll
-  for (int j = 3; j >= 1; --j) {
-    const int dj = (int)((T + 128) & 255) - 128;
-    d[j] = dj;
-    T = (T - dj) >> 8;
-  }
-  d[0] = (int)T;
-#pragma unroll
-  for (int j = 0; j < 4; ++j) s[j] = bf16_of_int(sgn * d[j]);
-}
-
-__device__ __forceinline__ bool digits4(double v, int E, uint16_t (&s)[4]) {
-  const unsigned long long bits = (unsigned long long)__double_as_longlong(v);
-  const int eb = (int)((bits >> 52) & 0x7FF);
-  long long T = 0;
-  bool out_of_range = eb == 0x7FF;
-  if (eb != 0 && eb != 0x7FF) {
-    const unsigned long long mant = (bits & ((1ull << 52) - 1)) | (1ull << 52);
-    const int sh = E - (eb - 1023) + 22;      // >= 23 when |v| < 2^E
-    if (sh < 23) {                            // out of range: saturate and report
-      T = 1ll << 30;
-      out_of_range = true;
-    } else if (sh < 64) {
-      T = (long long)((mant + (1ull << (sh - 1))) >> sh);
-    }
-  }
-  const int neg = (bits >> 63) ? -1 : 1;
-  digits_of_T(T, neg, s);
-  return out_of_range;
-}
 
 // f 2^k for an FP32 f, by moving its exponent field (no FP64 and no exp2f range limit): values
 // that would leave FP32's normal range below give 0 (far under every digit), above give
@@ -250,7 +210,7 @@ __device__ __forceinline__ bool digits4_df(float hi, float lo, int E, uint16_t (
   return false;
 }
 
-// digits4 of an FP64 value with FP32 and 32-bit integer operations only: w = v 2^(6 - E) is
+// The digits of an FP64 value with FP32 and 32-bit integer operations only: w = v 2^(6 - E) is
 // cut from v's bits into an FP32 pair (the top 24 significand bits, then the next 24 of the
 // remaining 29, truncated: below 2^-47 of w), then digits_of_pair.  Zero and subnormal v give
 // zero digits (below every digit of any scale the kernels use); |v| > 2^E (beyond rounding) or
