@@ -92,9 +92,6 @@ int run_job(const fsht_plan* base, const fsht_job& j, unsigned char* arena, size
   jp.d_ws = arena + L.ws_off;
   jp.d_eb = reinterpret_cast<int*>(arena + L.eb_off);
   jp.d_lbuf = arena + L.lb_off;
-  jp.d_blkexp = nullptr;          // the base plan's exponent records are not this job's
-  jp.d_blkmax = nullptr;
-  jp.blkexp_out = nullptr;
   jp.prof = nullptr;
   switch (j.kind) {
     case FSHT_JOB_T2ALM: return fsht_t2alm(&jp, j.in0, j.out0, j.nmaps, 0, 0);

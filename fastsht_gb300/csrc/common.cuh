@@ -153,12 +153,6 @@ struct fsht_plan {
   // recursion rows, and the lambda-digit staging buffer with its waves of m
   unsigned char* d_ws;
   int* d_eb;
-  // split form: the forward FFT's largest FP64 exponent field per (north ring, block of 32
-  // orders, map) when blkexp_out points at d_blkexp, and its maximum over the kept rings per
-  // (block, map): column scales for the slicing without a pass over the phase matrix
-  int* d_blkexp;                   // [nnorth][nblk][kchunk]
-  int* d_blkmax;                   // [nblk][kchunk]
-  int* blkexp_out;
   size_t ws_bytes;
   FshtLamRow* d_lamtab;            // triangular, (l, m) at m(2 lmax + 3 - m)/2 + l - m
   long long* d_lam_off;            // per pair-ordered index q: first 16 KB tile unit
@@ -283,8 +277,7 @@ size_t fsht_split_eb_bytes(const fsht_plan* p, int kc);
 // adds when accumulate).
 int fsht_split_tables_init(fsht_plan* p);
 int fsht_launch_split_slice(fsht_plan* p, int w, const double2* W, unsigned char* WS, int* EB,
-                            int kc, cudaStream_t s, const int* blkmax = nullptr);
-int fsht_launch_split_blkmax(fsht_plan* p, int kc, cudaStream_t s);
+                            int kc, cudaStream_t s);
 int fsht_launch_split_lambda(fsht_plan* p, int w, unsigned char* lbuf, cudaStream_t s);
 int fsht_launch_split_gemm(fsht_plan* p, int w, const unsigned char* WS, const int* EB,
                            const unsigned char* lbuf, double* alm, int nmaps_total, int k0,

@@ -47,8 +47,6 @@ struct SliceArgs {
   unsigned char* WS;
   int* EB;
   int* err;              // plan error word (kErrRange when a value misses its scale)
-  const int* blkmax;     // null, or the forward FFT's largest exponent field per (block of 32
-                         // orders, map), [nblk][kc]: then no pass over W for the maxima
 };
 
 // grid (q in wave, 4 x group), 128 threads = (ring half, map, parity, Re/Im) over one quarter
@@ -82,11 +80,7 @@ __global__ void __launch_bounds__(kSliceThreads, 6) k_slice_phase(SliceArgs a) {
   // max runs on GB300's FP64 pipe at two per clock per SM, which bound this pass).
   constexpr unsigned long long kAbs = 0x7FFFFFFFFFFFFFFFull;
   unsigned long long mx = 0;
-  if (a.blkmax) {
-    // the scale of the column's block of 32 orders (over {S, D} x {Re, Im} and the block's
-    // kept rings): a power of two at least the column's own; E below reads the exponent field
-    if (valid) mx = (unsigned long long)a.blkmax[(size_t)(m >> 5) * a.kc + k] << 52;
-  } else if (valid) {
+  if (valid) {
     // eight independent loads in flight per thread
     int r = r_begin;
     for (; r + 8 <= r_end; r += 8) {
@@ -1042,7 +1036,7 @@ size_t fsht_split_eb_bytes(const fsht_plan* p, int kc) {
 }
 
 int fsht_launch_split_slice(fsht_plan* p, int w, const double2* W, unsigned char* WS, int* EB,
-                            int kc, cudaStream_t s, const int* blkmax) {
+                            int kc, cudaStream_t s) {
   const int* wv = p->h_waves + kWaveInts * w;
   SliceArgs sa;
   sa.W = reinterpret_cast<const double*>(W);
@@ -1056,31 +1050,7 @@ int fsht_launch_split_slice(fsht_plan* p, int w, const double2* W, unsigned char
   sa.WS = WS;
   sa.EB = EB;
   sa.err = p->d_err;
-  sa.blkmax = blkmax;
   k_slice_phase<<<dim3(wv[1] - wv[0], 4 * sa.ngroups), kSliceThreads, 0, s>>>(sa);
-  FSHT_LAUNCH_CHECK();
-  return FSHT_OK;
-}
-
-// The forward FFT's per-ring block exponents reduced over the rings each block keeps (rings
-// from ring_i0 of the block's first order, the rings the FFT wrote for it): thread per map.
-namespace {
-__global__ void k_blk_max(const int* __restrict__ blkexp, int* __restrict__ blkmax,
-                          const int* __restrict__ ring_i0, int nnorth, int nblk, int kc) {
-  const int b = blockIdx.x;
-  const int k = blockIdx.y * blockDim.x + threadIdx.x;
-  if (k >= kc) return;
-  int mx = 0;
-  for (int i = ring_i0[32 * b]; i < nnorth; ++i)
-    mx = max(mx, __ldg(&blkexp[((size_t)i * nblk + b) * kc + k]));
-  blkmax[(size_t)b * kc + k] = mx;
-}
-}  // namespace
-
-int fsht_launch_split_blkmax(fsht_plan* p, int kc, cudaStream_t s) {
-  const int nblk = (p->lmax + 32) / 32;
-  k_blk_max<<<dim3(nblk, (kc + 127) / 128), 128, 0, s>>>(p->d_blkexp, p->d_blkmax, p->d_ring_i0,
-                                                         p->nnorth, nblk, kc);
   FSHT_LAUNCH_CHECK();
   return FSHT_OK;
 }

@@ -118,8 +118,6 @@ void free_plan_memory(fsht_plan* p) {
   cudaFree(p->d_err);
   cudaFree(p->d_ws);
   cudaFree(p->d_eb);
-  cudaFree(p->d_blkexp);
-  cudaFree(p->d_blkmax);
   cudaFree(p->d_lamtab);
   cudaFree(p->d_lam_off);
   cudaFree(p->d_lbuf);
@@ -353,14 +351,6 @@ int fsht_plan_create(int nside, int lmax, int nmaps_max, int flags, int precisio
     p->ws_bytes = f * fsht_split_ws_bytes(p, p->kchunk);
     if ((rc = dalloc((void**)&p->d_ws, p->ws_bytes))) return fail(rc);
     if ((rc = dalloc((void**)&p->d_eb, f * fsht_split_eb_bytes(p, p->kchunk)))) return fail(rc);
-    {
-      const size_t nblk = (size_t)(lmax + 32) / 32;
-      if ((rc = dalloc((void**)&p->d_blkexp,
-                       sizeof(int) * (size_t)p->nnorth * nblk * (size_t)p->kchunk)))
-        return fail(rc);
-      if ((rc = dalloc((void**)&p->d_blkmax, sizeof(int) * nblk * (size_t)p->kchunk)))
-        return fail(rc);
-    }
     if ((rc = dalloc((void**)&p->d_lbuf, p->lbuf_bytes))) return fail(rc);
     if ((rc = dalloc((void**)&p->d_lbuf2, p->lbuf_bytes))) return fail(rc);
     if ((ce = cudaStreamCreateWithFlags(&p->aux, cudaStreamNonBlocking)) != cudaSuccess) {
@@ -721,8 +711,7 @@ static int xfer_orders_done(fsht_plan* p, HostXfer& x, const double* dalm, int n
 // accumulate), and synthesis of alm into W = {G_N, G_S}.  started: lam_start already ran
 // (before the FFT).  hx: copy each wave's finished alm columns to the host.
 static int split_analysis(fsht_plan* p, const double2* W, double* alm, int nmaps, int c0, int kc,
-                          int accumulate, bool started = false, HostXfer* hx = nullptr,
-                          const int* blkmax = nullptr) {
+                          int accumulate, bool started = false, HostXfer* hx = nullptr) {
   // every alm element of the chunk is written by exactly one unit of the contraction (its
   // first ring part stores, later parts add), so alm needs no clearing
   if (!started) FSHT_TRY(lam_start(p, fsht_launch_split_lambda));
@@ -738,7 +727,7 @@ static int split_analysis(fsht_plan* p, const double2* W, double* alm, int nmaps
   auto eb_of = [&](int w) { return p->d_eb + (ahead ? (size_t)(w & 1) * eb1 : 0); };
   auto slice_on = [&](int w, cudaStream_t st) -> int {
     FSHT_PROF_ON(FSHT_KCAT_SLICE, st);
-    return fsht_launch_split_slice(p, w, W, ws_of(w), eb_of(w), kc, st, blkmax);
+    return fsht_launch_split_slice(p, w, W, ws_of(w), eb_of(w), kc, st);
   };
   if (ahead) {
     FSHT_CUDA_TRY(cudaEventRecord(p->evs[0], p->stream));
@@ -922,10 +911,6 @@ static int t2alm_impl(fsht_plan* p, const double* maps, double* alm, int nmaps, 
     if (split) FSHT_TRY(lam_start(p, fsht_launch_split_lambda));
     // the chunk's maps as the FFT reads them: device buffer, or host memory read in place
     const double* cmaps = (hx && hx->direct ? hx->direct : maps) + (size_t)c0 * p->npix;
-    // the split form's FFT records the largest exponent per ring, block of 32 orders and map
-    // on the way, which gives the slicing its column scales without a pass over W
-    const bool blk = split && p->d_blkexp != nullptr;
-    p->blkexp_out = blk ? p->d_blkexp : nullptr;
     if (!hx || hx->direct) {
       FSHT_PROF(FSHT_KCAT_FFT_FWD);
       // (page-locked maps mapped into the device's address space are read over the host link
@@ -947,11 +932,8 @@ static int t2alm_impl(fsht_plan* p, const double* maps, double* alm, int nmaps, 
         FSHT_TRY(fsht_launch_ring_fft_fwd_part(p, cmaps, p->npix, kc, k0, cnt, W0, p->stream));
       }
     }
-    p->blkexp_out = nullptr;
-    if (blk) FSHT_TRY(fsht_launch_split_blkmax(p, kc, p->stream));
     if (split) {
-      FSHT_TRY(split_analysis(p, W0, alm, nmaps, c0, kc, 0, true, niter == 0 ? hx : nullptr,
-                              blk ? p->d_blkmax : nullptr));
+      FSHT_TRY(split_analysis(p, W0, alm, nmaps, c0, kc, 0, true, niter == 0 ? hx : nullptr));
       // Jacobi refinement: FP64 Fourier-space residual of a split synthesis, analysed
       // in split precision and added
       for (int it = 0; it < niter; ++it) {

@@ -31,19 +31,7 @@ struct FwdDfArgs {
   const cdd* rtw;
   const int* ring_i0;
   double2* W;
-  int* blkexp;              // null, or [nnorth][nblk][kc]: per ring, block of 32 orders and map,
-  int nblk;                 // the largest FP64 exponent field of the block's {S, D} values
 };
-
-// The largest exponent field of an (m, map) entry's four values, reduced over the warp, whose
-// 32 lanes hold the 32 orders of one block (dead lanes give 0), stored by lane 0.
-__device__ __forceinline__ void blkexp_note(int* slot, bool live, double2 S, double2 D) {
-  int e = live ? max(max(dd_exp_field(S.x), dd_exp_field(S.y)),
-                     max(dd_exp_field(D.x), dd_exp_field(D.y)))
-               : 0;
-  e = __reduce_max_sync(0xffffffffu, e);
-  if ((threadIdx.x & 31) == 0 && slot) *slot = e;
-}
 
 __device__ __forceinline__ cdd cdd_from_fp64(double re, double im) {
   cdd r;
@@ -210,35 +198,25 @@ __global__ void __launch_bounds__(NT, MINB) k_ring_fft_fwd_df(FwdDfArgs a) {
         if (tid == 0) s_emax[(it & 1) ^ 1] = 0;
         const int sh = load_scaled(buf, S, nd, x, x + 1, 2, &s_emax[it & 1]);
         DP::template dft<GEN>(buf, rf, S, a.tw, a.tw16, chirp, bhat);
-        // warp-uniform trip count (the block-exponent record reduces over whole warps)
-        for (int m = tid; m - (tid & 31) <= mtop; m += nt) {
-          const bool live = m <= mtop;
-          double2 Sv{}, Dv{};
-          if (live) {
-            const int q = m % n;
-            const bool cj = q > nd;
-            const int kk = cj ? n - q : q;
-            const cdd za = buf[S(dft_bin(rf, kk == nd ? 0 : kk))];
-            const cdd zb = cconj(buf[S(dft_bin(rf, kk == 0 ? 0 : nd - kk))]);
-            const cdd e = cadd_lz(za, zb);                       // 2 E
-            const cdd o = cmul_mi(csub_lz(za, zb));              // 2 O
-            cdd xq = cadd_lz(e, cmul_lz(o, ldg_cdd(&rtw[kk])));  // 2 X
-            if (cj) xq = cconj(xq);
-            const double2 f = cdd_to_fp64(cmul_lz(xq, ph[m]), sh);
-            double2* w = a.W + (((long long)m * a.nnorth + i) * a.kc + k) * 2;
-            if (side == 0) {
-              w[0] = f;
-              w[1] = f;
-            } else {
-              Sv = cadd(w[0], f);
-              Dv = csub(w[1], f);
-              w[0] = Sv;
-              w[1] = Dv;
-            }
+        for (int m = tid; m <= mtop; m += nt) {
+          const int q = m % n;
+          const bool cj = q > nd;
+          const int kk = cj ? n - q : q;
+          const cdd za = buf[S(dft_bin(rf, kk == nd ? 0 : kk))];
+          const cdd zb = cconj(buf[S(dft_bin(rf, kk == 0 ? 0 : nd - kk))]);
+          const cdd e = cadd_lz(za, zb);                       // 2 E
+          const cdd o = cmul_mi(csub_lz(za, zb));              // 2 O
+          cdd xq = cadd_lz(e, cmul_lz(o, ldg_cdd(&rtw[kk])));  // 2 X
+          if (cj) xq = cconj(xq);
+          const double2 f = cdd_to_fp64(cmul_lz(xq, ph[m]), sh);
+          double2* w = a.W + (((long long)m * a.nnorth + i) * a.kc + k) * 2;
+          if (side == 0) {
+            w[0] = f;
+            w[1] = f;
+          } else {
+            w[0] = cadd(w[0], f);
+            w[1] = csub(w[1], f);
           }
-          if (a.blkexp && side == 1)
-            blkexp_note(live ? a.blkexp + ((size_t)i * a.nblk + (m >> 5)) * a.kc + k : nullptr,
-                        live, Sv, Dv);
         }
       }
     }
@@ -257,41 +235,34 @@ __global__ void __launch_bounds__(NT, MINB) k_ring_fft_fwd_df(FwdDfArgs a) {
     const long long wstep = (long long)nt * a.nnorth * a.kc * 2;
     int q = tid % n;
     double2* w = a.W + (((long long)tid * a.nnorth + i) * a.kc + k) * 2;
-    // warp-uniform trip count (the block-exponent record reduces over whole warps)
-    for (int m = tid; m - (tid & 31) <= mtop; m += nt, w += wstep) {
-      const bool live = m <= mtop;
-      double2 Sv{}, Dv{};
-      if (live) {
-        const int qn = (q == 0) ? 0 : n - q;
-        const cdd zq = buf[S(dft_bin(rf, q))];
-        const cdd zn = cconj(buf[S(dft_bin(rf, qn))]);
-        q += qstep;
-        if (q >= n) q -= n;
-        const cdd xN = cadd_lz(zq, zn);                          // 2 X_N
-        const cdd xS = cmul_mi(csub_lz(zq, zn));                 // 2 X_S
-        if (!sflag) {
-          // phi0 = 0: the phase factor is the real 1/2, folded into the output exponent
-          if (equator) {
-            Sv = Dv = cdd_to_fp64(xN, sh - 1);
-          } else {
-            Sv = cdd_to_fp64(cadd_lz(xN, xS), sh - 1);
-            Dv = cdd_to_fp64(csub_lz(xN, xS), sh - 1);
-          }
+    for (int m = tid; m <= mtop; m += nt, w += wstep) {
+      const int qn = (q == 0) ? 0 : n - q;
+      const cdd zq = buf[S(dft_bin(rf, q))];
+      const cdd zn = cconj(buf[S(dft_bin(rf, qn))]);
+      q += qstep;
+      if (q >= n) q -= n;
+      const cdd xN = cadd_lz(zq, zn);                          // 2 X_N
+      const cdd xS = cmul_mi(csub_lz(zq, zn));                 // 2 X_S
+      double2 S, D;
+      if (!sflag) {
+        // phi0 = 0: the phase factor is the real 1/2, folded into the output exponent
+        if (equator) {
+          S = D = cdd_to_fp64(xN, sh - 1);
         } else {
-          const cdd p = ph[m];
-          if (equator) {
-            Sv = Dv = cdd_to_fp64(cmul_lz(xN, p), sh);
-          } else {
-            Sv = cdd_to_fp64(cmul_lz(cadd_lz(xN, xS), p), sh);  // F_N + F_S
-            Dv = cdd_to_fp64(cmul_lz(csub_lz(xN, xS), p), sh);  // F_N - F_S
-          }
+          S = cdd_to_fp64(cadd_lz(xN, xS), sh - 1);
+          D = cdd_to_fp64(csub_lz(xN, xS), sh - 1);
         }
-        w[0] = Sv;
-        w[1] = Dv;
+      } else {
+        const cdd p = ph[m];
+        if (equator) {
+          S = D = cdd_to_fp64(cmul_lz(xN, p), sh);
+        } else {
+          S = cdd_to_fp64(cmul_lz(cadd_lz(xN, xS), p), sh);  // F_N + F_S
+          D = cdd_to_fp64(cmul_lz(csub_lz(xN, xS), p), sh);  // F_N - F_S
+        }
       }
-      if (a.blkexp)
-        blkexp_note(live ? a.blkexp + ((size_t)i * a.nblk + (m >> 5)) * a.kc + k : nullptr, live,
-                    Sv, Dv);
+      w[0] = S;
+      w[1] = D;
     }
   }
 }
@@ -544,8 +515,6 @@ int fsht_launch_ring_fft_fwd_df(fsht_plan* p, const double* maps, long long map_
   a.tw16 = reinterpret_cast<const cdd*>(p->d_tw16_df);
   a.ring_i0 = p->d_ring_i0;
   a.W = W;
-  a.blkexp = p->blkexp_out;
-  a.nblk = (p->lmax + 32) / 32;
   a.maps_per_block = p->fft_mpb > 0 ? p->fft_mpb : fsht_fft_maps_per_block(kb, p->nnorth);
   void (*const ks[6])(FwdDfArgs) = {k_ring_fft_fwd_df<256, 2, true>, k_ring_fft_fwd_df<512, 1, true>,
                                     k_ring_fft_fwd_df<512, 2, false>,
