@@ -30,3 +30,20 @@ def test_requests_of_equal_shape_are_distinct_in_queues():
 def test_reserved_slots_take_only_small_jobs(free, small, want):
     srv = SimpleNamespace(_free_slots=list(free), reserved=2)
     assert Server._slot_for(srv, small) == want
+
+
+def test_cost_model_counts_whole_map_tiles():
+    """A job of fewer maps than a 64-map tile costs the whole tile's contraction (only its ring
+    FFTs scale with the maps), so the duration cap never splits a request below one tile."""
+    for prec in ("fp64", "split"):
+        one = Server.cost_s("t2alm", 1024, 2047, prec, 1)
+        tile = Server.cost_s("t2alm", 1024, 2047, prec, 64)
+        two = Server.cost_s("t2alm", 1024, 2047, prec, 65)
+        fft_per_map = (0.4e-3 if prec == "split" else 1.3e-3)
+        assert tile - one == pytest.approx(63 * fft_per_map, rel=1e-9)
+        leg_tile = 64 * 4.0 * 1024 * 2048 * 2049 / (80e12 if prec == "split" else 1e12)
+        assert two - tile == pytest.approx(leg_tile + fft_per_map, rel=1e-9)   # a second tile
+    # Q/U pairs cost four times the T contraction
+    t = Server.cost_s("t2alm", 256, 512, "fp64", 64) - 64 * 1.3e-3 / 16
+    qu = Server.cost_s("qu2eb", 256, 512, "fp64", 64) - 2 * 64 * 1.3e-3 / 16
+    assert qu == pytest.approx(4 * t, rel=1e-9)
