@@ -243,26 +243,26 @@ __global__ void __launch_bounds__(NT, MINB) k_ring_fft_fwd_df(FwdDfArgs a) {
       if (q >= n) q -= n;
       const cdd xN = cadd_lz(zq, zn);                          // 2 X_N
       const cdd xS = cmul_mi(csub_lz(zq, zn));                 // 2 X_S
-      double2 S, D;
+      double2 Sv, Dv;   // the {S, D} entries of (m, ring, map)
       if (!sflag) {
         // phi0 = 0: the phase factor is the real 1/2, folded into the output exponent
         if (equator) {
-          S = D = cdd_to_fp64(xN, sh - 1);
+          Sv = Dv = cdd_to_fp64(xN, sh - 1);
         } else {
-          S = cdd_to_fp64(cadd_lz(xN, xS), sh - 1);
-          D = cdd_to_fp64(csub_lz(xN, xS), sh - 1);
+          Sv = cdd_to_fp64(cadd_lz(xN, xS), sh - 1);
+          Dv = cdd_to_fp64(csub_lz(xN, xS), sh - 1);
         }
       } else {
         const cdd p = ph[m];
         if (equator) {
-          S = D = cdd_to_fp64(cmul_lz(xN, p), sh);
+          Sv = Dv = cdd_to_fp64(cmul_lz(xN, p), sh);
         } else {
-          S = cdd_to_fp64(cmul_lz(cadd_lz(xN, xS), p), sh);  // F_N + F_S
-          D = cdd_to_fp64(cmul_lz(csub_lz(xN, xS), p), sh);  // F_N - F_S
+          Sv = cdd_to_fp64(cmul_lz(cadd_lz(xN, xS), p), sh);  // F_N + F_S
+          Dv = cdd_to_fp64(cmul_lz(csub_lz(xN, xS), p), sh);  // F_N - F_S
         }
       }
-      w[0] = S;
-      w[1] = D;
+      w[0] = Sv;
+      w[1] = Dv;
     }
   }
 }
